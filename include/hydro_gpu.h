@@ -1,0 +1,258 @@
+/*
+ * hydro_gpu.h -- C-ABI of the GB300 (sm_103a) implementation of hydro's
+ * time-step hot path: SIMPLE momentum assembly, pressure-correction solve,
+ * velocity/flux correction and TVD partial-density advection on a uniform
+ * Cartesian block (2D or 3D).
+ *
+ * Every entry point returns an int status (enum hydro_status).  Plain
+ * pointers and sizes only; host arrays are in the reference's raw order:
+ *   cell  (i,j,k)      -> i + Nx*(j + Ny*k)                  (mesh.hpp:552-561)
+ *   faces              -> direction-blocked, x-faces first, each block
+ *                         x-fastest over (N_d+1) in its own direction
+ *                                                            (mesh.hpp:640-720)
+ *   vector cell fields -> component-major (all x components, then y, then z).
+ *                         The reference stores Vect per cell; the C++ adapter
+ *                         (hydro_gb300/adapter/fluid_simple_gpu.hpp) converts.
+ *
+ * Reference interfaces replaced (paths inside divfree/hydro):
+ *   hydro_gpu_create        FluidSimple ctor (source/hydro2dmpi/fluid.hpp:644-792)
+ *                           + AdvectionSolverMultiExplicit ctor
+ *                           (source/hydro2dmpi/advection.hpp:388-415)
+ *   hydro_gpu_update_properties  hydro<Mesh>::UpdateFluidProperties
+ *                           (source/hydro2dmpi/hydro2d.hpp:1404-1430)
+ *   hydro_gpu_start_step    FluidSimple::StartStep (fluid.hpp:793-812)
+ *   hydro_gpu_make_iteration FluidSimple::MakeIteration (fluid.hpp:814-1158)
+ *   hydro_gpu_finish_step   FluidSimple::FinishStep (fluid.hpp:1159-1169)
+ *   hydro_gpu_get_convergence_indicator
+ *                           FluidSimple::GetConvergenceIndicator (fluid.hpp:1170-1172)
+ *   hydro_gpu_get_iteration_count / hydro_gpu_is_converged
+ *                           UnsteadyIterativeSolver (solver.hpp:710-751)
+ *   hydro_gpu_get_auto_time_step FluidSimple::GetAutoTimeStep (fluid.hpp:1191-1206)
+ *   hydro_gpu_set_time_step / hydro_gpu_get_time
+ *                           UnsteadySolver (solver.hpp:679-708)
+ *   hydro_gpu_advection_step AdvectionSolverMultiExplicit Start/MakeIteration/
+ *                           Finish (advection.hpp:417-545)
+ *   hydro_gpu_step          hydro<Mesh>::step (hydro2d.hpp:1531-1621)
+ *   hydro_gpu_calc_stat     hydro<Mesh>::CalcStat (hydro2d.hpp:1432-1529)
+ *   hydro_gpu_get_field / hydro_gpu_set_field
+ *                           FluidSolver::GetVelocity/GetPressure/GetVolumeFlux
+ *                           (fluid.hpp:244-249), AdvectionSolverMulti::GetField
+ *                           (advection.hpp:82), and the raw mixture-field
+ *                           pointers the module hands to FluidSimple
+ *                           (hydro2d.hpp:449-463)
+ *   hydro_gpu_stencil_solve LinearSolver<Scal,IdxCell,Expr>::Solve
+ *                           (linear.hpp:302-310) for symmetric 1+2d stencil rows
+ */
+#ifndef HYDRO_GPU_H_
+#define HYDRO_GPU_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HYDRO_MAX_PHASES 4
+
+enum hydro_status {
+  HYDRO_OK = 0,
+  HYDRO_ERR_ARG = 1,          /* invalid argument / unsupported size */
+  HYDRO_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+  HYDRO_ERR_NAN = 3,          /* NaN in pressure or velocity (fluid.hpp:795-797,1164-1166) */
+  HYDRO_NOT_CONVERGED = 4,    /* a linear solve hit its iteration limit */
+  HYDRO_ERR_UNSUPPORTED = 5,  /* option the GPU path does not implement */
+  HYDRO_ERR_NOMEM = 6,        /* device allocation failed */
+  HYDRO_ERR_NO_DEVICE = 7     /* no CUDA device visible */
+};
+
+/* Sides of the block, in the reference's neighbour-face order
+ * (mesh3d.hpp:297-303): xm, xp, ym, yp, zm, zp. */
+enum hydro_side { HYDRO_XM = 0, HYDRO_XP, HYDRO_YM, HYDRO_YP, HYDRO_ZM, HYDRO_ZP };
+
+/* Fluid boundary condition kinds (fluid.hpp:259-337, parsed at 392-417). */
+enum hydro_bc_kind { HYDRO_BC_WALL = 0, HYDRO_BC_INLET = 1, HYDRO_BC_OUTLET = 2 };
+
+/* Linear solvers.  GAUSS_SEIDEL and LU exist only on the CPU side (oracle);
+ * the GPU runs JACOBI for velocity and CG (Jacobi-preconditioned conjugate
+ * gradients) for pressure. */
+enum hydro_linear {
+  HYDRO_LINEAR_GAUSS_SEIDEL = 0, /* linear.hpp:671-716 */
+  HYDRO_LINEAR_JACOBI = 1,       /* linear.hpp:736-783 */
+  HYDRO_LINEAR_CG = 2,           /* new: no Krylov solver in the reference */
+  HYDRO_LINEAR_LU = 3            /* linear.hpp:527-567 (one symmetric sweep) */
+};
+
+/* Arithmetic of the pressure solve.  MIXED runs the PCG in FP32 inside an
+ * FP64 iterative-refinement loop whose residual, dots and norms stay FP64. */
+enum hydro_precision { HYDRO_FP64 = 0, HYDRO_MIXED = 1 };
+
+/* Field ids for get/set.  Vector fields have dim components (component-major). */
+enum hydro_field {
+  HYDRO_FIELD_VELOCITY = 0,        /* cells x dim; layers: all four */
+  HYDRO_FIELD_PRESSURE = 1,        /* cells; layers: all four */
+  HYDRO_FIELD_VOLUME_FLUX = 2,     /* faces; layers: all four */
+  HYDRO_FIELD_PARTIAL_DENSITY = 3, /* cells x num_phases (phase-major); time_curr only */
+  HYDRO_FIELD_VOLUME_FRACTION = 4, /* cells x num_phases, normalised (hydro2d.hpp:980-997) */
+  HYDRO_FIELD_DENSITY = 5,         /* smoothed mixture density handed to the fluid solver */
+  HYDRO_FIELD_VISCOSITY = 6,       /* smoothed mixture viscosity */
+  HYDRO_FIELD_FORCE = 7,           /* cells x dim: body force rho*g + f (hydro2d.hpp:1308-1316) */
+  HYDRO_FIELD_VOLUME_SOURCE = 8,   /* cells */
+  HYDRO_FIELD_MASS_SOURCE = 9,     /* cells */
+  HYDRO_FIELD_PRESSURE_CORRECTION = 10, /* cells: last p' solved */
+  HYDRO_FIELD_DIAG_COEFF = 11      /* cells: last momentum diagonal D_c (fluid.hpp:876-883) */
+};
+
+/* Same order as solver::Layers (solver.hpp:762). */
+enum hydro_layer {
+  HYDRO_TIME_CURR = 0, HYDRO_TIME_PREV = 1, HYDRO_ITER_CURR = 2, HYDRO_ITER_PREV = 3
+};
+
+/* Case description: the in-scope keys of a .hydroconf script
+ * (examples/general.hydroconf), as consumed by hydro<Mesh>::Init* and the
+ * FluidSimple / AdvectionSolverMultiExplicit constructors. */
+typedef struct hydro_desc {
+  int dim;                      /* 2 or 3 */
+  int n[3];                     /* Nx, Ny, Nz (Nz ignored when dim == 2) */
+  double lo[3], hi[3];          /* domain A, B */
+
+  int bc_kind[6];               /* enum hydro_bc_kind per side (condition_left, ...) */
+  double bc_velocity[6][3];     /* wall / inlet velocity per side */
+
+  double dt;                    /* fixed time step (dt) */
+  int dt_auto;                  /* dt = cfl * min V/|F| each step (hydro2d.hpp:1536-1544) */
+  double cfl, cfl_advection;
+  double dt_max;                /* >0: cap on dt when dt_auto (the reference has none;
+                                   at rest its auto step is 1e10, fluid.hpp:1192) */
+
+  double velocity_relaxation_factor;
+  double pressure_relaxation_factor;
+  double rhie_chow_factor;
+  int time_second_order;
+  int force_geometric_average;
+  double guess_extrapolation;
+  double meshvel[3];
+  double convergence_tolerance; /* SIMPLE: max |u_s - u_{s-1}| */
+  int num_iterations_limit;     /* SIMPLE outer iterations per step */
+  int simpler;                  /* must be 0: SIMPLER branch is not built */
+
+  int velocity_solver;          /* enum hydro_linear */
+  double velocity_tolerance;    /* max |update| per sweep */
+  int velocity_iters_limit;
+  double velocity_omega;        /* relaxation of the sweep */
+  int pressure_solver;          /* enum hydro_linear */
+  double pressure_tolerance;    /* CG: ||r||_2 <= tol*||b||_2; GS/Jacobi: max |update| */
+  int pressure_iters_limit;
+  double pressure_omega;
+  int precision;                /* enum hydro_precision */
+
+  int pressure_fixed_cell;      /* -1: none (pressure_fixed_point) */
+  double pressure_fixed_value;
+
+  int num_phases;
+  double density[HYDRO_MAX_PHASES];
+  double viscosity[HYDRO_MAX_PHASES];
+  double gravity[3], force[3];
+  double sigma;                 /* surface tension coefficient */
+  int density_smooth_times, viscosity_smooth_times, force_smooth_times;
+
+  int advection_enable;
+  double advection_dt_factor;
+  int tvd_split;
+  double sharp;
+
+  void* stream;                 /* cudaStream_t to run on; NULL = library-owned stream */
+} hydro_desc;
+
+typedef struct hydro_step_stats {
+  int status;
+  int outer_iterations;         /* SIMPLE iterations this step */
+  double convergence_indicator; /* last max |u_s - u_{s-1}| */
+  int velocity_sweeps;          /* total momentum sweeps */
+  int pressure_iterations;      /* total pressure-solver iterations */
+  double pressure_residual;     /* last relative residual of the pressure solve */
+  int advection_substeps;
+  double dt, dt_advection, time;
+} hydro_step_stats;
+
+typedef struct hydro_stat {
+  /* hydro<Mesh>::CalcStat per phase (hydro2d.hpp:1432-1529) */
+  double volume[HYDRO_MAX_PHASES];
+  double mass[HYDRO_MAX_PHASES];
+  double pd_min[HYDRO_MAX_PHASES], pd_max[HYDRO_MAX_PHASES];
+  double center[HYDRO_MAX_PHASES][3];
+  double velocity[HYDRO_MAX_PHASES][3];
+  /* sum_c q_i(c) V_c in FP64: the quantity TVD advection conserves */
+  double partial_mass[HYDRO_MAX_PHASES];
+} hydro_stat;
+
+typedef struct hydro_ctx hydro_ctx;
+
+/* Fill *d with the defaults of examples/general.hydroconf for the keys above
+ * (2D 100x100 unit square, walls, dt 0.01, relaxations 0.8/0.9, ...). */
+int hydro_desc_default(hydro_desc* d);
+
+int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out);
+int hydro_gpu_destroy(hydro_ctx* ctx);
+
+/* Copy a host array into / out of a field.  n = number of doubles. */
+int hydro_gpu_set_field(hydro_ctx* ctx, int field, int layer, const double* src, size_t n);
+int hydro_gpu_get_field(hydro_ctx* ctx, int field, int layer, double* dst, size_t n);
+/* Device pointer of a field layer (no copy); NULL if the field is unknown. */
+int hydro_gpu_field_ptr(hydro_ctx* ctx, int field, int layer, double** ptr);
+
+/* Initial state: velocity (time_curr = time_prev = given), partial densities.
+ * Computes the initial face fluxes (fluid.hpp:770-791) and then the mixture
+ * properties.  Call once after set_field of the initial arrays. */
+int hydro_gpu_init_state(hydro_ctx* ctx);
+
+int hydro_gpu_update_properties(hydro_ctx* ctx);
+int hydro_gpu_start_step(hydro_ctx* ctx);
+int hydro_gpu_make_iteration(hydro_ctx* ctx);
+int hydro_gpu_finish_step(hydro_ctx* ctx);
+int hydro_gpu_get_convergence_indicator(hydro_ctx* ctx, double* out);
+int hydro_gpu_get_iteration_count(hydro_ctx* ctx, int* out);
+int hydro_gpu_is_converged(hydro_ctx* ctx, int* out);
+int hydro_gpu_get_auto_time_step(hydro_ctx* ctx, double* out);
+int hydro_gpu_set_time_step(hydro_ctx* ctx, double dt, double dt_advection);
+int hydro_gpu_get_time(hydro_ctx* ctx, double* fluid_time, double* advection_time);
+/* All advection substeps that bring advection time up to fluid time
+ * (hydro2d.hpp:1596-1604). */
+int hydro_gpu_advection_step(hydro_ctx* ctx, int* substeps);
+
+/* One full time step: dt_auto, SIMPLE loop to convergence, advection
+ * substeps, property update.  stats may be NULL. */
+int hydro_gpu_step(hydro_ctx* ctx, hydro_step_stats* stats);
+int hydro_gpu_calc_stat(hydro_ctx* ctx, hydro_stat* out);
+
+/* Solve sum_j a_j x_j + c = 0 for a symmetric 7-point (3D) / 5-point (2D)
+ * stencil on an nx*ny*nz block, the rows the pressure system has
+ * (fluid.hpp:972-1027): coupling coefficients per face, diagonal implied as
+ * the sum of the face couplings plus `shift`.
+ *   face_coeff: device pointer, direction-blocked face array (same layout as
+ *               volume fluxes); coupling of the two cells of an inner face is
+ *               -face_coeff[f]; boundary-face entries are ignored.
+ *   rhs:        device pointer, cells: the row constant c (so A x = -c).
+ *   x:          device pointer, cells: output (initial guess on input when
+ *               use_guess != 0).
+ *   workspace:  device pointer of at least hydro_gpu_stencil_workspace_size()
+ *               bytes.
+ *   pinned_cell: -1, or a cell whose row is x = pinned_value with that value
+ *               substituted into its neighbours' rows (the symmetric
+ *               treatment of a fixed-pressure cell, fluid.hpp:996-1014).
+ * Singular (shift == 0, no pinned cell) systems are solved in the subspace
+ * orthogonal to the constants and return the zero-mean solution.  Returns HYDRO_NOT_CONVERGED when the limit is
+ * hit; *iterations and *residual report the relative residual reached. */
+size_t hydro_gpu_stencil_workspace_size(int dim, int nx, int ny, int nz);
+int hydro_gpu_stencil_solve(int dim, int nx, int ny, int nz,
+                            const double* face_coeff, double shift,
+                            long pinned_cell, double pinned_value,
+                            const double* rhs, double* x, int use_guess,
+                            double tolerance, int iters_limit,
+                            void* workspace, void* stream,
+                            int* iterations, double* residual);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HYDRO_GPU_H_ */
