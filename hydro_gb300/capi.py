@@ -268,3 +268,35 @@ def _declare(lib, prefix):
                             ctypes.c_double, D, D, I, ctypes.c_double, I,
                             ctypes.POINTER(I), D]
     stencil.restype = I
+
+
+def desc_to_dict(d):
+    """Plain-dict form of a HydroDesc (fixtures, logs)."""
+    out = {}
+    for name, ctype in HydroDesc._fields_:
+        if name == "stream":
+            continue
+        v = getattr(d, name)
+        if hasattr(v, "__len__"):
+            v = [list(x) if hasattr(x, "__len__") else x for x in v]
+        out[name] = v
+    return out
+
+
+def desc_from_dict(src):
+    d = default_desc()
+    for name, ctype in HydroDesc._fields_:
+        if name == "stream" or name not in src:
+            continue
+        v = src[name]
+        if isinstance(v, list):
+            arr = getattr(d, name)
+            for i, x in enumerate(v):
+                if isinstance(x, list):
+                    for j, y in enumerate(x):
+                        arr[i][j] = y
+                else:
+                    arr[i] = x
+        else:
+            setattr(d, name, v)
+    return d

@@ -1,0 +1,176 @@
+// common.cuh -- mesh indexing, launch geometry and deterministic reductions
+// shared by the sm_103a kernels of the hydro hot path.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hg {
+
+// Uniform Cartesian block.  Cells: i + nx*(j + ny*k); faces direction-
+// blocked, x-fastest over (n_d+1) in their own direction (the reference's
+// raw order, mesh.hpp:552-561 and 640-720).  Geometry is implicit:
+// h_d = (B_d - A_d)/N_d, V = prod h, A_d = V/h_d (InitUniformMesh,
+// mesh.hpp:722-736).
+struct Mesh {
+  int dim;
+  int n[3];
+  long long nc, nf;
+  long long fofs[3];  // first face of each direction block
+  int fnx[3], fny[3]; // x/y extents of each direction block
+  double h[3], V, A[3];
+  double lo[3];
+};
+
+__host__ __device__ inline long long cell_id(const Mesh& m, int i, int j, int k) {
+  return i + (long long)m.n[0] * (j + (long long)m.n[1] * k);
+}
+__host__ __device__ inline long long face_id(const Mesh& m, int d, int i, int j, int k) {
+  return m.fofs[d] + i + (long long)m.fnx[d] * (j + (long long)m.fny[d] * k);
+}
+// stride between neighbouring cells along d
+__host__ __device__ inline long long cell_stride(const Mesh& m, int d) {
+  return d == 0 ? 1 : (d == 1 ? (long long)m.n[0] : (long long)m.n[0] * m.n[1]);
+}
+// stride between the low and high face of a cell along d
+__host__ __device__ inline long long face_stride(const Mesh& m, int d) {
+  return d == 0 ? 1 : (d == 1 ? (long long)m.fnx[1] : (long long)m.fnx[2] * m.fny[2]);
+}
+
+// Launch geometry: blocks of 32x8 threads over (i, j); each block marches
+// KCH planes in k so that the grid stays a few waves deep on 152 SMs.
+constexpr int BX = 32, BY = 8, NT = BX * BY;
+
+struct Launch {
+  dim3 grid, block;
+  int kch;
+  int nblocks() const { return grid.x * grid.y * grid.z; }
+};
+
+inline Launch cell_launch(const Mesh& m, int target_blocks = 152 * 16) {
+  Launch L;
+  L.block = dim3(BX, BY, 1);
+  int gx = (m.n[0] + BX - 1) / BX, gy = (m.n[1] + BY - 1) / BY;
+  int nz = m.dim == 3 ? m.n[2] : 1;
+  int per = gx * gy;
+  int gz = (target_blocks + per - 1) / per;
+  if (gz > nz) gz = nz;
+  if (gz < 1) gz = 1;
+  L.kch = (nz + gz - 1) / gz;
+  gz = (nz + L.kch - 1) / L.kch;
+  L.grid = dim3(gx, gy, gz);
+  return L;
+}
+
+// ------------------------------------------------------------ reductions --
+// Deterministic grid reduction: every block writes its partial, the last
+// block to arrive (atomic ticket) combines the partials in index order and
+// runs the finaliser.  The ticket is reset for the next launch.
+
+template <class T>
+__device__ inline T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+template <class T>
+__device__ inline T warp_max(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    T w = __shfl_down_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+template <class T>
+__device__ inline T warp_min(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    T w = __shfl_down_sync(0xffffffffu, v, o);
+    v = w < v ? w : v;
+  }
+  return v;
+}
+
+enum RedOp { RED_SUM = 0, RED_MAX = 1, RED_MIN = 2 };
+
+template <int OP, class T>
+__device__ inline T red_combine(T a, T b) {
+  if (OP == RED_SUM) return a + b;
+  if (OP == RED_MAX) return a > b ? a : b;
+  return a < b ? a : b;
+}
+template <int OP, class T>
+__device__ inline T warp_red(T v) {
+  if (OP == RED_SUM) return warp_sum(v);
+  if (OP == RED_MAX) return warp_max(v);
+  return warp_min(v);
+}
+
+// Block reduction of NV values; result valid in thread 0.
+template <int OP, int NV, class T>
+__device__ inline void block_reduce(T (&v)[NV], T* sh /* [NV][32] */) {
+  int tid = threadIdx.x + blockDim.x * threadIdx.y;
+  int lane = tid & 31, wid = tid >> 5;
+  int nw = (blockDim.x * blockDim.y + 31) >> 5;
+#pragma unroll
+  for (int a = 0; a < NV; ++a) v[a] = warp_red<OP>(v[a]);
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int a = 0; a < NV; ++a) sh[a * 32 + wid] = v[a];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int a = 0; a < NV; ++a) {
+      T x = lane < nw ? sh[a * 32 + lane] : (OP == RED_SUM ? T(0) : sh[a * 32]);
+      v[a] = warp_red<OP>(x);
+    }
+  }
+}
+
+// Writes this block's NV partials; returns true in the (single) last block,
+// whose thread 0..NT-1 then see `out` = the reduced values in shared memory.
+// partials layout: [NV][nblocks].
+template <int OP, int NV, class T>
+__device__ inline bool grid_reduce(T (&v)[NV], T* partials, unsigned* ticket, T* out_sh) {
+  __shared__ T sh[NV * 32];
+  __shared__ bool last;
+  block_reduce<OP, NV>(v, sh);
+  int tid = threadIdx.x + blockDim.x * threadIdx.y;
+  int nthr = blockDim.x * blockDim.y;
+  unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+  unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  if (tid == 0) {
+#pragma unroll
+    for (int a = 0; a < NV; ++a) partials[(size_t)a * nb + bid] = v[a];
+    __threadfence();
+    unsigned t = atomicAdd(ticket, 1u);
+    last = (t == nb - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  // fixed-order combine: thread t folds partials t, t+nthr, ... in order,
+  // then a fixed tree over threads
+  T acc[NV];
+#pragma unroll
+  for (int a = 0; a < NV; ++a) {
+    const volatile T* pa = partials + (size_t)a * nb;
+    T x = (tid < (int)nb) ? pa[tid] : T(0);
+    for (unsigned b = tid + nthr; b < nb; b += nthr) x = red_combine<OP>(x, (T)pa[b]);
+    if (tid >= (int)nb) x = (OP == RED_SUM) ? T(0) : (T)pa[0];
+    acc[a] = x;
+  }
+  block_reduce<OP, NV>(acc, sh);
+  if (tid == 0) {
+#pragma unroll
+    for (int a = 0; a < NV; ++a) out_sh[a] = acc[a];
+    *ticket = 0u;
+  }
+  __syncthreads();
+  return true;
+}
+
+}  // namespace hg

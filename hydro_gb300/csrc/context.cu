@@ -1,0 +1,844 @@
+// context.cu -- the C-ABI of include/hydro_gpu.h and the host-side
+// orchestration (C++) of the hot path on one GPU:
+//   FluidSimple::StartStep / MakeIteration / FinishStep (fluid.hpp:793-1169)
+//   AdvectionSolverMultiExplicit substeps (advection.hpp:417-545,
+//     hydro2d.hpp:1596-1604)
+//   hydro<Mesh>::UpdateFluidProperties / CalcStat / step (hydro2d.hpp:1404-1621)
+//
+// All fields live in one device arena owned by the context; host arrays are
+// copied only by set_field/get_field.  Inner loops (momentum sweeps, CG
+// iterations) are queued in chunks; kernels stop themselves once the
+// device-side convergence flag is set and the host reads the flags once per
+// chunk, so the GPU never waits on the host between iterations of a chunk.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <utility>
+
+#include "../../include/hydro_gpu.h"
+#include "kernels.h"
+#include "loop.cuh"
+
+using namespace hg;
+
+namespace {
+
+constexpr int kSweepChunk = 8;
+constexpr int kCgChunk = 32;
+
+struct Arena {
+  char* base = nullptr;
+  size_t used = 0, cap = 0;
+  template <class T>
+  T* take(size_t n) {
+    size_t bytes = ((n * sizeof(T)) + 255) & ~size_t(255);
+    T* p = reinterpret_cast<T*>(base + used);
+    used += bytes;
+    return p;
+  }
+};
+
+}  // namespace
+
+struct hydro_ctx {
+  hydro_desc d;
+  Mesh m;
+  int dim = 2, nph = 1;
+  int device = 0;
+  cudaStream_t st = nullptr;
+  bool own_stream = false;
+  Arena arena;
+  // fluid layers (solver::Layers order); vector fields component-major
+  double* u[4] = {};
+  double* p[4] = {};
+  double* F[4] = {};
+  // mixture fields (hydro2d.hpp:449-463)
+  double *rho = nullptr, *mu = nullptr, *rho_raw = nullptr, *smtmp = nullptr;
+  double *force = nullptr, *stforce = nullptr, *Sv = nullptr, *Sm = nullptr;
+  // phases
+  double *q = nullptr, *qtmp = nullptr, *alpha = nullptr, *qflux = nullptr;
+  // iteration work
+  double *G = nullptr, *fo = nullptr, *fres = nullptr, *coef = nullptr, *res = nullptr;
+  double* du[2] = {};
+  double *Dc = nullptr, *Fs = nullptr, *kf = nullptr, *pc = nullptr, *prhs = nullptr;
+  PcgWork pw{};
+  double* stat_out = nullptr;
+  unsigned* stat_ticket = nullptr;
+  DevScalars* hds = nullptr;  // pinned host mirror
+  // scalars
+  double time = 0., dt = 0., adv_time = 0., adv_dt = 0.;
+  int iter_count = 0, cd_iter_count = 0;
+  int vel_sweeps = 0, p_iters = 0;
+  double p_res = 0., indicator = 1.;
+  int du_cur = 0;
+  int status = HYDRO_OK;
+  FluidCoef fc{};
+  PhaseProps pp{};
+
+  double* ucomp(int layer, int k) { return u[layer] + (size_t)k * m.nc; }
+  C3 uc3(int layer) {
+    C3 r{};
+    for (int k = 0; k < 3; ++k) r.a[k] = k < dim ? ucomp(layer, k) : nullptr;
+    return r;
+  }
+  W3 uw3(int layer) {
+    W3 r{};
+    for (int k = 0; k < 3; ++k) r.a[k] = k < dim ? ucomp(layer, k) : nullptr;
+    return r;
+  }
+  template <class P>
+  P vec(double* base, int n, long long stride) {
+    P r{};
+    for (int k = 0; k < n; ++k) r.a[k] = base + (size_t)k * stride;
+    return r;
+  }
+};
+
+namespace {
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return HYDRO_OK;
+  if (e == cudaErrorMemoryAllocation) return HYDRO_ERR_NOMEM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return HYDRO_ERR_NO_DEVICE;
+  return HYDRO_ERR_CUDA;
+}
+
+#define CK(expr)                              \
+  do {                                        \
+    cudaError_t e_ = (expr);                  \
+    if (e_ != cudaSuccess) return cuda_status(e_); \
+  } while (0)
+
+int init_mesh(Mesh& m, int dim, const int* n, const double* lo, const double* hi) {
+  memset(&m, 0, sizeof(m));
+  if (dim != 2 && dim != 3) return HYDRO_ERR_ARG;
+  m.dim = dim;
+  for (int d = 0; d < 3; ++d) {
+    m.n[d] = d < dim ? n[d] : 1;
+    if (d < dim && m.n[d] < 2) return HYDRO_ERR_ARG;
+    m.lo[d] = d < dim ? lo[d] : 0.;
+    m.h[d] = d < dim ? (hi[d] - lo[d]) / (double)n[d] : 1.;
+    if (d < dim && !(m.h[d] > 0.)) return HYDRO_ERR_ARG;
+  }
+  m.nc = (long long)m.n[0] * m.n[1] * m.n[2];
+  long long off = 0;
+  for (int d = 0; d < 3; ++d) {
+    m.fnx[d] = m.n[0] + (d == 0);
+    m.fny[d] = m.n[1] + (d == 1);
+    m.fofs[d] = off;
+    if (d < dim) off += (long long)m.fnx[d] * m.fny[d] * (m.n[2] + (d == 2));
+  }
+  m.nf = off;
+  m.V = 1.;
+  for (int d = 0; d < dim; ++d) m.V *= m.h[d];
+  for (int d = 0; d < 3; ++d) m.A[d] = d < dim ? m.V / m.h[d] : 0.;
+  return HYDRO_OK;
+}
+
+// GetDerivativeApproxCoeffs(0, {-2dt, -dt, 0}, skip) (solver.hpp:815-861).
+void bdf_coeffs(double dt, int second, double* co) {
+  double args[3] = {-2. * dt, -dt, 0.};
+  int skip = second ? 0 : 1;
+  int sz = 3 - skip;
+  co[0] = co[1] = co[2] = 0.;
+  for (int i = 0; i < sz; ++i) {
+    double denom = 1., numer = 0.;
+    for (int j = 0; j < sz; ++j) {
+      if (j == i) continue;
+      denom *= args[skip + i] - args[skip + j];
+      double term = 1.;
+      for (int k = 0; k < sz; ++k)
+        if (k != i && k != j) term *= 0. - args[skip + k];
+      numer += term;
+    }
+    co[skip + i] = numer / denom;
+  }
+}
+
+int sync_scalars(hydro_ctx* x) {
+  CK(cudaMemcpyAsync(x->hds, x->pw.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, x->st));
+  CK(cudaStreamSynchronize(x->st));
+  return HYDRO_OK;
+}
+
+int reset_flags(hydro_ctx* x, int first, int count) {
+  CK(cudaMemsetAsync(&x->pw.ds->flag[first], 0, sizeof(int) * count, x->st));
+  return HYDRO_OK;
+}
+
+// ------------------------------------------------------------- momentum --
+int solve_momentum(hydro_ctx* x, C3 up) {
+  const hydro_desc& d = x->d;
+  int dim = x->dim;
+  CP<7> cc = x->vec<CP<7>>(x->coef, 2 * dim + 1, x->m.nc);
+  C3 resc = x->vec<C3>(x->res, dim, x->m.nc);
+  int rc = reset_flags(x, FL_MOM_DONE, 2);
+  if (rc) return rc;
+  int limit = d.velocity_iters_limit + 1;  // do { } while (iter++ < limit)
+  int queued = 0;
+  for (;;) {
+    int n = std::min(kSweepChunk, limit - queued);
+    for (int s = 0; s < n; ++s) {
+      int k = queued + s;
+      C3 din = x->vec<C3>(x->du[(k + 1) % 2], dim, x->m.nc);
+      W3 dout = x->vec<W3>(x->du[k % 2], dim, x->m.nc);
+      CK(launch_mom_sweep(x->m, d.velocity_omega, d.velocity_tolerance, cc, resc, din, dout,
+                          k == 0, x->pw.partials, x->pw.ds, x->st));
+    }
+    queued += n;
+    rc = sync_scalars(x);
+    if (rc) return rc;
+    if (x->hds->flag[FL_MOM_DONE] || queued >= limit) break;
+  }
+  int sweeps = x->hds->flag[FL_MOM_SWEEPS];
+  x->vel_sweeps += sweeps;
+  x->du_cur = (sweeps - 1) % 2;
+  return HYDRO_OK;
+}
+
+// ------------------------------------------------------------- pressure --
+int solve_pressure(hydro_ctx* x) {
+  const hydro_desc& d = x->d;
+  const Mesh& m = x->m;
+  int singular = (d.pressure_fixed_cell < 0);
+  PcgWork& w = x->pw;
+  w.pin = d.pressure_fixed_cell;
+  if (w.pin >= 0) CK(pin_rhs(m, x->kf, x->prhs, w.pin, d.pressure_fixed_value, x->st));
+  int mixed = (d.precision == HYDRO_MIXED);
+  CK(pcg_prepare(m, x->kf, 0., w, mixed, x->st));
+  int rc;
+  if (!mixed) {
+    w.limit = d.pressure_iters_limit;
+    CK(pcg_init(m, x->kf, x->prhs, x->pc, 0, d.pressure_tolerance, singular, w, x->st));
+    int queued = 0;
+    for (;;) {
+      int n = std::min(kCgChunk, std::max(1, d.pressure_iters_limit - queued));
+      CK(pcg_iterate(m, x->kf, x->pc, n, w, x->st));
+      queued += n;
+      rc = sync_scalars(x);
+      if (rc) return rc;
+      if (x->hds->flag[FL_PCG_DONE] || queued >= d.pressure_iters_limit) break;
+    }
+    int it = x->hds->flag[FL_PCG_ITERS];
+    x->p_iters += it;
+    double ff = x->hds->red[RS_PCG_FF];
+    x->p_res = ff > 0. ? sqrt(x->hds->red[RS_PCG_RR] / ff) : 0.;
+  } else {
+    // FP64 iterative refinement around FP32 PCG
+    if (singular) CK(mean_sum(m, x->prhs, w, x->st));
+    CK(cudaMemsetAsync(x->pc, 0, sizeof(double) * m.nc, x->st));
+    double ff = -1.;
+    int total = 0;
+    const double inner_tol = 1e-4;
+    for (int outer = 0; outer < 50; ++outer) {
+      CK(ir_residual(m, x->kf, x->prhs, x->pc, singular, w, x->st));
+      rc = sync_scalars(x);
+      if (rc) return rc;
+      double rr = x->hds->red[RS_IR_RR];
+      if (ff < 0.) ff = rr;
+      x->p_res = ff > 0. ? sqrt(rr / ff) : 0.;
+      if (ff == 0. || rr <= d.pressure_tolerance * d.pressure_tolerance * ff) break;
+      if (total >= d.pressure_iters_limit) break;
+      w.limit = d.pressure_iters_limit - total;
+      double tol = std::max(inner_tol, 0.5 * d.pressure_tolerance * sqrt(ff / rr));
+      CK(f32_pcg_init(m, tol, w, x->st));
+      int queued = 0;
+      for (;;) {
+        CK(f32_pcg_iterate(m, kCgChunk, w, x->st));
+        queued += kCgChunk;
+        rc = sync_scalars(x);
+        if (rc) return rc;
+        if (x->hds->flag[FL_PCG_DONE] || queued >= w.limit) break;
+      }
+      total += x->hds->flag[FL_PCG_ITERS];
+      CK(f32_accumulate(m, x->pc, w, x->st));
+    }
+    x->p_iters += total;
+  }
+  if (singular) CK(sub_mean(m, x->pc, w, x->st));
+  return HYDRO_OK;
+}
+
+int nan_check(hydro_ctx* x, const double* a, long long n) {
+  CK(launch_nan_count(n, a, x->pw.partials, x->pw.ds, x->st));
+  int rc = sync_scalars(x);
+  if (rc) return rc;
+  return x->hds->red[RS_NAN] > 0. ? HYDRO_ERR_NAN : HYDRO_OK;
+}
+
+int fluid_field(hydro_ctx* x, int field, int layer, double** ptr, long long* n) {
+  const Mesh& m = x->m;
+  if (layer < 0 || layer > 3) return HYDRO_ERR_ARG;
+  *n = m.nc;
+  switch (field) {
+    case HYDRO_FIELD_VELOCITY: *ptr = x->u[layer]; *n = m.nc * x->dim; return HYDRO_OK;
+    case HYDRO_FIELD_PRESSURE: *ptr = x->p[layer]; return HYDRO_OK;
+    case HYDRO_FIELD_VOLUME_FLUX: *ptr = x->F[layer]; *n = m.nf; return HYDRO_OK;
+    case HYDRO_FIELD_PARTIAL_DENSITY: *ptr = x->q; *n = m.nc * x->nph; return HYDRO_OK;
+    case HYDRO_FIELD_VOLUME_FRACTION: *ptr = x->alpha; *n = m.nc * x->nph; return HYDRO_OK;
+    case HYDRO_FIELD_DENSITY: *ptr = x->rho; return HYDRO_OK;
+    case HYDRO_FIELD_VISCOSITY: *ptr = x->mu; return HYDRO_OK;
+    case HYDRO_FIELD_FORCE: *ptr = x->force; *n = m.nc * x->dim; return HYDRO_OK;
+    case HYDRO_FIELD_VOLUME_SOURCE: *ptr = x->Sv; return HYDRO_OK;
+    case HYDRO_FIELD_MASS_SOURCE: *ptr = x->Sm; return HYDRO_OK;
+    case HYDRO_FIELD_PRESSURE_CORRECTION: *ptr = x->pc; return HYDRO_OK;
+    case HYDRO_FIELD_DIAG_COEFF: *ptr = x->Dc; return HYDRO_OK;
+  }
+  return HYDRO_ERR_ARG;
+}
+
+}  // namespace
+
+// ================================================================ C-ABI ==
+extern "C" {
+
+int hydro_desc_default(hydro_desc* d) {
+  if (!d) return HYDRO_ERR_ARG;
+  memset(d, 0, sizeof(*d));
+  d->dim = 2;
+  d->n[0] = 100; d->n[1] = 100; d->n[2] = 5;
+  for (int k = 0; k < 3; ++k) { d->lo[k] = 0.; d->hi[k] = 1.; }
+  for (int s = 0; s < 6; ++s) d->bc_kind[s] = HYDRO_BC_WALL;
+  d->dt = 0.01;
+  d->cfl = 0.5;
+  d->cfl_advection = 0.5;
+  d->velocity_relaxation_factor = 0.8;
+  d->pressure_relaxation_factor = 0.9;
+  d->rhie_chow_factor = 1.;
+  d->time_second_order = 1;
+  d->convergence_tolerance = 1e-2;
+  d->num_iterations_limit = 10;
+  d->velocity_solver = HYDRO_LINEAR_JACOBI;
+  d->velocity_tolerance = 1e-3;
+  d->velocity_iters_limit = 1000;
+  d->velocity_omega = 1.;
+  d->pressure_solver = HYDRO_LINEAR_CG;
+  d->pressure_tolerance = 1e-8;
+  d->pressure_iters_limit = 100000;
+  d->pressure_omega = 1.;
+  d->precision = HYDRO_FP64;
+  d->pressure_fixed_cell = -1;
+  d->num_phases = 1;
+  for (int i = 0; i < HYDRO_MAX_PHASES; ++i) { d->density[i] = 1.; d->viscosity[i] = 1.; }
+  d->density_smooth_times = 2;
+  d->viscosity_smooth_times = 2;
+  d->advection_enable = 1;
+  d->advection_dt_factor = 0.1;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
+  if (!desc || !out) return HYDRO_ERR_ARG;
+  *out = nullptr;
+  if (desc->simpler) return HYDRO_ERR_UNSUPPORTED;
+  if (desc->num_phases < 1 || desc->num_phases > HYDRO_MAX_PHASES) return HYDRO_ERR_ARG;
+  for (int s = 0; s < 2 * desc->dim && s < 6; ++s)
+    if (desc->bc_kind[s] != HYDRO_BC_WALL) return HYDRO_ERR_UNSUPPORTED;
+  if (desc->velocity_omega <= 0. || desc->velocity_relaxation_factor <= 0.)
+    return HYDRO_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return HYDRO_ERR_NO_DEVICE;
+  hydro_ctx* x = new (std::nothrow) hydro_ctx();
+  if (!x) return HYDRO_ERR_NOMEM;
+  x->d = *desc;
+  int rc = init_mesh(x->m, desc->dim, desc->n, desc->lo, desc->hi);
+  if (rc) { delete x; return rc; }
+  if (desc->pressure_fixed_cell >= x->m.nc) { delete x; return HYDRO_ERR_ARG; }
+  const Mesh& m = x->m;
+  x->dim = desc->dim;
+  x->nph = desc->num_phases;
+  cudaGetDevice(&x->device);
+  if (desc->stream) {
+    x->st = (cudaStream_t)desc->stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&x->st, cudaStreamNonBlocking) != cudaSuccess) {
+      delete x;
+      return HYDRO_ERR_CUDA;
+    }
+    x->own_stream = true;
+  }
+  // arena layout
+  long long nc = m.nc, nf = m.nf;
+  int dim = x->dim, nph = x->nph;
+  auto plan = [&](Arena& a) {
+    for (int l = 0; l < 4; ++l) x->u[l] = a.take<double>(nc * dim);
+    for (int l = 0; l < 4; ++l) x->p[l] = a.take<double>(nc);
+    for (int l = 0; l < 4; ++l) x->F[l] = a.take<double>(nf);
+    x->rho = a.take<double>(nc);
+    x->mu = a.take<double>(nc);
+    x->rho_raw = a.take<double>(nc);
+    x->smtmp = a.take<double>(nc);
+    x->force = a.take<double>(nc * dim);
+    x->stforce = a.take<double>(nc * dim);
+    x->Sv = a.take<double>(nc);
+    x->Sm = a.take<double>(nc);
+    x->q = a.take<double>(nc * nph);
+    x->qtmp = a.take<double>(nc * nph);
+    x->alpha = a.take<double>(nc * nph);
+    x->qflux = a.take<double>(nf * nph);
+    x->G = a.take<double>(nc * dim * dim);
+    x->fo = a.take<double>(nc * dim);
+    x->fres = a.take<double>(nc * dim);
+    x->coef = a.take<double>(nc * (2 * dim + 1));
+    x->res = a.take<double>(nc * dim);
+    x->du[0] = a.take<double>(nc * dim);
+    x->du[1] = a.take<double>(nc * dim);
+    x->Dc = a.take<double>(nc);
+    x->Fs = a.take<double>(nf);
+    x->kf = a.take<double>(nf);
+    x->pc = a.take<double>(nc);
+    x->prhs = a.take<double>(nc);
+    PcgWork& w = x->pw;
+    w.r = a.take<double>(nc);
+    w.z = a.take<double>(nc);
+    w.p = a.take<double>(nc);
+    w.Ap = a.take<double>(nc);
+    w.dg = a.take<double>(nc);
+    w.idg = a.take<double>(nc);
+    w.r32 = a.take<float>(nc);
+    w.z32 = a.take<float>(nc);
+    w.p32 = a.take<float>(nc);
+    w.Ap32 = a.take<float>(nc);
+    w.dg32 = a.take<float>(nc);
+    w.idg32 = a.take<float>(nc);
+    w.x32 = a.take<float>(nc);
+    w.kf32 = a.take<float>(nf);
+    w.partials = a.take<double>((size_t)10 * kMaxBlocks);
+    w.ds = a.take<DevScalars>(1);
+    x->stat_out = a.take<double>(16);
+    x->stat_ticket = a.take<unsigned>(4);
+  };
+  Arena probe;
+  plan(probe);
+  size_t bytes = probe.used;
+  if (cudaMalloc(&x->arena.base, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    if (x->own_stream) cudaStreamDestroy(x->st);
+    delete x;
+    return HYDRO_ERR_NOMEM;
+  }
+  x->arena.cap = bytes;
+  plan(x->arena);
+  if (cudaMallocHost(&x->hds, sizeof(DevScalars)) != cudaSuccess) {
+    cudaFree(x->arena.base);
+    if (x->own_stream) cudaStreamDestroy(x->st);
+    delete x;
+    return HYDRO_ERR_NOMEM;
+  }
+  if (cudaMemsetAsync(x->arena.base, 0, bytes, x->st) != cudaSuccess ||
+      cudaStreamSynchronize(x->st) != cudaSuccess) {
+    hydro_gpu_destroy(x);
+    return HYDRO_ERR_CUDA;
+  }
+  x->pw.pin = desc->pressure_fixed_cell;
+  // constants
+  for (int s = 0; s < 6; ++s)
+    for (int k = 0; k < 3; ++k) x->fc.bcu[s][k] = (k < dim) ? desc->bc_velocity[s][k] : 0.;
+  x->fc.relax_u = desc->velocity_relaxation_factor;
+  x->fc.relax_p = desc->pressure_relaxation_factor;
+  x->fc.rc = desc->rhie_chow_factor;
+  for (int k = 0; k < 3; ++k) x->fc.meshvel[k] = k < dim ? desc->meshvel[k] : 0.;
+  x->fc.geometric = desc->force_geometric_average;
+  x->fc.sources = 0;
+  for (int i = 0; i < HYDRO_MAXPH; ++i) {
+    x->pp.dens[i] = desc->density[i];
+    x->pp.visc[i] = desc->viscosity[i];
+  }
+  for (int k = 0; k < 3; ++k) {
+    x->pp.grav[k] = k < dim ? desc->gravity[k] : 0.;
+    x->pp.f0[k] = k < dim ? desc->force[k] : 0.;
+  }
+  x->dt = desc->dt;
+  x->adv_dt = desc->dt * desc->advection_dt_factor;
+  *out = x;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_destroy(hydro_ctx* x) {
+  if (!x) return HYDRO_OK;
+  if (x->st) cudaStreamSynchronize(x->st);
+  if (x->arena.base) cudaFree(x->arena.base);
+  if (x->hds) cudaFreeHost(x->hds);
+  if (x->own_stream && x->st) cudaStreamDestroy(x->st);
+  delete x;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_field_ptr(hydro_ctx* x, int field, int layer, double** ptr) {
+  if (!x || !ptr) return HYDRO_ERR_ARG;
+  long long n;
+  return fluid_field(x, field, layer, ptr, &n);
+}
+
+int hydro_gpu_set_field(hydro_ctx* x, int field, int layer, const double* src, size_t n) {
+  if (!x || !src) return HYDRO_ERR_ARG;
+  double* p;
+  long long len;
+  int rc = fluid_field(x, field, layer, &p, &len);
+  if (rc) return rc;
+  if ((long long)n != len) return HYDRO_ERR_ARG;
+  CK(cudaMemcpyAsync(p, src, sizeof(double) * n, cudaMemcpyHostToDevice, x->st));
+  CK(cudaStreamSynchronize(x->st));
+  return HYDRO_OK;
+}
+
+int hydro_gpu_get_field(hydro_ctx* x, int field, int layer, double* dst, size_t n) {
+  if (!x || !dst) return HYDRO_ERR_ARG;
+  double* p;
+  long long len;
+  int rc = fluid_field(x, field, layer, &p, &len);
+  if (rc) return rc;
+  if ((long long)n != len) return HYDRO_ERR_ARG;
+  CK(cudaMemcpyAsync(dst, p, sizeof(double) * n, cudaMemcpyDeviceToHost, x->st));
+  CK(cudaStreamSynchronize(x->st));
+  return HYDRO_OK;
+}
+
+int hydro_gpu_update_properties(hydro_ctx* x) {
+  if (!x) return HYDRO_ERR_ARG;
+  const Mesh& m = x->m;
+  const hydro_desc& d = x->d;
+  int dim = x->dim;
+  CK(launch_props(m, x->nph, x->pp, x->vec<CP<HYDRO_MAXPH>>(x->q, x->nph, m.nc),
+                  x->vec<WP<HYDRO_MAXPH>>(x->alpha, x->nph, m.nc), x->rho_raw, x->rho, x->mu,
+                  x->vec<W3>(x->force, dim, m.nc), x->Sv, x->Sm, x->st));
+  auto smooth = [&](double* a, int times) -> int {
+    double* in = a;
+    double* tmp = x->smtmp;
+    for (int r = 0; r < times; ++r) {
+      CK(launch_smooth(m, in, tmp, x->st));
+      std::swap(in, tmp);
+    }
+    if (in != a) CK(cudaMemcpyAsync(a, in, sizeof(double) * m.nc, cudaMemcpyDeviceToDevice, x->st));
+    return HYDRO_OK;
+  };
+  int rc = smooth(x->rho, d.density_smooth_times);
+  if (rc) return rc;
+  rc = smooth(x->mu, d.viscosity_smooth_times);
+  if (rc) return rc;
+  if (x->nph >= 2 && d.sigma != 0.) {
+    CK(launch_stforce(m, d.sigma, x->alpha + m.nc, x->vec<W3>(x->G, dim, m.nc),
+                      x->vec<W3>(x->stforce, dim, m.nc), x->st));
+  }
+  for (int k = 0; k < dim; ++k) {
+    rc = smooth(x->force + (size_t)k * m.nc, d.force_smooth_times);
+    if (rc) return rc;
+  }
+  CK(cudaGetLastError());
+  return HYDRO_OK;
+}
+
+int hydro_gpu_init_state(hydro_ctx* x) {
+  if (!x) return HYDRO_ERR_ARG;
+  const Mesh& m = x->m;
+  CK(cudaMemcpyAsync(x->u[HYDRO_TIME_PREV], x->u[HYDRO_TIME_CURR],
+                     sizeof(double) * m.nc * x->dim, cudaMemcpyDeviceToDevice, x->st));
+  CK(cudaMemsetAsync(x->p[HYDRO_TIME_CURR], 0, sizeof(double) * m.nc, x->st));
+  CK(cudaMemsetAsync(x->p[HYDRO_TIME_PREV], 0, sizeof(double) * m.nc, x->st));
+  CK(launch_init_flux(m, x->fc, x->uc3(HYDRO_TIME_CURR), x->F[HYDRO_TIME_CURR], x->st));
+  CK(cudaMemcpyAsync(x->F[HYDRO_TIME_PREV], x->F[HYDRO_TIME_CURR], sizeof(double) * m.nf,
+                     cudaMemcpyDeviceToDevice, x->st));
+  x->time = 0.;
+  x->adv_time = 0.;
+  return hydro_gpu_update_properties(x);
+}
+
+int hydro_gpu_start_step(hydro_ctx* x) {
+  if (!x) return HYDRO_ERR_ARG;
+  const Mesh& m = x->m;
+  x->iter_count = 0;
+  x->cd_iter_count = 0;
+  x->vel_sweeps = 0;
+  x->p_iters = 0;
+  x->p_res = 0.;
+  x->indicator = 1.;
+  bdf_coeffs(x->dt, x->d.time_second_order, x->fc.co);
+  CK(launch_start_step(m, x->d.guess_extrapolation, x->uw3(HYDRO_ITER_CURR),
+                       x->uc3(HYDRO_TIME_CURR), x->uc3(HYDRO_TIME_PREV), x->p[HYDRO_ITER_CURR],
+                       x->p[HYDRO_TIME_CURR], x->p[HYDRO_TIME_PREV], x->F[HYDRO_ITER_CURR],
+                       x->F[HYDRO_TIME_CURR], x->F[HYDRO_TIME_PREV], x->st));
+  return HYDRO_OK;
+}
+
+int hydro_gpu_make_iteration(hydro_ctx* x) {
+  if (!x) return HYDRO_ERR_ARG;
+  const Mesh& m = x->m;
+  int dim = x->dim;
+  // layer shift: iter_prev <- iter_curr (fluid.hpp:815-818, conv_diff.hpp:133)
+  std::swap(x->p[HYDRO_ITER_CURR], x->p[HYDRO_ITER_PREV]);
+  std::swap(x->F[HYDRO_ITER_CURR], x->F[HYDRO_ITER_PREV]);
+  std::swap(x->u[HYDRO_ITER_CURR], x->u[HYDRO_ITER_PREV]);
+  C3 up = x->uc3(HYDRO_ITER_PREV);
+  const double* pip = x->p[HYDRO_ITER_PREV];
+  const double* Fip = x->F[HYDRO_ITER_PREV];
+  C3 force = x->vec<C3>(x->force, dim, m.nc);
+  C3 fres = x->vec<C3>(x->fres, dim, m.nc);
+  CK(launch_vel_grad(m, x->fc, up, x->vec<WP<9>>(x->G, dim * dim, m.nc), x->st));
+  CK(launch_force(m, x->fc, up, x->vec<CP<9>>(x->G, dim * dim, m.nc), pip, x->mu, x->rho, force,
+                  x->vec<C3>(x->stforce, dim, m.nc), x->Sv, x->Sm, x->vec<W3>(x->fo, dim, m.nc),
+                  x->vec<W3>(x->fres, dim, m.nc), x->st));
+  CK(launch_mom_assemble(m, x->fc, up, x->uc3(HYDRO_TIME_CURR), x->uc3(HYDRO_TIME_PREV),
+                         x->vec<CP<9>>(x->G, dim * dim, m.nc), Fip, x->rho, x->mu,
+                         x->vec<C3>(x->fo, dim, m.nc), x->vec<WP<7>>(x->coef, 2 * dim + 1, m.nc),
+                         x->vec<W3>(x->res, dim, m.nc), x->Dc, x->st));
+  int rc = solve_momentum(x, up);
+  if (rc) return rc;
+  C3 du = x->vec<C3>(x->du[x->du_cur], dim, m.nc);
+  x->cd_iter_count++;
+  CK(launch_rhie_chow(m, x->fc, up, du, pip, force, fres, x->Dc, x->Fs, x->kf, x->st));
+  CK(launch_pressure_rhs(m, x->Fs, nullptr, x->prhs, x->st));
+  rc = solve_pressure(x);
+  if (rc) return rc;
+  CK(launch_correct(m, x->fc, up, du, x->uw3(HYDRO_ITER_CURR), pip, x->p[HYDRO_ITER_CURR], x->pc,
+                    x->Dc, x->Fs, x->kf, x->F[HYDRO_ITER_CURR], x->pw.partials, x->pw.ds, x->st));
+  rc = sync_scalars(x);
+  if (rc) return rc;
+  x->indicator = x->hds->red[RS_INDICATOR];
+  x->iter_count++;
+  if (isnan(x->indicator)) return HYDRO_ERR_NAN;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_get_convergence_indicator(hydro_ctx* x, double* out) {
+  if (!x || !out) return HYDRO_ERR_ARG;
+  *out = x->cd_iter_count == 0 ? 1. : x->indicator;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_get_iteration_count(hydro_ctx* x, int* out) {
+  if (!x || !out) return HYDRO_ERR_ARG;
+  *out = x->iter_count;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_is_converged(hydro_ctx* x, int* out) {
+  if (!x || !out) return HYDRO_ERR_ARG;
+  double ind = x->cd_iter_count == 0 ? 1. : x->indicator;
+  *out = (x->iter_count >= x->d.num_iterations_limit) || (ind < x->d.convergence_tolerance);
+  return HYDRO_OK;
+}
+
+int hydro_gpu_finish_step(hydro_ctx* x) {
+  if (!x) return HYDRO_ERR_ARG;
+  const Mesh& m = x->m;
+  // time_prev <- time_curr (pointer rotation), time_curr <- iter_curr (copy)
+  std::swap(x->p[HYDRO_TIME_PREV], x->p[HYDRO_TIME_CURR]);
+  std::swap(x->F[HYDRO_TIME_PREV], x->F[HYDRO_TIME_CURR]);
+  std::swap(x->u[HYDRO_TIME_PREV], x->u[HYDRO_TIME_CURR]);
+  CK(cudaMemcpyAsync(x->p[HYDRO_TIME_CURR], x->p[HYDRO_ITER_CURR], sizeof(double) * m.nc,
+                     cudaMemcpyDeviceToDevice, x->st));
+  CK(cudaMemcpyAsync(x->F[HYDRO_TIME_CURR], x->F[HYDRO_ITER_CURR], sizeof(double) * m.nf,
+                     cudaMemcpyDeviceToDevice, x->st));
+  CK(cudaMemcpyAsync(x->u[HYDRO_TIME_CURR], x->u[HYDRO_ITER_CURR],
+                     sizeof(double) * m.nc * x->dim, cudaMemcpyDeviceToDevice, x->st));
+  x->time += x->dt;
+  return nan_check(x, x->p[HYDRO_TIME_CURR], m.nc);
+}
+
+int hydro_gpu_get_auto_time_step(hydro_ctx* x, double* out) {
+  if (!x || !out) return HYDRO_ERR_ARG;
+  CK(launch_auto_dt(x->m, x->F[HYDRO_TIME_CURR], x->pw.partials, x->pw.ds, x->st));
+  int rc = sync_scalars(x);
+  if (rc) return rc;
+  *out = x->hds->red[RS_AUTO_DT];
+  return HYDRO_OK;
+}
+
+int hydro_gpu_set_time_step(hydro_ctx* x, double dt, double dta) {
+  if (!x || !(dt > 0.) || !(dta > 0.)) return HYDRO_ERR_ARG;
+  x->dt = dt;
+  x->adv_dt = dta;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_get_time(hydro_ctx* x, double* ft, double* at) {
+  if (!x) return HYDRO_ERR_ARG;
+  if (ft) *ft = x->time;
+  if (at) *at = x->adv_time;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_advection_step(hydro_ctx* x, int* substeps) {
+  if (!x) return HYDRO_ERR_ARG;
+  const Mesh& m = x->m;
+  const hydro_desc& d = x->d;
+  int nst = d.tvd_split ? x->dim : 1;
+  int ns = 0;
+  const double* F = x->F[HYDRO_TIME_CURR];
+  while (x->adv_time < x->time - 0.5 * x->adv_dt) {
+    for (int stage = 0; stage < nst; ++stage) {
+      CK(launch_adv_faces(m, x->nph, stage, nst, F, x->vec<CP<HYDRO_MAXPH>>(x->q, x->nph, m.nc),
+                          x->vec<WP<HYDRO_MAXPH>>(x->qflux, x->nph, m.nf), x->st));
+      CK(launch_adv_update(m, x->nph, stage, nst, x->adv_dt,
+                           x->vec<CP<HYDRO_MAXPH>>(x->qflux, x->nph, m.nf),
+                           x->vec<CP<HYDRO_MAXPH>>(x->q, x->nph, m.nc),
+                           x->vec<WP<HYDRO_MAXPH>>(x->qtmp, x->nph, m.nc), x->st));
+      std::swap(x->q, x->qtmp);
+    }
+    if (fabs(d.sharp) > 1e-10) {
+      for (int i = 0; i < x->nph; ++i)
+        CK(launch_adv_sharpen(m, i, d.sharp, d.density[i], x->adv_dt, F,
+                              x->q + (size_t)i * m.nc, x->smtmp, x->vec<W3>(x->G, x->dim, m.nc),
+                              x->Fs, x->st));
+    }
+    x->adv_time += x->adv_dt;
+    ++ns;
+  }
+  if (substeps) *substeps = ns;
+  CK(cudaGetLastError());
+  return HYDRO_OK;
+}
+
+int hydro_gpu_step(hydro_ctx* x, hydro_step_stats* stats) {
+  if (!x) return HYDRO_ERR_ARG;
+  const hydro_desc& d = x->d;
+  hydro_step_stats s;
+  memset(&s, 0, sizeof(s));
+  int rc;
+  if (d.dt_auto) {
+    double dtm;
+    rc = hydro_gpu_get_auto_time_step(x, &dtm);
+    if (rc) return rc;
+    double dt = dtm * d.cfl, dta = dtm * d.cfl_advection;
+    if (d.dt_max > 0. && dt > d.dt_max) {
+      dta = dta * (d.dt_max / dt);
+      dt = d.dt_max;
+    }
+    x->dt = dt;
+    x->adv_dt = dta;
+  }
+  rc = hydro_gpu_start_step(x);
+  if (rc) return rc;
+  for (;;) {
+    int conv;
+    hydro_gpu_is_converged(x, &conv);
+    if (conv) break;
+    rc = hydro_gpu_make_iteration(x);
+    if (rc) {
+      if (stats) { s.status = rc; *stats = s; }
+      return rc;
+    }
+  }
+  hydro_gpu_get_convergence_indicator(x, &s.convergence_indicator);
+  s.outer_iterations = x->iter_count;
+  s.velocity_sweeps = x->vel_sweeps;
+  s.pressure_iterations = x->p_iters;
+  s.pressure_residual = x->p_res;
+  rc = hydro_gpu_finish_step(x);
+  if (rc) {
+    if (stats) { s.status = rc; *stats = s; }
+    return rc;
+  }
+  if (d.advection_enable) {
+    rc = hydro_gpu_advection_step(x, &s.advection_substeps);
+    if (rc) return rc;
+  }
+  rc = hydro_gpu_update_properties(x);
+  if (rc) return rc;
+  s.dt = x->dt;
+  s.dt_advection = x->adv_dt;
+  s.time = x->time;
+  s.status = HYDRO_OK;
+  if (stats) *stats = s;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_calc_stat(hydro_ctx* x, hydro_stat* out) {
+  if (!x || !out) return HYDRO_ERR_ARG;
+  const Mesh& m = x->m;
+  memset(out, 0, sizeof(*out));
+  double h[16];
+  for (int i = 0; i < x->nph; ++i) {
+    CK(cudaMemsetAsync(x->stat_ticket, 0, sizeof(unsigned) * 4, x->st));
+    CK(launch_stat(m, x->q + (size_t)i * m.nc, x->alpha + (size_t)i * m.nc,
+                   x->uc3(HYDRO_TIME_CURR), x->pw.partials, x->stat_out, x->stat_ticket, x->st));
+    CK(cudaMemcpyAsync(h, x->stat_out, sizeof(double) * 10, cudaMemcpyDeviceToHost, x->st));
+    CK(cudaStreamSynchronize(x->st));
+    out->volume[i] = h[0];
+    out->mass[i] = h[0] * x->d.density[i];
+    for (int k = 0; k < x->dim; ++k) {
+      out->center[i][k] = h[1 + k] / h[0];
+      out->velocity[i][k] = h[4 + k] / h[0];
+    }
+    out->partial_mass[i] = h[7];
+    out->pd_min[i] = h[8];
+    out->pd_max[i] = h[9];
+  }
+  return HYDRO_OK;
+}
+
+// ------------------------------------------------- stencil solve (C-ABI) --
+size_t hydro_gpu_stencil_workspace_size(int dim, int nx, int ny, int nz) {
+  Mesh m;
+  int n[3] = {nx, ny, nz};
+  double lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+  if (init_mesh(m, dim, n, lo, hi)) return 0;
+  Arena a;
+  for (int i = 0; i < 7; ++i) a.take<double>(m.nc);
+  a.take<double>((size_t)4 * kMaxBlocks);
+  a.take<DevScalars>(1);
+  return a.used + 256;
+}
+
+int hydro_gpu_stencil_solve(int dim, int nx, int ny, int nz, const double* face_coeff,
+                            double shift, long pinned_cell, double pinned_value,
+                            const double* rhs, double* xsol, int use_guess, double tolerance,
+                            int iters_limit, void* workspace, void* stream, int* iterations,
+                            double* residual) {
+  Mesh m;
+  int n[3] = {nx, ny, nz};
+  double lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+  if (init_mesh(m, dim, n, lo, hi)) return HYDRO_ERR_ARG;
+  if (!face_coeff || !rhs || !xsol || !workspace) return HYDRO_ERR_ARG;
+  if (pinned_cell >= m.nc || iters_limit < 1 || !(tolerance >= 0.)) return HYDRO_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  Arena a;
+  a.base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+  PcgWork w{};
+  w.r = a.take<double>(m.nc);
+  w.z = a.take<double>(m.nc);
+  w.p = a.take<double>(m.nc);
+  w.Ap = a.take<double>(m.nc);
+  w.dg = a.take<double>(m.nc);
+  w.idg = a.take<double>(m.nc);
+  double* f = a.take<double>(m.nc);
+  w.partials = a.take<double>((size_t)4 * kMaxBlocks);
+  w.ds = a.take<DevScalars>(1);
+  w.pin = pinned_cell;
+  w.limit = iters_limit;
+  CK(cudaMemsetAsync(w.ds, 0, sizeof(DevScalars), st));
+  // f = -c
+  CK(cudaMemcpyAsync(f, rhs, sizeof(double) * m.nc, cudaMemcpyDeviceToDevice, st));
+  CK(scale_vector(m.nc, f, -1., st));
+  if (pinned_cell >= 0) CK(pin_rhs(m, face_coeff, f, pinned_cell, pinned_value, st));
+  int singular = (shift == 0. && pinned_cell < 0);
+  CK(pcg_prepare(m, face_coeff, shift, w, 0, st));
+  CK(pcg_init(m, face_coeff, f, xsol, use_guess, tolerance, singular, w, st));
+  DevScalars h;
+  int queued = 0;
+  for (;;) {
+    int nchunk = std::min(kCgChunk, iters_limit - queued);
+    if (nchunk < 1) nchunk = 1;
+    CK(pcg_iterate(m, face_coeff, xsol, nchunk, w, st));
+    queued += nchunk;
+    CK(cudaMemcpyAsync(&h, w.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (h.flag[FL_PCG_DONE] || queued >= iters_limit) break;
+  }
+  if (singular) {
+    PcgWork& ww = w;
+    CK(sub_mean(m, xsol, ww, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  double ff = h.red[RS_PCG_FF], rr = h.red[RS_PCG_RR];
+  double res = ff > 0. ? sqrt(rr / ff) : 0.;
+  if (iterations) *iterations = h.flag[FL_PCG_ITERS];
+  if (residual) *residual = res;
+  return (ff > 0. && rr > tolerance * tolerance * ff) ? HYDRO_NOT_CONVERGED : HYDRO_OK;
+}
+
+}  // extern "C"

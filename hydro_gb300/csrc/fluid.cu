@@ -1,0 +1,701 @@
+// fluid.cu -- sm_103a kernels of one SIMPLE iteration (FluidSimple::
+// MakeIteration, fluid.hpp:814-1158) and of the fluid-property update
+// (hydro<Mesh>::UpdateFluidProperties, hydro2d.hpp:1404-1430).
+//
+// One thread owns one (i, j) column of a 32x8 tile and marches the block's
+// k range, so x-neighbours come from the same warp, y-neighbours from the
+// same block and z-neighbours from the previous/next plane (L1/L2 hits);
+// every load is coalesced along x.  Geometry is implicit (uniform h).
+// Face arrays are written once per face: each cell owns its low face in
+// every direction and, on the high end of the block, its high face.
+#include <math.h>
+
+#include "kernels.h"
+#include "loop.cuh"
+
+namespace hg {
+
+namespace {
+
+// Geometric average of two vectors (solver.hpp:380-390), component d.
+template <int DIM>
+__device__ double vgeo(const double* a, const double* b, int d) {
+  double av[DIM], n2 = 0., na = 0., nb = 0.;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) {
+    av[k] = (a[k] + b[k]) * 0.5;
+    n2 += av[k] * av[k];
+    na += a[k] * a[k];
+    nb += b[k] * b[k];
+  }
+  double an = sqrt(n2);
+  if (an < 1e-8) return av[d];
+  return av[d] / an * sqrt(sqrt(na) * sqrt(nb));
+}
+
+// Face value (component d) of a cell vector field between cells cm and cp.
+template <int DIM>
+__device__ double face_vec(const C3& f, long long cm, long long cp, int d, int geometric) {
+  if (!geometric) return avg(f.a[d][cm], f.a[d][cp]);
+  double a[DIM], b[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) {
+    a[k] = f.a[k][cm];
+    b[k] = f.a[k][cp];
+  }
+  return vgeo<DIM>(a, b, d);
+}
+
+__device__ __forceinline__ double face_scal(double a, double b, int geometric) {
+  return geometric ? sqrt(a * b) : avg(a, b);
+}
+
+// ------------------------------------------------------------ StartStep --
+__global__ void k_axpy_extrap(long long n, double ge, double* out, const double* tc,
+                              const double* tp) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = tc[i] + (tc[i] - tp[i]) * ge;
+}
+
+// ------------------------------------------------------- velocity grads --
+// G[n*DIM+m] = d u_n / d x_m at cells, faces carrying the velocity value
+// condition (Gradient(Interpolate(u_n, cond_n)), solver.hpp:392-470,658-677).
+template <int DIM>
+__global__ void k_vel_grad(Mesh m, Geo g, FluidCoef fc, C3 u, WP<9> G, int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long s = cell_stride(m, d);
+    int id = X.i[d], nd = m.n[d];
+#pragma unroll
+    for (int n = 0; n < DIM; ++n) {
+      double uc = u.a[n][X.c];
+      double flo = id > 0 ? avg(u.a[n][X.c - s], uc) : fc.bcu[2 * d][n];
+      double fhi = id < nd - 1 ? avg(uc, u.a[n][X.c + s]) : fc.bcu[2 * d + 1][n];
+      G.a[n * DIM + d][X.c] = (fhi - flo) * g.inv_h[d];
+    }
+  }
+  CELL_LOOP_END
+}
+
+// ---------------------------------------------------------------- force --
+// Explicit momentum source (fluid.hpp:834-870): transposed viscous term
+// sum_n d/dx_n (mu du_n/dx_m) with face gradients averaged from cells
+// (zero-derivative boundaries), minus grad p (extrapolated boundary faces),
+// plus the "restored" external force (fluid.hpp:612-625), surface-tension
+// force and the volume-source momentum term.  Also stores the restored
+// force for the Rhie-Chow kernel.
+template <int DIM>
+__global__ void k_force(Mesh m, Geo g, FluidCoef fc, C3 u, CP<9> G, const double* p,
+                        const double* mu, const double* rho, C3 force, C3 stforce,
+                        const double* Sv, const double* Sm, W3 fo, W3 fres, int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+  double acc[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) acc[k] = 0.;
+  const double muc = mu[X.c];
+#pragma unroll
+  for (int n = 0; n < DIM; ++n) {
+    long long s = cell_stride(m, n);
+    int id = X.i[n], nd = m.n[n];
+    double mlo, mhi;
+    double glo[DIM], ghi[DIM];
+    if (id > 0) {
+      mlo = face_scal(mu[X.c - s], muc, fc.geometric);
+#pragma unroll
+      for (int k = 0; k < DIM; ++k)
+        glo[k] = avg(G.a[n * DIM + k][X.c - s], G.a[n * DIM + k][X.c]);
+    } else {
+      mlo = muc;
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) glo[k] = G.a[n * DIM + k][X.c];
+    }
+    if (id < nd - 1) {
+      mhi = face_scal(muc, mu[X.c + s], fc.geometric);
+#pragma unroll
+      for (int k = 0; k < DIM; ++k)
+        ghi[k] = avg(G.a[n * DIM + k][X.c], G.a[n * DIM + k][X.c + s]);
+    } else {
+      mhi = muc;
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) ghi[k] = G.a[n * DIM + k][X.c];
+    }
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) acc[k] += (ghi[k] * mhi - glo[k] * mlo) * g.inv_h[n];
+  }
+  double src = fc.sources ? rho[X.c] * Sv[X.c] - Sm[X.c] : 0.;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) {
+    long long s = cell_stride(m, k);
+    int id = X.i[k], nd = m.n[k];
+    double gp = grad_extrap(p, X.c, id, nd, s, g.inv_h[k]);
+    double fcv = force.a[k][X.c];
+    double flo = id > 0 ? face_vec<DIM>(force, X.c - s, X.c, k, fc.geometric) : fcv;
+    double fhi = id < nd - 1 ? face_vec<DIM>(force, X.c, X.c + s, k, fc.geometric) : fcv;
+    double fr = 0.5 * (flo + fhi);
+    fres.a[k][X.c] = fr;
+    double v = -gp + fr + stforce.a[k][X.c];
+    if (fc.sources) v += u.a[k][X.c] * src;
+    fo.a[k][X.c] = acc[k] + v;
+  }
+  CELL_LOOP_END
+}
+
+// ------------------------------------------------------ momentum system --
+// ConvectionDiffusionScalarImplicit::MakeIteration assembly
+// (conv_diff.hpp:130-227) for all components at once: the coefficients
+// depend only on F, rho, mu and are shared; the constants differ.
+// Convective face value: deferred second-order upwind (solver.hpp:201-243,
+// threshold 1e-10); diffusion: two-point (solver.hpp:283-341); BDF time
+// term (solver.hpp:815-861).  Stores the relaxed diagonal, the 2*DIM
+// off-diagonals (face order xm,xp,ym,yp,zm,zp; 0 on boundary faces), the
+// delta-form residuals r_n = row_n(u_prev) and D_c = sum of the relaxed
+// row coefficients (fluid.hpp:876-883).
+template <int DIM>
+__global__ void k_mom_assemble(Mesh m, Geo g, FluidCoef fc, C3 up, C3 utc, C3 utp, CP<9> G,
+                               const double* F, const double* rho, const double* mu, C3 fo,
+                               WP<7> coef, W3 res, double* Dc, int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+  const double rhoc = rho[X.c], muc = mu[X.c];
+  double aP = fc.co[2] * rhoc;
+  double aq[2 * DIM];
+  double cst[DIM];
+#pragma unroll
+  for (int n = 0; n < DIM; ++n)
+    cst[n] = (fc.co[0] * utp.a[n][X.c] + fc.co[1] * utc.a[n][X.c]) * rhoc - fo.a[n][X.c];
+  const double rv = rhoc * g.invV;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long s = cell_stride(m, d);
+    long long fs = face_stride(m, d);
+    int id = X.i[d], nd = m.n[d];
+    long long flo = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+    const double hh = 0.5 * g.h[d];
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      long long f = flo + side * fs;
+      double Ff = F[f];
+      double so = side ? 1. : -1.;
+      bool inner = side ? (id < nd - 1) : (id > 0);
+      if (inner) {
+        long long nb = side ? X.c + s : X.c - s;
+        double dif = face_scal(muc, mu[nb], fc.geometric) * g.inv_h2[d];
+        double wm, wp;
+        int up_side;  // 0: cm upwind, 1: cp upwind, -1: central
+        if (Ff > 1e-10) {
+          wm = 1.; wp = 0.; up_side = 0;
+        } else if (Ff < -1e-10) {
+          wm = 0.; wp = 1.; up_side = 1;
+        } else {
+          wm = 0.5; wp = 0.5; up_side = -1;
+        }
+        // the cell is cm of its high face and cp of its low face
+        double wown = side ? wm : wp, wnb = side ? wp : wm;
+        aP += (wown * Ff * so) * rv + dif;
+        aq[2 * d + side] = (wnb * Ff * so) * rv - dif;
+        if (up_side >= 0) {
+          bool up_is_own = side ? (up_side == 0) : (up_side == 1);
+          long long cu = up_is_own ? X.c : nb;
+          double sg = up_side == 0 ? hh : -hh;  // -(x_up - x_f) along d
+#pragma unroll
+          for (int n = 0; n < DIM; ++n) cst[n] += (G.a[n * DIM + d][cu] * sg * Ff * so) * rv;
+        }
+      } else {
+        double dif = 2. * muc * g.inv_h2[d];
+        aP += dif;
+        aq[2 * d + side] = 0.;
+#pragma unroll
+        for (int n = 0; n < DIM; ++n) {
+          double val = fc.bcu[2 * d + side][n];
+          cst[n] += (val * Ff * so) * rv - dif * val;
+        }
+      }
+    }
+  }
+  double cs = aP;
+#pragma unroll
+  for (int q = 0; q < 2 * DIM; ++q) cs += aq[q];
+#pragma unroll
+  for (int n = 0; n < DIM; ++n) {
+    double r = cst[n] + aP * up.a[n][X.c];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      long long s = cell_stride(m, d);
+      if (X.i[d] > 0) r += aq[2 * d] * up.a[n][X.c - s];
+      if (X.i[d] < m.n[d] - 1) r += aq[2 * d + 1] * up.a[n][X.c + s];
+    }
+    res.a[n][X.c] = r;
+  }
+  double aPr = aP / fc.relax_u;
+  coef.a[0][X.c] = aPr;
+#pragma unroll
+  for (int q = 0; q < 2 * DIM; ++q) coef.a[1 + q][X.c] = aq[q];
+  Dc[X.c] = cs - aP + aPr;
+  CELL_LOOP_END
+}
+
+// Jacobi sweep for all components (Jacobi::Solve, linear.hpp:750-782):
+// value = -(r + sum_nb a du_nb)/aP, du' = du + omega*(value - du); the max
+// |value - du| is reduced into ds->red[RS_MOM_DIFF].  A launch after
+// convergence returns at once.
+template <int DIM>
+__global__ void __launch_bounds__(NT) k_mom_sweep(Mesh m, double omega, double tol,
+                                                  CP<7> coef, C3 res, C3 din, W3 dout,
+                                                  int first, double* partials, DevScalars* ds,
+                                                  int kch) {
+  if (ds->flag[FL_MOM_DONE]) return;
+  double dmax = 0.;
+  CELL_LOOP_BEGIN(m, kch)
+  double aP = coef.a[0][X.c];
+  double a[2 * DIM];
+#pragma unroll
+  for (int q = 0; q < 2 * DIM; ++q) a[q] = coef.a[1 + q][X.c];
+#pragma unroll
+  for (int n = 0; n < DIM; ++n) {
+    double sum = 0., cur = 0.;
+    if (!first) {
+      cur = din.a[n][X.c];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        long long s = cell_stride(m, d);
+        if (X.i[d] > 0) sum += a[2 * d] * din.a[n][X.c - s];
+        if (X.i[d] < m.n[d] - 1) sum += a[2 * d + 1] * din.a[n][X.c + s];
+      }
+    }
+    double value = -(res.a[n][X.c] + sum) / aP;
+    double corr = value - cur;
+    dmax = fmax(dmax, fabs(corr));
+    dout.a[n][X.c] = cur + corr * omega;
+  }
+  CELL_LOOP_END
+  double v[1] = {dmax};
+  __shared__ double out[1];
+  if (grid_reduce<RED_MAX, 1>(v, partials, &ds->ticket[TK_MOM], out)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      ds->red[RS_MOM_DIFF] = out[0];
+      ds->flag[FL_MOM_SWEEPS] += 1;
+      if (!(out[0] > tol)) ds->flag[FL_MOM_DONE] = 1;
+    }
+  }
+}
+
+// ------------------------------------------------------------ Rhie-Chow --
+// Face volume fluxes F* by momentum interpolation (fluid.hpp:889-942) and
+// face couplings kf = A/(h D_f) of the flux-correction expressions
+// (fluid.hpp:946-970); boundary faces carry u_wall.S and kf = 0.
+template <int DIM>
+__global__ void k_rhie_chow(Mesh m, Geo g, FluidCoef fc, C3 up, C3 du, const double* p,
+                            C3 force, C3 fres, const double* Dc, double* Fs, double* kf,
+                            int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long s = cell_stride(m, d);
+    int id = X.i[d], nd = m.n[d];
+    long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+    double mv = fc.meshvel[d] * g.A[d];
+    if (id > 0) {
+      long long cm = X.c - s, cp = X.c;
+      double uf = avg(up.a[d][cm] + du.a[d][cm], up.a[d][cp] + du.a[d][cp]);
+      double vfi = uf * g.A[d];
+      double gpm = grad_extrap(p, cm, id - 1, nd, s, g.inv_h[d]);
+      double gpp = grad_extrap(p, cp, id, nd, s, g.inv_h[d]);
+      double gpf = avg(gpm, gpp);
+      double frf = face_vec<DIM>(fres, cm, cp, d, fc.geometric);
+      double fxf = face_vec<DIM>(force, cm, cp, d, fc.geometric);
+      double wide = (gpf - frf) * g.A[d];
+      double compact = (p[cp] - p[cm]) * g.inv_h[d] * g.A[d] - fxf * g.A[d];
+      double Df = avg(Dc[cm], Dc[cp]);
+      Fs[f] = vfi + fc.rc * (wide - compact) / Df - mv;
+      kf[f] = g.A[d] / (g.h[d] * Df);
+    } else {
+      Fs[f] = fc.bcu[2 * d][d] * g.A[d] - mv;
+      kf[f] = 0.;
+    }
+    if (id == nd - 1) {
+      long long fh = f + face_stride(m, d);
+      Fs[fh] = fc.bcu[2 * d + 1][d] * g.A[d] - mv;
+      kf[fh] = 0.;
+    }
+  }
+  CELL_LOOP_END
+}
+
+// Right-hand side of the pressure-correction rows (fluid.hpp:972-994):
+// b_c = sum_f s_f F*_f - S_v V, written as f = -b (A p' = f).
+template <int DIM>
+__global__ void k_pressure_rhs(Mesh m, Geo g, const double* Fs, const double* Sv, double* f,
+                               int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+  double b = 0.;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+    b += Fs[fl + face_stride(m, d)] - Fs[fl];
+  }
+  if (Sv) b -= Sv[X.c] * g.V;
+  f[X.c] = -b;
+  CELL_LOOP_END
+}
+
+// ----------------------------------------------------------- correction --
+// fluid.hpp:1033-1057: p += alpha_p p'; u = u* - grad p'/D_c (p' faces
+// extrapolated); F = F* + kf (p'_cm - p'_cp).  Reduces the SIMPLE
+// convergence indicator max_c |u_c - u_prev,c| (CalcDiff,
+// solver.hpp:804-813) into ds->red[RS_INDICATOR].
+template <int DIM>
+__global__ void __launch_bounds__(NT) k_correct(Mesh m, Geo g, FluidCoef fc, C3 up, C3 du,
+                                                W3 uic, const double* pip, double* pic,
+                                                const double* pc, const double* Dc,
+                                                const double* Fs, const double* kf,
+                                                double* Fic, double* partials, DevScalars* ds,
+                                                int kch) {
+  double dmax = 0.;
+  CELL_LOOP_BEGIN(m, kch)
+  pic[X.c] = pip[X.c] + fc.relax_p * pc[X.c];
+  double dc = Dc[X.c];
+  double d2 = 0.;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) {
+    long long s = cell_stride(m, k);
+    double gpc = grad_extrap(pc, X.c, X.i[k], m.n[k], s, g.inv_h[k]);
+    double u0 = up.a[k][X.c];
+    double un = (u0 + du.a[k][X.c]) + gpc / (-dc);
+    uic.a[k][X.c] = un;
+    double dd = un - u0;
+    d2 += dd * dd;
+    long long f = face_id(m, k, X.i[0], X.i[1], X.i[2]);
+    if (X.i[k] > 0) Fic[f] = Fs[f] + kf[f] * (pc[X.c - s] - pc[X.c]);
+    else Fic[f] = Fs[f];
+    if (X.i[k] == m.n[k] - 1) {
+      long long fh = f + face_stride(m, k);
+      Fic[fh] = Fs[fh];
+    }
+  }
+  dmax = fmax(dmax, sqrt(d2));
+  CELL_LOOP_END
+  double v[1] = {dmax};
+  __shared__ double out[1];
+  if (grid_reduce<RED_MAX, 1>(v, partials, &ds->ticket[TK_IND], out)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) ds->red[RS_INDICATOR] = out[0];
+  }
+}
+
+// --------------------------------------------------------- auto time step --
+// FluidSimple::GetAutoTimeStep (fluid.hpp:1191-1206): min over faces with
+// F != 0 of |V/F|, 1e10 when there is none.
+__global__ void __launch_bounds__(NT) k_auto_dt(long long nf, double V, const double* F,
+                                                double* partials, DevScalars* ds) {
+  double dmin = 1e10;
+  long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
+  for (long long f = blockIdx.x * (long long)NT + tid; f < nf; f += (long long)gridDim.x * NT) {
+    double fl = F[f];
+    if (fl != 0.) dmin = fmin(dmin, fabs(V / fl));
+  }
+  double v[1] = {dmin};
+  __shared__ double out[1];
+  if (grid_reduce<RED_MIN, 1>(v, partials, &ds->ticket[TK_DT], out)) {
+    if (tid == 0) ds->red[RS_AUTO_DT] = out[0];
+  }
+}
+
+__global__ void __launch_bounds__(NT) k_nan_count(long long n, const double* a,
+                                                  double* partials, DevScalars* ds) {
+  double cnt = 0.;
+  long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
+  for (long long i = blockIdx.x * (long long)NT + tid; i < n; i += (long long)gridDim.x * NT)
+    if (isnan(a[i])) cnt += 1.;
+  double v[1] = {cnt};
+  __shared__ double out[1];
+  if (grid_reduce<RED_SUM, 1>(v, partials, &ds->ticket[TK_NAN], out)) {
+    if (tid == 0) ds->red[RS_NAN] = out[0];
+  }
+}
+
+// ----------------------------------------------------------- properties --
+// CalcPhasesVolumeFraction (hydro2d.hpp:980-997), GetVolumeAveraged of
+// densities and viscosities (1221-1246), zero mass and volume sources
+// (chemistry intensity 0), body force rho*g + f with the unsmoothed
+// mixture density (CalcForce, hydro2d.hpp:1308-1316).
+template <int DIM>
+__global__ void k_props(Mesh m, int nph, PhaseProps pp, CP<HYDRO_MAXPH> q,
+                        WP<HYDRO_MAXPH> alpha, double* rho_raw, double* rho, double* mu,
+                        W3 force, double* Sv, double* Sm, int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+  double a[HYDRO_MAXPH];
+  double sum = 0.;
+#pragma unroll
+  for (int i = 0; i < HYDRO_MAXPH; ++i) {
+    if (i < nph) {
+      a[i] = q.a[i][X.c] / pp.dens[i];
+      sum += a[i];
+    }
+  }
+  double rr = 0., mm = 0.;
+#pragma unroll
+  for (int i = 0; i < HYDRO_MAXPH; ++i) {
+    if (i < nph) {
+      a[i] /= sum;
+      alpha.a[i][X.c] = a[i];
+      rr += pp.dens[i] * a[i];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < HYDRO_MAXPH; ++i)
+    if (i < nph) mm += pp.visc[i] * a[i];
+  rho_raw[X.c] = rr;
+  rho[X.c] = rr;
+  mu[X.c] = mm;
+  Sv[X.c] = 0.;
+  Sm[X.c] = 0.;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) force.a[k][X.c] = pp.grav[k] * rr + pp.f0[k];
+  CELL_LOOP_END
+}
+
+// One pass of GetSmoothField (solver.hpp:636-656): face averages with
+// zero-derivative boundaries, then the average over the 2*DIM faces
+// (solver.hpp:621-634).
+template <int DIM>
+__global__ void k_smooth(Mesh m, const double* in, double* out, int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+  double vc = in[X.c];
+  double sum = 0.;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long s = cell_stride(m, d);
+    sum += X.i[d] > 0 ? avg(in[X.c - s], vc) : vc;
+    sum += X.i[d] < m.n[d] - 1 ? avg(vc, in[X.c + s]) : vc;
+  }
+  out[X.c] = sum / (2. * DIM);
+  CELL_LOOP_END
+}
+
+// Cell gradient of a scalar with zero-derivative boundary faces.
+template <int DIM>
+__global__ void k_scal_grad(Mesh m, Geo g, const double* a, W3 G, int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+  double vc = a[X.c];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long s = cell_stride(m, d);
+    double flo = X.i[d] > 0 ? avg(a[X.c - s], vc) : vc;
+    double fhi = X.i[d] < m.n[d] - 1 ? avg(vc, a[X.c + s]) : vc;
+    G.a[d][X.c] = (fhi - flo) * g.inv_h[d];
+  }
+  CELL_LOOP_END
+}
+
+// Surface-tension force (hydro2d.hpp:1318-1370): g the face gradient of the
+// phase-1 volume fraction, n = g/(|g|+1e-6),
+// f_c = sigma/V sum_f [ g (S.n) - S |g| ].
+template <int DIM>
+__global__ void k_stforce(Mesh m, Geo g, double sigma, C3 G, W3 out, int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+  double f[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) f[k] = 0.;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long s = cell_stride(m, d);
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      bool inner = side ? X.i[d] < m.n[d] - 1 : X.i[d] > 0;
+      long long nb = side ? X.c + s : X.c - s;
+      double gv[DIM], n2 = 0.;
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) {
+        gv[k] = inner ? avg(G.a[k][side ? X.c : nb], G.a[k][side ? nb : X.c]) : G.a[k][X.c];
+        n2 += gv[k] * gv[k];
+      }
+      double gn = sqrt(n2);
+      double so = (side ? 1. : -1.) * g.A[d];
+      double sn = so * (gv[d] / (gn + 1e-6));
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) f[k] += gv[k] * sn;
+      f[d] -= so * gn;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) out.a[k][X.c] = f[k] * g.invV * sigma;
+  CELL_LOOP_END
+}
+
+// CalcStat (hydro2d.hpp:1432-1467) of one phase: sums of alpha V,
+// x alpha V, u alpha V and q V; min and max of q.
+template <int DIM>
+__global__ void __launch_bounds__(NT) k_stat(Mesh m, Geo g, const double* q, const double* al,
+                                             C3 u, double* partials, double* out,
+                                             unsigned* ticket, int kch) {
+  double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  double qmin = 1e10, qmax = -1e10;
+  CELL_LOOP_BEGIN(m, kch)
+  double a = al[X.c] * g.V;
+  s[0] += a;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) {
+    double xc = m.lo[k] + (X.i[k] + 0.5) * g.h[k];
+    s[1 + k] += xc * a;
+    s[4 + k] += u.a[k][X.c] * a;
+  }
+  double qc = q[X.c];
+  s[7] += qc * g.V;
+  qmin = fmin(qmin, qc);
+  qmax = fmax(qmax, qc);
+  CELL_LOOP_END
+  __shared__ double o8[8], o1[1], o2[1];
+  if (grid_reduce<RED_SUM, 8>(s, partials, &ticket[0], o8)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0)
+      for (int a = 0; a < 8; ++a) out[a] = o8[a];
+  }
+  double vmin[1] = {qmin}, vmax[1] = {qmax};
+  if (grid_reduce<RED_MIN, 1>(vmin, partials + 8 * kMaxBlocks, &ticket[1], o1)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) out[8] = o1[0];
+  }
+  if (grid_reduce<RED_MAX, 1>(vmax, partials + 9 * kMaxBlocks, &ticket[2], o2)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) out[9] = o2[0];
+  }
+}
+
+// Initial volume fluxes of the FluidSimple ctor (fluid.hpp:770-784):
+// F = u_f.S - meshvel.S with the velocity value condition on boundaries.
+template <int DIM>
+__global__ void k_init_flux(Mesh m, Geo g, FluidCoef fc, C3 u, double* F, int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long s = cell_stride(m, d);
+    long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+    double mv = fc.meshvel[d] * g.A[d];
+    if (X.i[d] > 0) F[f] = avg(u.a[d][X.c - s], u.a[d][X.c]) * g.A[d] - mv;
+    else F[f] = fc.bcu[2 * d][d] * g.A[d] - mv;
+    if (X.i[d] == m.n[d] - 1) F[f + face_stride(m, d)] = fc.bcu[2 * d + 1][d] * g.A[d] - mv;
+  }
+  CELL_LOOP_END
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ launchers --
+#define DISPATCH_DIM(m, KERNEL, ...)                                     \
+  do {                                                                   \
+    Launch L = cell_launch(m);                                           \
+    if ((m).dim == 3)                                                    \
+      KERNEL<3><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);         \
+    else                                                                 \
+      KERNEL<2><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);         \
+    return cudaGetLastError();                                           \
+  } while (0)
+
+static int flat_blocks(long long n) {
+  long long b = (n + NT - 1) / NT;
+  if (b > kMaxBlocks) b = kMaxBlocks;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+cudaError_t launch_start_step(const Mesh& m, double ge, W3 u_ic, C3 u_tc, C3 u_tp,
+                              double* p_ic, const double* p_tc, const double* p_tp,
+                              double* F_ic, const double* F_tc, const double* F_tp,
+                              cudaStream_t st) {
+  int nb = flat_blocks(m.nc);
+  for (int k = 0; k < m.dim; ++k)
+    k_axpy_extrap<<<nb, NT, 0, st>>>(m.nc, ge, u_ic.a[k], u_tc.a[k], u_tp.a[k]);
+  k_axpy_extrap<<<nb, NT, 0, st>>>(m.nc, ge, p_ic, p_tc, p_tp);
+  k_axpy_extrap<<<flat_blocks(m.nf), NT, 0, st>>>(m.nf, ge, F_ic, F_tc, F_tp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_flux(const Mesh& m, const FluidCoef& fc, C3 u, double* F,
+                             cudaStream_t st) {
+  DISPATCH_DIM(m, k_init_flux, m, make_geo(m), fc, u, F);
+}
+
+cudaError_t launch_vel_grad(const Mesh& m, const FluidCoef& fc, C3 u, WP<9> G, cudaStream_t st) {
+  DISPATCH_DIM(m, k_vel_grad, m, make_geo(m), fc, u, G);
+}
+
+cudaError_t launch_force(const Mesh& m, const FluidCoef& fc, C3 u, CP<9> G, const double* p,
+                         const double* mu, const double* rho, C3 force, C3 stforce,
+                         const double* Sv, const double* Sm, W3 fo, W3 fres, cudaStream_t st) {
+  DISPATCH_DIM(m, k_force, m, make_geo(m), fc, u, G, p, mu, rho, force, stforce, Sv, Sm, fo,
+               fres);
+}
+
+cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 u_tc,
+                                C3 u_tp, CP<9> G, const double* F, const double* rho,
+                                const double* mu, C3 fo, WP<7> coef, W3 res, double* Dc,
+                                cudaStream_t st) {
+  DISPATCH_DIM(m, k_mom_assemble, m, make_geo(m), fc, u_prev, u_tc, u_tp, G, F, rho, mu, fo,
+               coef, res, Dc);
+}
+
+cudaError_t launch_mom_sweep(const Mesh& m, double omega, double tol, CP<7> coef, C3 res,
+                             C3 din, W3 dout, int first, double* partials, DevScalars* ds,
+                             cudaStream_t st) {
+  DISPATCH_DIM(m, k_mom_sweep, m, omega, tol, coef, res, din, dout, first, partials, ds);
+}
+
+cudaError_t launch_rhie_chow(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du,
+                             const double* p, C3 force, C3 fres, const double* Dc, double* Fs,
+                             double* kf, cudaStream_t st) {
+  DISPATCH_DIM(m, k_rhie_chow, m, make_geo(m), fc, u_prev, du, p, force, fres, Dc, Fs, kf);
+}
+
+cudaError_t launch_pressure_rhs(const Mesh& m, const double* Fs, const double* Sv, double* f,
+                                cudaStream_t st) {
+  DISPATCH_DIM(m, k_pressure_rhs, m, make_geo(m), Fs, Sv, f);
+}
+
+cudaError_t launch_correct(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du, W3 u_ic,
+                           const double* p_ip, double* p_ic, const double* pc,
+                           const double* Dc, const double* Fs, const double* kf,
+                           double* F_ic, double* partials, DevScalars* ds, cudaStream_t st) {
+  DISPATCH_DIM(m, k_correct, m, make_geo(m), fc, u_prev, du, u_ic, p_ip, p_ic, pc, Dc, Fs, kf,
+               F_ic, partials, ds);
+}
+
+cudaError_t launch_auto_dt(const Mesh& m, const double* F, double* partials, DevScalars* ds,
+                           cudaStream_t st) {
+  k_auto_dt<<<flat_blocks(m.nf), dim3(BX, BY), 0, st>>>(m.nf, m.V, F, partials, ds);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nan_count(long long n, const double* a, double* partials, DevScalars* ds,
+                             cudaStream_t st) {
+  k_nan_count<<<flat_blocks(n), dim3(BX, BY), 0, st>>>(n, a, partials, ds);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_props(const Mesh& m, int nph, const PhaseProps& pp, CP<HYDRO_MAXPH> q,
+                         WP<HYDRO_MAXPH> alpha, double* rho_raw, double* rho, double* mu,
+                         W3 force, double* Sv, double* Sm, cudaStream_t st) {
+  DISPATCH_DIM(m, k_props, m, nph, pp, q, alpha, rho_raw, rho, mu, force, Sv, Sm);
+}
+
+cudaError_t launch_smooth(const Mesh& m, const double* in, double* out, cudaStream_t st) {
+  DISPATCH_DIM(m, k_smooth, m, in, out);
+}
+
+cudaError_t launch_stforce(const Mesh& m, double sigma, const double* alpha1, W3 G, W3 out,
+                           cudaStream_t st) {
+  Launch L = cell_launch(m);
+  Geo g = make_geo(m);
+  C3 Gc = {{G.a[0], G.a[1], G.a[2]}};
+  if (m.dim == 3) {
+    k_scal_grad<3><<<L.grid, L.block, 0, st>>>(m, g, alpha1, G, L.kch);
+    k_stforce<3><<<L.grid, L.block, 0, st>>>(m, g, sigma, Gc, out, L.kch);
+  } else {
+    k_scal_grad<2><<<L.grid, L.block, 0, st>>>(m, g, alpha1, G, L.kch);
+    k_stforce<2><<<L.grid, L.block, 0, st>>>(m, g, sigma, Gc, out, L.kch);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stat(const Mesh& m, const double* q, const double* alpha, C3 u,
+                        double* partials, double* out, unsigned* ticket, cudaStream_t st) {
+  DISPATCH_DIM(m, k_stat, m, make_geo(m), q, alpha, u, partials, out, ticket);
+}
+
+}  // namespace hg

@@ -1,0 +1,160 @@
+// kernels.h -- host-side launchers of the sm_103a kernels (fluid.cu,
+// linear.cu, advection.cu).  All pointers are device pointers; every
+// launcher enqueues on `st` and returns the launch status.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace hg {
+
+#define HYDRO_MAXPH 4
+
+// Pointer tables passed by value as kernel parameters.
+template <int N>
+struct CP {
+  const double* a[N];
+};
+template <int N>
+struct WP {
+  double* a[N];
+};
+using C3 = CP<3>;
+using W3 = WP<3>;
+
+// Per-case constants of the momentum / pressure-correction kernels.
+struct FluidCoef {
+  double bcu[6][3];  // wall velocity per side and component
+  double relax_u;    // velocity_relaxation_factor
+  double relax_p;    // pressure_relaxation_factor
+  double rc;         // rhie_chow_factor
+  double co[3];      // BDF coefficients for (n-1, n, n+1)
+  double meshvel[3];
+  int geometric;     // force_geometric_average
+  int sources;       // volume/mass sources present
+};
+
+// Device scalars shared by reductions and convergence flags.
+struct DevScalars {
+  double red[32];        // reduced values (see enum below)
+  int flag[16];          // done flags / counters
+  unsigned ticket[32];   // grid-reduction tickets, one per call site
+};
+enum {
+  RS_MOM_DIFF = 0,       // max |update| of the last momentum sweep
+  RS_PCG_RZ = 1, RS_PCG_RZ_OLD = 2, RS_PCG_PAP = 3, RS_PCG_RR = 4, RS_PCG_FF = 5,
+  RS_PCG_ALPHA = 6, RS_PCG_BETA = 7,
+  RS_INDICATOR = 8,      // SIMPLE convergence indicator
+  RS_AUTO_DT = 9,
+  RS_MEAN = 10,          // sum used for mean projection
+  RS_PCG_TOL2 = 11,      // tol^2 * ||f||^2
+  RS_IR_RR = 12,         // refinement residual norm^2
+  RS_NAN = 13,
+  RS_XMEAN = 14
+};
+enum { FL_MOM_DONE = 0, FL_MOM_SWEEPS = 1, FL_PCG_DONE = 2, FL_PCG_ITERS = 3, FL_NAN = 4 };
+enum {
+  TK_MOM = 0, TK_PCG_A = 1, TK_PCG_B = 2, TK_PCG_INIT = 3, TK_IND = 4, TK_DT = 5,
+  TK_MEAN = 6, TK_MEAN2 = 7, TK_STAT = 8, TK_STAT2 = 9, TK_STAT3 = 10, TK_IR = 11,
+  TK_NAN = 12, TK_PCG_INIT2 = 13, TK_F32_A = 14, TK_F32_B = 15, TK_F32_INIT = 16
+};
+
+// ---------------------------------------------------------------- fluid --
+cudaError_t launch_start_step(const Mesh& m, double ge, W3 u_ic, C3 u_tc, C3 u_tp,
+                              double* p_ic, const double* p_tc, const double* p_tp,
+                              double* F_ic, const double* F_tc, const double* F_tp,
+                              cudaStream_t st);
+cudaError_t launch_init_flux(const Mesh& m, const FluidCoef& fc, C3 u, double* F,
+                             cudaStream_t st);
+cudaError_t launch_vel_grad(const Mesh& m, const FluidCoef& fc, C3 u, WP<9> G, cudaStream_t st);
+cudaError_t launch_force(const Mesh& m, const FluidCoef& fc, C3 u, CP<9> G, const double* p,
+                         const double* mu, const double* rho, C3 force, C3 stforce,
+                         const double* Sv, const double* Sm, W3 fo, W3 fres, cudaStream_t st);
+cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 u_tc,
+                                C3 u_tp, CP<9> G, const double* F, const double* rho,
+                                const double* mu, C3 fo, WP<7> coef, W3 res, double* Dc,
+                                cudaStream_t st);
+cudaError_t launch_mom_sweep(const Mesh& m, double omega, double tol, CP<7> coef, C3 res,
+                             C3 din, W3 dout, int first, double* partials, DevScalars* ds,
+                             cudaStream_t st);
+cudaError_t launch_rhie_chow(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du,
+                             const double* p, C3 force, C3 fres, const double* Dc, double* Fs,
+                             double* kf, cudaStream_t st);
+cudaError_t launch_pressure_rhs(const Mesh& m, const double* Fs, const double* Sv, double* f,
+                                cudaStream_t st);
+cudaError_t launch_correct(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du, W3 u_ic,
+                           const double* p_ip, double* p_ic, const double* pc,
+                           const double* Dc, const double* Fs, const double* kf,
+                           double* F_ic, double* partials, DevScalars* ds, cudaStream_t st);
+cudaError_t launch_auto_dt(const Mesh& m, const double* F, double* partials, DevScalars* ds,
+                           cudaStream_t st);
+cudaError_t launch_nan_count(long long n, const double* a, double* partials, DevScalars* ds,
+                             cudaStream_t st);
+
+// ----------------------------------------------------------- properties --
+struct PhaseProps {
+  double dens[HYDRO_MAXPH], visc[HYDRO_MAXPH], grav[3], f0[3];
+};
+cudaError_t launch_props(const Mesh& m, int nph, const PhaseProps& pp,
+                         CP<HYDRO_MAXPH> q, WP<HYDRO_MAXPH> alpha, double* rho_raw,
+                         double* rho, double* mu, W3 force, double* Sv, double* Sm,
+                         cudaStream_t st);
+cudaError_t launch_smooth(const Mesh& m, const double* in, double* out, cudaStream_t st);
+cudaError_t launch_stforce(const Mesh& m, double sigma, const double* alpha1, W3 G,
+                           W3 out, cudaStream_t st);
+// out (device): [8 sums, min, max]; partials >= 10*4096 doubles; ticket[3]
+cudaError_t launch_stat(const Mesh& m, const double* q, const double* alpha, C3 u,
+                        double* partials, double* out, unsigned* ticket, cudaStream_t st);
+
+// ------------------------------------------------------------ advection --
+// Face fluxes q_f F_f of every phase (Superbee, solver.hpp:550-619) on the
+// faces of direction `stage` (all directions when nstages == 1).
+cudaError_t launch_adv_faces(const Mesh& m, int nph, int stage, int nstages, const double* F,
+                             CP<HYDRO_MAXPH> q, WP<HYDRO_MAXPH> qflux, cudaStream_t st);
+cudaError_t launch_adv_update(const Mesh& m, int nph, int stage, int nstages, double dt,
+                              CP<HYDRO_MAXPH> qflux, CP<HYDRO_MAXPH> qin,
+                              WP<HYDRO_MAXPH> qout, cudaStream_t st);
+// Interface sharpening (advection.hpp:481-530), in place on q (work: 1 face
+// array + DIM cell arrays + 1 cell array).
+cudaError_t launch_adv_sharpen(const Mesh& m, int phase, double sharp, double amax, double dt,
+                               const double* F, double* q, double* qtmp, W3 G,
+                               double* fwork, cudaStream_t st);
+
+// --------------------------------------------------------------- linear --
+// Pressure-correction solve on face couplings kf (coupling -kf between the
+// cells of an inner face, diagonal sum kf + shift), A x = f.
+struct PcgWork {
+  double *r, *z, *p, *Ap, *dg, *idg;                     // FP64 vectors
+  float *r32, *z32, *p32, *Ap32, *dg32, *idg32, *x32, *kf32;  // FP32 inner solve
+  double* partials;  // >= 8 * kMaxBlocks doubles
+  DevScalars* ds;
+  long long pin;     // pinned cell or -1
+  int limit;         // iteration limit of one (inner) solve
+};
+// Diagonal and its reciprocal (plus FP32 copies of couplings when fp32).
+cudaError_t pcg_prepare(const Mesh& m, const double* kf, double shift, PcgWork& w, int fp32,
+                        cudaStream_t st);
+// Plain FP64 PCG: init, then chunks of iterations with device-side early
+// exit (ds->flag[FL_PCG_DONE], iterations in ds->flag[FL_PCG_ITERS]).
+cudaError_t pcg_init(const Mesh& m, const double* kf, const double* f, double* x, int use_guess,
+                     double tol, int singular, PcgWork& w, cudaStream_t st);
+cudaError_t pcg_iterate(const Mesh& m, const double* kf, double* x, int chunk, PcgWork& w,
+                        cudaStream_t st);
+// sum(f) into ds->red[RS_MEAN]; x -= mean(x).
+cudaError_t mean_sum(const Mesh& m, const double* f, PcgWork& w, cudaStream_t st);
+cudaError_t sub_mean(const Mesh& m, double* x, PcgWork& w, cudaStream_t st);
+// Mixed precision: FP64 residual r = f' - A x (||r||^2 in ds->red[RS_IR_RR]),
+// FP32 PCG for A e = r to a relative tolerance, x += e.
+cudaError_t ir_residual(const Mesh& m, const double* kf, const double* f, const double* x,
+                        int singular, PcgWork& w, cudaStream_t st);
+cudaError_t f32_pcg_init(const Mesh& m, double tol, PcgWork& w, cudaStream_t st);
+cudaError_t f32_pcg_iterate(const Mesh& m, int chunk, PcgWork& w, cudaStream_t st);
+cudaError_t f32_accumulate(const Mesh& m, double* x, PcgWork& w, cudaStream_t st);
+cudaError_t scale_vector(long long n, double* a, double s, cudaStream_t st);
+// Right-hand side of a pinned cell (fluid.hpp:996-1014): f[pin] = value and
+// the pinned value moved into the neighbours' rows.
+cudaError_t pin_rhs(const Mesh& m, const double* kf, double* f, long long pin, double value,
+                    cudaStream_t st);
+
+}  // namespace hg

@@ -1,0 +1,369 @@
+// linear.cu -- pressure-correction solve on sm_103a: Jacobi-preconditioned
+// conjugate gradients, matrix-free on the face couplings kf of the
+// flux-correction expressions (fluid.hpp:946-1014: coupling -kf between the
+// two cells of an inner face, diagonal sum kf).  The reference solves these
+// rows with serial Gauss-Seidel (linear.hpp:685-715); CG replaces it.
+//
+// Templated on the element type T: T = double is the plain FP64 path;
+// T = float is the inner solve of the mixed-precision path (FP32 vectors and
+// couplings, FP64 dot products / norms, FP64 iterative refinement around it).
+//
+// One CG iteration = three launches, each returning at once after the
+// device-side `done` flag is set (so the host queues iterations in chunks
+// and reads the flag once per chunk):
+//   k_cg_dir    p = z + beta p
+//   k_cg_spmv   Ap = A p, <p,Ap> -> alpha = rz/<p,Ap>
+//   k_cg_update x += alpha p, r -= alpha Ap, z = r/diag, <r,z>, <r,r> -> beta
+#include <math.h>
+
+#include "kernels.h"
+#include "loop.cuh"
+
+namespace hg {
+
+namespace {
+
+// Matrix-free stencil product (A p)_c = diag_c p_c - sum_f kf_f p_nb with a
+// pinned cell's row the identity and its value excluded from neighbours'.
+template <int DIM, class T>
+__device__ __forceinline__ T stencil_row(const Mesh& m, const Cell& X, const T* kf,
+                                         const T* dg, const T* p, long long pin) {
+  if (X.c == pin) return p[X.c];
+  T acc = dg[X.c] * p[X.c];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long s = cell_stride(m, d);
+    long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+    if (X.i[d] > 0 && X.c - s != pin) acc -= kf[fl] * p[X.c - s];
+    if (X.i[d] < m.n[d] - 1 && X.c + s != pin) acc -= kf[fl + face_stride(m, d)] * p[X.c + s];
+  }
+  return acc;
+}
+
+// diag = sum of the inner-face couplings + shift (1 on the pinned row);
+// idg = 1/diag.
+template <int DIM, class T>
+__global__ void k_diag(Mesh m, const double* kf, double shift, long long pin, T* dg, T* idg,
+                       T* kf32, int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+  double s = shift;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+    if (X.i[d] > 0) s += kf[fl];
+    if (X.i[d] < m.n[d] - 1) s += kf[fl + face_stride(m, d)];
+    if (kf32) {
+      kf32[fl] = (T)kf[fl];
+      if (X.i[d] == m.n[d] - 1) kf32[fl + face_stride(m, d)] = (T)kf[fl + face_stride(m, d)];
+    }
+  }
+  if (X.c == pin) s = 1.;
+  dg[X.c] = (T)s;
+  idg[X.c] = (T)(1. / s);
+  CELL_LOOP_END
+}
+
+// sum of a vector (for the mean projection of singular systems).
+template <class T>
+__global__ void __launch_bounds__(NT) k_sum(long long n, const T* a, double* partials,
+                                            double* out, unsigned* ticket) {
+  double s = 0.;
+  long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
+  for (long long i = blockIdx.x * (long long)NT + tid; i < n; i += (long long)gridDim.x * NT)
+    s += (double)a[i];
+  double v[1] = {s};
+  __shared__ double o[1];
+  if (grid_reduce<RED_SUM, 1>(v, partials, ticket, o))
+    if (tid == 0) *out = o[0];
+}
+
+__global__ void k_sub_mean(long long n, double* x, const double* sum) {
+  double mean = *sum / (double)n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] -= mean;
+}
+
+// r = f - mean(f) - A x (x == 0 unless use_guess), z = r/diag, p = z;
+// reduces <r,z>, <r,r>, <f',f'> and sets the tolerance and done flag.
+template <int DIM, class T>
+__global__ void __launch_bounds__(NT) k_cg_init(Mesh m, const T* kf, const T* dg, const T* idg,
+                                                const double* f, const double* fmean_sum,
+                                                const T* x, int use_guess, long long pin,
+                                                T* r, T* z, T* p, double tol, double* partials,
+                                                DevScalars* ds, int kch) {
+  double s[3] = {0., 0., 0.};
+  double mean = fmean_sum ? *fmean_sum / (double)m.nc : 0.;
+  CELL_LOOP_BEGIN(m, kch)
+  double fc = f[X.c] - mean;
+  double rc = fc;
+  if (use_guess) rc -= (double)stencil_row<DIM>(m, X, kf, dg, x, pin);
+  T rt = (T)rc;
+  T zt = rt * idg[X.c];
+  r[X.c] = rt;
+  z[X.c] = zt;
+  p[X.c] = zt;
+  s[0] += (double)rt * (double)zt;
+  s[1] += (double)rt * (double)rt;
+  s[2] += fc * fc;
+  CELL_LOOP_END
+  __shared__ double o[3];
+  if (grid_reduce<RED_SUM, 3>(s, partials, &ds->ticket[TK_PCG_INIT], o)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      ds->red[RS_PCG_RZ] = o[0];
+      ds->red[RS_PCG_RR] = o[1];
+      ds->red[RS_PCG_FF] = o[2];
+      ds->red[RS_PCG_TOL2] = tol * tol * o[2];
+      ds->flag[FL_PCG_ITERS] = 0;
+      ds->flag[FL_PCG_DONE] = (o[2] == 0. || o[1] <= tol * tol * o[2]) ? 1 : 0;
+    }
+  }
+}
+
+template <class T>
+__global__ void k_cg_dir(long long n, const T* z, T* p, const DevScalars* ds) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  T beta = (T)ds->red[RS_PCG_BETA];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    p[i] = z[i] + beta * p[i];
+}
+
+template <int DIM, class T>
+__global__ void __launch_bounds__(NT) k_cg_spmv(Mesh m, const T* kf, const T* dg, const T* p,
+                                                T* Ap, long long pin, double* partials,
+                                                DevScalars* ds, int kch) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  double s = 0.;
+  CELL_LOOP_BEGIN(m, kch)
+  T a = stencil_row<DIM>(m, X, kf, dg, p, pin);
+  Ap[X.c] = a;
+  s += (double)p[X.c] * (double)a;
+  CELL_LOOP_END
+  double v[1] = {s};
+  __shared__ double o[1];
+  if (grid_reduce<RED_SUM, 1>(v, partials, &ds->ticket[TK_PCG_A], o)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      ds->red[RS_PCG_PAP] = o[0];
+      ds->red[RS_PCG_ALPHA] = ds->red[RS_PCG_RZ] / o[0];
+    }
+  }
+}
+
+template <class TX, class T>
+__global__ void __launch_bounds__(NT) k_cg_update(long long n, TX* x, T* r, T* z, const T* p,
+                                                  const T* Ap, const T* idg, double* partials,
+                                                  DevScalars* ds, int limit) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  double alpha = ds->red[RS_PCG_ALPHA];
+  T at = (T)alpha;
+  double s[2] = {0., 0.};
+  long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
+  for (long long i = blockIdx.x * (long long)NT + tid; i < n; i += (long long)gridDim.x * NT) {
+    x[i] += (TX)(at * p[i]);
+    T ri = r[i] - at * Ap[i];
+    T zi = ri * idg[i];
+    r[i] = ri;
+    z[i] = zi;
+    s[0] += (double)ri * (double)zi;
+    s[1] += (double)ri * (double)ri;
+  }
+  __shared__ double o[2];
+  if (grid_reduce<RED_SUM, 2>(s, partials, &ds->ticket[TK_PCG_B], o)) {
+    if (tid == 0) {
+      double rz_old = ds->red[RS_PCG_RZ];
+      ds->red[RS_PCG_BETA] = o[0] / rz_old;
+      ds->red[RS_PCG_RZ] = o[0];
+      ds->red[RS_PCG_RR] = o[1];
+      int it = ds->flag[FL_PCG_ITERS] + 1;
+      ds->flag[FL_PCG_ITERS] = it;
+      if (o[1] <= ds->red[RS_PCG_TOL2] || it >= limit) ds->flag[FL_PCG_DONE] = 1;
+    }
+  }
+}
+
+// FP64 residual of the refinement loop: r = f' - A x (f' = f - mean when
+// singular), <r,r> reduced; r also written as FP32 for the inner solve.
+template <int DIM>
+__global__ void __launch_bounds__(NT) k_ir_residual(Mesh m, const double* kf, const double* dg,
+                                                    const double* f, const double* fmean_sum,
+                                                    const double* x, long long pin, double* r,
+                                                    double* partials, DevScalars* ds, int kch) {
+  double s = 0.;
+  double mean = fmean_sum ? *fmean_sum / (double)m.nc : 0.;
+  CELL_LOOP_BEGIN(m, kch)
+  double rc = (f[X.c] - mean) - stencil_row<DIM>(m, X, kf, dg, x, pin);
+  r[X.c] = rc;
+  s += rc * rc;
+  CELL_LOOP_END
+  double v[1] = {s};
+  __shared__ double o[1];
+  if (grid_reduce<RED_SUM, 1>(v, partials, &ds->ticket[TK_IR], o))
+    if (threadIdx.x == 0 && threadIdx.y == 0) ds->red[RS_IR_RR] = o[0];
+}
+
+int flat_blocks_l(long long n) {
+  long long b = (n + NT - 1) / NT;
+  if (b > kMaxBlocks) b = kMaxBlocks;
+  if (b < 1) b = 1;
+  if (b > 152 * 16) b = 152 * 16;
+  return (int)b;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------- drivers ------
+#define LAUNCH_DIM(KERNEL, ...)                                        \
+  do {                                                                 \
+    if (m.dim == 3)                                                    \
+      KERNEL<3><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);       \
+    else                                                               \
+      KERNEL<2><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);       \
+  } while (0)
+#define LAUNCH_DIM_T(KERNEL, T, ...)                                   \
+  do {                                                                 \
+    if (m.dim == 3)                                                    \
+      KERNEL<3, T><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);    \
+    else                                                               \
+      KERNEL<2, T><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);    \
+  } while (0)
+
+cudaError_t pcg_prepare(const Mesh& m, const double* kf, double shift, PcgWork& w, int fp32,
+                        cudaStream_t st) {
+  Launch L = cell_launch(m);
+  if (m.dim == 3) {
+    k_diag<3, double><<<L.grid, L.block, 0, st>>>(m, kf, shift, w.pin, w.dg, w.idg, nullptr, L.kch);
+    if (fp32)
+      k_diag<3, float><<<L.grid, L.block, 0, st>>>(m, kf, shift, w.pin, w.dg32, w.idg32, w.kf32,
+                                                   L.kch);
+  } else {
+    k_diag<2, double><<<L.grid, L.block, 0, st>>>(m, kf, shift, w.pin, w.dg, w.idg, nullptr, L.kch);
+    if (fp32)
+      k_diag<2, float><<<L.grid, L.block, 0, st>>>(m, kf, shift, w.pin, w.dg32, w.idg32, w.kf32,
+                                                   L.kch);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t mean_sum(const Mesh& m, const double* f, PcgWork& w, cudaStream_t st) {
+  k_sum<double><<<flat_blocks_l(m.nc), dim3(BX, BY), 0, st>>>(m.nc, f, w.partials,
+                                                             &w.ds->red[RS_MEAN],
+                                                             &w.ds->ticket[TK_MEAN]);
+  return cudaGetLastError();
+}
+
+cudaError_t sub_mean(const Mesh& m, double* x, PcgWork& w, cudaStream_t st) {
+  k_sum<double><<<flat_blocks_l(m.nc), dim3(BX, BY), 0, st>>>(m.nc, x, w.partials,
+                                                             &w.ds->red[RS_XMEAN],
+                                                             &w.ds->ticket[TK_MEAN2]);
+  k_sub_mean<<<flat_blocks_l(m.nc), NT, 0, st>>>(m.nc, x, &w.ds->red[RS_XMEAN]);
+  return cudaGetLastError();
+}
+
+cudaError_t pcg_init(const Mesh& m, const double* kf, const double* f, double* x, int use_guess,
+                     double tol, int singular, PcgWork& w, cudaStream_t st) {
+  Launch L = cell_launch(m);
+  const double* msum = nullptr;
+  if (singular) {
+    mean_sum(m, f, w, st);
+    msum = &w.ds->red[RS_MEAN];
+  }
+  LAUNCH_DIM_T(k_cg_init, double, m, kf, w.dg, w.idg, f, msum, x, use_guess, w.pin, w.r, w.z,
+             w.p, tol, w.partials, w.ds);
+  if (!use_guess) cudaMemsetAsync(x, 0, sizeof(double) * m.nc, st);
+  return cudaGetLastError();
+}
+
+cudaError_t pcg_iterate(const Mesh& m, const double* kf, double* x, int chunk, PcgWork& w,
+                        cudaStream_t st) {
+  Launch L = cell_launch(m);
+  int fb = flat_blocks_l(m.nc);
+  for (int it = 0; it < chunk; ++it) {
+    LAUNCH_DIM_T(k_cg_spmv, double, m, kf, w.dg, w.p, w.Ap, w.pin, w.partials, w.ds);
+    k_cg_update<double, double><<<fb, dim3(BX, BY), 0, st>>>(m.nc, x, w.r, w.z, w.p, w.Ap, w.idg,
+                                                             w.partials, w.ds, w.limit);
+    k_cg_dir<double><<<fb, NT, 0, st>>>(m.nc, w.z, w.p, w.ds);
+  }
+  return cudaGetLastError();
+}
+
+// ------------------------------------------- mixed-precision (FP32) ------
+cudaError_t ir_residual(const Mesh& m, const double* kf, const double* f, const double* x,
+                        int singular, PcgWork& w, cudaStream_t st) {
+  Launch L = cell_launch(m);
+  const double* msum = singular ? &w.ds->red[RS_MEAN] : nullptr;
+  LAUNCH_DIM(k_ir_residual, m, kf, w.dg, f, msum, x, w.pin, w.r, w.partials, w.ds);
+  return cudaGetLastError();
+}
+
+cudaError_t f32_pcg_init(const Mesh& m, double tol, PcgWork& w, cudaStream_t st) {
+  Launch L = cell_launch(m);
+  cudaMemsetAsync(w.x32, 0, sizeof(float) * m.nc, st);
+  LAUNCH_DIM_T(k_cg_init, float, m, w.kf32, w.dg32, w.idg32, w.r, (const double*)nullptr,
+             w.x32, 0, w.pin, w.r32, w.z32, w.p32, tol, w.partials, w.ds);
+  return cudaGetLastError();
+}
+
+cudaError_t f32_pcg_iterate(const Mesh& m, int chunk, PcgWork& w, cudaStream_t st) {
+  Launch L = cell_launch(m);
+  int fb = flat_blocks_l(m.nc);
+  for (int it = 0; it < chunk; ++it) {
+    LAUNCH_DIM_T(k_cg_spmv, float, m, w.kf32, w.dg32, w.p32, w.Ap32, w.pin, w.partials, w.ds);
+    k_cg_update<float, float><<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.x32, w.r32, w.z32, w.p32,
+                                                           w.Ap32, w.idg32, w.partials, w.ds,
+                                                           w.limit);
+    k_cg_dir<float><<<fb, NT, 0, st>>>(m.nc, w.z32, w.p32, w.ds);
+  }
+  return cudaGetLastError();
+}
+
+namespace {
+__global__ void k_accumulate(long long n, double* x, const float* e) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] += (double)e[i];
+}
+}  // namespace
+
+namespace {
+__global__ void k_scale(long long n, double* a, double s) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    a[i] *= s;
+}
+}  // namespace
+
+cudaError_t scale_vector(long long n, double* a, double s, cudaStream_t st) {
+  k_scale<<<flat_blocks_l(n), NT, 0, st>>>(n, a, s);
+  return cudaGetLastError();
+}
+
+namespace {
+__global__ void k_pin_rhs(Mesh m, const double* kf, double* f, long long pin, double value) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int i[3];
+  i[0] = (int)(pin % m.n[0]);
+  i[1] = (int)((pin / m.n[0]) % m.n[1]);
+  i[2] = (int)(pin / ((long long)m.n[0] * m.n[1]));
+  for (int d = 0; d < m.dim; ++d) {
+    long long s = cell_stride(m, d);
+    long long fl = face_id(m, d, i[0], i[1], i[2]);
+    if (i[d] > 0) f[pin - s] += kf[fl] * value;
+    if (i[d] < m.n[d] - 1) f[pin + s] += kf[fl + face_stride(m, d)] * value;
+  }
+  f[pin] = value;
+}
+}  // namespace
+
+cudaError_t pin_rhs(const Mesh& m, const double* kf, double* f, long long pin, double value,
+                    cudaStream_t st) {
+  k_pin_rhs<<<1, 32, 0, st>>>(m, kf, f, pin, value);
+  return cudaGetLastError();
+}
+
+cudaError_t f32_accumulate(const Mesh& m, double* x, PcgWork& w, cudaStream_t st) {
+  k_accumulate<<<flat_blocks_l(m.nc), NT, 0, st>>>(m.nc, x, w.x32);
+  return cudaGetLastError();
+}
+
+}  // namespace hg

@@ -1,0 +1,79 @@
+// loop.cuh -- per-cell loop and stencil helpers shared by the kernel files.
+#pragma once
+
+#include "common.cuh"
+
+namespace hg {
+
+// Upper bound of blocks of any reduction launch; partial-sum buffers hold
+// kMaxBlocks entries per reduced value.
+constexpr int kMaxBlocks = 1 << 17;
+
+__device__ __forceinline__ double avg(double a, double b) { return a * 0.5 + b * 0.5; }
+__device__ __forceinline__ float avg(float a, float b) { return a * 0.5f + b * 0.5f; }
+
+struct Cell {
+  int i[3];
+  long long c;
+};
+
+// Thread (x, y) of block (bx, by, bz) visits cells (i, j, k) with
+// i = bx*BX + x, j = by*BY + y and k in [bz*kch, bz*kch + kch).
+#define CELL_LOOP_BEGIN(m, kch)                           \
+  {                                                       \
+    Cell X;                                               \
+    X.i[0] = blockIdx.x * BX + threadIdx.x;               \
+    X.i[1] = blockIdx.y * BY + threadIdx.y;               \
+    const bool act_ = X.i[0] < m.n[0] && X.i[1] < m.n[1]; \
+    const int nz_ = m.dim == 3 ? m.n[2] : 1;              \
+    const int k0_ = blockIdx.z * (kch);                   \
+    const int k1_ = min(k0_ + (kch), nz_);                \
+    for (int kk_ = k0_; kk_ < k1_; ++kk_) {               \
+      X.i[2] = kk_;                                       \
+      if (!act_) continue;                                \
+      X.c = cell_id(m, X.i[0], X.i[1], kk_);
+#define CELL_LOOP_END \
+  }                   \
+  }
+
+// Cell gradient (component along the axis of stride s) of a scalar whose
+// boundary faces are extrapolated (ConditionFaceExtrapolation,
+// solver.hpp:446-464).  On a uniform block that formula reduces to
+// p_b = 2 p_c - p_f(opposite face); needs nd >= 2.
+template <class T>
+__device__ __forceinline__ T grad_extrap(const T* p, long long c, int id, int nd, long long s,
+                                         T inv_h) {
+  T pc = p[c];
+  T flo, fhi;
+  if (id > 0 && id < nd - 1) {
+    flo = avg(p[c - s], pc);
+    fhi = avg(pc, p[c + s]);
+  } else if (id == 0) {
+    fhi = avg(pc, p[c + s]);
+    flo = T(2) * pc - fhi;
+  } else {
+    flo = avg(p[c - s], pc);
+    fhi = T(2) * pc - flo;
+  }
+  return (fhi - flo) * inv_h;
+}
+
+struct Geo {
+  double inv_h[3], h[3], A[3], V, invV;
+  double inv_h2[3];
+};
+
+inline Geo make_geo(const Mesh& m) {
+  Geo g;
+  for (int d = 0; d < 3; ++d) {
+    g.h[d] = m.h[d];
+    g.inv_h[d] = 1. / m.h[d];
+    g.inv_h2[d] = 1. / (m.h[d] * m.h[d]);
+    g.A[d] = m.A[d];
+  }
+  g.V = m.V;
+  g.invV = 1. / m.V;
+  return g;
+}
+
+}  // namespace hg

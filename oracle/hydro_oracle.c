@@ -185,6 +185,40 @@ static void interp(const Mesh* m, const double* fc, double* ff, int bc,
   }
 }
 
+/* Interpolate of a vector cell field (components fc[0..dim-1]) with
+ * zero-derivative boundaries.  With `geometric` the inner faces take the
+ * Vect overload of GetGeometricAverage (solver.hpp:380-390): direction of
+ * the arithmetic mean, magnitude sqrt(|a| |b|). */
+static void interp_vec(const Mesh* m, double* const* fc, double* const* ff, int geometric) {
+  int dim = m->dim;
+  if (!geometric) {
+    for (int k = 0; k < dim; ++k) interp(m, fc[k], ff[k], BC_ZERODER, NULL, 0);
+    return;
+  }
+  long f;
+#pragma omp parallel for num_threads(g_threads)
+  for (f = 0; f < m->nf; ++f) {
+    int d;
+    long mi[3], cm, cp;
+    fdecode(m, f, &d, mi, &cm, &cp);
+    if (cm >= 0 && cp >= 0) {
+      double av[3], n2 = 0., na = 0., nb = 0.;
+      for (int k = 0; k < dim; ++k) {
+        av[k] = (fc[k][cm] + fc[k][cp]) * 0.5;
+        n2 += av[k] * av[k];
+        na += fc[k][cm] * fc[k][cm];
+        nb += fc[k][cp] * fc[k][cp];
+      }
+      double an = sqrt(n2);
+      for (int k = 0; k < dim; ++k)
+        ff[k][f] = an < 1e-8 ? av[k] : av[k] / an * sqrt(sqrt(na) * sqrt(nb));
+    } else {
+      long cc = cm >= 0 ? cm : cp;
+      for (int k = 0; k < dim; ++k) ff[k][f] = fc[k][cc];
+    }
+  }
+}
+
 /* Gradient (solver.hpp:658-677): Green-Gauss from face values. */
 static void gradient(const Mesh* m, const double* ff, double* const* gc) {
   long c;
@@ -923,8 +957,7 @@ int oracle_make_iteration(oracle_ctx* x) {
   double* ffext[3] = {x->fw[0], x->fw[1], x->fw[2]};
   double* fres[3] = {x->cw[6], x->cw[7], x->cw[8]};
   double* ffres[3] = {x->fw[3], x->fw[4], x->fw[6]};
-  for (int k = 0; k < dim; ++k)
-    interp(m, x->force[k], ffext[k], BC_ZERODER, NULL, d->force_geometric_average);
+  interp_vec(m, x->force, ffext, d->force_geometric_average);
   for (long c = 0; c < nc; ++c) {
     long mi[3];
     cmidx(m, c, mi);
@@ -936,8 +969,7 @@ int oracle_make_iteration(oracle_ctx* x) {
       fres[k][c] = sum / m->V;
     }
   }
-  for (int k = 0; k < dim; ++k)
-    interp(m, fres[k], ffres[k], BC_ZERODER, NULL, d->force_geometric_average);
+  interp_vec(m, fres, ffres, d->force_geometric_average);
 
   /* CalcKinematicViscosity (fluid.hpp:632-641) */
   double* muf = x->fw[7];

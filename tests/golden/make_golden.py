@@ -1,0 +1,138 @@
+"""Generates the golden vectors of the parity tests from the reference.
+
+Run in a container that holds the reference tree (default /root/reference;
+override with HYDRO_REFERENCE):
+
+    make -C oracle            # builds oracle/_ref/libhydro_ref.so from it
+    python tests/golden/make_golden.py
+
+1. For each case below, the reference's own FluidSimple +
+   AdvectionSolverMultiExplicit (driven by oracle/ref_harness.cpp) runs
+   from the stated initial fields; inputs, final fields and per-step
+   statistics go to tests/golden/<name>.npz.
+2. The reference's checked-in sample run of examples/cavity (64x64,
+   Re 3200, 1000 SIMPLE iterations) is read from its .vts / .plt output and
+   stored as tests/golden/cavity_sample.npz (6 significant digits, as
+   printed by the reference).
+"""
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from hydro_gb300 import capi, cases  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+REF = os.environ.get("HYDRO_REFERENCE", "/root/reference")
+
+
+def tight(d, solver=capi.LINEAR_GAUSS_SEIDEL):
+    d.velocity_solver = solver
+    d.pressure_solver = capi.LINEAR_GAUSS_SEIDEL
+    d.velocity_tolerance = 1e-13
+    d.velocity_iters_limit = 100000
+    d.pressure_tolerance = 1e-11
+    d.pressure_iters_limit = 100000
+    d.pressure_omega = 1.5
+    return d
+
+
+def golden_cases():
+    out = []
+    d, u0, q0 = cases.cavity(n=16, mu=0.01, dt=1e-2)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    out.append(("cavity2d_fixed", d, u0, q0, 3, True))
+
+    d, u0, q0 = cases.cavity(n=16, mu=0.01, dt=1e-2)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 1e-9, 200
+    out.append(("cavity2d_converged", d, u0, q0, 2, True))
+
+    d, u0, q0 = cases.broken_dam(nx=40, ny=20, dt_auto=True, dt_max=5e-4, smooth_times=2)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 1e-7, 40
+    out.append(("dam2d_auto", d, u0, q0, 3, True))
+
+    d, u0, q0 = cases.broken_dam(nx=24, ny=12, dt_auto=False, dt=1e-3, smooth_times=1)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 2
+    d.tvd_split, d.sigma, d.force_geometric_average = 1, 0.05, 1
+    out.append(("dam2d_split_sigma_geo", d, u0, q0, 2, True))
+
+    d, u0, q0, _ = cases.rising_drops(n=12, seed=3, dt_max=5e-3)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    out.append(("drops3d", d, u0, q0, 2, True))
+
+    d, u0, q0 = cases.cavity(n=10, dim=3, dt=1e-2)
+    d.n[2] = 7
+    u0, q0 = np.zeros(d.ncells * 3), np.ones(d.ncells)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    d.pressure_fixed_cell, d.time_second_order = 123, 0
+    out.append(("cavity3d_pinned_first_order", d, u0, q0, 2, True))
+
+    d, u0, q0 = cases.cavity(n=12, mu=0.02, dt=5e-3)
+    d.n[0], d.n[1], d.hi[0] = 20, 12, 1.7
+    u0, q0 = np.zeros(d.ncells * 2), np.ones(d.ncells)
+    tight(d, capi.LINEAR_JACOBI)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 4
+    d.guess_extrapolation, d.velocity_relaxation_factor = 0.5, 0.7
+    out.append(("cavity2d_jacobi_extrap", d, u0, q0, 3, True))
+
+    # reference defaults for the linear solvers: one LU sweep for velocity
+    # (an approximate solve; CPU-only semantics), SOR pressure
+    d, u0, q0 = cases.broken_dam(nx=16, ny=8, dt_auto=False, dt=2e-3, smooth_times=2)
+    d.velocity_solver = capi.LINEAR_LU
+    d.pressure_solver = capi.LINEAR_GAUSS_SEIDEL
+    d.pressure_tolerance, d.pressure_iters_limit, d.pressure_omega = 1e-3, 1000, 1.9
+    d.convergence_tolerance, d.num_iterations_limit = 1e-2, 10
+    d.sharp = 0.5
+    out.append(("dam2d_lu_sor_sharp", d, u0, q0, 3, False))
+    return out
+
+
+def make_cases():
+    for name, d, u0, q0, nsteps, gpu_ok in golden_cases():
+        u, p, F, q, stats = O.ref_run(d, u0, q0, nsteps)
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(
+            path, desc=json.dumps(capi.desc_to_dict(d)), u0=u0, q0=q0, nsteps=nsteps,
+            gpu_comparable=gpu_ok, u=u, p=p, F=F, q=q,
+            outer_iterations=np.array([s["outer_iterations"] for s in stats]),
+            indicator=np.array([s["convergence_indicator"] for s in stats]),
+            dt=np.array([s["dt"] for s in stats]),
+            substeps=np.array([s["advection_substeps"] for s in stats]))
+        print("wrote", path, [s["outer_iterations"] for s in stats])
+
+
+def make_sample():
+    sdir = os.path.join(REF, "examples", "cavity", "sample")
+    vts = open(os.path.join(sdir, "exp.field.0.vts")).read()
+
+    def arr(name):
+        m = re.search(r'Name="%s"[^>]*>\s*([^<]*)<' % name, vts)
+        return np.array([float(v) for v in m.group(1).split()])
+
+    hist = []
+    for line in open(os.path.join(sdir, "exp.iter_history.plt")):
+        if re.match(r"^\d+ ", line):
+            hist.append(float(line.split()[1]))
+    path = os.path.join(HERE, "cavity_sample.npz")
+    np.savez_compressed(path, velocity_x=arr("velocity_x"), velocity_y=arr("velocity_y"),
+                        pressure=arr("pressure"), iter_history=np.array(hist))
+    print("wrote", path)
+
+
+if __name__ == "__main__":
+    if not O.ref_available():
+        O.build(ref=True)
+    make_cases()
+    make_sample()

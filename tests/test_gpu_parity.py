@@ -1,0 +1,183 @@
+"""GPU parity: libhydro_gpu.so (CUDA, sm_103a) against the CPU oracle on the
+same seeded inputs.  Linear solves are tight on both sides and the number of
+SIMPLE iterations per step is pinned, so iterates must agree to rounding:
+velocity, pressure (up to its free constant), fluxes and partial densities
+to relative L2 <= 1e-10 (the tolerance of the FP64 drop-in)."""
+import numpy as np
+import pytest
+
+from hydro_gb300 import capi, cases
+from tests.util import compare, rel, run, tight
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+
+
+def _pair(d, u0, q0, nsteps):
+    from hydro_gb300.solver import Hydro
+    from oracle.oracle import Oracle
+    g = run(Hydro(d), u0, q0, nsteps)
+    do = d.copy()
+    do.velocity_solver = capi.LINEAR_GAUSS_SEIDEL
+    do.pressure_solver = capi.LINEAR_CG
+    o = run(Oracle(do), u0, q0, nsteps)
+    return g, o
+
+
+def _check(g, o, tol=TOL):
+    errs = compare(g, o)
+    assert all(v <= tol for v in errs.values()), errs
+    for sg, so in zip(g["stats"], o["stats"]):
+        assert sg["outer_iterations"] == so["outer_iterations"]
+        assert sg["advection_substeps"] == so["advection_substeps"]
+        assert abs(sg["dt"] - so["dt"]) <= 1e-12 * so["dt"]
+    return errs
+
+
+def test_cavity_2d(built):
+    d, u0, q0 = cases.cavity(n=16, mu=0.01, dt=1e-2)
+    tight(d)
+    d.convergence_tolerance = 0.0
+    d.num_iterations_limit = 3
+    g, o = _pair(d, u0, q0, 3)
+    _check(g, o)
+
+
+def test_cavity_2d_nonsquare_pinned(built):
+    d, u0, q0 = cases.cavity(n=12, mu=0.02, dt=5e-3)
+    d.n[0], d.n[1] = 20, 12
+    d.hi[0] = 1.7
+    u0 = np.zeros(d.ncells * 2)
+    q0 = np.ones(d.ncells)
+    d.pressure_fixed_cell = 37
+    d.pressure_fixed_value = 0.0
+    d.guess_extrapolation = 0.5
+    d.velocity_relaxation_factor = 0.7
+    tight(d)
+    d.convergence_tolerance = 0.0
+    d.num_iterations_limit = 4
+    g, o = _pair(d, u0, q0, 3)
+    _check(g, o)
+
+
+def test_broken_dam_2d_advection(built):
+    d, u0, q0 = cases.broken_dam(nx=40, ny=20, dt_auto=True, dt_max=5e-4, smooth_times=2)
+    tight(d)
+    d.convergence_tolerance = 1e-7
+    d.num_iterations_limit = 40
+    g, o = _pair(d, u0, q0, 3)
+    _check(g, o, tol=1e-9)
+
+
+def test_broken_dam_split_sigma(built):
+    d, u0, q0 = cases.broken_dam(nx=24, ny=12, dt_auto=False, dt=1e-3, smooth_times=1)
+    tight(d)
+    d.convergence_tolerance = 0.0
+    d.num_iterations_limit = 2
+    d.tvd_split = 1
+    d.sigma = 0.05
+    d.force_geometric_average = 1
+    g, o = _pair(d, u0, q0, 2)
+    _check(g, o)
+
+
+def test_rising_drops_3d(built):
+    d, u0, q0, _ = cases.rising_drops(n=12, seed=3, dt_max=5e-3)
+    tight(d)
+    d.convergence_tolerance = 0.0
+    d.num_iterations_limit = 3
+    g, o = _pair(d, u0, q0, 2)
+    _check(g, o)
+
+
+def test_cavity_3d_first_order_time(built):
+    d, u0, q0 = cases.cavity(n=10, dim=3, dt=1e-2)
+    d.n[2] = 7
+    u0 = np.zeros(d.ncells * 3)
+    q0 = np.ones(d.ncells)
+    d.time_second_order = 0
+    tight(d)
+    d.convergence_tolerance = 0.0
+    d.num_iterations_limit = 3
+    g, o = _pair(d, u0, q0, 2)
+    _check(g, o)
+
+
+def test_mixed_precision_matches_fp64(built):
+    from hydro_gb300.solver import Hydro
+    d, u0, q0, _ = cases.rising_drops(n=16, seed=5, dt_max=5e-3)
+    d.pressure_tolerance = 1e-10
+    d.velocity_tolerance = 1e-12
+    d.convergence_tolerance = 0.0
+    d.num_iterations_limit = 4
+    a = run(Hydro(d), u0, q0, 3)
+    dm = d.copy()
+    dm.precision = capi.MIXED
+    b = run(Hydro(dm), u0, q0, 3)
+    errs = compare(b, a)
+    assert all(v <= 1e-6 for v in errs.values()), errs
+    for s in b["stats"]:
+        assert s["pressure_residual"] <= 1e-10
+
+
+def test_stencil_solve_matches_oracle(built):
+    from hydro_gb300.solver import stencil_solve
+    from oracle import oracle as O
+    rng = np.random.default_rng(7)
+    for dim, n, pin in ((2, (13, 9, 1), -1), (3, (6, 5, 7), 11), (3, (8, 8, 8), -1)):
+        nc = n[0] * n[1] * (n[2] if dim == 3 else 1)
+        d = capi.default_desc()
+        d.dim = dim
+        for k in range(3):
+            d.n[k] = n[k]
+        nf = d.nfaces
+        kf = rng.uniform(0.5, 2.0, nf)
+        c = rng.normal(size=nc)
+        if pin < 0:
+            c -= c.mean()
+        st, x, it, res = stencil_solve(dim, n, kf, 0.0, pin, 0.3, c, 1e-12, 5000)
+        sto, xo, ito, reso = O.stencil_solve(dim, n, kf, 0.0, pin, 0.3, c, 1e-12, 5000)
+        assert st == capi.OK and sto == capi.OK
+        assert res <= 1e-12
+        assert rel(x, xo) <= 1e-9, (dim, n, rel(x, xo))
+
+
+def test_mass_conservation_and_stats(built):
+    from hydro_gb300.solver import Hydro
+    from oracle.oracle import Oracle
+    d, u0, q0 = cases.broken_dam(nx=48, ny=24, dt_auto=True, dt_max=5e-4, smooth_times=2)
+    d.convergence_tolerance = 1e-6
+    d.num_iterations_limit = 30
+    h = Hydro(d)
+    run(h, u0, q0, 0)
+    m0 = h.calc_stat()
+    for _ in range(4):
+        h.step()
+    m1 = h.calc_stat()
+    for i in range(2):
+        assert abs(m1.partial_mass[i] - m0.partial_mass[i]) <= 1e-11 * abs(m0.partial_mass[i])
+    o = Oracle(d)
+    run(o, u0, q0, 0)
+    so = o.calc_stat()
+    for i in range(2):
+        assert abs(so.volume[i] - m0.volume[i]) <= 1e-12 * abs(so.volume[i])
+        assert abs(so.pd_max[i] - m0.pd_max[i]) <= 1e-12 * abs(so.pd_max[i])
+
+
+@pytest.mark.parametrize("name", [n for n in __import__("tests.goldens", fromlist=["x"]).names()])
+def test_gpu_matches_reference_golden(built, name):
+    """GPU against the reference's own outputs (golden vectors)."""
+    from hydro_gb300.solver import Hydro
+    from tests import goldens
+    g = goldens.load(name)
+    if not g["gpu_comparable"]:
+        pytest.skip("reference LU velocity sweep is a sequential approximate solve")
+    d = g["desc"].copy()
+    d.velocity_solver = capi.LINEAR_JACOBI
+    d.pressure_solver = capi.LINEAR_CG
+    d.velocity_tolerance, d.velocity_iters_limit = 1e-14, 20000
+    d.pressure_tolerance, d.pressure_iters_limit = 1e-13, 20000
+    out = run(Hydro(d), g["u0"], g["q0"], g["nsteps"])
+    errs = compare(out, g)
+    assert all(v <= 1e-9 for v in errs.values()), errs
+    assert [s["outer_iterations"] for s in out["stats"]] == list(g["outer_iterations"])
