@@ -1,0 +1,452 @@
+#!/usr/bin/env python
+"""Benchmark of the hydro time-step hot path on GB300.
+
+Workload: 3D rising drops at 192^3 (unit cube, ambient rho 10 / drops rho 1,
+mu 1e-2, g = -1 along z, 1-8 seeded drops), FP64, a pinned number of SIMPLE
+iterations per step (both arms do the same work per step), pressure solve to
+relative residual 1e-8, TVD advection of both phases, property update.
+Synthetic seeded inputs of that shape (no external data).
+
+Metric: Mcell-updates/s = cells x time steps / wall seconds, whole job.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+  python bench.py --impl reference ...   # the reference algorithm on the CPU
+
+Multi-GPU: replicas only (the reference's MPI mode runs redundant replicas;
+the path has no exchange step here) -- each rank advances its own seeded
+case, time is the max over ranks, value the cells x steps of all ranks.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Algorithmic (compulsory) bytes per cell of one launch of each kernel group,
+# FP64 path, 3D: each distinct input read once, each output written once;
+# face arrays count ~1 entry per cell per direction.
+ALG_BYTES_PER_CELL_FP64 = {
+    "cg_spmv": 8 * (1 + 3 + 1 + 1),        # read p, kf[3], diag; write Ap
+    "cg_update": 8 * (5 + 3),              # read x, r, p, Ap, 1/diag; write x, r, z
+    "cg_dir": 8 * (2 + 1),                 # read z, p; write p
+    "mom_sweep": 8 * (7 + 3 + 3 + 3),      # read coef[7], res[3], du[3]; write du[3]
+    "mom_assemble": 8 * (26 + 11),         # read u,utc,utp,G[9],F[3],rho,mu,fo[3]; write coef[7],res[3],Dc
+    "force": 8 * (3 + 9 + 1 + 1 + 3 + 3 + 6),  # read u,G,p,mu,force,stforce; write fo,fres
+    "vel_grad": 8 * (3 + 9),
+    "rhie_chow": 8 * (6 + 1 + 6 + 1 + 6),  # read u,du,p,force,fres,Dc; write Fs[3], kf[3]
+    "correct": 8 * (6 + 2 + 1 + 1 + 6 + 3 + 1 + 3),  # read u,du,p,pc,Dc,Fs,kf; write u,p,F
+    "adv_faces": 8 * (2 + 3 + 6),          # read q[2], F[3]; write qflux[2x3]
+    "adv_update": 8 * (2 + 6 + 2),
+}
+# FP32 inner solve of the mixed path (vectors 4 B)
+ALG_BYTES_PER_CELL_FP32 = {
+    "cg_spmv": 4 * (1 + 3 + 1 + 1),
+    "cg_update": 4 * (5 + 3),
+    "cg_dir": 4 * (2 + 1),
+}
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(n, seed, precision, outer):
+    from hydro_gb300 import capi, cases
+    d, u0, q0, drops = cases.rising_drops(n=n, seed=seed, dt_max=2e-3)
+    d.convergence_tolerance = 0.0
+    d.num_iterations_limit = outer
+    d.velocity_tolerance = 1e-8
+    d.velocity_iters_limit = 200
+    d.pressure_tolerance = 1e-8
+    d.pressure_iters_limit = 20000
+    d.precision = capi.MIXED if precision == "mixed" else capi.FP64
+    return d, u0, q0, drops
+
+
+def init_dist():
+    world = env_int("WORLD_SIZE", 1)
+    rank = env_int("RANK", 0)
+    local = env_int("LOCAL_RANK", 0)
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        try:
+            import torch
+            if not torch.cuda.is_available():
+                backend = "gloo"
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ----------------------------------------------------------- CPU baseline --
+def cpu_sample(n, seed, outer, sweeps=(4, 12), threads=None):
+    """The reference algorithm (CPU oracle port: plain-C restatement of
+    FluidSimple with the reference's default linear solvers -- one LU sweep
+    for velocity, Gauss-Seidel/SOR 1.9 for pressure with tolerance 1e-3 and
+    at most 1001 sweeps) on the same 192^3 case.  Bounded sample: two SIMPLE
+    iterations with a few pressure sweeps each, timed; cost per iteration =
+    rest + sweeps x per-sweep time, extrapolated to the 1001 sweeps of the
+    default limit, times `outer` iterations per step (plus the advection and
+    property update timed once)."""
+    from hydro_gb300 import capi
+    from oracle.oracle import Oracle
+    threads = threads or os.cpu_count() or 1
+    d, u0, q0, _ = workload(n, seed, "fp64", outer)
+    d.velocity_solver = capi.LINEAR_LU
+    d.pressure_solver = capi.LINEAR_GAUSS_SEIDEL
+    d.pressure_omega = 1.9
+    d.pressure_tolerance = 1e-3
+    # at rest the auto step is capped (dt_max), as in the GPU arm
+    dt = d.dt_max
+    times = []
+    t_rest_step = 0.0
+    for s in sweeps:
+        dd = d.copy()
+        dd.pressure_iters_limit = s - 1
+        oo = Oracle(dd, threads=threads)
+        oo.set_field(capi.F_VELOCITY, u0)
+        oo.set_field(capi.F_PARTIAL_DENSITY, q0)
+        oo.init_state()
+        oo.set_time_step(dt, dt * d.cfl_advection / d.cfl)
+        oo.start_step()
+        t0 = time.perf_counter()
+        oo.make_iteration()
+        times.append(time.perf_counter() - t0)
+        if s == sweeps[-1]:
+            oo.finish_step()
+            t0 = time.perf_counter()
+            oo.advection_step()
+            oo.update_properties()
+            t_rest_step = time.perf_counter() - t0
+    per_sweep = max((times[1] - times[0]) / (sweeps[1] - sweeps[0]), 0.0)
+    rest = max(times[0] - sweeps[0] * per_sweep, 0.0)
+    t_iter = rest + 1001 * per_sweep
+    t_step = outer * t_iter + t_rest_step
+    ncells = n ** 3
+    return {
+        "value": ncells / t_step / 1e6,
+        "unit": "Mcell-updates/s",
+        "cores": threads,
+        "kind": "port",
+        "sample": ("oracle (C restatement of the reference) at %d^3: 2 SIMPLE iterations with "
+                   "%d and %d SOR sweeps timed (%.2f s, %.2f s) -> %.3f s/sweep + %.2f s rest; "
+                   "step = %d iterations x (rest + 1001 sweeps, the reference's default limit) + "
+                   "advection/properties %.2f s" % (n, sweeps[0], sweeps[1], times[0], times[1],
+                                                    per_sweep, rest, outer, t_rest_step)),
+        "seconds_per_step": t_step,
+    }
+
+
+# ---------------------------------------------------------------- our arm --
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    from hydro_gb300 import capi
+    from hydro_gb300 import solver as S
+
+    torch.cuda.set_device(local)
+    try:
+        capi.load()
+    except RuntimeError:
+        from hydro_gb300 import build
+        build.build_library()
+        capi.load()
+    stream = torch.cuda.Stream()
+    d, u0, q0, drops = workload(args.n, args.seed + rank, args.precision, args.outer)
+    h = S.make(d, u0, q0, stream=stream.cuda_stream)
+    N = d.ncells
+
+    for _ in range(args.warmup):
+        h.step()
+    # timed region: device time with CUDA events on the library's stream
+    h.reset_profile()
+    h.set_profiling(True)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = S.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    stats = [h.step() for _ in range(args.steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    launches = S.launch_count() - l0
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    prof = h.profile()
+    h.set_profiling(False)
+    ms_max = max_over_ranks(ms, world)
+    value = world * N * args.steps / (ms_max / 1e3) / 1e6
+
+    # e2e: through the public C-ABI with host buffers; every step uploads the
+    # state from pinned host memory and reads the result back
+    nph = d.num_phases
+    pin_u = torch.empty(N * d.dim, dtype=torch.float64, pin_memory=True).numpy()
+    pin_q = torch.empty(N * nph, dtype=torch.float64, pin_memory=True).numpy()
+    pin_p = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    pin_u[:] = h.get_field(capi.F_VELOCITY)
+    pin_q[:] = h.get_field(capi.F_PARTIAL_DENSITY)
+    lib = capi.load()
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        lib.hydro_gpu_set_field(h.ctx, capi.F_VELOCITY, capi.TIME_CURR, dp(pin_u), pin_u.size)
+        lib.hydro_gpu_set_field(h.ctx, capi.F_PARTIAL_DENSITY, capi.TIME_CURR, dp(pin_q), pin_q.size)
+        h.step()
+        lib.hydro_gpu_get_field(h.ctx, capi.F_VELOCITY, capi.TIME_CURR, dp(pin_u), pin_u.size)
+        lib.hydro_gpu_get_field(h.ctx, capi.F_PRESSURE, capi.TIME_CURR, dp(pin_p), pin_p.size)
+        lib.hydro_gpu_get_field(h.ctx, capi.F_PARTIAL_DENSITY, capi.TIME_CURR, dp(pin_q), pin_q.size)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_value = world * N * args.steps / e2e_s / 1e6
+    h2d = (d.dim + nph) * N * 8
+    d2h = (d.dim + 1 + nph) * N * 8
+
+    # roofline of the dominant kernel group
+    peak, peak_kind = measured_peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
+    roof = None
+    if dom:
+        name, (nl, tms) = dom
+        table = ALG_BYTES_PER_CELL_FP32 if args.precision == "mixed" else ALG_BYTES_PER_CELL_FP64
+        per_cell = table.get(name)
+        eff = nl
+        if name in ("cg_spmv", "cg_update", "cg_dir"):
+            eff = sum(s["pressure_iterations"] for s in stats)
+        elif name == "mom_sweep":
+            eff = sum(s["velocity_sweeps"] for s in stats)
+        if per_cell:
+            bytes_launch = per_cell * N
+            achieved = bytes_launch * eff / (tms / 1e3) / 1e9
+            roof = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1),
+                    "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                    "traffic": None, "peak_source": peak_kind,
+                    "bytes_per_launch": bytes_launch, "launches": nl,
+                    "effective_launches": eff, "avg_launch_us": round(tms * 1e3 / max(eff, 1), 2)}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_sample(args.n, args.seed, args.outer)
+        except Exception as e:  # the baseline is reported, not required
+            cpu = {"error": str(e)}
+
+    if rank == 0:
+        out = {
+            "metric": "Mcell-updates/s",
+            "value": round(value, 4),
+            "unit": "Mcell-updates/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(ms_max / args.steps, 3),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f64+f32",
+            "data": "synthetic: seeded rising drops (%d drops), no external data" % len(drops),
+            "config": {
+                "workload": "rising_drops_%d^3" % args.n,
+                "cells": N,
+                "precision": args.precision,
+                "simple_iterations_per_step": args.outer,
+                "pressure_residual": 1e-8,
+                "seed": args.seed,
+                "parallelism": "replicas" if world > 1 else "single",
+                "l2": "working set %.1f GB > 129 MB L2" % (N * 8 * 80 / 1e9),
+            },
+            "e2e": {"value": round(e2e_value, 4), "unit": "Mcell-updates/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+            "step_stats": {
+                "outer_iterations": [s["outer_iterations"] for s in stats],
+                "pressure_iterations": [s["pressure_iterations"] for s in stats],
+                "velocity_sweeps": [s["velocity_sweeps"] for s in stats],
+                "pressure_residual_max": max(s["pressure_residual"] for s in stats),
+                "dt": stats[-1]["dt"],
+            },
+            "profile_ms": {k: round(v[1], 3) for k, v in sorted(prof.items())},
+        }
+        print(json.dumps(out))
+
+
+def run_reference(args, rank, world):
+    """The reference's algorithm on the host cores (the CPU oracle port; the
+    reference's own build needs its source tree, absent on the GPU host)."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    samples = []
+    for _ in range(args.warmup + args.steps):
+        samples.append(cpu_sample(args.n, args.seed, args.outer, threads=threads))
+    timed = samples[args.warmup:]
+    t_step = statistics.median(s["seconds_per_step"] for s in timed)
+    value = args.n ** 3 / t_step / 1e6
+    out = {
+        "impl": "reference",
+        "metric": "Mcell-updates/s",
+        "value": round(value, 6),
+        "unit": "Mcell-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(t_step * 1e3, 1),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic: seeded rising drops, no external data",
+        "config": {"workload": "rising_drops_%d^3" % args.n, "cells": args.n ** 3,
+                   "precision": "fp64", "simple_iterations_per_step": args.outer,
+                   "seed": args.seed},
+        "cpu_baseline": {"value": round(value, 6), "unit": "Mcell-updates/s", "cores": threads,
+                         "kind": "port", "sample": timed[-1]["sample"]},
+        "e2e": {"value": round(value, 6), "unit": "Mcell-updates/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--n", type=int, default=192)
+    ap.add_argument("--outer", type=int, default=5, help="SIMPLE iterations per step")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = init_dist()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -35,6 +35,10 @@ FP64, MIXED = range(2)
  F_PRESSURE_CORRECTION, F_DIAG_COEFF) = range(12)
 # enum hydro_layer (solver::Layers order)
 TIME_CURR, TIME_PREV, ITER_CURR, ITER_PREV = range(4)
+# enum hydro_prof_group
+PROF_GROUPS = ["vel_grad", "force", "mom_assemble", "mom_sweep", "rhie_chow", "pressure_rhs",
+               "cg_init", "cg_spmv", "cg_update", "cg_dir", "ir_residual", "correct",
+               "adv_faces", "adv_update", "props", "other"]
 
 
 class HydroDesc(ctypes.Structure):
@@ -263,6 +267,14 @@ def _declare(lib, prefix):
         lib.hydro_gpu_field_ptr.restype = I
         lib.hydro_desc_default.argtypes = [ctypes.POINTER(HydroDesc)]
         lib.hydro_desc_default.restype = I
+        lib.hydro_gpu_set_profiling.argtypes = [P, I]
+        lib.hydro_gpu_set_profiling.restype = I
+        lib.hydro_gpu_reset_profile.argtypes = [P]
+        lib.hydro_gpu_reset_profile.restype = I
+        lib.hydro_gpu_get_profile.argtypes = [P, I, ctypes.POINTER(ctypes.c_longlong), D]
+        lib.hydro_gpu_get_profile.restype = I
+        lib.hydro_gpu_get_launch_count.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
+        lib.hydro_gpu_get_launch_count.restype = I
     else:
         stencil.argtypes = [I, I, I, I, D, ctypes.c_double, ctypes.c_long,
                             ctypes.c_double, D, D, I, ctypes.c_double, I,

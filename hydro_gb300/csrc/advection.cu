@@ -152,6 +152,7 @@ cudaError_t launch_adv_faces(const Mesh& m, int nph, int stage, int nstages, con
     k_adv_faces<3><<<L.grid, L.block, 0, st>>>(m, g, nph, stage, nstages, F, q, qflux, L.kch);
   else
     k_adv_faces<2><<<L.grid, L.block, 0, st>>>(m, g, nph, stage, nstages, F, q, qflux, L.kch);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -166,6 +167,7 @@ cudaError_t launch_adv_update(const Mesh& m, int nph, int stage, int nstages, do
   else
     k_adv_update<2><<<L.grid, L.block, 0, st>>>(m, nph, stage, nstages, mdtv, qflux, qin, qout,
                                                L.kch);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -186,6 +188,7 @@ cudaError_t launch_adv_sharpen(const Mesh& m, int phase, double sharp, double am
     k_sharpen<2><<<L.grid, L.block, 0, st>>>(m, g, sharp, amax, dtv, F, q, Gc, qtmp, L.kch);
   }
   cudaMemcpyAsync(q, qtmp, sizeof(double) * m.nc, cudaMemcpyDeviceToDevice, st);
+  count_launches(2);
   return cudaGetLastError();
 }
 

@@ -16,8 +16,10 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <new>
 #include <utility>
+#include <vector>
 
 #include "../../include/hydro_gpu.h"
 #include "kernels.h"
@@ -25,7 +27,75 @@
 
 using namespace hg;
 
+namespace hg {
+static std::atomic<long long> g_launches{0};
+void count_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+}  // namespace hg
+
 namespace {
+
+// CUDA-event timing of kernel groups (hydro_gpu_set_profiling).
+struct EventProfiler : Profiler {
+  bool on = false;
+  cudaEvent_t open = nullptr;
+  struct Pair {
+    int g;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pair> pending;
+  std::vector<cudaEvent_t> pool;
+  long long launches[HYDRO_PROF_COUNT] = {};
+  double ms[HYDRO_PROF_COUNT] = {};
+  cudaEvent_t get() {
+    if (pool.empty()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      return e;
+    }
+    cudaEvent_t e = pool.back();
+    pool.pop_back();
+    return e;
+  }
+  void begin(int, cudaStream_t st) override {
+    if (!on) return;
+    open = get();
+    cudaEventRecord(open, st);
+  }
+  void end(int g, cudaStream_t st) override {
+    if (!on || !open) return;
+    cudaEvent_t e = get();
+    cudaEventRecord(e, st);
+    pending.push_back({g, open, e});
+    open = nullptr;
+  }
+  // after a stream synchronisation: fold finished pairs into the totals
+  void collect() {
+    for (auto& p : pending) {
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, p.a, p.b) == cudaSuccess) {
+        launches[p.g] += 1;
+        ms[p.g] += t;
+      }
+      pool.push_back(p.a);
+      pool.push_back(p.b);
+    }
+    pending.clear();
+  }
+  void reset() {
+    for (int g = 0; g < HYDRO_PROF_COUNT; ++g) {
+      launches[g] = 0;
+      ms[g] = 0.;
+    }
+  }
+  ~EventProfiler() {
+    for (auto& p : pending) {
+      cudaEventDestroy(p.a);
+      cudaEventDestroy(p.b);
+    }
+    for (auto e : pool) cudaEventDestroy(e);
+    if (open) cudaEventDestroy(open);
+  }
+};
 
 constexpr int kSweepChunk = 8;
 constexpr int kCgChunk = 32;
@@ -78,6 +148,7 @@ struct hydro_ctx {
   int status = HYDRO_OK;
   FluidCoef fc{};
   PhaseProps pp{};
+  EventProfiler prof;
 
   double* ucomp(int layer, int k) { return u[layer] + (size_t)k * m.nc; }
   C3 uc3(int layer) {
@@ -110,6 +181,15 @@ int cuda_status(cudaError_t e) {
 #define CK(expr)                              \
   do {                                        \
     cudaError_t e_ = (expr);                  \
+    if (e_ != cudaSuccess) return cuda_status(e_); \
+  } while (0)
+
+// CK with the launch bracketed by the profiler's events for `group`.
+#define PK(x, group, expr)                         \
+  do {                                             \
+    (x)->prof.begin(group, (x)->st);               \
+    cudaError_t e_ = (expr);                       \
+    (x)->prof.end(group, (x)->st);                 \
     if (e_ != cudaSuccess) return cuda_status(e_); \
   } while (0)
 
@@ -162,6 +242,7 @@ void bdf_coeffs(double dt, int second, double* co) {
 int sync_scalars(hydro_ctx* x) {
   CK(cudaMemcpyAsync(x->hds, x->pw.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, x->st));
   CK(cudaStreamSynchronize(x->st));
+  x->prof.collect();
   return HYDRO_OK;
 }
 
@@ -186,7 +267,8 @@ int solve_momentum(hydro_ctx* x, C3 up) {
       int k = queued + s;
       C3 din = x->vec<C3>(x->du[(k + 1) % 2], dim, x->m.nc);
       W3 dout = x->vec<W3>(x->du[k % 2], dim, x->m.nc);
-      CK(launch_mom_sweep(x->m, d.velocity_omega, d.velocity_tolerance, cc, resc, din, dout,
+      PK(x, HYDRO_PROF_MOM_SWEEP,
+         launch_mom_sweep(x->m, d.velocity_omega, d.velocity_tolerance, cc, resc, din, dout,
                           k == 0, x->pw.partials, x->pw.ds, x->st));
     }
     queued += n;
@@ -213,7 +295,8 @@ int solve_pressure(hydro_ctx* x) {
   int rc;
   if (!mixed) {
     w.limit = d.pressure_iters_limit;
-    CK(pcg_init(m, x->kf, x->prhs, x->pc, 0, d.pressure_tolerance, singular, w, x->st));
+    PK(x, HYDRO_PROF_CG_INIT,
+       pcg_init(m, x->kf, x->prhs, x->pc, 0, d.pressure_tolerance, singular, w, x->st));
     int queued = 0;
     for (;;) {
       int n = std::min(kCgChunk, std::max(1, d.pressure_iters_limit - queued));
@@ -245,7 +328,7 @@ int solve_pressure(hydro_ctx* x) {
       if (total >= d.pressure_iters_limit) break;
       w.limit = d.pressure_iters_limit - total;
       double tol = std::max(inner_tol, 0.5 * d.pressure_tolerance * sqrt(ff / rr));
-      CK(f32_pcg_init(m, tol, w, x->st));
+      PK(x, HYDRO_PROF_CG_INIT, f32_pcg_init(m, tol, w, x->st));
       int queued = 0;
       for (;;) {
         CK(f32_pcg_iterate(m, kCgChunk, w, x->st));
@@ -435,6 +518,7 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
     return HYDRO_ERR_CUDA;
   }
   x->pw.pin = desc->pressure_fixed_cell;
+  x->pw.prof = &x->prof;
   // constants
   for (int s = 0; s < 6; ++s)
     for (int k = 0; k < 3; ++k) x->fc.bcu[s][k] = (k < dim) ? desc->bc_velocity[s][k] : 0.;
@@ -503,14 +587,14 @@ int hydro_gpu_update_properties(hydro_ctx* x) {
   const Mesh& m = x->m;
   const hydro_desc& d = x->d;
   int dim = x->dim;
-  CK(launch_props(m, x->nph, x->pp, x->vec<CP<HYDRO_MAXPH>>(x->q, x->nph, m.nc),
+  PK(x, HYDRO_PROF_PROPS, launch_props(m, x->nph, x->pp, x->vec<CP<HYDRO_MAXPH>>(x->q, x->nph, m.nc),
                   x->vec<WP<HYDRO_MAXPH>>(x->alpha, x->nph, m.nc), x->rho_raw, x->rho, x->mu,
                   x->vec<W3>(x->force, dim, m.nc), x->Sv, x->Sm, x->st));
   auto smooth = [&](double* a, int times) -> int {
     double* in = a;
     double* tmp = x->smtmp;
     for (int r = 0; r < times; ++r) {
-      CK(launch_smooth(m, in, tmp, x->st));
+      PK(x, HYDRO_PROF_PROPS, launch_smooth(m, in, tmp, x->st));
       std::swap(in, tmp);
     }
     if (in != a) CK(cudaMemcpyAsync(a, in, sizeof(double) * m.nc, cudaMemcpyDeviceToDevice, x->st));
@@ -577,11 +661,11 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
   const double* Fip = x->F[HYDRO_ITER_PREV];
   C3 force = x->vec<C3>(x->force, dim, m.nc);
   C3 fres = x->vec<C3>(x->fres, dim, m.nc);
-  CK(launch_vel_grad(m, x->fc, up, x->vec<WP<9>>(x->G, dim * dim, m.nc), x->st));
-  CK(launch_force(m, x->fc, up, x->vec<CP<9>>(x->G, dim * dim, m.nc), pip, x->mu, x->rho, force,
+  PK(x, HYDRO_PROF_VEL_GRAD, launch_vel_grad(m, x->fc, up, x->vec<WP<9>>(x->G, dim * dim, m.nc), x->st));
+  PK(x, HYDRO_PROF_FORCE, launch_force(m, x->fc, up, x->vec<CP<9>>(x->G, dim * dim, m.nc), pip, x->mu, x->rho, force,
                   x->vec<C3>(x->stforce, dim, m.nc), x->Sv, x->Sm, x->vec<W3>(x->fo, dim, m.nc),
                   x->vec<W3>(x->fres, dim, m.nc), x->st));
-  CK(launch_mom_assemble(m, x->fc, up, x->uc3(HYDRO_TIME_CURR), x->uc3(HYDRO_TIME_PREV),
+  PK(x, HYDRO_PROF_MOM_ASSEMBLE, launch_mom_assemble(m, x->fc, up, x->uc3(HYDRO_TIME_CURR), x->uc3(HYDRO_TIME_PREV),
                          x->vec<CP<9>>(x->G, dim * dim, m.nc), Fip, x->rho, x->mu,
                          x->vec<C3>(x->fo, dim, m.nc), x->vec<WP<7>>(x->coef, 2 * dim + 1, m.nc),
                          x->vec<W3>(x->res, dim, m.nc), x->Dc, x->st));
@@ -589,11 +673,12 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
   if (rc) return rc;
   C3 du = x->vec<C3>(x->du[x->du_cur], dim, m.nc);
   x->cd_iter_count++;
-  CK(launch_rhie_chow(m, x->fc, up, du, pip, force, fres, x->Dc, x->Fs, x->kf, x->st));
-  CK(launch_pressure_rhs(m, x->Fs, nullptr, x->prhs, x->st));
+  PK(x, HYDRO_PROF_RHIE_CHOW,
+     launch_rhie_chow(m, x->fc, up, du, pip, force, fres, x->Dc, x->Fs, x->kf, x->st));
+  PK(x, HYDRO_PROF_PRESSURE_RHS, launch_pressure_rhs(m, x->Fs, nullptr, x->prhs, x->st));
   rc = solve_pressure(x);
   if (rc) return rc;
-  CK(launch_correct(m, x->fc, up, du, x->uw3(HYDRO_ITER_CURR), pip, x->p[HYDRO_ITER_CURR], x->pc,
+  PK(x, HYDRO_PROF_CORRECT, launch_correct(m, x->fc, up, du, x->uw3(HYDRO_ITER_CURR), pip, x->p[HYDRO_ITER_CURR], x->pc,
                     x->Dc, x->Fs, x->kf, x->F[HYDRO_ITER_CURR], x->pw.partials, x->pw.ds, x->st));
   rc = sync_scalars(x);
   if (rc) return rc;
@@ -671,9 +756,9 @@ int hydro_gpu_advection_step(hydro_ctx* x, int* substeps) {
   const double* F = x->F[HYDRO_TIME_CURR];
   while (x->adv_time < x->time - 0.5 * x->adv_dt) {
     for (int stage = 0; stage < nst; ++stage) {
-      CK(launch_adv_faces(m, x->nph, stage, nst, F, x->vec<CP<HYDRO_MAXPH>>(x->q, x->nph, m.nc),
+      PK(x, HYDRO_PROF_ADV_FACES, launch_adv_faces(m, x->nph, stage, nst, F, x->vec<CP<HYDRO_MAXPH>>(x->q, x->nph, m.nc),
                           x->vec<WP<HYDRO_MAXPH>>(x->qflux, x->nph, m.nf), x->st));
-      CK(launch_adv_update(m, x->nph, stage, nst, x->adv_dt,
+      PK(x, HYDRO_PROF_ADV_UPDATE, launch_adv_update(m, x->nph, stage, nst, x->adv_dt,
                            x->vec<CP<HYDRO_MAXPH>>(x->qflux, x->nph, m.nf),
                            x->vec<CP<HYDRO_MAXPH>>(x->q, x->nph, m.nc),
                            x->vec<WP<HYDRO_MAXPH>>(x->qtmp, x->nph, m.nc), x->st));
@@ -768,6 +853,37 @@ int hydro_gpu_calc_stat(hydro_ctx* x, hydro_stat* out) {
     out->pd_min[i] = h[8];
     out->pd_max[i] = h[9];
   }
+  return HYDRO_OK;
+}
+
+int hydro_gpu_set_profiling(hydro_ctx* x, int on) {
+  if (!x) return HYDRO_ERR_ARG;
+  CK(cudaStreamSynchronize(x->st));
+  x->prof.collect();
+  x->prof.on = on != 0;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_reset_profile(hydro_ctx* x) {
+  if (!x) return HYDRO_ERR_ARG;
+  CK(cudaStreamSynchronize(x->st));
+  x->prof.collect();
+  x->prof.reset();
+  return HYDRO_OK;
+}
+
+int hydro_gpu_get_profile(hydro_ctx* x, int group, long long* launches, double* ms) {
+  if (!x || group < 0 || group >= HYDRO_PROF_COUNT) return HYDRO_ERR_ARG;
+  CK(cudaStreamSynchronize(x->st));
+  x->prof.collect();
+  if (launches) *launches = x->prof.launches[group];
+  if (ms) *ms = x->prof.ms[group];
+  return HYDRO_OK;
+}
+
+int hydro_gpu_get_launch_count(long long* out) {
+  if (!out) return HYDRO_ERR_ARG;
+  *out = hg::g_launches.load();
   return HYDRO_OK;
 }
 

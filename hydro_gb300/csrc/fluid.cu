@@ -585,6 +585,7 @@ __global__ void k_init_flux(Mesh m, Geo g, FluidCoef fc, C3 u, double* F, int kc
       KERNEL<3><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);         \
     else                                                                 \
       KERNEL<2><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);         \
+    count_launches(1);                                                   \
     return cudaGetLastError();                                           \
   } while (0)
 
@@ -604,6 +605,7 @@ cudaError_t launch_start_step(const Mesh& m, double ge, W3 u_ic, C3 u_tc, C3 u_t
     k_axpy_extrap<<<nb, NT, 0, st>>>(m.nc, ge, u_ic.a[k], u_tc.a[k], u_tp.a[k]);
   k_axpy_extrap<<<nb, NT, 0, st>>>(m.nc, ge, p_ic, p_tc, p_tp);
   k_axpy_extrap<<<flat_blocks(m.nf), NT, 0, st>>>(m.nf, ge, F_ic, F_tc, F_tp);
+  count_launches(m.dim + 2);
   return cudaGetLastError();
 }
 
@@ -659,12 +661,14 @@ cudaError_t launch_correct(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du,
 cudaError_t launch_auto_dt(const Mesh& m, const double* F, double* partials, DevScalars* ds,
                            cudaStream_t st) {
   k_auto_dt<<<flat_blocks(m.nf), dim3(BX, BY), 0, st>>>(m.nf, m.V, F, partials, ds);
+  count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_nan_count(long long n, const double* a, double* partials, DevScalars* ds,
                              cudaStream_t st) {
   k_nan_count<<<flat_blocks(n), dim3(BX, BY), 0, st>>>(n, a, partials, ds);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -690,6 +694,7 @@ cudaError_t launch_stforce(const Mesh& m, double sigma, const double* alpha1, W3
     k_scal_grad<2><<<L.grid, L.block, 0, st>>>(m, g, alpha1, G, L.kch);
     k_stforce<2><<<L.grid, L.block, 0, st>>>(m, g, sigma, Gc, out, L.kch);
   }
+  count_launches(2);
   return cudaGetLastError();
 }
 

@@ -124,6 +124,15 @@ cudaError_t launch_adv_sharpen(const Mesh& m, int phase, double sharp, double am
 // --------------------------------------------------------------- linear --
 // Pressure-correction solve on face couplings kf (coupling -kf between the
 // cells of an inner face, diagonal sum kf + shift), A x = f.
+// Optional timing of kernel groups with CUDA events (measurement only).
+struct Profiler {
+  virtual void begin(int group, cudaStream_t st) = 0;
+  virtual void end(int group, cudaStream_t st) = 0;
+  virtual ~Profiler() {}
+};
+// Kernel launches issued by this library since load (all contexts).
+void count_launches(int n);
+
 struct PcgWork {
   double *r, *z, *p, *Ap, *dg, *idg;                     // FP64 vectors
   float *r32, *z32, *p32, *Ap32, *dg32, *idg32, *x32, *kf32;  // FP32 inner solve
@@ -131,6 +140,7 @@ struct PcgWork {
   DevScalars* ds;
   long long pin;     // pinned cell or -1
   int limit;         // iteration limit of one (inner) solve
+  Profiler* prof;    // may be null
 };
 // Diagonal and its reciprocal (plus FP32 copies of couplings when fp32).
 cudaError_t pcg_prepare(const Mesh& m, const double* kf, double shift, PcgWork& w, int fp32,

@@ -21,6 +21,8 @@
 
 namespace hg {
 
+enum { PG_CG_SPMV = 7, PG_CG_UPDATE = 8, PG_CG_DIR = 9, PG_IR_RESIDUAL = 10 };
+
 namespace {
 
 // Matrix-free stencil product (A p)_c = diag_c p_c - sum_f kf_f p_nb with a
@@ -242,6 +244,7 @@ cudaError_t pcg_prepare(const Mesh& m, const double* kf, double shift, PcgWork& 
       k_diag<2, float><<<L.grid, L.block, 0, st>>>(m, kf, shift, w.pin, w.dg32, w.idg32, w.kf32,
                                                    L.kch);
   }
+  count_launches(fp32 ? 2 : 1);
   return cudaGetLastError();
 }
 
@@ -249,6 +252,7 @@ cudaError_t mean_sum(const Mesh& m, const double* f, PcgWork& w, cudaStream_t st
   k_sum<double><<<flat_blocks_l(m.nc), dim3(BX, BY), 0, st>>>(m.nc, f, w.partials,
                                                              &w.ds->red[RS_MEAN],
                                                              &w.ds->ticket[TK_MEAN]);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -257,6 +261,7 @@ cudaError_t sub_mean(const Mesh& m, double* x, PcgWork& w, cudaStream_t st) {
                                                              &w.ds->red[RS_XMEAN],
                                                              &w.ds->ticket[TK_MEAN2]);
   k_sub_mean<<<flat_blocks_l(m.nc), NT, 0, st>>>(m.nc, x, &w.ds->red[RS_XMEAN]);
+  count_launches(2);
   return cudaGetLastError();
 }
 
@@ -271,6 +276,7 @@ cudaError_t pcg_init(const Mesh& m, const double* kf, const double* f, double* x
   LAUNCH_DIM_T(k_cg_init, double, m, kf, w.dg, w.idg, f, msum, x, use_guess, w.pin, w.r, w.z,
              w.p, tol, w.partials, w.ds);
   if (!use_guess) cudaMemsetAsync(x, 0, sizeof(double) * m.nc, st);
+  count_launches(singular ? 2 : 1);
   return cudaGetLastError();
 }
 
@@ -279,11 +285,18 @@ cudaError_t pcg_iterate(const Mesh& m, const double* kf, double* x, int chunk, P
   Launch L = cell_launch(m);
   int fb = flat_blocks_l(m.nc);
   for (int it = 0; it < chunk; ++it) {
+    if (w.prof) w.prof->begin(PG_CG_SPMV, st);
     LAUNCH_DIM_T(k_cg_spmv, double, m, kf, w.dg, w.p, w.Ap, w.pin, w.partials, w.ds);
+    if (w.prof) w.prof->end(PG_CG_SPMV, st);
+    if (w.prof) w.prof->begin(PG_CG_UPDATE, st);
     k_cg_update<double, double><<<fb, dim3(BX, BY), 0, st>>>(m.nc, x, w.r, w.z, w.p, w.Ap, w.idg,
                                                              w.partials, w.ds, w.limit);
+    if (w.prof) w.prof->end(PG_CG_UPDATE, st);
+    if (w.prof) w.prof->begin(PG_CG_DIR, st);
     k_cg_dir<double><<<fb, NT, 0, st>>>(m.nc, w.z, w.p, w.ds);
+    if (w.prof) w.prof->end(PG_CG_DIR, st);
   }
+  count_launches(3 * chunk);
   return cudaGetLastError();
 }
 
@@ -292,7 +305,10 @@ cudaError_t ir_residual(const Mesh& m, const double* kf, const double* f, const 
                         int singular, PcgWork& w, cudaStream_t st) {
   Launch L = cell_launch(m);
   const double* msum = singular ? &w.ds->red[RS_MEAN] : nullptr;
+  if (w.prof) w.prof->begin(PG_IR_RESIDUAL, st);
   LAUNCH_DIM(k_ir_residual, m, kf, w.dg, f, msum, x, w.pin, w.r, w.partials, w.ds);
+  if (w.prof) w.prof->end(PG_IR_RESIDUAL, st);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -301,6 +317,7 @@ cudaError_t f32_pcg_init(const Mesh& m, double tol, PcgWork& w, cudaStream_t st)
   cudaMemsetAsync(w.x32, 0, sizeof(float) * m.nc, st);
   LAUNCH_DIM_T(k_cg_init, float, m, w.kf32, w.dg32, w.idg32, w.r, (const double*)nullptr,
              w.x32, 0, w.pin, w.r32, w.z32, w.p32, tol, w.partials, w.ds);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -308,12 +325,19 @@ cudaError_t f32_pcg_iterate(const Mesh& m, int chunk, PcgWork& w, cudaStream_t s
   Launch L = cell_launch(m);
   int fb = flat_blocks_l(m.nc);
   for (int it = 0; it < chunk; ++it) {
+    if (w.prof) w.prof->begin(PG_CG_SPMV, st);
     LAUNCH_DIM_T(k_cg_spmv, float, m, w.kf32, w.dg32, w.p32, w.Ap32, w.pin, w.partials, w.ds);
+    if (w.prof) w.prof->end(PG_CG_SPMV, st);
+    if (w.prof) w.prof->begin(PG_CG_UPDATE, st);
     k_cg_update<float, float><<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.x32, w.r32, w.z32, w.p32,
                                                            w.Ap32, w.idg32, w.partials, w.ds,
                                                            w.limit);
+    if (w.prof) w.prof->end(PG_CG_UPDATE, st);
+    if (w.prof) w.prof->begin(PG_CG_DIR, st);
     k_cg_dir<float><<<fb, NT, 0, st>>>(m.nc, w.z32, w.p32, w.ds);
+    if (w.prof) w.prof->end(PG_CG_DIR, st);
   }
+  count_launches(3 * chunk);
   return cudaGetLastError();
 }
 
@@ -335,6 +359,7 @@ __global__ void k_scale(long long n, double* a, double s) {
 
 cudaError_t scale_vector(long long n, double* a, double s, cudaStream_t st) {
   k_scale<<<flat_blocks_l(n), NT, 0, st>>>(n, a, s);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -358,11 +383,13 @@ __global__ void k_pin_rhs(Mesh m, const double* kf, double* f, long long pin, do
 cudaError_t pin_rhs(const Mesh& m, const double* kf, double* f, long long pin, double value,
                     cudaStream_t st) {
   k_pin_rhs<<<1, 32, 0, st>>>(m, kf, f, pin, value);
+  count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t f32_accumulate(const Mesh& m, double* x, PcgWork& w, cudaStream_t st) {
   k_accumulate<<<flat_blocks_l(m.nc), NT, 0, st>>>(m.nc, x, w.x32);
+  count_launches(1);
   return cudaGetLastError();
 }
 

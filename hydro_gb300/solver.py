@@ -160,6 +160,29 @@ class Hydro:
         self._call("calc_stat", ctypes.byref(s))
         return s
 
+    # ---- measurement hooks
+    def set_profiling(self, on):
+        self._call("set_profiling", 1 if on else 0)
+
+    def reset_profile(self):
+        self._call("reset_profile")
+
+    def profile(self):
+        out = {}
+        for g, name in enumerate(capi.PROF_GROUPS):
+            n = ctypes.c_longlong()
+            ms = ctypes.c_double()
+            self._call("get_profile", g, ctypes.byref(n), ctypes.byref(ms))
+            if n.value:
+                out[name] = (n.value, ms.value)
+        return out
+
+
+def launch_count():
+    n = ctypes.c_longlong()
+    capi.load().hydro_gpu_get_launch_count(ctypes.byref(n))
+    return n.value
+
 
 def make(desc, u0, q0, stream=None):
     """Create a context, upload the initial velocity and partial densities

@@ -251,6 +251,24 @@ int hydro_gpu_stencil_solve(int dim, int nx, int ny, int nz,
                             void* workspace, void* stream,
                             int* iterations, double* residual);
 
+/* Measurement hooks (no counterpart in the reference; the reference's
+ * MultiTimer labels fluid.0..fluid.8, fluid.hpp:603-1061, play this role
+ * there).  With profiling on, every launch of the groups below is
+ * bracketed by CUDA events on the context's stream; get_profile returns
+ * the launches and summed device milliseconds of one group since the last
+ * reset.  The launch count covers every kernel this library enqueued. */
+enum hydro_prof_group {
+  HYDRO_PROF_VEL_GRAD = 0, HYDRO_PROF_FORCE, HYDRO_PROF_MOM_ASSEMBLE, HYDRO_PROF_MOM_SWEEP,
+  HYDRO_PROF_RHIE_CHOW, HYDRO_PROF_PRESSURE_RHS, HYDRO_PROF_CG_INIT, HYDRO_PROF_CG_SPMV,
+  HYDRO_PROF_CG_UPDATE, HYDRO_PROF_CG_DIR, HYDRO_PROF_IR_RESIDUAL, HYDRO_PROF_CORRECT,
+  HYDRO_PROF_ADV_FACES, HYDRO_PROF_ADV_UPDATE, HYDRO_PROF_PROPS, HYDRO_PROF_OTHER,
+  HYDRO_PROF_COUNT
+};
+int hydro_gpu_set_profiling(hydro_ctx* ctx, int on);
+int hydro_gpu_reset_profile(hydro_ctx* ctx);
+int hydro_gpu_get_profile(hydro_ctx* ctx, int group, long long* launches, double* ms);
+int hydro_gpu_get_launch_count(long long* out);
+
 #ifdef __cplusplus
 }
 #endif
