@@ -32,7 +32,8 @@ FP64, MIXED = range(2)
 # enum hydro_field
 (F_VELOCITY, F_PRESSURE, F_VOLUME_FLUX, F_PARTIAL_DENSITY, F_VOLUME_FRACTION,
  F_DENSITY, F_VISCOSITY, F_FORCE, F_VOLUME_SOURCE, F_MASS_SOURCE,
- F_PRESSURE_CORRECTION, F_DIAG_COEFF) = range(12)
+ F_PRESSURE_CORRECTION, F_DIAG_COEFF, F_SURFACE_FORCE) = range(13)
+VECTOR_FIELDS = (F_VELOCITY, F_FORCE, F_SURFACE_FORCE)
 # enum hydro_layer (solver::Layers order)
 TIME_CURR, TIME_PREV, ITER_CURR, ITER_PREV = range(4)
 # enum hydro_prof_group
@@ -249,6 +250,7 @@ def _declare(lib, prefix):
         "set_time_step": [P, ctypes.c_double, ctypes.c_double],
         "get_time": [P, D, D],
         "advection_step": [P, ctypes.POINTER(I)],
+        "advection_substep": [P],
         "step": [P, ctypes.POINTER(StepStats)],
         "calc_stat": [P, ctypes.POINTER(Stat)],
     }

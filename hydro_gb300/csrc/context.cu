@@ -370,6 +370,7 @@ int fluid_field(hydro_ctx* x, int field, int layer, double** ptr, long long* n) 
     case HYDRO_FIELD_MASS_SOURCE: *ptr = x->Sm; return HYDRO_OK;
     case HYDRO_FIELD_PRESSURE_CORRECTION: *ptr = x->pc; return HYDRO_OK;
     case HYDRO_FIELD_DIAG_COEFF: *ptr = x->Dc; return HYDRO_OK;
+    case HYDRO_FIELD_SURFACE_FORCE: *ptr = x->stforce; *n = m.nc * x->dim; return HYDRO_OK;
   }
   return HYDRO_ERR_ARG;
 }
@@ -567,6 +568,15 @@ int hydro_gpu_set_field(hydro_ctx* x, int field, int layer, const double* src, s
   if ((long long)n != len) return HYDRO_ERR_ARG;
   CK(cudaMemcpyAsync(p, src, sizeof(double) * n, cudaMemcpyHostToDevice, x->st));
   CK(cudaStreamSynchronize(x->st));
+  // caller-supplied sources enter the force sum and the pressure rows
+  // (fluid.hpp:861-869, 985-988)
+  if (field == HYDRO_FIELD_VOLUME_SOURCE || field == HYDRO_FIELD_MASS_SOURCE) {
+    for (size_t i = 0; i < n; ++i)
+      if (src[i] != 0.) {
+        x->fc.sources = 1;
+        break;
+      }
+  }
   return HYDRO_OK;
 }
 
@@ -675,7 +685,7 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
   x->cd_iter_count++;
   PK(x, HYDRO_PROF_RHIE_CHOW,
      launch_rhie_chow(m, x->fc, up, du, pip, force, fres, x->Dc, x->Fs, x->kf, x->st));
-  PK(x, HYDRO_PROF_PRESSURE_RHS, launch_pressure_rhs(m, x->Fs, nullptr, x->prhs, x->st));
+  PK(x, HYDRO_PROF_PRESSURE_RHS, launch_pressure_rhs(m, x->Fs, x->fc.sources ? x->Sv : nullptr, x->prhs, x->st));
   rc = solve_pressure(x);
   if (rc) return rc;
   PK(x, HYDRO_PROF_CORRECT, launch_correct(m, x->fc, up, du, x->uw3(HYDRO_ITER_CURR), pip, x->p[HYDRO_ITER_CURR], x->pc,
@@ -734,9 +744,9 @@ int hydro_gpu_get_auto_time_step(hydro_ctx* x, double* out) {
 }
 
 int hydro_gpu_set_time_step(hydro_ctx* x, double dt, double dta) {
-  if (!x || !(dt > 0.) || !(dta > 0.)) return HYDRO_ERR_ARG;
-  x->dt = dt;
-  x->adv_dt = dta;
+  if (!x || isnan(dt) || isnan(dta)) return HYDRO_ERR_ARG;
+  if (dt > 0.) x->dt = dt;
+  if (dta > 0.) x->adv_dt = dta;
   return HYDRO_OK;
 }
 
@@ -747,34 +757,42 @@ int hydro_gpu_get_time(hydro_ctx* x, double* ft, double* at) {
   return HYDRO_OK;
 }
 
-int hydro_gpu_advection_step(hydro_ctx* x, int* substeps) {
+int hydro_gpu_advection_substep(hydro_ctx* x) {
   if (!x) return HYDRO_ERR_ARG;
   const Mesh& m = x->m;
   const hydro_desc& d = x->d;
   int nst = d.tvd_split ? x->dim : 1;
-  int ns = 0;
   const double* F = x->F[HYDRO_TIME_CURR];
+  for (int stage = 0; stage < nst; ++stage) {
+    PK(x, HYDRO_PROF_ADV_FACES,
+       launch_adv_faces(m, x->nph, stage, nst, F, x->vec<CP<HYDRO_MAXPH>>(x->q, x->nph, m.nc),
+                        x->vec<WP<HYDRO_MAXPH>>(x->qflux, x->nph, m.nf), x->st));
+    PK(x, HYDRO_PROF_ADV_UPDATE,
+       launch_adv_update(m, x->nph, stage, nst, x->adv_dt,
+                         x->vec<CP<HYDRO_MAXPH>>(x->qflux, x->nph, m.nf),
+                         x->vec<CP<HYDRO_MAXPH>>(x->q, x->nph, m.nc),
+                         x->vec<WP<HYDRO_MAXPH>>(x->qtmp, x->nph, m.nc), x->st));
+    std::swap(x->q, x->qtmp);
+  }
+  if (fabs(d.sharp) > 1e-10) {
+    for (int i = 0; i < x->nph; ++i)
+      CK(launch_adv_sharpen(m, i, d.sharp, d.density[i], x->adv_dt, F, x->q + (size_t)i * m.nc,
+                            x->smtmp, x->vec<W3>(x->G, x->dim, m.nc), x->Fs, x->st));
+  }
+  x->adv_time += x->adv_dt;
+  CK(cudaGetLastError());
+  return HYDRO_OK;
+}
+
+int hydro_gpu_advection_step(hydro_ctx* x, int* substeps) {
+  if (!x) return HYDRO_ERR_ARG;
+  int ns = 0;
   while (x->adv_time < x->time - 0.5 * x->adv_dt) {
-    for (int stage = 0; stage < nst; ++stage) {
-      PK(x, HYDRO_PROF_ADV_FACES, launch_adv_faces(m, x->nph, stage, nst, F, x->vec<CP<HYDRO_MAXPH>>(x->q, x->nph, m.nc),
-                          x->vec<WP<HYDRO_MAXPH>>(x->qflux, x->nph, m.nf), x->st));
-      PK(x, HYDRO_PROF_ADV_UPDATE, launch_adv_update(m, x->nph, stage, nst, x->adv_dt,
-                           x->vec<CP<HYDRO_MAXPH>>(x->qflux, x->nph, m.nf),
-                           x->vec<CP<HYDRO_MAXPH>>(x->q, x->nph, m.nc),
-                           x->vec<WP<HYDRO_MAXPH>>(x->qtmp, x->nph, m.nc), x->st));
-      std::swap(x->q, x->qtmp);
-    }
-    if (fabs(d.sharp) > 1e-10) {
-      for (int i = 0; i < x->nph; ++i)
-        CK(launch_adv_sharpen(m, i, d.sharp, d.density[i], x->adv_dt, F,
-                              x->q + (size_t)i * m.nc, x->smtmp, x->vec<W3>(x->G, x->dim, m.nc),
-                              x->Fs, x->st));
-    }
-    x->adv_time += x->adv_dt;
+    int rc = hydro_gpu_advection_substep(x);
+    if (rc) return rc;
     ++ns;
   }
   if (substeps) *substeps = ns;
-  CK(cudaGetLastError());
   return HYDRO_OK;
 }
 

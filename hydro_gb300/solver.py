@@ -57,7 +57,7 @@ class Hydro:
     def _size(self, field):
         if field == capi.F_VOLUME_FLUX:
             return self.nf
-        if field in (capi.F_VELOCITY, capi.F_FORCE):
+        if field in capi.VECTOR_FIELDS:
             return self.nc * self.dim
         if field in (capi.F_PARTIAL_DENSITY, capi.F_VOLUME_FRACTION):
             return self.nc * self.desc.num_phases

@@ -99,7 +99,8 @@ enum hydro_field {
   HYDRO_FIELD_VOLUME_SOURCE = 8,   /* cells */
   HYDRO_FIELD_MASS_SOURCE = 9,     /* cells */
   HYDRO_FIELD_PRESSURE_CORRECTION = 10, /* cells: last p' solved */
-  HYDRO_FIELD_DIAG_COEFF = 11      /* cells: last momentum diagonal D_c (fluid.hpp:876-883) */
+  HYDRO_FIELD_DIAG_COEFF = 11,     /* cells: last momentum diagonal D_c (fluid.hpp:876-883) */
+  HYDRO_FIELD_SURFACE_FORCE = 12   /* cells x dim: surface-tension force (p_fc_stforce) */
 };
 
 /* Same order as solver::Layers (solver.hpp:762). */
@@ -213,11 +214,15 @@ int hydro_gpu_get_convergence_indicator(hydro_ctx* ctx, double* out);
 int hydro_gpu_get_iteration_count(hydro_ctx* ctx, int* out);
 int hydro_gpu_is_converged(hydro_ctx* ctx, int* out);
 int hydro_gpu_get_auto_time_step(hydro_ctx* ctx, double* out);
+/* A value <= 0 leaves that time step unchanged. */
 int hydro_gpu_set_time_step(hydro_ctx* ctx, double dt, double dt_advection);
 int hydro_gpu_get_time(hydro_ctx* ctx, double* fluid_time, double* advection_time);
 /* All advection substeps that bring advection time up to fluid time
  * (hydro2d.hpp:1596-1604). */
 int hydro_gpu_advection_step(hydro_ctx* ctx, int* substeps);
+/* Exactly one substep: AdvectionSolverMultiExplicit StartStep +
+ * MakeIteration + FinishStep (advection.hpp:417-545). */
+int hydro_gpu_advection_substep(hydro_ctx* ctx);
 
 /* One full time step: dt_auto, SIMPLE loop to convergence, advection
  * substeps, property update.  stats may be NULL. */

@@ -636,6 +636,9 @@ static int field_arrays(oracle_ctx* x, int field, int layer, double** arr,
     case HYDRO_FIELD_MASS_SOURCE: arr[0] = x->Sm; *narr = 1; return HYDRO_OK;
     case HYDRO_FIELD_PRESSURE_CORRECTION: arr[0] = x->pcorr; *narr = 1; return HYDRO_OK;
     case HYDRO_FIELD_DIAG_COEFF: arr[0] = x->Dc; *narr = 1; return HYDRO_OK;
+    case HYDRO_FIELD_SURFACE_FORCE:
+      for (int d = 0; d < dim; ++d) arr[d] = x->stforce[d];
+      *narr = dim; return HYDRO_OK;
   }
   return HYDRO_ERR_ARG;
 }
@@ -1350,6 +1353,12 @@ static void advection_iteration(oracle_ctx* x) {
 }
 
 /* hydro2d.hpp:1596-1604: substeps until advection time reaches fluid time. */
+int oracle_advection_substep(oracle_ctx* x) {
+  advection_iteration(x);
+  x->adv_time += x->adv_dt;
+  return HYDRO_OK;
+}
+
 int oracle_advection_step(oracle_ctx* x, int* substeps) {
   int ns = 0;
   while (x->adv_time < x->time - 0.5 * x->adv_dt) {

@@ -40,6 +40,7 @@ int oracle_get_auto_time_step(oracle_ctx* ctx, double* out);
 int oracle_set_time_step(oracle_ctx* ctx, double dt, double dt_advection);
 int oracle_get_time(oracle_ctx* ctx, double* fluid_time, double* advection_time);
 int oracle_advection_step(oracle_ctx* ctx, int* substeps);
+int oracle_advection_substep(oracle_ctx* ctx);
 int oracle_step(oracle_ctx* ctx, hydro_step_stats* stats);
 int oracle_calc_stat(oracle_ctx* ctx, hydro_stat* out);
 /* GetSmoothField (solver.hpp:636-656) on a cell array, in place. */
