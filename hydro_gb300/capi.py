@@ -265,6 +265,10 @@ def _declare(lib, prefix):
                             ctypes.POINTER(I), D]
         lib.hydro_gpu_stencil_workspace_size.argtypes = [I, I, I, I]
         lib.hydro_gpu_stencil_workspace_size.restype = ctypes.c_size_t
+        lib.hydro_gpu_stencil_solve_noalloc.argtypes = [
+            I, I, I, I, P, ctypes.c_double, ctypes.c_long, ctypes.c_double, P, P, I,
+            ctypes.c_double, I, P, ctypes.POINTER(I), D]
+        lib.hydro_gpu_stencil_solve_noalloc.restype = I
         lib.hydro_gpu_field_ptr.argtypes = [P, I, I, ctypes.POINTER(D)]
         lib.hydro_gpu_field_ptr.restype = I
         lib.hydro_desc_default.argtypes = [ctypes.POINTER(HydroDesc)]

@@ -256,6 +256,39 @@ int hydro_gpu_stencil_solve(int dim, int nx, int ny, int nz,
                             void* workspace, void* stream,
                             int* iterations, double* residual);
 
+/* hydro_gpu_stencil_solve without a workspace argument, for callers that
+ * cannot allocate device memory.  No counterpart in the reference (whose
+ * solvers allocate host vectors on every call, linear.hpp:686).
+ *
+ * Who needs it: code that may not call cudaMalloc -- a plugin running
+ * inside a host application that owns and budgets all device memory, or a
+ * latency-critical loop where cudaMalloc's possible implicit device
+ * synchronisation or out-of-memory failure is not acceptable.  The caller
+ * still passes the inputs and the output (face_coeff, rhs, x: device
+ * pointers); everything else the solve needs comes from one file-scope
+ * device array of this library, 18,875,392 bytes (18 MiB), which every GPU
+ * that loads the library holds until the process exits.
+ *
+ * Limits and rules:
+ *  - at most HYDRO_NOALLOC_MAX_CELLS cells; larger blocks return
+ *    HYDRO_ERR_ARG without touching the GPU;
+ *  - the first call on each device looks up the array's device address
+ *    (cudaGetSymbolAddress, with that device current) and caches it; make
+ *    that first call before any stream capture;
+ *  - all calls share the one array, which keeps the last call's contents
+ *    (each call clears what must start at zero itself); calls that overlap
+ *    on the GPU -- two streams or host threads at once -- race on it, so
+ *    the caller must serialise them;
+ *  - it calls no cudaMalloc, cudaFree or allocating library routine.
+ * Arguments, results and status codes are those of hydro_gpu_stencil_solve. */
+#define HYDRO_NOALLOC_MAX_CELLS 262144
+int hydro_gpu_stencil_solve_noalloc(int dim, int nx, int ny, int nz,
+                                    const double* face_coeff, double shift,
+                                    long pinned_cell, double pinned_value,
+                                    const double* rhs, double* x, int use_guess,
+                                    double tolerance, int iters_limit, void* stream,
+                                    int* iterations, double* residual);
+
 /* Measurement hooks (no counterpart in the reference; the reference's
  * MultiTimer labels fluid.0..fluid.8, fluid.hpp:603-1061, play this role
  * there).  With profiling on, every launch of the groups below is
