@@ -129,7 +129,7 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def workload(n, seed, precision, outer):
+def workload(n, seed, precision, outer, solver="cg"):
     from hydro_gb300 import capi, cases
     d, u0, q0, drops = cases.rising_drops(n=n, seed=seed, dt_max=2e-3)
     d.convergence_tolerance = 0.0
@@ -139,6 +139,7 @@ def workload(n, seed, precision, outer):
     d.pressure_tolerance = 1e-8
     d.pressure_iters_limit = 20000
     d.precision = capi.MIXED if precision == "mixed" else capi.FP64
+    d.pressure_solver = capi.LINEAR_MGCG if solver == "mgcg" else capi.LINEAR_CG
     return d, u0, q0, drops
 
 
@@ -262,7 +263,7 @@ def run_ours(args, rank, world, local):
         build.build_library()
         capi.load()
     stream = torch.cuda.Stream()
-    d, u0, q0, drops = workload(args.n, args.seed + rank, args.precision, args.outer)
+    d, u0, q0, drops = workload(args.n, args.seed + rank, args.precision, args.outer, args.solver)
     h = S.make(d, u0, q0, stream=stream.cuda_stream)
     N = d.ncells
 
@@ -431,6 +432,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--solver", default="cg", choices=["cg", "mgcg"],
+                    help="pressure: Jacobi-PCG or multigrid-PCG (mixed only)")
     ap.add_argument("--n", type=int, default=192)
     ap.add_argument("--outer", type=int, default=5, help="SIMPLE iterations per step")
     ap.add_argument("--seed", type=int, default=0)

@@ -24,9 +24,9 @@ XM, XP, YM, YP, ZM, ZP = range(6)
 # enum hydro_bc_kind
 BC_WALL, BC_INLET, BC_OUTLET = range(3)
 # enum hydro_linear
-LINEAR_GAUSS_SEIDEL, LINEAR_JACOBI, LINEAR_CG, LINEAR_LU = range(4)
+LINEAR_GAUSS_SEIDEL, LINEAR_JACOBI, LINEAR_CG, LINEAR_LU, LINEAR_MGCG = range(5)
 LINEAR_NAMES = {"gauss_seidel": LINEAR_GAUSS_SEIDEL, "jacobi": LINEAR_JACOBI,
-                "cg": LINEAR_CG, "lu": LINEAR_LU}
+                "cg": LINEAR_CG, "lu": LINEAR_LU, "mgcg": LINEAR_MGCG}
 # enum hydro_precision
 FP64, MIXED = range(2)
 # enum hydro_field
@@ -39,7 +39,7 @@ TIME_CURR, TIME_PREV, ITER_CURR, ITER_PREV = range(4)
 # enum hydro_prof_group
 PROF_GROUPS = ["vel_grad", "force", "mom_assemble", "mom_sweep", "rhie_chow", "pressure_rhs",
                "cg_init", "cg_spmv", "cg_update", "cg_dir", "ir_residual", "correct",
-               "adv_faces", "adv_update", "props", "other"]
+               "adv_faces", "adv_update", "props", "mg_vcycle", "other"]
 
 
 class HydroDesc(ctypes.Structure):

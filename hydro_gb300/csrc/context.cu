@@ -99,6 +99,7 @@ struct EventProfiler : Profiler {
 
 constexpr int kSweepChunk = 8;
 constexpr int kCgChunk = 32;
+constexpr int kMgChunk = 4;
 
 struct Arena {
   char* base = nullptr;
@@ -149,6 +150,7 @@ struct hydro_ctx {
   FluidCoef fc{};
   PhaseProps pp{};
   EventProfiler prof;
+  MgWork mg{};
 
   double* ucomp(int layer, int k) { return u[layer] + (size_t)k * m.nc; }
   C3 uc3(int layer) {
@@ -311,12 +313,15 @@ int solve_pressure(hydro_ctx* x) {
     double ff = x->hds->red[RS_PCG_FF];
     x->p_res = ff > 0. ? sqrt(x->hds->red[RS_PCG_RR] / ff) : 0.;
   } else {
-    // FP64 iterative refinement around FP32 PCG
+    // FP64 iterative refinement around an FP32 PCG (Jacobi or multigrid
+    // preconditioned)
+    const bool mgcg = d.pressure_solver == HYDRO_LINEAR_MGCG;
+    if (mgcg) CK(mg_setup(x->mg, w, x->st));
     if (singular) CK(mean_sum(m, x->prhs, w, x->st));
     CK(cudaMemsetAsync(x->pc, 0, sizeof(double) * m.nc, x->st));
     double ff = -1.;
     int total = 0;
-    const double inner_tol = 1e-4;
+    const double inner_tol = mgcg ? 1e-5 : 1e-4;
     for (int outer = 0; outer < 50; ++outer) {
       CK(ir_residual(m, x->kf, x->prhs, x->pc, singular, w, x->st));
       rc = sync_scalars(x);
@@ -328,11 +333,18 @@ int solve_pressure(hydro_ctx* x) {
       if (total >= d.pressure_iters_limit) break;
       w.limit = d.pressure_iters_limit - total;
       double tol = std::max(inner_tol, 0.5 * d.pressure_tolerance * sqrt(ff / rr));
-      PK(x, HYDRO_PROF_CG_INIT, f32_pcg_init(m, tol, w, x->st));
+      if (mgcg)
+        PK(x, HYDRO_PROF_CG_INIT, mgcg_init(m, tol, w, x->mg, x->st));
+      else
+        PK(x, HYDRO_PROF_CG_INIT, f32_pcg_init(m, tol, w, x->st));
       int queued = 0;
+      const int chunk = mgcg ? kMgChunk : kCgChunk;
       for (;;) {
-        CK(f32_pcg_iterate(m, kCgChunk, w, x->st));
-        queued += kCgChunk;
+        if (mgcg)
+          CK(mgcg_iterate(m, chunk, queued == 0, w, x->mg, x->st));
+        else
+          CK(f32_pcg_iterate(m, chunk, queued == 0, w, x->st));
+        queued += chunk;
         rc = sync_scalars(x);
         if (rc) return rc;
         if (x->hds->flag[FL_PCG_DONE] || queued >= w.limit) break;
@@ -424,6 +436,8 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
     if (desc->bc_kind[s] != HYDRO_BC_WALL) return HYDRO_ERR_UNSUPPORTED;
   if (desc->velocity_omega <= 0. || desc->velocity_relaxation_factor <= 0.)
     return HYDRO_ERR_ARG;
+  if (desc->pressure_solver == HYDRO_LINEAR_MGCG && desc->precision != HYDRO_MIXED)
+    return HYDRO_ERR_UNSUPPORTED;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return HYDRO_ERR_NO_DEVICE;
   hydro_ctx* x = new (std::nothrow) hydro_ctx();
@@ -486,12 +500,29 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
     w.r32 = a.take<float>(nc);
     w.z32 = a.take<float>(nc);
     w.p32 = a.take<float>(nc);
+    w.p32b = a.take<float>(nc);
     w.Ap32 = a.take<float>(nc);
     w.dg32 = a.take<float>(nc);
     w.idg32 = a.take<float>(nc);
     w.x32 = a.take<float>(nc);
     w.kf32 = a.take<float>(nf);
     w.partials = a.take<double>((size_t)10 * kMaxBlocks);
+    // multigrid hierarchy (level 0 shares the FP32 CG arrays)
+    MgWork& mg = x->mg;
+    mg.nlev = desc->pressure_solver == HYDRO_LINEAR_MGCG ? mg_levels_for(m) : 0;
+    mg.nsweep = 2;
+    mg.coarse_sweeps = 64;
+    mg.coarse_sweeps_large = 16;
+    if (mg.nlev > 0) mg.lev[0].m = m;
+    for (int l = 1; l < mg.nlev; ++l) {
+      MgLevel& lv = mg.lev[l];
+      lv.m = mg_coarse_mesh(mg.lev[l - 1].m);
+      lv.kf = a.take<float>(lv.m.nf);
+      lv.dg = a.take<float>(lv.m.nc);
+      lv.idg = a.take<float>(lv.m.nc);
+      lv.x = a.take<float>(lv.m.nc);
+      lv.b = a.take<float>(lv.m.nc);
+    }
     w.ds = a.take<DevScalars>(1);
     x->stat_out = a.take<double>(16);
     x->stat_ticket = a.take<unsigned>(4);

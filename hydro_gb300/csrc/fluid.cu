@@ -228,7 +228,7 @@ __global__ void k_mom_assemble(Mesh m, Geo g, FluidCoef fc, C3 up, C3 utc, C3 ut
     res.a[n][X.c] = r;
   }
   double aPr = aP / fc.relax_u;
-  coef.a[0][X.c] = aPr;
+  coef.a[0][X.c] = 1. / aPr;  // the sweep multiplies by the inverse diagonal
 #pragma unroll
   for (int q = 0; q < 2 * DIM; ++q) coef.a[1 + q][X.c] = aq[q];
   Dc[X.c] = cs - aP + aPr;
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(NT) k_mom_sweep(Mesh m, double omega, double t
   if (ds->flag[FL_MOM_DONE]) return;
   double dmax = 0.;
   CELL_LOOP_BEGIN(m, kch)
-  double aP = coef.a[0][X.c];
+  double iaP = coef.a[0][X.c];
   double a[2 * DIM];
 #pragma unroll
   for (int q = 0; q < 2 * DIM; ++q) a[q] = coef.a[1 + q][X.c];
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(NT) k_mom_sweep(Mesh m, double omega, double t
         if (X.i[d] < m.n[d] - 1) sum += a[2 * d + 1] * din.a[n][X.c + s];
       }
     }
-    double value = -(res.a[n][X.c] + sum) / aP;
+    double value = -(res.a[n][X.c] + sum) * iaP;
     double corr = value - cur;
     dmax = fmax(dmax, fabs(corr));
     dout.a[n][X.c] = cur + corr * omega;

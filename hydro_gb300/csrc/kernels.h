@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include "../../include/hydro_gpu.h"
 #include "common.cuh"
 
 namespace hg {
@@ -135,7 +136,8 @@ void count_launches(int n);
 
 struct PcgWork {
   double *r, *z, *p, *Ap, *dg, *idg;                     // FP64 vectors
-  float *r32, *z32, *p32, *Ap32, *dg32, *idg32, *x32, *kf32;  // FP32 inner solve
+  float *r32, *z32, *p32, *p32b, *Ap32, *dg32, *idg32, *x32, *kf32;  // FP32 inner solve
+  int p32_parity;    // which of p32/p32b holds the current direction
   double* partials;  // >= 8 * kMaxBlocks doubles
   DevScalars* ds;
   long long pin;     // pinned cell or -1
@@ -159,7 +161,39 @@ cudaError_t sub_mean(const Mesh& m, double* x, PcgWork& w, cudaStream_t st);
 cudaError_t ir_residual(const Mesh& m, const double* kf, const double* f, const double* x,
                         int singular, PcgWork& w, cudaStream_t st);
 cudaError_t f32_pcg_init(const Mesh& m, double tol, PcgWork& w, cudaStream_t st);
-cudaError_t f32_pcg_iterate(const Mesh& m, int chunk, PcgWork& w, cudaStream_t st);
+cudaError_t f32_pcg_iterate(const Mesh& m, int chunk, int first, PcgWork& w, cudaStream_t st);
+// One launch: p_new = z + beta p_old (z on `first`), Ap = A p_new,
+// <p_new, Ap> -> alpha (FP32 vectors, double-float dot).
+cudaError_t cg32_dir_spmv(const Mesh& m, const float* kf, const float* dg, const float* z,
+                          const float* pold, float* pnew, float* Ap, long long pin, int first,
+                          double* partials, DevScalars* ds, cudaStream_t st);
+
+// ------------------------------------------------------------ multigrid --
+constexpr int kMgMaxLevels = 12;
+constexpr long long kMgCoarseMax = 4096;    // coarsest level solved in one block
+constexpr long long kMgCoarseTarget = 512;  // coarsening stops at or below this
+struct MgLevel {
+  Mesh m;
+  float *kf, *dg, *idg, *x, *b;
+};
+struct MgWork {
+  int nlev;
+  int nsweep;              // (red, black) sweeps before / after the correction
+  int coarse_sweeps;       // sweeps of the one-block coarsest solve
+  int coarse_sweeps_large; // sweeps when the coarsest level stays large
+  MgLevel lev[kMgMaxLevels];
+};
+Mesh mg_coarse_mesh(const Mesh& fine);
+int mg_levels_for(const Mesh& m);
+// Coarse couplings and diagonals from level 0 (w.kf32 / dg32 / idg32).
+cudaError_t mg_setup(MgWork& mg, PcgWork& w, cudaStream_t st);
+cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevScalars* ds,
+                      cudaStream_t st);
+// Inner solve of the mixed path with the V-cycle as preconditioner:
+// init from the FP64 residual in w.r, chunks of iterations into w.x32.
+cudaError_t mgcg_init(const Mesh& m, double tol, PcgWork& w, MgWork& mg, cudaStream_t st);
+cudaError_t mgcg_iterate(const Mesh& m, int chunk, int first, PcgWork& w, MgWork& mg,
+                         cudaStream_t st);
 cudaError_t f32_accumulate(const Mesh& m, double* x, PcgWork& w, cudaStream_t st);
 cudaError_t scale_vector(long long n, double* a, double s, cudaStream_t st);
 // Right-hand side of a pinned cell (fluid.hpp:996-1014): f[pin] = value and

@@ -21,7 +21,12 @@
 
 namespace hg {
 
-enum { PG_CG_SPMV = 7, PG_CG_UPDATE = 8, PG_CG_DIR = 9, PG_IR_RESIDUAL = 10 };
+enum {
+  PG_CG_SPMV = HYDRO_PROF_CG_SPMV,
+  PG_CG_UPDATE = HYDRO_PROF_CG_UPDATE,
+  PG_CG_DIR = HYDRO_PROF_CG_DIR,
+  PG_IR_RESIDUAL = HYDRO_PROF_IR_RESIDUAL
+};
 
 namespace {
 
@@ -314,6 +319,7 @@ cudaError_t ir_residual(const Mesh& m, const double* kf, const double* f, const 
 
 cudaError_t f32_pcg_init(const Mesh& m, double tol, PcgWork& w, cudaStream_t st) {
   Launch L = cell_launch(m);
+  w.p32_parity = 0;
   cudaMemsetAsync(w.x32, 0, sizeof(float) * m.nc, st);
   LAUNCH_DIM_T(k_cg_init, float, m, w.kf32, w.dg32, w.idg32, w.r, (const double*)nullptr,
              w.x32, 0, w.pin, w.r32, w.z32, w.p32, tol, w.partials, w.ds);
@@ -321,23 +327,143 @@ cudaError_t f32_pcg_init(const Mesh& m, double tol, PcgWork& w, cudaStream_t st)
   return cudaGetLastError();
 }
 
-cudaError_t f32_pcg_iterate(const Mesh& m, int chunk, PcgWork& w, cudaStream_t st) {
+namespace {
+
+// Double-float accumulation of dot products on the FP32 pipe: products are
+// split exactly (p + e == a*b via fmaf), partial sums carried as an
+// unevaluated pair (TwoSum), so a thread's share of a dot product is
+// accurate to about 2^-44 relative before it is combined across threads in
+// FP64.  GB300 runs FP64 at 1/57 of the FP32 rate, which makes per-cell
+// FP64 accumulation the bottleneck of the FP32 kernels.
+struct DFAcc {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    float p = a * b;
+    float e = fmaf(a, b, -p);
+    float t = hi + p;
+    float bp = t - hi;
+    float err = (hi - (t - bp)) + (p - bp);
+    hi = t;
+    lo += err + e;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// p_new = z + beta p_old (p_new = z on the first iteration) evaluated at the
+// cell and its neighbours, A p_new, <p_new, A p_new> -> alpha.
+template <int DIM>
+__global__ void __launch_bounds__(NT) k_cg32_dir_spmv(Mesh m, const float* kf, const float* dg,
+                                                      const float* z, const float* pold,
+                                                      float* pnew, float* Ap, long long pin,
+                                                      int first, double* partials,
+                                                      DevScalars* ds, int kch) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  const float beta = first ? 0.f : (float)ds->red[RS_PCG_BETA];
+  DFAcc acc;
+  CELL_LOOP_BEGIN(m, kch)
+  auto P = [&](long long c) { return first ? z[c] : fmaf(beta, pold[c], z[c]); };
+  float pc = P(X.c);
+  pnew[X.c] = pc;
+  float a;
+  if (X.c == pin) {
+    a = pc;
+  } else {
+    a = dg[X.c] * pc;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      long long s = cell_stride(m, d);
+      long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+      if (X.i[d] > 0 && X.c - s != pin) a = fmaf(-kf[fl], P(X.c - s), a);
+      if (X.i[d] < m.n[d] - 1 && X.c + s != pin) a = fmaf(-kf[fl + face_stride(m, d)], P(X.c + s), a);
+    }
+  }
+  Ap[X.c] = a;
+  acc.add_prod(pc, a);
+  CELL_LOOP_END
+  double v[1] = {acc.value()};
+  __shared__ double o[1];
+  if (grid_reduce<RED_SUM, 1>(v, partials, &ds->ticket[TK_F32_A], o)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      ds->red[RS_PCG_PAP] = o[0];
+      ds->red[RS_PCG_ALPHA] = ds->red[RS_PCG_RZ] / o[0];
+    }
+  }
+}
+
+// x += alpha p, r -= alpha Ap, z = r/diag; <r,z>, <r,r> -> beta, stop test.
+__global__ void __launch_bounds__(NT) k_cg32_update(long long n, float* x, float* r, float* z,
+                                                    const float* p, const float* Ap,
+                                                    const float* idg, double* partials,
+                                                    DevScalars* ds, int limit) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  const float at = (float)ds->red[RS_PCG_ALPHA];
+  DFAcc rz, rr;
+  long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
+  for (long long i = blockIdx.x * (long long)NT + tid; i < n; i += (long long)gridDim.x * NT) {
+    x[i] = fmaf(at, p[i], x[i]);
+    float ri = fmaf(-at, Ap[i], r[i]);
+    float zi = ri * idg[i];
+    r[i] = ri;
+    z[i] = zi;
+    rz.add_prod(ri, zi);
+    rr.add_prod(ri, ri);
+  }
+  double s[2] = {rz.value(), rr.value()};
+  __shared__ double o[2];
+  if (grid_reduce<RED_SUM, 2>(s, partials, &ds->ticket[TK_F32_B], o)) {
+    if (tid == 0) {
+      double rz_old = ds->red[RS_PCG_RZ];
+      ds->red[RS_PCG_BETA] = o[0] / rz_old;
+      ds->red[RS_PCG_RZ] = o[0];
+      ds->red[RS_PCG_RR] = o[1];
+      int it = ds->flag[FL_PCG_ITERS] + 1;
+      ds->flag[FL_PCG_ITERS] = it;
+      if (o[1] <= ds->red[RS_PCG_TOL2] || it >= limit) ds->flag[FL_PCG_DONE] = 1;
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t cg32_dir_spmv(const Mesh& m, const float* kf, const float* dg, const float* z,
+                          const float* pold, float* pnew, float* Ap, long long pin, int first,
+                          double* partials, DevScalars* ds, cudaStream_t st) {
+  Launch L = cell_launch(m);
+  if (m.dim == 3)
+    k_cg32_dir_spmv<3><<<L.grid, L.block, 0, st>>>(m, kf, dg, z, pold, pnew, Ap, pin, first,
+                                                   partials, ds, L.kch);
+  else
+    k_cg32_dir_spmv<2><<<L.grid, L.block, 0, st>>>(m, kf, dg, z, pold, pnew, Ap, pin, first,
+                                                   partials, ds, L.kch);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t f32_pcg_iterate(const Mesh& m, int chunk, int first, PcgWork& w, cudaStream_t st) {
   Launch L = cell_launch(m);
   int fb = flat_blocks_l(m.nc);
   for (int it = 0; it < chunk; ++it) {
+    // p lives in w.p32 / w.p32b alternately; its parity only matters while
+    // iterating, and a launch after convergence returns at once
+    float* pold = (w.p32_parity & 1) ? w.p32b : w.p32;
+    float* pnew = (w.p32_parity & 1) ? w.p32 : w.p32b;
     if (w.prof) w.prof->begin(PG_CG_SPMV, st);
-    LAUNCH_DIM_T(k_cg_spmv, float, m, w.kf32, w.dg32, w.p32, w.Ap32, w.pin, w.partials, w.ds);
+    if (m.dim == 3)
+      k_cg32_dir_spmv<3><<<L.grid, L.block, 0, st>>>(m, w.kf32, w.dg32, w.z32, pold, pnew, w.Ap32,
+                                                     w.pin, first && it == 0, w.partials, w.ds,
+                                                     L.kch);
+    else
+      k_cg32_dir_spmv<2><<<L.grid, L.block, 0, st>>>(m, w.kf32, w.dg32, w.z32, pold, pnew, w.Ap32,
+                                                     w.pin, first && it == 0, w.partials, w.ds,
+                                                     L.kch);
     if (w.prof) w.prof->end(PG_CG_SPMV, st);
     if (w.prof) w.prof->begin(PG_CG_UPDATE, st);
-    k_cg_update<float, float><<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.x32, w.r32, w.z32, w.p32,
-                                                           w.Ap32, w.idg32, w.partials, w.ds,
-                                                           w.limit);
+    k_cg32_update<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.x32, w.r32, w.z32, pnew, w.Ap32, w.idg32,
+                                               w.partials, w.ds, w.limit);
     if (w.prof) w.prof->end(PG_CG_UPDATE, st);
-    if (w.prof) w.prof->begin(PG_CG_DIR, st);
-    k_cg_dir<float><<<fb, NT, 0, st>>>(m.nc, w.z32, w.p32, w.ds);
-    if (w.prof) w.prof->end(PG_CG_DIR, st);
+    w.p32_parity ^= 1;
   }
-  count_launches(3 * chunk);
+  count_launches(2 * chunk);
   return cudaGetLastError();
 }
 

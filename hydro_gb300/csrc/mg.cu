@@ -1,0 +1,459 @@
+// mg.cu -- geometric multigrid preconditioner for the pressure-correction
+// solve of the mixed-precision path (FP32, sm_103a).
+//
+// The reference solves the pressure rows with Gauss-Seidel sweeps
+// (linear.hpp:685-715) and has no multigrid on its main path (a dormant
+// two-level experiment sits in source/test_module/test_module.hpp:311-379).
+// On a uniform block the pressure operator is a 7-point (5-point) stencil of
+// face couplings kf; the hierarchy here coarsens it 2:1 per direction:
+//   coarse coupling  = 1/2 * sum of the 4 (2) fine couplings of the face
+//                      (area x2^(dim-1), distance x2),
+//   restriction      = sum of the residuals of the 2^dim children,
+//   prolongation     = piecewise-constant injection,
+//   smoother         = red-black Gauss-Seidel, (red, black) before and
+//                      (black, red) after the coarse correction, so the
+//                      V-cycle is symmetric and usable inside CG,
+//   coarsest level   = <= kMgCoarseMax cells, one block of red-black sweeps
+//                      on the zero-mean right-hand side.
+// All kernels return at once when the CG's done flag is set, so iterations
+// can be queued in chunks like the other solvers.
+#include <math.h>
+
+#include "kernels.h"
+#include "loop.cuh"
+
+namespace hg {
+
+namespace {
+
+// Red-black GS half-sweep on the cells with (i+j+k) % 2 == color.  Thread
+// (x, y) handles the color-matching cell of the pair (2x, 2x+1) in row
+// (j, k).  With `zero` set the cell's neighbours are taken as 0 (first
+// half-sweep from x = 0).
+template <int DIM>
+__global__ void k_mg_smooth(Mesh m, const float* kf, const float* idg, const float* b, float* x,
+                            int color, int zero, long long pin, const DevScalars* ds, int kch) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  const int ih = blockIdx.x * BX + threadIdx.x;
+  const int j = blockIdx.y * BY + threadIdx.y;
+  const int nz = DIM == 3 ? m.n[2] : 1;
+  const int k0 = blockIdx.z * kch, k1 = min(k0 + kch, nz);
+  if (j >= m.n[1]) return;
+  for (int k = k0; k < k1; ++k) {
+    int i = 2 * ih + ((j + k + color) & 1);
+    if (i >= m.n[0]) continue;
+    long long c = cell_id(m, i, j, k);
+    if (c == pin) {
+      x[c] = b[c];
+      continue;
+    }
+    float acc = b[c];
+    if (!zero) {
+      int id[3] = {i, j, k};
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        long long s = cell_stride(m, d);
+        long long fl = face_id(m, d, i, j, k);
+        if (id[d] > 0 && c - s != pin) acc = fmaf(kf[fl], x[c - s], acc);
+        if (id[d] < m.n[d] - 1 && c + s != pin) acc = fmaf(kf[fl + face_stride(m, d)], x[c + s], acc);
+      }
+    }
+    x[c] = acc * idg[c];
+  }
+}
+
+// Coarse couplings: 1/2 of the sum of the fine couplings of each coarse face.
+template <int DIM>
+__global__ void k_mg_coarsen(Mesh fm, Mesh cm, const float* fkf, float* ckf, int kch) {
+  CELL_LOOP_BEGIN(cm, kch)
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long cf = face_id(cm, d, X.i[0], X.i[1], X.i[2]);
+    // fine faces of the coarse low face: index 2I along d, 2I and 2I+1 across
+    float sum = 0.f;
+    int e1 = (d + 1) % DIM, e2 = (d + 2) % DIM;
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+#pragma unroll
+      for (int bq = 0; bq < (DIM == 3 ? 2 : 1); ++bq) {
+        int fi[3] = {2 * X.i[0], 2 * X.i[1], 2 * X.i[2]};
+        fi[e1] += a;
+        if (DIM == 3) fi[e2] += bq;
+        sum += fkf[face_id(fm, d, fi[0], fi[1], DIM == 3 ? fi[2] : 0)];
+      }
+    }
+    float kc = X.i[d] > 0 ? 0.5f * sum : 0.f;
+    ckf[cf] = kc;
+    if (X.i[d] == cm.n[d] - 1) ckf[cf + face_stride(cm, d)] = 0.f;
+  }
+  CELL_LOOP_END
+}
+
+template <int DIM>
+__global__ void k_mg_diag(Mesh m, const float* kf, float* dg, float* idg, int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+  float s = 0.f;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+    s += kf[fl] + kf[fl + face_stride(m, d)];
+  }
+  dg[X.c] = s;
+  idg[X.c] = s > 0.f ? 1.f / s : 0.f;
+  CELL_LOOP_END
+}
+
+// Coarse right-hand side = sum over the 2^DIM children of the fine residual
+// b - A x; also clears the coarse correction.
+template <int DIM>
+__global__ void k_mg_restrict(Mesh fm, Mesh cm, const float* kf, const float* dg, const float* b,
+                              const float* x, float* cb, float* cx, long long pin,
+                              const DevScalars* ds, int kch) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  CELL_LOOP_BEGIN(cm, kch)
+  float sum = 0.f;
+#pragma unroll
+  for (int ck = 0; ck < (DIM == 3 ? 2 : 1); ++ck)
+#pragma unroll
+    for (int cj = 0; cj < 2; ++cj)
+#pragma unroll
+      for (int ci = 0; ci < 2; ++ci) {
+        int id[3] = {2 * X.i[0] + ci, 2 * X.i[1] + cj, DIM == 3 ? 2 * X.i[2] + ck : 0};
+        long long c = cell_id(fm, id[0], id[1], id[2]);
+        float r;
+        if (c == pin) {
+          r = b[c] - x[c];
+        } else {
+          float ax = dg[c] * x[c];
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) {
+            long long s = cell_stride(fm, d);
+            long long fl = face_id(fm, d, id[0], id[1], id[2]);
+            if (id[d] > 0 && c - s != pin) ax = fmaf(-kf[fl], x[c - s], ax);
+            if (id[d] < fm.n[d] - 1 && c + s != pin) ax = fmaf(-kf[fl + face_stride(fm, d)], x[c + s], ax);
+          }
+          r = b[c] - ax;
+        }
+        sum += r;
+      }
+  cb[X.c] = sum;
+  cx[X.c] = 0.f;
+  CELL_LOOP_END
+}
+
+// x_fine += x_coarse(parent)
+template <int DIM>
+__global__ void k_mg_prolong(Mesh fm, const float* cx, float* x, int cnx, int cny,
+                             const DevScalars* ds, int kch) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  CELL_LOOP_BEGIN(fm, kch)
+  long long pc = (X.i[0] >> 1) + (long long)cnx * ((X.i[1] >> 1) + (long long)cny * (X.i[2] >> 1));
+  x[X.c] += cx[pc];
+  CELL_LOOP_END
+}
+
+// Coarsest level in one block: zero-mean right-hand side, then `sweeps`
+// red-black GS sweeps from x = 0.
+template <int DIM>
+__global__ void k_mg_coarse_solve(Mesh m, const float* kf, const float* idg, float* b, float* x,
+                                  int sweeps, const DevScalars* ds) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  __shared__ float red[32];
+  __shared__ float mean;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const long long n = m.nc;
+  float s = 0.f;
+  for (long long c = tid; c < n; c += nt) s += b[c];
+  s = warp_sum(s);
+  if ((tid & 31) == 0) red[tid >> 5] = s;
+  __syncthreads();
+  if (tid < 32) {
+    float v = tid < (nt + 31) / 32 ? red[tid] : 0.f;
+    v = warp_sum(v);
+    if (tid == 0) mean = v / (float)n;
+  }
+  __syncthreads();
+  for (long long c = tid; c < n; c += nt) {
+    b[c] -= mean;
+    x[c] = 0.f;
+  }
+  __syncthreads();
+  for (int sw = 0; sw < sweeps; ++sw) {
+    for (int color = 0; color < 2; ++color) {
+      for (long long c = tid; c < n; c += nt) {
+        int id[3];
+        id[0] = (int)(c % m.n[0]);
+        id[1] = (int)((c / m.n[0]) % m.n[1]);
+        id[2] = DIM == 3 ? (int)(c / ((long long)m.n[0] * m.n[1])) : 0;
+        if (((id[0] + id[1] + id[2]) & 1) != color) continue;
+        float acc = b[c];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          long long st = cell_stride(m, d);
+          long long fl = face_id(m, d, id[0], id[1], id[2]);
+          if (id[d] > 0) acc = fmaf(kf[fl], x[c - st], acc);
+          if (id[d] < m.n[d] - 1) acc = fmaf(kf[fl + face_stride(m, d)], x[c + st], acc);
+        }
+        x[c] = acc * idg[c];
+      }
+      __syncthreads();
+    }
+  }
+}
+
+struct DFAcc2 {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    float p = a * b;
+    float e = fmaf(a, b, -p);
+    float t = hi + p;
+    float bp = t - hi;
+    float err = (hi - (t - bp)) + (p - bp);
+    hi = t;
+    lo += err + e;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// Inner-solve start: r = FP32 copy of the FP64 refinement residual; ||r||^2
+// sets the stop test.
+__global__ void __launch_bounds__(NT) k_mgcg_init(long long n, const double* r64, float* r,
+                                                  float* x, double tol, double* partials,
+                                                  DevScalars* ds) {
+  double s = 0.;
+  long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
+  for (long long i = blockIdx.x * (long long)NT + tid; i < n; i += (long long)gridDim.x * NT) {
+    double v = r64[i];
+    r[i] = (float)v;
+    x[i] = 0.f;
+    s += v * v;
+  }
+  double v[1] = {s};
+  __shared__ double o[1];
+  if (grid_reduce<RED_SUM, 1>(v, partials, &ds->ticket[TK_F32_INIT], o)) {
+    if (tid == 0) {
+      ds->red[RS_PCG_FF] = o[0];
+      ds->red[RS_PCG_RR] = o[0];
+      ds->red[RS_PCG_TOL2] = tol * tol * o[0];
+      ds->flag[FL_PCG_ITERS] = 0;
+      ds->flag[FL_PCG_DONE] = (o[0] == 0.) ? 1 : 0;
+    }
+  }
+}
+
+// x += alpha p, r -= alpha Ap; ||r||^2 and the stop test.
+__global__ void __launch_bounds__(NT) k_mgcg_update(long long n, float* x, float* r,
+                                                    const float* p, const float* Ap,
+                                                    double* partials, DevScalars* ds, int limit) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  const float at = (float)ds->red[RS_PCG_ALPHA];
+  DFAcc2 rr;
+  long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
+  for (long long i = blockIdx.x * (long long)NT + tid; i < n; i += (long long)gridDim.x * NT) {
+    x[i] = fmaf(at, p[i], x[i]);
+    float ri = fmaf(-at, Ap[i], r[i]);
+    r[i] = ri;
+    rr.add_prod(ri, ri);
+  }
+  double s[1] = {rr.value()};
+  __shared__ double o[1];
+  if (grid_reduce<RED_SUM, 1>(s, partials, &ds->ticket[TK_F32_B], o)) {
+    if (tid == 0) {
+      ds->red[RS_PCG_RR] = o[0];
+      int it = ds->flag[FL_PCG_ITERS] + 1;
+      ds->flag[FL_PCG_ITERS] = it;
+      if (o[0] <= ds->red[RS_PCG_TOL2] || it >= limit) ds->flag[FL_PCG_DONE] = 1;
+    }
+  }
+}
+
+// <r, z> -> beta = <r,z>/<r,z>_old (first: only stores <r,z>).
+__global__ void __launch_bounds__(NT) k_mgcg_dot(long long n, const float* r, const float* z,
+                                                 int first, double* partials, DevScalars* ds) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  DFAcc2 rz;
+  long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
+  for (long long i = blockIdx.x * (long long)NT + tid; i < n; i += (long long)gridDim.x * NT)
+    rz.add_prod(r[i], z[i]);
+  double s[1] = {rz.value()};
+  __shared__ double o[1];
+  if (grid_reduce<RED_SUM, 1>(s, partials, &ds->ticket[TK_PCG_INIT2], o)) {
+    if (tid == 0) {
+      if (!first) ds->red[RS_PCG_BETA] = o[0] / ds->red[RS_PCG_RZ];
+      ds->red[RS_PCG_RZ] = o[0];
+    }
+  }
+}
+
+int flat_blocks_mg(long long n) {
+  long long b = (n + NT - 1) / NT;
+  if (b > 152 * 16) b = 152 * 16;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+Launch half_launch(const Mesh& m) {
+  Launch L = cell_launch(m);
+  int halfx = (m.n[0] + 1) / 2;
+  L.grid.x = (halfx + BX - 1) / BX;
+  return L;
+}
+
+}  // namespace
+
+Mesh mg_coarse_mesh(const Mesh& f) {
+  Mesh c = f;
+  for (int d = 0; d < f.dim; ++d) {
+    c.n[d] = f.n[d] / 2;
+    c.h[d] = f.h[d] * 2.;
+  }
+  c.nc = (long long)c.n[0] * c.n[1] * (f.dim == 3 ? c.n[2] : 1);
+  long long off = 0;
+  for (int d = 0; d < 3; ++d) {
+    c.fnx[d] = c.n[0] + (d == 0);
+    c.fny[d] = c.n[1] + (d == 1);
+    c.fofs[d] = off;
+    if (d < f.dim) off += (long long)c.fnx[d] * c.fny[d] * ((f.dim == 3 ? c.n[2] : 1) + (d == 2));
+  }
+  c.nf = off;
+  return c;
+}
+
+int mg_levels_for(const Mesh& m) {
+  int nlev = 1;
+  Mesh cur = m;
+  while (nlev < kMgMaxLevels && cur.nc > kMgCoarseTarget) {
+    bool ok = true;
+    for (int d = 0; d < cur.dim; ++d)
+      if (cur.n[d] % 2 != 0 || cur.n[d] / 2 < 2) ok = false;
+    if (!ok) break;
+    cur = mg_coarse_mesh(cur);
+    ++nlev;
+  }
+  return nlev;
+}
+
+#define MG_LAUNCH(KERNEL, L, ...)                                               \
+  do {                                                                          \
+    if (dim == 3)                                                               \
+      KERNEL<3><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);          \
+    else                                                                        \
+      KERNEL<2><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);          \
+    count_launches(1);                                                          \
+  } while (0)
+
+cudaError_t mg_setup(MgWork& mg, PcgWork& w, cudaStream_t st) {
+  int dim = mg.lev[0].m.dim;
+  mg.lev[0].kf = w.kf32;
+  mg.lev[0].dg = w.dg32;
+  mg.lev[0].idg = w.idg32;
+  for (int l = 1; l < mg.nlev; ++l) {
+    MgLevel& f = mg.lev[l - 1];
+    MgLevel& c = mg.lev[l];
+    Launch L = cell_launch(c.m);
+    MG_LAUNCH(k_mg_coarsen, L, f.m, c.m, f.kf, c.kf);
+    MG_LAUNCH(k_mg_diag, L, c.m, c.kf, c.dg, c.idg);
+  }
+  return cudaGetLastError();
+}
+
+// z = M^-1 r: one V-cycle with `nsweep` (red, black) sweeps before and
+// (black, red) sweeps after each coarse correction.
+cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevScalars* ds,
+                      cudaStream_t st) {
+  int dim = mg.lev[0].m.dim;
+  mg.lev[0].b = const_cast<float*>(r);
+  mg.lev[0].x = z;
+  const int ns = mg.nsweep;
+  for (int l = 0; l + 1 < mg.nlev; ++l) {
+    MgLevel& f = mg.lev[l];
+    long long lp = l == 0 ? pin : -1;
+    Launch H = half_launch(f.m);
+    for (int s = 0; s < ns; ++s) {
+      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 0, s == 0, lp, ds);
+      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, ds);
+    }
+    MgLevel& c = mg.lev[l + 1];
+    Launch L = cell_launch(c.m);
+    MG_LAUNCH(k_mg_restrict, L, f.m, c.m, f.kf, f.dg, f.b, f.x, c.b, c.x, lp, ds);
+  }
+  MgLevel& cl = mg.lev[mg.nlev - 1];
+  if (mg.nlev > 1 && cl.m.nc <= kMgCoarseMax) {
+    if (dim == 3)
+      k_mg_coarse_solve<3><<<1, 1024, 0, st>>>(cl.m, cl.kf, cl.idg, cl.b, cl.x, mg.coarse_sweeps, ds);
+    else
+      k_mg_coarse_solve<2><<<1, 1024, 0, st>>>(cl.m, cl.kf, cl.idg, cl.b, cl.x, mg.coarse_sweeps, ds);
+    count_launches(1);
+  } else {
+    // large coarsest level (odd dimensions) or a single level: symmetric
+    // smoothing only, (red, black)^s then (black, red)^s
+    long long lp = mg.nlev == 1 ? pin : -1;
+    Launch H = half_launch(cl.m);
+    const int half = mg.coarse_sweeps_large / 2 > 0 ? mg.coarse_sweeps_large / 2 : 1;
+    for (int s = 0; s < half; ++s) {
+      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, s == 0, lp, ds);
+      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 1, 0, lp, ds);
+    }
+    for (int s = 0; s < half; ++s) {
+      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 1, 0, lp, ds);
+      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, 0, lp, ds);
+    }
+  }
+  for (int l = mg.nlev - 2; l >= 0; --l) {
+    MgLevel& f = mg.lev[l];
+    MgLevel& c = mg.lev[l + 1];
+    long long lp = l == 0 ? pin : -1;
+    Launch L = cell_launch(f.m);
+    MG_LAUNCH(k_mg_prolong, L, f.m, c.x, f.x, c.m.n[0], c.m.n[1], ds);
+    Launch H = half_launch(f.m);
+    for (int s = 0; s < ns; ++s) {
+      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, ds);
+      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 0, 0, lp, ds);
+    }
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t mgcg_init(const Mesh& m, double tol, PcgWork& w, MgWork& mg, cudaStream_t st) {
+  int fb = flat_blocks_mg(m.nc);
+  w.p32_parity = 0;
+  k_mgcg_init<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.r, w.r32, w.x32, tol, w.partials, w.ds);
+  count_launches(1);
+  if (w.prof) w.prof->begin(HYDRO_PROF_MG_VCYCLE, st);
+  mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st);
+  if (w.prof) w.prof->end(HYDRO_PROF_MG_VCYCLE, st);
+  k_mgcg_dot<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.r32, w.z32, 1, w.partials, w.ds);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t mgcg_iterate(const Mesh& m, int chunk, int first, PcgWork& w, MgWork& mg,
+                         cudaStream_t st) {
+  Launch L = cell_launch(m);
+  int fb = flat_blocks_mg(m.nc);
+  int dim = m.dim;
+  for (int it = 0; it < chunk; ++it) {
+    float* pold = (w.p32_parity & 1) ? w.p32b : w.p32;
+    float* pnew = (w.p32_parity & 1) ? w.p32 : w.p32b;
+    if (w.prof) w.prof->begin(HYDRO_PROF_CG_SPMV, st);
+    cudaError_t e = cg32_dir_spmv(m, w.kf32, w.dg32, w.z32, pold, pnew, w.Ap32, w.pin,
+                                  first && it == 0, w.partials, w.ds, st);
+    if (w.prof) w.prof->end(HYDRO_PROF_CG_SPMV, st);
+    if (e != cudaSuccess) return e;
+    if (w.prof) w.prof->begin(HYDRO_PROF_CG_UPDATE, st);
+    k_mgcg_update<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.x32, w.r32, pnew, w.Ap32, w.partials, w.ds,
+                                               w.limit);
+    if (w.prof) w.prof->end(HYDRO_PROF_CG_UPDATE, st);
+    if (w.prof) w.prof->begin(HYDRO_PROF_MG_VCYCLE, st);
+    mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st);
+    if (w.prof) w.prof->end(HYDRO_PROF_MG_VCYCLE, st);
+    k_mgcg_dot<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.r32, w.z32, 0, w.partials, w.ds);
+    count_launches(2);
+    w.p32_parity ^= 1;
+  }
+  (void)L;
+  (void)dim;
+  return cudaGetLastError();
+}
+
+}  // namespace hg

@@ -79,7 +79,9 @@ enum hydro_linear {
   HYDRO_LINEAR_GAUSS_SEIDEL = 0, /* linear.hpp:671-716 */
   HYDRO_LINEAR_JACOBI = 1,       /* linear.hpp:736-783 */
   HYDRO_LINEAR_CG = 2,           /* new: no Krylov solver in the reference */
-  HYDRO_LINEAR_LU = 3            /* linear.hpp:527-567 (one symmetric sweep) */
+  HYDRO_LINEAR_LU = 3,           /* linear.hpp:527-567 (one symmetric sweep) */
+  HYDRO_LINEAR_MGCG = 4          /* new: CG preconditioned by a geometric multigrid
+                                    V-cycle (GPU: mixed precision only) */
 };
 
 /* Arithmetic of the pressure solve.  MIXED runs the PCG in FP32 inside an
@@ -299,7 +301,8 @@ enum hydro_prof_group {
   HYDRO_PROF_VEL_GRAD = 0, HYDRO_PROF_FORCE, HYDRO_PROF_MOM_ASSEMBLE, HYDRO_PROF_MOM_SWEEP,
   HYDRO_PROF_RHIE_CHOW, HYDRO_PROF_PRESSURE_RHS, HYDRO_PROF_CG_INIT, HYDRO_PROF_CG_SPMV,
   HYDRO_PROF_CG_UPDATE, HYDRO_PROF_CG_DIR, HYDRO_PROF_IR_RESIDUAL, HYDRO_PROF_CORRECT,
-  HYDRO_PROF_ADV_FACES, HYDRO_PROF_ADV_UPDATE, HYDRO_PROF_PROPS, HYDRO_PROF_OTHER,
+  HYDRO_PROF_ADV_FACES, HYDRO_PROF_ADV_UPDATE, HYDRO_PROF_PROPS, HYDRO_PROF_MG_VCYCLE,
+  HYDRO_PROF_OTHER,
   HYDRO_PROF_COUNT
 };
 int hydro_gpu_set_profiling(hydro_ctx* ctx, int on);

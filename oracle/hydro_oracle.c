@@ -1126,7 +1126,9 @@ int oracle_make_iteration(oracle_ctx* x) {
   double* pc = x->pcorr;
   int it = 0;
   int st;
-  if (d->pressure_solver == HYDRO_LINEAR_CG) {
+  /* the multigrid-preconditioned CG of the GPU converges to the same
+     solution; the oracle uses plain CG for it */
+  if (d->pressure_solver == HYDRO_LINEAR_CG || d->pressure_solver == HYDRO_LINEAR_MGCG) {
     double* f = x->cw[21];
     for (long c = 0; c < nc; ++c) f[c] = -x->rowc[c];
     if (pin >= 0) {

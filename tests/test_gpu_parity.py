@@ -120,6 +120,36 @@ def test_mixed_precision_matches_fp64(built):
         assert s["pressure_residual"] <= 1e-10
 
 
+@pytest.mark.parametrize("shape", [(16, 16, 16), (24, 16, 8), (20, 12, 10)])
+def test_multigrid_cg_matches_fp64(built, shape):
+    """Mixed precision with the multigrid-preconditioned CG: same fields as
+    the FP64 Jacobi-CG path within the mixed tolerance, pressure residual
+    reached, few iterations (power-of-two and non-power-of-two blocks)."""
+    from hydro_gb300.solver import Hydro
+    d, u0, q0, _ = cases.rising_drops(n=16, seed=5, dt_max=5e-3)
+    d.n[0], d.n[1], d.n[2] = shape
+    d.hi[0], d.hi[1], d.hi[2] = shape[0] / 16.0, shape[1] / 16.0, shape[2] / 16.0
+    from hydro_gb300.cases import cell_centers, two_phase_q
+    x, y, z = cell_centers(d)
+    alpha1 = (((x - 0.4) ** 2 + (y - 0.3) ** 2 + (z - 0.25) ** 2) < 0.15 ** 2).astype(float)
+    q0 = two_phase_q(d, alpha1, 2)
+    u0 = np.zeros(d.ncells * 3)
+    d.pressure_tolerance = 1e-10
+    d.velocity_tolerance = 1e-12
+    d.convergence_tolerance = 0.0
+    d.num_iterations_limit = 3
+    a = run(Hydro(d), u0, q0, 3)
+    dm = d.copy()
+    dm.precision = capi.MIXED
+    dm.pressure_solver = capi.LINEAR_MGCG
+    b = run(Hydro(dm), u0, q0, 3)
+    errs = compare(b, a)
+    assert all(v <= 1e-6 for v in errs.values()), errs
+    for sa, sb in zip(a["stats"], b["stats"]):
+        assert sb["pressure_residual"] <= 1e-10
+        assert sb["pressure_iterations"] < sa["pressure_iterations"]
+
+
 def test_stencil_solve_matches_oracle(built):
     from hydro_gb300.solver import stencil_solve
     from oracle import oracle as O
