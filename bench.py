@@ -47,9 +47,13 @@ ALG_BYTES_PER_CELL_FP64 = {
 }
 # FP32 inner solve of the mixed path (vectors 4 B)
 ALG_BYTES_PER_CELL_FP32 = {
-    "cg_spmv": 4 * (1 + 3 + 1 + 1),
-    "cg_update": 4 * (5 + 3),
-    "cg_dir": 4 * (2 + 1),
+    "cg_spmv": 4 * (6 + 2),                # read z, p_old, kf[3], diag; write p_new, Ap
+    "cg_update": 4 * (4 + 2),              # read x, r, p, Ap; write x, r
+    "mom_sweep": 4 * (10 + 3 + 3),         # read coef[7]+res[3], du[3]; write du[3]
+    # one V-cycle: finest level 4 red-black sweeps (x r/w, b, kf[3], 1/diag)
+    # + restriction (x, b, kf[3], diag) + prolongation (x r/w), coarser
+    # levels 1/8 per level
+    "mg_vcycle": int(round(4 * (4 * 7 + 6 + 2) * 8 / 7)),
 }
 
 
@@ -248,28 +252,22 @@ def cpu_sample(n, seed, outer, sweeps=(4, 12), threads=None):
 
 
 # ---------------------------------------------------------------- our arm --
-def run_ours(args, rank, world, local):
+def measure(args, form, rank, world, local, stream, e2e=True):
+    """Times args.steps steps of one form ("mixed_mg": mixed precision with
+    the multigrid CG, "fp64": plain FP64 with Jacobi CG) after args.warmup
+    untimed steps; returns a dict of results."""
     import numpy as np
     import torch
 
     from hydro_gb300 import capi
     from hydro_gb300 import solver as S
 
-    torch.cuda.set_device(local)
-    try:
-        capi.load()
-    except RuntimeError:
-        from hydro_gb300 import build
-        build.build_library()
-        capi.load()
-    stream = torch.cuda.Stream()
-    d, u0, q0, drops = workload(args.n, args.seed + rank, args.precision, args.outer, args.solver)
+    precision, solver = ("mixed", "mgcg") if form == "mixed_mg" else ("fp64", "cg")
+    d, u0, q0, drops = workload(args.n, args.seed + rank, precision, args.outer, solver)
     h = S.make(d, u0, q0, stream=stream.cuda_stream)
     N = d.ncells
-
     for _ in range(args.warmup):
         h.step()
-    # timed region: device time with CUDA events on the library's stream
     h.reset_profile()
     h.set_profiling(True)
     barrier(world)
@@ -290,102 +288,146 @@ def run_ours(args, rank, world, local):
     prof = h.profile()
     h.set_profiling(False)
     ms_max = max_over_ranks(ms, world)
-    value = world * N * args.steps / (ms_max / 1e3) / 1e6
+    out = {"form": form, "precision": precision, "solver": solver, "N": N, "drops": len(drops),
+           "ms": ms_max, "value": world * N * args.steps / (ms_max / 1e3) / 1e6,
+           "launches": launches, "clocks": clk, "stats": stats, "prof": prof, "desc": d}
+    if e2e:
+        # through the public C-ABI with host buffers: every step uploads the
+        # state from pinned host memory and reads the result back
+        nph = d.num_phases
+        pin_u = torch.empty(N * d.dim, dtype=torch.float64, pin_memory=True).numpy()
+        pin_q = torch.empty(N * nph, dtype=torch.float64, pin_memory=True).numpy()
+        pin_p = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+        pin_u[:] = h.get_field(capi.F_VELOCITY)
+        pin_q[:] = h.get_field(capi.F_PARTIAL_DENSITY)
+        lib = capi.load()
+        dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            lib.hydro_gpu_set_field(h.ctx, capi.F_VELOCITY, capi.TIME_CURR, dp(pin_u), pin_u.size)
+            lib.hydro_gpu_set_field(h.ctx, capi.F_PARTIAL_DENSITY, capi.TIME_CURR, dp(pin_q),
+                                    pin_q.size)
+            h.step()
+            lib.hydro_gpu_get_field(h.ctx, capi.F_VELOCITY, capi.TIME_CURR, dp(pin_u), pin_u.size)
+            lib.hydro_gpu_get_field(h.ctx, capi.F_PRESSURE, capi.TIME_CURR, dp(pin_p), pin_p.size)
+            lib.hydro_gpu_get_field(h.ctx, capi.F_PARTIAL_DENSITY, capi.TIME_CURR, dp(pin_q),
+                                    pin_q.size)
+        torch.cuda.synchronize()
+        e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+        out["e2e"] = {"value": round(world * N * args.steps / e2e_s / 1e6, 4),
+                      "unit": "Mcell-updates/s",
+                      "h2d_bytes_per_step": (d.dim + nph) * N * 8,
+                      "d2h_bytes_per_step": (d.dim + 1 + nph) * N * 8}
+    h.close()
+    return out
 
-    # e2e: through the public C-ABI with host buffers; every step uploads the
-    # state from pinned host memory and reads the result back
-    nph = d.num_phases
-    pin_u = torch.empty(N * d.dim, dtype=torch.float64, pin_memory=True).numpy()
-    pin_q = torch.empty(N * nph, dtype=torch.float64, pin_memory=True).numpy()
-    pin_p = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
-    pin_u[:] = h.get_field(capi.F_VELOCITY)
-    pin_q[:] = h.get_field(capi.F_PARTIAL_DENSITY)
-    lib = capi.load()
-    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
-    barrier(world)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        lib.hydro_gpu_set_field(h.ctx, capi.F_VELOCITY, capi.TIME_CURR, dp(pin_u), pin_u.size)
-        lib.hydro_gpu_set_field(h.ctx, capi.F_PARTIAL_DENSITY, capi.TIME_CURR, dp(pin_q), pin_q.size)
-        h.step()
-        lib.hydro_gpu_get_field(h.ctx, capi.F_VELOCITY, capi.TIME_CURR, dp(pin_u), pin_u.size)
-        lib.hydro_gpu_get_field(h.ctx, capi.F_PRESSURE, capi.TIME_CURR, dp(pin_p), pin_p.size)
-        lib.hydro_gpu_get_field(h.ctx, capi.F_PARTIAL_DENSITY, capi.TIME_CURR, dp(pin_q), pin_q.size)
-    torch.cuda.synchronize()
-    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
-    e2e_value = world * N * args.steps / e2e_s / 1e6
-    h2d = (d.dim + nph) * N * 8
-    d2h = (d.dim + 1 + nph) * N * 8
 
-    # roofline of the dominant kernel group
+def roofline(res):
+    """Roofline figure of the dominant kernel group of one measured form."""
     peak, peak_kind = measured_peaks()
-    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
-    roof = None
-    if dom:
-        name, (nl, tms) = dom
-        table = ALG_BYTES_PER_CELL_FP32 if args.precision == "mixed" else ALG_BYTES_PER_CELL_FP64
-        per_cell = table.get(name)
-        eff = nl
-        if name in ("cg_spmv", "cg_update", "cg_dir"):
-            eff = sum(s["pressure_iterations"] for s in stats)
-        elif name == "mom_sweep":
-            eff = sum(s["velocity_sweeps"] for s in stats)
-        if per_cell:
-            bytes_launch = per_cell * N
-            achieved = bytes_launch * eff / (tms / 1e3) / 1e9
-            roof = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1),
-                    "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                    "traffic": None, "peak_source": peak_kind,
-                    "bytes_per_launch": bytes_launch, "launches": nl,
-                    "effective_launches": eff, "avg_launch_us": round(tms * 1e3 / max(eff, 1), 2)}
+    prof, stats, N = res["prof"], res["stats"], res["N"]
+    if not prof:
+        return None
+    name, (nl, tms) = max(prof.items(), key=lambda kv: kv[1][1])
+    table = dict(ALG_BYTES_PER_CELL_FP64)
+    if res["precision"] == "mixed":
+        table.update(ALG_BYTES_PER_CELL_FP32)
+    per_cell = table.get(name)
+    if not per_cell:
+        return {"bound": "hbm", "kernel": name, "achieved": None, "peak": peak, "unit": "GB/s",
+                "frac": None, "traffic": None}
+    eff = nl
+    if name in ("cg_spmv", "cg_update", "cg_dir"):
+        eff = sum(s["pressure_iterations"] for s in stats)
+    elif name == "mom_sweep":
+        eff = sum(s["velocity_sweeps"] for s in stats)
+    bytes_launch = per_cell * N
+    achieved = bytes_launch * eff / (tms / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+            "peak_source": peak_kind, "bytes_per_launch": bytes_launch, "launches": nl,
+            "effective_launches": eff, "avg_launch_us": round(tms * 1e3 / max(eff, 1), 2)}
+
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    from hydro_gb300 import capi
+
+    torch.cuda.set_device(local)
+    try:
+        capi.load()
+    except RuntimeError:
+        from hydro_gb300 import build
+        build.build_library()
+        capi.load()
+    stream = torch.cuda.Stream()
+    head = measure(args, args.form, rank, world, local, stream)
+    plain = None
+    if args.form != "fp64" and not args.no_plain:
+        plain = measure(args, "fp64", rank, world, local, stream, e2e=False)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
             cpu = cpu_sample(args.n, args.seed, args.outer)
         except Exception as e:  # the baseline is reported, not required
             cpu = {"error": str(e)}
-
-    if rank == 0:
-        out = {
-            "metric": "Mcell-updates/s",
-            "value": round(value, 4),
-            "unit": "Mcell-updates/s",
-            "n_gpus": world,
-            "steps": args.steps,
-            "warmup": args.warmup,
-            "ms_per_step": round(ms_max / args.steps, 3),
-            "higher_is_better": True,
-            "scaling": "weak",
-            "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "f64+f32",
-            "data": "synthetic: seeded rising drops (%d drops), no external data" % len(drops),
-            "config": {
-                "workload": "rising_drops_%d^3" % args.n,
-                "cells": N,
-                "precision": args.precision,
-                "simple_iterations_per_step": args.outer,
-                "pressure_residual": 1e-8,
-                "seed": args.seed,
-                "parallelism": "replicas" if world > 1 else "single",
-                "l2": "working set %.1f GB > 129 MB L2" % (N * 8 * 80 / 1e9),
-            },
-            "e2e": {"value": round(e2e_value, 4), "unit": "Mcell-updates/s",
-                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches,
-            "roofline": roof,
-            "clocks": clk,
-            "cpu_baseline": cpu,
-            "step_stats": {
-                "outer_iterations": [s["outer_iterations"] for s in stats],
-                "pressure_iterations": [s["pressure_iterations"] for s in stats],
-                "velocity_sweeps": [s["velocity_sweeps"] for s in stats],
-                "pressure_residual_max": max(s["pressure_residual"] for s in stats),
-                "dt": stats[-1]["dt"],
-            },
-            "profile_ms": {k: round(v[1], 3) for k, v in sorted(prof.items())},
+    if rank != 0:
+        return
+    stats = head["stats"]
+    N = head["N"]
+    out = {
+        "metric": "Mcell-updates/s",
+        "value": round(head["value"], 4),
+        "unit": "Mcell-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(head["ms"] / args.steps, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64+f32" if head["precision"] == "mixed" else "f64",
+        "data": "synthetic: seeded rising drops (%d drops), no external data" % head["drops"],
+        "config": {
+            "workload": "rising_drops_%d^3" % args.n,
+            "cells": N,
+            "form": head["form"],
+            "precision": head["precision"],
+            "pressure_solver": head["solver"],
+            "simple_iterations_per_step": args.outer,
+            "pressure_residual": 1e-8,
+            "seed": args.seed,
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "inputs larger than L2: working set %.1f GB > 129 MB" % (N * 8 * 80 / 1e9),
+        },
+        "e2e": head.get("e2e"),
+        "gpu_launches": head["launches"],
+        "roofline": roofline(head),
+        "clocks": head["clocks"],
+        "cpu_baseline": cpu,
+        "step_stats": {
+            "outer_iterations": [s["outer_iterations"] for s in stats],
+            "pressure_iterations": [s["pressure_iterations"] for s in stats],
+            "velocity_sweeps": [s["velocity_sweeps"] for s in stats],
+            "pressure_residual_max": max(s["pressure_residual"] for s in stats),
+            "dt": stats[-1]["dt"],
+        },
+        "profile_ms": {k: round(v[1], 3) for k, v in sorted(head["prof"].items())},
+    }
+    if plain:
+        out["plain_fp64"] = {
+            "value": round(plain["value"], 4),
+            "ms_per_step": round(plain["ms"] / args.steps, 3),
+            "speedup_of_headline": round(head["value"] / plain["value"], 2),
+            "pressure_iterations": [s["pressure_iterations"] for s in plain["stats"]],
+            "roofline": roofline(plain),
+            "clocks": plain["clocks"],
+            "profile_ms": {k: round(v[1], 3) for k, v in sorted(plain["prof"].items())},
         }
-        print(json.dumps(out))
+    print(json.dumps(out))
 
 
 def run_reference(args, rank, world):
@@ -431,9 +473,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--solver", default="cg", choices=["cg", "mgcg"],
-                    help="pressure: Jacobi-PCG or multigrid-PCG (mixed only)")
+    ap.add_argument("--form", default="mixed_mg", choices=["mixed_mg", "fp64"],
+                    help="headline form: mixed precision + multigrid CG, or plain FP64")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the plain FP64 measurement reported beside the headline")
     ap.add_argument("--n", type=int, default=192)
     ap.add_argument("--outer", type=int, default=5, help="SIMPLE iterations per step")
     ap.add_argument("--seed", type=int, default=0)

@@ -135,6 +135,17 @@ struct hydro_ctx {
   // iteration work
   double *G = nullptr, *fo = nullptr, *fres = nullptr, *coef = nullptr, *res = nullptr;
   double* du[2] = {};
+  // mixed path: FP32 momentum coefficients/residuals and Jacobi iterates
+  float* o32 = nullptr;
+  float* du32[2] = {};
+  FP<10> o32p() {
+    FP<10> r{};
+    if (!o32) return r;
+    int w = 2 * dim + 1;
+    for (int q = 0; q < w; ++q) r.a[q] = o32 + (size_t)q * m.nc;
+    for (int k = 0; k < dim; ++k) r.a[7 + k] = o32 + (size_t)(w + k) * m.nc;
+    return r;
+  }
   double *Dc = nullptr, *Fs = nullptr, *kf = nullptr, *pc = nullptr, *prhs = nullptr;
   PcgWork pw{};
   double* stat_out = nullptr;
@@ -263,15 +274,28 @@ int solve_momentum(hydro_ctx* x, C3 up) {
   if (rc) return rc;
   int limit = d.velocity_iters_limit + 1;  // do { } while (iter++ < limit)
   int queued = 0;
+  const bool f32 = x->o32 != nullptr;
+  auto fp3 = [&](float* base) {
+    FP<3> r{};
+    for (int k = 0; k < dim; ++k) r.a[k] = base + (size_t)k * x->m.nc;
+    return r;
+  };
   for (;;) {
     int n = std::min(kSweepChunk, limit - queued);
     for (int s = 0; s < n; ++s) {
       int k = queued + s;
-      C3 din = x->vec<C3>(x->du[(k + 1) % 2], dim, x->m.nc);
-      W3 dout = x->vec<W3>(x->du[k % 2], dim, x->m.nc);
-      PK(x, HYDRO_PROF_MOM_SWEEP,
-         launch_mom_sweep(x->m, d.velocity_omega, d.velocity_tolerance, cc, resc, din, dout,
-                          k == 0, x->pw.partials, x->pw.ds, x->st));
+      if (f32) {
+        PK(x, HYDRO_PROF_MOM_SWEEP,
+           launch_mom_sweep32(x->m, d.velocity_omega, d.velocity_tolerance, x->o32p(),
+                              fp3(x->du32[(k + 1) % 2]), fp3(x->du32[k % 2]), k == 0,
+                              x->pw.partials, x->pw.ds, x->st));
+      } else {
+        C3 din = x->vec<C3>(x->du[(k + 1) % 2], dim, x->m.nc);
+        W3 dout = x->vec<W3>(x->du[k % 2], dim, x->m.nc);
+        PK(x, HYDRO_PROF_MOM_SWEEP,
+           launch_mom_sweep(x->m, d.velocity_omega, d.velocity_tolerance, cc, resc, din, dout,
+                            k == 0, x->pw.partials, x->pw.ds, x->st));
+      }
     }
     queued += n;
     rc = sync_scalars(x);
@@ -281,6 +305,11 @@ int solve_momentum(hydro_ctx* x, C3 up) {
   int sweeps = x->hds->flag[FL_MOM_SWEEPS];
   x->vel_sweeps += sweeps;
   x->du_cur = (sweeps - 1) % 2;
+  if (f32) {
+    // the FP32 correction joins the FP64 state: u* = u_prev + du
+    CK(launch_f2d3(x->m, fp3(x->du32[x->du_cur]), x->vec<W3>(x->du[x->du_cur], dim, x->m.nc),
+                   x->st));
+  }
   return HYDRO_OK;
 }
 
@@ -485,6 +514,11 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
     x->res = a.take<double>(nc * dim);
     x->du[0] = a.take<double>(nc * dim);
     x->du[1] = a.take<double>(nc * dim);
+    if (desc->precision == HYDRO_MIXED) {
+      x->o32 = a.take<float>(nc * (2 * dim + 1 + dim));
+      x->du32[0] = a.take<float>(nc * dim);
+      x->du32[1] = a.take<float>(nc * dim);
+    }
     x->Dc = a.take<double>(nc);
     x->Fs = a.take<double>(nf);
     x->kf = a.take<double>(nf);
@@ -709,7 +743,7 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
   PK(x, HYDRO_PROF_MOM_ASSEMBLE, launch_mom_assemble(m, x->fc, up, x->uc3(HYDRO_TIME_CURR), x->uc3(HYDRO_TIME_PREV),
                          x->vec<CP<9>>(x->G, dim * dim, m.nc), Fip, x->rho, x->mu,
                          x->vec<C3>(x->fo, dim, m.nc), x->vec<WP<7>>(x->coef, 2 * dim + 1, m.nc),
-                         x->vec<W3>(x->res, dim, m.nc), x->Dc, x->st));
+                         x->vec<W3>(x->res, dim, m.nc), x->o32p(), x->Dc, x->st));
   int rc = solve_momentum(x, up);
   if (rc) return rc;
   C3 du = x->vec<C3>(x->du[x->du_cur], dim, m.nc);

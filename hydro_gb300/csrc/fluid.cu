@@ -155,7 +155,7 @@ __global__ void k_force(Mesh m, Geo g, FluidCoef fc, C3 u, CP<9> G, const double
 template <int DIM>
 __global__ void k_mom_assemble(Mesh m, Geo g, FluidCoef fc, C3 up, C3 utc, C3 utp, CP<9> G,
                                const double* F, const double* rho, const double* mu, C3 fo,
-                               WP<7> coef, W3 res, double* Dc, int kch) {
+                               WP<7> coef, W3 res, FP<10> o32, double* Dc, int kch) {
   CELL_LOOP_BEGIN(m, kch)
   const double rhoc = rho[X.c], muc = mu[X.c];
   double aP = fc.co[2] * rhoc;
@@ -225,12 +225,20 @@ __global__ void k_mom_assemble(Mesh m, Geo g, FluidCoef fc, C3 up, C3 utc, C3 ut
       if (X.i[d] > 0) r += aq[2 * d] * up.a[n][X.c - s];
       if (X.i[d] < m.n[d] - 1) r += aq[2 * d + 1] * up.a[n][X.c + s];
     }
-    res.a[n][X.c] = r;
+    if (o32.a[0]) o32.a[7 + n][X.c] = (float)r;
+    else res.a[n][X.c] = r;
   }
   double aPr = aP / fc.relax_u;
-  coef.a[0][X.c] = 1. / aPr;  // the sweep multiplies by the inverse diagonal
+  // the sweep multiplies by the inverse diagonal
+  if (o32.a[0]) {
+    o32.a[0][X.c] = (float)(1. / aPr);
 #pragma unroll
-  for (int q = 0; q < 2 * DIM; ++q) coef.a[1 + q][X.c] = aq[q];
+    for (int q = 0; q < 2 * DIM; ++q) o32.a[1 + q][X.c] = (float)aq[q];
+  } else {
+    coef.a[0][X.c] = 1. / aPr;
+#pragma unroll
+    for (int q = 0; q < 2 * DIM; ++q) coef.a[1 + q][X.c] = aq[q];
+  }
   Dc[X.c] = cs - aP + aPr;
   CELL_LOOP_END
 }
@@ -278,6 +286,55 @@ __global__ void __launch_bounds__(NT) k_mom_sweep(Mesh m, double omega, double t
       if (!(out[0] > tol)) ds->flag[FL_MOM_DONE] = 1;
     }
   }
+}
+
+// The same Jacobi sweep on the FP32 coefficients and residuals of the
+// mixed-precision path (o32 of k_mom_assemble: inverse diagonal, 2*DIM
+// off-diagonals, DIM residuals): FP32 arithmetic, FP64 only for the max.
+template <int DIM>
+__global__ void __launch_bounds__(NT) k_mom_sweep32(Mesh m, float omega, double tol, FP<10> c,
+                                                    FP<3> din, FP<3> dout, int first,
+                                                    double* partials, DevScalars* ds, int kch) {
+  if (ds->flag[FL_MOM_DONE]) return;
+  float dmax = 0.f;
+  CELL_LOOP_BEGIN(m, kch)
+  float iaP = c.a[0][X.c];
+  float a[2 * DIM];
+#pragma unroll
+  for (int q = 0; q < 2 * DIM; ++q) a[q] = c.a[1 + q][X.c];
+#pragma unroll
+  for (int n = 0; n < DIM; ++n) {
+    float sum = 0.f, cur = 0.f;
+    if (!first) {
+      cur = din.a[n][X.c];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        long long s = cell_stride(m, d);
+        if (X.i[d] > 0) sum = fmaf(a[2 * d], din.a[n][X.c - s], sum);
+        if (X.i[d] < m.n[d] - 1) sum = fmaf(a[2 * d + 1], din.a[n][X.c + s], sum);
+      }
+    }
+    float value = -(c.a[7 + n][X.c] + sum) * iaP;
+    float corr = value - cur;
+    dmax = fmaxf(dmax, fabsf(corr));
+    dout.a[n][X.c] = fmaf(corr, omega, cur);
+  }
+  CELL_LOOP_END
+  double v[1] = {(double)dmax};
+  __shared__ double out[1];
+  if (grid_reduce<RED_MAX, 1>(v, partials, &ds->ticket[TK_MOM], out)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      ds->red[RS_MOM_DIFF] = out[0];
+      ds->flag[FL_MOM_SWEEPS] += 1;
+      if (!(out[0] > tol)) ds->flag[FL_MOM_DONE] = 1;
+    }
+  }
+}
+
+__global__ void k_f2d3(long long n, int dim, FP<3> in, W3 out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    for (int k = 0; k < dim; ++k) out.a[k][i] = (double)in.a[k][i];
 }
 
 // ------------------------------------------------------------ Rhie-Chow --
@@ -627,10 +684,22 @@ cudaError_t launch_force(const Mesh& m, const FluidCoef& fc, C3 u, CP<9> G, cons
 
 cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 u_tc,
                                 C3 u_tp, CP<9> G, const double* F, const double* rho,
-                                const double* mu, C3 fo, WP<7> coef, W3 res, double* Dc,
-                                cudaStream_t st) {
+                                const double* mu, C3 fo, WP<7> coef, W3 res, FP<10> o32,
+                                double* Dc, cudaStream_t st) {
   DISPATCH_DIM(m, k_mom_assemble, m, make_geo(m), fc, u_prev, u_tc, u_tp, G, F, rho, mu, fo,
-               coef, res, Dc);
+               coef, res, o32, Dc);
+}
+
+cudaError_t launch_mom_sweep32(const Mesh& m, double omega, double tol, FP<10> c, FP<3> din,
+                               FP<3> dout, int first, double* partials, DevScalars* ds,
+                               cudaStream_t st) {
+  DISPATCH_DIM(m, k_mom_sweep32, m, (float)omega, tol, c, din, dout, first, partials, ds);
+}
+
+cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st) {
+  k_f2d3<<<flat_blocks(m.nc), NT, 0, st>>>(m.nc, m.dim, in, out);
+  count_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_mom_sweep(const Mesh& m, double omega, double tol, CP<7> coef, C3 res,

@@ -23,6 +23,10 @@ struct WP {
 };
 using C3 = CP<3>;
 using W3 = WP<3>;
+template <int N>
+struct FP {
+  float* a[N];
+};
 
 // Per-case constants of the momentum / pressure-correction kernels.
 struct FluidCoef {
@@ -74,8 +78,14 @@ cudaError_t launch_force(const Mesh& m, const FluidCoef& fc, C3 u, CP<9> G, cons
                          const double* Sv, const double* Sm, W3 fo, W3 fres, cudaStream_t st);
 cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 u_tc,
                                 C3 u_tp, CP<9> G, const double* F, const double* rho,
-                                const double* mu, C3 fo, WP<7> coef, W3 res, double* Dc,
-                                cudaStream_t st);
+                                const double* mu, C3 fo, WP<7> coef, W3 res, FP<10> o32,
+                                double* Dc, cudaStream_t st);
+// Mixed path: FP32 Jacobi sweep on the o32 output of the assembly
+// (o32 = {1/diag, 2*DIM off-diagonals, DIM residuals}); FP32 -> FP64 copy.
+cudaError_t launch_mom_sweep32(const Mesh& m, double omega, double tol, FP<10> c, FP<3> din,
+                               FP<3> dout, int first, double* partials, DevScalars* ds,
+                               cudaStream_t st);
+cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st);
 cudaError_t launch_mom_sweep(const Mesh& m, double omega, double tol, CP<7> coef, C3 res,
                              C3 din, W3 dout, int first, double* partials, DevScalars* ds,
                              cudaStream_t st);
