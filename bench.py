@@ -9,8 +9,15 @@ Synthetic seeded inputs of that shape (no external data).
 
 Metric: Mcell-updates/s = cells x time steps / wall seconds, whole job.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--form mixed_mg|fp64]
+                  [--no-plain] [--no-cpu-baseline]
   python bench.py --impl reference ...   # the reference algorithm on the CPU
+
+The headline form is "mixed_mg": FP64 iterative refinement around an FP32
+conjugate-gradient pressure solve preconditioned by geometric multigrid, with
+FP32 momentum sweeps (FP64 assembly, residuals and corrections).  The plain
+FP64 form (Jacobi-preconditioned CG, FP64 sweeps) is timed beside it in the
+same run as "plain_fp64" unless --no-plain is given.
 
 Multi-GPU: replicas only (the reference's MPI mode runs redundant replicas;
 the path has no exchange step here) -- each rank advances its own seeded
