@@ -147,6 +147,18 @@ struct hydro_ctx {
     return r;
   }
   double *Dc = nullptr, *Fs = nullptr, *kf = nullptr, *pc = nullptr, *prhs = nullptr;
+  double* gp = nullptr;  // FP64 cell pressure gradient of the iteration
+  // mixed path: FP32 shadows of the state and mixture fields read by the
+  // FP32 SIMPLE-iteration kernels (refreshed at StartStep, the iterate by
+  // the correction kernel) and their FP32 work arrays
+  struct Shadow32 {
+    float* u[4] = {};  // per layer, component-major
+    float* F[4] = {};  // iteration layers only
+    float *rho = nullptr, *mu = nullptr, *force = nullptr, *stforce = nullptr;
+    float *Sv = nullptr, *Sm = nullptr;
+    float *G = nullptr, *fo = nullptr, *fres = nullptr, *Dc = nullptr;
+  } s32;
+  bool mixed = false;
   PcgWork pw{};
   double* stat_out = nullptr;
   unsigned* stat_ticket = nullptr;
@@ -178,6 +190,13 @@ struct hydro_ctx {
   P vec(double* base, int n, long long stride) {
     P r{};
     for (int k = 0; k < n; ++k) r.a[k] = base + (size_t)k * stride;
+    return r;
+  }
+  // FP32 component tables over nc-strided arrays
+  template <class P>
+  P vf(float* base, int n) {
+    P r{};
+    for (int k = 0; k < n && base; ++k) r.a[k] = base + (size_t)k * m.nc;
     return r;
   }
 };
@@ -305,11 +324,7 @@ int solve_momentum(hydro_ctx* x, C3 up) {
   int sweeps = x->hds->flag[FL_MOM_SWEEPS];
   x->vel_sweeps += sweeps;
   x->du_cur = (sweeps - 1) % 2;
-  if (f32) {
-    // the FP32 correction joins the FP64 state: u* = u_prev + du
-    CK(launch_f2d3(x->m, fp3(x->du32[x->du_cur]), x->vec<W3>(x->du[x->du_cur], dim, x->m.nc),
-                   x->st));
-  }
+  // mixed path: the Rhie-Chow and correction kernels read du32 directly
   return HYDRO_OK;
 }
 
@@ -478,6 +493,7 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
   const Mesh& m = x->m;
   x->dim = desc->dim;
   x->nph = desc->num_phases;
+  x->mixed = desc->precision == HYDRO_MIXED;
   cudaGetDevice(&x->device);
   if (desc->stream) {
     x->st = (cudaStream_t)desc->stream;
@@ -518,7 +534,21 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
       x->o32 = a.take<float>(nc * (2 * dim + 1 + dim));
       x->du32[0] = a.take<float>(nc * dim);
       x->du32[1] = a.take<float>(nc * dim);
+      auto& s3 = x->s32;
+      for (int l = 0; l < 4; ++l) s3.u[l] = a.take<float>(nc * dim);
+      for (int l : {HYDRO_ITER_CURR, HYDRO_ITER_PREV}) s3.F[l] = a.take<float>(nf);
+      s3.rho = a.take<float>(nc);
+      s3.mu = a.take<float>(nc);
+      s3.force = a.take<float>(nc * dim);
+      s3.stforce = a.take<float>(nc * dim);
+      s3.Sv = a.take<float>(nc);
+      s3.Sm = a.take<float>(nc);
+      s3.G = a.take<float>(nc * dim * dim);
+      s3.fo = a.take<float>(nc * dim);
+      s3.fres = a.take<float>(nc * dim);
+      s3.Dc = a.take<float>(nc);
     }
+    x->gp = a.take<double>(nc * dim);
     x->Dc = a.take<double>(nc);
     x->Fs = a.take<double>(nf);
     x->kf = a.take<double>(nf);
@@ -720,6 +750,24 @@ int hydro_gpu_start_step(hydro_ctx* x) {
                        x->uc3(HYDRO_TIME_CURR), x->uc3(HYDRO_TIME_PREV), x->p[HYDRO_ITER_CURR],
                        x->p[HYDRO_TIME_CURR], x->p[HYDRO_TIME_PREV], x->F[HYDRO_ITER_CURR],
                        x->F[HYDRO_TIME_CURR], x->F[HYDRO_TIME_PREV], x->st));
+  if (x->mixed) {
+    // FP32 shadows of everything the FP32 iteration kernels read; the
+    // iteration layers are kept current by the correction kernel
+    auto& s3 = x->s32;
+    const long long nu = m.nc * x->dim;
+    CK(launch_d2f(nu, x->u[HYDRO_ITER_CURR], s3.u[HYDRO_ITER_CURR], x->st));
+    CK(launch_d2f(nu, x->u[HYDRO_TIME_CURR], s3.u[HYDRO_TIME_CURR], x->st));
+    CK(launch_d2f(nu, x->u[HYDRO_TIME_PREV], s3.u[HYDRO_TIME_PREV], x->st));
+    CK(launch_d2f(m.nf, x->F[HYDRO_ITER_CURR], s3.F[HYDRO_ITER_CURR], x->st));
+    CK(launch_d2f(m.nc, x->rho, s3.rho, x->st));
+    CK(launch_d2f(m.nc, x->mu, s3.mu, x->st));
+    CK(launch_d2f(nu, x->force, s3.force, x->st));
+    CK(launch_d2f(nu, x->stforce, s3.stforce, x->st));
+    if (x->fc.sources) {
+      CK(launch_d2f(m.nc, x->Sv, s3.Sv, x->st));
+      CK(launch_d2f(m.nc, x->Sm, s3.Sm, x->st));
+    }
+  }
   return HYDRO_OK;
 }
 
@@ -734,27 +782,83 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
   C3 up = x->uc3(HYDRO_ITER_PREV);
   const double* pip = x->p[HYDRO_ITER_PREV];
   const double* Fip = x->F[HYDRO_ITER_PREV];
-  C3 force = x->vec<C3>(x->force, dim, m.nc);
-  C3 fres = x->vec<C3>(x->fres, dim, m.nc);
-  PK(x, HYDRO_PROF_VEL_GRAD, launch_vel_grad(m, x->fc, up, x->vec<WP<9>>(x->G, dim * dim, m.nc), x->st));
-  PK(x, HYDRO_PROF_FORCE, launch_force(m, x->fc, up, x->vec<CP<9>>(x->G, dim * dim, m.nc), pip, x->mu, x->rho, force,
-                  x->vec<C3>(x->stforce, dim, m.nc), x->Sv, x->Sm, x->vec<W3>(x->fo, dim, m.nc),
-                  x->vec<W3>(x->fres, dim, m.nc), x->st));
-  PK(x, HYDRO_PROF_MOM_ASSEMBLE, launch_mom_assemble(m, x->fc, up, x->uc3(HYDRO_TIME_CURR), x->uc3(HYDRO_TIME_PREV),
-                         x->vec<CP<9>>(x->G, dim * dim, m.nc), Fip, x->rho, x->mu,
-                         x->vec<C3>(x->fo, dim, m.nc), x->vec<WP<7>>(x->coef, 2 * dim + 1, m.nc),
-                         x->vec<W3>(x->res, dim, m.nc), x->o32p(), x->Dc, x->st));
-  int rc = solve_momentum(x, up);
-  if (rc) return rc;
-  C3 du = x->vec<C3>(x->du[x->du_cur], dim, m.nc);
-  x->cd_iter_count++;
-  PK(x, HYDRO_PROF_RHIE_CHOW,
-     launch_rhie_chow(m, x->fc, up, du, pip, force, fres, x->Dc, x->Fs, x->kf, x->st));
+  auto& s3 = x->s32;
+  int rc;
+  if (x->mixed) {
+    // FP32 assembly on the shadows
+    std::swap(s3.F[HYDRO_ITER_CURR], s3.F[HYDRO_ITER_PREV]);
+    std::swap(s3.u[HYDRO_ITER_CURR], s3.u[HYDRO_ITER_PREV]);
+    using R3 = RT<float, 3>;
+    using V3 = WT<float, 3>;
+    R3 up32 = x->vf<R3>(s3.u[HYDRO_ITER_PREV], dim);
+    R3 force32 = x->vf<R3>(s3.force, dim), fres32 = x->vf<R3>(s3.fres, dim);
+    PK(x, HYDRO_PROF_VEL_GRAD,
+       launch_vel_grad<float>(m, x->fc, up32, x->vf<WT<float, 9>>(s3.G, dim * dim), x->st));
+    PK(x, HYDRO_PROF_FORCE,
+       launch_force<float>(m, x->fc, up32, x->vf<RT<float, 9>>(s3.G, dim * dim), pip, s3.mu,
+                           s3.rho, force32, x->vf<R3>(s3.stforce, dim), s3.Sv, s3.Sm,
+                           x->vf<V3>(s3.fo, dim), x->vf<V3>(s3.fres, dim),
+                           x->vec<W3>(x->gp, dim, m.nc), x->st));
+    FP<10> o = x->o32p();
+    WT<float, 7> coef32{};
+    V3 res32{};
+    for (int q = 0; q < 2 * dim + 1; ++q) coef32.a[q] = o.a[q];
+    for (int k = 0; k < dim; ++k) res32.a[k] = o.a[7 + k];
+    PK(x, HYDRO_PROF_MOM_ASSEMBLE,
+       launch_mom_assemble<float>(m, x->fc, up32, x->vf<R3>(s3.u[HYDRO_TIME_CURR], dim),
+                                  x->vf<R3>(s3.u[HYDRO_TIME_PREV], dim),
+                                  x->vf<RT<float, 9>>(s3.G, dim * dim), s3.F[HYDRO_ITER_PREV],
+                                  s3.rho, s3.mu, x->vf<R3>(s3.fo, dim), up,
+                                  x->uc3(HYDRO_TIME_CURR), x->uc3(HYDRO_TIME_PREV), coef32,
+                                  res32, s3.Dc, x->st));
+    rc = solve_momentum(x, up);
+    if (rc) return rc;
+    x->cd_iter_count++;
+    PK(x, HYDRO_PROF_RHIE_CHOW,
+       launch_rhie_chow<float>(m, x->fc, up, x->vf<R3>(x->du32[x->du_cur], dim), pip,
+                               x->vec<C3>(x->gp, dim, m.nc), force32, fres32, s3.Dc, x->Fs,
+                               x->kf, nullptr, x->st));
+  } else {
+    C3 force = x->vec<C3>(x->force, dim, m.nc);
+    C3 fres = x->vec<C3>(x->fres, dim, m.nc);
+    PK(x, HYDRO_PROF_VEL_GRAD,
+       launch_vel_grad<double>(m, x->fc, up, x->vec<WP<9>>(x->G, dim * dim, m.nc), x->st));
+    PK(x, HYDRO_PROF_FORCE,
+       launch_force<double>(m, x->fc, up, x->vec<CP<9>>(x->G, dim * dim, m.nc), pip, x->mu,
+                            x->rho, force, x->vec<C3>(x->stforce, dim, m.nc), x->Sv, x->Sm,
+                            x->vec<W3>(x->fo, dim, m.nc), x->vec<W3>(x->fres, dim, m.nc),
+                            x->vec<W3>(x->gp, dim, m.nc), x->st));
+    PK(x, HYDRO_PROF_MOM_ASSEMBLE,
+       launch_mom_assemble<double>(m, x->fc, up, x->uc3(HYDRO_TIME_CURR),
+                                   x->uc3(HYDRO_TIME_PREV),
+                                   x->vec<CP<9>>(x->G, dim * dim, m.nc), Fip, x->rho, x->mu,
+                                   x->vec<C3>(x->fo, dim, m.nc), up, x->uc3(HYDRO_TIME_CURR),
+                                   x->uc3(HYDRO_TIME_PREV),
+                                   x->vec<WP<7>>(x->coef, 2 * dim + 1, m.nc),
+                                   x->vec<W3>(x->res, dim, m.nc), x->Dc, x->st));
+    rc = solve_momentum(x, up);
+    if (rc) return rc;
+    C3 du = x->vec<C3>(x->du[x->du_cur], dim, m.nc);
+    x->cd_iter_count++;
+    PK(x, HYDRO_PROF_RHIE_CHOW,
+       launch_rhie_chow<double>(m, x->fc, up, du, pip, x->vec<C3>(x->gp, dim, m.nc), force, fres,
+                                x->Dc, x->Fs, x->kf, nullptr, x->st));
+  }
   PK(x, HYDRO_PROF_PRESSURE_RHS, launch_pressure_rhs(m, x->Fs, x->fc.sources ? x->Sv : nullptr, x->prhs, x->st));
   rc = solve_pressure(x);
   if (rc) return rc;
-  PK(x, HYDRO_PROF_CORRECT, launch_correct(m, x->fc, up, du, x->uw3(HYDRO_ITER_CURR), pip, x->p[HYDRO_ITER_CURR], x->pc,
-                    x->Dc, x->Fs, x->kf, x->F[HYDRO_ITER_CURR], x->pw.partials, x->pw.ds, x->st));
+  C3 du = x->vec<C3>(x->du[x->du_cur], dim, m.nc);
+  if (x->mixed)
+    PK(x, HYDRO_PROF_CORRECT,
+       launch_correct(m, x->fc, up, du, x->vf<RT<float, 3>>(x->du32[x->du_cur], dim), s3.Dc,
+                      x->uw3(HYDRO_ITER_CURR), pip, x->p[HYDRO_ITER_CURR], x->pc, x->Dc, x->Fs,
+                      x->kf, x->F[HYDRO_ITER_CURR], x->vf<FP<3>>(s3.u[HYDRO_ITER_CURR], dim),
+                      nullptr, s3.F[HYDRO_ITER_CURR], x->pw.partials, x->pw.ds, x->st));
+  else
+    PK(x, HYDRO_PROF_CORRECT,
+       launch_correct(m, x->fc, up, du, RT<float, 3>{}, nullptr, x->uw3(HYDRO_ITER_CURR), pip,
+                      x->p[HYDRO_ITER_CURR], x->pc, x->Dc, x->Fs, x->kf, x->F[HYDRO_ITER_CURR],
+                      FP<3>{}, nullptr, nullptr, x->pw.partials, x->pw.ds, x->st));
   rc = sync_scalars(x);
   if (rc) return rc;
   x->indicator = x->hds->red[RS_INDICATOR];

@@ -17,37 +17,49 @@ namespace hg {
 
 namespace {
 
+// FP64 operands of the BDF time difference (the residual's cancelling part).
+struct Unsteady64 {
+  double co[3];
+  const double* up[3];
+  const double* utc[3];
+  const double* utp[3];
+};
+
+__device__ __forceinline__ double tsqrt(double v) { return sqrt(v); }
+__device__ __forceinline__ float tsqrt(float v) { return sqrtf(v); }
+
 // Geometric average of two vectors (solver.hpp:380-390), component d.
-template <int DIM>
-__device__ double vgeo(const double* a, const double* b, int d) {
-  double av[DIM], n2 = 0., na = 0., nb = 0.;
+template <int DIM, class T>
+__device__ T vgeo(const T* a, const T* b, int d) {
+  T av[DIM], n2 = T(0), na = T(0), nb = T(0);
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
-    av[k] = (a[k] + b[k]) * 0.5;
+    av[k] = (a[k] + b[k]) * T(0.5);
     n2 += av[k] * av[k];
     na += a[k] * a[k];
     nb += b[k] * b[k];
   }
-  double an = sqrt(n2);
-  if (an < 1e-8) return av[d];
-  return av[d] / an * sqrt(sqrt(na) * sqrt(nb));
+  T an = tsqrt(n2);
+  if (an < T(1e-8)) return av[d];
+  return av[d] / an * tsqrt(tsqrt(na) * tsqrt(nb));
 }
 
 // Face value (component d) of a cell vector field between cells cm and cp.
-template <int DIM>
-__device__ double face_vec(const C3& f, long long cm, long long cp, int d, int geometric) {
+template <int DIM, class T>
+__device__ T face_vec(const RT<T, 3>& f, long long cm, long long cp, int d, int geometric) {
   if (!geometric) return avg(f.a[d][cm], f.a[d][cp]);
-  double a[DIM], b[DIM];
+  T a[DIM], b[DIM];
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
     a[k] = f.a[k][cm];
     b[k] = f.a[k][cp];
   }
-  return vgeo<DIM>(a, b, d);
+  return vgeo<DIM, T>(a, b, d);
 }
 
-__device__ __forceinline__ double face_scal(double a, double b, int geometric) {
-  return geometric ? sqrt(a * b) : avg(a, b);
+template <class T>
+__device__ __forceinline__ T face_scal(T a, T b, int geometric) {
+  return geometric ? tsqrt(a * b) : avg(a, b);
 }
 
 // ------------------------------------------------------------ StartStep --
@@ -58,11 +70,19 @@ __global__ void k_axpy_extrap(long long n, double ge, double* out, const double*
     out[i] = tc[i] + (tc[i] - tp[i]) * ge;
 }
 
+// FP32 copies of FP64 arrays (the shadows read by the FP32 kernels).
+__global__ void k_d2f(long long n, const double* in, float* out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
 // ------------------------------------------------------- velocity grads --
 // G[n*DIM+m] = d u_n / d x_m at cells, faces carrying the velocity value
 // condition (Gradient(Interpolate(u_n, cond_n)), solver.hpp:392-470,658-677).
-template <int DIM>
-__global__ void k_vel_grad(Mesh m, Geo g, FluidCoef fc, C3 u, WP<9> G, int kch) {
+template <int DIM, class T>
+__global__ void k_vel_grad(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, WT<T, 9> G,
+                           int kch) {
   CELL_LOOP_BEGIN(m, kch)
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
@@ -70,9 +90,9 @@ __global__ void k_vel_grad(Mesh m, Geo g, FluidCoef fc, C3 u, WP<9> G, int kch) 
     int id = X.i[d], nd = m.n[d];
 #pragma unroll
     for (int n = 0; n < DIM; ++n) {
-      double uc = u.a[n][X.c];
-      double flo = id > 0 ? avg(u.a[n][X.c - s], uc) : fc.bcu[2 * d][n];
-      double fhi = id < nd - 1 ? avg(uc, u.a[n][X.c + s]) : fc.bcu[2 * d + 1][n];
+      T uc = u.a[n][X.c];
+      T flo = id > 0 ? avg(u.a[n][X.c - s], uc) : fc.bcu[2 * d][n];
+      T fhi = id < nd - 1 ? avg(uc, u.a[n][X.c + s]) : fc.bcu[2 * d + 1][n];
       G.a[n * DIM + d][X.c] = (fhi - flo) * g.inv_h[d];
     }
   }
@@ -85,22 +105,23 @@ __global__ void k_vel_grad(Mesh m, Geo g, FluidCoef fc, C3 u, WP<9> G, int kch) 
 // (zero-derivative boundaries), minus grad p (extrapolated boundary faces),
 // plus the "restored" external force (fluid.hpp:612-625), surface-tension
 // force and the volume-source momentum term.  Also stores the restored
-// force for the Rhie-Chow kernel.
-template <int DIM>
-__global__ void k_force(Mesh m, Geo g, FluidCoef fc, C3 u, CP<9> G, const double* p,
-                        const double* mu, const double* rho, C3 force, C3 stforce,
-                        const double* Sv, const double* Sm, W3 fo, W3 fres, int kch) {
+// force and the FP64 cell pressure gradient for the Rhie-Chow kernel.
+template <int DIM, class T>
+__global__ void k_force(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T, 9> G,
+                        const double* p, Geo g64, const T* mu, const T* rho,
+                        RT<T, 3> force, RT<T, 3> stforce, const T* Sv, const T* Sm,
+                        WT<T, 3> fo, WT<T, 3> fres, W3 gp64, int kch) {
   CELL_LOOP_BEGIN(m, kch)
-  double acc[DIM];
+  T acc[DIM];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) acc[k] = 0.;
-  const double muc = mu[X.c];
+  for (int k = 0; k < DIM; ++k) acc[k] = T(0);
+  const T muc = mu[X.c];
 #pragma unroll
   for (int n = 0; n < DIM; ++n) {
     long long s = cell_stride(m, n);
     int id = X.i[n], nd = m.n[n];
-    double mlo, mhi;
-    double glo[DIM], ghi[DIM];
+    T mlo, mhi;
+    T glo[DIM], ghi[DIM];
     if (id > 0) {
       mlo = face_scal(mu[X.c - s], muc, fc.geometric);
 #pragma unroll
@@ -124,18 +145,22 @@ __global__ void k_force(Mesh m, Geo g, FluidCoef fc, C3 u, CP<9> G, const double
 #pragma unroll
     for (int k = 0; k < DIM; ++k) acc[k] += (ghi[k] * mhi - glo[k] * mlo) * g.inv_h[n];
   }
-  double src = fc.sources ? rho[X.c] * Sv[X.c] - Sm[X.c] : 0.;
+  T src = fc.sources ? rho[X.c] * Sv[X.c] - Sm[X.c] : T(0);
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
     long long s = cell_stride(m, k);
     int id = X.i[k], nd = m.n[k];
-    double gp = grad_extrap(p, X.c, id, nd, s, g.inv_h[k]);
-    double fcv = force.a[k][X.c];
-    double flo = id > 0 ? face_vec<DIM>(force, X.c - s, X.c, k, fc.geometric) : fcv;
-    double fhi = id < nd - 1 ? face_vec<DIM>(force, X.c, X.c + s, k, fc.geometric) : fcv;
-    double fr = 0.5 * (flo + fhi);
+    // the pressure gradient stays FP64: p carries the hydrostatic level,
+    // whose FP32 rounding would swamp differences across a cell
+    double gpd = grad_extrap(p, X.c, id, nd, s, g64.inv_h[k]);
+    gp64.a[k][X.c] = gpd;
+    T gp = (T)gpd;
+    T fcv = force.a[k][X.c];
+    T flo = id > 0 ? face_vec<DIM, T>(force, X.c - s, X.c, k, fc.geometric) : fcv;
+    T fhi = id < nd - 1 ? face_vec<DIM, T>(force, X.c, X.c + s, k, fc.geometric) : fcv;
+    T fr = T(0.5) * (flo + fhi);
     fres.a[k][X.c] = fr;
-    double v = -gp + fr + stforce.a[k][X.c];
+    T v = -gp + fr + stforce.a[k][X.c];
     if (fc.sources) v += u.a[k][X.c] * src;
     fo.a[k][X.c] = acc[k] + v;
   }
@@ -148,97 +173,96 @@ __global__ void k_force(Mesh m, Geo g, FluidCoef fc, C3 u, CP<9> G, const double
 // depend only on F, rho, mu and are shared; the constants differ.
 // Convective face value: deferred second-order upwind (solver.hpp:201-243,
 // threshold 1e-10); diffusion: two-point (solver.hpp:283-341); BDF time
-// term (solver.hpp:815-861).  Stores the relaxed diagonal, the 2*DIM
-// off-diagonals (face order xm,xp,ym,yp,zm,zp; 0 on boundary faces), the
-// delta-form residuals r_n = row_n(u_prev) and D_c = sum of the relaxed
-// row coefficients (fluid.hpp:876-883).
-template <int DIM>
-__global__ void k_mom_assemble(Mesh m, Geo g, FluidCoef fc, C3 up, C3 utc, C3 utp, CP<9> G,
-                               const double* F, const double* rho, const double* mu, C3 fo,
-                               WP<7> coef, W3 res, FP<10> o32, double* Dc, int kch) {
+// term (solver.hpp:815-861).  Stores the inverse of the relaxed diagonal,
+// the 2*DIM off-diagonals (face order xm,xp,ym,yp,zm,zp; 0 on boundary
+// faces), the delta-form residuals r_n = row_n(u_prev) and D_c = sum of the
+// relaxed row coefficients (fluid.hpp:876-883).  Per inner face the
+// convective flux enters as s_f F rho/V with the upwind weights selected,
+// not multiplied, and the deferred correction's factor is formed once for
+// the DIM components.  The BDF time difference of the residual is formed
+// in FP64 from the FP64 layers (us) whatever T is.
+template <int DIM, class T>
+__global__ void k_mom_assemble(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> up, RT<T, 3> utc,
+                               RT<T, 3> utp, RT<T, 9> G, const T* F, const T* rho, const T* mu,
+                               RT<T, 3> fo, Unsteady64 us, WT<T, 7> coef, WT<T, 3> res, T* Dc,
+                               int kch) {
   CELL_LOOP_BEGIN(m, kch)
-  const double rhoc = rho[X.c], muc = mu[X.c];
-  double aP = fc.co[2] * rhoc;
-  double aq[2 * DIM];
-  double cst[DIM];
+  const T rhoc = rho[X.c], muc = mu[X.c];
+  T aPc = T(0);  // convective and diffusive part of the diagonal
+  T aq[2 * DIM];
+  T cst[DIM];
 #pragma unroll
-  for (int n = 0; n < DIM; ++n)
-    cst[n] = (fc.co[0] * utp.a[n][X.c] + fc.co[1] * utc.a[n][X.c]) * rhoc - fo.a[n][X.c];
-  const double rv = rhoc * g.invV;
+  for (int n = 0; n < DIM; ++n) cst[n] = -fo.a[n][X.c];
+  const T rv = rhoc * g.invV;
+  const T thr = T(1e-10);
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     long long s = cell_stride(m, d);
     long long fs = face_stride(m, d);
     int id = X.i[d], nd = m.n[d];
     long long flo = face_id(m, d, X.i[0], X.i[1], X.i[2]);
-    const double hh = 0.5 * g.h[d];
+    const T hh = T(0.5) * g.h[d];
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
       long long f = flo + side * fs;
-      double Ff = F[f];
-      double so = side ? 1. : -1.;
+      const T Ff = F[f];
+      // outward convective flux times rho/V (s_f = -1 on the low face)
+      const T Fo = side ? Ff * rv : -(Ff * rv);
       bool inner = side ? (id < nd - 1) : (id > 0);
       if (inner) {
         long long nb = side ? X.c + s : X.c - s;
-        double dif = face_scal(muc, mu[nb], fc.geometric) * g.inv_h2[d];
-        double wm, wp;
-        int up_side;  // 0: cm upwind, 1: cp upwind, -1: central
-        if (Ff > 1e-10) {
-          wm = 1.; wp = 0.; up_side = 0;
-        } else if (Ff < -1e-10) {
-          wm = 0.; wp = 1.; up_side = 1;
-        } else {
-          wm = 0.5; wp = 0.5; up_side = -1;
-        }
-        // the cell is cm of its high face and cp of its low face
-        double wown = side ? wm : wp, wnb = side ? wp : wm;
-        aP += (wown * Ff * so) * rv + dif;
-        aq[2 * d + side] = (wnb * Ff * so) * rv - dif;
-        if (up_side >= 0) {
-          bool up_is_own = side ? (up_side == 0) : (up_side == 1);
-          long long cu = up_is_own ? X.c : nb;
-          double sg = up_side == 0 ? hh : -hh;  // -(x_up - x_f) along d
+        T dif = face_scal(muc, mu[nb], fc.geometric) * g.inv_h2[d];
+        // the cell is the low-side cell (cm) of its high face and the
+        // high-side cell (cp) of its low face
+        const bool up_m = Ff > thr, up_p = Ff < -thr;
+        const bool own_up = side ? up_m : up_p;
+        const bool nb_up = side ? up_p : up_m;
+        const T half = T(0.5) * Fo;
+        T ao = own_up ? Fo : (nb_up ? T(0) : half);
+        T an = nb_up ? Fo : (own_up ? T(0) : half);
+        aPc += ao + dif;
+        aq[2 * d + side] = an - dif;
+        if (up_m || up_p) {
+          long long cu = own_up ? X.c : nb;
+          // -(x_up - x_f) along d times the outward flux
+          T t = (up_m ? hh : -hh) * Fo;
 #pragma unroll
-          for (int n = 0; n < DIM; ++n) cst[n] += (G.a[n * DIM + d][cu] * sg * Ff * so) * rv;
+          for (int n = 0; n < DIM; ++n) cst[n] += G.a[n * DIM + d][cu] * t;
         }
       } else {
-        double dif = 2. * muc * g.inv_h2[d];
-        aP += dif;
-        aq[2 * d + side] = 0.;
+        T dif = T(2) * muc * g.inv_h2[d];
+        aPc += dif;
+        aq[2 * d + side] = T(0);
+        const T w = Fo - dif;
 #pragma unroll
-        for (int n = 0; n < DIM; ++n) {
-          double val = fc.bcu[2 * d + side][n];
-          cst[n] += (val * Ff * so) * rv - dif * val;
-        }
+        for (int n = 0; n < DIM; ++n) cst[n] += fc.bcu[2 * d + side][n] * w;
       }
     }
   }
-  double cs = aP;
+  const T aP = fc.co[2] * rhoc + aPc;
+  T cs = aP;
 #pragma unroll
   for (int q = 0; q < 2 * DIM; ++q) cs += aq[q];
 #pragma unroll
   for (int n = 0; n < DIM; ++n) {
-    double r = cst[n] + aP * up.a[n][X.c];
+    // BDF time difference in FP64 (its terms cancel to the small change
+    // of u over the step), then scaled by rho in T
+    double ut = us.co[0] * us.utp[n][X.c] + us.co[1] * us.utc[n][X.c] +
+                us.co[2] * us.up[n][X.c];
+    T r = (T)ut * rhoc + cst[n] + aPc * up.a[n][X.c];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       long long s = cell_stride(m, d);
       if (X.i[d] > 0) r += aq[2 * d] * up.a[n][X.c - s];
       if (X.i[d] < m.n[d] - 1) r += aq[2 * d + 1] * up.a[n][X.c + s];
     }
-    if (o32.a[0]) o32.a[7 + n][X.c] = (float)r;
-    else res.a[n][X.c] = r;
+    res.a[n][X.c] = r;
   }
-  double aPr = aP / fc.relax_u;
+  T aPr = aP / fc.relax_u;
   // the sweep multiplies by the inverse diagonal
-  if (o32.a[0]) {
-    o32.a[0][X.c] = (float)(1. / aPr);
+  coef.a[0][X.c] = T(1) / aPr;
 #pragma unroll
-    for (int q = 0; q < 2 * DIM; ++q) o32.a[1 + q][X.c] = (float)aq[q];
-  } else {
-    coef.a[0][X.c] = 1. / aPr;
-#pragma unroll
-    for (int q = 0; q < 2 * DIM; ++q) coef.a[1 + q][X.c] = aq[q];
-  }
+  for (int q = 0; q < 2 * DIM; ++q) coef.a[1 + q][X.c] = aq[q];
   Dc[X.c] = cs - aP + aPr;
   CELL_LOOP_END
 }
@@ -340,40 +364,51 @@ __global__ void k_f2d3(long long n, int dim, FP<3> in, W3 out) {
 // ------------------------------------------------------------ Rhie-Chow --
 // Face volume fluxes F* by momentum interpolation (fluid.hpp:889-942) and
 // face couplings kf = A/(h D_f) of the flux-correction expressions
-// (fluid.hpp:946-970); boundary faces carry u_wall.S and kf = 0.
-template <int DIM>
-__global__ void k_rhie_chow(Mesh m, Geo g, FluidCoef fc, C3 up, C3 du, const double* p,
-                            C3 force, C3 fres, const double* Dc, double* Fs, double* kf,
-                            int kch) {
+// (fluid.hpp:946-970); boundary faces carry u_wall.S and kf = 0.  F* and kf
+// are stored in FP64 whatever the arithmetic type T, so that the pressure
+// system, its FP64 residual and the flux correction see the same numbers;
+// kf32 (optional) receives the FP32 couplings of the mixed-precision solve.
+// The face velocity and the pressure part of the correction are FP64 (up,
+// p, gp are the FP64 iterate and cell pressure gradient); D_f, the force
+// terms and du are in T.
+template <int DIM, class T>
+__global__ void k_rhie_chow(Mesh m, Geo g64, GeoT<T> g, FluidCoef fc64, FluidCoefT<T> fc, C3 up,
+                            RT<T, 3> du, const double* p, C3 gp, RT<T, 3> force, RT<T, 3> fres,
+                            const T* Dc, double* Fs, double* kf, float* kf32, int kch) {
   CELL_LOOP_BEGIN(m, kch)
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     long long s = cell_stride(m, d);
     int id = X.i[d], nd = m.n[d];
     long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
-    double mv = fc.meshvel[d] * g.A[d];
+    const double A = g64.A[d];
+    const double mv = fc64.meshvel[d] * A;
     if (id > 0) {
       long long cm = X.c - s, cp = X.c;
-      double uf = avg(up.a[d][cm] + du.a[d][cm], up.a[d][cp] + du.a[d][cp]);
-      double vfi = uf * g.A[d];
-      double gpm = grad_extrap(p, cm, id - 1, nd, s, g.inv_h[d]);
-      double gpp = grad_extrap(p, cp, id, nd, s, g.inv_h[d]);
-      double gpf = avg(gpm, gpp);
-      double frf = face_vec<DIM>(fres, cm, cp, d, fc.geometric);
-      double fxf = face_vec<DIM>(force, cm, cp, d, fc.geometric);
-      double wide = (gpf - frf) * g.A[d];
-      double compact = (p[cp] - p[cm]) * g.inv_h[d] * g.A[d] - fxf * g.A[d];
-      double Df = avg(Dc[cm], Dc[cp]);
-      Fs[f] = vfi + fc.rc * (wide - compact) / Df - mv;
-      kf[f] = g.A[d] / (g.h[d] * Df);
+      // FP64: the interpolated velocity and the difference of the wide and
+      // compact pressure gradients (the cell gradients come from k_force)
+      double uf = avg(up.a[d][cm] + (double)du.a[d][cm], up.a[d][cp] + (double)du.a[d][cp]);
+      double vfi = uf * A;
+      double gpf = avg(gp.a[d][cm], gp.a[d][cp]);
+      double dpw = gpf - (p[cp] - p[cm]) * g64.inv_h[d];
+      T frf = face_vec<DIM, T>(fres, cm, cp, d, fc.geometric);
+      T fxf = face_vec<DIM, T>(force, cm, cp, d, fc.geometric);
+      T iDf = T(1) / avg(Dc[cm], Dc[cp]);
+      T k = g.A[d] * g.inv_h[d] * iDf;
+      T corr = fc.rc * (((T)dpw + (fxf - frf)) * g.A[d]) * iDf;
+      Fs[f] = vfi + (double)corr - mv;
+      kf[f] = (double)k;
+      if (kf32) kf32[f] = (float)k;
     } else {
-      Fs[f] = fc.bcu[2 * d][d] * g.A[d] - mv;
+      Fs[f] = fc64.bcu[2 * d][d] * A - mv;
       kf[f] = 0.;
+      if (kf32) kf32[f] = 0.f;
     }
     if (id == nd - 1) {
       long long fh = f + face_stride(m, d);
-      Fs[fh] = fc.bcu[2 * d + 1][d] * g.A[d] - mv;
+      Fs[fh] = fc64.bcu[2 * d + 1][d] * A - mv;
       kf[fh] = 0.;
+      if (kf32) kf32[fh] = 0.f;
     }
   }
   CELL_LOOP_END
@@ -400,34 +435,44 @@ __global__ void k_pressure_rhs(Mesh m, Geo g, const double* Fs, const double* Sv
 // fluid.hpp:1033-1057: p += alpha_p p'; u = u* - grad p'/D_c (p' faces
 // extrapolated); F = F* + kf (p'_cm - p'_cp).  Reduces the SIMPLE
 // convergence indicator max_c |u_c - u_prev,c| (CalcDiff,
-// solver.hpp:804-813) into ds->red[RS_INDICATOR].
+// solver.hpp:804-813) into ds->red[RS_INDICATOR].  Mixed precision: the
+// velocity correction du and D_c come in FP32 (du32, Dc32 non-null), the
+// update itself is FP64, and the FP32 shadows of the new iterate (u32,
+// p32, F32) are written beside it.
 template <int DIM>
 __global__ void __launch_bounds__(NT) k_correct(Mesh m, Geo g, FluidCoef fc, C3 up, C3 du,
-                                                W3 uic, const double* pip, double* pic,
+                                                RT<float, 3> du32, const float* Dc32, W3 uic,
+                                                const double* pip, double* pic,
                                                 const double* pc, const double* Dc,
                                                 const double* Fs, const double* kf,
-                                                double* Fic, double* partials, DevScalars* ds,
-                                                int kch) {
+                                                double* Fic, FP<3> u32, float* p32, float* F32,
+                                                double* partials, DevScalars* ds, int kch) {
   double dmax = 0.;
   CELL_LOOP_BEGIN(m, kch)
-  pic[X.c] = pip[X.c] + fc.relax_p * pc[X.c];
-  double dc = Dc[X.c];
+  double pn = pip[X.c] + fc.relax_p * pc[X.c];
+  pic[X.c] = pn;
+  if (p32) p32[X.c] = (float)pn;
+  double idc = -1. / (Dc32 ? (double)Dc32[X.c] : Dc[X.c]);
   double d2 = 0.;
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
     long long s = cell_stride(m, k);
     double gpc = grad_extrap(pc, X.c, X.i[k], m.n[k], s, g.inv_h[k]);
     double u0 = up.a[k][X.c];
-    double un = (u0 + du.a[k][X.c]) + gpc / (-dc);
+    double duk = du32.a[0] ? (double)du32.a[k][X.c] : du.a[k][X.c];
+    double un = (u0 + duk) + gpc * idc;
     uic.a[k][X.c] = un;
+    if (u32.a[0]) u32.a[k][X.c] = (float)un;
     double dd = un - u0;
     d2 += dd * dd;
     long long f = face_id(m, k, X.i[0], X.i[1], X.i[2]);
-    if (X.i[k] > 0) Fic[f] = Fs[f] + kf[f] * (pc[X.c - s] - pc[X.c]);
-    else Fic[f] = Fs[f];
+    double fv = X.i[k] > 0 ? Fs[f] + kf[f] * (pc[X.c - s] - pc[X.c]) : Fs[f];
+    Fic[f] = fv;
+    if (F32) F32[f] = (float)fv;
     if (X.i[k] == m.n[k] - 1) {
       long long fh = f + face_stride(m, k);
       Fic[fh] = Fs[fh];
+      if (F32) F32[fh] = (float)Fs[fh];
     }
   }
   dmax = fmax(dmax, sqrt(d2));
@@ -645,6 +690,33 @@ __global__ void k_init_flux(Mesh m, Geo g, FluidCoef fc, C3 u, double* F, int kc
     count_launches(1);                                                   \
     return cudaGetLastError();                                           \
   } while (0)
+#define DISPATCH_DIM_T(m, KERNEL, T, ...)                                \
+  do {                                                                   \
+    Launch L = cell_launch(m);                                           \
+    if ((m).dim == 3)                                                    \
+      KERNEL<3, T><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);      \
+    else                                                                 \
+      KERNEL<2, T><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);      \
+    count_launches(1);                                                   \
+    return cudaGetLastError();                                           \
+  } while (0)
+
+template <class T>
+FluidCoefT<T> coef_as(const FluidCoef& fc) {
+  FluidCoefT<T> r;
+  for (int a = 0; a < 6; ++a)
+    for (int k = 0; k < 3; ++k) r.bcu[a][k] = (T)fc.bcu[a][k];
+  r.relax_u = (T)fc.relax_u;
+  r.relax_p = (T)fc.relax_p;
+  r.rc = (T)fc.rc;
+  for (int k = 0; k < 3; ++k) {
+    r.co[k] = (T)fc.co[k];
+    r.meshvel[k] = (T)fc.meshvel[k];
+  }
+  r.geometric = fc.geometric;
+  r.sources = fc.sources;
+  return r;
+}
 
 static int flat_blocks(long long n) {
   long long b = (n + NT - 1) / NT;
@@ -671,23 +743,68 @@ cudaError_t launch_init_flux(const Mesh& m, const FluidCoef& fc, C3 u, double* F
   DISPATCH_DIM(m, k_init_flux, m, make_geo(m), fc, u, F);
 }
 
-cudaError_t launch_vel_grad(const Mesh& m, const FluidCoef& fc, C3 u, WP<9> G, cudaStream_t st) {
-  DISPATCH_DIM(m, k_vel_grad, m, make_geo(m), fc, u, G);
+template <class T>
+cudaError_t launch_vel_grad(const Mesh& m, const FluidCoef& fc, RT<T, 3> u, WT<T, 9> G,
+                            cudaStream_t st) {
+  DISPATCH_DIM_T(m, k_vel_grad, T, m, make_geo<T>(m), coef_as<T>(fc), u, G);
 }
 
-cudaError_t launch_force(const Mesh& m, const FluidCoef& fc, C3 u, CP<9> G, const double* p,
-                         const double* mu, const double* rho, C3 force, C3 stforce,
-                         const double* Sv, const double* Sm, W3 fo, W3 fres, cudaStream_t st) {
-  DISPATCH_DIM(m, k_force, m, make_geo(m), fc, u, G, p, mu, rho, force, stforce, Sv, Sm, fo,
-               fres);
+template <class T>
+cudaError_t launch_force(const Mesh& m, const FluidCoef& fc, RT<T, 3> u, RT<T, 9> G,
+                         const double* p, const T* mu, const T* rho, RT<T, 3> force,
+                         RT<T, 3> stforce, const T* Sv, const T* Sm, WT<T, 3> fo,
+                         WT<T, 3> fres, W3 gp, cudaStream_t st) {
+  DISPATCH_DIM_T(m, k_force, T, m, make_geo<T>(m), coef_as<T>(fc), u, G, p, make_geo(m), mu,
+                 rho, force, stforce, Sv, Sm, fo, fres, gp);
 }
 
-cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 u_tc,
-                                C3 u_tp, CP<9> G, const double* F, const double* rho,
-                                const double* mu, C3 fo, WP<7> coef, W3 res, FP<10> o32,
-                                double* Dc, cudaStream_t st) {
-  DISPATCH_DIM(m, k_mom_assemble, m, make_geo(m), fc, u_prev, u_tc, u_tp, G, F, rho, mu, fo,
-               coef, res, o32, Dc);
+template <class T>
+cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, RT<T, 3> u_prev,
+                                RT<T, 3> u_tc, RT<T, 3> u_tp, RT<T, 9> G, const T* F,
+                                const T* rho, const T* mu, RT<T, 3> fo, C3 up64, C3 utc64,
+                                C3 utp64, WT<T, 7> coef, WT<T, 3> res, T* Dc, cudaStream_t st) {
+  Unsteady64 us;
+  for (int k = 0; k < 3; ++k) {
+    us.co[k] = fc.co[k];
+    us.up[k] = up64.a[k];
+    us.utc[k] = utc64.a[k];
+    us.utp[k] = utp64.a[k];
+  }
+  DISPATCH_DIM_T(m, k_mom_assemble, T, m, make_geo<T>(m), coef_as<T>(fc), u_prev, u_tc, u_tp,
+                 G, F, rho, mu, fo, us, coef, res, Dc);
+}
+
+template <class T>
+cudaError_t launch_rhie_chow(const Mesh& m, const FluidCoef& fc, C3 u_prev, RT<T, 3> du,
+                             const double* p, C3 gp, RT<T, 3> force, RT<T, 3> fres,
+                             const T* Dc, double* Fs, double* kf, float* kf32,
+                             cudaStream_t st) {
+  DISPATCH_DIM_T(m, k_rhie_chow, T, m, make_geo(m), make_geo<T>(m), fc, coef_as<T>(fc), u_prev,
+                 du, p, gp, force, fres, Dc, Fs, kf, kf32);
+}
+
+#define HG_INST_FLUID(T)                                                                      \
+  template cudaError_t launch_vel_grad<T>(const Mesh&, const FluidCoef&, RT<T, 3>, WT<T, 9>,  \
+                                          cudaStream_t);                                      \
+  template cudaError_t launch_force<T>(const Mesh&, const FluidCoef&, RT<T, 3>, RT<T, 9>,     \
+                                       const double*, const T*, const T*, RT<T, 3>, RT<T, 3>, \
+                                       const T*, const T*, WT<T, 3>, WT<T, 3>, W3,            \
+                                       cudaStream_t);                                         \
+  template cudaError_t launch_mom_assemble<T>(const Mesh&, const FluidCoef&, RT<T, 3>,        \
+                                              RT<T, 3>, RT<T, 3>, RT<T, 9>, const T*,         \
+                                              const T*, const T*, RT<T, 3>, C3, C3, C3,       \
+                                              WT<T, 7>, WT<T, 3>, T*, cudaStream_t);          \
+  template cudaError_t launch_rhie_chow<T>(const Mesh&, const FluidCoef&, C3, RT<T, 3>,       \
+                                           const double*, C3, RT<T, 3>, RT<T, 3>, const T*,   \
+                                           double*, double*, float*, cudaStream_t);
+HG_INST_FLUID(double)
+HG_INST_FLUID(float)
+#undef HG_INST_FLUID
+
+cudaError_t launch_d2f(long long n, const double* in, float* out, cudaStream_t st) {
+  k_d2f<<<flat_blocks(n), NT, 0, st>>>(n, in, out);
+  count_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_mom_sweep32(const Mesh& m, double omega, double tol, FP<10> c, FP<3> din,
@@ -708,23 +825,18 @@ cudaError_t launch_mom_sweep(const Mesh& m, double omega, double tol, CP<7> coef
   DISPATCH_DIM(m, k_mom_sweep, m, omega, tol, coef, res, din, dout, first, partials, ds);
 }
 
-cudaError_t launch_rhie_chow(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du,
-                             const double* p, C3 force, C3 fres, const double* Dc, double* Fs,
-                             double* kf, cudaStream_t st) {
-  DISPATCH_DIM(m, k_rhie_chow, m, make_geo(m), fc, u_prev, du, p, force, fres, Dc, Fs, kf);
-}
-
 cudaError_t launch_pressure_rhs(const Mesh& m, const double* Fs, const double* Sv, double* f,
                                 cudaStream_t st) {
   DISPATCH_DIM(m, k_pressure_rhs, m, make_geo(m), Fs, Sv, f);
 }
 
-cudaError_t launch_correct(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du, W3 u_ic,
-                           const double* p_ip, double* p_ic, const double* pc,
-                           const double* Dc, const double* Fs, const double* kf,
-                           double* F_ic, double* partials, DevScalars* ds, cudaStream_t st) {
-  DISPATCH_DIM(m, k_correct, m, make_geo(m), fc, u_prev, du, u_ic, p_ip, p_ic, pc, Dc, Fs, kf,
-               F_ic, partials, ds);
+cudaError_t launch_correct(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du,
+                           RT<float, 3> du32, const float* Dc32, W3 u_ic, const double* p_ip,
+                           double* p_ic, const double* pc, const double* Dc, const double* Fs,
+                           const double* kf, double* F_ic, FP<3> u32, float* p32, float* F32,
+                           double* partials, DevScalars* ds, cudaStream_t st) {
+  DISPATCH_DIM(m, k_correct, m, make_geo(m), fc, u_prev, du, du32, Dc32, u_ic, p_ip, p_ic, pc,
+               Dc, Fs, kf, F_ic, u32, p32, F32, partials, ds);
 }
 
 cudaError_t launch_auto_dt(const Mesh& m, const double* F, double* partials, DevScalars* ds,

@@ -12,33 +12,38 @@ namespace hg {
 
 #define HYDRO_MAXPH 4
 
-// Pointer tables passed by value as kernel parameters.
-template <int N>
-struct CP {
-  const double* a[N];
+// Pointer tables passed by value as kernel parameters: RT reads, WT writes.
+template <class T, int N>
+struct RT {
+  const T* a[N];
+};
+template <class T, int N>
+struct WT {
+  T* a[N];
 };
 template <int N>
-struct WP {
-  double* a[N];
-};
+using CP = RT<double, N>;
+template <int N>
+using WP = WT<double, N>;
+template <int N>
+using FP = WT<float, N>;
 using C3 = CP<3>;
 using W3 = WP<3>;
-template <int N>
-struct FP {
-  float* a[N];
-};
 
-// Per-case constants of the momentum / pressure-correction kernels.
-struct FluidCoef {
-  double bcu[6][3];  // wall velocity per side and component
-  double relax_u;    // velocity_relaxation_factor
-  double relax_p;    // pressure_relaxation_factor
-  double rc;         // rhie_chow_factor
-  double co[3];      // BDF coefficients for (n-1, n, n+1)
-  double meshvel[3];
-  int geometric;     // force_geometric_average
-  int sources;       // volume/mass sources present
+// Per-case constants of the momentum / pressure-correction kernels, in the
+// arithmetic type of the kernel that reads them.
+template <class T>
+struct FluidCoefT {
+  T bcu[6][3];  // wall velocity per side and component
+  T relax_u;    // velocity_relaxation_factor
+  T relax_p;    // pressure_relaxation_factor
+  T rc;         // rhie_chow_factor
+  T co[3];      // BDF coefficients for (n-1, n, n+1)
+  T meshvel[3];
+  int geometric;  // force_geometric_average
+  int sources;    // volume/mass sources present
 };
+using FluidCoef = FluidCoefT<double>;
 
 // Device scalars shared by reductions and convergence flags.
 struct DevScalars {
@@ -72,14 +77,30 @@ cudaError_t launch_start_step(const Mesh& m, double ge, W3 u_ic, C3 u_tc, C3 u_t
                               cudaStream_t st);
 cudaError_t launch_init_flux(const Mesh& m, const FluidCoef& fc, C3 u, double* F,
                              cudaStream_t st);
-cudaError_t launch_vel_grad(const Mesh& m, const FluidCoef& fc, C3 u, WP<9> G, cudaStream_t st);
-cudaError_t launch_force(const Mesh& m, const FluidCoef& fc, C3 u, CP<9> G, const double* p,
-                         const double* mu, const double* rho, C3 force, C3 stforce,
-                         const double* Sv, const double* Sm, W3 fo, W3 fres, cudaStream_t st);
-cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 u_tc,
-                                C3 u_tp, CP<9> G, const double* F, const double* rho,
-                                const double* mu, C3 fo, WP<7> coef, W3 res, FP<10> o32,
-                                double* Dc, cudaStream_t st);
+// The SIMPLE-iteration kernels, templated on the arithmetic type: double
+// for the FP64 path, float for the mixed path (FP32 shadows of the state).
+template <class T>
+cudaError_t launch_vel_grad(const Mesh& m, const FluidCoef& fc, RT<T, 3> u, WT<T, 9> G,
+                            cudaStream_t st);
+template <class T>
+cudaError_t launch_force(const Mesh& m, const FluidCoef& fc, RT<T, 3> u, RT<T, 9> G,
+                         const double* p, const T* mu, const T* rho, RT<T, 3> force,
+                         RT<T, 3> stforce, const T* Sv, const T* Sm, WT<T, 3> fo,
+                         WT<T, 3> fres, W3 gp, cudaStream_t st);
+// coef = {1/diag, 2*DIM off-diagonals}, res = DIM residuals; up64/utc64/
+// utp64 are the FP64 velocity layers of the residual's time difference
+template <class T>
+cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, RT<T, 3> u_prev,
+                                RT<T, 3> u_tc, RT<T, 3> u_tp, RT<T, 9> G, const T* F,
+                                const T* rho, const T* mu, RT<T, 3> fo, C3 up64, C3 utc64,
+                                C3 utp64, WT<T, 7> coef, WT<T, 3> res, T* Dc, cudaStream_t st);
+// u_prev, p, gp (cell pressure gradient from launch_force) are FP64
+template <class T>
+cudaError_t launch_rhie_chow(const Mesh& m, const FluidCoef& fc, C3 u_prev, RT<T, 3> du,
+                             const double* p, C3 gp, RT<T, 3> force, RT<T, 3> fres,
+                             const T* Dc, double* Fs, double* kf, float* kf32,
+                             cudaStream_t st);
+cudaError_t launch_d2f(long long n, const double* in, float* out, cudaStream_t st);
 // Mixed path: FP32 Jacobi sweep on the o32 output of the assembly
 // (o32 = {1/diag, 2*DIM off-diagonals, DIM residuals}); FP32 -> FP64 copy.
 cudaError_t launch_mom_sweep32(const Mesh& m, double omega, double tol, FP<10> c, FP<3> din,
@@ -89,15 +110,15 @@ cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st);
 cudaError_t launch_mom_sweep(const Mesh& m, double omega, double tol, CP<7> coef, C3 res,
                              C3 din, W3 dout, int first, double* partials, DevScalars* ds,
                              cudaStream_t st);
-cudaError_t launch_rhie_chow(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du,
-                             const double* p, C3 force, C3 fres, const double* Dc, double* Fs,
-                             double* kf, cudaStream_t st);
 cudaError_t launch_pressure_rhs(const Mesh& m, const double* Fs, const double* Sv, double* f,
                                 cudaStream_t st);
-cudaError_t launch_correct(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du, W3 u_ic,
-                           const double* p_ip, double* p_ic, const double* pc,
-                           const double* Dc, const double* Fs, const double* kf,
-                           double* F_ic, double* partials, DevScalars* ds, cudaStream_t st);
+// du32/Dc32 non-null: FP32 velocity correction and D_c of the mixed path;
+// u32, p32, F32 non-null: also write those FP32 shadows of the iterate.
+cudaError_t launch_correct(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du,
+                           RT<float, 3> du32, const float* Dc32, W3 u_ic, const double* p_ip,
+                           double* p_ic, const double* pc, const double* Dc, const double* Fs,
+                           const double* kf, double* F_ic, FP<3> u32, float* p32, float* F32,
+                           double* partials, DevScalars* ds, cudaStream_t st);
 cudaError_t launch_auto_dt(const Mesh& m, const double* F, double* partials, DevScalars* ds,
                            cudaStream_t st);
 cudaError_t launch_nan_count(long long n, const double* a, double* partials, DevScalars* ds,

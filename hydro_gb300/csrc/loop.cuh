@@ -38,41 +38,40 @@ struct Cell {
 
 // Cell gradient (component along the axis of stride s) of a scalar whose
 // boundary faces are extrapolated (ConditionFaceExtrapolation,
-// solver.hpp:446-464).  On a uniform block that formula reduces to
-// p_b = 2 p_c - p_f(opposite face); needs nd >= 2.
+// solver.hpp:446-464): Green-Gauss over the two faces, face values the
+// mean of the adjacent cells, on a boundary face p_b = 2 p_c - p_f(opposite
+// face) (what the reference's extrapolation reduces to on a uniform block).
+// The cell value cancels, leaving one difference and one product:
+// interior (p+ - p-)/(2h), low end (p+ - p_c)/h, high end (p_c - p-)/h.
+// Needs nd >= 2.
 template <class T>
 __device__ __forceinline__ T grad_extrap(const T* p, long long c, int id, int nd, long long s,
                                          T inv_h) {
-  T pc = p[c];
-  T flo, fhi;
-  if (id > 0 && id < nd - 1) {
-    flo = avg(p[c - s], pc);
-    fhi = avg(pc, p[c + s]);
-  } else if (id == 0) {
-    fhi = avg(pc, p[c + s]);
-    flo = T(2) * pc - fhi;
-  } else {
-    flo = avg(p[c - s], pc);
-    fhi = T(2) * pc - flo;
-  }
-  return (fhi - flo) * inv_h;
+  if (id > 0 && id < nd - 1) return (p[c + s] - p[c - s]) * (T(0.5) * inv_h);
+  if (id == 0) return (p[c + s] - p[c]) * inv_h;
+  return (p[c] - p[c - s]) * inv_h;
 }
 
-struct Geo {
-  double inv_h[3], h[3], A[3], V, invV;
-  double inv_h2[3];
+template <class T>
+struct GeoT {
+  T inv_h[3], h[3], A[3], V, invV;
+  T inv_h2[3];
 };
+using Geo = GeoT<double>;
 
-inline Geo make_geo(const Mesh& m) {
-  Geo g;
+// Geometry of a uniform block; the factors are formed in FP64 and rounded
+// once to the kernel's arithmetic type.
+template <class T = double>
+inline GeoT<T> make_geo(const Mesh& m) {
+  GeoT<T> g;
   for (int d = 0; d < 3; ++d) {
-    g.h[d] = m.h[d];
-    g.inv_h[d] = 1. / m.h[d];
-    g.inv_h2[d] = 1. / (m.h[d] * m.h[d]);
-    g.A[d] = m.A[d];
+    g.h[d] = (T)m.h[d];
+    g.inv_h[d] = (T)(1. / m.h[d]);
+    g.inv_h2[d] = (T)(1. / (m.h[d] * m.h[d]));
+    g.A[d] = (T)m.A[d];
   }
-  g.V = m.V;
-  g.invV = 1. / m.V;
+  g.V = (T)m.V;
+  g.invV = (T)(1. / m.V);
   return g;
 }
 
