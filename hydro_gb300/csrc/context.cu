@@ -575,7 +575,7 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
     MgWork& mg = x->mg;
     mg.nlev = desc->pressure_solver == HYDRO_LINEAR_MGCG ? mg_levels_for(m) : 0;
     mg.nsweep = 2;
-    mg.coarse_sweeps = 64;
+    mg.coarse_sweeps = 8;
     mg.coarse_sweeps_large = 16;
     if (mg.nlev > 0) mg.lev[0].m = m;
     for (int l = 1; l < mg.nlev; ++l) {

@@ -201,16 +201,18 @@ cudaError_t cg32_dir_spmv(const Mesh& m, const float* kf, const float* dg, const
 
 // ------------------------------------------------------------ multigrid --
 constexpr int kMgMaxLevels = 12;
-constexpr long long kMgCoarseMax = 4096;    // coarsest level solved in one block
-constexpr long long kMgCoarseTarget = 512;  // coarsening stops at or below this
+constexpr long long kMgBlockMax = 4096;    // levels this small run inside one CTA
+constexpr long long kMgCoarseTarget = 64;  // coarsening stops at or below this
 struct MgLevel {
   Mesh m;
   float *kf, *dg, *idg, *x, *b;
 };
 struct MgWork {
   int nlev;
+  int top;                 // first level run inside one CTA (nlev: none)
+  int smem_bytes;          // shared memory of that CTA
   int nsweep;              // (red, black) sweeps before / after the correction
-  int coarse_sweeps;       // sweeps of the one-block coarsest solve
+  int coarse_sweeps;       // sweeps of the coarsest solve inside the CTA
   int coarse_sweeps_large; // sweeps when the coarsest level stays large
   MgLevel lev[kMgMaxLevels];
 };

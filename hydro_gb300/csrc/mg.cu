@@ -13,8 +13,10 @@
 //   smoother         = red-black Gauss-Seidel, (red, black) before and
 //                      (black, red) after the coarse correction, so the
 //                      V-cycle is symmetric and usable inside CG,
-//   coarsest level   = <= kMgCoarseMax cells, one block of red-black sweeps
-//                      on the zero-mean right-hand side.
+//   small levels     = every level of <= kMgBlockMax cells runs inside one
+//                      CTA in shared memory (a complete sub-V-cycle, its
+//                      coarsest level solved by symmetric red-black sweeps
+//                      on the zero-mean right-hand side).
 // All kernels return at once when the CG's done flag is set, so iterations
 // can be queued in chunks like the other solvers.
 #include <math.h>
@@ -29,10 +31,14 @@ namespace {
 // Red-black GS half-sweep on the cells with (i+j+k) % 2 == color.  Thread
 // (x, y) handles the color-matching cell of the pair (2x, 2x+1) in row
 // (j, k).  With `zero` set the cell's neighbours are taken as 0 (first
-// half-sweep from x = 0).
+// half-sweep from x = 0).  With `cx` set the neighbours are read as
+// x + cx(parent): the prolongation of the coarse correction fused into the
+// first post-smoothing half-sweep (the cells of the other color are
+// overwritten by the next half-sweep, which never reads their old value).
 template <int DIM>
 __global__ void k_mg_smooth(Mesh m, const float* kf, const float* idg, const float* b, float* x,
-                            int color, int zero, long long pin, const DevScalars* ds, int kch) {
+                            int color, int zero, long long pin, const float* cx, int cnx,
+                            int cny, const DevScalars* ds, int kch) {
   if (ds->flag[FL_PCG_DONE]) return;
   const int ih = blockIdx.x * BX + threadIdx.x;
   const int j = blockIdx.y * BY + threadIdx.y;
@@ -54,8 +60,19 @@ __global__ void k_mg_smooth(Mesh m, const float* kf, const float* idg, const flo
       for (int d = 0; d < DIM; ++d) {
         long long s = cell_stride(m, d);
         long long fl = face_id(m, d, i, j, k);
-        if (id[d] > 0 && c - s != pin) acc = fmaf(kf[fl], x[c - s], acc);
-        if (id[d] < m.n[d] - 1 && c + s != pin) acc = fmaf(kf[fl + face_stride(m, d)], x[c + s], acc);
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+          bool in = side ? id[d] < m.n[d] - 1 : id[d] > 0;
+          long long nb = side ? c + s : c - s;
+          if (!in || nb == pin) continue;
+          float xv = x[nb];
+          if (cx) {
+            int q[3] = {i, j, k};
+            q[d] += side ? 1 : -1;
+            xv += cx[(q[0] >> 1) + (long long)cnx * ((q[1] >> 1) + (long long)cny * (q[2] >> 1))];
+          }
+          acc = fmaf(kf[side ? fl + face_stride(m, d) : fl], xv, acc);
+        }
       }
     }
     x[c] = acc * idg[c];
@@ -141,64 +158,182 @@ __global__ void k_mg_restrict(Mesh fm, Mesh cm, const float* kf, const float* dg
   CELL_LOOP_END
 }
 
-// x_fine += x_coarse(parent)
+// ------------------------------------------------ levels inside one CTA --
+// The levels of at most kMgBlockMax cells form a complete sub-V-cycle run
+// by one CTA in shared memory: every level's couplings, inverse diagonal,
+// right-hand side and iterate live in shared memory, and the smoothing,
+// restriction and prolongation steps are separated by __syncthreads instead
+// of kernel launches.  Same smoother and transfers as the grid levels; the
+// coarsest level is solved by symmetric red-black sweeps, (red, black)^s
+// then (black, red)^s, on its zero-mean right-hand side.
+constexpr int kBlkThreads = 1024;
+
+struct MgBlock {
+  int nl;  // levels in the CTA, top first
+  int nsweep, coarse_sweeps;
+  long long pin;  // pinned cell of the top level (-1: none)
+  Mesh m[kMgMaxLevels];
+  const float* kf[kMgMaxLevels];
+  const float* idg[kMgMaxLevels];
+  int ox[kMgMaxLevels], ob[kMgMaxLevels], oi[kMgMaxLevels], ok[kMgMaxLevels];
+};
+
 template <int DIM>
-__global__ void k_mg_prolong(Mesh fm, const float* cx, float* x, int cnx, int cny,
-                             const DevScalars* ds, int kch) {
-  if (ds->flag[FL_PCG_DONE]) return;
-  CELL_LOOP_BEGIN(fm, kch)
-  long long pc = (X.i[0] >> 1) + (long long)cnx * ((X.i[1] >> 1) + (long long)cny * (X.i[2] >> 1));
-  x[X.c] += cx[pc];
-  CELL_LOOP_END
+__device__ __forceinline__ void blk_ijk(const Mesh& m, int c, int* id) {
+  id[0] = c % m.n[0];
+  int r = c / m.n[0];
+  id[1] = DIM == 3 ? r % m.n[1] : r;
+  id[2] = DIM == 3 ? r / m.n[1] : 0;
 }
 
-// Coarsest level in one block: zero-mean right-hand side, then `sweeps`
-// red-black GS sweeps from x = 0.
 template <int DIM>
-__global__ void k_mg_coarse_solve(Mesh m, const float* kf, const float* idg, float* b, float* x,
-                                  int sweeps, const DevScalars* ds) {
-  if (ds->flag[FL_PCG_DONE]) return;
-  __shared__ float red[32];
-  __shared__ float mean;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const long long n = m.nc;
-  float s = 0.f;
-  for (long long c = tid; c < n; c += nt) s += b[c];
-  s = warp_sum(s);
-  if ((tid & 31) == 0) red[tid >> 5] = s;
-  __syncthreads();
-  if (tid < 32) {
-    float v = tid < (nt + 31) / 32 ? red[tid] : 0.f;
-    v = warp_sum(v);
-    if (tid == 0) mean = v / (float)n;
-  }
-  __syncthreads();
-  for (long long c = tid; c < n; c += nt) {
-    b[c] -= mean;
-    x[c] = 0.f;
-  }
-  __syncthreads();
-  for (int sw = 0; sw < sweeps; ++sw) {
-    for (int color = 0; color < 2; ++color) {
-      for (long long c = tid; c < n; c += nt) {
-        int id[3];
-        id[0] = (int)(c % m.n[0]);
-        id[1] = (int)((c / m.n[0]) % m.n[1]);
-        id[2] = DIM == 3 ? (int)(c / ((long long)m.n[0] * m.n[1])) : 0;
-        if (((id[0] + id[1] + id[2]) & 1) != color) continue;
-        float acc = b[c];
+__device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const float* b,
+                         float* x, int color, bool zero, long long pin) {
+  const int n = (int)m.nc;
+  for (int c = threadIdx.x; c < n; c += blockDim.x) {
+    int id[3];
+    blk_ijk<DIM>(m, c, id);
+    if (((id[0] + id[1] + id[2]) & 1) != color) continue;
+    if (c == pin) {
+      x[c] = b[c];
+      continue;
+    }
+    float acc = b[c];
+    if (!zero) {
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          long long st = cell_stride(m, d);
-          long long fl = face_id(m, d, id[0], id[1], id[2]);
-          if (id[d] > 0) acc = fmaf(kf[fl], x[c - st], acc);
-          if (id[d] < m.n[d] - 1) acc = fmaf(kf[fl + face_stride(m, d)], x[c + st], acc);
+      for (int d = 0; d < DIM; ++d) {
+        int s = (int)cell_stride(m, d);
+        int fl = (int)face_id(m, d, id[0], id[1], id[2]);
+        if (id[d] > 0 && c - s != pin) acc = fmaf(kf[fl], x[c - s], acc);
+        if (id[d] < m.n[d] - 1 && c + s != pin)
+          acc = fmaf(kf[fl + (int)face_stride(m, d)], x[c + s], acc);
+      }
+    }
+    x[c] = acc * idg[c];
+  }
+  __syncthreads();
+}
+
+// coarse rhs = sum over the children of the fine residual b - A x
+template <int DIM>
+__device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, const float* b,
+                             const float* x, float* cb, long long pin) {
+  const int n = (int)cm.nc;
+  for (int C = threadIdx.x; C < n; C += blockDim.x) {
+    int I[3];
+    blk_ijk<DIM>(cm, C, I);
+    float sum = 0.f;
+#pragma unroll
+    for (int ck = 0; ck < (DIM == 3 ? 2 : 1); ++ck)
+#pragma unroll
+      for (int cj = 0; cj < 2; ++cj)
+#pragma unroll
+        for (int ci = 0; ci < 2; ++ci) {
+          int id[3] = {2 * I[0] + ci, 2 * I[1] + cj, DIM == 3 ? 2 * I[2] + ck : 0};
+          int c = (int)cell_id(fm, id[0], id[1], id[2]);
+          float r;
+          if (c == pin) {
+            r = b[c] - x[c];
+          } else {
+            float dg = 0.f, off = 0.f;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+              int s = (int)cell_stride(fm, d);
+              int fl = (int)face_id(fm, d, id[0], id[1], id[2]);
+              float klo = kf[fl], khi = kf[fl + (int)face_stride(fm, d)];
+              dg += klo + khi;
+              if (id[d] > 0 && c - s != pin) off = fmaf(klo, x[c - s], off);
+              if (id[d] < fm.n[d] - 1 && c + s != pin) off = fmaf(khi, x[c + s], off);
+            }
+            r = b[c] - (dg * x[c] - off);
+          }
+          sum += r;
         }
-        x[c] = acc * idg[c];
+    cb[C] = sum;
+  }
+  __syncthreads();
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kBlkThreads)
+    k_mg_block_vcycle(MgBlock B, const float* btop, float* xtop, const DevScalars* ds) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  extern __shared__ float sm[];
+  __shared__ float red[32];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int l = 0; l < B.nl; ++l) {
+    const int nf = (int)B.m[l].nf, nc = (int)B.m[l].nc;
+    for (int q = tid; q < nf; q += nt) sm[B.ok[l] + q] = B.kf[l][q];
+    for (int q = tid; q < nc; q += nt) sm[B.oi[l] + q] = B.idg[l][q];
+  }
+  for (int q = tid; q < (int)B.m[0].nc; q += nt) sm[B.ob[0] + q] = btop[q];
+  __syncthreads();
+  const int ns = B.nsweep;
+  for (int l = 0; l + 1 < B.nl; ++l) {
+    const Mesh& m = B.m[l];
+    long long lp = l == 0 ? B.pin : -1;
+    const float *kf = sm + B.ok[l], *idg = sm + B.oi[l], *b = sm + B.ob[l];
+    float* x = sm + B.ox[l];
+    for (int s = 0; s < ns; ++s) {
+      blk_half<DIM>(m, kf, idg, b, x, 0, s == 0, lp);
+      blk_half<DIM>(m, kf, idg, b, x, 1, false, lp);
+    }
+    blk_restrict<DIM>(m, B.m[l + 1], kf, b, x, sm + B.ob[l + 1], lp);
+  }
+  {
+    const int l = B.nl - 1;
+    const Mesh& m = B.m[l];
+    long long lp = l == 0 ? B.pin : -1;
+    const float *kf = sm + B.ok[l], *idg = sm + B.oi[l];
+    float* b = sm + B.ob[l];
+    float* x = sm + B.ox[l];
+    const int n = (int)m.nc;
+    if (lp < 0) {
+      // singular Neumann block: project the right-hand side to zero mean
+      float sv = 0.f;
+      for (int c = tid; c < n; c += nt) sv += b[c];
+      sv = warp_sum(sv);
+      if ((tid & 31) == 0) red[tid >> 5] = sv;
+      __syncthreads();
+      if (tid < 32) {
+        float v = tid < (nt + 31) / 32 ? red[tid] : 0.f;
+        v = warp_sum(v);
+        if (tid == 0) red[0] = v / (float)n;
       }
       __syncthreads();
+      const float mean = red[0];
+      for (int c = tid; c < n; c += nt) b[c] -= mean;
+      __syncthreads();
+    }
+    const int half = B.coarse_sweeps / 2 > 0 ? B.coarse_sweeps / 2 : 1;
+    for (int s = 0; s < half; ++s) {
+      blk_half<DIM>(m, kf, idg, b, x, 0, s == 0, lp);
+      blk_half<DIM>(m, kf, idg, b, x, 1, false, lp);
+    }
+    for (int s = 0; s < half; ++s) {
+      blk_half<DIM>(m, kf, idg, b, x, 1, false, lp);
+      blk_half<DIM>(m, kf, idg, b, x, 0, false, lp);
     }
   }
+  for (int l = B.nl - 2; l >= 0; --l) {
+    const Mesh& m = B.m[l];
+    const Mesh& cm = B.m[l + 1];
+    long long lp = l == 0 ? B.pin : -1;
+    const float *kf = sm + B.ok[l], *idg = sm + B.oi[l], *b = sm + B.ob[l];
+    float* x = sm + B.ox[l];
+    const float* cx = sm + B.ox[l + 1];
+    for (int c = tid; c < (int)m.nc; c += nt) {
+      int id[3];
+      blk_ijk<DIM>(m, c, id);
+      x[c] += cx[(int)cell_id(cm, id[0] >> 1, id[1] >> 1, id[2] >> 1)];
+    }
+    __syncthreads();
+    for (int s = 0; s < ns; ++s) {
+      blk_half<DIM>(m, kf, idg, b, x, 1, false, lp);
+      blk_half<DIM>(m, kf, idg, b, x, 0, false, lp);
+    }
+  }
+  for (int q = tid; q < (int)B.m[0].nc; q += nt) xtop[q] = sm[B.ox[0] + q];
 }
 
 struct DFAcc2 {
@@ -342,6 +477,24 @@ int mg_levels_for(const Mesh& m) {
     count_launches(1);                                                          \
   } while (0)
 
+// First level handled inside one CTA and that CTA's shared memory (x, b,
+// inverse diagonal and couplings of every level from there down, each
+// array 16-byte aligned); top = nlev when the coarsest level is too large.
+void mg_plan_block(MgWork& mg) {
+  mg.top = mg.nlev;
+  for (int l = 0; l < mg.nlev; ++l)
+    if (mg.lev[l].m.nc <= kMgBlockMax) {
+      mg.top = l;
+      break;
+    }
+  long long fl = 0;
+  for (int l = mg.top; l < mg.nlev; ++l) {
+    const Mesh& m = mg.lev[l].m;
+    fl += 3 * ((m.nc + 3) / 4 * 4) + (m.nf + 3) / 4 * 4;
+  }
+  mg.smem_bytes = (int)(fl * sizeof(float));
+}
+
 cudaError_t mg_setup(MgWork& mg, PcgWork& w, cudaStream_t st) {
   int dim = mg.lev[0].m.dim;
   mg.lev[0].kf = w.kf32;
@@ -354,61 +507,91 @@ cudaError_t mg_setup(MgWork& mg, PcgWork& w, cudaStream_t st) {
     MG_LAUNCH(k_mg_coarsen, L, f.m, c.m, f.kf, c.kf);
     MG_LAUNCH(k_mg_diag, L, c.m, c.kf, c.dg, c.idg);
   }
+  mg_plan_block(mg);
+  if (mg.top < mg.nlev) {
+    cudaError_t e = dim == 3 ? cudaFuncSetAttribute(k_mg_block_vcycle<3>,
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    mg.smem_bytes)
+                             : cudaFuncSetAttribute(k_mg_block_vcycle<2>,
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    mg.smem_bytes);
+    if (e != cudaSuccess) return e;
+  }
   return cudaGetLastError();
 }
 
 // z = M^-1 r: one V-cycle with `nsweep` (red, black) sweeps before and
-// (black, red) sweeps after each coarse correction.
+// (black, red) sweeps after each coarse correction.  Levels above `top`
+// are grid launches; `top` and below run in one CTA.
 cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevScalars* ds,
                       cudaStream_t st) {
   int dim = mg.lev[0].m.dim;
   mg.lev[0].b = const_cast<float*>(r);
   mg.lev[0].x = z;
   const int ns = mg.nsweep;
-  for (int l = 0; l + 1 < mg.nlev; ++l) {
+  const int top = mg.top < mg.nlev ? mg.top : mg.nlev - 1;
+  for (int l = 0; l < top; ++l) {
     MgLevel& f = mg.lev[l];
     long long lp = l == 0 ? pin : -1;
     Launch H = half_launch(f.m);
     for (int s = 0; s < ns; ++s) {
-      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 0, s == 0, lp, ds);
-      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, ds);
+      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 0, s == 0, lp, nullptr, 0, 0, ds);
+      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, nullptr, 0, 0, ds);
     }
     MgLevel& c = mg.lev[l + 1];
     Launch L = cell_launch(c.m);
     MG_LAUNCH(k_mg_restrict, L, f.m, c.m, f.kf, f.dg, f.b, f.x, c.b, c.x, lp, ds);
   }
-  MgLevel& cl = mg.lev[mg.nlev - 1];
-  if (mg.nlev > 1 && cl.m.nc <= kMgCoarseMax) {
+  if (mg.top < mg.nlev) {
+    MgBlock B;
+    B.nl = mg.nlev - mg.top;
+    B.nsweep = ns;
+    B.coarse_sweeps = mg.coarse_sweeps;
+    B.pin = mg.top == 0 ? pin : -1;
+    int off = 0;
+    for (int q = 0; q < B.nl; ++q) {
+      const MgLevel& lv = mg.lev[mg.top + q];
+      B.m[q] = lv.m;
+      B.kf[q] = lv.kf;
+      B.idg[q] = lv.idg;
+      const int c4 = (int)((lv.m.nc + 3) / 4 * 4), f4 = (int)((lv.m.nf + 3) / 4 * 4);
+      B.ox[q] = off; off += c4;
+      B.ob[q] = off; off += c4;
+      B.oi[q] = off; off += c4;
+      B.ok[q] = off; off += f4;
+    }
+    MgLevel& t = mg.lev[mg.top];
     if (dim == 3)
-      k_mg_coarse_solve<3><<<1, 1024, 0, st>>>(cl.m, cl.kf, cl.idg, cl.b, cl.x, mg.coarse_sweeps, ds);
+      k_mg_block_vcycle<3><<<1, kBlkThreads, mg.smem_bytes, st>>>(B, t.b, t.x, ds);
     else
-      k_mg_coarse_solve<2><<<1, 1024, 0, st>>>(cl.m, cl.kf, cl.idg, cl.b, cl.x, mg.coarse_sweeps, ds);
+      k_mg_block_vcycle<2><<<1, kBlkThreads, mg.smem_bytes, st>>>(B, t.b, t.x, ds);
     count_launches(1);
   } else {
     // large coarsest level (odd dimensions) or a single level: symmetric
     // smoothing only, (red, black)^s then (black, red)^s
-    long long lp = mg.nlev == 1 ? pin : -1;
+    MgLevel& cl = mg.lev[top];
+    long long lp = top == 0 ? pin : -1;
     Launch H = half_launch(cl.m);
     const int half = mg.coarse_sweeps_large / 2 > 0 ? mg.coarse_sweeps_large / 2 : 1;
     for (int s = 0; s < half; ++s) {
-      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, s == 0, lp, ds);
-      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 1, 0, lp, ds);
+      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, s == 0, lp, nullptr, 0, 0, ds);
+      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 1, 0, lp, nullptr, 0, 0, ds);
     }
     for (int s = 0; s < half; ++s) {
-      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 1, 0, lp, ds);
-      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, 0, lp, ds);
+      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 1, 0, lp, nullptr, 0, 0, ds);
+      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, 0, lp, nullptr, 0, 0, ds);
     }
   }
-  for (int l = mg.nlev - 2; l >= 0; --l) {
+  for (int l = top - 1; l >= 0; --l) {
     MgLevel& f = mg.lev[l];
     MgLevel& c = mg.lev[l + 1];
     long long lp = l == 0 ? pin : -1;
-    Launch L = cell_launch(f.m);
-    MG_LAUNCH(k_mg_prolong, L, f.m, c.x, f.x, c.m.n[0], c.m.n[1], ds);
     Launch H = half_launch(f.m);
     for (int s = 0; s < ns; ++s) {
-      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, ds);
-      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 0, 0, lp, ds);
+      // the first half-sweep adds the coarse correction on the fly
+      const float* cx = s == 0 ? c.x : nullptr;
+      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, cx, c.m.n[0], c.m.n[1], ds);
+      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 0, 0, lp, nullptr, 0, 0, ds);
     }
   }
   return cudaGetLastError();

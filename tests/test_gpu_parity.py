@@ -120,11 +120,14 @@ def test_mixed_precision_matches_fp64(built):
         assert s["pressure_residual"] <= 1e-10
 
 
-@pytest.mark.parametrize("shape", [(16, 16, 16), (24, 16, 8), (20, 12, 10)])
+@pytest.mark.parametrize("shape", [(16, 16, 16), (24, 16, 8), (20, 12, 10), (32, 32, 16),
+                                   (48, 32, 24)])
 def test_multigrid_cg_matches_fp64(built, shape):
     """Mixed precision with the multigrid-preconditioned CG: same fields as
     the FP64 Jacobi-CG path within the mixed tolerance, pressure residual
-    reached, few iterations (power-of-two and non-power-of-two blocks)."""
+    reached, few iterations (power-of-two and non-power-of-two blocks; the
+    first three run the whole V-cycle inside one CTA, the last two have one
+    and two grid levels above the in-CTA levels)."""
     from hydro_gb300.solver import Hydro
     d, u0, q0, _ = cases.rising_drops(n=16, seed=5, dt_max=5e-3)
     d.n[0], d.n[1], d.n[2] = shape
