@@ -281,6 +281,8 @@ def _declare(lib, prefix):
         lib.hydro_gpu_get_profile.restype = I
         lib.hydro_gpu_get_launch_count.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
         lib.hydro_gpu_get_launch_count.restype = I
+        lib.hydro_gpu_step_graph.argtypes = [P, ctypes.POINTER(StepStats)]
+        lib.hydro_gpu_step_graph.restype = I
     else:
         stencil.argtypes = [I, I, I, I, D, ctypes.c_double, ctypes.c_long,
                             ctypes.c_double, D, D, I, ctypes.c_double, I,

@@ -159,6 +159,17 @@ struct hydro_ctx {
     float *G = nullptr, *fo = nullptr, *fres = nullptr, *Dc = nullptr;
   } s32;
   bool mixed = false;
+  // graph-captured step (hydro_gpu_step_graph): capture state and the
+  // instantiated step with the values it was captured for
+  bool graph_mode = false;
+  cudaGraph_t cap_graph = nullptr;
+  cudaStream_t cap_streams[4] = {};
+  int cap_depth = 0;
+  struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    double dt = -1., adv_dt = -1.;
+    int substeps = -1, sources = -1;
+  } sg;
   PcgWork pw{};
   double* stat_out = nullptr;
   unsigned* stat_ticket = nullptr;
@@ -283,39 +294,119 @@ int reset_flags(hydro_ctx* x, int first, int count) {
   return HYDRO_OK;
 }
 
+// ------------------------------------------------- graph-captured loops --
+// Conditional handles belong to the top-level graph being captured.
+int new_handle(hydro_ctx* x, unsigned def, cudaGraphConditionalHandle* h) {
+  CK(cudaGraphConditionalHandleCreate(h, x->cap_graph, def, cudaGraphCondAssignDefault));
+  return HYDRO_OK;
+}
+
+// Adds a WHILE (or IF) node after the work captured so far on x->st and
+// captures `body` into it on the next capture stream.
+template <class Body>
+int add_conditional(hydro_ctx* x, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                    Body body) {
+  if (x->cap_depth >= 4) return HYDRO_ERR_UNSUPPORTED;
+  cudaStream_t outer = x->st;
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  CK(cudaStreamGetCaptureInfo(outer, &cs, nullptr, &g, &deps, nullptr, &nd));
+  if (cs != cudaStreamCaptureStatusActive) return HYDRO_ERR_CUDA;
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = type;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+  CK(cudaStreamUpdateCaptureDependencies(outer, &node, nullptr, 1,
+                                         cudaStreamSetCaptureDependencies));
+  cudaGraph_t bg = p.conditional.phGraph_out[0];
+  cudaStream_t inner = x->cap_streams[x->cap_depth++];
+  CK(cudaStreamBeginCaptureToGraph(inner, bg, nullptr, nullptr, 0,
+                                   cudaStreamCaptureModeRelaxed));
+  x->st = inner;
+  int rc = body();
+  x->st = outer;
+  cudaGraph_t done = nullptr;
+  cudaError_t e = cudaStreamEndCapture(inner, &done);
+  x->cap_depth--;
+  if (rc) return rc;
+  CK(e);
+  return HYDRO_OK;
+}
+template <class Body>
+int add_while(hydro_ctx* x, cudaGraphConditionalHandle h, Body body) {
+  return add_conditional(x, h, cudaGraphCondTypeWhile, body);
+}
+// A WHILE loop entered with its condition set (a handle's default value is
+// applied only once per launch, not on each entry into an enclosing body).
+template <class Body>
+int add_loop(hydro_ctx* x, cudaGraphConditionalHandle h, Body body) {
+  CK(launch_set_cond(h, 1u, x->st));
+  return add_conditional(x, h, cudaGraphCondTypeWhile, body);
+}
+template <class Body>
+int add_if(hydro_ctx* x, cudaGraphConditionalHandle h, Body body) {
+  return add_conditional(x, h, cudaGraphCondTypeIf, body);
+}
+
 // ------------------------------------------------------------- momentum --
-int solve_momentum(hydro_ctx* x, C3 up) {
+// Jacobi sweeps until the device flags convergence or `limit` sweeps
+// (do { } while (iter++ < limit)); sweep k reads du[(k+1)%2], writes du[k%2].
+int solve_momentum(hydro_ctx* x) {
   const hydro_desc& d = x->d;
   int dim = x->dim;
   CP<7> cc = x->vec<CP<7>>(x->coef, 2 * dim + 1, x->m.nc);
   C3 resc = x->vec<C3>(x->res, dim, x->m.nc);
   int rc = reset_flags(x, FL_MOM_DONE, 2);
   if (rc) return rc;
-  int limit = d.velocity_iters_limit + 1;  // do { } while (iter++ < limit)
-  int queued = 0;
+  const int limit = d.velocity_iters_limit + 1;
   const bool f32 = x->o32 != nullptr;
   auto fp3 = [&](float* base) {
     FP<3> r{};
     for (int k = 0; k < dim; ++k) r.a[k] = base + (size_t)k * x->m.nc;
     return r;
   };
+  auto sweep = [&](int k) -> int {
+    if (f32) {
+      PK(x, HYDRO_PROF_MOM_SWEEP,
+         launch_mom_sweep32(x->m, d.velocity_omega, d.velocity_tolerance, x->o32p(),
+                            fp3(x->du32[(k + 1) % 2]), fp3(x->du32[k % 2]), limit,
+                            x->pw.partials, x->pw.ds, x->st));
+    } else {
+      C3 din = x->vec<C3>(x->du[(k + 1) % 2], dim, x->m.nc);
+      W3 dout = x->vec<W3>(x->du[k % 2], dim, x->m.nc);
+      PK(x, HYDRO_PROF_MOM_SWEEP,
+         launch_mom_sweep(x->m, d.velocity_omega, d.velocity_tolerance, cc, resc, din, dout,
+                          limit, x->pw.partials, x->pw.ds, x->st));
+    }
+    return HYDRO_OK;
+  };
+  if (x->graph_mode) {
+    cudaGraphConditionalHandle h;
+    if ((rc = new_handle(x, 1, &h))) return rc;
+    rc = add_loop(x, h, [&]() -> int {
+      int r;
+      if ((r = sweep(0)) || (r = sweep(1))) return r;
+      CK(launch_ctl_sweeps(x->pw.ds, limit, h, 1, x->st));
+      return HYDRO_OK;
+    });
+    if (rc) return rc;
+    // the correction always ends in du[0] / du32[0]
+    const long long n = x->m.nc * dim;
+    CK(launch_select_sweep(n, f32 ? nullptr : x->du[1], x->du[0], f32 ? x->du32[1] : nullptr,
+                           x->du32[0], x->pw.ds, x->st));
+    x->du_cur = 0;
+    return HYDRO_OK;
+  }
+  int queued = 0;
   for (;;) {
     int n = std::min(kSweepChunk, limit - queued);
-    for (int s = 0; s < n; ++s) {
-      int k = queued + s;
-      if (f32) {
-        PK(x, HYDRO_PROF_MOM_SWEEP,
-           launch_mom_sweep32(x->m, d.velocity_omega, d.velocity_tolerance, x->o32p(),
-                              fp3(x->du32[(k + 1) % 2]), fp3(x->du32[k % 2]), k == 0,
-                              x->pw.partials, x->pw.ds, x->st));
-      } else {
-        C3 din = x->vec<C3>(x->du[(k + 1) % 2], dim, x->m.nc);
-        W3 dout = x->vec<W3>(x->du[k % 2], dim, x->m.nc);
-        PK(x, HYDRO_PROF_MOM_SWEEP,
-           launch_mom_sweep(x->m, d.velocity_omega, d.velocity_tolerance, cc, resc, din, dout,
-                            k == 0, x->pw.partials, x->pw.ds, x->st));
-      }
-    }
+    for (int s = 0; s < n; ++s)
+      if ((rc = sweep(queued + s))) return rc;
     queued += n;
     rc = sync_scalars(x);
     if (rc) return rc;
@@ -329,6 +420,61 @@ int solve_momentum(hydro_ctx* x, C3 up) {
 }
 
 // ------------------------------------------------------------- pressure --
+// Graph-captured form of the pressure solve: the refinement and Krylov loops
+// become WHILE nodes steered by the control kernels.
+int solve_pressure_graph(hydro_ctx* x, int singular, int mixed) {
+  const hydro_desc& d = x->d;
+  const Mesh& m = x->m;
+  PcgWork& w = x->pw;
+  int rc;
+  if (!mixed) {
+    w.limit = d.pressure_iters_limit;
+    CK(pcg_init(m, x->kf, x->prhs, x->pc, 0, d.pressure_tolerance, singular, w, x->st));
+    cudaGraphConditionalHandle h;
+    if ((rc = new_handle(x, 1, &h))) return rc;
+    rc = add_loop(x, h, [&]() -> int {
+      CK(pcg_iterate(m, x->kf, x->pc, 4, w, x->st));
+      CK(launch_ctl_krylov(w.ds, h, 1, x->st));
+      return HYDRO_OK;
+    });
+    if (rc) return rc;
+    CK(launch_ctl_krylov_done(w.ds, x->st));
+  } else {
+    const bool mgcg = d.pressure_solver == HYDRO_LINEAR_MGCG;
+    const double inner_min = mgcg ? 1e-5 : 1e-4;
+    if (mgcg) CK(mg_setup(x->mg, w, x->st));
+    if (singular) CK(mean_sum(m, x->prhs, w, x->st));
+    CK(cudaMemsetAsync(x->pc, 0, sizeof(double) * m.nc, x->st));
+    if ((rc = reset_flags(x, FL_IR_STATE, 1))) return rc;
+    cudaGraphConditionalHandle hr, hk;
+    if ((rc = new_handle(x, 0, &hr))) return rc;
+    if ((rc = new_handle(x, 1, &hk))) return rc;
+    CK(ir_residual(m, x->kf, x->prhs, x->pc, singular, w, x->st));
+    CK(launch_ctl_refine(w.ds, d.pressure_tolerance, inner_min, d.pressure_iters_limit, hr, 1,
+                         x->st));
+    rc = add_while(x, hr, [&]() -> int {
+      int r;
+      if (mgcg) CK(mgcg_init(m, 0., 1, w, x->mg, x->st));
+      else CK(f32_pcg_init(m, 0., 1, w, x->st));
+      r = add_loop(x, hk, [&]() -> int {
+        if (mgcg) CK(mgcg_iterate(m, 2, w, x->mg, x->st));
+        else CK(f32_pcg_iterate(m, 4, w, x->st));
+        CK(launch_ctl_krylov(w.ds, hk, 1, x->st));
+        return HYDRO_OK;
+      });
+      if (r) return r;
+      CK(f32_accumulate(m, x->pc, w, x->st));
+      CK(ir_residual(m, x->kf, x->prhs, x->pc, singular, w, x->st));
+      CK(launch_ctl_refine(w.ds, d.pressure_tolerance, inner_min, d.pressure_iters_limit, hr, 1,
+                           x->st));
+      return HYDRO_OK;
+    });
+    if (rc) return rc;
+  }
+  if (singular) CK(sub_mean(m, x->pc, w, x->st));
+  return HYDRO_OK;
+}
+
 int solve_pressure(hydro_ctx* x) {
   const hydro_desc& d = x->d;
   const Mesh& m = x->m;
@@ -338,6 +484,7 @@ int solve_pressure(hydro_ctx* x) {
   if (w.pin >= 0) CK(pin_rhs(m, x->kf, x->prhs, w.pin, d.pressure_fixed_value, x->st));
   int mixed = (d.precision == HYDRO_MIXED);
   CK(pcg_prepare(m, x->kf, 0., w, mixed, x->st));
+  if (x->graph_mode) return solve_pressure_graph(x, singular, mixed);
   int rc;
   if (!mixed) {
     w.limit = d.pressure_iters_limit;
@@ -378,16 +525,16 @@ int solve_pressure(hydro_ctx* x) {
       w.limit = d.pressure_iters_limit - total;
       double tol = std::max(inner_tol, 0.5 * d.pressure_tolerance * sqrt(ff / rr));
       if (mgcg)
-        PK(x, HYDRO_PROF_CG_INIT, mgcg_init(m, tol, w, x->mg, x->st));
+        PK(x, HYDRO_PROF_CG_INIT, mgcg_init(m, tol, 0, w, x->mg, x->st));
       else
-        PK(x, HYDRO_PROF_CG_INIT, f32_pcg_init(m, tol, w, x->st));
+        PK(x, HYDRO_PROF_CG_INIT, f32_pcg_init(m, tol, 0, w, x->st));
       int queued = 0;
       const int chunk = mgcg ? kMgChunk : kCgChunk;
       for (;;) {
         if (mgcg)
-          CK(mgcg_iterate(m, chunk, queued == 0, w, x->mg, x->st));
+          CK(mgcg_iterate(m, chunk, w, x->mg, x->st));
         else
-          CK(f32_pcg_iterate(m, chunk, queued == 0, w, x->st));
+          CK(f32_pcg_iterate(m, chunk, w, x->st));
         queued += chunk;
         rc = sync_scalars(x);
         if (rc) return rc;
@@ -615,6 +762,10 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
   }
   x->pw.pin = desc->pressure_fixed_cell;
   x->pw.prof = &x->prof;
+  if (mg_prepare(x->mg) != cudaSuccess) {
+    hydro_gpu_destroy(x);
+    return HYDRO_ERR_CUDA;
+  }
   // constants
   for (int s = 0; s < 6; ++s)
     for (int k = 0; k < 3; ++k) x->fc.bcu[s][k] = (k < dim) ? desc->bc_velocity[s][k] : 0.;
@@ -641,6 +792,9 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
 int hydro_gpu_destroy(hydro_ctx* x) {
   if (!x) return HYDRO_OK;
   if (x->st) cudaStreamSynchronize(x->st);
+  if (x->sg.exec) cudaGraphExecDestroy(x->sg.exec);
+  for (auto& cs : x->cap_streams)
+    if (cs) cudaStreamDestroy(cs);
   if (x->arena.base) cudaFree(x->arena.base);
   if (x->hds) cudaFreeHost(x->hds);
   if (x->own_stream && x->st) cudaStreamDestroy(x->st);
@@ -811,7 +965,7 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
                                   s3.rho, s3.mu, x->vf<R3>(s3.fo, dim), up,
                                   x->uc3(HYDRO_TIME_CURR), x->uc3(HYDRO_TIME_PREV), coef32,
                                   res32, s3.Dc, x->st));
-    rc = solve_momentum(x, up);
+    rc = solve_momentum(x);
     if (rc) return rc;
     x->cd_iter_count++;
     PK(x, HYDRO_PROF_RHIE_CHOW,
@@ -836,7 +990,7 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
                                    x->uc3(HYDRO_TIME_PREV),
                                    x->vec<WP<7>>(x->coef, 2 * dim + 1, m.nc),
                                    x->vec<W3>(x->res, dim, m.nc), x->Dc, x->st));
-    rc = solve_momentum(x, up);
+    rc = solve_momentum(x);
     if (rc) return rc;
     C3 du = x->vec<C3>(x->du[x->du_cur], dim, m.nc);
     x->cd_iter_count++;
@@ -859,6 +1013,11 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
        launch_correct(m, x->fc, up, du, RT<float, 3>{}, nullptr, x->uw3(HYDRO_ITER_CURR), pip,
                       x->p[HYDRO_ITER_CURR], x->pc, x->Dc, x->Fs, x->kf, x->F[HYDRO_ITER_CURR],
                       FP<3>{}, nullptr, nullptr, x->pw.partials, x->pw.ds, x->st));
+  if (x->graph_mode) {
+    // the SIMPLE loop's control kernel reads the indicator on the device
+    x->iter_count++;
+    return HYDRO_OK;
+  }
   rc = sync_scalars(x);
   if (rc) return rc;
   x->indicator = x->hds->red[RS_INDICATOR];
@@ -1017,6 +1176,195 @@ int hydro_gpu_step(hydro_ctx* x, hydro_step_stats* stats) {
   s.status = HYDRO_OK;
   if (stats) *stats = s;
   return HYDRO_OK;
+}
+
+// ------------------------------------------------------ graph-captured step --
+namespace {
+
+// Number of advection substeps the host loop of hydro_gpu_advection_step
+// would take after the fluid time advanced by dt; *t_out is the advection
+// time it ends at.
+int advection_substeps(const hydro_ctx* x, double dt, double* t_out) {
+  double t = x->adv_time, tf = x->time + dt;
+  int n = 0;
+  if (x->d.advection_enable)
+    while (t < tf - 0.5 * x->adv_dt && n < 1000000) {
+      t += x->adv_dt;
+      ++n;
+    }
+  *t_out = t;
+  return n;
+}
+
+// Captures one whole step (StartStep, SIMPLE loop, FinishStep, advection
+// substeps, property update, next auto time step) into x->sg.exec.  Loops
+// whose length the device decides are WHILE nodes; two SIMPLE iterations
+// are captured per loop trip (the second under an IF node) so that the
+// iteration layers alternate their buffers as the pointer swaps of the
+// host-driven step do; select copies leave every result where the host
+// pointers expect it.  Host-side scalars changed while capturing are
+// restored afterwards.
+int capture_step(hydro_ctx* x, int substeps) {
+  const Mesh& m = x->m;
+  const hydro_desc& d = x->d;
+  for (int i = 0; i < 4; ++i)
+    if (!x->cap_streams[i]) CK(cudaStreamCreateWithFlags(&x->cap_streams[i], cudaStreamNonBlocking));
+  if (x->sg.exec) {
+    cudaGraphExecDestroy(x->sg.exec);
+    x->sg.exec = nullptr;
+  }
+  // host state to restore
+  const double time0 = x->time, adv_time0 = x->adv_time;
+  const int ic0 = x->iter_count, cdc0 = x->cd_iter_count, vs0 = x->vel_sweeps, pi0 = x->p_iters;
+  const double pres0 = x->p_res, ind0 = x->indicator;
+  double* q0 = x->q;
+  const bool prof0 = x->prof.on;
+  x->prof.on = false;
+  x->graph_mode = true;
+  CK(cudaGraphCreate(&x->cap_graph, 0));
+  int rc = HYDRO_OK;
+  cudaError_t e = cudaStreamBeginCaptureToGraph(x->st, x->cap_graph, nullptr, nullptr, 0,
+                                                cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) {
+    auto body = [&]() -> int {
+      int r;
+      if ((r = reset_flags(x, FL_STEP_SWEEPS, 3))) return r;  // sweeps, p iterations, SIMPLE
+      if ((r = hydro_gpu_start_step(x))) return r;
+      const int limit = d.num_iterations_limit;
+      const double tol = d.convergence_tolerance;
+      const int cont0 = !(0 >= limit || 1. < tol);
+      cudaGraphConditionalHandle hw, hi;
+      if ((r = new_handle(x, cont0, &hw)) || (r = new_handle(x, 0, &hi))) return r;
+      r = add_while(x, hw, [&]() -> int {
+        int q;
+        if ((q = hydro_gpu_make_iteration(x))) return q;
+        CK(launch_ctl_simple2(x->pw.ds, limit, tol, hi, hw, x->st));
+        return add_if(x, hi, [&]() -> int {
+          int z;
+          if ((z = hydro_gpu_make_iteration(x))) return z;
+          CK(launch_ctl_simple(x->pw.ds, limit, tol, hw, 1, x->st));
+          return HYDRO_OK;
+        });
+      });
+      if (r) return r;
+      // an odd iteration count leaves the iterate in the other buffer
+      CK(launch_select_iter(m.nc * x->dim, x->u[HYDRO_ITER_PREV], x->u[HYDRO_ITER_CURR],
+                            x->pw.ds, x->st));
+      CK(launch_select_iter(m.nc, x->p[HYDRO_ITER_PREV], x->p[HYDRO_ITER_CURR], x->pw.ds,
+                            x->st));
+      CK(launch_select_iter(m.nf, x->F[HYDRO_ITER_PREV], x->F[HYDRO_ITER_CURR], x->pw.ds,
+                            x->st));
+      // FinishStep with copies instead of the pointer rotation
+      CK(cudaMemcpyAsync(x->p[HYDRO_TIME_PREV], x->p[HYDRO_TIME_CURR], sizeof(double) * m.nc,
+                         cudaMemcpyDeviceToDevice, x->st));
+      CK(cudaMemcpyAsync(x->F[HYDRO_TIME_PREV], x->F[HYDRO_TIME_CURR], sizeof(double) * m.nf,
+                         cudaMemcpyDeviceToDevice, x->st));
+      CK(cudaMemcpyAsync(x->u[HYDRO_TIME_PREV], x->u[HYDRO_TIME_CURR],
+                         sizeof(double) * m.nc * x->dim, cudaMemcpyDeviceToDevice, x->st));
+      CK(cudaMemcpyAsync(x->p[HYDRO_TIME_CURR], x->p[HYDRO_ITER_CURR], sizeof(double) * m.nc,
+                         cudaMemcpyDeviceToDevice, x->st));
+      CK(cudaMemcpyAsync(x->F[HYDRO_TIME_CURR], x->F[HYDRO_ITER_CURR], sizeof(double) * m.nf,
+                         cudaMemcpyDeviceToDevice, x->st));
+      CK(cudaMemcpyAsync(x->u[HYDRO_TIME_CURR], x->u[HYDRO_ITER_CURR],
+                         sizeof(double) * m.nc * x->dim, cudaMemcpyDeviceToDevice, x->st));
+      CK(launch_nan_count(m.nc, x->p[HYDRO_TIME_CURR], x->pw.partials, x->pw.ds, x->st));
+      x->time += x->dt;
+      for (int i = 0; i < substeps; ++i)
+        if ((r = hydro_gpu_advection_substep(x))) return r;
+      if (x->q != q0) {
+        // odd number of stage swaps: bring the fractions back to the buffer
+        // the next launch reads
+        CK(cudaMemcpyAsync(q0, x->q, sizeof(double) * m.nc * x->nph, cudaMemcpyDeviceToDevice,
+                           x->st));
+        std::swap(x->q, x->qtmp);
+      }
+      if ((r = hydro_gpu_update_properties(x))) return r;
+      CK(launch_auto_dt(m, x->F[HYDRO_TIME_CURR], x->pw.partials, x->pw.ds, x->st));
+      return HYDRO_OK;
+    };
+    rc = body();
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(x->st, &g);
+    if (!rc && e2 != cudaSuccess) rc = HYDRO_ERR_CUDA;
+    if (!rc && cudaGraphInstantiate(&x->sg.exec, x->cap_graph, 0) != cudaSuccess) {
+      x->sg.exec = nullptr;
+      rc = HYDRO_ERR_CUDA;
+    }
+  } else {
+    rc = HYDRO_ERR_CUDA;
+  }
+  cudaGraphDestroy(x->cap_graph);
+  x->cap_graph = nullptr;
+  x->graph_mode = false;
+  x->prof.on = prof0;
+  x->time = time0;
+  x->adv_time = adv_time0;
+  x->iter_count = ic0;
+  x->cd_iter_count = cdc0;
+  x->vel_sweeps = vs0;
+  x->p_iters = pi0;
+  x->p_res = pres0;
+  x->indicator = ind0;
+  cudaGetLastError();
+  return rc;
+}
+
+}  // namespace
+
+int hydro_gpu_step_graph(hydro_ctx* x, hydro_step_stats* stats) {
+  if (!x) return HYDRO_ERR_ARG;
+  const hydro_desc& d = x->d;
+  hydro_step_stats s;
+  memset(&s, 0, sizeof(s));
+  int rc;
+  if (d.dt_auto) {
+    double dtm;
+    rc = hydro_gpu_get_auto_time_step(x, &dtm);
+    if (rc) return rc;
+    double dt = dtm * d.cfl, dta = dtm * d.cfl_advection;
+    if (d.dt_max > 0. && dt > d.dt_max) {
+      dta = dta * (d.dt_max / dt);
+      dt = d.dt_max;
+    }
+    x->dt = dt;
+    x->adv_dt = dta;
+  }
+  double adv_end;
+  const int substeps = advection_substeps(x, x->dt, &adv_end);
+  if (!x->sg.exec || x->sg.dt != x->dt || x->sg.adv_dt != x->adv_dt ||
+      x->sg.substeps != substeps || x->sg.sources != x->fc.sources) {
+    rc = capture_step(x, substeps);
+    if (rc) return rc;
+    x->sg.dt = x->dt;
+    x->sg.adv_dt = x->adv_dt;
+    x->sg.substeps = substeps;
+    x->sg.sources = x->fc.sources;
+  }
+  CK(cudaGraphLaunch(x->sg.exec, x->st));
+  rc = sync_scalars(x);
+  if (rc) return rc;
+  const DevScalars& h = *x->hds;
+  x->iter_count = h.flag[FL_ITERS];
+  x->cd_iter_count = h.flag[FL_ITERS];
+  x->indicator = h.red[RS_INDICATOR];
+  x->p_res = h.red[RS_P_RES];
+  x->vel_sweeps = h.flag[FL_STEP_SWEEPS];
+  x->p_iters = h.flag[FL_STEP_PITERS];
+  x->du_cur = 0;
+  x->time += x->dt;
+  x->adv_time = adv_end;
+  s.outer_iterations = x->iter_count;
+  s.convergence_indicator = x->cd_iter_count == 0 ? 1. : x->indicator;
+  s.velocity_sweeps = x->vel_sweeps;
+  s.pressure_iterations = x->p_iters;
+  s.pressure_residual = x->p_res;
+  s.advection_substeps = substeps;
+  s.dt = x->dt;
+  s.dt_advection = x->adv_dt;
+  s.time = x->time;
+  s.status = (h.red[RS_NAN] > 0. || isnan(x->indicator)) ? HYDRO_ERR_NAN : HYDRO_OK;
+  if (stats) *stats = s;
+  return s.status;
 }
 
 int hydro_gpu_calc_stat(hydro_ctx* x, hydro_stat* out) {

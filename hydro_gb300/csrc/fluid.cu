@@ -270,13 +270,15 @@ __global__ void k_mom_assemble(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> up,
 // Jacobi sweep for all components (Jacobi::Solve, linear.hpp:750-782):
 // value = -(r + sum_nb a du_nb)/aP, du' = du + omega*(value - du); the max
 // |value - du| is reduced into ds->red[RS_MOM_DIFF].  A launch after
-// convergence returns at once.
+// convergence or after `limit` sweeps returns at once; the first sweep
+// (count 0) starts from du = 0.
 template <int DIM>
 __global__ void __launch_bounds__(NT) k_mom_sweep(Mesh m, double omega, double tol,
                                                   CP<7> coef, C3 res, C3 din, W3 dout,
-                                                  int first, double* partials, DevScalars* ds,
+                                                  int limit, double* partials, DevScalars* ds,
                                                   int kch) {
-  if (ds->flag[FL_MOM_DONE]) return;
+  if (ds->flag[FL_MOM_DONE] || ds->flag[FL_MOM_SWEEPS] >= limit) return;
+  const bool first = ds->flag[FL_MOM_SWEEPS] == 0;
   double dmax = 0.;
   CELL_LOOP_BEGIN(m, kch)
   double iaP = coef.a[0][X.c];
@@ -317,9 +319,10 @@ __global__ void __launch_bounds__(NT) k_mom_sweep(Mesh m, double omega, double t
 // off-diagonals, DIM residuals): FP32 arithmetic, FP64 only for the max.
 template <int DIM>
 __global__ void __launch_bounds__(NT) k_mom_sweep32(Mesh m, float omega, double tol, FP<10> c,
-                                                    FP<3> din, FP<3> dout, int first,
+                                                    FP<3> din, FP<3> dout, int limit,
                                                     double* partials, DevScalars* ds, int kch) {
-  if (ds->flag[FL_MOM_DONE]) return;
+  if (ds->flag[FL_MOM_DONE] || ds->flag[FL_MOM_SWEEPS] >= limit) return;
+  const bool first = ds->flag[FL_MOM_SWEEPS] == 0;
   float dmax = 0.f;
   CELL_LOOP_BEGIN(m, kch)
   float iaP = c.a[0][X.c];
@@ -808,9 +811,9 @@ cudaError_t launch_d2f(long long n, const double* in, float* out, cudaStream_t s
 }
 
 cudaError_t launch_mom_sweep32(const Mesh& m, double omega, double tol, FP<10> c, FP<3> din,
-                               FP<3> dout, int first, double* partials, DevScalars* ds,
+                               FP<3> dout, int limit, double* partials, DevScalars* ds,
                                cudaStream_t st) {
-  DISPATCH_DIM(m, k_mom_sweep32, m, (float)omega, tol, c, din, dout, first, partials, ds);
+  DISPATCH_DIM(m, k_mom_sweep32, m, (float)omega, tol, c, din, dout, limit, partials, ds);
 }
 
 cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st) {
@@ -820,9 +823,9 @@ cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st) {
 }
 
 cudaError_t launch_mom_sweep(const Mesh& m, double omega, double tol, CP<7> coef, C3 res,
-                             C3 din, W3 dout, int first, double* partials, DevScalars* ds,
+                             C3 din, W3 dout, int limit, double* partials, DevScalars* ds,
                              cudaStream_t st) {
-  DISPATCH_DIM(m, k_mom_sweep, m, omega, tol, coef, res, din, dout, first, partials, ds);
+  DISPATCH_DIM(m, k_mom_sweep, m, omega, tol, coef, res, din, dout, limit, partials, ds);
 }
 
 cudaError_t launch_pressure_rhs(const Mesh& m, const double* Fs, const double* Sv, double* f,

@@ -48,7 +48,7 @@ using FluidCoef = FluidCoefT<double>;
 // Device scalars shared by reductions and convergence flags.
 struct DevScalars {
   double red[32];        // reduced values (see enum below)
-  int flag[16];          // done flags / counters
+  int flag[32];          // done flags / counters
   unsigned ticket[32];   // grid-reduction tickets, one per call site
 };
 enum {
@@ -61,9 +61,22 @@ enum {
   RS_PCG_TOL2 = 11,      // tol^2 * ||f||^2
   RS_IR_RR = 12,         // refinement residual norm^2
   RS_NAN = 13,
-  RS_XMEAN = 14
+  RS_XMEAN = 14,
+  RS_INNER_TOL = 15,     // tolerance of the next inner solve (device-driven refinement)
+  RS_P_RES = 16,         // relative pressure residual of the last solve
+  RS_IR_FF = 17          // refinement: ||f||^2 of the first residual
 };
-enum { FL_MOM_DONE = 0, FL_MOM_SWEEPS = 1, FL_PCG_DONE = 2, FL_PCG_ITERS = 3, FL_NAN = 4 };
+enum {
+  FL_MOM_DONE = 0, FL_MOM_SWEEPS = 1, FL_PCG_DONE = 2, FL_PCG_ITERS = 3, FL_NAN = 4,
+  FL_PCG_LIMIT = 5,      // iteration limit of the running Krylov solve
+  FL_IR_STATE = 6,       // refinement: 0 before its first residual
+  FL_IR_TOTAL = 7,       // refinement: inner iterations so far
+  FL_STEP_SWEEPS = 8,    // momentum sweeps of the step (graph-captured step)
+  FL_STEP_PITERS = 9,    // pressure iterations of the step
+  FL_ITERS = 10,         // SIMPLE iterations of the step
+  FL_IR_OUTER = 11,      // refinement cycles
+  FL_CONT = 12           // last loop decision
+};
 enum {
   TK_MOM = 0, TK_PCG_A = 1, TK_PCG_B = 2, TK_PCG_INIT = 3, TK_IND = 4, TK_DT = 5,
   TK_MEAN = 6, TK_MEAN2 = 7, TK_STAT = 8, TK_STAT2 = 9, TK_STAT3 = 10, TK_IR = 11,
@@ -104,11 +117,11 @@ cudaError_t launch_d2f(long long n, const double* in, float* out, cudaStream_t s
 // Mixed path: FP32 Jacobi sweep on the o32 output of the assembly
 // (o32 = {1/diag, 2*DIM off-diagonals, DIM residuals}); FP32 -> FP64 copy.
 cudaError_t launch_mom_sweep32(const Mesh& m, double omega, double tol, FP<10> c, FP<3> din,
-                               FP<3> dout, int first, double* partials, DevScalars* ds,
+                               FP<3> dout, int limit, double* partials, DevScalars* ds,
                                cudaStream_t st);
 cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st);
 cudaError_t launch_mom_sweep(const Mesh& m, double omega, double tol, CP<7> coef, C3 res,
-                             C3 din, W3 dout, int first, double* partials, DevScalars* ds,
+                             C3 din, W3 dout, int limit, double* partials, DevScalars* ds,
                              cudaStream_t st);
 cudaError_t launch_pressure_rhs(const Mesh& m, const double* Fs, const double* Sv, double* f,
                                 cudaStream_t st);
@@ -191,12 +204,16 @@ cudaError_t sub_mean(const Mesh& m, double* x, PcgWork& w, cudaStream_t st);
 // FP32 PCG for A e = r to a relative tolerance, x += e.
 cudaError_t ir_residual(const Mesh& m, const double* kf, const double* f, const double* x,
                         int singular, PcgWork& w, cudaStream_t st);
-cudaError_t f32_pcg_init(const Mesh& m, double tol, PcgWork& w, cudaStream_t st);
-cudaError_t f32_pcg_iterate(const Mesh& m, int chunk, int first, PcgWork& w, cudaStream_t st);
-// One launch: p_new = z + beta p_old (z on `first`), Ap = A p_new,
-// <p_new, Ap> -> alpha (FP32 vectors, double-float dot).
+// Inner-solve start.  dev_params = 0: tolerance `tol` and limit `w.limit`
+// from the host (stored on the device); 1: both already on the device
+// (RS_INNER_TOL, FL_PCG_LIMIT, set by launch_ctl_refine).
+cudaError_t f32_pcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, cudaStream_t st);
+cudaError_t f32_pcg_iterate(const Mesh& m, int chunk, PcgWork& w, cudaStream_t st);
+// One launch: p_new = z + beta p_old (z on the first iteration, read from
+// the device's iteration count), Ap = A p_new, <p_new, Ap> -> alpha (FP32
+// vectors, double-float dot).
 cudaError_t cg32_dir_spmv(const Mesh& m, const float* kf, const float* dg, const float* z,
-                          const float* pold, float* pnew, float* Ap, long long pin, int first,
+                          const float* pold, float* pnew, float* Ap, long long pin,
                           double* partials, DevScalars* ds, cudaStream_t st);
 
 // ------------------------------------------------------------ multigrid --
@@ -218,20 +235,62 @@ struct MgWork {
 };
 Mesh mg_coarse_mesh(const Mesh& fine);
 int mg_levels_for(const Mesh& m);
+// Once per context: which levels run inside one CTA and that CTA's shared
+// memory (set as the kernel's dynamic shared-memory limit).
+cudaError_t mg_prepare(MgWork& mg);
 // Coarse couplings and diagonals from level 0 (w.kf32 / dg32 / idg32).
 cudaError_t mg_setup(MgWork& mg, PcgWork& w, cudaStream_t st);
 cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevScalars* ds,
                       cudaStream_t st);
 // Inner solve of the mixed path with the V-cycle as preconditioner:
 // init from the FP64 residual in w.r, chunks of iterations into w.x32.
-cudaError_t mgcg_init(const Mesh& m, double tol, PcgWork& w, MgWork& mg, cudaStream_t st);
-cudaError_t mgcg_iterate(const Mesh& m, int chunk, int first, PcgWork& w, MgWork& mg,
-                         cudaStream_t st);
+cudaError_t mgcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, MgWork& mg,
+                      cudaStream_t st);
+cudaError_t mgcg_iterate(const Mesh& m, int chunk, PcgWork& w, MgWork& mg, cudaStream_t st);
 cudaError_t f32_accumulate(const Mesh& m, double* x, PcgWork& w, cudaStream_t st);
 cudaError_t scale_vector(long long n, double* a, double s, cudaStream_t st);
 // Right-hand side of a pinned cell (fluid.hpp:996-1014): f[pin] = value and
 // the pinned value moved into the neighbours' rows.
 cudaError_t pin_rhs(const Mesh& m, const double* kf, double* f, long long pin, double value,
                     cudaStream_t st);
+
+// ------------------------------------------------------- loop control --
+// One-thread kernels that take the decisions of the step's loops on the
+// device.  Each writes its decision to ds->flag[FL_CONT] and, when `use`
+// is set, to the graph conditional `h` of the WHILE node that repeats the
+// loop (graph-captured step); the host-driven step reads the same flags.
+// Momentum sweeps: continue while not converged and fewer than `limit`;
+// accumulates the finished loop's sweeps into FL_STEP_SWEEPS when it stops.
+cudaError_t launch_ctl_sweeps(DevScalars* ds, int limit, cudaGraphConditionalHandle h, int use,
+                              cudaStream_t st);
+// Krylov inner loop: continue while not done.
+cudaError_t launch_ctl_krylov(DevScalars* ds, cudaGraphConditionalHandle h, int use,
+                              cudaStream_t st);
+// Refinement cycle after a residual: records ||f||^2 on the first call,
+// the relative residual in RS_P_RES, adds the finished inner solve's
+// iterations; continues while above `tol`, below `limit` iterations and 50
+// cycles, then sets the next inner tolerance (>= inner_min) and limit.
+cudaError_t launch_ctl_refine(DevScalars* ds, double tol, double inner_min, int limit,
+                              cudaGraphConditionalHandle h, int use, cudaStream_t st);
+// End of a FP64 Krylov solve: RS_P_RES and FL_STEP_PITERS.
+cudaError_t launch_ctl_krylov_done(DevScalars* ds, cudaStream_t st);
+// SIMPLE loop after an iteration: FL_ITERS += 1; continue while below
+// `limit` and the indicator is not below `tol`.
+cudaError_t launch_ctl_simple(DevScalars* ds, int limit, double tol,
+                              cudaGraphConditionalHandle h, int use, cudaStream_t st);
+// The same for graph-captured loops with two conditionals (both set).
+cudaError_t launch_ctl_simple2(DevScalars* ds, int limit, double tol,
+                               cudaGraphConditionalHandle h1, cudaGraphConditionalHandle h2,
+                               cudaStream_t st);
+// Sets a graph conditional (re-arms a loop nested in another loop's body).
+cudaError_t launch_set_cond(cudaGraphConditionalHandle h, unsigned v, cudaStream_t st);
+// Copies src to dst when the momentum sweep count is even (the last sweep
+// wrote the second buffer), so the correction is always in the first.
+cudaError_t launch_select_sweep(long long n, const double* src, double* dst, const float* src32,
+                                float* dst32, const DevScalars* ds, cudaStream_t st);
+// Copies src to dst when the SIMPLE iteration count is odd (the captured
+// iterations alternate their layer buffers two by two).
+cudaError_t launch_select_iter(long long n, const double* src, double* dst,
+                               const DevScalars* ds, cudaStream_t st);
 
 }  // namespace hg

@@ -97,7 +97,8 @@ template <int DIM, class T>
 __global__ void __launch_bounds__(NT) k_cg_init(Mesh m, const T* kf, const T* dg, const T* idg,
                                                 const double* f, const double* fmean_sum,
                                                 const T* x, int use_guess, long long pin,
-                                                T* r, T* z, T* p, double tol, double* partials,
+                                                T* r, T* z, T* p, double tol, int limit,
+                                                int dev_params, double* partials,
                                                 DevScalars* ds, int kch) {
   double s[3] = {0., 0., 0.};
   double mean = fmean_sum ? *fmean_sum / (double)m.nc : 0.;
@@ -117,12 +118,15 @@ __global__ void __launch_bounds__(NT) k_cg_init(Mesh m, const T* kf, const T* dg
   __shared__ double o[3];
   if (grid_reduce<RED_SUM, 3>(s, partials, &ds->ticket[TK_PCG_INIT], o)) {
     if (threadIdx.x == 0 && threadIdx.y == 0) {
+      if (dev_params) tol = ds->red[RS_INNER_TOL];
+      else ds->flag[FL_PCG_LIMIT] = limit;
       ds->red[RS_PCG_RZ] = o[0];
       ds->red[RS_PCG_RR] = o[1];
       ds->red[RS_PCG_FF] = o[2];
       ds->red[RS_PCG_TOL2] = tol * tol * o[2];
       ds->flag[FL_PCG_ITERS] = 0;
-      ds->flag[FL_PCG_DONE] = (o[2] == 0. || o[1] <= tol * tol * o[2]) ? 1 : 0;
+      ds->flag[FL_PCG_DONE] =
+          (o[2] == 0. || o[1] <= tol * tol * o[2] || ds->flag[FL_PCG_LIMIT] <= 0) ? 1 : 0;
     }
   }
 }
@@ -160,7 +164,7 @@ __global__ void __launch_bounds__(NT) k_cg_spmv(Mesh m, const T* kf, const T* dg
 template <class TX, class T>
 __global__ void __launch_bounds__(NT) k_cg_update(long long n, TX* x, T* r, T* z, const T* p,
                                                   const T* Ap, const T* idg, double* partials,
-                                                  DevScalars* ds, int limit) {
+                                                  DevScalars* ds) {
   if (ds->flag[FL_PCG_DONE]) return;
   double alpha = ds->red[RS_PCG_ALPHA];
   T at = (T)alpha;
@@ -184,7 +188,8 @@ __global__ void __launch_bounds__(NT) k_cg_update(long long n, TX* x, T* r, T* z
       ds->red[RS_PCG_RR] = o[1];
       int it = ds->flag[FL_PCG_ITERS] + 1;
       ds->flag[FL_PCG_ITERS] = it;
-      if (o[1] <= ds->red[RS_PCG_TOL2] || it >= limit) ds->flag[FL_PCG_DONE] = 1;
+      if (o[1] <= ds->red[RS_PCG_TOL2] || it >= ds->flag[FL_PCG_LIMIT] || isnan(o[1]))
+        ds->flag[FL_PCG_DONE] = 1;
     }
   }
 }
@@ -279,7 +284,7 @@ cudaError_t pcg_init(const Mesh& m, const double* kf, const double* f, double* x
     msum = &w.ds->red[RS_MEAN];
   }
   LAUNCH_DIM_T(k_cg_init, double, m, kf, w.dg, w.idg, f, msum, x, use_guess, w.pin, w.r, w.z,
-             w.p, tol, w.partials, w.ds);
+             w.p, tol, w.limit, 0, w.partials, w.ds);
   if (!use_guess) cudaMemsetAsync(x, 0, sizeof(double) * m.nc, st);
   count_launches(singular ? 2 : 1);
   return cudaGetLastError();
@@ -295,7 +300,7 @@ cudaError_t pcg_iterate(const Mesh& m, const double* kf, double* x, int chunk, P
     if (w.prof) w.prof->end(PG_CG_SPMV, st);
     if (w.prof) w.prof->begin(PG_CG_UPDATE, st);
     k_cg_update<double, double><<<fb, dim3(BX, BY), 0, st>>>(m.nc, x, w.r, w.z, w.p, w.Ap, w.idg,
-                                                             w.partials, w.ds, w.limit);
+                                                             w.partials, w.ds);
     if (w.prof) w.prof->end(PG_CG_UPDATE, st);
     if (w.prof) w.prof->begin(PG_CG_DIR, st);
     k_cg_dir<double><<<fb, NT, 0, st>>>(m.nc, w.z, w.p, w.ds);
@@ -317,12 +322,12 @@ cudaError_t ir_residual(const Mesh& m, const double* kf, const double* f, const 
   return cudaGetLastError();
 }
 
-cudaError_t f32_pcg_init(const Mesh& m, double tol, PcgWork& w, cudaStream_t st) {
+cudaError_t f32_pcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, cudaStream_t st) {
   Launch L = cell_launch(m);
   w.p32_parity = 0;
   cudaMemsetAsync(w.x32, 0, sizeof(float) * m.nc, st);
   LAUNCH_DIM_T(k_cg_init, float, m, w.kf32, w.dg32, w.idg32, w.r, (const double*)nullptr,
-             w.x32, 0, w.pin, w.r32, w.z32, w.p32, tol, w.partials, w.ds);
+             w.x32, 0, w.pin, w.r32, w.z32, w.p32, tol, w.limit, dev_params, w.partials, w.ds);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -355,9 +360,10 @@ template <int DIM>
 __global__ void __launch_bounds__(NT) k_cg32_dir_spmv(Mesh m, const float* kf, const float* dg,
                                                       const float* z, const float* pold,
                                                       float* pnew, float* Ap, long long pin,
-                                                      int first, double* partials,
-                                                      DevScalars* ds, int kch) {
+                                                      double* partials, DevScalars* ds,
+                                                      int kch) {
   if (ds->flag[FL_PCG_DONE]) return;
+  const bool first = ds->flag[FL_PCG_ITERS] == 0;
   const float beta = first ? 0.f : (float)ds->red[RS_PCG_BETA];
   DFAcc acc;
   CELL_LOOP_BEGIN(m, kch)
@@ -394,7 +400,7 @@ __global__ void __launch_bounds__(NT) k_cg32_dir_spmv(Mesh m, const float* kf, c
 __global__ void __launch_bounds__(NT) k_cg32_update(long long n, float* x, float* r, float* z,
                                                     const float* p, const float* Ap,
                                                     const float* idg, double* partials,
-                                                    DevScalars* ds, int limit) {
+                                                    DevScalars* ds) {
   if (ds->flag[FL_PCG_DONE]) return;
   const float at = (float)ds->red[RS_PCG_ALPHA];
   DFAcc rz, rr;
@@ -418,7 +424,8 @@ __global__ void __launch_bounds__(NT) k_cg32_update(long long n, float* x, float
       ds->red[RS_PCG_RR] = o[1];
       int it = ds->flag[FL_PCG_ITERS] + 1;
       ds->flag[FL_PCG_ITERS] = it;
-      if (o[1] <= ds->red[RS_PCG_TOL2] || it >= limit) ds->flag[FL_PCG_DONE] = 1;
+      if (o[1] <= ds->red[RS_PCG_TOL2] || it >= ds->flag[FL_PCG_LIMIT] || isnan(o[1]))
+        ds->flag[FL_PCG_DONE] = 1;
     }
   }
 }
@@ -426,20 +433,20 @@ __global__ void __launch_bounds__(NT) k_cg32_update(long long n, float* x, float
 }  // namespace
 
 cudaError_t cg32_dir_spmv(const Mesh& m, const float* kf, const float* dg, const float* z,
-                          const float* pold, float* pnew, float* Ap, long long pin, int first,
+                          const float* pold, float* pnew, float* Ap, long long pin,
                           double* partials, DevScalars* ds, cudaStream_t st) {
   Launch L = cell_launch(m);
   if (m.dim == 3)
-    k_cg32_dir_spmv<3><<<L.grid, L.block, 0, st>>>(m, kf, dg, z, pold, pnew, Ap, pin, first,
-                                                   partials, ds, L.kch);
+    k_cg32_dir_spmv<3><<<L.grid, L.block, 0, st>>>(m, kf, dg, z, pold, pnew, Ap, pin, partials,
+                                                   ds, L.kch);
   else
-    k_cg32_dir_spmv<2><<<L.grid, L.block, 0, st>>>(m, kf, dg, z, pold, pnew, Ap, pin, first,
-                                                   partials, ds, L.kch);
+    k_cg32_dir_spmv<2><<<L.grid, L.block, 0, st>>>(m, kf, dg, z, pold, pnew, Ap, pin, partials,
+                                                   ds, L.kch);
   count_launches(1);
   return cudaGetLastError();
 }
 
-cudaError_t f32_pcg_iterate(const Mesh& m, int chunk, int first, PcgWork& w, cudaStream_t st) {
+cudaError_t f32_pcg_iterate(const Mesh& m, int chunk, PcgWork& w, cudaStream_t st) {
   Launch L = cell_launch(m);
   int fb = flat_blocks_l(m.nc);
   for (int it = 0; it < chunk; ++it) {
@@ -450,16 +457,14 @@ cudaError_t f32_pcg_iterate(const Mesh& m, int chunk, int first, PcgWork& w, cud
     if (w.prof) w.prof->begin(PG_CG_SPMV, st);
     if (m.dim == 3)
       k_cg32_dir_spmv<3><<<L.grid, L.block, 0, st>>>(m, w.kf32, w.dg32, w.z32, pold, pnew, w.Ap32,
-                                                     w.pin, first && it == 0, w.partials, w.ds,
-                                                     L.kch);
+                                                     w.pin, w.partials, w.ds, L.kch);
     else
       k_cg32_dir_spmv<2><<<L.grid, L.block, 0, st>>>(m, w.kf32, w.dg32, w.z32, pold, pnew, w.Ap32,
-                                                     w.pin, first && it == 0, w.partials, w.ds,
-                                                     L.kch);
+                                                     w.pin, w.partials, w.ds, L.kch);
     if (w.prof) w.prof->end(PG_CG_SPMV, st);
     if (w.prof) w.prof->begin(PG_CG_UPDATE, st);
     k_cg32_update<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.x32, w.r32, w.z32, pnew, w.Ap32, w.idg32,
-                                               w.partials, w.ds, w.limit);
+                                               w.partials, w.ds);
     if (w.prof) w.prof->end(PG_CG_UPDATE, st);
     w.p32_parity ^= 1;
   }

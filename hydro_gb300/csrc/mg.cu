@@ -353,8 +353,8 @@ struct DFAcc2 {
 // Inner-solve start: r = FP32 copy of the FP64 refinement residual; ||r||^2
 // sets the stop test.
 __global__ void __launch_bounds__(NT) k_mgcg_init(long long n, const double* r64, float* r,
-                                                  float* x, double tol, double* partials,
-                                                  DevScalars* ds) {
+                                                  float* x, double tol, int limit, int dev_params,
+                                                  double* partials, DevScalars* ds) {
   double s = 0.;
   long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
   for (long long i = blockIdx.x * (long long)NT + tid; i < n; i += (long long)gridDim.x * NT) {
@@ -367,11 +367,13 @@ __global__ void __launch_bounds__(NT) k_mgcg_init(long long n, const double* r64
   __shared__ double o[1];
   if (grid_reduce<RED_SUM, 1>(v, partials, &ds->ticket[TK_F32_INIT], o)) {
     if (tid == 0) {
+      if (dev_params) tol = ds->red[RS_INNER_TOL];
+      else ds->flag[FL_PCG_LIMIT] = limit;
       ds->red[RS_PCG_FF] = o[0];
       ds->red[RS_PCG_RR] = o[0];
       ds->red[RS_PCG_TOL2] = tol * tol * o[0];
       ds->flag[FL_PCG_ITERS] = 0;
-      ds->flag[FL_PCG_DONE] = (o[0] == 0.) ? 1 : 0;
+      ds->flag[FL_PCG_DONE] = (o[0] == 0. || ds->flag[FL_PCG_LIMIT] <= 0) ? 1 : 0;
     }
   }
 }
@@ -379,7 +381,7 @@ __global__ void __launch_bounds__(NT) k_mgcg_init(long long n, const double* r64
 // x += alpha p, r -= alpha Ap; ||r||^2 and the stop test.
 __global__ void __launch_bounds__(NT) k_mgcg_update(long long n, float* x, float* r,
                                                     const float* p, const float* Ap,
-                                                    double* partials, DevScalars* ds, int limit) {
+                                                    double* partials, DevScalars* ds) {
   if (ds->flag[FL_PCG_DONE]) return;
   const float at = (float)ds->red[RS_PCG_ALPHA];
   DFAcc2 rr;
@@ -397,7 +399,8 @@ __global__ void __launch_bounds__(NT) k_mgcg_update(long long n, float* x, float
       ds->red[RS_PCG_RR] = o[0];
       int it = ds->flag[FL_PCG_ITERS] + 1;
       ds->flag[FL_PCG_ITERS] = it;
-      if (o[0] <= ds->red[RS_PCG_TOL2] || it >= limit) ds->flag[FL_PCG_DONE] = 1;
+      if (o[0] <= ds->red[RS_PCG_TOL2] || it >= ds->flag[FL_PCG_LIMIT] || isnan(o[0]))
+        ds->flag[FL_PCG_DONE] = 1;
     }
   }
 }
@@ -507,17 +510,20 @@ cudaError_t mg_setup(MgWork& mg, PcgWork& w, cudaStream_t st) {
     MG_LAUNCH(k_mg_coarsen, L, f.m, c.m, f.kf, c.kf);
     MG_LAUNCH(k_mg_diag, L, c.m, c.kf, c.dg, c.idg);
   }
-  mg_plan_block(mg);
-  if (mg.top < mg.nlev) {
-    cudaError_t e = dim == 3 ? cudaFuncSetAttribute(k_mg_block_vcycle<3>,
-                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                    mg.smem_bytes)
-                             : cudaFuncSetAttribute(k_mg_block_vcycle<2>,
-                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                    mg.smem_bytes);
-    if (e != cudaSuccess) return e;
-  }
   return cudaGetLastError();
+}
+
+cudaError_t mg_prepare(MgWork& mg) {
+  mg_plan_block(mg);
+  if (mg.nlev > 0 && mg.top < mg.nlev) {
+    if (mg.smem_bytes > 227 * 1024) return cudaErrorInvalidValue;
+    return mg.lev[0].m.dim == 3
+               ? cudaFuncSetAttribute(k_mg_block_vcycle<3>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, mg.smem_bytes)
+               : cudaFuncSetAttribute(k_mg_block_vcycle<2>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, mg.smem_bytes);
+  }
+  return cudaSuccess;
 }
 
 // z = M^-1 r: one V-cycle with `nsweep` (red, black) sweeps before and
@@ -597,10 +603,12 @@ cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevSc
   return cudaGetLastError();
 }
 
-cudaError_t mgcg_init(const Mesh& m, double tol, PcgWork& w, MgWork& mg, cudaStream_t st) {
+cudaError_t mgcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, MgWork& mg,
+                      cudaStream_t st) {
   int fb = flat_blocks_mg(m.nc);
   w.p32_parity = 0;
-  k_mgcg_init<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.r, w.r32, w.x32, tol, w.partials, w.ds);
+  k_mgcg_init<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.r, w.r32, w.x32, tol, w.limit, dev_params,
+                                           w.partials, w.ds);
   count_launches(1);
   if (w.prof) w.prof->begin(HYDRO_PROF_MG_VCYCLE, st);
   mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st);
@@ -610,8 +618,7 @@ cudaError_t mgcg_init(const Mesh& m, double tol, PcgWork& w, MgWork& mg, cudaStr
   return cudaGetLastError();
 }
 
-cudaError_t mgcg_iterate(const Mesh& m, int chunk, int first, PcgWork& w, MgWork& mg,
-                         cudaStream_t st) {
+cudaError_t mgcg_iterate(const Mesh& m, int chunk, PcgWork& w, MgWork& mg, cudaStream_t st) {
   Launch L = cell_launch(m);
   int fb = flat_blocks_mg(m.nc);
   int dim = m.dim;
@@ -620,12 +627,12 @@ cudaError_t mgcg_iterate(const Mesh& m, int chunk, int first, PcgWork& w, MgWork
     float* pnew = (w.p32_parity & 1) ? w.p32 : w.p32b;
     if (w.prof) w.prof->begin(HYDRO_PROF_CG_SPMV, st);
     cudaError_t e = cg32_dir_spmv(m, w.kf32, w.dg32, w.z32, pold, pnew, w.Ap32, w.pin,
-                                  first && it == 0, w.partials, w.ds, st);
+                                  w.partials, w.ds, st);
     if (w.prof) w.prof->end(HYDRO_PROF_CG_SPMV, st);
     if (e != cudaSuccess) return e;
     if (w.prof) w.prof->begin(HYDRO_PROF_CG_UPDATE, st);
-    k_mgcg_update<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.x32, w.r32, pnew, w.Ap32, w.partials, w.ds,
-                                               w.limit);
+    k_mgcg_update<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.x32, w.r32, pnew, w.Ap32, w.partials,
+                                               w.ds);
     if (w.prof) w.prof->end(HYDRO_PROF_CG_UPDATE, st);
     if (w.prof) w.prof->begin(HYDRO_PROF_MG_VCYCLE, st);
     mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st);

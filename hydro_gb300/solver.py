@@ -155,6 +155,12 @@ class Hydro:
         self._call("step", ctypes.byref(st))
         return st.as_dict()
 
+    def step_graph(self):
+        """The same step as one CUDA-graph launch (hydro_gpu_step_graph)."""
+        st = capi.StepStats()
+        self._call("step_graph", ctypes.byref(st))
+        return st.as_dict()
+
     def calc_stat(self):
         s = capi.Stat()
         self._call("calc_stat", ctypes.byref(s))

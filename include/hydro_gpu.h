@@ -229,6 +229,16 @@ int hydro_gpu_advection_substep(hydro_ctx* ctx);
 /* One full time step: dt_auto, SIMPLE loop to convergence, advection
  * substeps, property update.  stats may be NULL. */
 int hydro_gpu_step(hydro_ctx* ctx, hydro_step_stats* stats);
+/* The same step as one CUDA-graph launch (hydro<Mesh>::step,
+ * hydro2d.hpp:1531-1621): the SIMPLE loop, momentum sweeps, refinement and
+ * Krylov loops are graph WHILE nodes steered by device-side decisions, so
+ * the host waits once per step.  Same results and stats as hydro_gpu_step.
+ * The graph is captured on the first call and again whenever dt, the
+ * advection substep count or the presence of sources changes.  Profiling
+ * groups are not recorded inside it.  Afterwards the iteration layers hold
+ * the final iterate in both ITER_CURR and, after an odd iteration count,
+ * ITER_PREV; the time layers are as after hydro_gpu_step. */
+int hydro_gpu_step_graph(hydro_ctx* ctx, hydro_step_stats* stats);
 int hydro_gpu_calc_stat(hydro_ctx* ctx, hydro_stat* out);
 
 /* Solve sum_j a_j x_j + c = 0 for a symmetric 7-point (3D) / 5-point (2D)
