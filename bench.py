@@ -299,8 +299,22 @@ def measure(args, form, rank, world, local, stream, e2e=True):
            "ms": ms_max, "value": world * N * args.steps / (ms_max / 1e3) / 1e6,
            "launches": launches, "clocks": clk, "stats": stats, "prof": prof, "desc": d}
     if e2e:
-        # through the public C-ABI with host buffers: every step uploads the
-        # state from pinned host memory and reads the result back
+        # the same steps as one CUDA-graph launch each (hydro_gpu_step_graph,
+        # loops steered on the device); no per-group events inside the graph
+        h.step_graph()  # capture
+        barrier(world)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        gstats = [h.step_graph() for _ in range(args.steps)]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        gms = max_over_ranks(e0.elapsed_time(e1), world)
+        out["graph"] = {"ms": gms, "value": world * N * args.steps / (gms / 1e3) / 1e6,
+                        "stats": gstats}
+        # through the public C-ABI with host buffers (the graph-captured step):
+        # every step uploads the state from pinned host memory and reads the
+        # result back
         nph = d.num_phases
         pin_u = torch.empty(N * d.dim, dtype=torch.float64, pin_memory=True).numpy()
         pin_q = torch.empty(N * nph, dtype=torch.float64, pin_memory=True).numpy()
@@ -316,7 +330,7 @@ def measure(args, form, rank, world, local, stream, e2e=True):
             lib.hydro_gpu_set_field(h.ctx, capi.F_VELOCITY, capi.TIME_CURR, dp(pin_u), pin_u.size)
             lib.hydro_gpu_set_field(h.ctx, capi.F_PARTIAL_DENSITY, capi.TIME_CURR, dp(pin_q),
                                     pin_q.size)
-            h.step()
+            h.step_graph()
             lib.hydro_gpu_get_field(h.ctx, capi.F_VELOCITY, capi.TIME_CURR, dp(pin_u), pin_u.size)
             lib.hydro_gpu_get_field(h.ctx, capi.F_PRESSURE, capi.TIME_CURR, dp(pin_p), pin_p.size)
             lib.hydro_gpu_get_field(h.ctx, capi.F_PARTIAL_DENSITY, capi.TIME_CURR, dp(pin_q),
@@ -324,7 +338,7 @@ def measure(args, form, rank, world, local, stream, e2e=True):
         torch.cuda.synchronize()
         e2e_s = max_over_ranks(time.perf_counter() - t0, world)
         out["e2e"] = {"value": round(world * N * args.steps / e2e_s / 1e6, 4),
-                      "unit": "Mcell-updates/s",
+                      "unit": "Mcell-updates/s", "api": "hydro_gpu_step_graph",
                       "h2d_bytes_per_step": (d.dim + nph) * N * 8,
                       "d2h_bytes_per_step": (d.dim + 1 + nph) * N * 8}
     h.close()
@@ -400,6 +414,7 @@ def run_ours(args, rank, world, local):
         "data": "synthetic: seeded rising drops (%d drops), no external data" % head["drops"],
         "config": {
             "workload": "rising_drops_%d^3" % args.n,
+            "step": "host-driven (hydro_gpu_step), per-group CUDA events on",
             "cells": N,
             "form": head["form"],
             "precision": head["precision"],
@@ -423,6 +438,14 @@ def run_ours(args, rank, world, local):
             "dt": stats[-1]["dt"],
         },
         "profile_ms": {k: round(v[1], 3) for k, v in sorted(head["prof"].items())},
+        "graph_step": {
+            "value": round(head["graph"]["value"], 4),
+            "ms_per_step": round(head["graph"]["ms"] / args.steps, 3),
+            "api": "hydro_gpu_step_graph",
+            "note": "same steps, one CUDA-graph launch per step; value above is the "
+                    "host-driven step with per-group CUDA events (roofline source)",
+            "pressure_iterations": [s["pressure_iterations"] for s in head["graph"]["stats"]],
+        },
     }
     if plain:
         out["plain_fp64"] = {
