@@ -283,6 +283,18 @@ def _declare(lib, prefix):
         lib.hydro_gpu_get_launch_count.restype = I
         lib.hydro_gpu_step_graph.argtypes = [P, ctypes.POINTER(StepStats)]
         lib.hydro_gpu_step_graph.restype = I
+        batch = {
+            "batch_create": [ctypes.POINTER(HydroDesc), I, ctypes.POINTER(P)],
+            "batch_destroy": [P],
+            "batch_size": [P, ctypes.POINTER(I)],
+            "batch_case": [P, I, ctypes.POINTER(P)],
+            "batch_init_state": [P],
+            "batch_step": [P, ctypes.POINTER(StepStats)],
+        }
+        for name, args in batch.items():
+            fn = getattr(lib, "hydro_gpu_" + name)
+            fn.argtypes = args
+            fn.restype = I
     else:
         stencil.argtypes = [I, I, I, I, D, ctypes.c_double, ctypes.c_long,
                             ctypes.c_double, D, D, I, ctypes.c_double, I,

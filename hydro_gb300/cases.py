@@ -214,3 +214,18 @@ def rising_drops(n=192, seed=0, dt_auto=True, cfl=0.25, dt_max=2e-3,
     q0 = two_phase_q(d, alpha1, smooth_times)
     u0 = np.zeros(d.ncells * 3)
     return d, u0, q0, drops
+
+
+def cavity_batch(ncases=512, seed=0, sizes=(64, 96, 128, 192, 256), dt=1e-3):
+    """Independent 2D lid-driven cavities of uneven size: per case the grid
+    size is drawn uniformly from `sizes`, Re = exp(U[ln 100, ln 5000]) and
+    mu = 1/Re (rho = 1, unit square, lid velocity 1), dt pinned.  Seeded
+    (Philox).  Returns a list of (desc, u0, q0, Re)."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    out = []
+    for _ in range(ncases):
+        n = int(sizes[rng.integers(len(sizes))])
+        re = float(np.exp(rng.uniform(np.log(100.0), np.log(5000.0))))
+        d, u0, q0 = cavity(n=n, mu=1.0 / re, dt=dt, lid=1.0)
+        out.append((d, u0, q0, re))
+    return out

@@ -1196,153 +1196,172 @@ int advection_substeps(const hydro_ctx* x, double dt, double* t_out) {
   return n;
 }
 
-// Captures one whole step (StartStep, SIMPLE loop, FinishStep, advection
-// substeps, property update, next auto time step) into x->sg.exec.  Loops
-// whose length the device decides are WHILE nodes; two SIMPLE iterations
-// are captured per loop trip (the second under an IF node) so that the
-// iteration layers alternate their buffers as the pointer swaps of the
-// host-driven step do; select copies leave every result where the host
-// pointers expect it.  Host-side scalars changed while capturing are
-// restored afterwards.
-int capture_step(hydro_ctx* x, int substeps) {
-  const Mesh& m = x->m;
-  const hydro_desc& d = x->d;
+// Host-side scalars a capture changes (it enqueues work of a step that has
+// not run); restored once the capture is complete.
+struct HostSnapshot {
+  double time, adv_time, p_res, indicator;
+  int iter_count, cd_iter_count, vel_sweeps, p_iters;
+  bool prof;
+};
+
+int begin_capture_of(hydro_ctx* x, HostSnapshot* s) {
   for (int i = 0; i < 4; ++i)
     if (!x->cap_streams[i]) CK(cudaStreamCreateWithFlags(&x->cap_streams[i], cudaStreamNonBlocking));
+  *s = {x->time, x->adv_time, x->p_res, x->indicator, x->iter_count, x->cd_iter_count,
+        x->vel_sweeps, x->p_iters, x->prof.on};
+  x->prof.on = false;
+  x->graph_mode = true;
+  return HYDRO_OK;
+}
+
+void end_capture_of(hydro_ctx* x, const HostSnapshot& s) {
+  x->graph_mode = false;
+  x->cap_graph = nullptr;
+  x->prof.on = s.prof;
+  x->time = s.time;
+  x->adv_time = s.adv_time;
+  x->p_res = s.p_res;
+  x->indicator = s.indicator;
+  x->iter_count = s.iter_count;
+  x->cd_iter_count = s.cd_iter_count;
+  x->vel_sweeps = s.vel_sweeps;
+  x->p_iters = s.p_iters;
+}
+
+// Enqueues one whole step (StartStep, SIMPLE loop, FinishStep, advection
+// substeps, property update, next auto time step) on x->st, which is
+// capturing into x->cap_graph.  Loops whose length the device decides are
+// WHILE nodes; two SIMPLE iterations are captured per loop trip (the second
+// under an IF node) so that the iteration layers alternate their buffers as
+// the pointer swaps of the host-driven step do; select copies leave every
+// result where the host pointers expect it.
+int enqueue_step_body(hydro_ctx* x, int substeps) {
+  const Mesh& m = x->m;
+  const hydro_desc& d = x->d;
+  double* q0 = x->q;
+    int r;
+    if ((r = reset_flags(x, FL_STEP_SWEEPS, 3))) return r;  // sweeps, p iterations, SIMPLE
+    if ((r = hydro_gpu_start_step(x))) return r;
+    const int limit = d.num_iterations_limit;
+    const double tol = d.convergence_tolerance;
+    const int cont0 = !(0 >= limit || 1. < tol);
+    cudaGraphConditionalHandle hw, hi;
+    if ((r = new_handle(x, cont0, &hw)) || (r = new_handle(x, 0, &hi))) return r;
+    r = add_while(x, hw, [&]() -> int {
+      int q;
+      if ((q = hydro_gpu_make_iteration(x))) return q;
+      CK(launch_ctl_simple2(x->pw.ds, limit, tol, hi, hw, x->st));
+      return add_if(x, hi, [&]() -> int {
+        int z;
+        if ((z = hydro_gpu_make_iteration(x))) return z;
+        CK(launch_ctl_simple(x->pw.ds, limit, tol, hw, 1, x->st));
+        return HYDRO_OK;
+      });
+    });
+    if (r) return r;
+    // an odd iteration count leaves the iterate in the other buffer
+    CK(launch_select_iter(m.nc * x->dim, x->u[HYDRO_ITER_PREV], x->u[HYDRO_ITER_CURR],
+                          x->pw.ds, x->st));
+    CK(launch_select_iter(m.nc, x->p[HYDRO_ITER_PREV], x->p[HYDRO_ITER_CURR], x->pw.ds,
+                          x->st));
+    CK(launch_select_iter(m.nf, x->F[HYDRO_ITER_PREV], x->F[HYDRO_ITER_CURR], x->pw.ds,
+                          x->st));
+    // FinishStep with copies instead of the pointer rotation
+    CK(cudaMemcpyAsync(x->p[HYDRO_TIME_PREV], x->p[HYDRO_TIME_CURR], sizeof(double) * m.nc,
+                       cudaMemcpyDeviceToDevice, x->st));
+    CK(cudaMemcpyAsync(x->F[HYDRO_TIME_PREV], x->F[HYDRO_TIME_CURR], sizeof(double) * m.nf,
+                       cudaMemcpyDeviceToDevice, x->st));
+    CK(cudaMemcpyAsync(x->u[HYDRO_TIME_PREV], x->u[HYDRO_TIME_CURR],
+                       sizeof(double) * m.nc * x->dim, cudaMemcpyDeviceToDevice, x->st));
+    CK(cudaMemcpyAsync(x->p[HYDRO_TIME_CURR], x->p[HYDRO_ITER_CURR], sizeof(double) * m.nc,
+                       cudaMemcpyDeviceToDevice, x->st));
+    CK(cudaMemcpyAsync(x->F[HYDRO_TIME_CURR], x->F[HYDRO_ITER_CURR], sizeof(double) * m.nf,
+                       cudaMemcpyDeviceToDevice, x->st));
+    CK(cudaMemcpyAsync(x->u[HYDRO_TIME_CURR], x->u[HYDRO_ITER_CURR],
+                       sizeof(double) * m.nc * x->dim, cudaMemcpyDeviceToDevice, x->st));
+    CK(launch_nan_count(m.nc, x->p[HYDRO_TIME_CURR], x->pw.partials, x->pw.ds, x->st));
+    x->time += x->dt;
+    for (int i = 0; i < substeps; ++i)
+      if ((r = hydro_gpu_advection_substep(x))) return r;
+    if (x->q != q0) {
+      // odd number of stage swaps: bring the fractions back to the buffer
+      // the next launch reads
+      CK(cudaMemcpyAsync(q0, x->q, sizeof(double) * m.nc * x->nph, cudaMemcpyDeviceToDevice,
+                         x->st));
+      std::swap(x->q, x->qtmp);
+    }
+    if ((r = hydro_gpu_update_properties(x))) return r;
+    CK(launch_auto_dt(m, x->F[HYDRO_TIME_CURR], x->pw.partials, x->pw.ds, x->st));
+    return HYDRO_OK;
+}
+
+// Captures one step of one context into x->sg.exec.
+int capture_step(hydro_ctx* x, int substeps) {
   if (x->sg.exec) {
     cudaGraphExecDestroy(x->sg.exec);
     x->sg.exec = nullptr;
   }
-  // host state to restore
-  const double time0 = x->time, adv_time0 = x->adv_time;
-  const int ic0 = x->iter_count, cdc0 = x->cd_iter_count, vs0 = x->vel_sweeps, pi0 = x->p_iters;
-  const double pres0 = x->p_res, ind0 = x->indicator;
-  double* q0 = x->q;
-  const bool prof0 = x->prof.on;
-  x->prof.on = false;
-  x->graph_mode = true;
-  CK(cudaGraphCreate(&x->cap_graph, 0));
-  int rc = HYDRO_OK;
-  cudaError_t e = cudaStreamBeginCaptureToGraph(x->st, x->cap_graph, nullptr, nullptr, 0,
-                                                cudaStreamCaptureModeRelaxed);
-  if (e == cudaSuccess) {
-    auto body = [&]() -> int {
-      int r;
-      if ((r = reset_flags(x, FL_STEP_SWEEPS, 3))) return r;  // sweeps, p iterations, SIMPLE
-      if ((r = hydro_gpu_start_step(x))) return r;
-      const int limit = d.num_iterations_limit;
-      const double tol = d.convergence_tolerance;
-      const int cont0 = !(0 >= limit || 1. < tol);
-      cudaGraphConditionalHandle hw, hi;
-      if ((r = new_handle(x, cont0, &hw)) || (r = new_handle(x, 0, &hi))) return r;
-      r = add_while(x, hw, [&]() -> int {
-        int q;
-        if ((q = hydro_gpu_make_iteration(x))) return q;
-        CK(launch_ctl_simple2(x->pw.ds, limit, tol, hi, hw, x->st));
-        return add_if(x, hi, [&]() -> int {
-          int z;
-          if ((z = hydro_gpu_make_iteration(x))) return z;
-          CK(launch_ctl_simple(x->pw.ds, limit, tol, hw, 1, x->st));
-          return HYDRO_OK;
-        });
-      });
-      if (r) return r;
-      // an odd iteration count leaves the iterate in the other buffer
-      CK(launch_select_iter(m.nc * x->dim, x->u[HYDRO_ITER_PREV], x->u[HYDRO_ITER_CURR],
-                            x->pw.ds, x->st));
-      CK(launch_select_iter(m.nc, x->p[HYDRO_ITER_PREV], x->p[HYDRO_ITER_CURR], x->pw.ds,
-                            x->st));
-      CK(launch_select_iter(m.nf, x->F[HYDRO_ITER_PREV], x->F[HYDRO_ITER_CURR], x->pw.ds,
-                            x->st));
-      // FinishStep with copies instead of the pointer rotation
-      CK(cudaMemcpyAsync(x->p[HYDRO_TIME_PREV], x->p[HYDRO_TIME_CURR], sizeof(double) * m.nc,
-                         cudaMemcpyDeviceToDevice, x->st));
-      CK(cudaMemcpyAsync(x->F[HYDRO_TIME_PREV], x->F[HYDRO_TIME_CURR], sizeof(double) * m.nf,
-                         cudaMemcpyDeviceToDevice, x->st));
-      CK(cudaMemcpyAsync(x->u[HYDRO_TIME_PREV], x->u[HYDRO_TIME_CURR],
-                         sizeof(double) * m.nc * x->dim, cudaMemcpyDeviceToDevice, x->st));
-      CK(cudaMemcpyAsync(x->p[HYDRO_TIME_CURR], x->p[HYDRO_ITER_CURR], sizeof(double) * m.nc,
-                         cudaMemcpyDeviceToDevice, x->st));
-      CK(cudaMemcpyAsync(x->F[HYDRO_TIME_CURR], x->F[HYDRO_ITER_CURR], sizeof(double) * m.nf,
-                         cudaMemcpyDeviceToDevice, x->st));
-      CK(cudaMemcpyAsync(x->u[HYDRO_TIME_CURR], x->u[HYDRO_ITER_CURR],
-                         sizeof(double) * m.nc * x->dim, cudaMemcpyDeviceToDevice, x->st));
-      CK(launch_nan_count(m.nc, x->p[HYDRO_TIME_CURR], x->pw.partials, x->pw.ds, x->st));
-      x->time += x->dt;
-      for (int i = 0; i < substeps; ++i)
-        if ((r = hydro_gpu_advection_substep(x))) return r;
-      if (x->q != q0) {
-        // odd number of stage swaps: bring the fractions back to the buffer
-        // the next launch reads
-        CK(cudaMemcpyAsync(q0, x->q, sizeof(double) * m.nc * x->nph, cudaMemcpyDeviceToDevice,
-                           x->st));
-        std::swap(x->q, x->qtmp);
-      }
-      if ((r = hydro_gpu_update_properties(x))) return r;
-      CK(launch_auto_dt(m, x->F[HYDRO_TIME_CURR], x->pw.partials, x->pw.ds, x->st));
-      return HYDRO_OK;
-    };
-    rc = body();
-    cudaGraph_t g = nullptr;
-    cudaError_t e2 = cudaStreamEndCapture(x->st, &g);
+  HostSnapshot snap;
+  int rc = begin_capture_of(x, &snap);
+  if (rc) return rc;
+  cudaGraph_t g = nullptr;
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) {
+    end_capture_of(x, snap);
+    return HYDRO_ERR_CUDA;
+  }
+  x->cap_graph = g;
+  if (cudaStreamBeginCaptureToGraph(x->st, g, nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeRelaxed) == cudaSuccess) {
+    rc = enqueue_step_body(x, substeps);
+    cudaGraph_t out = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(x->st, &out);
     if (!rc && e2 != cudaSuccess) rc = HYDRO_ERR_CUDA;
-    if (!rc && cudaGraphInstantiate(&x->sg.exec, x->cap_graph, 0) != cudaSuccess) {
+    if (!rc && cudaGraphInstantiate(&x->sg.exec, g, 0) != cudaSuccess) {
       x->sg.exec = nullptr;
       rc = HYDRO_ERR_CUDA;
     }
   } else {
     rc = HYDRO_ERR_CUDA;
   }
-  cudaGraphDestroy(x->cap_graph);
-  x->cap_graph = nullptr;
-  x->graph_mode = false;
-  x->prof.on = prof0;
-  x->time = time0;
-  x->adv_time = adv_time0;
-  x->iter_count = ic0;
-  x->cd_iter_count = cdc0;
-  x->vel_sweeps = vs0;
-  x->p_iters = pi0;
-  x->p_res = pres0;
-  x->indicator = ind0;
+  cudaGraphDestroy(g);
+  end_capture_of(x, snap);
   cudaGetLastError();
   return rc;
 }
 
-}  // namespace
-
-int hydro_gpu_step_graph(hydro_ctx* x, hydro_step_stats* stats) {
-  if (!x) return HYDRO_ERR_ARG;
+// dt of the coming step (hydro<Mesh>::step, hydro2d.hpp:1541-1553).
+int next_dt(hydro_ctx* x) {
   const hydro_desc& d = x->d;
+  if (!d.dt_auto) return HYDRO_OK;
+  double dtm;
+  int rc = hydro_gpu_get_auto_time_step(x, &dtm);
+  if (rc) return rc;
+  double dt = dtm * d.cfl, dta = dtm * d.cfl_advection;
+  if (d.dt_max > 0. && dt > d.dt_max) {
+    dta = dta * (d.dt_max / dt);
+    dt = d.dt_max;
+  }
+  x->dt = dt;
+  x->adv_dt = dta;
+  return HYDRO_OK;
+}
+
+bool graph_stale(const hydro_ctx* x, int substeps) {
+  return x->sg.dt != x->dt || x->sg.adv_dt != x->adv_dt || x->sg.substeps != substeps ||
+         x->sg.sources != x->fc.sources;
+}
+
+void graph_key(hydro_ctx* x, int substeps) {
+  x->sg.dt = x->dt;
+  x->sg.adv_dt = x->adv_dt;
+  x->sg.substeps = substeps;
+  x->sg.sources = x->fc.sources;
+}
+
+// After a graph launch completed and x->hds holds the device scalars.
+int finish_graph_step(hydro_ctx* x, int substeps, double adv_end, hydro_step_stats* stats) {
   hydro_step_stats s;
   memset(&s, 0, sizeof(s));
-  int rc;
-  if (d.dt_auto) {
-    double dtm;
-    rc = hydro_gpu_get_auto_time_step(x, &dtm);
-    if (rc) return rc;
-    double dt = dtm * d.cfl, dta = dtm * d.cfl_advection;
-    if (d.dt_max > 0. && dt > d.dt_max) {
-      dta = dta * (d.dt_max / dt);
-      dt = d.dt_max;
-    }
-    x->dt = dt;
-    x->adv_dt = dta;
-  }
-  double adv_end;
-  const int substeps = advection_substeps(x, x->dt, &adv_end);
-  if (!x->sg.exec || x->sg.dt != x->dt || x->sg.adv_dt != x->adv_dt ||
-      x->sg.substeps != substeps || x->sg.sources != x->fc.sources) {
-    rc = capture_step(x, substeps);
-    if (rc) return rc;
-    x->sg.dt = x->dt;
-    x->sg.adv_dt = x->adv_dt;
-    x->sg.substeps = substeps;
-    x->sg.sources = x->fc.sources;
-  }
-  CK(cudaGraphLaunch(x->sg.exec, x->st));
-  rc = sync_scalars(x);
-  if (rc) return rc;
   const DevScalars& h = *x->hds;
   x->iter_count = h.flag[FL_ITERS];
   x->cd_iter_count = h.flag[FL_ITERS];
@@ -1365,6 +1384,185 @@ int hydro_gpu_step_graph(hydro_ctx* x, hydro_step_stats* stats) {
   s.status = (h.red[RS_NAN] > 0. || isnan(x->indicator)) ? HYDRO_ERR_NAN : HYDRO_OK;
   if (stats) *stats = s;
   return s.status;
+}
+
+}  // namespace
+
+int hydro_gpu_step_graph(hydro_ctx* x, hydro_step_stats* stats) {
+  if (!x) return HYDRO_ERR_ARG;
+  int rc = next_dt(x);
+  if (rc) return rc;
+  double adv_end;
+  const int substeps = advection_substeps(x, x->dt, &adv_end);
+  if (!x->sg.exec || graph_stale(x, substeps)) {
+    rc = capture_step(x, substeps);
+    if (rc) return rc;
+    graph_key(x, substeps);
+  }
+  CK(cudaGraphLaunch(x->sg.exec, x->st));
+  rc = sync_scalars(x);
+  if (rc) return rc;
+  return finish_graph_step(x, substeps, adv_end, stats);
+}
+
+// ----------------------------------------------------------------- batch --
+// Many independent cases (hydro_gpu_batch_*): one context per case, and one
+// CUDA graph per batch step in which every case's step is an independent
+// branch (fork from the launching stream, join back), so a single launch
+// runs all cases concurrently with their loops steered on the device.
+struct hydro_batch {
+  std::vector<hydro_ctx*> cases;
+  cudaStream_t st = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<int> substeps;
+  std::vector<double> adv_end;
+};
+
+int hydro_gpu_batch_destroy(hydro_batch* b) {
+  if (!b) return HYDRO_OK;
+  if (b->st) cudaStreamSynchronize(b->st);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (auto* x : b->cases) hydro_gpu_destroy(x);
+  for (auto e : b->join) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_batch_create(const hydro_desc* descs, int ncases, hydro_batch** out) {
+  if (!descs || !out || ncases < 1) return HYDRO_ERR_ARG;
+  *out = nullptr;
+  hydro_batch* b = new (std::nothrow) hydro_batch();
+  if (!b) return HYDRO_ERR_NOMEM;
+  if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
+    hydro_gpu_batch_destroy(b);
+    return HYDRO_ERR_CUDA;
+  }
+  for (int i = 0; i < ncases; ++i) {
+    hydro_desc d = descs[i];
+    d.stream = nullptr;  // every case owns its stream (its graph branch)
+    hydro_ctx* x = nullptr;
+    int rc = hydro_gpu_create(&d, &x);
+    if (rc) {
+      hydro_gpu_batch_destroy(b);
+      return rc;
+    }
+    b->cases.push_back(x);
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      hydro_gpu_batch_destroy(b);
+      return HYDRO_ERR_CUDA;
+    }
+    b->join.push_back(e);
+  }
+  b->substeps.assign(ncases, -1);
+  b->adv_end.assign(ncases, 0.);
+  *out = b;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_batch_size(hydro_batch* b, int* n) {
+  if (!b || !n) return HYDRO_ERR_ARG;
+  *n = (int)b->cases.size();
+  return HYDRO_OK;
+}
+
+int hydro_gpu_batch_case(hydro_batch* b, int i, hydro_ctx** out) {
+  if (!b || !out || i < 0 || i >= (int)b->cases.size()) return HYDRO_ERR_ARG;
+  *out = b->cases[i];
+  return HYDRO_OK;
+}
+
+int hydro_gpu_batch_init_state(hydro_batch* b) {
+  if (!b) return HYDRO_ERR_ARG;
+  for (auto* x : b->cases) {
+    int rc = hydro_gpu_init_state(x);
+    if (rc) return rc;
+  }
+  return HYDRO_OK;
+}
+
+namespace {
+
+int capture_batch(hydro_batch* b) {
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  CK(cudaGraphCreate(&g, 0));
+  int rc = HYDRO_OK;
+  const int n = (int)b->cases.size();
+  std::vector<HostSnapshot> snaps(n);
+  std::vector<int> begun(n, 0);
+  if (cudaStreamBeginCaptureToGraph(b->st, g, nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return HYDRO_ERR_CUDA;
+  }
+  if (cudaEventRecord(b->fork, b->st) != cudaSuccess) rc = HYDRO_ERR_CUDA;
+  for (int i = 0; i < n && !rc; ++i) {
+    hydro_ctx* x = b->cases[i];
+    if ((rc = begin_capture_of(x, &snaps[i]))) break;
+    begun[i] = 1;
+    x->cap_graph = g;
+    if (cudaStreamWaitEvent(x->st, b->fork, 0) != cudaSuccess) {
+      rc = HYDRO_ERR_CUDA;
+      break;
+    }
+    rc = enqueue_step_body(x, b->substeps[i]);
+    if (!rc && (cudaEventRecord(b->join[i], x->st) != cudaSuccess ||
+                cudaStreamWaitEvent(b->st, b->join[i], 0) != cudaSuccess))
+      rc = HYDRO_ERR_CUDA;
+  }
+  cudaGraph_t outg = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(b->st, &outg);
+  if (!rc && e2 != cudaSuccess) rc = HYDRO_ERR_CUDA;
+  if (!rc && cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) {
+    b->exec = nullptr;
+    rc = HYDRO_ERR_CUDA;
+  }
+  cudaGraphDestroy(g);
+  for (int i = 0; i < n; ++i)
+    if (begun[i]) end_capture_of(b->cases[i], snaps[i]);
+  cudaGetLastError();
+  return rc;
+}
+
+}  // namespace
+
+int hydro_gpu_batch_step(hydro_batch* b, hydro_step_stats* stats) {
+  if (!b) return HYDRO_ERR_ARG;
+  const int n = (int)b->cases.size();
+  bool stale = !b->exec;
+  for (int i = 0; i < n; ++i) {
+    hydro_ctx* x = b->cases[i];
+    int rc = next_dt(x);
+    if (rc) return rc;
+    int ns = advection_substeps(x, x->dt, &b->adv_end[i]);
+    if (ns != b->substeps[i] || graph_stale(x, ns)) stale = true;
+    b->substeps[i] = ns;
+  }
+  if (stale) {
+    int rc = capture_batch(b);
+    if (rc) return rc;
+    for (int i = 0; i < n; ++i) graph_key(b->cases[i], b->substeps[i]);
+  }
+  CK(cudaGraphLaunch(b->exec, b->st));
+  for (auto* x : b->cases)
+    CK(cudaMemcpyAsync(x->hds, x->pw.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, b->st));
+  CK(cudaStreamSynchronize(b->st));
+  int status = HYDRO_OK;
+  for (int i = 0; i < n; ++i) {
+    int rc = finish_graph_step(b->cases[i], b->substeps[i], b->adv_end[i],
+                               stats ? &stats[i] : nullptr);
+    if (rc && !status) status = rc;
+  }
+  return status;
 }
 
 int hydro_gpu_calc_stat(hydro_ctx* x, hydro_stat* out) {

@@ -26,14 +26,18 @@ def _dp(a):
 class Hydro:
     prefix = "hydro_gpu"
 
-    def __init__(self, desc, stream=None):
+    def __init__(self, desc, stream=None, _ctx=None):
         self.lib = capi.load()
         self.desc = desc.copy()
         if stream is not None:
             self.desc.stream = ctypes.c_void_p(stream)
-        self.ctx = ctypes.c_void_p()
-        self._check(self.lib.hydro_gpu_create(ctypes.byref(self.desc), ctypes.byref(self.ctx)),
-                    "hydro_gpu_create")
+        self._owned = _ctx is None
+        if _ctx is None:
+            self.ctx = ctypes.c_void_p()
+            self._check(self.lib.hydro_gpu_create(ctypes.byref(self.desc),
+                                                  ctypes.byref(self.ctx)), "hydro_gpu_create")
+        else:
+            self.ctx = _ctx
         self.nc = self.desc.ncells
         self.nf = self.desc.nfaces
         self.dim = self.desc.dim
@@ -45,7 +49,8 @@ class Hydro:
 
     def close(self):
         if getattr(self, "ctx", None):
-            self.lib.hydro_gpu_destroy(self.ctx)
+            if getattr(self, "_owned", True):
+                self.lib.hydro_gpu_destroy(self.ctx)
             self.ctx = None
 
     def __del__(self):
@@ -188,6 +193,45 @@ def launch_count():
     n = ctypes.c_longlong()
     capi.load().hydro_gpu_get_launch_count(ctypes.byref(n))
     return n.value
+
+
+class Batch:
+    """Independent cases advanced together, one CUDA-graph launch per batch
+    step (hydro_gpu_batch_*).  ``cases[i]`` is a ``Hydro`` view of case i
+    (fields, stats) owned by the batch."""
+
+    def __init__(self, descs):
+        self.lib = capi.load()
+        arr = (capi.HydroDesc * len(descs))()
+        for i, d in enumerate(descs):
+            arr[i] = d.copy()
+        self.b = ctypes.c_void_p()
+        Hydro._check(self.lib.hydro_gpu_batch_create(arr, len(descs), ctypes.byref(self.b)),
+                     "hydro_gpu_batch_create")
+        self.cases = []
+        for i, d in enumerate(descs):
+            c = ctypes.c_void_p()
+            Hydro._check(self.lib.hydro_gpu_batch_case(self.b, i, ctypes.byref(c)),
+                         "hydro_gpu_batch_case")
+            self.cases.append(Hydro(d, _ctx=c))
+
+    def init_state(self):
+        Hydro._check(self.lib.hydro_gpu_batch_init_state(self.b), "hydro_gpu_batch_init_state")
+
+    def step(self):
+        st = (capi.StepStats * len(self.cases))()
+        Hydro._check(self.lib.hydro_gpu_batch_step(self.b, st), "hydro_gpu_batch_step")
+        return [s.as_dict() for s in st]
+
+    def close(self):
+        if getattr(self, "b", None):
+            for c in self.cases:
+                c.ctx = None
+            self.lib.hydro_gpu_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        self.close()
 
 
 def make(desc, u0, q0, stream=None):

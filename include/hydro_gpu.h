@@ -241,6 +241,30 @@ int hydro_gpu_step(hydro_ctx* ctx, hydro_step_stats* stats);
 int hydro_gpu_step_graph(hydro_ctx* ctx, hydro_step_stats* stats);
 int hydro_gpu_calc_stat(hydro_ctx* ctx, hydro_stat* out);
 
+/* ---- many independent cases ------------------------------------------
+ * A batch of independent cases of uneven size (one hydro_desc each, e.g.
+ * hundreds of small cavities), advanced together: every batch step is ONE
+ * CUDA-graph launch in which each case's whole step (as in
+ * hydro_gpu_step_graph) is an independent branch, so the GPU runs all cases
+ * at once and the host waits once per batch step.  The reference has no
+ * counterpart on its solver interface: it runs independent experiments as
+ * one host thread per experiment (console.cpp:162-178, 922-965); each case
+ * here behaves exactly like its own hydro_ctx stepped with hydro_gpu_step
+ * (same results and stats).  Cases are reached with hydro_gpu_batch_case for
+ * set_field / get_field / calc_stat; the batch owns them (do not destroy
+ * them).  The batch graph is captured again when any case's dt, substep
+ * count or sources change. */
+typedef struct hydro_batch hydro_batch;
+int hydro_gpu_batch_create(const hydro_desc* descs, int ncases, hydro_batch** out);
+int hydro_gpu_batch_destroy(hydro_batch* batch);
+int hydro_gpu_batch_size(hydro_batch* batch, int* ncases);
+int hydro_gpu_batch_case(hydro_batch* batch, int index, hydro_ctx** out);
+/* hydro_gpu_init_state of every case. */
+int hydro_gpu_batch_init_state(hydro_batch* batch);
+/* One step of every case; stats (may be NULL) receives ncases entries.
+ * Returns the first non-OK case status. */
+int hydro_gpu_batch_step(hydro_batch* batch, hydro_step_stats* stats);
+
 /* Solve sum_j a_j x_j + c = 0 for a symmetric 7-point (3D) / 5-point (2D)
  * stencil on an nx*ny*nz block, the rows the pressure system has
  * (fluid.hpp:972-1027): coupling coefficients per face, diagonal implied as
