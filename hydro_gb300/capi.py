@@ -11,12 +11,14 @@ import os
 HYDRO_MAX_PHASES = 4
 
 # enum hydro_status
-OK, ERR_ARG, ERR_CUDA, ERR_NAN, NOT_CONVERGED, ERR_UNSUPPORTED, ERR_NOMEM, ERR_NO_DEVICE = range(8)
+(OK, ERR_ARG, ERR_CUDA, ERR_NAN, NOT_CONVERGED, ERR_UNSUPPORTED, ERR_NOMEM, ERR_NO_DEVICE,
+ ERR_IO) = range(9)
 STATUS_NAMES = {
     OK: "HYDRO_OK", ERR_ARG: "HYDRO_ERR_ARG", ERR_CUDA: "HYDRO_ERR_CUDA",
     ERR_NAN: "HYDRO_ERR_NAN", NOT_CONVERGED: "HYDRO_NOT_CONVERGED",
     ERR_UNSUPPORTED: "HYDRO_ERR_UNSUPPORTED", ERR_NOMEM: "HYDRO_ERR_NOMEM",
     ERR_NO_DEVICE: "HYDRO_ERR_NO_DEVICE",
+    ERR_IO: "HYDRO_ERR_IO",
 }
 
 # enum hydro_side
@@ -142,6 +144,8 @@ class Stat(ctypes.Structure):
         ("center", (ctypes.c_double * 3) * HYDRO_MAX_PHASES),
         ("velocity", (ctypes.c_double * 3) * HYDRO_MAX_PHASES),
         ("partial_mass", ctypes.c_double * HYDRO_MAX_PHASES),
+        ("volume_flux_in", ctypes.c_double * HYDRO_MAX_PHASES),
+        ("volume_flux_out", ctypes.c_double * HYDRO_MAX_PHASES),
     ]
 
 
@@ -293,6 +297,25 @@ def _declare(lib, prefix):
         }
         for name, args in batch.items():
             fn = getattr(lib, "hydro_gpu_" + name)
+            fn.argtypes = args
+            fn.restype = I
+        C = ctypes.c_char_p
+        extra = {
+            "hydro_gpu_get_desc": [P, ctypes.POINTER(HydroDesc)],
+            "hydro_gpu_get_stream": [P, ctypes.POINTER(P)],
+            "hydro_gpu_get_time_step": [P, D],
+            "hydro_output_open": [P, C, C, ctypes.POINTER(P)],
+            "hydro_output_write": [P, ctypes.c_double],
+            "hydro_output_flush": [P],
+            "hydro_output_close": [P],
+            "hydro_vts_write_host": [C, I, ctypes.POINTER(I), D, D, I, ctypes.POINTER(C),
+                                     ctypes.POINTER(I), ctypes.POINTER(D)],
+            "hydro_scalar_output_open": [P, C, ctypes.POINTER(P)],
+            "hydro_scalar_output_write": [P, ctypes.c_double, I],
+            "hydro_scalar_output_close": [P],
+        }
+        for name, args in extra.items():
+            fn = getattr(lib, name)
             fn.argtypes = args
             fn.restype = I
     else:

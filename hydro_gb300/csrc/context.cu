@@ -717,7 +717,7 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
     w.idg32 = a.take<float>(nc);
     w.x32 = a.take<float>(nc);
     w.kf32 = a.take<float>(nf);
-    w.partials = a.take<double>((size_t)10 * kMaxBlocks);
+    w.partials = a.take<double>((size_t)12 * kMaxBlocks);
     // multigrid hierarchy (level 0 shares the FP32 CG arrays)
     MgWork& mg = x->mg;
     mg.nlev = desc->pressure_solver == HYDRO_LINEAR_MGCG ? mg_levels_for(m) : 0;
@@ -799,6 +799,25 @@ int hydro_gpu_destroy(hydro_ctx* x) {
   if (x->hds) cudaFreeHost(x->hds);
   if (x->own_stream && x->st) cudaStreamDestroy(x->st);
   delete x;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_get_desc(hydro_ctx* x, hydro_desc* d) {
+  if (!x || !d) return HYDRO_ERR_ARG;
+  *d = x->d;
+  d->stream = (void*)x->st;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_get_stream(hydro_ctx* x, void** st) {
+  if (!x || !st) return HYDRO_ERR_ARG;
+  *st = (void*)x->st;
+  return HYDRO_OK;
+}
+
+int hydro_gpu_get_time_step(hydro_ctx* x, double* dt) {
+  if (!x || !dt) return HYDRO_ERR_ARG;
+  *dt = x->dt;
   return HYDRO_OK;
 }
 
@@ -1573,8 +1592,9 @@ int hydro_gpu_calc_stat(hydro_ctx* x, hydro_stat* out) {
   for (int i = 0; i < x->nph; ++i) {
     CK(cudaMemsetAsync(x->stat_ticket, 0, sizeof(unsigned) * 4, x->st));
     CK(launch_stat(m, x->q + (size_t)i * m.nc, x->alpha + (size_t)i * m.nc,
-                   x->uc3(HYDRO_TIME_CURR), x->pw.partials, x->stat_out, x->stat_ticket, x->st));
-    CK(cudaMemcpyAsync(h, x->stat_out, sizeof(double) * 10, cudaMemcpyDeviceToHost, x->st));
+                   x->uc3(HYDRO_TIME_CURR), x->F[HYDRO_TIME_CURR], x->pw.partials, x->stat_out,
+                   x->stat_ticket, x->st));
+    CK(cudaMemcpyAsync(h, x->stat_out, sizeof(double) * 12, cudaMemcpyDeviceToHost, x->st));
     CK(cudaStreamSynchronize(x->st));
     out->volume[i] = h[0];
     out->mass[i] = h[0] * x->d.density[i];
@@ -1583,8 +1603,10 @@ int hydro_gpu_calc_stat(hydro_ctx* x, hydro_stat* out) {
       out->velocity[i][k] = h[4 + k] / h[0];
     }
     out->partial_mass[i] = h[7];
-    out->pd_min[i] = h[8];
-    out->pd_max[i] = h[9];
+    out->volume_flux_in[i] = h[8];
+    out->volume_flux_out[i] = h[9];
+    out->pd_min[i] = h[10];
+    out->pd_max[i] = h[11];
   }
   return HYDRO_OK;
 }

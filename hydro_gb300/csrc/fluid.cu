@@ -627,16 +627,19 @@ __global__ void k_stforce(Mesh m, Geo g, double sigma, C3 G, W3 out, int kch) {
   CELL_LOOP_END
 }
 
-// CalcStat (hydro2d.hpp:1432-1467) of one phase: sums of alpha V,
-// x alpha V, u alpha V and q V; min and max of q.
+// CalcStat (hydro2d.hpp:1432-1493) of one phase: sums of alpha V,
+// x alpha V, u alpha V and q V, the boundary volume flux of the phase into
+// and out of the domain (flux towards the cell times alpha); min and max
+// of q.
 template <int DIM>
 __global__ void __launch_bounds__(NT) k_stat(Mesh m, Geo g, const double* q, const double* al,
-                                             C3 u, double* partials, double* out,
-                                             unsigned* ticket, int kch) {
-  double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                                             C3 u, const double* F, double* partials,
+                                             double* out, unsigned* ticket, int kch) {
+  double s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   double qmin = 1e10, qmax = -1e10;
   CELL_LOOP_BEGIN(m, kch)
-  double a = al[X.c] * g.V;
+  const double alc = al[X.c];
+  double a = alc * g.V;
   s[0] += a;
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
@@ -646,20 +649,33 @@ __global__ void __launch_bounds__(NT) k_stat(Mesh m, Geo g, const double* q, con
   }
   double qc = q[X.c];
   s[7] += qc * g.V;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+    // low boundary face: the cell is its second neighbour (flux towards
+    // the cell = +F); high boundary face: its first (-F)
+    for (int side = 0; side < 2; ++side) {
+      bool bnd = side ? X.i[d] == m.n[d] - 1 : X.i[d] == 0;
+      if (!bnd) continue;
+      double ftc = side ? -F[f + face_stride(m, d)] : F[f];
+      if (ftc >= 0.) s[8] += ftc * alc;
+      else s[9] -= ftc * alc;
+    }
+  }
   qmin = fmin(qmin, qc);
   qmax = fmax(qmax, qc);
   CELL_LOOP_END
-  __shared__ double o8[8], o1[1], o2[1];
-  if (grid_reduce<RED_SUM, 8>(s, partials, &ticket[0], o8)) {
+  __shared__ double o10[10], o1[1], o2[1];
+  if (grid_reduce<RED_SUM, 10>(s, partials, &ticket[0], o10)) {
     if (threadIdx.x == 0 && threadIdx.y == 0)
-      for (int a = 0; a < 8; ++a) out[a] = o8[a];
+      for (int a = 0; a < 10; ++a) out[a] = o10[a];
   }
   double vmin[1] = {qmin}, vmax[1] = {qmax};
-  if (grid_reduce<RED_MIN, 1>(vmin, partials + 8 * kMaxBlocks, &ticket[1], o1)) {
-    if (threadIdx.x == 0 && threadIdx.y == 0) out[8] = o1[0];
+  if (grid_reduce<RED_MIN, 1>(vmin, partials + 10 * kMaxBlocks, &ticket[1], o1)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) out[10] = o1[0];
   }
-  if (grid_reduce<RED_MAX, 1>(vmax, partials + 9 * kMaxBlocks, &ticket[2], o2)) {
-    if (threadIdx.x == 0 && threadIdx.y == 0) out[9] = o2[0];
+  if (grid_reduce<RED_MAX, 1>(vmax, partials + 11 * kMaxBlocks, &ticket[2], o2)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) out[11] = o2[0];
   }
 }
 
@@ -883,8 +899,9 @@ cudaError_t launch_stforce(const Mesh& m, double sigma, const double* alpha1, W3
 }
 
 cudaError_t launch_stat(const Mesh& m, const double* q, const double* alpha, C3 u,
-                        double* partials, double* out, unsigned* ticket, cudaStream_t st) {
-  DISPATCH_DIM(m, k_stat, m, make_geo(m), q, alpha, u, partials, out, ticket);
+                        const double* F, double* partials, double* out, unsigned* ticket,
+                        cudaStream_t st) {
+  DISPATCH_DIM(m, k_stat, m, make_geo(m), q, alpha, u, F, partials, out, ticket);
 }
 
 }  // namespace hg

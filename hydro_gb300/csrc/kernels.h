@@ -148,9 +148,11 @@ cudaError_t launch_props(const Mesh& m, int nph, const PhaseProps& pp,
 cudaError_t launch_smooth(const Mesh& m, const double* in, double* out, cudaStream_t st);
 cudaError_t launch_stforce(const Mesh& m, double sigma, const double* alpha1, W3 G,
                            W3 out, cudaStream_t st);
-// out (device): [8 sums, min, max]; partials >= 10*4096 doubles; ticket[3]
+// out (device): [10 sums, min, max]; partials >= 12*kMaxBlocks doubles;
+// ticket[3]; F: time_curr volume fluxes
 cudaError_t launch_stat(const Mesh& m, const double* q, const double* alpha, C3 u,
-                        double* partials, double* out, unsigned* ticket, cudaStream_t st);
+                        const double* F, double* partials, double* out, unsigned* ticket,
+                        cudaStream_t st);
 
 // ------------------------------------------------------------ advection --
 // Face fluxes q_f F_f of every phase (Superbee, solver.hpp:550-619) on the

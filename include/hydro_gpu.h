@@ -62,7 +62,8 @@ enum hydro_status {
   HYDRO_NOT_CONVERGED = 4,    /* a linear solve hit its iteration limit */
   HYDRO_ERR_UNSUPPORTED = 5,  /* option the GPU path does not implement */
   HYDRO_ERR_NOMEM = 6,        /* device allocation failed */
-  HYDRO_ERR_NO_DEVICE = 7     /* no CUDA device visible */
+  HYDRO_ERR_NO_DEVICE = 7,    /* no CUDA device visible */
+  HYDRO_ERR_IO = 8            /* an output file could not be written */
 };
 
 /* Sides of the block, in the reference's neighbour-face order
@@ -186,6 +187,10 @@ typedef struct hydro_stat {
   double velocity[HYDRO_MAX_PHASES][3];
   /* sum_c q_i(c) V_c in FP64: the quantity TVD advection conserves */
   double partial_mass[HYDRO_MAX_PHASES];
+  /* volume flux of phase i into / out of the domain through the boundary
+   * faces per unit time (hydro2d.hpp:1474-1493; the module accumulates them
+   * times dt into stat_volume_in/out) */
+  double volume_flux_in[HYDRO_MAX_PHASES], volume_flux_out[HYDRO_MAX_PHASES];
 } hydro_stat;
 
 typedef struct hydro_ctx hydro_ctx;
@@ -202,6 +207,13 @@ int hydro_gpu_set_field(hydro_ctx* ctx, int field, int layer, const double* src,
 int hydro_gpu_get_field(hydro_ctx* ctx, int field, int layer, double* dst, size_t n);
 /* Device pointer of a field layer (no copy); NULL if the field is unknown. */
 int hydro_gpu_field_ptr(hydro_ctx* ctx, int field, int layer, double** ptr);
+/* The description the context was created with (d->stream: its stream). */
+int hydro_gpu_get_desc(hydro_ctx* ctx, hydro_desc* d);
+/* The CUDA stream (cudaStream_t) all of the context's work is ordered on;
+ * work a caller enqueues on it runs after the context's pending steps. */
+int hydro_gpu_get_stream(hydro_ctx* ctx, void** stream);
+/* The fluid time step of the last / coming step (GetTimeStep). */
+int hydro_gpu_get_time_step(hydro_ctx* ctx, double* dt);
 
 /* Initial state: velocity (time_curr = time_prev = given), partial densities.
  * Computes the initial face fluxes (fluid.hpp:770-791) and then the mixture
@@ -264,6 +276,47 @@ int hydro_gpu_batch_init_state(hydro_batch* batch);
 /* One step of every case; stats (may be NULL) receives ncases entries.
  * Returns the first non-OK case status. */
 int hydro_gpu_batch_step(hydro_batch* batch, hydro_step_stats* stats);
+
+/* ---- output in the reference's file formats ---------------------------
+ * Fields: SessionParaviewStructured (output_paraview.hpp:34-175), one ASCII
+ * .vts StructuredGrid file per frame named <basename>.<frame>.vts and the
+ * collection <basename>.pvd.  `fields` lists entry names, comma or space
+ * separated, of the reference's output_<name> flags (hydro2d.hpp:710-816):
+ * x y z (nodes), velocity_x/y/z, pressure, density, viscosity,
+ * volume_source, excluded, divergence, mass_fraction_<i>, density_<i>,
+ * partial_density_<i>, volume_fraction_<i>; they are written in the
+ * reference's order whatever the order of the list.  NULL or "" selects the
+ * defaults of examples/general.hydroconf (x y [z] velocity_x velocity_y
+ * [velocity_z] pressure volume_fraction_0 volume_fraction_1).  Names the hot
+ * path does not compute (radiation, temperature, mass_source_<i>,
+ * target_density_<i>) give HYDRO_ERR_UNSUPPORTED.
+ * hydro_output_write copies the time_curr fields to pinned host memory on
+ * a side stream ordered after the context's stream and returns; a worker
+ * thread formats and writes the file while the GPU carries on (one frame in
+ * flight: the next write, flush or close waits for it).  Values print as
+ * the reference's ostream does (%g). */
+typedef struct hydro_output hydro_output;
+int hydro_output_open(hydro_ctx* ctx, const char* basename, const char* fields,
+                      hydro_output** out);
+int hydro_output_write(hydro_output* out, double time);
+int hydro_output_flush(hydro_output* out);
+/* Flushes, writes the collection footer, frees. */
+int hydro_output_close(hydro_output* out);
+/* One .vts frame from host arrays, synchronously: `nentries` arrays named
+ * names[i], node arrays ((nx+1)(ny+1)[(nz+1)] values) where on_nodes[i],
+ * else cell arrays; PointData first, then CellData, each in the given
+ * order.  Needs no GPU. */
+int hydro_vts_write_host(const char* path, int dim, const int* n, const double* lo,
+                         const double* hi, int nentries, const char* const* names,
+                         const int* on_nodes, const double* const* data);
+/* Scalar series: SessionPlainScalar (output.hpp:231-261) with the entries of
+ * hydro<Mesh> (hydro2d.hpp:825-905): time num_iters iter_diff_velocity,
+ * per phase mass/mass_in/mass_out, volume/volume_in/volume_out,
+ * pd_min/pd_max, centre and velocity components.  A row per write. */
+typedef struct hydro_scalar_output hydro_scalar_output;
+int hydro_scalar_output_open(hydro_ctx* ctx, const char* filename, hydro_scalar_output** out);
+int hydro_scalar_output_write(hydro_scalar_output* out, double time, int num_iters);
+int hydro_scalar_output_close(hydro_scalar_output* out);
 
 /* Solve sum_j a_j x_j + c = 0 for a symmetric 7-point (3D) / 5-point (2D)
  * stencil on an nx*ny*nz block, the rows the pressure system has

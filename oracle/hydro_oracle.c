@@ -1413,7 +1413,7 @@ int oracle_step(oracle_ctx* x, hydro_step_stats* st) {
   return HYDRO_OK;
 }
 
-/* hydro<Mesh>::CalcStat (hydro2d.hpp:1432-1467), plus sum q V. */
+/* hydro<Mesh>::CalcStat (hydro2d.hpp:1432-1493), plus sum q V. */
 int oracle_calc_stat(oracle_ctx* x, hydro_stat* out) {
   const Mesh* m = &x->m;
   memset(out, 0, sizeof(*out));
@@ -1444,6 +1444,30 @@ int oracle_calc_stat(oracle_ctx* x, hydro_stat* out) {
       out->center[i][k] = cen[k] / vol;
       out->velocity[i][k] = vel[k] / vol;
     }
+    /* boundary volume fluxes of the phase (hydro2d.hpp:1474-1493): flux
+     * towards the valid neighbour (+F on a low face, -F on a high face)
+     * times its volume fraction, split by sign */
+    double fin = 0., fout = 0.;
+    for (int d = 0; d < m->dim; ++d) {
+      long nn[3] = {m->n[0], m->n[1], m->n[2]};
+      for (long k = 0; k < nn[2]; ++k)
+        for (long j = 0; j < nn[1]; ++j)
+          for (long ii = 0; ii < nn[0]; ++ii) {
+            long mi[3] = {ii, j, k};
+            long c = ii + nn[0] * (j + nn[1] * k);
+            for (int side = 0; side < 2; ++side) {
+              if (side ? mi[d] != nn[d] - 1 : mi[d] != 0) continue;
+              long fm[3] = {ii, j, k};
+              if (side) fm[d] += 1;
+              double ftc = x->F[HYDRO_TIME_CURR][fidx(m, d, fm[0], fm[1], fm[2])];
+              if (side) ftc = -ftc;
+              if (ftc >= 0.) fin += ftc * x->alpha[i][c];
+              else fout -= ftc * x->alpha[i][c];
+            }
+          }
+    }
+    out->volume_flux_in[i] = fin;
+    out->volume_flux_out[i] = fout;
   }
   return HYDRO_OK;
 }

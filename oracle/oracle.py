@@ -56,6 +56,12 @@ def ref_lib():
         _ref.ref_run.restype = ctypes.c_int
         _ref.ref_smooth.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), D, ctypes.c_int]
         _ref.ref_smooth.restype = ctypes.c_int
+        C = ctypes.c_char_p
+        _ref.ref_write_vts.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), D, D,
+                                       ctypes.c_int, ctypes.POINTER(C), ctypes.POINTER(D),
+                                       ctypes.c_int, ctypes.POINTER(C), ctypes.POINTER(D), C,
+                                       ctypes.c_int, D]
+        _ref.ref_write_vts.restype = ctypes.c_int
     return _ref
 
 
@@ -207,6 +213,29 @@ def ref_run(desc, u0, q0, nsteps):
                    _dp(q), stats)
     _check(st, "ref_run")
     return u, p, F, q, [stats[i].as_dict() for i in range(nsteps)]
+
+
+def ref_write_vts(dim, n, lo, hi, node_fields, cell_fields, base, times):
+    """Frames written by the reference's own ParaView session
+    (output_paraview.hpp) for the given {name: array} node and cell entries;
+    one frame per entry of `times`, files <base>.<k>.vts and <base>.pvd."""
+    R = ref_lib()
+    C = ctypes.c_char_p
+
+    def pack(fields):
+        names = (C * max(1, len(fields)))(*[k.encode() for k in fields])
+        arrs = [np.ascontiguousarray(v, dtype=np.float64) for v in fields.values()]
+        ptrs = (ctypes.POINTER(ctypes.c_double) * max(1, len(arrs)))(*[_dp(a) for a in arrs])
+        return names, ptrs, arrs
+
+    nn, nptr, keep1 = pack(node_fields)
+    cn, cptr, keep2 = pack(cell_fields)
+    t = np.ascontiguousarray(times, dtype=np.float64)
+    _check(R.ref_write_vts(dim, (ctypes.c_int * 3)(*n), _dp(np.asarray(lo, dtype=np.float64)),
+                           _dp(np.asarray(hi, dtype=np.float64)), len(node_fields), nn, nptr,
+                           len(cell_fields), cn, cptr, base.encode(), len(t), _dp(t)),
+           "ref_write_vts")
+    del keep1, keep2
 
 
 def ref_smooth(dim, n, field, repeat):

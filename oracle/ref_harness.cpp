@@ -21,6 +21,18 @@
 #include "fluid.hpp"
 #include "advection.hpp"
 
+// The ParaView session names its files with an integer-to-text helper from
+// the reference's common library (not part of these headers); the harness
+// supplies one (decimal, as an ostream prints it).
+#include <sstream>
+#include <string>
+static std::string IntToStr(size_t a) {
+  std::ostringstream s;
+  s << a;
+  return s.str();
+}
+#include "output_paraview.hpp"
+
 #include "../include/hydro_gpu.h"
 
 namespace {
@@ -338,4 +350,57 @@ extern "C" int ref_smooth(int dim, const int* n, double* field, int repeat) {
   fc = solver::GetSmoothField(fc, m, repeat);
   for (size_t c = 0; c < m.GetNumCells(); ++c) field[c] = fc[geom::IdxCell(c)];
   return HYDRO_OK;
+}
+
+// Writes one frame with the reference's ParaView session
+// (output_paraview.hpp:34-175) for given node and cell arrays on a uniform
+// block (InitUniformMesh, mesh.hpp:723-736); the collection footer is
+// written when the session ends.  Golden output for the GPU library's
+// .vts/.pvd writer.
+namespace {
+template <class Mesh>
+int write_vts(const int* n, const double* lo, const double* hi, int nnode, const char** nnames,
+              const double** ndata, int ncell, const char** cnames, const double** cdata,
+              const char* base, int nframes, const double* times) {
+  using MIdx = typename Mesh::MIdx;
+  using Vect = typename Mesh::Vect;
+  using IdxNode = geom::IdxNode;
+  using IdxCell = geom::IdxCell;
+  Mesh mesh;
+  MIdx size;
+  Vect a, b;
+  for (size_t k = 0; k < Mesh::dim; ++k) {
+    size[k] = n[k];
+    a[k] = lo[k];
+    b[k] = hi[k];
+  }
+  geom::InitUniformMesh(mesh, geom::Rect<Vect>(a, b), size);
+  output::Content content;
+  for (int i = 0; i < nnode; ++i) {
+    const double* f = ndata[i];
+    content.push_back(std::make_shared<output::EntryFunction<double, IdxNode, Mesh>>(
+        nnames[i], mesh, [f](IdxNode idx) { return f[idx.GetRaw()]; }));
+  }
+  for (int i = 0; i < ncell; ++i) {
+    const double* f = cdata[i];
+    content.push_back(std::make_shared<output::EntryFunction<double, IdxCell, Mesh>>(
+        cnames[i], mesh, [f](IdxCell idx) { return f[idx.GetRaw()]; }));
+  }
+  {
+    output::SessionParaviewStructured<Mesh> session(content, "title", base, mesh);
+    for (int f = 0; f < nframes; ++f) session.Write(times[f], "");
+  }
+  return 0;
+}
+}  // namespace
+
+extern "C" int ref_write_vts(int dim, const int* n, const double* lo, const double* hi,
+                             int nnode, const char** nnames, const double** ndata, int ncell,
+                             const char** cnames, const double** cdata, const char* base,
+                             int nframes, const double* times) {
+  if (dim == 2)
+    return write_vts<geom::geom2d::MeshStructured<double>>(n, lo, hi, nnode, nnames, ndata, ncell,
+                                                           cnames, cdata, base, nframes, times);
+  return write_vts<geom::geom3d::MeshStructured<double>>(n, lo, hi, nnode, nnames, ndata, ncell,
+                                                         cnames, cdata, base, nframes, times);
 }

@@ -134,8 +134,55 @@ def make_sample():
     print("wrote", path)
 
 
+def make_vts():
+    """Frames of the reference's ParaView writer for seeded fields on small
+    2D and 3D blocks (values of mixed sign and magnitude), with the entry
+    set the defaults select; the inputs are stored beside the output."""
+    import tempfile
+    rng = np.random.default_rng(20261203)
+    for name, dim, n, lo, hi in (("vts2d", 2, (5, 3, 1), (0.0, -0.5, 0.0), (1.25, 0.7, 1.0)),
+                                 ("vts3d", 3, (3, 2, 4), (0.0, 0.0, 0.0), (1.0, 0.5, 2.0))):
+        nc = n[0] * n[1] * n[2]
+        nnode = (n[0] + 1) * (n[1] + 1) * ((n[2] + 1) if dim == 3 else 1)
+        hx = [(hi[k] - lo[k]) for k in range(3)]
+        nodes = {}
+        idx = np.arange(nnode)
+        ii = idx % (n[0] + 1)
+        jj = (idx // (n[0] + 1)) % (n[1] + 1)
+        kk = idx // ((n[0] + 1) * (n[1] + 1))
+        nodes["x"] = lo[0] + (ii / n[0]) * hx[0]
+        nodes["y"] = lo[1] + (jj / n[1]) * hx[1]
+        if dim == 3:
+            nodes["z"] = lo[2] + (kk / n[2]) * hx[2]
+        cells = {"velocity_x": rng.normal(size=nc) * 1e-3,
+                 "velocity_y": rng.normal(size=nc) * 10.0 ** rng.integers(-6, 3, size=nc)}
+        if dim == 3:
+            cells["velocity_z"] = rng.normal(size=nc)
+        cells["pressure"] = rng.uniform(-1, 1, size=nc) * 1234.5678
+        cells["volume_fraction_0"] = np.clip(rng.uniform(-0.2, 1.2, size=nc), 0, 1)
+        cells["volume_fraction_1"] = 1.0 - cells["volume_fraction_0"]
+        times = [0.0, 0.0125]
+        with tempfile.TemporaryDirectory() as td:
+            cwd = os.getcwd()
+            os.chdir(td)
+            try:
+                O.ref_write_vts(dim, n, lo, hi, nodes, cells, name + ".field", times)
+                frames = [open(name + ".field.%d.vts" % k).read() for k in range(len(times))]
+                pvd = open(name + ".field.pvd").read()
+            finally:
+                os.chdir(cwd)
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, dim=dim, n=np.array(n), lo=np.array(lo), hi=np.array(hi),
+                            node_names=np.array(list(nodes)), cell_names=np.array(list(cells)),
+                            times=np.array(times), frames=np.array(frames), pvd=pvd,
+                            **{"node_" + k: v for k, v in nodes.items()},
+                            **{"cell_" + k: v for k, v in cells.items()})
+        print("wrote", path)
+
+
 if __name__ == "__main__":
     if not O.ref_available():
         O.build(ref=True)
     make_cases()
+    make_vts()
     make_sample()
