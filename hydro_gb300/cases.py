@@ -229,3 +229,40 @@ def cavity_batch(ncases=512, seed=0, sizes=(64, 96, 128, 192, 256), dt=1e-3):
         d, u0, q0 = cavity(n=n, mu=1.0 / re, dt=dt, lid=1.0)
         out.append((d, u0, q0, re))
     return out
+
+
+def channel(nx=40, ny=20, nz=1, dim=2, length=2.0, u_in=1.0, mu=0.01, dt=1e-2, reverse=False,
+            two_phase=False):
+    """Channel flow: inlet on one x side with velocity (u_in, 0[, 0]) into
+    the domain, outlet on the other (rebalanced to the inflow), walls
+    elsewhere; starts at rest.  With two_phase, phase 1 (rho 2, mu 2 mu)
+    fills the inlet half of the channel below y = 0.5 and the inlet faces
+    inject it; phase 0 has rho 1."""
+    d = capi.default_desc()
+    d.dim = dim
+    n = (nx, ny, nz if dim == 3 else 1)
+    hi = (length, 1.0, 1.0)
+    for k in range(3):
+        d.n[k] = n[k]
+        d.lo[k], d.hi[k] = 0.0, hi[k]
+    inlet, outlet = (capi.XP, capi.XM) if reverse else (capi.XM, capi.XP)
+    d.bc_kind[inlet] = capi.BC_INLET
+    d.bc_kind[outlet] = capi.BC_OUTLET
+    d.bc_velocity[inlet][0] = -u_in if reverse else u_in
+    d.dt = dt
+    d.num_phases = 2 if two_phase else 1
+    d.density[0], d.viscosity[0] = 1.0, mu
+    d.density[1], d.viscosity[1] = 2.0, 2 * mu
+    d.advection_enable = 1 if two_phase else 0
+    d.gravity[0] = d.gravity[1] = d.gravity[2] = 0.0
+    _common(d)
+    nc = d.ncells
+    u0 = np.zeros(nc * dim)
+    if two_phase:
+        x, y = cell_centers(d)[:2]
+        near = (x > length / 2) if reverse else (x < length / 2)
+        alpha1 = (near & (y < 0.5)).astype(float)
+        q0 = two_phase_q(d, alpha1, 0)
+    else:
+        q0 = np.ones(nc) * d.density[0]
+    return d, u0, q0

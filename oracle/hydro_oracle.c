@@ -50,6 +50,11 @@ struct oracle_ctx {
   double* alpha[HYDRO_MAX_PHASES];
   /* last pressure correction and momentum diagonal */
   double *pcorr, *Dc;
+  /* boundary conditions per face (entries of boundary faces are used):
+   * velocity of the value condition per component (walls and inlets fixed,
+   * outlets refreshed every iteration), partial density of inlet faces */
+  double* bcu[3];
+  double* qin[HYDRO_MAX_PHASES];
   /* scratch */
   double* fw[10];   /* face arrays */
   double* cw[24];   /* cell arrays */
@@ -130,7 +135,7 @@ static int slot_q(int dim, int q) {
 
 /* ------------------------------------------------------ interpolation -- */
 
-enum { BC_VALUE = 0, BC_ZERODER = 1, BC_EXTRAP = 2, BC_NONE = 3 };
+enum { BC_VALUE = 0, BC_ZERODER = 1, BC_EXTRAP = 2, BC_NONE = 3, BC_FACE = 4 };
 
 /* Interpolate (solver.hpp:392-470) of a scalar cell field to faces.
  * bc: BC_VALUE -> boundary face = bcval[side]; BC_ZERODER -> cell value
@@ -167,6 +172,8 @@ static void interp(const Mesh* m, const double* fc, double* ff, int bc,
     double dist = 0.5 * m->h[d];
     if (bc == BC_VALUE) {
       ff[f] = bcval[side];
+    } else if (bc == BC_FACE) {
+      ff[f] = bcval[f];
     } else if (bc == BC_ZERODER) {
       ff[f] = fc[cc] + 0. * (dist * factor);
     } else {
@@ -551,9 +558,9 @@ int oracle_create(const hydro_desc* desc, oracle_ctx** out) {
     return HYDRO_ERR_ARG;
   }
   for (int s = 0; s < 2 * desc->dim; ++s)
-    if (desc->bc_kind[s] != HYDRO_BC_WALL) {
+    if (desc->bc_kind[s] < HYDRO_BC_WALL || desc->bc_kind[s] > HYDRO_BC_OUTLET) {
       free(x);
-      return HYDRO_ERR_UNSUPPORTED;
+      return HYDRO_ERR_ARG;
     }
   const Mesh* m = &x->m;
   x->nph = desc->num_phases;
@@ -577,6 +584,19 @@ int oracle_create(const hydro_desc* desc, oracle_ctx** out) {
   }
   x->pcorr = alloc0(m->nc);
   x->Dc = alloc0(m->nc);
+  for (int k = 0; k < 3; ++k) x->bcu[k] = alloc0(m->nf);
+  for (int i = 0; i < HYDRO_MAX_PHASES; ++i) x->qin[i] = alloc0(m->nf);
+  /* value conditions of the velocity: wall and inlet velocities as given,
+   * outlets start at zero (OutletAuto, fluid.hpp:340-364) */
+  for (long f = 0; f < m->nf; ++f) {
+    int d;
+    long mi[3], cm, cp;
+    fdecode(m, f, &d, mi, &cm, &cp);
+    if (cm >= 0 && cp >= 0) continue;
+    int side = fside(m, d, mi);
+    for (int k = 0; k < desc->dim; ++k)
+      x->bcu[k][f] = desc->bc_kind[side] == HYDRO_BC_OUTLET ? 0. : desc->bc_velocity[side][k];
+  }
   for (int i = 0; i < 10; ++i) x->fw[i] = alloc0(m->nf);
   for (int i = 0; i < 24; ++i) x->cw[i] = alloc0(m->nc);
   x->rows = alloc0(m->nc * (2 * m->dim + 1));
@@ -599,6 +619,8 @@ int oracle_destroy(oracle_ctx* x) {
   free(x->Sv); free(x->Sm);
   for (int i = 0; i < HYDRO_MAX_PHASES; ++i) { free(x->q[i]); free(x->alpha[i]); }
   free(x->pcorr); free(x->Dc);
+  for (int k = 0; k < 3; ++k) free(x->bcu[k]);
+  for (int i = 0; i < HYDRO_MAX_PHASES; ++i) free(x->qin[i]);
   for (int i = 0; i < 10; ++i) free(x->fw[i]);
   for (int i = 0; i < 24; ++i) free(x->cw[i]);
   free(x->rows); free(x->rowc);
@@ -759,10 +781,18 @@ int oracle_init_state(oracle_ctx* x) {
   double* uf = x->fw[1];
   double* F = x->F[HYDRO_TIME_CURR];
   for (long f = 0; f < m->nf; ++f) F[f] = 0.;
+  /* inlet faces carry the initial partial density of their cell
+   * (hydro2d.hpp:566-582) */
+  for (long f = 0; f < m->nf; ++f) {
+    int d;
+    long mi[3], cm, cp;
+    fdecode(m, f, &d, mi, &cm, &cp);
+    if (cm >= 0 && cp >= 0) continue;
+    if (x->d.bc_kind[fside(m, d, mi)] != HYDRO_BC_INLET) continue;
+    for (int i = 0; i < x->nph; ++i) x->qin[i][f] = x->q[i][cm >= 0 ? cm : cp];
+  }
   for (int k = 0; k < dim; ++k) {
-    double bcv[6];
-    for (int s = 0; s < 6; ++s) bcv[s] = x->d.bc_velocity[s][k];
-    interp(m, x->u[HYDRO_TIME_CURR][k], uf, BC_VALUE, bcv, 0);
+    interp(m, x->u[HYDRO_TIME_CURR][k], uf, BC_FACE, x->bcu[k], 0);
     long f0 = m->fofs[k], f1 = f0 + m->fcnt[k];
     for (long f = f0; f < f1; ++f) F[f] = uf[f] * m->A[k];
   }
@@ -833,11 +863,9 @@ static void assemble_momentum(oracle_ctx* x, int n, const double* u_prev,
                               const double* src) {
   const Mesh* m = &x->m;
   int dim = m->dim, w = 2 * dim + 1;
-  double bcv[6];
-  for (int s = 0; s < 6; ++s) bcv[s] = x->d.bc_velocity[s][n];
   double* ff = x->fw[5];
   double* gc[3] = {x->cw[3], x->cw[4], x->cw[5]};
-  interp(m, u_prev, ff, BC_VALUE, bcv, 0);
+  interp(m, u_prev, ff, BC_FACE, x->bcu[n], 0);
   gradient(m, ff, gc);
   double co[3];
   bdf_coeffs(x->dt, x->d.time_second_order, co);
@@ -881,7 +909,7 @@ static void assemble_momentum(oracle_ctx* x, int n, const double* u_prev,
       } else {
         /* boundary: InterpolationBoundaryFaceNearestCell /
            DerivativeBoundaryFacePlain with a value condition */
-        double val = bcv[2 * d + side];
+        double val = x->bcu[n][fq];
         cconst += (val * Ff) * s;
         double factor = side ? 1. : -1.;  /* id 0 when cm is the valid cell */
         double al = 1. / (0.5 * m->h[d]) * factor;
@@ -942,6 +970,49 @@ static int linear_solve(oracle_ctx* x, int which, double* sol, int* iters) {
 }
 
 /* FluidSimple::MakeIteration (fluid.hpp:814-1158), SIMPLER off. */
+/* UpdateOutletBaseConditions (fluid.hpp:542-600): outlet faces take the
+ * velocity of their cell (the latest iterate), then a uniform normal
+ * correction makes the outlet volume flux equal to the inlet flux plus the
+ * volume sources; boundary faces in raw index order (std::map order). */
+static void update_outlets(oracle_ctx* x) {
+  const Mesh* m = &x->m;
+  const hydro_desc* d = &x->d;
+  int any = 0;
+  for (int s = 0; s < 2 * m->dim; ++s) any |= d->bc_kind[s] == HYDRO_BC_OUTLET;
+  if (!any) return;
+  double** uic = x->u[HYDRO_ITER_CURR];
+  double in = 0., out = 0., area = 0.;
+  for (long f = 0; f < m->nf; ++f) {
+    int dd;
+    long mi[3], cm, cp;
+    fdecode(m, f, &dd, mi, &cm, &cp);
+    if (cm >= 0 && cp >= 0) continue;
+    int kind = d->bc_kind[fside(m, dd, mi)];
+    int id = cm >= 0 ? 0 : 1;
+    long cc = id == 0 ? cm : cp;
+    if (kind == HYDRO_BC_OUTLET) {
+      double factor = id == 0 ? 1. : -1.;
+      for (int k = 0; k < m->dim; ++k) x->bcu[k][f] = uic[k][cc];
+      out += x->bcu[dd][f] * m->A[dd] * factor;
+      area += m->A[dd];
+    } else if (kind == HYDRO_BC_INLET) {
+      double factor = id == 0 ? -1. : 1.;
+      in += x->bcu[dd][f] * m->A[dd] * factor;
+    }
+  }
+  for (long c = 0; c < m->nc; ++c) in += x->Sv[c] * m->V;
+  double corr = (in - out) / area;
+  for (long f = 0; f < m->nf; ++f) {
+    int dd;
+    long mi[3], cm, cp;
+    fdecode(m, f, &dd, mi, &cm, &cp);
+    if (cm >= 0 && cp >= 0) continue;
+    if (d->bc_kind[fside(m, dd, mi)] != HYDRO_BC_OUTLET) continue;
+    double factor = cm >= 0 ? 1. : -1.;
+    x->bcu[dd][f] = x->bcu[dd][f] + corr * factor;
+  }
+}
+
 int oracle_make_iteration(oracle_ctx* x) {
   const Mesh* m = &x->m;
   const hydro_desc* d = &x->d;
@@ -955,6 +1026,7 @@ int oracle_make_iteration(oracle_ctx* x) {
   memcpy(pip, pic, sizeof(double) * nc);
   memcpy(x->F[HYDRO_ITER_PREV], x->F[HYDRO_ITER_CURR], sizeof(double) * nf);
   const double* Fp = x->F[HYDRO_ITER_PREV];
+  update_outlets(x);
 
   /* CalcExtForce (fluid.hpp:602-631) */
   double* ffext[3] = {x->fw[0], x->fw[1], x->fw[2]};
@@ -994,9 +1066,7 @@ int oracle_make_iteration(oracle_ctx* x) {
     double* ff = x->fw[9];
     double* gc[3] = {x->cw[16], x->cw[17], x->cw[18]};
     for (int n = 0; n < dim; ++n) {
-      double bcv[6];
-      for (int s = 0; s < 6; ++s) bcv[s] = d->bc_velocity[s][n];
-      interp(m, uic[n], ff, BC_VALUE, bcv, 0);
+      interp(m, uic[n], ff, BC_FACE, x->bcu[n], 0);
       gradient(m, ff, gc);
       /* gf = Interpolate(gc, zero derivative): evaluate per face on the fly */
       for (long c = 0; c < nc; ++c) {
@@ -1062,7 +1132,8 @@ int oracle_make_iteration(oracle_ctx* x) {
       int side = fside(m, dd, mi);
       double uf;
       if (cm >= 0 && cp >= 0) uf = uic[dd][cm] * (1. - 0.5) + uic[dd][cp] * 0.5;
-      else uf = d->bc_velocity[side][dd];
+      else uf = x->bcu[dd][f];
+      (void)side;
       double vfi = uf * m->A[dd];
       if (cm >= 0 && cp >= 0) {
         double gpf_ = gp[dd][cm] * (1. - 0.5) + gp[dd][cp] * 0.5;
@@ -1279,7 +1350,16 @@ static void advection_iteration(oracle_ctx* x) {
     double* cur = x->q[i];
     int nst = d->tvd_split ? dim : 1;
     for (int stage = 0; stage < nst; ++stage) {
+      /* advection conditions (hydro2d.hpp:566-582): inlet faces hold the
+       * inlet value, the others zero derivative */
       interp(m, cur, ff, BC_ZERODER, NULL, 0);
+      for (long f = 0; f < m->nf; ++f) {
+        int dd;
+        long mi[3], P, E;
+        fdecode(m, f, &dd, mi, &P, &E);
+        if (P >= 0 && E >= 0) continue;
+        if (d->bc_kind[fside(m, dd, mi)] == HYDRO_BC_INLET) ff[f] = x->qin[i][f];
+      }
       gradient(m, ff, gc);
       /* InterpolateSuperbee (solver.hpp:560-619) */
       for (long f = 0; f < m->nf; ++f) {
@@ -1297,6 +1377,8 @@ static void advection_iteration(oracle_ctx* x) {
           } else {
             qf[f] = 0.5 * (cur[P] + cur[E]);
           }
+        } else if (d->bc_kind[fside(m, dd, mi)] == HYDRO_BC_INLET) {
+          qf[f] = x->qin[i][f];
         } else {
           qf[f] = cur[P >= 0 ? P : E] + 0. * (0.5 * m->h[dd]);
         }

@@ -115,6 +115,9 @@ struct Case {
         if (d.bc_kind[s] == HYDRO_BC_INLET) {
           fluid_cond[f] = std::make_shared<solver::fluid_condition::InletFixed<Mesh>>(
               vel, mesh.GetValidNeighbourCellId(f));
+        } else if (d.bc_kind[s] == HYDRO_BC_OUTLET) {
+          fluid_cond[f] = std::make_shared<solver::fluid_condition::OutletAuto<Mesh>>(
+              mesh.GetValidNeighbourCellId(f));
         } else {
           fluid_cond[f] =
               std::make_shared<solver::fluid_condition::NoSlipWallFixed<Mesh>>(vel);

@@ -90,6 +90,24 @@ def golden_cases():
     d.guess_extrapolation, d.velocity_relaxation_factor = 0.5, 0.7
     out.append(("cavity2d_jacobi_extrap", d, u0, q0, 3, True))
 
+    # inlet / outlet (UpdateOutletBaseConditions, fluid.hpp:542-600)
+    d, u0, q0 = cases.channel(nx=24, ny=10, dt=1e-2)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    out.append(("channel2d", d, u0, q0, 3, True))
+
+    d, u0, q0 = cases.channel(nx=20, ny=8, dt=1e-2, reverse=True, two_phase=True)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    d.tvd_split = 1
+    out.append(("channel2d_reverse_two_phase", d, u0, q0, 3, True))
+
+    d, u0, q0 = cases.channel(nx=10, ny=6, nz=5, dim=3, dt=1e-2)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 2
+    d.pressure_fixed_cell = 7
+    out.append(("channel3d_pinned", d, u0, q0, 2, True))
+
     # reference defaults for the linear solvers: one LU sweep for velocity
     # (an approximate solve; CPU-only semantics), SOR pressure
     d, u0, q0 = cases.broken_dam(nx=16, ny=8, dt_auto=False, dt=2e-3, smooth_times=2)
