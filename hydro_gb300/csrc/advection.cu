@@ -23,18 +23,20 @@ __device__ __forceinline__ double superbee(double p, double q) {
 }
 
 // Superbee value on the inner face between P (low) and E (high) along an
-// axis of stride s; idP is P's index along that axis.
+// axis of stride s; idP is P's index along that axis.  bP / bE: values of
+// P's low / E's high face when those are boundary faces (the advection
+// condition: the inlet value, else the cell's own, zero derivative).
 __device__ __forceinline__ double superbee_face(const double* q, long long P, long long E,
                                                 long long s, int idP, int nd, double Ff,
-                                                double h, double inv_h) {
+                                                double h, double inv_h, double bP, double bE) {
   double qP = q[P], qE = q[E];
   if (Ff > 1e-8) {
-    double flo = idP > 0 ? avg(q[P - s], qP) : qP;
+    double flo = idP > 0 ? avg(q[P - s], qP) : bP;
     double gP = (avg(qP, qE) - flo) * inv_h;
     double dq = qE - qP;
     return qP + 0.5 * superbee(dq, -4. * (gP * (-0.5 * h)) - dq);
   } else if (Ff < -1e-8) {
-    double fhi = idP + 1 < nd - 1 ? avg(qE, q[E + s]) : qE;
+    double fhi = idP + 1 < nd - 1 ? avg(qE, q[E + s]) : bE;
     double gE = (fhi - avg(qP, qE)) * inv_h;
     double dq = qE - qP;
     return qE - 0.5 * superbee(dq, 4. * (gE * (0.5 * h)) - dq);
@@ -42,9 +44,12 @@ __device__ __forceinline__ double superbee_face(const double* q, long long P, lo
   return 0.5 * (qP + qE);
 }
 
+// inlet_mask: bit q set when side q (xm, xp, ym, ...) is an inlet; qin
+// holds the inlet values on those boundary faces.
 template <int DIM>
 __global__ void k_adv_faces(Mesh m, Geo g, int nph, int stage, int nstages, const double* F,
-                            CP<HYDRO_MAXPH> q, WP<HYDRO_MAXPH> qflux, int kch) {
+                            CP<HYDRO_MAXPH> q, int inlet_mask, CP<HYDRO_MAXPH> qin,
+                            WP<HYDRO_MAXPH> qflux, int kch) {
   CELL_LOOP_BEGIN(m, kch)
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
@@ -52,19 +57,27 @@ __global__ void k_adv_faces(Mesh m, Geo g, int nph, int stage, int nstages, cons
     long long s = cell_stride(m, d);
     int id = X.i[d], nd = m.n[d];
     long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+    long long fs = face_stride(m, d);
+    const bool in_lo = (inlet_mask >> (2 * d)) & 1, in_hi = (inlet_mask >> (2 * d + 1)) & 1;
     double Ff = F[f];
     for (int i = 0; i < nph; ++i) {
       double qf;
-      if (id > 0)
-        qf = superbee_face(q.a[i], X.c - s, X.c, s, id - 1, nd, Ff, g.h[d], g.inv_h[d]);
-      else
-        qf = q.a[i][X.c];
+      if (id > 0) {
+        // P = X.c - s: its low face is a boundary face when id == 1; the
+        // current cell E's high face when id == nd - 1
+        double bP = q.a[i][X.c - s], bE = q.a[i][X.c];
+        if (id == 1 && in_lo) bP = qin.a[i][f - fs];
+        if (id == nd - 1 && in_hi) bE = qin.a[i][f + fs];
+        qf = superbee_face(q.a[i], X.c - s, X.c, s, id - 1, nd, Ff, g.h[d], g.inv_h[d], bP, bE);
+      } else {
+        qf = in_lo ? qin.a[i][f] : q.a[i][X.c];
+      }
       qflux.a[i][f] = qf * Ff;
     }
     if (id == nd - 1) {
-      long long fh = f + face_stride(m, d);
+      long long fh = f + fs;
       double Fh = F[fh];
-      for (int i = 0; i < nph; ++i) qflux.a[i][fh] = q.a[i][X.c] * Fh;
+      for (int i = 0; i < nph; ++i) qflux.a[i][fh] = (in_hi ? qin.a[i][fh] : q.a[i][X.c]) * Fh;
     }
   }
   CELL_LOOP_END
@@ -145,13 +158,16 @@ __global__ void k_grad0(Mesh m, Geo g, const double* a, W3 G, int kch) {
 }  // namespace
 
 cudaError_t launch_adv_faces(const Mesh& m, int nph, int stage, int nstages, const double* F,
-                             CP<HYDRO_MAXPH> q, WP<HYDRO_MAXPH> qflux, cudaStream_t st) {
+                             CP<HYDRO_MAXPH> q, int inlet_mask, CP<HYDRO_MAXPH> qin,
+                             WP<HYDRO_MAXPH> qflux, cudaStream_t st) {
   Launch L = cell_launch(m);
   Geo g = make_geo(m);
   if (m.dim == 3)
-    k_adv_faces<3><<<L.grid, L.block, 0, st>>>(m, g, nph, stage, nstages, F, q, qflux, L.kch);
+    k_adv_faces<3><<<L.grid, L.block, 0, st>>>(m, g, nph, stage, nstages, F, q, inlet_mask, qin,
+                                               qflux, L.kch);
   else
-    k_adv_faces<2><<<L.grid, L.block, 0, st>>>(m, g, nph, stage, nstages, F, q, qflux, L.kch);
+    k_adv_faces<2><<<L.grid, L.block, 0, st>>>(m, g, nph, stage, nstages, F, q, inlet_mask, qin,
+                                               qflux, L.kch);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -148,6 +148,14 @@ struct hydro_ctx {
   }
   double *Dc = nullptr, *Fs = nullptr, *kf = nullptr, *pc = nullptr, *prhs = nullptr;
   double* gp = nullptr;  // FP64 cell pressure gradient of the iteration
+  // boundary conditions: per-face velocity of the value condition (dim face
+  // arrays; walls and inlets fixed, outlets refreshed every iteration), its
+  // FP32 mirror for the mixed path, inlet partial densities per phase
+  BcSpec bc{};
+  double* bcu = nullptr;
+  float* bcu32 = nullptr;
+  double* qin = nullptr;
+  int inlet_mask = 0, has_outlet = 0;
   // mixed path: FP32 shadows of the state and mixture fields read by the
   // FP32 SIMPLE-iteration kernels (refreshed at StartStep, the iterate by
   // the correction kernel) and their FP32 work arrays
@@ -201,6 +209,12 @@ struct hydro_ctx {
   P vec(double* base, int n, long long stride) {
     P r{};
     for (int k = 0; k < n; ++k) r.a[k] = base + (size_t)k * stride;
+    return r;
+  }
+  // FP32 component table over arrays of stride `stride`
+  FP<3> vf3f(float* base, long long stride) {
+    FP<3> r{};
+    for (int k = 0; k < dim; ++k) r.a[k] = base + (size_t)k * stride;
     return r;
   }
   // FP32 component tables over nc-strided arrays
@@ -624,7 +638,8 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
   if (desc->simpler) return HYDRO_ERR_UNSUPPORTED;
   if (desc->num_phases < 1 || desc->num_phases > HYDRO_MAX_PHASES) return HYDRO_ERR_ARG;
   for (int s = 0; s < 2 * desc->dim && s < 6; ++s)
-    if (desc->bc_kind[s] != HYDRO_BC_WALL) return HYDRO_ERR_UNSUPPORTED;
+    if (desc->bc_kind[s] < HYDRO_BC_WALL || desc->bc_kind[s] > HYDRO_BC_OUTLET)
+      return HYDRO_ERR_ARG;
   if (desc->velocity_omega <= 0. || desc->velocity_relaxation_factor <= 0.)
     return HYDRO_ERR_ARG;
   if (desc->pressure_solver == HYDRO_LINEAR_MGCG && desc->precision != HYDRO_MIXED)
@@ -696,6 +711,9 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
       s3.Dc = a.take<float>(nc);
     }
     x->gp = a.take<double>(nc * dim);
+    x->bcu = a.take<double>(nf * dim);
+    if (desc->precision == HYDRO_MIXED) x->bcu32 = a.take<float>(nf * dim);
+    x->qin = a.take<double>(nf * nph);
     x->Dc = a.take<double>(nc);
     x->Fs = a.take<double>(nf);
     x->kf = a.take<double>(nf);
@@ -763,6 +781,19 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
   x->pw.pin = desc->pressure_fixed_cell;
   x->pw.prof = &x->prof;
   if (mg_prepare(x->mg) != cudaSuccess) {
+    hydro_gpu_destroy(x);
+    return HYDRO_ERR_CUDA;
+  }
+  for (int q = 0; q < 6; ++q) {
+    const int kind = q < 2 * dim ? desc->bc_kind[q] : HYDRO_BC_WALL;
+    x->bc.kind[q] = kind;
+    for (int k = 0; k < 3; ++k) x->bc.vel[q][k] = k < dim ? desc->bc_velocity[q][k] : 0.;
+    if (kind == HYDRO_BC_INLET) x->inlet_mask |= 1 << q;
+    if (kind == HYDRO_BC_OUTLET) x->has_outlet = 1;
+  }
+  if (launch_bc_fill(m, x->bc, x->vec<W3>(x->bcu, dim, m.nf),
+                     x->bcu32 ? x->vf3f(x->bcu32, m.nf) : FP<3>{}, x->st) != cudaSuccess ||
+      cudaStreamSynchronize(x->st) != cudaSuccess) {
     hydro_gpu_destroy(x);
     return HYDRO_ERR_CUDA;
   }
@@ -901,7 +932,10 @@ int hydro_gpu_init_state(hydro_ctx* x) {
                      sizeof(double) * m.nc * x->dim, cudaMemcpyDeviceToDevice, x->st));
   CK(cudaMemsetAsync(x->p[HYDRO_TIME_CURR], 0, sizeof(double) * m.nc, x->st));
   CK(cudaMemsetAsync(x->p[HYDRO_TIME_PREV], 0, sizeof(double) * m.nc, x->st));
-  CK(launch_init_flux(m, x->fc, x->uc3(HYDRO_TIME_CURR), x->F[HYDRO_TIME_CURR], x->st));
+  CK(launch_qin_fill(m, x->bc, x->nph, x->vec<CP<HYDRO_MAXPH>>(x->q, x->nph, m.nc),
+                     x->vec<WP<HYDRO_MAXPH>>(x->qin, x->nph, m.nf), x->st));
+  CK(launch_init_flux(m, x->fc, x->uc3(HYDRO_TIME_CURR), x->vec<C3>(x->bcu, x->dim, m.nf),
+                      x->F[HYDRO_TIME_CURR], x->st));
   CK(cudaMemcpyAsync(x->F[HYDRO_TIME_PREV], x->F[HYDRO_TIME_CURR], sizeof(double) * m.nf,
                      cudaMemcpyDeviceToDevice, x->st));
   x->time = 0.;
@@ -957,6 +991,12 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
   const double* Fip = x->F[HYDRO_ITER_PREV];
   auto& s3 = x->s32;
   int rc;
+  // UpdateOutletBaseConditions (fluid.hpp:542-600) from the latest iterate
+  if (x->has_outlet)
+    CK(launch_outlet_update(m, x->bc, up, x->vec<W3>(x->bcu, dim, m.nf),
+                            x->bcu32 ? x->vf3f(x->bcu32, m.nf) : FP<3>{},
+                            x->fc.sources ? x->Sv : nullptr, x->pw.partials, x->pw.ds, x->st));
+  C3 bv64 = x->vec<C3>(x->bcu, dim, m.nf);
   if (x->mixed) {
     // FP32 assembly on the shadows
     std::swap(s3.F[HYDRO_ITER_CURR], s3.F[HYDRO_ITER_PREV]);
@@ -964,9 +1004,12 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
     using R3 = RT<float, 3>;
     using V3 = WT<float, 3>;
     R3 up32 = x->vf<R3>(s3.u[HYDRO_ITER_PREV], dim);
+    R3 bv32{};
+    for (int k = 0; k < dim; ++k) bv32.a[k] = x->bcu32 + (size_t)k * m.nf;
     R3 force32 = x->vf<R3>(s3.force, dim), fres32 = x->vf<R3>(s3.fres, dim);
     PK(x, HYDRO_PROF_VEL_GRAD,
-       launch_vel_grad<float>(m, x->fc, up32, x->vf<WT<float, 9>>(s3.G, dim * dim), x->st));
+       launch_vel_grad<float>(m, x->fc, up32, bv32, x->vf<WT<float, 9>>(s3.G, dim * dim),
+                              x->st));
     PK(x, HYDRO_PROF_FORCE,
        launch_force<float>(m, x->fc, up32, x->vf<RT<float, 9>>(s3.G, dim * dim), pip, s3.mu,
                            s3.rho, force32, x->vf<R3>(s3.stforce, dim), s3.Sv, s3.Sm,
@@ -982,20 +1025,21 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
                                   x->vf<R3>(s3.u[HYDRO_TIME_PREV], dim),
                                   x->vf<RT<float, 9>>(s3.G, dim * dim), s3.F[HYDRO_ITER_PREV],
                                   s3.rho, s3.mu, x->vf<R3>(s3.fo, dim), up,
-                                  x->uc3(HYDRO_TIME_CURR), x->uc3(HYDRO_TIME_PREV), coef32,
-                                  res32, s3.Dc, x->st));
+                                  x->uc3(HYDRO_TIME_CURR), x->uc3(HYDRO_TIME_PREV), bv32,
+                                  coef32, res32, s3.Dc, x->st));
     rc = solve_momentum(x);
     if (rc) return rc;
     x->cd_iter_count++;
     PK(x, HYDRO_PROF_RHIE_CHOW,
        launch_rhie_chow<float>(m, x->fc, up, x->vf<R3>(x->du32[x->du_cur], dim), pip,
-                               x->vec<C3>(x->gp, dim, m.nc), force32, fres32, s3.Dc, x->Fs,
-                               x->kf, nullptr, x->st));
+                               x->vec<C3>(x->gp, dim, m.nc), force32, fres32, s3.Dc, bv64,
+                               x->Fs, x->kf, nullptr, x->st));
   } else {
     C3 force = x->vec<C3>(x->force, dim, m.nc);
     C3 fres = x->vec<C3>(x->fres, dim, m.nc);
     PK(x, HYDRO_PROF_VEL_GRAD,
-       launch_vel_grad<double>(m, x->fc, up, x->vec<WP<9>>(x->G, dim * dim, m.nc), x->st));
+       launch_vel_grad<double>(m, x->fc, up, bv64, x->vec<WP<9>>(x->G, dim * dim, m.nc),
+                               x->st));
     PK(x, HYDRO_PROF_FORCE,
        launch_force<double>(m, x->fc, up, x->vec<CP<9>>(x->G, dim * dim, m.nc), pip, x->mu,
                             x->rho, force, x->vec<C3>(x->stforce, dim, m.nc), x->Sv, x->Sm,
@@ -1006,7 +1050,7 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
                                    x->uc3(HYDRO_TIME_PREV),
                                    x->vec<CP<9>>(x->G, dim * dim, m.nc), Fip, x->rho, x->mu,
                                    x->vec<C3>(x->fo, dim, m.nc), up, x->uc3(HYDRO_TIME_CURR),
-                                   x->uc3(HYDRO_TIME_PREV),
+                                   x->uc3(HYDRO_TIME_PREV), bv64,
                                    x->vec<WP<7>>(x->coef, 2 * dim + 1, m.nc),
                                    x->vec<W3>(x->res, dim, m.nc), x->Dc, x->st));
     rc = solve_momentum(x);
@@ -1015,7 +1059,7 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
     x->cd_iter_count++;
     PK(x, HYDRO_PROF_RHIE_CHOW,
        launch_rhie_chow<double>(m, x->fc, up, du, pip, x->vec<C3>(x->gp, dim, m.nc), force, fres,
-                                x->Dc, x->Fs, x->kf, nullptr, x->st));
+                                x->Dc, bv64, x->Fs, x->kf, nullptr, x->st));
   }
   PK(x, HYDRO_PROF_PRESSURE_RHS, launch_pressure_rhs(m, x->Fs, x->fc.sources ? x->Sv : nullptr, x->prhs, x->st));
   rc = solve_pressure(x);
@@ -1113,6 +1157,7 @@ int hydro_gpu_advection_substep(hydro_ctx* x) {
   for (int stage = 0; stage < nst; ++stage) {
     PK(x, HYDRO_PROF_ADV_FACES,
        launch_adv_faces(m, x->nph, stage, nst, F, x->vec<CP<HYDRO_MAXPH>>(x->q, x->nph, m.nc),
+                        x->inlet_mask, x->vec<CP<HYDRO_MAXPH>>(x->qin, x->nph, m.nf),
                         x->vec<WP<HYDRO_MAXPH>>(x->qflux, x->nph, m.nf), x->st));
     PK(x, HYDRO_PROF_ADV_UPDATE,
        launch_adv_update(m, x->nph, stage, nst, x->adv_dt,

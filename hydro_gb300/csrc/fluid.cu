@@ -81,18 +81,19 @@ __global__ void k_d2f(long long n, const double* in, float* out) {
 // G[n*DIM+m] = d u_n / d x_m at cells, faces carrying the velocity value
 // condition (Gradient(Interpolate(u_n, cond_n)), solver.hpp:392-470,658-677).
 template <int DIM, class T>
-__global__ void k_vel_grad(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, WT<T, 9> G,
-                           int kch) {
+__global__ void k_vel_grad(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T, 3> bv,
+                           WT<T, 9> G, int kch) {
   CELL_LOOP_BEGIN(m, kch)
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     long long s = cell_stride(m, d);
     int id = X.i[d], nd = m.n[d];
+    long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
 #pragma unroll
     for (int n = 0; n < DIM; ++n) {
       T uc = u.a[n][X.c];
-      T flo = id > 0 ? avg(u.a[n][X.c - s], uc) : fc.bcu[2 * d][n];
-      T fhi = id < nd - 1 ? avg(uc, u.a[n][X.c + s]) : fc.bcu[2 * d + 1][n];
+      T flo = id > 0 ? avg(u.a[n][X.c - s], uc) : bv.a[n][fl];
+      T fhi = id < nd - 1 ? avg(uc, u.a[n][X.c + s]) : bv.a[n][fl + face_stride(m, d)];
       G.a[n * DIM + d][X.c] = (fhi - flo) * g.inv_h[d];
     }
   }
@@ -184,8 +185,8 @@ __global__ void k_force(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T, 9
 template <int DIM, class T>
 __global__ void k_mom_assemble(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> up, RT<T, 3> utc,
                                RT<T, 3> utp, RT<T, 9> G, const T* F, const T* rho, const T* mu,
-                               RT<T, 3> fo, Unsteady64 us, WT<T, 7> coef, WT<T, 3> res, T* Dc,
-                               int kch) {
+                               RT<T, 3> fo, Unsteady64 us, RT<T, 3> bv, WT<T, 7> coef,
+                               WT<T, 3> res, T* Dc, int kch) {
   CELL_LOOP_BEGIN(m, kch)
   const T rhoc = rho[X.c], muc = mu[X.c];
   T aPc = T(0);  // convective and diffusive part of the diagonal
@@ -235,7 +236,7 @@ __global__ void k_mom_assemble(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> up,
         aq[2 * d + side] = T(0);
         const T w = Fo - dif;
 #pragma unroll
-        for (int n = 0; n < DIM; ++n) cst[n] += fc.bcu[2 * d + side][n] * w;
+        for (int n = 0; n < DIM; ++n) cst[n] += bv.a[n][f] * w;
       }
     }
   }
@@ -377,7 +378,7 @@ __global__ void k_f2d3(long long n, int dim, FP<3> in, W3 out) {
 template <int DIM, class T>
 __global__ void k_rhie_chow(Mesh m, Geo g64, GeoT<T> g, FluidCoef fc64, FluidCoefT<T> fc, C3 up,
                             RT<T, 3> du, const double* p, C3 gp, RT<T, 3> force, RT<T, 3> fres,
-                            const T* Dc, double* Fs, double* kf, float* kf32, int kch) {
+                            const T* Dc, C3 bv, double* Fs, double* kf, float* kf32, int kch) {
   CELL_LOOP_BEGIN(m, kch)
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
@@ -403,13 +404,13 @@ __global__ void k_rhie_chow(Mesh m, Geo g64, GeoT<T> g, FluidCoef fc64, FluidCoe
       kf[f] = (double)k;
       if (kf32) kf32[f] = (float)k;
     } else {
-      Fs[f] = fc64.bcu[2 * d][d] * A - mv;
+      Fs[f] = bv.a[d][f] * A - mv;
       kf[f] = 0.;
       if (kf32) kf32[f] = 0.f;
     }
     if (id == nd - 1) {
       long long fh = f + face_stride(m, d);
-      Fs[fh] = fc64.bcu[2 * d + 1][d] * A - mv;
+      Fs[fh] = bv.a[d][fh] * A - mv;
       kf[fh] = 0.;
       if (kf32) kf32[fh] = 0.f;
     }
@@ -682,7 +683,7 @@ __global__ void __launch_bounds__(NT) k_stat(Mesh m, Geo g, const double* q, con
 // Initial volume fluxes of the FluidSimple ctor (fluid.hpp:770-784):
 // F = u_f.S - meshvel.S with the velocity value condition on boundaries.
 template <int DIM>
-__global__ void k_init_flux(Mesh m, Geo g, FluidCoef fc, C3 u, double* F, int kch) {
+__global__ void k_init_flux(Mesh m, Geo g, FluidCoef fc, C3 u, C3 bv, double* F, int kch) {
   CELL_LOOP_BEGIN(m, kch)
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
@@ -690,8 +691,116 @@ __global__ void k_init_flux(Mesh m, Geo g, FluidCoef fc, C3 u, double* F, int kc
     long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
     double mv = fc.meshvel[d] * g.A[d];
     if (X.i[d] > 0) F[f] = avg(u.a[d][X.c - s], u.a[d][X.c]) * g.A[d] - mv;
-    else F[f] = fc.bcu[2 * d][d] * g.A[d] - mv;
-    if (X.i[d] == m.n[d] - 1) F[f + face_stride(m, d)] = fc.bcu[2 * d + 1][d] * g.A[d] - mv;
+    else F[f] = bv.a[d][f] * g.A[d] - mv;
+    if (X.i[d] == m.n[d] - 1)
+      F[f + face_stride(m, d)] = bv.a[d][f + face_stride(m, d)] * g.A[d] - mv;
+  }
+  CELL_LOOP_END
+}
+
+// ------------------------------------------------- boundary conditions --
+// Value conditions of the velocity on the boundary faces (fluid.hpp:695-731):
+// walls and inlets their given velocity, outlets zero until the first
+// rebalancing (OutletAuto, fluid.hpp:340-364).  Side kinds in `kind`.
+template <int DIM>
+__global__ void k_bc_fill(Mesh m, BcSpec sp, W3 bv, FP<3> bv32, int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      if (side ? X.i[d] != m.n[d] - 1 : X.i[d] != 0) continue;
+      long long fb = side ? f + face_stride(m, d) : f;
+      int q = 2 * d + side;
+      for (int k = 0; k < DIM; ++k) {
+        double v = sp.kind[q] == HYDRO_BC_OUTLET ? 0. : sp.vel[q][k];
+        bv.a[k][fb] = v;
+        if (bv32.a[0]) bv32.a[k][fb] = (float)v;
+      }
+    }
+  }
+  CELL_LOOP_END
+}
+
+// Inlet faces carry the partial densities of their cell at the start
+// (hydro2d.hpp:566-582).
+template <int DIM>
+__global__ void k_qin_fill(Mesh m, BcSpec sp, int nph, CP<HYDRO_MAXPH> q, WP<HYDRO_MAXPH> qin,
+                           int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      if (side ? X.i[d] != m.n[d] - 1 : X.i[d] != 0) continue;
+      if (sp.kind[2 * d + side] != HYDRO_BC_INLET) continue;
+      long long fb = side ? f + face_stride(m, d) : f;
+      for (int i = 0; i < nph; ++i) qin.a[i][fb] = q.a[i][X.c];
+    }
+  }
+  CELL_LOOP_END
+}
+
+// UpdateOutletBaseConditions (fluid.hpp:542-600), reduction part: outlet
+// faces take the velocity of their cell (the latest iterate u); sums of the
+// outlet volume flux (outward), the outlet area, the inlet volume flux
+// (inward) and the volume sources S_v V go to ds->red[RS_OUT_*].
+template <int DIM>
+__global__ void __launch_bounds__(NT) k_outlet_sums(Mesh m, Geo g, BcSpec sp, C3 u, W3 bv,
+                                                    const double* Sv, double* partials,
+                                                    DevScalars* ds, int kch) {
+  double sm[4] = {0., 0., 0., 0.};
+  CELL_LOOP_BEGIN(m, kch)
+  if (Sv) sm[3] += Sv[X.c] * g.V;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      if (side ? X.i[d] != m.n[d] - 1 : X.i[d] != 0) continue;
+      long long fb = side ? f + face_stride(m, d) : f;
+      int kind = sp.kind[2 * d + side];
+      // the cell is the face's first neighbour on the high side
+      if (kind == HYDRO_BC_OUTLET) {
+        for (int k = 0; k < DIM; ++k) bv.a[k][fb] = u.a[k][X.c];
+        sm[0] += bv.a[d][fb] * g.A[d] * (side ? 1. : -1.);
+        sm[1] += g.A[d];
+      } else if (kind == HYDRO_BC_INLET) {
+        sm[2] += bv.a[d][fb] * g.A[d] * (side ? -1. : 1.);
+      }
+    }
+  }
+  CELL_LOOP_END
+  __shared__ double o[4];
+  if (grid_reduce<RED_SUM, 4>(sm, partials, &ds->ticket[TK_OUTLET], o)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      ds->red[RS_OUT_FLUX] = o[0];
+      ds->red[RS_OUT_AREA] = o[1];
+      ds->red[RS_IN_FLUX] = o[2] + o[3];
+    }
+  }
+}
+
+// Correction part: outlet velocity += normal (in - out)/area (outward).
+template <int DIM>
+__global__ void k_outlet_set(Mesh m, BcSpec sp, W3 bv, FP<3> bv32, const DevScalars* ds,
+                             int kch) {
+  const double corr = (ds->red[RS_IN_FLUX] - ds->red[RS_OUT_FLUX]) / ds->red[RS_OUT_AREA];
+  CELL_LOOP_BEGIN(m, kch)
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      if (side ? X.i[d] != m.n[d] - 1 : X.i[d] != 0) continue;
+      if (sp.kind[2 * d + side] != HYDRO_BC_OUTLET) continue;
+      long long fb = side ? f + face_stride(m, d) : f;
+      bv.a[d][fb] = bv.a[d][fb] + corr * (side ? 1. : -1.);
+      if (bv32.a[0])
+        for (int k = 0; k < DIM; ++k) bv32.a[k][fb] = (float)bv.a[k][fb];
+    }
   }
   CELL_LOOP_END
 }
@@ -757,15 +866,40 @@ cudaError_t launch_start_step(const Mesh& m, double ge, W3 u_ic, C3 u_tc, C3 u_t
   return cudaGetLastError();
 }
 
-cudaError_t launch_init_flux(const Mesh& m, const FluidCoef& fc, C3 u, double* F,
+cudaError_t launch_init_flux(const Mesh& m, const FluidCoef& fc, C3 u, C3 bv, double* F,
                              cudaStream_t st) {
-  DISPATCH_DIM(m, k_init_flux, m, make_geo(m), fc, u, F);
+  DISPATCH_DIM(m, k_init_flux, m, make_geo(m), fc, u, bv, F);
+}
+
+cudaError_t launch_bc_fill(const Mesh& m, const BcSpec& sp, W3 bv, FP<3> bv32, cudaStream_t st) {
+  DISPATCH_DIM(m, k_bc_fill, m, sp, bv, bv32);
+}
+
+cudaError_t launch_qin_fill(const Mesh& m, const BcSpec& sp, int nph, CP<HYDRO_MAXPH> q,
+                            WP<HYDRO_MAXPH> qin, cudaStream_t st) {
+  DISPATCH_DIM(m, k_qin_fill, m, sp, nph, q, qin);
+}
+
+cudaError_t launch_outlet_update(const Mesh& m, const BcSpec& sp, C3 u, W3 bv, FP<3> bv32,
+                                 const double* Sv, double* partials, DevScalars* ds,
+                                 cudaStream_t st) {
+  Launch L = cell_launch(m);
+  Geo g = make_geo(m);
+  if (m.dim == 3) {
+    k_outlet_sums<3><<<L.grid, L.block, 0, st>>>(m, g, sp, u, bv, Sv, partials, ds, L.kch);
+    k_outlet_set<3><<<L.grid, L.block, 0, st>>>(m, sp, bv, bv32, ds, L.kch);
+  } else {
+    k_outlet_sums<2><<<L.grid, L.block, 0, st>>>(m, g, sp, u, bv, Sv, partials, ds, L.kch);
+    k_outlet_set<2><<<L.grid, L.block, 0, st>>>(m, sp, bv, bv32, ds, L.kch);
+  }
+  count_launches(2);
+  return cudaGetLastError();
 }
 
 template <class T>
-cudaError_t launch_vel_grad(const Mesh& m, const FluidCoef& fc, RT<T, 3> u, WT<T, 9> G,
-                            cudaStream_t st) {
-  DISPATCH_DIM_T(m, k_vel_grad, T, m, make_geo<T>(m), coef_as<T>(fc), u, G);
+cudaError_t launch_vel_grad(const Mesh& m, const FluidCoef& fc, RT<T, 3> u, RT<T, 3> bv,
+                            WT<T, 9> G, cudaStream_t st) {
+  DISPATCH_DIM_T(m, k_vel_grad, T, m, make_geo<T>(m), coef_as<T>(fc), u, bv, G);
 }
 
 template <class T>
@@ -781,7 +915,8 @@ template <class T>
 cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, RT<T, 3> u_prev,
                                 RT<T, 3> u_tc, RT<T, 3> u_tp, RT<T, 9> G, const T* F,
                                 const T* rho, const T* mu, RT<T, 3> fo, C3 up64, C3 utc64,
-                                C3 utp64, WT<T, 7> coef, WT<T, 3> res, T* Dc, cudaStream_t st) {
+                                C3 utp64, RT<T, 3> bv, WT<T, 7> coef, WT<T, 3> res, T* Dc,
+                                cudaStream_t st) {
   Unsteady64 us;
   for (int k = 0; k < 3; ++k) {
     us.co[k] = fc.co[k];
@@ -790,21 +925,21 @@ cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, RT<T, 3> u_p
     us.utp[k] = utp64.a[k];
   }
   DISPATCH_DIM_T(m, k_mom_assemble, T, m, make_geo<T>(m), coef_as<T>(fc), u_prev, u_tc, u_tp,
-                 G, F, rho, mu, fo, us, coef, res, Dc);
+                 G, F, rho, mu, fo, us, bv, coef, res, Dc);
 }
 
 template <class T>
 cudaError_t launch_rhie_chow(const Mesh& m, const FluidCoef& fc, C3 u_prev, RT<T, 3> du,
                              const double* p, C3 gp, RT<T, 3> force, RT<T, 3> fres,
-                             const T* Dc, double* Fs, double* kf, float* kf32,
+                             const T* Dc, C3 bv, double* Fs, double* kf, float* kf32,
                              cudaStream_t st) {
   DISPATCH_DIM_T(m, k_rhie_chow, T, m, make_geo(m), make_geo<T>(m), fc, coef_as<T>(fc), u_prev,
-                 du, p, gp, force, fres, Dc, Fs, kf, kf32);
+                 du, p, gp, force, fres, Dc, bv, Fs, kf, kf32);
 }
 
 #define HG_INST_FLUID(T)                                                                      \
-  template cudaError_t launch_vel_grad<T>(const Mesh&, const FluidCoef&, RT<T, 3>, WT<T, 9>,  \
-                                          cudaStream_t);                                      \
+  template cudaError_t launch_vel_grad<T>(const Mesh&, const FluidCoef&, RT<T, 3>, RT<T, 3>,  \
+                                          WT<T, 9>, cudaStream_t);                            \
   template cudaError_t launch_force<T>(const Mesh&, const FluidCoef&, RT<T, 3>, RT<T, 9>,     \
                                        const double*, const T*, const T*, RT<T, 3>, RT<T, 3>, \
                                        const T*, const T*, WT<T, 3>, WT<T, 3>, W3,            \
@@ -812,10 +947,10 @@ cudaError_t launch_rhie_chow(const Mesh& m, const FluidCoef& fc, C3 u_prev, RT<T
   template cudaError_t launch_mom_assemble<T>(const Mesh&, const FluidCoef&, RT<T, 3>,        \
                                               RT<T, 3>, RT<T, 3>, RT<T, 9>, const T*,         \
                                               const T*, const T*, RT<T, 3>, C3, C3, C3,       \
-                                              WT<T, 7>, WT<T, 3>, T*, cudaStream_t);          \
+                                              RT<T, 3>, WT<T, 7>, WT<T, 3>, T*, cudaStream_t);\
   template cudaError_t launch_rhie_chow<T>(const Mesh&, const FluidCoef&, C3, RT<T, 3>,       \
                                            const double*, C3, RT<T, 3>, RT<T, 3>, const T*,   \
-                                           double*, double*, float*, cudaStream_t);
+                                           C3, double*, double*, float*, cudaStream_t);
 HG_INST_FLUID(double)
 HG_INST_FLUID(float)
 #undef HG_INST_FLUID

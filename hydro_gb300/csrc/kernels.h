@@ -45,6 +45,13 @@ struct FluidCoefT {
 };
 using FluidCoef = FluidCoefT<double>;
 
+// Boundary-condition kinds and given velocities per side (xm, xp, ym, yp,
+// zm, zp).
+struct BcSpec {
+  int kind[6];
+  double vel[6][3];
+};
+
 // Device scalars shared by reductions and convergence flags.
 struct DevScalars {
   double red[32];        // reduced values (see enum below)
@@ -64,7 +71,8 @@ enum {
   RS_XMEAN = 14,
   RS_INNER_TOL = 15,     // tolerance of the next inner solve (device-driven refinement)
   RS_P_RES = 16,         // relative pressure residual of the last solve
-  RS_IR_FF = 17          // refinement: ||f||^2 of the first residual
+  RS_IR_FF = 17,         // refinement: ||f||^2 of the first residual
+  RS_OUT_FLUX = 18, RS_OUT_AREA = 19, RS_IN_FLUX = 20  // outlet rebalancing sums
 };
 enum {
   FL_MOM_DONE = 0, FL_MOM_SWEEPS = 1, FL_PCG_DONE = 2, FL_PCG_ITERS = 3, FL_NAN = 4,
@@ -80,7 +88,8 @@ enum {
 enum {
   TK_MOM = 0, TK_PCG_A = 1, TK_PCG_B = 2, TK_PCG_INIT = 3, TK_IND = 4, TK_DT = 5,
   TK_MEAN = 6, TK_MEAN2 = 7, TK_STAT = 8, TK_STAT2 = 9, TK_STAT3 = 10, TK_IR = 11,
-  TK_NAN = 12, TK_PCG_INIT2 = 13, TK_F32_A = 14, TK_F32_B = 15, TK_F32_INIT = 16
+  TK_NAN = 12, TK_PCG_INIT2 = 13, TK_F32_A = 14, TK_F32_B = 15, TK_F32_INIT = 16,
+  TK_OUTLET = 17
 };
 
 // ---------------------------------------------------------------- fluid --
@@ -88,13 +97,22 @@ cudaError_t launch_start_step(const Mesh& m, double ge, W3 u_ic, C3 u_tc, C3 u_t
                               double* p_ic, const double* p_tc, const double* p_tp,
                               double* F_ic, const double* F_tc, const double* F_tp,
                               cudaStream_t st);
-cudaError_t launch_init_flux(const Mesh& m, const FluidCoef& fc, C3 u, double* F,
+// bv: per-face value conditions of the velocity (boundary entries used)
+cudaError_t launch_init_flux(const Mesh& m, const FluidCoef& fc, C3 u, C3 bv, double* F,
                              cudaStream_t st);
+cudaError_t launch_bc_fill(const Mesh& m, const BcSpec& sp, W3 bv, FP<3> bv32, cudaStream_t st);
+cudaError_t launch_qin_fill(const Mesh& m, const BcSpec& sp, int nph, CP<HYDRO_MAXPH> q,
+                            WP<HYDRO_MAXPH> qin, cudaStream_t st);
+// UpdateOutletBaseConditions: outlet faces from the latest iterate u, then
+// the uniform normal correction (bv32, when set, mirrors bv in FP32).
+cudaError_t launch_outlet_update(const Mesh& m, const BcSpec& sp, C3 u, W3 bv, FP<3> bv32,
+                                 const double* Sv, double* partials, DevScalars* ds,
+                                 cudaStream_t st);
 // The SIMPLE-iteration kernels, templated on the arithmetic type: double
 // for the FP64 path, float for the mixed path (FP32 shadows of the state).
 template <class T>
-cudaError_t launch_vel_grad(const Mesh& m, const FluidCoef& fc, RT<T, 3> u, WT<T, 9> G,
-                            cudaStream_t st);
+cudaError_t launch_vel_grad(const Mesh& m, const FluidCoef& fc, RT<T, 3> u, RT<T, 3> bv,
+                            WT<T, 9> G, cudaStream_t st);
 template <class T>
 cudaError_t launch_force(const Mesh& m, const FluidCoef& fc, RT<T, 3> u, RT<T, 9> G,
                          const double* p, const T* mu, const T* rho, RT<T, 3> force,
@@ -106,12 +124,13 @@ template <class T>
 cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, RT<T, 3> u_prev,
                                 RT<T, 3> u_tc, RT<T, 3> u_tp, RT<T, 9> G, const T* F,
                                 const T* rho, const T* mu, RT<T, 3> fo, C3 up64, C3 utc64,
-                                C3 utp64, WT<T, 7> coef, WT<T, 3> res, T* Dc, cudaStream_t st);
+                                C3 utp64, RT<T, 3> bv, WT<T, 7> coef, WT<T, 3> res, T* Dc,
+                                cudaStream_t st);
 // u_prev, p, gp (cell pressure gradient from launch_force) are FP64
 template <class T>
 cudaError_t launch_rhie_chow(const Mesh& m, const FluidCoef& fc, C3 u_prev, RT<T, 3> du,
                              const double* p, C3 gp, RT<T, 3> force, RT<T, 3> fres,
-                             const T* Dc, double* Fs, double* kf, float* kf32,
+                             const T* Dc, C3 bv, double* Fs, double* kf, float* kf32,
                              cudaStream_t st);
 cudaError_t launch_d2f(long long n, const double* in, float* out, cudaStream_t st);
 // Mixed path: FP32 Jacobi sweep on the o32 output of the assembly
@@ -157,8 +176,11 @@ cudaError_t launch_stat(const Mesh& m, const double* q, const double* alpha, C3 
 // ------------------------------------------------------------ advection --
 // Face fluxes q_f F_f of every phase (Superbee, solver.hpp:550-619) on the
 // faces of direction `stage` (all directions when nstages == 1).
+// inlet_mask: bit q set when side q is an inlet; qin: inlet values on
+// those boundary faces, per phase
 cudaError_t launch_adv_faces(const Mesh& m, int nph, int stage, int nstages, const double* F,
-                             CP<HYDRO_MAXPH> q, WP<HYDRO_MAXPH> qflux, cudaStream_t st);
+                             CP<HYDRO_MAXPH> q, int inlet_mask, CP<HYDRO_MAXPH> qin,
+                             WP<HYDRO_MAXPH> qflux, cudaStream_t st);
 cudaError_t launch_adv_update(const Mesh& m, int nph, int stage, int nstages, double dt,
                               CP<HYDRO_MAXPH> qflux, CP<HYDRO_MAXPH> qin,
                               WP<HYDRO_MAXPH> qout, cudaStream_t st);

@@ -214,3 +214,62 @@ def test_gpu_matches_reference_golden(built, name):
     errs = compare(out, g)
     assert all(v <= 1e-9 for v in errs.values()), errs
     assert [s["outer_iterations"] for s in out["stats"]] == list(g["outer_iterations"])
+
+
+def test_channel_inlet_outlet_vs_oracle(built):
+    """Inlet / outlet (outlet rebalanced every iteration, two phases with
+    an inflow of phase 1, split advection): GPU against the oracle, and the
+    boundary volume fluxes of CalcStat: inflow of the mixture equals the
+    rebalanced outflow."""
+    from hydro_gb300.solver import Hydro
+    from oracle.oracle import Oracle
+    d, u0, q0 = cases.channel(nx=24, ny=12, dt=1e-2, two_phase=True)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    d.tvd_split = 1
+    a = run(Hydro(d), u0, q0, 3)
+    b = run(Oracle(d), u0, q0, 3)
+    errs = compare(a, b)
+    assert all(v <= 1e-10 for v in errs.values()), errs
+    h = Hydro(d)
+    run(h, u0, q0, 2)
+    o = Oracle(d)
+    run(o, u0, q0, 2)
+    sg, so = h.calc_stat(), o.calc_stat()
+    for i in range(2):
+        for k in ("volume_flux_in", "volume_flux_out", "volume"):
+            assert getattr(sg, k)[i] == pytest.approx(getattr(so, k)[i], rel=1e-10, abs=1e-14), k
+    vin = sg.volume_flux_in[0] + sg.volume_flux_in[1]
+    vout = sg.volume_flux_out[0] + sg.volume_flux_out[1]
+    assert vin == pytest.approx(1.0, rel=1e-12)   # u_in 1 through a unit-height inlet
+    assert vout == pytest.approx(vin, rel=1e-9)
+
+
+def test_channel_mixed_and_graph(built):
+    """The outlet rebalancing inside the mixed path (FP32 mirror of the
+    conditions) and inside the graph-captured step."""
+    from hydro_gb300.solver import Hydro
+    d, u0, q0 = cases.channel(nx=16, ny=8, nz=8, dim=3, dt=1e-2, reverse=True)
+    d.pressure_tolerance, d.velocity_tolerance = 1e-10, 1e-12
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    a = run(Hydro(d), u0, q0, 3)
+    dm = d.copy()
+    dm.precision = capi.MIXED
+    dm.pressure_solver = capi.LINEAR_MGCG
+    b = run(Hydro(dm), u0, q0, 3)
+    errs = compare(b, a)
+    # velocity and fluxes within the mixed bar; the pressure of a channel
+    # started from rest carries the FP32 rounding of the assembled momentum
+    # fluxes relative to its own (smaller) scale: measured 1.6e-6
+    assert errs["u"] <= 1e-6 and errs["F"] <= 1e-6 and errs["q"] <= 1e-6, errs
+    assert errs["p"] <= 5e-6, errs
+    h = Hydro(dm)
+    h.set_field(capi.F_VELOCITY, u0)
+    h.set_field(capi.F_PARTIAL_DENSITY, q0)
+    h.init_state()
+    for _ in range(3):
+        h.step_graph()
+    c = {"u": h.get_field(capi.F_VELOCITY), "p": h.get_field(capi.F_PRESSURE),
+         "F": h.get_field(capi.F_VOLUME_FLUX), "q": h.get_field(capi.F_PARTIAL_DENSITY)}
+    errs = compare(c, b)
+    assert all(v <= 1e-12 for v in errs.values()), errs
