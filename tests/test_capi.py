@@ -70,8 +70,8 @@ def test_create_rejects_bad_desc(lib):
     d.simpler = 1
     assert lib.hydro_gpu_create(ctypes.byref(d), ctypes.byref(ctx)) == capi.ERR_UNSUPPORTED
     d = capi.default_desc()
-    d.bc_kind[capi.XP] = capi.BC_OUTLET
-    assert lib.hydro_gpu_create(ctypes.byref(d), ctypes.byref(ctx)) == capi.ERR_UNSUPPORTED
+    d.bc_kind[capi.XP] = 7  # not a boundary kind
+    assert lib.hydro_gpu_create(ctypes.byref(d), ctypes.byref(ctx)) == capi.ERR_ARG
     d = capi.default_desc()
     d.num_phases = 9
     assert lib.hydro_gpu_create(ctypes.byref(d), ctypes.byref(ctx)) == capi.ERR_ARG
