@@ -489,13 +489,16 @@ int solve_pressure_graph(hydro_ctx* x, int singular, int mixed) {
   return HYDRO_OK;
 }
 
-int solve_pressure(hydro_ctx* x) {
+// apply_pin = false: x->prhs is already the complete right-hand side (its
+// pinned row included), as for the SIMPLER solve.
+int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
   const hydro_desc& d = x->d;
   const Mesh& m = x->m;
   int singular = (d.pressure_fixed_cell < 0);
   PcgWork& w = x->pw;
   w.pin = d.pressure_fixed_cell;
-  if (w.pin >= 0) CK(pin_rhs(m, x->kf, x->prhs, w.pin, d.pressure_fixed_value, x->st));
+  if (w.pin >= 0 && apply_pin)
+    CK(pin_rhs(m, x->kf, x->prhs, w.pin, d.pressure_fixed_value, x->st));
   int mixed = (d.precision == HYDRO_MIXED);
   CK(pcg_prepare(m, x->kf, 0., w, mixed, x->st));
   if (x->graph_mode) return solve_pressure_graph(x, singular, mixed);
@@ -635,7 +638,9 @@ int hydro_desc_default(hydro_desc* d) {
 int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
   if (!desc || !out) return HYDRO_ERR_ARG;
   *out = nullptr;
-  if (desc->simpler) return HYDRO_ERR_UNSUPPORTED;
+  // SIMPLER is built on the FP64 path (its equations are the FP64 rows)
+  if (desc->simpler && desc->precision != HYDRO_FP64) return HYDRO_ERR_UNSUPPORTED;
+  if (desc->simpler && desc->rhie_chow_factor == 0.) return HYDRO_ERR_ARG;
   if (desc->num_phases < 1 || desc->num_phases > HYDRO_MAX_PHASES) return HYDRO_ERR_ARG;
   for (int s = 0; s < 2 * desc->dim && s < 6; ++s)
     if (desc->bc_kind[s] < HYDRO_BC_WALL || desc->bc_kind[s] > HYDRO_BC_OUTLET)
@@ -981,6 +986,7 @@ int hydro_gpu_start_step(hydro_ctx* x) {
 int hydro_gpu_make_iteration(hydro_ctx* x) {
   if (!x) return HYDRO_ERR_ARG;
   const Mesh& m = x->m;
+  const hydro_desc& d = x->d;
   int dim = x->dim;
   // layer shift: iter_prev <- iter_curr (fluid.hpp:815-818, conv_diff.hpp:133)
   std::swap(x->p[HYDRO_ITER_CURR], x->p[HYDRO_ITER_PREV]);
@@ -1076,6 +1082,20 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
        launch_correct(m, x->fc, up, du, RT<float, 3>{}, nullptr, x->uw3(HYDRO_ITER_CURR), pip,
                       x->p[HYDRO_ITER_CURR], x->pc, x->Dc, x->Fs, x->kf, x->F[HYDRO_ITER_CURR],
                       FP<3>{}, nullptr, nullptr, x->pw.partials, x->pw.ds, x->st));
+  if (d.simpler) {
+    // SIMPLER pressure (fluid.hpp:1059-1155): a second solve with the same
+    // matrix, in delta form around the corrected pressure
+    const long long pin = d.pressure_fixed_cell;
+    CK(launch_simpler_rhs(m, x->fc, x->vec<CP<7>>(x->coef, 2 * dim + 1, m.nc),
+                          x->vec<C3>(x->res, dim, m.nc), x->uc3(HYDRO_ITER_CURR), up,
+                          x->vec<C3>(x->fres, dim, m.nc), x->vec<C3>(x->gp, dim, m.nc),
+                          x->vec<C3>(x->force, dim, m.nc), x->Dc, x->F[HYDRO_ITER_CURR], x->kf,
+                          x->pw.dg, x->p[HYDRO_ITER_CURR], pin, d.pressure_fixed_value,
+                          x->vec<W3>(x->fo, dim, m.nc), x->prhs, x->st));
+    rc = solve_pressure(x, false);
+    if (rc) return rc;
+    CK(launch_add(m.nc, x->p[HYDRO_ITER_CURR], x->pc, x->st));
+  }
   if (x->graph_mode) {
     // the SIMPLE loop's control kernel reads the indicator on the device
     x->iter_count++;

@@ -488,6 +488,76 @@ __global__ void __launch_bounds__(NT) k_correct(Mesh m, Geo g, FluidCoef fc, C3 
   }
 }
 
+// ------------------------------------------------------------- SIMPLER --
+// fluid.hpp:1059-1155, first part: the momentum equations of the iteration
+// (relaxed diagonal 1/iaP, off-diagonals, delta-form constants) evaluated
+// at the velocity change of the iteration, plus the restored force minus
+// the iteration's cell pressure gradient.
+template <int DIM>
+__global__ void k_simpler_eval(Mesh m, CP<7> coef, C3 res, C3 uic, C3 up, C3 fres, C3 gp, W3 ev,
+                               int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+  const double aPr = 1. / coef.a[0][X.c];
+#pragma unroll
+  for (int n = 0; n < DIM; ++n) {
+    double r = res.a[n][X.c] + aPr * (uic.a[n][X.c] - up.a[n][X.c]);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      long long s = cell_stride(m, d);
+      if (X.i[d] > 0) r += coef.a[1 + 2 * d][X.c] * (uic.a[n][X.c - s] - up.a[n][X.c - s]);
+      if (X.i[d] < m.n[d] - 1)
+        r += coef.a[2 + 2 * d][X.c] * (uic.a[n][X.c + s] - up.a[n][X.c + s]);
+    }
+    ev.a[n][X.c] = r + (fres.a[n][X.c] - gp.a[n][X.c]);
+  }
+  CELL_LOOP_END
+}
+
+// Second part: on inner faces r_f = (ev_f - f_f).S / D_f + (F_f - u_f.S) /
+// rhie_chow_factor, the constant of the pressure rows is -sum_f s_f r_f, and
+// the system is solved in delta form around the corrected pressure p:
+// A x = sum_f s_f r_f - A' p (A' without the pinned cell's coupling, whose
+// row becomes x = value - p).
+template <int DIM>
+__global__ void k_simpler_rhs(Mesh m, Geo g, FluidCoef fc, C3 ev, C3 force, const double* Dc,
+                              const double* Fic, C3 uic, const double* kf, const double* dg,
+                              const double* p, long long pin, double pin_value, double* f,
+                              int kch) {
+  CELL_LOOP_BEGIN(m, kch)
+  if (X.c == pin) {
+    f[X.c] = pin_value - p[X.c];
+    continue;
+  }
+  double sum = 0., ap = dg[X.c] * p[X.c];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long s = cell_stride(m, d);
+    long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      bool inner = side ? X.i[d] < m.n[d] - 1 : X.i[d] > 0;
+      if (!inner) continue;
+      long long nb = side ? X.c + s : X.c - s;
+      long long cm = side ? X.c : nb, cp = side ? nb : X.c;
+      long long fq = side ? fl + face_stride(m, d) : fl;
+      double e = avg(ev.a[d][cm], ev.a[d][cp]) - face_vec<DIM, double>(force, cm, cp, d, fc.geometric);
+      double Df = avg(Dc[cm], Dc[cp]);
+      double uf = avg(uic.a[d][cm], uic.a[d][cp]);
+      double r = e * g.A[d] / Df + (Fic[fq] - uf * g.A[d]) / fc.rc;
+      sum += side ? r : -r;
+      if (nb != pin) ap -= kf[fq] * p[nb];
+    }
+  }
+  f[X.c] = sum - ap;
+  CELL_LOOP_END
+}
+
+__global__ void k_add(long long n, double* a, const double* b) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    a[i] += b[i];
+}
+
 // --------------------------------------------------------- auto time step --
 // FluidSimple::GetAutoTimeStep (fluid.hpp:1191-1206): min over faces with
 // F != 0 of |V/F|, 1e10 when there is none.
@@ -991,6 +1061,34 @@ cudaError_t launch_correct(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du,
                            double* partials, DevScalars* ds, cudaStream_t st) {
   DISPATCH_DIM(m, k_correct, m, make_geo(m), fc, u_prev, du, du32, Dc32, u_ic, p_ip, p_ic, pc,
                Dc, Fs, kf, F_ic, u32, p32, F32, partials, ds);
+}
+
+cudaError_t launch_simpler_rhs(const Mesh& m, const FluidCoef& fc, CP<7> coef, C3 res, C3 uic,
+                               C3 up, C3 fres, C3 gp, C3 force, const double* Dc,
+                               const double* Fic, const double* kf, const double* dg,
+                               const double* p, long long pin, double pin_value, W3 ev,
+                               double* f, cudaStream_t st) {
+  Launch L = cell_launch(m);
+  Geo g = make_geo(m);
+  C3 evc{};
+  for (int k = 0; k < 3; ++k) evc.a[k] = ev.a[k];
+  if (m.dim == 3) {
+    k_simpler_eval<3><<<L.grid, L.block, 0, st>>>(m, coef, res, uic, up, fres, gp, ev, L.kch);
+    k_simpler_rhs<3><<<L.grid, L.block, 0, st>>>(m, g, fc, evc, force, Dc, Fic, uic, kf, dg, p,
+                                                 pin, pin_value, f, L.kch);
+  } else {
+    k_simpler_eval<2><<<L.grid, L.block, 0, st>>>(m, coef, res, uic, up, fres, gp, ev, L.kch);
+    k_simpler_rhs<2><<<L.grid, L.block, 0, st>>>(m, g, fc, evc, force, Dc, Fic, uic, kf, dg, p,
+                                                 pin, pin_value, f, L.kch);
+  }
+  count_launches(2);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_add(long long n, double* a, const double* b, cudaStream_t st) {
+  k_add<<<flat_blocks(n), NT, 0, st>>>(n, a, b);
+  count_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_auto_dt(const Mesh& m, const double* F, double* partials, DevScalars* ds,

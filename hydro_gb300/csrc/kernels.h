@@ -153,6 +153,14 @@ cudaError_t launch_correct(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du,
                            double* partials, DevScalars* ds, cudaStream_t st);
 cudaError_t launch_auto_dt(const Mesh& m, const double* F, double* partials, DevScalars* ds,
                            cudaStream_t st);
+// SIMPLER (FP64 path): right-hand side f of the delta-form pressure solve
+// A x = f around the corrected pressure p; ev: dim cell arrays of scratch.
+cudaError_t launch_simpler_rhs(const Mesh& m, const FluidCoef& fc, CP<7> coef, C3 res, C3 uic,
+                               C3 up, C3 fres, C3 gp, C3 force, const double* Dc,
+                               const double* Fic, const double* kf, const double* dg,
+                               const double* p, long long pin, double pin_value, W3 ev,
+                               double* f, cudaStream_t st);
+cudaError_t launch_add(long long n, double* a, const double* b, cudaStream_t st);
 cudaError_t launch_nan_count(long long n, const double* a, double* partials, DevScalars* ds,
                              cudaStream_t st);
 

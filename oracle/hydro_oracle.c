@@ -55,6 +55,9 @@ struct oracle_ctx {
    * outlets refreshed every iteration), partial density of inlet faces */
   double* bcu[3];
   double* qin[HYDRO_MAX_PHASES];
+  /* momentum rows of the iteration per component (kept for SIMPLER) */
+  double* mrows[3];
+  double* mrowc[3];
   /* scratch */
   double* fw[10];   /* face arrays */
   double* cw[24];   /* cell arrays */
@@ -549,7 +552,7 @@ static double* alloc0(long n) { return (double*)calloc((size_t)(n > 0 ? n : 1), 
 
 int oracle_create(const hydro_desc* desc, oracle_ctx** out) {
   if (!desc || !out) return HYDRO_ERR_ARG;
-  if (desc->simpler) return HYDRO_ERR_UNSUPPORTED;
+  if (desc->simpler && desc->rhie_chow_factor == 0.) return HYDRO_ERR_ARG;
   if (desc->num_phases < 1 || desc->num_phases > HYDRO_MAX_PHASES) return HYDRO_ERR_ARG;
   oracle_ctx* x = (oracle_ctx*)calloc(1, sizeof(oracle_ctx));
   x->d = *desc;
@@ -585,6 +588,10 @@ int oracle_create(const hydro_desc* desc, oracle_ctx** out) {
   x->pcorr = alloc0(m->nc);
   x->Dc = alloc0(m->nc);
   for (int k = 0; k < 3; ++k) x->bcu[k] = alloc0(m->nf);
+  for (int k = 0; k < 3; ++k) {
+    x->mrows[k] = alloc0(m->nc * (2 * m->dim + 1));
+    x->mrowc[k] = alloc0(m->nc);
+  }
   for (int i = 0; i < HYDRO_MAX_PHASES; ++i) x->qin[i] = alloc0(m->nf);
   /* value conditions of the velocity: wall and inlet velocities as given,
    * outlets start at zero (OutletAuto, fluid.hpp:340-364) */
@@ -620,6 +627,7 @@ int oracle_destroy(oracle_ctx* x) {
   for (int i = 0; i < HYDRO_MAX_PHASES; ++i) { free(x->q[i]); free(x->alpha[i]); }
   free(x->pcorr); free(x->Dc);
   for (int k = 0; k < 3; ++k) free(x->bcu[k]);
+  for (int k = 0; k < 3; ++k) { free(x->mrows[k]); free(x->mrowc[k]); }
   for (int i = 0; i < HYDRO_MAX_PHASES; ++i) free(x->qin[i]);
   for (int i = 0; i < 10; ++i) free(x->fw[i]);
   for (int i = 0; i < 24; ++i) free(x->cw[i]);
@@ -1108,6 +1116,8 @@ int oracle_make_iteration(oracle_ctx* x) {
     assemble_momentum(x, n, uip[n], x->u[HYDRO_TIME_CURR][n],
                       x->u[HYDRO_TIME_PREV][n], Fp, muf, fo[n]);
     for (long c = 0; c < nc; ++c) Dsum[c] += coeff_sum(m, x->rows, c);
+    memcpy(x->mrows[n], x->rows, sizeof(double) * nc * w);
+    memcpy(x->mrowc[n], x->rowc, sizeof(double) * nc);
     int it = 0;
     int st = linear_solve(x, 0, x->cw[20], &it);
     x->vel_sweeps += it;
@@ -1235,6 +1245,99 @@ int oracle_make_iteration(oracle_ctx* x) {
       v += pc[cp] * cf;
     }
     Fic[f] = v;
+  }
+
+  /* SIMPLER (fluid.hpp:1059-1155): the momentum equations evaluated at the
+   * correction of this iteration, plus restored force and minus the
+   * iteration's pressure gradient, give face terms whose divergence is the
+   * constant of the pressure system (same matrix); solved in delta form
+   * around the corrected pressure, which is then replaced. */
+  if (d->simpler) {
+    double* gp0[3] = {x->cw[16], x->cw[17], x->cw[18]};
+    interp(m, pip, pf, BC_EXTRAP, NULL, 0);
+    gradient(m, pf, gp0);
+    double* ev[3] = {x->cw[13], x->cw[14], x->cw[15]};
+    for (int n = 0; n < dim; ++n) {
+      for (long c = 0; c < nc; ++c) {
+        long mi[3];
+        cmidx(m, c, mi);
+        double r = x->mrowc[n][c];
+        for (int t = 0; t < w; ++t) {
+          long idx;
+          if (t == slot_c(dim)) idx = c;
+          else {
+            int q = t < dim ? 2 * (dim - 1 - t) : 2 * (t - dim - 1) + 1;
+            idx = cnb(m, mi, q);
+            if (idx < 0) continue;
+          }
+          r += (uic[n][idx] - uip[n][idx]) * x->mrows[n][c * w + t];
+        }
+        ev[n][c] = r + (fres[n][c] - gp0[n][c]);
+      }
+    }
+    /* face scratch: kf (fw[1]) and D_f (fw[9]) are still needed */
+    double* ffx[3] = {x->fw[3], x->fw[4], x->fw[6]};
+    double* fev[3] = {x->fw[0], x->fw[2], x->fw[5]};
+    double* fvel = x->fw[7];
+    double* rf = x->fw[8];
+    interp_vec(m, x->force, ffx, d->force_geometric_average);
+    for (int n = 0; n < dim; ++n) interp(m, ev[n], fev[n], BC_NONE, NULL, 0);
+    for (long f = 0; f < nf; ++f) rf[f] = 0.;
+    for (int n = 0; n < dim; ++n) {
+      interp(m, uic[n], fvel, BC_FACE, x->bcu[n], 0);
+      long f0 = m->fofs[n], f1 = f0 + m->fcnt[n];
+      for (long f = f0; f < f1; ++f) {
+        int dd;
+        long mi[3], cm, cp;
+        fdecode(m, f, &dd, mi, &cm, &cp);
+        if (cm < 0 || cp < 0) continue;
+        double e = fev[dd][f] - ffx[dd][f];
+        rf[f] = e * m->A[dd] / Df[f] + (Fic[f] - fvel[f] * m->A[dd]) / d->rhie_chow_factor;
+      }
+    }
+    for (long c = 0; c < nc; ++c) {
+      long mi[3];
+      cmidx(m, c, mi);
+      double sum = 0.;
+      for (int q = 0; q < 2 * dim; ++q) sum += rf[cface(m, mi, q)] * outward(q);
+      x->rowc[c] = -sum;
+    }
+    if (pin >= 0 && pin < nc) x->rowc[pin] = -d->pressure_fixed_value;
+    /* constant = equation evaluated at the corrected pressure */
+    for (long c = 0; c < nc; ++c) {
+      long mi[3];
+      cmidx(m, c, mi);
+      double r = x->rowc[c];
+      for (int t = 0; t < w; ++t) {
+        long idx;
+        if (t == slot_c(dim)) idx = c;
+        else {
+          int q = t < dim ? 2 * (dim - 1 - t) : 2 * (t - dim - 1) + 1;
+          idx = cnb(m, mi, q);
+          if (idx < 0) continue;
+        }
+        r += pic[idx] * x->rows[c * w + t];
+      }
+      x->cw[12][c] = r;
+    }
+    memcpy(x->rowc, x->cw[12], sizeof(double) * nc);
+    double* xs = x->cw[22];
+    it = 0;
+    if (d->pressure_solver == HYDRO_LINEAR_CG || d->pressure_solver == HYDRO_LINEAR_MGCG) {
+      double* f = x->cw[21];
+      for (long c = 0; c < nc; ++c) f[c] = -x->rowc[c];
+      double* wk[5] = {x->cw[0], x->cw[1], x->cw[2], x->cw[3], x->cw[4]};
+      double res = 0.;
+      st = pcg(m, kf, 0., pin, f, xs, 0, d->pressure_tolerance, d->pressure_iters_limit, wk,
+               &it, &res);
+      x->p_res = res;
+    } else {
+      for (long c = 0; c < nc; ++c) xs[c] = 0.;
+      st = linear_solve(x, 1, xs, &it);
+    }
+    x->p_iters += it;
+    if (st != HYDRO_OK && st != HYDRO_NOT_CONVERGED) return st;
+    for (long c = 0; c < nc; ++c) pic[c] += xs[c];
   }
   x->iter_count++;
   return HYDRO_OK;

@@ -152,7 +152,7 @@ struct Case {
         &fc_viscosity_smooth, &fc_force, &fc_stforce, &ff_stforce,
         &fc_volume_source, &fc_mass_source, 0., d.dt, *fv, *fp,
         d.convergence_tolerance, d.num_iterations_limit, &timer,
-        d.time_second_order != 0, false, d.force_geometric_average != 0,
+        d.time_second_order != 0, d.simpler != 0, d.force_geometric_average != 0,
         d.guess_extrapolation, V3(d.meshvel));
 
     // advection (hydro2d.hpp:483-600): zero-derivative walls, value inlets

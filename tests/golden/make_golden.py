@@ -108,6 +108,20 @@ def golden_cases():
     d.pressure_fixed_cell = 7
     out.append(("channel3d_pinned", d, u0, q0, 2, True))
 
+    # SIMPLER (fluid.hpp:1059-1155): singular walls, pinned two-phase
+    d, u0, q0 = cases.cavity(n=16, mu=0.01, dt=1e-2)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    d.simpler = 1
+    out.append(("cavity2d_simpler", d, u0, q0, 3, True))
+
+    d, u0, q0 = cases.broken_dam(nx=24, ny=12, dt_auto=False, dt=1e-3, smooth_times=2)
+    tight(d, p_tol=1e-10)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    d.simpler = 1
+    d.pressure_fixed_cell = 30
+    out.append(("dam2d_simpler_pinned", d, u0, q0, 2, True))
+
     # reference defaults for the linear solvers: one LU sweep for velocity
     # (an approximate solve; CPU-only semantics), SOR pressure
     d, u0, q0 = cases.broken_dam(nx=16, ny=8, dt_auto=False, dt=2e-3, smooth_times=2)

@@ -68,6 +68,7 @@ def test_create_rejects_bad_desc(lib):
     d = capi.default_desc()
     ctx = ctypes.c_void_p()
     d.simpler = 1
+    d.precision = capi.MIXED  # SIMPLER runs on the FP64 path only
     assert lib.hydro_gpu_create(ctypes.byref(d), ctypes.byref(ctx)) == capi.ERR_UNSUPPORTED
     d = capi.default_desc()
     d.bc_kind[capi.XP] = 7  # not a boundary kind

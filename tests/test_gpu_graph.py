@@ -98,3 +98,14 @@ def test_graph_step_multigrid_grid_levels(built):
     d.convergence_tolerance = 0.0
     d.num_iterations_limit = 2
     _check(d, u0, q0, 2)
+
+
+def test_graph_step_simpler_channel(built):
+    """SIMPLER's second pressure solve and the outlet rebalancing inside the
+    graph-captured loops."""
+    d, u0, q0 = cases.channel(nx=20, ny=10, dt=1e-2)
+    d.simpler = 1
+    d.pressure_fixed_cell = 3
+    d.convergence_tolerance = 1e-5
+    d.num_iterations_limit = 7
+    _check(d, u0, q0, 3)
