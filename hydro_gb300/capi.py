@@ -92,6 +92,7 @@ class HydroDesc(ctypes.Structure):
         ("tvd_split", ctypes.c_int),
         ("sharp", ctypes.c_double),
         ("stream", ctypes.c_void_p),
+        ("periodic", ctypes.c_int * 3),
     ]
 
     @property

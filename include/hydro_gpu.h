@@ -165,6 +165,12 @@ typedef struct hydro_desc {
   double sharp;
 
   void* stream;                 /* cudaStream_t to run on; NULL = library-owned stream */
+  /* periodic directions (mesh2d.hpp / mesh3d.hpp PERX, PERZ, compile-time
+   * switches in the reference, any direction here): both boundary faces of a
+   * periodic direction join its last and first cells, carry no condition
+   * and are solved as inner faces.  Multigrid needs an even cell count
+   * along a periodic direction to coarsen it. */
+  int periodic[3];
 } hydro_desc;
 
 typedef struct hydro_step_stats {

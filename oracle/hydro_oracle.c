@@ -32,6 +32,7 @@ typedef struct {
   long fofs[3], fcnt[3];
   double h[3], V, A[3];
   double lo[3];
+  int per[3]; /* periodic directions (mesh2d.hpp / mesh3d.hpp PERX, PERZ) */
 } Mesh;
 
 struct oracle_ctx {
@@ -98,12 +99,16 @@ static long cface(const Mesh* m, const long* mi, int q) {
   a[d] += s;
   return fidx(m, d, a[0], a[1], a[2]);
 }
-/* Neighbour cell across face q of cell mi, or -1. */
+/* Neighbour cell across face q of cell mi, or -1; across a periodic
+ * direction the last and first cells are neighbours (mesh3d.hpp:348-392). */
 static long cnb(const Mesh* m, const long* mi, int q) {
   int d = q / 2, s = q % 2;
   long a[3] = {mi[0], mi[1], mi[2]};
   a[d] += s ? 1 : -1;
-  if (a[d] < 0 || a[d] >= m->n[d]) return -1;
+  if (a[d] < 0 || a[d] >= m->n[d]) {
+    if (!m->per[d]) return -1;
+    a[d] = a[d] < 0 ? m->n[d] - 1 : 0;
+  }
   return cidx(m, a[0], a[1], a[2]);
 }
 /* Decode face f: direction, multi-index, neighbour cells cm (id 0) and cp (id 1). */
@@ -120,6 +125,14 @@ static void fdecode(const Mesh* m, long f, int* dir, long* mi, long* cm, long* c
   *cp = (a[d] < m->n[d]) ? cidx(m, a[0], a[1], a[2]) : -1;
   a[d] -= 1;
   *cm = (a[d] >= 0) ? cidx(m, a[0], a[1], a[2]) : -1;
+  if (m->per[d] && (*cm < 0 || *cp < 0)) {
+    /* both end faces of a periodic direction join cells n-1 and 0 */
+    long b[3] = {mi[0], mi[1], mi[2]};
+    b[d] = m->n[d] - 1;
+    *cm = cidx(m, b[0], b[1], b[2]);
+    b[d] = 0;
+    *cp = cidx(m, b[0], b[1], b[2]);
+  }
 }
 /* Side (enum hydro_side) of a boundary face, or -1 for an inner face. */
 static int fside(const Mesh* m, int d, const long* mi) {
@@ -560,6 +573,7 @@ int oracle_create(const hydro_desc* desc, oracle_ctx** out) {
     free(x);
     return HYDRO_ERR_ARG;
   }
+  for (int d = 0; d < desc->dim; ++d) x->m.per[d] = desc->periodic[d] != 0;
   for (int s = 0; s < 2 * desc->dim; ++s)
     if (desc->bc_kind[s] < HYDRO_BC_WALL || desc->bc_kind[s] > HYDRO_BC_OUTLET) {
       free(x);

@@ -46,8 +46,22 @@ def ref_available():
     return os.path.exists(REF_LIB)
 
 
-def ref_lib():
+_ref_variants = {}
+
+
+def ref_lib(variant=""):
+    """The reference harness; variant "perx" / "perxz" is the build with the
+    reference's compile-time periodicity switches PERX / PERX+PERZ."""
     global _ref
+    if variant:
+        if variant not in _ref_variants:
+            lib = ctypes.CDLL(REF_LIB.replace(".so", "_%s.so" % variant))
+            D = ctypes.POINTER(ctypes.c_double)
+            lib.ref_run.argtypes = [ctypes.POINTER(capi.HydroDesc), D, D, ctypes.c_int,
+                                    D, D, D, D, ctypes.POINTER(capi.StepStats)]
+            lib.ref_run.restype = ctypes.c_int
+            _ref_variants[variant] = lib
+        return _ref_variants[variant]
     if _ref is None:
         _ref = ctypes.CDLL(REF_LIB)
         D = ctypes.POINTER(ctypes.c_double)
@@ -197,8 +211,16 @@ def stencil_solve(dim, n, face_coeff, shift, pinned_cell, pinned_value, rhs, tol
 
 def ref_run(desc, u0, q0, nsteps):
     """Run the reference's own FluidSimple + AdvectionSolverMultiExplicit for
-    nsteps steps; returns (u, p, F, q, stats list)."""
-    R = ref_lib()
+    nsteps steps; returns (u, p, F, q, stats list).  Periodic directions x
+    (and z in 3D) select the harness built with PERX (PERZ)."""
+    per = tuple(bool(desc.periodic[k]) for k in range(3))
+    variants = {(False, False, False): "", (True, False, False): "perx",
+                (True, False, True): "perxz"}
+    if desc.dim == 2:
+        per = (per[0], per[1], False)
+    if per not in variants:
+        raise ValueError("the reference switches periodicity on x (PERX) and x+z (PERZ) only")
+    R = ref_lib(variants[per])
     nc, nf, dim = desc.ncells, desc.nfaces, desc.dim
     nph = desc.num_phases
     u0 = np.ascontiguousarray(u0, dtype=np.float64).ravel()

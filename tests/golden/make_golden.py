@@ -108,6 +108,24 @@ def golden_cases():
     d.pressure_fixed_cell = 7
     out.append(("channel3d_pinned", d, u0, q0, 2, True))
 
+    # periodicity (mesh2d.hpp / mesh3d.hpp PERX, PERZ): a two-phase layer
+    # periodic in x; a 3D box periodic in x and z with a moving lid
+    d, u0, q0 = cases.broken_dam(nx=24, ny=12, dt_auto=False, dt=1e-3, smooth_times=2)
+    tight(d, p_tol=1e-10)
+    d.periodic[0] = 1
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    d.tvd_split = 1
+    out.append(("dam2d_periodic_x", d, u0, q0, 2, True))
+
+    d, u0, q0 = cases.cavity(n=8, dim=3, dt=1e-2)
+    d.n[0], d.n[2] = 10, 6
+    u0, q0 = np.zeros(d.ncells * 3), np.ones(d.ncells)
+    u0[: d.ncells] = 0.1 * np.sin(2 * np.pi * (np.arange(d.ncells) % 10) / 10.0)
+    tight(d)
+    d.periodic[0] = d.periodic[2] = 1
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    out.append(("box3d_periodic_xz", d, u0, q0, 2, True))
+
     # SIMPLER (fluid.hpp:1059-1155): singular walls, pinned two-phase
     d, u0, q0 = cases.cavity(n=16, mu=0.01, dt=1e-2)
     tight(d)
