@@ -22,22 +22,17 @@ __device__ __forceinline__ double superbee(double p, double q) {
   return 0.;
 }
 
-// Superbee value on the inner face between P (low) and E (high) along an
-// axis of stride s; idP is P's index along that axis.  bP / bE: values of
-// P's low / E's high face when those are boundary faces (the advection
-// condition: the inlet value, else the cell's own, zero derivative).
-__device__ __forceinline__ double superbee_face(const double* q, long long P, long long E,
-                                                long long s, int idP, int nd, double Ff,
-                                                double h, double inv_h, double bP, double bE) {
-  double qP = q[P], qE = q[E];
+// Superbee value on the inner face between P (low side) and E (high side)
+// with flux Ff; fP = value of P's other (low) face, fE = value of E's other
+// (high) face, as the Green-Gauss cell gradients of P and E use them.
+__device__ __forceinline__ double superbee_face(double qP, double qE, double fP, double fE,
+                                                double Ff, double h, double inv_h) {
   if (Ff > 1e-8) {
-    double flo = idP > 0 ? avg(q[P - s], qP) : bP;
-    double gP = (avg(qP, qE) - flo) * inv_h;
+    double gP = (avg(qP, qE) - fP) * inv_h;
     double dq = qE - qP;
     return qP + 0.5 * superbee(dq, -4. * (gP * (-0.5 * h)) - dq);
   } else if (Ff < -1e-8) {
-    double fhi = idP + 1 < nd - 1 ? avg(qE, q[E + s]) : bE;
-    double gE = (fhi - avg(qP, qE)) * inv_h;
+    double gE = (fE - avg(qP, qE)) * inv_h;
     double dq = qE - qP;
     return qE - 0.5 * superbee(dq, 4. * (gE * (0.5 * h)) - dq);
   }
@@ -45,7 +40,9 @@ __device__ __forceinline__ double superbee_face(const double* q, long long P, lo
 }
 
 // inlet_mask: bit q set when side q (xm, xp, ym, ...) is an inlet; qin
-// holds the inlet values on those boundary faces.
+// holds the inlet values on those boundary faces.  Boundary faces carry
+// the advection condition (the inlet value, else zero derivative: the
+// cell's own value); across a periodic end the faces are inner.
 template <int DIM>
 __global__ void k_adv_faces(Mesh m, Geo g, int nph, int stage, int nstages, const double* F,
                             CP<HYDRO_MAXPH> q, int inlet_mask, CP<HYDRO_MAXPH> qin,
@@ -59,16 +56,31 @@ __global__ void k_adv_faces(Mesh m, Geo g, int nph, int stage, int nstages, cons
     long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
     long long fs = face_stride(m, d);
     const bool in_lo = (inlet_mask >> (2 * d)) & 1, in_hi = (inlet_mask >> (2 * d + 1)) & 1;
+    // the low-side face value of cell c (index ic along d) and the
+    // high-side face value, for the cell gradients
+    auto lo_face = [&](const double* qa, const double* qi, long long c, int ic, long long fc) {
+      if (has_lo(m, d, ic)) return avg(qa[nb_lo(m, d, ic, c, s)], qa[c]);
+      return in_lo ? qi[fc] : qa[c];
+    };
+    auto hi_face = [&](const double* qa, const double* qi, long long c, int ic, long long fc) {
+      if (has_hi(m, d, ic)) return avg(qa[c], qa[nb_hi(m, d, ic, c, s)]);
+      return in_hi ? qi[fc] : qa[c];
+    };
+    // inner face between P (index ip) and E (index ie) with face index ff
+    auto inner = [&](const double* qa, const double* qi, long long P, int ip, long long E, int ie,
+                     long long ff, double Ff) {
+      // P's low face is ff - fs unless P wraps (then the periodic end face);
+      // E's high face is ff + fs likewise
+      double fP = lo_face(qa, qi, P, ip, ff - fs);
+      double fE = hi_face(qa, qi, E, ie, ff + fs);
+      return superbee_face(qa[P], qa[E], fP, fE, Ff, g.h[d], g.inv_h[d]);
+    };
     double Ff = F[f];
     for (int i = 0; i < nph; ++i) {
       double qf;
-      if (id > 0) {
-        // P = X.c - s: its low face is a boundary face when id == 1; the
-        // current cell E's high face when id == nd - 1
-        double bP = q.a[i][X.c - s], bE = q.a[i][X.c];
-        if (id == 1 && in_lo) bP = qin.a[i][f - fs];
-        if (id == nd - 1 && in_hi) bE = qin.a[i][f + fs];
-        qf = superbee_face(q.a[i], X.c - s, X.c, s, id - 1, nd, Ff, g.h[d], g.inv_h[d], bP, bE);
+      if (HAS_LO(d)) {
+        const int ip = id > 0 ? id - 1 : nd - 1;
+        qf = inner(q.a[i], qin.a[i], NB_LO(d, s), ip, X.c, id, f, Ff);
       } else {
         qf = in_lo ? qin.a[i][f] : q.a[i][X.c];
       }
@@ -77,7 +89,12 @@ __global__ void k_adv_faces(Mesh m, Geo g, int nph, int stage, int nstages, cons
     if (id == nd - 1) {
       long long fh = f + fs;
       double Fh = F[fh];
-      for (int i = 0; i < nph; ++i) qflux.a[i][fh] = (in_hi ? qin.a[i][fh] : q.a[i][X.c]) * Fh;
+      for (int i = 0; i < nph; ++i) {
+        double qf;
+        if (m.per[d]) qf = inner(q.a[i], qin.a[i], X.c, id, NB_HI(d, s), 0, fh, Fh);
+        else qf = in_hi ? qin.a[i][fh] : q.a[i][X.c];
+        qflux.a[i][fh] = qf * Fh;
+      }
     }
   }
   CELL_LOOP_END
@@ -117,8 +134,8 @@ __global__ void k_sharpen(Mesh m, Geo g, double sharp, double amax, double dtv, 
     long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
-      bool inner = side ? X.i[d] < m.n[d] - 1 : X.i[d] > 0;
-      long long nb = side ? X.c + s : X.c - s;
+      bool inner = side ? HAS_HI(d) : HAS_LO(d);
+      long long nb = inner ? (side ? NB_HI(d, s) : NB_LO(d, s)) : X.c;
       long long f = fl + side * face_stride(m, d);
       double af = inner ? avg(q[side ? X.c : nb], q[side ? nb : X.c]) : q[X.c];
       double gv[DIM], n2 = 0.;
@@ -148,8 +165,8 @@ __global__ void k_grad0(Mesh m, Geo g, const double* a, W3 G, int kch) {
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     long long s = cell_stride(m, d);
-    double flo = X.i[d] > 0 ? avg(a[X.c - s], vc) : vc;
-    double fhi = X.i[d] < m.n[d] - 1 ? avg(vc, a[X.c + s]) : vc;
+    double flo = HAS_LO(d) ? avg(a[NB_LO(d, s)], vc) : vc;
+    double fhi = HAS_HI(d) ? avg(vc, a[NB_HI(d, s)]) : vc;
     G.a[d][X.c] = (fhi - flo) * g.inv_h[d];
   }
   CELL_LOOP_END

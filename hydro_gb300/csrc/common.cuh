@@ -20,6 +20,7 @@ struct Mesh {
   int fnx[3], fny[3]; // x/y extents of each direction block
   double h[3], V, A[3];
   double lo[3];
+  int per[3];         // periodic directions: cells n-1 and 0 are neighbours
 };
 
 __host__ __device__ inline long long cell_id(const Mesh& m, int i, int j, int k) {
@@ -35,6 +36,20 @@ __host__ __device__ inline long long cell_stride(const Mesh& m, int d) {
 // stride between the low and high face of a cell along d
 __host__ __device__ inline long long face_stride(const Mesh& m, int d) {
   return d == 0 ? 1 : (d == 1 ? (long long)m.fnx[1] : (long long)m.fnx[2] * m.fny[2]);
+}
+
+// Neighbours along d of the cell c with index i along d.  A neighbour exists
+// inside the block, or across the end of a periodic direction (both end
+// faces then join cells n-1 and 0, mesh3d.hpp:348-392); s = cell_stride.
+__host__ __device__ inline bool has_lo(const Mesh& m, int d, int i) { return i > 0 || m.per[d]; }
+__host__ __device__ inline bool has_hi(const Mesh& m, int d, int i) {
+  return i < m.n[d] - 1 || m.per[d];
+}
+__host__ __device__ inline long long nb_lo(const Mesh& m, int d, int i, long long c, long long s) {
+  return i > 0 ? c - s : c + (long long)(m.n[d] - 1) * s;
+}
+__host__ __device__ inline long long nb_hi(const Mesh& m, int d, int i, long long c, long long s) {
+  return i < m.n[d] - 1 ? c + s : c - (long long)(m.n[d] - 1) * s;
 }
 
 // Launch geometry: blocks of 32x8 threads over (i, j); each block marches

@@ -656,6 +656,14 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
   x->d = *desc;
   int rc = init_mesh(x->m, desc->dim, desc->n, desc->lo, desc->hi);
   if (rc) { delete x; return rc; }
+  for (int d = 0; d < desc->dim; ++d) {
+    x->m.per[d] = desc->periodic[d] != 0;
+    // red-black multigrid colouring needs an even count across a periodic end
+    if (x->m.per[d] && desc->pressure_solver == HYDRO_LINEAR_MGCG && x->m.n[d] % 2) {
+      delete x;
+      return HYDRO_ERR_UNSUPPORTED;
+    }
+  }
   if (desc->pressure_fixed_cell >= x->m.nc) { delete x; return HYDRO_ERR_ARG; }
   const Mesh& m = x->m;
   x->dim = desc->dim;
@@ -790,7 +798,9 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
     return HYDRO_ERR_CUDA;
   }
   for (int q = 0; q < 6; ++q) {
-    const int kind = q < 2 * dim ? desc->bc_kind[q] : HYDRO_BC_WALL;
+    // the sides of a periodic direction carry no condition
+    const int kind =
+        (q < 2 * dim && !x->m.per[q / 2]) ? desc->bc_kind[q] : HYDRO_BC_WALL;
     x->bc.kind[q] = kind;
     for (int k = 0; k < 3; ++k) x->bc.vel[q][k] = k < dim ? desc->bc_velocity[q][k] : 0.;
     if (kind == HYDRO_BC_INLET) x->inlet_mask |= 1 << q;

@@ -92,8 +92,8 @@ __global__ void k_vel_grad(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T
 #pragma unroll
     for (int n = 0; n < DIM; ++n) {
       T uc = u.a[n][X.c];
-      T flo = id > 0 ? avg(u.a[n][X.c - s], uc) : bv.a[n][fl];
-      T fhi = id < nd - 1 ? avg(uc, u.a[n][X.c + s]) : bv.a[n][fl + face_stride(m, d)];
+      T flo = HAS_LO(d) ? avg(u.a[n][NB_LO(d, s)], uc) : bv.a[n][fl];
+      T fhi = HAS_HI(d) ? avg(uc, u.a[n][NB_HI(d, s)]) : bv.a[n][fl + face_stride(m, d)];
       G.a[n * DIM + d][X.c] = (fhi - flo) * g.inv_h[d];
     }
   }
@@ -123,21 +123,23 @@ __global__ void k_force(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T, 9
     int id = X.i[n], nd = m.n[n];
     T mlo, mhi;
     T glo[DIM], ghi[DIM];
-    if (id > 0) {
-      mlo = face_scal(mu[X.c - s], muc, fc.geometric);
+    if (HAS_LO(n)) {
+      const long long cl = NB_LO(n, s);
+      mlo = face_scal(mu[cl], muc, fc.geometric);
 #pragma unroll
       for (int k = 0; k < DIM; ++k)
-        glo[k] = avg(G.a[n * DIM + k][X.c - s], G.a[n * DIM + k][X.c]);
+        glo[k] = avg(G.a[n * DIM + k][cl], G.a[n * DIM + k][X.c]);
     } else {
       mlo = muc;
 #pragma unroll
       for (int k = 0; k < DIM; ++k) glo[k] = G.a[n * DIM + k][X.c];
     }
-    if (id < nd - 1) {
-      mhi = face_scal(muc, mu[X.c + s], fc.geometric);
+    if (HAS_HI(n)) {
+      const long long ch = NB_HI(n, s);
+      mhi = face_scal(muc, mu[ch], fc.geometric);
 #pragma unroll
       for (int k = 0; k < DIM; ++k)
-        ghi[k] = avg(G.a[n * DIM + k][X.c], G.a[n * DIM + k][X.c + s]);
+        ghi[k] = avg(G.a[n * DIM + k][X.c], G.a[n * DIM + k][ch]);
     } else {
       mhi = muc;
 #pragma unroll
@@ -153,12 +155,12 @@ __global__ void k_force(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T, 9
     int id = X.i[k], nd = m.n[k];
     // the pressure gradient stays FP64: p carries the hydrostatic level,
     // whose FP32 rounding would swamp differences across a cell
-    double gpd = grad_extrap(p, X.c, id, nd, s, g64.inv_h[k]);
+    double gpd = grad_extrap_m(m, p, X.c, k, id, s, g64.inv_h[k]);
     gp64.a[k][X.c] = gpd;
     T gp = (T)gpd;
     T fcv = force.a[k][X.c];
-    T flo = id > 0 ? face_vec<DIM, T>(force, X.c - s, X.c, k, fc.geometric) : fcv;
-    T fhi = id < nd - 1 ? face_vec<DIM, T>(force, X.c, X.c + s, k, fc.geometric) : fcv;
+    T flo = HAS_LO(k) ? face_vec<DIM, T>(force, NB_LO(k, s), X.c, k, fc.geometric) : fcv;
+    T fhi = HAS_HI(k) ? face_vec<DIM, T>(force, X.c, NB_HI(k, s), k, fc.geometric) : fcv;
     T fr = T(0.5) * (flo + fhi);
     fres.a[k][X.c] = fr;
     T v = -gp + fr + stforce.a[k][X.c];
@@ -209,9 +211,9 @@ __global__ void k_mom_assemble(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> up,
       const T Ff = F[f];
       // outward convective flux times rho/V (s_f = -1 on the low face)
       const T Fo = side ? Ff * rv : -(Ff * rv);
-      bool inner = side ? (id < nd - 1) : (id > 0);
+      bool inner = side ? HAS_HI(d) : HAS_LO(d);
       if (inner) {
-        long long nb = side ? X.c + s : X.c - s;
+        long long nb = side ? NB_HI(d, s) : NB_LO(d, s);
         T dif = face_scal(muc, mu[nb], fc.geometric) * g.inv_h2[d];
         // the cell is the low-side cell (cm) of its high face and the
         // high-side cell (cp) of its low face
@@ -254,8 +256,8 @@ __global__ void k_mom_assemble(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> up,
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       long long s = cell_stride(m, d);
-      if (X.i[d] > 0) r += aq[2 * d] * up.a[n][X.c - s];
-      if (X.i[d] < m.n[d] - 1) r += aq[2 * d + 1] * up.a[n][X.c + s];
+      if (HAS_LO(d)) r += aq[2 * d] * up.a[n][NB_LO(d, s)];
+      if (HAS_HI(d)) r += aq[2 * d + 1] * up.a[n][NB_HI(d, s)];
     }
     res.a[n][X.c] = r;
   }
@@ -294,8 +296,8 @@ __global__ void __launch_bounds__(NT) k_mom_sweep(Mesh m, double omega, double t
 #pragma unroll
       for (int d = 0; d < DIM; ++d) {
         long long s = cell_stride(m, d);
-        if (X.i[d] > 0) sum += a[2 * d] * din.a[n][X.c - s];
-        if (X.i[d] < m.n[d] - 1) sum += a[2 * d + 1] * din.a[n][X.c + s];
+        if (HAS_LO(d)) sum += a[2 * d] * din.a[n][NB_LO(d, s)];
+        if (HAS_HI(d)) sum += a[2 * d + 1] * din.a[n][NB_HI(d, s)];
       }
     }
     double value = -(res.a[n][X.c] + sum) * iaP;
@@ -338,8 +340,8 @@ __global__ void __launch_bounds__(NT) k_mom_sweep32(Mesh m, float omega, double 
 #pragma unroll
       for (int d = 0; d < DIM; ++d) {
         long long s = cell_stride(m, d);
-        if (X.i[d] > 0) sum = fmaf(a[2 * d], din.a[n][X.c - s], sum);
-        if (X.i[d] < m.n[d] - 1) sum = fmaf(a[2 * d + 1], din.a[n][X.c + s], sum);
+        if (HAS_LO(d)) sum = fmaf(a[2 * d], din.a[n][NB_LO(d, s)], sum);
+        if (HAS_HI(d)) sum = fmaf(a[2 * d + 1], din.a[n][NB_HI(d, s)], sum);
       }
     }
     float value = -(c.a[7 + n][X.c] + sum) * iaP;
@@ -387,8 +389,8 @@ __global__ void k_rhie_chow(Mesh m, Geo g64, GeoT<T> g, FluidCoef fc64, FluidCoe
     long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
     const double A = g64.A[d];
     const double mv = fc64.meshvel[d] * A;
-    if (id > 0) {
-      long long cm = X.c - s, cp = X.c;
+    // inner face between cm (low side) and cp (high side)
+    auto inner = [&](long long cm, long long cp, long long ff) {
       // FP64: the interpolated velocity and the difference of the wide and
       // compact pressure gradients (the cell gradients come from k_force)
       double uf = avg(up.a[d][cm] + (double)du.a[d][cm], up.a[d][cp] + (double)du.a[d][cp]);
@@ -400,9 +402,12 @@ __global__ void k_rhie_chow(Mesh m, Geo g64, GeoT<T> g, FluidCoef fc64, FluidCoe
       T iDf = T(1) / avg(Dc[cm], Dc[cp]);
       T k = g.A[d] * g.inv_h[d] * iDf;
       T corr = fc.rc * (((T)dpw + (fxf - frf)) * g.A[d]) * iDf;
-      Fs[f] = vfi + (double)corr - mv;
-      kf[f] = (double)k;
-      if (kf32) kf32[f] = (float)k;
+      Fs[ff] = vfi + (double)corr - mv;
+      kf[ff] = (double)k;
+      if (kf32) kf32[ff] = (float)k;
+    };
+    if (HAS_LO(d)) {
+      inner(NB_LO(d, s), X.c, f);
     } else {
       Fs[f] = bv.a[d][f] * A - mv;
       kf[f] = 0.;
@@ -410,9 +415,13 @@ __global__ void k_rhie_chow(Mesh m, Geo g64, GeoT<T> g, FluidCoef fc64, FluidCoe
     }
     if (id == nd - 1) {
       long long fh = f + face_stride(m, d);
-      Fs[fh] = bv.a[d][fh] * A - mv;
-      kf[fh] = 0.;
-      if (kf32) kf32[fh] = 0.f;
+      if (m.per[d]) {
+        inner(X.c, NB_HI(d, s), fh);
+      } else {
+        Fs[fh] = bv.a[d][fh] * A - mv;
+        kf[fh] = 0.;
+        if (kf32) kf32[fh] = 0.f;
+      }
     }
   }
   CELL_LOOP_END
@@ -461,7 +470,7 @@ __global__ void __launch_bounds__(NT) k_correct(Mesh m, Geo g, FluidCoef fc, C3 
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
     long long s = cell_stride(m, k);
-    double gpc = grad_extrap(pc, X.c, X.i[k], m.n[k], s, g.inv_h[k]);
+    double gpc = grad_extrap_m(m, pc, X.c, k, X.i[k], s, g.inv_h[k]);
     double u0 = up.a[k][X.c];
     double duk = du32.a[0] ? (double)du32.a[k][X.c] : du.a[k][X.c];
     double un = (u0 + duk) + gpc * idc;
@@ -470,13 +479,16 @@ __global__ void __launch_bounds__(NT) k_correct(Mesh m, Geo g, FluidCoef fc, C3 
     double dd = un - u0;
     d2 += dd * dd;
     long long f = face_id(m, k, X.i[0], X.i[1], X.i[2]);
-    double fv = X.i[k] > 0 ? Fs[f] + kf[f] * (pc[X.c - s] - pc[X.c]) : Fs[f];
+    double fv = HAS_LO(k) ? Fs[f] + kf[f] * (pc[NB_LO(k, s)] - pc[X.c]) : Fs[f];
     Fic[f] = fv;
     if (F32) F32[f] = (float)fv;
     if (X.i[k] == m.n[k] - 1) {
+      // high end face: a boundary face, or across a periodic end the face
+      // between this cell (cm) and the first cell (cp)
       long long fh = f + face_stride(m, k);
-      Fic[fh] = Fs[fh];
-      if (F32) F32[fh] = (float)Fs[fh];
+      double fvh = m.per[k] ? Fs[fh] + kf[fh] * (pc[X.c] - pc[NB_HI(k, s)]) : Fs[fh];
+      Fic[fh] = fvh;
+      if (F32) F32[fh] = (float)fvh;
     }
   }
   dmax = fmax(dmax, sqrt(d2));
@@ -504,9 +516,14 @@ __global__ void k_simpler_eval(Mesh m, CP<7> coef, C3 res, C3 uic, C3 up, C3 fre
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       long long s = cell_stride(m, d);
-      if (X.i[d] > 0) r += coef.a[1 + 2 * d][X.c] * (uic.a[n][X.c - s] - up.a[n][X.c - s]);
-      if (X.i[d] < m.n[d] - 1)
-        r += coef.a[2 + 2 * d][X.c] * (uic.a[n][X.c + s] - up.a[n][X.c + s]);
+      if (HAS_LO(d)) {
+        const long long cl = NB_LO(d, s);
+        r += coef.a[1 + 2 * d][X.c] * (uic.a[n][cl] - up.a[n][cl]);
+      }
+      if (HAS_HI(d)) {
+        const long long ch = NB_HI(d, s);
+        r += coef.a[2 + 2 * d][X.c] * (uic.a[n][ch] - up.a[n][ch]);
+      }
     }
     ev.a[n][X.c] = r + (fres.a[n][X.c] - gp.a[n][X.c]);
   }
@@ -535,9 +552,9 @@ __global__ void k_simpler_rhs(Mesh m, Geo g, FluidCoef fc, C3 ev, C3 force, cons
     long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
-      bool inner = side ? X.i[d] < m.n[d] - 1 : X.i[d] > 0;
+      bool inner = side ? HAS_HI(d) : HAS_LO(d);
       if (!inner) continue;
-      long long nb = side ? X.c + s : X.c - s;
+      long long nb = side ? NB_HI(d, s) : NB_LO(d, s);
       long long cm = side ? X.c : nb, cp = side ? nb : X.c;
       long long fq = side ? fl + face_stride(m, d) : fl;
       double e = avg(ev.a[d][cm], ev.a[d][cp]) - face_vec<DIM, double>(force, cm, cp, d, fc.geometric);
@@ -641,8 +658,8 @@ __global__ void k_smooth(Mesh m, const double* in, double* out, int kch) {
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     long long s = cell_stride(m, d);
-    sum += X.i[d] > 0 ? avg(in[X.c - s], vc) : vc;
-    sum += X.i[d] < m.n[d] - 1 ? avg(vc, in[X.c + s]) : vc;
+    sum += HAS_LO(d) ? avg(in[NB_LO(d, s)], vc) : vc;
+    sum += HAS_HI(d) ? avg(vc, in[NB_HI(d, s)]) : vc;
   }
   out[X.c] = sum / (2. * DIM);
   CELL_LOOP_END
@@ -656,8 +673,8 @@ __global__ void k_scal_grad(Mesh m, Geo g, const double* a, W3 G, int kch) {
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     long long s = cell_stride(m, d);
-    double flo = X.i[d] > 0 ? avg(a[X.c - s], vc) : vc;
-    double fhi = X.i[d] < m.n[d] - 1 ? avg(vc, a[X.c + s]) : vc;
+    double flo = HAS_LO(d) ? avg(a[NB_LO(d, s)], vc) : vc;
+    double fhi = HAS_HI(d) ? avg(vc, a[NB_HI(d, s)]) : vc;
     G.a[d][X.c] = (fhi - flo) * g.inv_h[d];
   }
   CELL_LOOP_END
@@ -677,8 +694,8 @@ __global__ void k_stforce(Mesh m, Geo g, double sigma, C3 G, W3 out, int kch) {
     long long s = cell_stride(m, d);
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
-      bool inner = side ? X.i[d] < m.n[d] - 1 : X.i[d] > 0;
-      long long nb = side ? X.c + s : X.c - s;
+      bool inner = side ? HAS_HI(d) : HAS_LO(d);
+      long long nb = inner ? (side ? NB_HI(d, s) : NB_LO(d, s)) : X.c;
       double gv[DIM], n2 = 0.;
 #pragma unroll
       for (int k = 0; k < DIM; ++k) {
@@ -727,7 +744,7 @@ __global__ void __launch_bounds__(NT) k_stat(Mesh m, Geo g, const double* q, con
     // the cell = +F); high boundary face: its first (-F)
     for (int side = 0; side < 2; ++side) {
       bool bnd = side ? X.i[d] == m.n[d] - 1 : X.i[d] == 0;
-      if (!bnd) continue;
+      if (!bnd || m.per[d]) continue;
       double ftc = side ? -F[f + face_stride(m, d)] : F[f];
       if (ftc >= 0.) s[8] += ftc * alc;
       else s[9] -= ftc * alc;
@@ -760,10 +777,12 @@ __global__ void k_init_flux(Mesh m, Geo g, FluidCoef fc, C3 u, C3 bv, double* F,
     long long s = cell_stride(m, d);
     long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
     double mv = fc.meshvel[d] * g.A[d];
-    if (X.i[d] > 0) F[f] = avg(u.a[d][X.c - s], u.a[d][X.c]) * g.A[d] - mv;
+    if (HAS_LO(d)) F[f] = avg(u.a[d][NB_LO(d, s)], u.a[d][X.c]) * g.A[d] - mv;
     else F[f] = bv.a[d][f] * g.A[d] - mv;
     if (X.i[d] == m.n[d] - 1)
-      F[f + face_stride(m, d)] = bv.a[d][f + face_stride(m, d)] * g.A[d] - mv;
+      F[f + face_stride(m, d)] =
+          m.per[d] ? avg(u.a[d][X.c], u.a[d][NB_HI(d, s)]) * g.A[d] - mv
+                   : bv.a[d][f + face_stride(m, d)] * g.A[d] - mv;
   }
   CELL_LOOP_END
 }
@@ -780,7 +799,7 @@ __global__ void k_bc_fill(Mesh m, BcSpec sp, W3 bv, FP<3> bv32, int kch) {
     long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
-      if (side ? X.i[d] != m.n[d] - 1 : X.i[d] != 0) continue;
+      if (m.per[d] || (side ? X.i[d] != m.n[d] - 1 : X.i[d] != 0)) continue;
       long long fb = side ? f + face_stride(m, d) : f;
       int q = 2 * d + side;
       for (int k = 0; k < DIM; ++k) {
@@ -804,7 +823,7 @@ __global__ void k_qin_fill(Mesh m, BcSpec sp, int nph, CP<HYDRO_MAXPH> q, WP<HYD
     long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
-      if (side ? X.i[d] != m.n[d] - 1 : X.i[d] != 0) continue;
+      if (m.per[d] || (side ? X.i[d] != m.n[d] - 1 : X.i[d] != 0)) continue;
       if (sp.kind[2 * d + side] != HYDRO_BC_INLET) continue;
       long long fb = side ? f + face_stride(m, d) : f;
       for (int i = 0; i < nph; ++i) qin.a[i][fb] = q.a[i][X.c];
@@ -829,7 +848,7 @@ __global__ void __launch_bounds__(NT) k_outlet_sums(Mesh m, Geo g, BcSpec sp, C3
     long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
-      if (side ? X.i[d] != m.n[d] - 1 : X.i[d] != 0) continue;
+      if (m.per[d] || (side ? X.i[d] != m.n[d] - 1 : X.i[d] != 0)) continue;
       long long fb = side ? f + face_stride(m, d) : f;
       int kind = sp.kind[2 * d + side];
       // the cell is the face's first neighbour on the high side
@@ -864,7 +883,7 @@ __global__ void k_outlet_set(Mesh m, BcSpec sp, W3 bv, FP<3> bv32, const DevScal
     long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
-      if (side ? X.i[d] != m.n[d] - 1 : X.i[d] != 0) continue;
+      if (m.per[d] || (side ? X.i[d] != m.n[d] - 1 : X.i[d] != 0)) continue;
       if (sp.kind[2 * d + side] != HYDRO_BC_OUTLET) continue;
       long long fb = side ? f + face_stride(m, d) : f;
       bv.a[d][fb] = bv.a[d][fb] + corr * (side ? 1. : -1.);

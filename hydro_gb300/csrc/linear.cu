@@ -41,8 +41,14 @@ __device__ __forceinline__ T stencil_row(const Mesh& m, const Cell& X, const T* 
   for (int d = 0; d < DIM; ++d) {
     long long s = cell_stride(m, d);
     long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
-    if (X.i[d] > 0 && X.c - s != pin) acc -= kf[fl] * p[X.c - s];
-    if (X.i[d] < m.n[d] - 1 && X.c + s != pin) acc -= kf[fl + face_stride(m, d)] * p[X.c + s];
+    if (HAS_LO(d)) {
+      const long long cl = NB_LO(d, s);
+      if (cl != pin) acc -= kf[fl] * p[cl];
+    }
+    if (HAS_HI(d)) {
+      const long long ch = NB_HI(d, s);
+      if (ch != pin) acc -= kf[fl + face_stride(m, d)] * p[ch];
+    }
   }
   return acc;
 }
@@ -57,8 +63,8 @@ __global__ void k_diag(Mesh m, const double* kf, double shift, long long pin, T*
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
-    if (X.i[d] > 0) s += kf[fl];
-    if (X.i[d] < m.n[d] - 1) s += kf[fl + face_stride(m, d)];
+    if (HAS_LO(d)) s += kf[fl];
+    if (HAS_HI(d)) s += kf[fl + face_stride(m, d)];
     if (kf32) {
       kf32[fl] = (T)kf[fl];
       if (X.i[d] == m.n[d] - 1) kf32[fl + face_stride(m, d)] = (T)kf[fl + face_stride(m, d)];
@@ -379,8 +385,14 @@ __global__ void __launch_bounds__(NT) k_cg32_dir_spmv(Mesh m, const float* kf, c
     for (int d = 0; d < DIM; ++d) {
       long long s = cell_stride(m, d);
       long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
-      if (X.i[d] > 0 && X.c - s != pin) a = fmaf(-kf[fl], P(X.c - s), a);
-      if (X.i[d] < m.n[d] - 1 && X.c + s != pin) a = fmaf(-kf[fl + face_stride(m, d)], P(X.c + s), a);
+      if (HAS_LO(d)) {
+        const long long cl = NB_LO(d, s);
+        if (cl != pin) a = fmaf(-kf[fl], P(cl), a);
+      }
+      if (HAS_HI(d)) {
+        const long long ch = NB_HI(d, s);
+        if (ch != pin) a = fmaf(-kf[fl + face_stride(m, d)], P(ch), a);
+      }
     }
   }
   Ap[X.c] = a;
@@ -504,8 +516,8 @@ __global__ void k_pin_rhs(Mesh m, const double* kf, double* f, long long pin, do
   for (int d = 0; d < m.dim; ++d) {
     long long s = cell_stride(m, d);
     long long fl = face_id(m, d, i[0], i[1], i[2]);
-    if (i[d] > 0) f[pin - s] += kf[fl] * value;
-    if (i[d] < m.n[d] - 1) f[pin + s] += kf[fl + face_stride(m, d)] * value;
+    if (has_lo(m, d, i[d])) f[nb_lo(m, d, i[d], pin, s)] += kf[fl] * value;
+    if (has_hi(m, d, i[d])) f[nb_hi(m, d, i[d], pin, s)] += kf[fl + face_stride(m, d)] * value;
   }
   f[pin] = value;
 }

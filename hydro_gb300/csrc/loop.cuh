@@ -51,6 +51,20 @@ __device__ __forceinline__ T grad_extrap(const T* p, long long c, int id, int nd
   if (id == 0) return (p[c + s] - p[c]) * inv_h;
   return (p[c] - p[c - s]) * inv_h;
 }
+// The same along direction d of mesh m, central across a periodic end.
+template <class T>
+__device__ __forceinline__ T grad_extrap_m(const Mesh& m, const T* p, long long c, int d,
+                                           int id, long long s, T inv_h) {
+  if (m.per[d])
+    return (p[nb_hi(m, d, id, c, s)] - p[nb_lo(m, d, id, c, s)]) * (T(0.5) * inv_h);
+  return grad_extrap(p, c, id, m.n[d], s, inv_h);
+}
+
+// Shorthands inside CELL_LOOP bodies: neighbours of the cell X along d.
+#define HAS_LO(d) has_lo(m, (d), X.i[d])
+#define HAS_HI(d) has_hi(m, (d), X.i[d])
+#define NB_LO(d, s) nb_lo(m, (d), X.i[d], X.c, (s))
+#define NB_HI(d, s) nb_hi(m, (d), X.i[d], X.c, (s))
 
 template <class T>
 struct GeoT {

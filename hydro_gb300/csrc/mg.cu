@@ -62,13 +62,16 @@ __global__ void k_mg_smooth(Mesh m, const float* kf, const float* idg, const flo
         long long fl = face_id(m, d, i, j, k);
 #pragma unroll
         for (int side = 0; side < 2; ++side) {
-          bool in = side ? id[d] < m.n[d] - 1 : id[d] > 0;
-          long long nb = side ? c + s : c - s;
-          if (!in || nb == pin) continue;
+          bool in = side ? has_hi(m, d, id[d]) : has_lo(m, d, id[d]);
+          if (!in) continue;
+          long long nb = side ? nb_hi(m, d, id[d], c, s) : nb_lo(m, d, id[d], c, s);
+          if (nb == pin) continue;
           float xv = x[nb];
           if (cx) {
             int q[3] = {i, j, k};
             q[d] += side ? 1 : -1;
+            if (q[d] < 0) q[d] = m.n[d] - 1;
+            if (q[d] >= m.n[d]) q[d] = 0;
             xv += cx[(q[0] >> 1) + (long long)cnx * ((q[1] >> 1) + (long long)cny * (q[2] >> 1))];
           }
           acc = fmaf(kf[side ? fl + face_stride(m, d) : fl], xv, acc);
@@ -79,29 +82,36 @@ __global__ void k_mg_smooth(Mesh m, const float* kf, const float* idg, const flo
   }
 }
 
-// Coarse couplings: 1/2 of the sum of the fine couplings of each coarse face.
+// Coarse couplings: 1/2 of the sum of the fine couplings of each coarse face
+// (zero on boundary faces; across a periodic end the coarse face joins the
+// last and first coarse cells like the fine one).
 template <int DIM>
 __global__ void k_mg_coarsen(Mesh fm, Mesh cm, const float* fkf, float* ckf, int kch) {
   CELL_LOOP_BEGIN(cm, kch)
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     long long cf = face_id(cm, d, X.i[0], X.i[1], X.i[2]);
-    // fine faces of the coarse low face: index 2I along d, 2I and 2I+1 across
-    float sum = 0.f;
     int e1 = (d + 1) % DIM, e2 = (d + 2) % DIM;
+    // fine faces of the coarse face at coarse index I along d: index 2I
+    // along d, 2I' and 2I'+1 across
+    auto fsum = [&](int I) {
+      float sum = 0.f;
 #pragma unroll
-    for (int a = 0; a < 2; ++a) {
+      for (int a = 0; a < 2; ++a) {
 #pragma unroll
-      for (int bq = 0; bq < (DIM == 3 ? 2 : 1); ++bq) {
-        int fi[3] = {2 * X.i[0], 2 * X.i[1], 2 * X.i[2]};
-        fi[e1] += a;
-        if (DIM == 3) fi[e2] += bq;
-        sum += fkf[face_id(fm, d, fi[0], fi[1], DIM == 3 ? fi[2] : 0)];
+        for (int bq = 0; bq < (DIM == 3 ? 2 : 1); ++bq) {
+          int fi[3] = {2 * X.i[0], 2 * X.i[1], 2 * X.i[2]};
+          fi[d] = 2 * I;
+          fi[e1] += a;
+          if (DIM == 3) fi[e2] += bq;
+          sum += fkf[face_id(fm, d, fi[0], fi[1], DIM == 3 ? fi[2] : 0)];
+        }
       }
-    }
-    float kc = X.i[d] > 0 ? 0.5f * sum : 0.f;
-    ckf[cf] = kc;
-    if (X.i[d] == cm.n[d] - 1) ckf[cf + face_stride(cm, d)] = 0.f;
+      return sum;
+    };
+    ckf[cf] = has_lo(cm, d, X.i[d]) ? 0.5f * fsum(X.i[d]) : 0.f;
+    if (X.i[d] == cm.n[d] - 1)
+      ckf[cf + face_stride(cm, d)] = cm.per[d] ? 0.5f * fsum(X.i[d] + 1) : 0.f;
   }
   CELL_LOOP_END
 }
@@ -146,8 +156,14 @@ __global__ void k_mg_restrict(Mesh fm, Mesh cm, const float* kf, const float* dg
           for (int d = 0; d < DIM; ++d) {
             long long s = cell_stride(fm, d);
             long long fl = face_id(fm, d, id[0], id[1], id[2]);
-            if (id[d] > 0 && c - s != pin) ax = fmaf(-kf[fl], x[c - s], ax);
-            if (id[d] < fm.n[d] - 1 && c + s != pin) ax = fmaf(-kf[fl + face_stride(fm, d)], x[c + s], ax);
+            if (has_lo(fm, d, id[d])) {
+              const long long cl = nb_lo(fm, d, id[d], c, s);
+              if (cl != pin) ax = fmaf(-kf[fl], x[cl], ax);
+            }
+            if (has_hi(fm, d, id[d])) {
+              const long long ch = nb_hi(fm, d, id[d], c, s);
+              if (ch != pin) ax = fmaf(-kf[fl + face_stride(fm, d)], x[ch], ax);
+            }
           }
           r = b[c] - ax;
         }
@@ -204,9 +220,14 @@ __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const
       for (int d = 0; d < DIM; ++d) {
         int s = (int)cell_stride(m, d);
         int fl = (int)face_id(m, d, id[0], id[1], id[2]);
-        if (id[d] > 0 && c - s != pin) acc = fmaf(kf[fl], x[c - s], acc);
-        if (id[d] < m.n[d] - 1 && c + s != pin)
-          acc = fmaf(kf[fl + (int)face_stride(m, d)], x[c + s], acc);
+        if (has_lo(m, d, id[d])) {
+          const int cl = (int)nb_lo(m, d, id[d], c, s);
+          if (cl != pin) acc = fmaf(kf[fl], x[cl], acc);
+        }
+        if (has_hi(m, d, id[d])) {
+          const int ch = (int)nb_hi(m, d, id[d], c, s);
+          if (ch != pin) acc = fmaf(kf[fl + (int)face_stride(m, d)], x[ch], acc);
+        }
       }
     }
     x[c] = acc * idg[c];
@@ -242,8 +263,14 @@ __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, co
               int fl = (int)face_id(fm, d, id[0], id[1], id[2]);
               float klo = kf[fl], khi = kf[fl + (int)face_stride(fm, d)];
               dg += klo + khi;
-              if (id[d] > 0 && c - s != pin) off = fmaf(klo, x[c - s], off);
-              if (id[d] < fm.n[d] - 1 && c + s != pin) off = fmaf(khi, x[c + s], off);
+              if (has_lo(fm, d, id[d])) {
+                const int cl = (int)nb_lo(fm, d, id[d], c, s);
+                if (cl != pin) off = fmaf(klo, x[cl], off);
+              }
+              if (has_hi(fm, d, id[d])) {
+                const int ch = (int)nb_hi(fm, d, id[d], c, s);
+                if (ch != pin) off = fmaf(khi, x[ch], off);
+              }
             }
             r = b[c] - (dg * x[c] - off);
           }
@@ -462,8 +489,12 @@ int mg_levels_for(const Mesh& m) {
   Mesh cur = m;
   while (nlev < kMgMaxLevels && cur.nc > kMgCoarseTarget) {
     bool ok = true;
-    for (int d = 0; d < cur.dim; ++d)
+    for (int d = 0; d < cur.dim; ++d) {
       if (cur.n[d] % 2 != 0 || cur.n[d] / 2 < 2) ok = false;
+      // a periodic direction keeps an even count (red-black colouring
+      // across the periodic end)
+      if (cur.per[d] && (cur.n[d] / 2) % 2 != 0) ok = false;
+    }
     if (!ok) break;
     cur = mg_coarse_mesh(cur);
     ++nlev;

@@ -1000,7 +1000,8 @@ static void update_outlets(oracle_ctx* x) {
   const Mesh* m = &x->m;
   const hydro_desc* d = &x->d;
   int any = 0;
-  for (int s = 0; s < 2 * m->dim; ++s) any |= d->bc_kind[s] == HYDRO_BC_OUTLET;
+  for (int s = 0; s < 2 * m->dim; ++s)
+    any |= d->bc_kind[s] == HYDRO_BC_OUTLET && !m->per[s / 2];
   if (!any) return;
   double** uic = x->u[HYDRO_ITER_CURR];
   double in = 0., out = 0., area = 0.;

@@ -273,3 +273,32 @@ def test_channel_mixed_and_graph(built):
          "F": h.get_field(capi.F_VOLUME_FLUX), "q": h.get_field(capi.F_PARTIAL_DENSITY)}
     errs = compare(c, b)
     assert all(v <= 1e-12 for v in errs.values()), errs
+
+
+def test_periodic_vs_oracle(built):
+    """Periodic directions (x in 2D; x and z in 3D) against the oracle: the
+    FP64 path, and the mixed path with the multigrid (periodic coarse
+    levels) against the FP64 path."""
+    from hydro_gb300.solver import Hydro
+    from oracle.oracle import Oracle
+    d, u0, q0 = cases.broken_dam(nx=32, ny=16, dt_auto=False, dt=1e-3, smooth_times=2)
+    tight(d)
+    d.periodic[0] = 1
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    d.tvd_split = 1
+    a = run(Hydro(d), u0, q0, 3)
+    b = run(Oracle(d), u0, q0, 3)
+    errs = compare(a, b)
+    assert all(v <= 1e-10 for v in errs.values()), errs
+    d, u0, q0, _ = cases.rising_drops(n=16, seed=7, dt_max=5e-3)
+    d.periodic[0] = d.periodic[2] = 1
+    d.gravity[1], d.gravity[2] = -1.0, 0.0  # gravity across the walled direction
+    d.pressure_tolerance, d.velocity_tolerance = 1e-10, 1e-12
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    a = run(Hydro(d), u0, q0, 2)
+    dm = d.copy()
+    dm.precision = capi.MIXED
+    dm.pressure_solver = capi.LINEAR_MGCG
+    b = run(Hydro(dm), u0, q0, 2)
+    errs = compare(b, a)
+    assert all(v <= 1e-6 for v in errs.values()), errs
