@@ -5,7 +5,9 @@
 //       constructed with FluidSimple's argument list (fluid.hpp:644-670)
 //   solver::AdvectionSolverMultiGpu<Mesh>   : solver::AdvectionSolverMulti<Mesh, FieldFace>
 //       constructed with AdvectionSolverMultiExplicit's list (advection.hpp:388-398)
-// Both share one GPU context (GpuHotPath).  Fields the module owns (density,
+//   solver::HeatSolverGpu<Mesh>             : solver::UnsteadyIterativeSolver
+//       constructed with HeatSolver's list (heat.hpp:33-47)
+// All share one GPU context (GpuHotPath).  Fields the module owns (density,
 // viscosity, force, surface-tension force, sources) are read through the
 // same raw pointers FluidSimple keeps and uploaded at StartStep; layers the
 // solver owns are downloaded on Get*(layer).  Errors follow the reference:
@@ -16,6 +18,7 @@
 // and link with -lhydro_gpu.
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <memory>
 #include <stdexcept>
@@ -47,6 +50,14 @@ class GpuHotPath {
       desc_.lo[d] = lo[d];
       desc_.hi[d] = hi[d];
     }
+    // the reference's compile-time periodicity (mesh2d.hpp:288,
+    // mesh3d.hpp:306-317)
+#ifdef PERX
+    desc_.periodic[0] = 1;
+#endif
+#ifdef PERZ
+    if (dim == 3) desc_.periodic[2] = 1;
+#endif
   }
   ~GpuHotPath() {
     if (ctx_) hydro_gpu_destroy(ctx_);
@@ -143,24 +154,39 @@ class FluidSimpleGpu : public FluidSolver<Mesh> {
         path_(std::make_shared<GpuHotPath<Mesh>>(mesh)),
         mesh_(mesh) {
     using namespace fluid_condition;
-    if (simpler) throw std::runtime_error("FluidSimpleGpu: SIMPLER is not built");
     hydro_desc& d = path_->desc();
-    // per-side wall velocities from the face conditions (fluid.hpp:695-731)
+    d.simpler = simpler;
+    // per-side kind and velocity from the face conditions (fluid.hpp:695-731):
+    // walls and inlets carry their velocity, outlets are rebalanced on the
+    // device (fluid.hpp:542-600); one kind and one velocity per side
     std::array<bool, 6> seen{};
     for (auto it = mf_cond.cbegin(); it != mf_cond.cend(); ++it) {
       IdxFace f = it->GetIdx();
-      auto* wall = dynamic_cast<NoSlipWall<Mesh>*>(it->GetValue().get());
-      if (!wall) throw std::runtime_error("FluidSimpleGpu: only wall conditions are built");
+      auto* c = it->GetValue().get();
+      int kind;
+      Vect v(0);
+      if (auto* wall = dynamic_cast<NoSlipWall<Mesh>*>(c)) {
+        kind = HYDRO_BC_WALL;
+        v = wall->GetVelocity();
+      } else if (auto* in = dynamic_cast<Inlet<Mesh>*>(c)) {
+        kind = HYDRO_BC_INLET;
+        v = in->GetVelocity();
+      } else if (dynamic_cast<Outlet<Mesh>*>(c)) {
+        kind = HYDRO_BC_OUTLET;
+      } else {
+        throw std::runtime_error("FluidSimpleGpu: unknown face condition");
+      }
       size_t dir = mesh.GetDirection(f);
       auto mi = mesh.GetBlockFaces().GetMIdx(f);
       int side = 2 * (int)dir + (mi[dir] == 0 ? 0 : 1);
-      Vect v = wall->GetVelocity();
+      if (seen[side] && d.bc_kind[side] != kind)
+        throw std::runtime_error("FluidSimpleGpu: one condition kind per side");
       for (size_t k = 0; k < dim; ++k) {
         if (seen[side] && d.bc_velocity[side][k] != v[k])
-          throw std::runtime_error("FluidSimpleGpu: wall velocity must be uniform per side");
+          throw std::runtime_error("FluidSimpleGpu: condition velocity must be uniform per side");
         d.bc_velocity[side][k] = v[k];
       }
-      d.bc_kind[side] = HYDRO_BC_WALL;
+      d.bc_kind[side] = kind;
       seen[side] = true;
     }
     for (auto it = mc_cond.cbegin(); it != mc_cond.cend(); ++it) {
@@ -325,6 +351,119 @@ class AdvectionSolverMultiGpu
   std::shared_ptr<GpuHotPath<Mesh>> path_;
   const Mesh& mesh_;
   std::vector<geom::FieldCell<Scal>> cache_;
+};
+
+// Drop-in for HeatSolver<Mesh> (heat.hpp:18-94) with its argument list,
+// plus the fluid adapter whose context and volume fluxes it shares.  The
+// temperature conditions must be the ones hydro<Mesh>::InitHeatSolver
+// builds (hydro2d.hpp:660-677): one fixed value on the boundary faces whose
+// centre lies in a box, zero derivative on the others.  The box is
+// recovered as the bounding box of the value faces' centres and checked
+// against the map.  The module's conductivity (p_fc_conductivity) is
+// uploaded at every StartStep; the source must be zero; the linear solve is
+// Jacobi sweeps (SetLinearTolerance; the factory is opaque).
+template <class Mesh>
+class HeatSolverGpu : public UnsteadyIterativeSolver {
+  using Scal = typename Mesh::Scal;
+  using Vect = typename Mesh::Vect;
+  static constexpr size_t dim = Mesh::dim;
+
+ public:
+  HeatSolverGpu(FluidSimpleGpu<Mesh>& fluid, const Mesh& mesh,
+                const geom::FieldCell<Scal>& fc_temperature_initial,
+                const geom::MapFace<std::shared_ptr<ConditionFace>>& mf_temperature_cond,
+                Scal relaxation_factor, const geom::FieldCell<Scal>* p_fc_conductivity,
+                const geom::FieldCell<Scal>* /*p_fc_source*/,
+                const geom::FieldFace<Scal>* /*p_ff_vol_flux*/, double time, double time_step,
+                const LinearSolverFactory& /*linear_factory*/, double convergence_tolerance,
+                size_t num_iterations_limit, bool time_second_order = true)
+      : UnsteadyIterativeSolver(time, time_step, convergence_tolerance, num_iterations_limit),
+        path_(fluid.path()),
+        mesh_(mesh),
+        p_fc_conductivity_(p_fc_conductivity),
+        t0_(fc_temperature_initial) {
+    hd_ = hydro_heat_desc();
+    hd_.relaxation_factor = relaxation_factor;
+    hd_.time_second_order = time_second_order;
+    hd_.solver = HYDRO_LINEAR_JACOBI;
+    hd_.tolerance = 1e-12;
+    hd_.iters_limit = 10000;
+    hd_.dt = time_step;
+    hd_.temperature_initial = fc_temperature_initial[geom::IdxCell(0)];
+    bool any = false;
+    Vect lo(0), hi(0);
+    for (auto it = mf_temperature_cond.cbegin(); it != mf_temperature_cond.cend(); ++it) {
+      auto* c = it->GetValue().get();
+      if (auto* v = dynamic_cast<ConditionFaceValueFixed<Scal>*>(c)) {
+        Vect x = mesh.GetCenter(it->GetIdx());
+        if (any && v->GetValue() != hd_.box_temperature)
+          throw std::runtime_error("HeatSolverGpu: one fixed temperature");
+        hd_.box_temperature = v->GetValue();
+        for (size_t k = 0; k < dim; ++k) {
+          lo[k] = any ? std::min(lo[k], x[k]) : x[k];
+          hi[k] = any ? std::max(hi[k], x[k]) : x[k];
+        }
+        any = true;
+      } else if (!dynamic_cast<ConditionFaceDerivativeFixed<Scal>*>(c)) {
+        throw std::runtime_error("HeatSolverGpu: value or zero-derivative conditions only");
+      }
+    }
+    for (size_t k = 0; k < 3; ++k) {
+      hd_.box_lo[k] = k < dim ? lo[k] : 0.;
+      hd_.box_hi[k] = k < dim ? hi[k] : 0.;
+    }
+    if (!any) {  // no value face: an empty box below the domain
+      for (size_t k = 0; k < 3; ++k) {
+        hd_.box_lo[k] = 1.;
+        hd_.box_hi[k] = -1.;
+      }
+    }
+    for (auto it = mf_temperature_cond.cbegin(); it != mf_temperature_cond.cend(); ++it) {
+      Vect x = mesh.GetCenter(it->GetIdx());
+      bool in = any;
+      for (size_t k = 0; k < dim; ++k) in = in && lo[k] <= x[k] && x[k] <= hi[k];
+      bool value = dynamic_cast<ConditionFaceValueFixed<Scal>*>(it->GetValue().get()) != nullptr;
+      if (in != value) throw std::runtime_error("HeatSolverGpu: value faces must form a box");
+    }
+  }
+  void SetLinearTolerance(double tol, int limit) {
+    hd_.tolerance = tol;
+    hd_.iters_limit = limit;
+  }
+  void StartStep() override {
+    this->ClearIterationCount();
+    if (!created_) {
+      GpuHotPath<Mesh>::Check(hydro_gpu_heat_create(path_->ctx(), &hd_), "heat_create");
+      path_->Upload(HYDRO_FIELD_TEMPERATURE, t0_);
+      GpuHotPath<Mesh>::Check(hydro_gpu_set_field(path_->ctx(), HYDRO_FIELD_TEMPERATURE,
+                                                  HYDRO_TIME_PREV, t0_.data(), t0_.size()),
+                              "set temperature");
+      created_ = true;
+    }
+    path_->Upload(HYDRO_FIELD_CONDUCTIVITY, *p_fc_conductivity_);
+  }
+  void MakeIteration() override {
+    GpuHotPath<Mesh>::Check(hydro_gpu_heat_step(path_->ctx()), "heat_step");
+    this->IncIterationCount();
+  }
+  void FinishStep() override { this->IncTime(); }
+  double GetConvergenceIndicator() const override { return 0.; }
+  const geom::FieldCell<Scal>& GetTemperature() { return GetTemperature(Layers::time_curr); }
+  const geom::FieldCell<Scal>& GetTemperature(Layers layer) {
+    if (!created_) return t0_;
+    auto& f = cache_.Get(layer);
+    path_->Download(HYDRO_FIELD_TEMPERATURE, (int)layer, f, mesh_.GetNumCells());
+    return f;
+  }
+
+ private:
+  std::shared_ptr<GpuHotPath<Mesh>> path_;
+  const Mesh& mesh_;
+  const geom::FieldCell<Scal>* p_fc_conductivity_;
+  geom::FieldCell<Scal> t0_;
+  hydro_heat_desc hd_;
+  bool created_ = false;
+  LayersData<geom::FieldCell<Scal>> cache_;
 };
 
 }  // namespace solver

@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["fluid.cu", "linear.cu", "mg.cu", "advection.cu", "control.cu", "context.cu",
+SOURCES = ["fluid.cu", "linear.cu", "mg.cu", "advection.cu", "control.cu", "context.cu", "heat.cu",
            "noalloc.cu", "output.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

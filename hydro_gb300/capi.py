@@ -34,7 +34,8 @@ FP64, MIXED = range(2)
 # enum hydro_field
 (F_VELOCITY, F_PRESSURE, F_VOLUME_FLUX, F_PARTIAL_DENSITY, F_VOLUME_FRACTION,
  F_DENSITY, F_VISCOSITY, F_FORCE, F_VOLUME_SOURCE, F_MASS_SOURCE,
- F_PRESSURE_CORRECTION, F_DIAG_COEFF, F_SURFACE_FORCE) = range(13)
+ F_PRESSURE_CORRECTION, F_DIAG_COEFF, F_SURFACE_FORCE, F_TEMPERATURE,
+ F_CONDUCTIVITY) = range(15)
 VECTOR_FIELDS = (F_VELOCITY, F_FORCE, F_SURFACE_FORCE)
 # enum hydro_layer (solver::Layers order)
 TIME_CURR, TIME_PREV, ITER_CURR, ITER_PREV = range(4)
@@ -134,6 +135,55 @@ class StepStats(ctypes.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class HeatDesc(ctypes.Structure):
+    _fields_ = [
+        ("temperature_initial", ctypes.c_double),
+        ("conductivity", ctypes.c_double * HYDRO_MAX_PHASES),
+        ("box_lo", ctypes.c_double * 3),
+        ("box_hi", ctypes.c_double * 3),
+        ("box_temperature", ctypes.c_double),
+        ("relaxation_factor", ctypes.c_double),
+        ("time_second_order", ctypes.c_int),
+        ("solver", ctypes.c_int),
+        ("tolerance", ctypes.c_double),
+        ("iters_limit", ctypes.c_int),
+        ("dt", ctypes.c_double),
+    ]
+
+
+def heat_to_dict(h):
+    out = {}
+    for name, _ in HeatDesc._fields_:
+        v = getattr(h, name)
+        out[name] = list(v) if hasattr(v, "__len__") else v
+    return out
+
+
+def heat_from_dict(dct):
+    h = HeatDesc()
+    for name, v in dct.items():
+        if isinstance(v, list):
+            arr = getattr(h, name)
+            for i, e in enumerate(v):
+                arr[i] = e
+        else:
+            setattr(h, name, v)
+    return h
+
+
+def default_heat_desc(dt):
+    """examples/general.hydroconf:80-91 (heat_relaxation_factor 1,
+    time_second_order_heat 1), Jacobi sweeps to 1e-12, the given dt."""
+    h = HeatDesc()
+    h.relaxation_factor = 1.0
+    h.time_second_order = 1
+    h.solver = LINEAR_JACOBI
+    h.tolerance = 1e-12
+    h.iters_limit = 10000
+    h.dt = dt
+    return h
 
 
 class Stat(ctypes.Structure):
@@ -305,6 +355,8 @@ def _declare(lib, prefix):
             "hydro_gpu_get_desc": [P, ctypes.POINTER(HydroDesc)],
             "hydro_gpu_get_stream": [P, ctypes.POINTER(P)],
             "hydro_gpu_get_time_step": [P, D],
+            "hydro_gpu_heat_create": [P, ctypes.POINTER(HeatDesc)],
+            "hydro_gpu_heat_step": [P],
             "hydro_output_open": [P, C, C, ctypes.POINTER(P)],
             "hydro_output_write": [P, ctypes.c_double],
             "hydro_output_flush": [P],

@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <new>
 #include <utility>
 #include <vector>
@@ -176,8 +177,21 @@ struct hydro_ctx {
   struct StepGraph {
     cudaGraphExec_t exec = nullptr;
     double dt = -1., adv_dt = -1.;
-    int substeps = -1, sources = -1;
+    int substeps = -1, sources = -1, heat_gen = -1;
   } sg;
+  // temperature (HeatSolver, heat.hpp:18-94; hydro_gpu_heat_create): its
+  // two time layers and the mixture conductivity; the step's gradient,
+  // rows and Jacobi iterates use the momentum work arrays G, coef, res and
+  // du, free once the fluid step has finished
+  struct HeatState {
+    bool on = false;
+    int gen = 0;  // bumped by every hydro_gpu_heat_create
+    hydro_heat_desc hd{};
+    HeatBc bc{};
+    HeatCoef hc{};
+    double* mem = nullptr;
+    double *tc = nullptr, *tp = nullptr, *kc = nullptr;
+  } heat;
   PcgWork pw{};
   double* stat_out = nullptr;
   unsigned* stat_ticket = nullptr;
@@ -433,6 +447,53 @@ int solve_momentum(hydro_ctx* x) {
   return HYDRO_OK;
 }
 
+// ----------------------------------------------------------------- heat --
+// One HeatSolver step (StartStep, one MakeIteration, FinishStep): rows of
+// the temperature equation around T_curr, Jacobi sweeps to the heat
+// tolerance (a WHILE node in a captured step, chunks between host checks
+// otherwise), then T_prev <- T_curr <- T_curr + correction.
+int heat_step(hydro_ctx* x) {
+  const Mesh& m = x->m;
+  auto& h = x->heat;
+  const int dim = x->dim;
+  int rc = reset_flags(x, FL_HEAT_DONE, 2);
+  if (rc) return rc;
+  CK(launch_heat_grad(m, h.bc, h.tc, x->vec<W3>(x->G, dim, m.nc), x->st));
+  CK(launch_heat_assemble(m, h.bc, h.hc, h.tc, h.tc, h.tp, x->F[HYDRO_ITER_CURR], h.kc,
+                          x->vec<C3>(x->G, dim, m.nc), x->vec<WP<7>>(x->coef, 2 * dim + 1, m.nc),
+                          x->res, x->st));
+  CP<7> cc = x->vec<CP<7>>(x->coef, 2 * dim + 1, m.nc);
+  const int limit = h.hd.iters_limit + 1;
+  auto sweep = [&](int k) -> int {
+    CK(launch_heat_sweep(m, h.hd.tolerance, cc, x->res, x->du[(k + 1) % 2], x->du[k % 2], limit,
+                         x->pw.partials, x->pw.ds, x->st));
+    return HYDRO_OK;
+  };
+  if (x->graph_mode) {
+    cudaGraphConditionalHandle hc;
+    if ((rc = new_handle(x, 1, &hc))) return rc;
+    rc = add_loop(x, hc, [&]() -> int {
+      int r;
+      if ((r = sweep(0)) || (r = sweep(1))) return r;
+      CK(launch_ctl_heat(x->pw.ds, limit, hc, 1, x->st));
+      return HYDRO_OK;
+    });
+    if (rc) return rc;
+  } else {
+    int queued = 0;
+    for (;;) {
+      int n = std::min(kSweepChunk, limit - queued);
+      for (int s = 0; s < n; ++s)
+        if ((rc = sweep(queued + s))) return rc;
+      queued += n;
+      if ((rc = sync_scalars(x))) return rc;
+      if (x->hds->flag[FL_HEAT_DONE] || queued >= limit) break;
+    }
+  }
+  CK(launch_heat_finish(m.nc, h.tc, h.tp, x->du[0], x->du[1], x->pw.ds, x->st));
+  return HYDRO_OK;
+}
+
 // ------------------------------------------------------------- pressure --
 // Graph-captured form of the pressure solve: the refinement and Krylov loops
 // become WHILE nodes steered by the control kernels.
@@ -591,6 +652,15 @@ int fluid_field(hydro_ctx* x, int field, int layer, double** ptr, long long* n) 
     case HYDRO_FIELD_PRESSURE_CORRECTION: *ptr = x->pc; return HYDRO_OK;
     case HYDRO_FIELD_DIAG_COEFF: *ptr = x->Dc; return HYDRO_OK;
     case HYDRO_FIELD_SURFACE_FORCE: *ptr = x->stforce; *n = m.nc * x->dim; return HYDRO_OK;
+    case HYDRO_FIELD_TEMPERATURE:
+      if (!x->heat.on) return HYDRO_ERR_ARG;
+      if (layer == HYDRO_TIME_CURR) { *ptr = x->heat.tc; return HYDRO_OK; }
+      if (layer == HYDRO_TIME_PREV) { *ptr = x->heat.tp; return HYDRO_OK; }
+      return HYDRO_ERR_ARG;
+    case HYDRO_FIELD_CONDUCTIVITY:
+      if (!x->heat.on) return HYDRO_ERR_ARG;
+      *ptr = x->heat.kc;
+      return HYDRO_OK;
   }
   return HYDRO_ERR_ARG;
 }
@@ -842,6 +912,7 @@ int hydro_gpu_destroy(hydro_ctx* x) {
   for (auto& cs : x->cap_streams)
     if (cs) cudaStreamDestroy(cs);
   if (x->arena.base) cudaFree(x->arena.base);
+  if (x->heat.mem) cudaFree(x->heat.mem);
   if (x->hds) cudaFreeHost(x->hds);
   if (x->own_stream && x->st) cudaStreamDestroy(x->st);
   delete x;
@@ -936,6 +1007,10 @@ int hydro_gpu_update_properties(hydro_ctx* x) {
     rc = smooth(x->force + (size_t)k * m.nc, d.force_smooth_times);
     if (rc) return rc;
   }
+  if (x->heat.on)
+    CK(launch_heat_conductivity(m, x->nph, x->heat.hc,
+                                x->vec<CP<HYDRO_MAXPH>>(x->alpha, x->nph, m.nc), x->heat.kc,
+                                x->st));
   CK(cudaGetLastError());
   return HYDRO_OK;
 }
@@ -1262,6 +1337,8 @@ int hydro_gpu_step(hydro_ctx* x, hydro_step_stats* stats) {
     rc = hydro_gpu_advection_step(x, &s.advection_substeps);
     if (rc) return rc;
   }
+  // heat after advection (hydro2d.hpp:1607-1613)
+  if (x->heat.on && (rc = heat_step(x))) return rc;
   rc = hydro_gpu_update_properties(x);
   if (rc) return rc;
   s.dt = x->dt;
@@ -1384,6 +1461,7 @@ int enqueue_step_body(hydro_ctx* x, int substeps) {
                          x->st));
       std::swap(x->q, x->qtmp);
     }
+    if (x->heat.on && (r = heat_step(x))) return r;
     if ((r = hydro_gpu_update_properties(x))) return r;
     CK(launch_auto_dt(m, x->F[HYDRO_TIME_CURR], x->pw.partials, x->pw.ds, x->st));
     return HYDRO_OK;
@@ -1442,7 +1520,7 @@ int next_dt(hydro_ctx* x) {
 
 bool graph_stale(const hydro_ctx* x, int substeps) {
   return x->sg.dt != x->dt || x->sg.adv_dt != x->adv_dt || x->sg.substeps != substeps ||
-         x->sg.sources != x->fc.sources;
+         x->sg.sources != x->fc.sources || x->sg.heat_gen != x->heat.gen;
 }
 
 void graph_key(hydro_ctx* x, int substeps) {
@@ -1450,6 +1528,7 @@ void graph_key(hydro_ctx* x, int substeps) {
   x->sg.adv_dt = x->adv_dt;
   x->sg.substeps = substeps;
   x->sg.sources = x->fc.sources;
+  x->sg.heat_gen = x->heat.gen;
 }
 
 // After a graph launch completed and x->hds holds the device scalars.
@@ -1657,6 +1736,72 @@ int hydro_gpu_batch_step(hydro_batch* b, hydro_step_stats* stats) {
     if (rc && !status) status = rc;
   }
   return status;
+}
+
+// --------------------------------------------------------------- heat --
+int hydro_gpu_heat_create(hydro_ctx* x, const hydro_heat_desc* hd) {
+  if (!x || !hd) return HYDRO_ERR_ARG;
+  if (!(hd->dt > 0.) || !(hd->relaxation_factor > 0.) || hd->iters_limit < 0 ||
+      !(hd->tolerance >= 0.) || !std::isfinite(hd->box_temperature) ||
+      !std::isfinite(hd->temperature_initial))
+    return HYDRO_ERR_ARG;
+  if (hd->solver != HYDRO_LINEAR_JACOBI && hd->solver != HYDRO_LINEAR_GAUSS_SEIDEL &&
+      hd->solver != HYDRO_LINEAR_LU)
+    return HYDRO_ERR_ARG;
+  const Mesh& m = x->m;
+  auto& h = x->heat;
+  if (!h.mem) {
+    if (cudaMalloc(&h.mem, sizeof(double) * 3 * m.nc) != cudaSuccess) {
+      cudaGetLastError();
+      h.mem = nullptr;
+      return HYDRO_ERR_NOMEM;
+    }
+    h.tc = h.mem;
+    h.tp = h.mem + m.nc;
+    h.kc = h.mem + 2 * m.nc;
+  }
+  h.hd = *hd;
+  // boundary faces in the box: centre coordinates as the mesh forms them
+  // (node lo + i h along the face normal, cell centre lo + (i + 1/2) h
+  // across), compared inclusively with the box
+  HeatBc bc{};
+  auto inside = [&](int k, double v) { return hd->box_lo[k] <= v && v <= hd->box_hi[k]; };
+  for (int k = 0; k < 3; ++k) {
+    bc.a[k] = 0;
+    bc.b[k] = 0;
+    if (k >= x->dim) continue;
+    int first = -1, last = -2;
+    for (int i = 0; i < m.n[k]; ++i)
+      if (inside(k, m.lo[k] + (i + 0.5) * m.h[k])) {
+        if (first < 0) first = i;
+        last = i;
+      }
+    if (first >= 0) {
+      bc.a[k] = first;
+      bc.b[k] = last + 1;
+    }
+    bc.side_in[2 * k] = inside(k, m.lo[k]);
+    bc.side_in[2 * k + 1] = inside(k, m.lo[k] + m.n[k] * m.h[k]);
+  }
+  bc.value = hd->box_temperature;
+  h.bc = bc;
+  for (int i = 0; i < HYDRO_MAXPH; ++i) h.hc.cond[i] = i < x->nph ? hd->conductivity[i] : 0.;
+  bdf_coeffs(hd->dt, hd->time_second_order, h.hc.co);
+  h.hc.relax = hd->relaxation_factor;
+  std::vector<double> t0((size_t)m.nc, hd->temperature_initial);
+  CK(cudaMemcpyAsync(h.tc, t0.data(), sizeof(double) * m.nc, cudaMemcpyHostToDevice, x->st));
+  CK(cudaMemcpyAsync(h.tp, t0.data(), sizeof(double) * m.nc, cudaMemcpyHostToDevice, x->st));
+  CK(launch_heat_conductivity(m, x->nph, h.hc, x->vec<CP<HYDRO_MAXPH>>(x->alpha, x->nph, m.nc),
+                              h.kc, x->st));
+  CK(cudaStreamSynchronize(x->st));
+  h.on = true;
+  h.gen += 1;  // a captured step holds the old constants
+  return HYDRO_OK;
+}
+
+int hydro_gpu_heat_step(hydro_ctx* x) {
+  if (!x || !x->heat.on) return HYDRO_ERR_ARG;
+  return heat_step(x);
 }
 
 int hydro_gpu_calc_stat(hydro_ctx* x, hydro_stat* out) {

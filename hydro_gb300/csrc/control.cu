@@ -30,6 +30,11 @@ __global__ void k_ctl_sweeps(DevScalars* ds, int limit, cudaGraphConditionalHand
   decide(ds, cont, h, use);
 }
 
+__global__ void k_ctl_heat(DevScalars* ds, int limit, cudaGraphConditionalHandle h, int use) {
+  if (threadIdx.x != 0) return;
+  decide(ds, !(ds->flag[FL_HEAT_DONE] || ds->flag[FL_HEAT_SWEEPS] >= limit), h, use);
+}
+
 __global__ void k_ctl_krylov(DevScalars* ds, cudaGraphConditionalHandle h, int use) {
   if (threadIdx.x != 0) return;
   decide(ds, !ds->flag[FL_PCG_DONE], h, use);
@@ -133,6 +138,13 @@ int copy_blocks(long long n) {
 cudaError_t launch_ctl_sweeps(DevScalars* ds, int limit, cudaGraphConditionalHandle h, int use,
                               cudaStream_t st) {
   k_ctl_sweeps<<<1, 32, 0, st>>>(ds, limit, h, use);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ctl_heat(DevScalars* ds, int limit, cudaGraphConditionalHandle h, int use,
+                            cudaStream_t st) {
+  k_ctl_heat<<<1, 32, 0, st>>>(ds, limit, h, use);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -72,7 +72,8 @@ enum {
   RS_INNER_TOL = 15,     // tolerance of the next inner solve (device-driven refinement)
   RS_P_RES = 16,         // relative pressure residual of the last solve
   RS_IR_FF = 17,         // refinement: ||f||^2 of the first residual
-  RS_OUT_FLUX = 18, RS_OUT_AREA = 19, RS_IN_FLUX = 20  // outlet rebalancing sums
+  RS_OUT_FLUX = 18, RS_OUT_AREA = 19, RS_IN_FLUX = 20,  // outlet rebalancing sums
+  RS_HEAT_DIFF = 21      // max |update| of the last temperature sweep
 };
 enum {
   FL_MOM_DONE = 0, FL_MOM_SWEEPS = 1, FL_PCG_DONE = 2, FL_PCG_ITERS = 3, FL_NAN = 4,
@@ -83,13 +84,14 @@ enum {
   FL_STEP_PITERS = 9,    // pressure iterations of the step
   FL_ITERS = 10,         // SIMPLE iterations of the step
   FL_IR_OUTER = 11,      // refinement cycles
-  FL_CONT = 12           // last loop decision
+  FL_CONT = 12,          // last loop decision
+  FL_HEAT_DONE = 13, FL_HEAT_SWEEPS = 14  // temperature solve
 };
 enum {
   TK_MOM = 0, TK_PCG_A = 1, TK_PCG_B = 2, TK_PCG_INIT = 3, TK_IND = 4, TK_DT = 5,
   TK_MEAN = 6, TK_MEAN2 = 7, TK_STAT = 8, TK_STAT2 = 9, TK_STAT3 = 10, TK_IR = 11,
   TK_NAN = 12, TK_PCG_INIT2 = 13, TK_F32_A = 14, TK_F32_B = 15, TK_F32_INIT = 16,
-  TK_OUTLET = 17
+  TK_OUTLET = 17, TK_HEAT = 18
 };
 
 // ---------------------------------------------------------------- fluid --
@@ -180,6 +182,47 @@ cudaError_t launch_stforce(const Mesh& m, double sigma, const double* alpha1, W3
 cudaError_t launch_stat(const Mesh& m, const double* q, const double* alpha, C3 u,
                         const double* F, double* partials, double* out, unsigned* ticket,
                         cudaStream_t st);
+
+// ----------------------------------------------------------------- heat --
+// Temperature boundary condition (hydro2d.hpp:660-677): a boundary face
+// holds the box temperature when its centre lies in the heat box
+// (Rect::IsInside, inclusive, vect.hpp:239-246), else a zero derivative.
+// Face centres on a side share that side's coordinate and the transverse
+// cell-centre coordinates, so the faces inside are: the sides whose plane
+// meets the box (side_in) and, on them, transverse cell indices i_k in
+// [a[k], b[k]).
+struct HeatBc {
+  int side_in[6];
+  int a[3], b[3];
+  double value;
+};
+struct HeatCoef {
+  double cond[HYDRO_MAXPH];  // conductivity per phase
+  double co[3];              // BDF coefficients of the heat time step
+  double relax;              // heat_relaxation_factor
+};
+// conductivity kc = sum_i k_i alpha_i (hydro2d.hpp:1428)
+cudaError_t launch_heat_conductivity(const Mesh& m, int nph, const HeatCoef& hc,
+                                     CP<HYDRO_MAXPH> alpha, double* kc, cudaStream_t st);
+// cell gradient of T with faces carrying the temperature condition
+cudaError_t launch_heat_grad(const Mesh& m, const HeatBc& bc, const double* T, W3 G,
+                             cudaStream_t st);
+// delta-form rows of the temperature equation around T_prev
+// (ConvectionDiffusionScalarImplicit::MakeIteration, conv_diff.hpp:130-251):
+// coef = [1/(aP/relax), 2*DIM off-diagonals], res = equation at T_prev
+cudaError_t launch_heat_assemble(const Mesh& m, const HeatBc& bc, const HeatCoef& hc,
+                                 const double* Tp, const double* Ttc, const double* Ttp,
+                                 const double* F, const double* kc, C3 G, WP<7> coef,
+                                 double* res, cudaStream_t st);
+// Jacobi sweep of the temperature correction (omega 1), the same exit
+// rules as launch_mom_sweep on FL_HEAT_DONE / FL_HEAT_SWEEPS
+cudaError_t launch_heat_sweep(const Mesh& m, double tol, CP<7> coef, const double* res,
+                              const double* din, double* dout, int limit, double* partials,
+                              DevScalars* ds, cudaStream_t st);
+// T_prev <- T_curr, T_curr <- T_curr + du, du the buffer the last sweep
+// wrote (du0 after an odd number of sweeps, else du1)
+cudaError_t launch_heat_finish(long long n, double* tc, double* tp, const double* du0,
+                               const double* du1, const DevScalars* ds, cudaStream_t st);
 
 // ------------------------------------------------------------ advection --
 // Face fluxes q_f F_f of every phase (Superbee, solver.hpp:550-619) on the
@@ -296,6 +339,9 @@ cudaError_t pin_rhs(const Mesh& m, const double* kf, double* f, long long pin, d
 cudaError_t launch_ctl_sweeps(DevScalars* ds, int limit, cudaGraphConditionalHandle h, int use,
                               cudaStream_t st);
 // Krylov inner loop: continue while not done.
+// The temperature sweep loop (FL_HEAT_DONE / FL_HEAT_SWEEPS).
+cudaError_t launch_ctl_heat(DevScalars* ds, int limit, cudaGraphConditionalHandle h, int use,
+                            cudaStream_t st);
 cudaError_t launch_ctl_krylov(DevScalars* ds, cudaGraphConditionalHandle h, int use,
                               cudaStream_t st);
 // Refinement cycle after a residual: records ||f||^2 on the first call,

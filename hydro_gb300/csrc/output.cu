@@ -33,7 +33,7 @@ namespace {
 enum Src {
   S_NODE_X, S_NODE_Y, S_NODE_Z, S_VEL, S_PRESSURE, S_DENSITY, S_VISCOSITY, S_VOLUME_SOURCE,
   S_EXCLUDED, S_DIVERGENCE, S_MASS_FRACTION, S_TRUE_DENSITY, S_PARTIAL_DENSITY,
-  S_VOLUME_FRACTION
+  S_VOLUME_FRACTION, S_TEMPERATURE
 };
 
 struct Entry {
@@ -120,8 +120,9 @@ int write_file(const std::string& path, const std::string& text) {
 }
 
 // Reference entry order (content_pool, hydro2d.hpp:710-816); phases are
-// expanded per group.  Names outside the hot path (radiation, temperature,
-// mass_source_i, target_density_i) are not produced here.
+// expanded per group.  "temperature" needs hydro_gpu_heat_create.  Names
+// outside the hot path (radiation, mass_source_i, target_density_i) are not
+// produced here.
 std::vector<Entry> all_entries(int nph) {
   std::vector<Entry> v = {
       {"x", S_NODE_X, 0},          {"y", S_NODE_Y, 1},
@@ -129,6 +130,7 @@ std::vector<Entry> all_entries(int nph) {
       {"velocity_y", S_VEL, 1},    {"velocity_z", S_VEL, 2},
       {"pressure", S_PRESSURE, 0}, {"density", S_DENSITY, 0},
       {"viscosity", S_VISCOSITY, 0}, {"volume_source", S_VOLUME_SOURCE, 0},
+      {"temperature", S_TEMPERATURE, 0},
       {"excluded", S_EXCLUDED, 0}, {"divergence", S_DIVERGENCE, 0}};
   const char* groups[4] = {"mass_fraction_", "density_", "partial_density_", "volume_fraction_"};
   const Src gs[4] = {S_MASS_FRACTION, S_TRUE_DENSITY, S_PARTIAL_DENSITY, S_VOLUME_FRACTION};
@@ -212,6 +214,7 @@ struct hydro_output {
   int frame = 0;
   // staging: pinned host copies of the device arrays a frame needs
   double *h_u = nullptr, *h_p = nullptr, *h_rho = nullptr, *h_mu = nullptr, *h_sv = nullptr;
+  double* h_T = nullptr;
   double *h_F = nullptr, *h_q = nullptr, *h_a = nullptr;
   std::vector<double> nodes[3];
   cudaStream_t st = nullptr;
@@ -262,6 +265,7 @@ void hydro_output::run() {
           case S_DENSITY: p = h_rho; break;
           case S_VISCOSITY: p = h_mu; break;
           case S_VOLUME_SOURCE: p = h_sv; break;
+          case S_TEMPERATURE: p = h_T; break;
           case S_EXCLUDED: tmp.emplace_back(nc, 0.); p = tmp.back().data(); break;
           case S_PARTIAL_DENSITY: p = h_q + (size_t)e.comp * nc; break;
           case S_VOLUME_FRACTION: p = h_a + (size_t)e.comp * nc; break;
@@ -331,7 +335,7 @@ void free_output(hydro_output* o) {
     o->cv.notify_all();
     o->worker.join();
   }
-  double* hs[] = {o->h_u, o->h_p, o->h_rho, o->h_mu, o->h_sv, o->h_F, o->h_q, o->h_a};
+  double* hs[] = {o->h_u, o->h_p, o->h_rho, o->h_mu, o->h_sv, o->h_F, o->h_q, o->h_a, o->h_T};
   for (double* h : hs)
     if (h) cudaFreeHost(h);
   if (o->ready) cudaEventDestroy(o->ready);
@@ -352,6 +356,10 @@ extern "C" int hydro_output_open(hydro_ctx* ctx, const char* basename, const cha
   o->ctx = ctx;
   int rc = hydro_gpu_get_desc(ctx, &o->d);
   if (!rc) rc = select_entries(fields, o->d.dim, o->d.num_phases, &o->ents);
+  if (!rc && o->need(S_TEMPERATURE)) {
+    double* t = nullptr;  // the temperature exists once heat is attached
+    rc = hydro_gpu_field_ptr(ctx, HYDRO_FIELD_TEMPERATURE, HYDRO_TIME_CURR, &t);
+  }
   if (rc) {
     delete o;
     return rc;
@@ -395,6 +403,7 @@ extern "C" int hydro_output_open(hydro_ctx* ctx, const char* basename, const cha
   if (o->need(S_DENSITY) || o->need(S_MASS_FRACTION)) pin(&o->h_rho, nc);
   if (o->need(S_VISCOSITY)) pin(&o->h_mu, nc);
   if (o->need(S_VOLUME_SOURCE)) pin(&o->h_sv, nc);
+  if (o->need(S_TEMPERATURE)) pin(&o->h_T, nc);
   if (o->need(S_DIVERGENCE)) pin(&o->h_F, nf);
   if (o->need(S_PARTIAL_DENSITY) || o->need(S_MASS_FRACTION)) pin(&o->h_q, nc * nph);
   if (o->need(S_VOLUME_FRACTION)) pin(&o->h_a, nc * nph);
@@ -449,6 +458,7 @@ extern "C" int hydro_output_write(hydro_output* o, double time) {
       (rc = copy(o->h_rho, HYDRO_FIELD_DENSITY, HYDRO_TIME_CURR, nc)) ||
       (rc = copy(o->h_mu, HYDRO_FIELD_VISCOSITY, HYDRO_TIME_CURR, nc)) ||
       (rc = copy(o->h_sv, HYDRO_FIELD_VOLUME_SOURCE, HYDRO_TIME_CURR, nc)) ||
+      (rc = copy(o->h_T, HYDRO_FIELD_TEMPERATURE, HYDRO_TIME_CURR, nc)) ||
       (rc = copy(o->h_F, HYDRO_FIELD_VOLUME_FLUX, HYDRO_TIME_CURR, nf)) ||
       (rc = copy(o->h_q, HYDRO_FIELD_PARTIAL_DENSITY, HYDRO_TIME_CURR, nc * nph)) ||
       (rc = copy(o->h_a, HYDRO_FIELD_VOLUME_FRACTION, HYDRO_TIME_CURR, nc * nph)))

@@ -171,6 +171,21 @@ class Hydro:
         self._call("calc_stat", ctypes.byref(s))
         return s
 
+    # ---- temperature (HeatSolver, heat.hpp:18-94)
+    def heat_create(self, heat):
+        """Attach the temperature equation (hydro_gpu_heat_create); every
+        step then advances it once after advection."""
+        self.heat = capi.HeatDesc.from_buffer_copy(heat)
+        self._call("heat_create", ctypes.byref(self.heat))
+
+    def heat_step(self):
+        self._call("heat_step")
+
+    def temperature(self, layer=capi.TIME_CURR):
+        return self.get_field(capi.F_TEMPERATURE, layer)
+
+    GetTemperature = temperature
+
     # ---- measurement hooks
     def set_profiling(self, on):
         self._call("set_profiling", 1 if on else 0)

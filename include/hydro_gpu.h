@@ -34,6 +34,9 @@
  *                           Finish (advection.hpp:417-545)
  *   hydro_gpu_step          hydro<Mesh>::step (hydro2d.hpp:1531-1621)
  *   hydro_gpu_calc_stat     hydro<Mesh>::CalcStat (hydro2d.hpp:1432-1529)
+ *   hydro_gpu_heat_create   hydro<Mesh>::InitHeatSolver (hydro2d.hpp:650-687)
+ *   hydro_gpu_heat_step     HeatSolver StartStep/CalcStep/FinishStep
+ *                           (heat.hpp:18-94, driven at hydro2d.hpp:1607-1613)
  *   hydro_gpu_get_field / hydro_gpu_set_field
  *                           FluidSolver::GetVelocity/GetPressure/GetVolumeFlux
  *                           (fluid.hpp:244-249), AdvectionSolverMulti::GetField
@@ -103,7 +106,12 @@ enum hydro_field {
   HYDRO_FIELD_MASS_SOURCE = 9,     /* cells */
   HYDRO_FIELD_PRESSURE_CORRECTION = 10, /* cells: last p' solved */
   HYDRO_FIELD_DIAG_COEFF = 11,     /* cells: last momentum diagonal D_c (fluid.hpp:876-883) */
-  HYDRO_FIELD_SURFACE_FORCE = 12   /* cells x dim: surface-tension force (p_fc_stforce) */
+  HYDRO_FIELD_SURFACE_FORCE = 12,  /* cells x dim: surface-tension force (p_fc_stforce) */
+  HYDRO_FIELD_TEMPERATURE = 13,    /* cells, layers TIME_CURR / TIME_PREV, after
+                                      hydro_gpu_heat_create (HeatSolver::GetTemperature,
+                                      heat.hpp:88-93) */
+  HYDRO_FIELD_CONDUCTIVITY = 14    /* cells, after hydro_gpu_heat_create: mixture
+                                      conductivity (fc_conductivity, hydro2d.hpp:1428) */
 };
 
 /* Same order as solver::Layers (solver.hpp:762). */
@@ -137,9 +145,11 @@ typedef struct hydro_desc {
   double meshvel[3];
   double convergence_tolerance; /* SIMPLE: max |u_s - u_{s-1}| */
   int num_iterations_limit;     /* SIMPLE outer iterations per step */
-  int simpler;                  /* must be 0: SIMPLER branch is not built */
+  int simpler;                  /* SIMPLER pressure (fluid.hpp:1059-1155); FP64 only */
 
-  int velocity_solver;          /* enum hydro_linear */
+  int velocity_solver;          /* enum hydro_linear; the GPU sweeps Jacobi for all three
+                                   (the parallel one): with a tight velocity_tolerance the
+                                   three reach the same solution */
   double velocity_tolerance;    /* max |update| per sweep */
   int velocity_iters_limit;
   double velocity_omega;        /* relaxation of the sweep */
@@ -201,6 +211,26 @@ typedef struct hydro_stat {
 
 typedef struct hydro_ctx hydro_ctx;
 
+/* HeatSolver (heat.hpp:18-94) as hydro<Mesh>::InitHeatSolver sets it up
+ * (hydro2d.hpp:650-687): temperature by ConvectionDiffusionScalarImplicit
+ * with unit scaling, the fluid's volume fluxes and a face conductivity
+ * interpolated from the mixture conductivity sum_i alpha_i k_i
+ * (hydro2d.hpp:1428); boundary faces whose centre lies in [box_lo, box_hi]
+ * (inclusive) hold box_temperature, the others zero derivative; one
+ * iteration per step (the module creates it with limit 1). */
+typedef struct hydro_heat_desc {
+  double temperature_initial;
+  double conductivity[HYDRO_MAX_PHASES];
+  double box_lo[3], box_hi[3];
+  double box_temperature;
+  double relaxation_factor;     /* heat_relaxation_factor */
+  int time_second_order;        /* time_second_order_heat */
+  int solver;                   /* enum hydro_linear (the GPU uses Jacobi sweeps) */
+  double tolerance;
+  int iters_limit;
+  double dt;                    /* the solver keeps the time step it is created with */
+} hydro_heat_desc;
+
 /* Fill *d with the defaults of examples/general.hydroconf for the keys above
  * (2D 100x100 unit square, walls, dt 0.01, relaxations 0.8/0.9, ...). */
 int hydro_desc_default(hydro_desc* d);
@@ -258,6 +288,19 @@ int hydro_gpu_step(hydro_ctx* ctx, hydro_step_stats* stats);
  * ITER_PREV; the time layers are as after hydro_gpu_step. */
 int hydro_gpu_step_graph(hydro_ctx* ctx, hydro_step_stats* stats);
 int hydro_gpu_calc_stat(hydro_ctx* ctx, hydro_stat* out);
+
+/* ---- temperature ------------------------------------------------------
+ * Attach a HeatSolver to the context: both temperature layers take
+ * temperature_initial and the conductivity is computed from the current
+ * volume fractions (call after hydro_gpu_init_state).  From then on every
+ * step (hydro_gpu_step, hydro_gpu_step_graph, batch steps) advances the
+ * temperature once after advection, with the fluid's final volume fluxes,
+ * and the property update refreshes the conductivity.  A second call
+ * re-initialises it with the new description.  The linear solve is Jacobi
+ * sweeps for every `solver` value (tight tolerance: the same solution). */
+int hydro_gpu_heat_create(hydro_ctx* ctx, const hydro_heat_desc* hd);
+/* One temperature step alone (what the steps above run after advection). */
+int hydro_gpu_heat_step(hydro_ctx* ctx);
 
 /* ---- many independent cases ------------------------------------------
  * A batch of independent cases of uneven size (one hydro_desc each, e.g.

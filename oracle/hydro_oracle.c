@@ -59,6 +59,13 @@ struct oracle_ctx {
   /* momentum rows of the iteration per component (kept for SIMPLER) */
   double* mrows[3];
   double* mrowc[3];
+  /* heat (HeatSolver, heat.hpp:18-94), when attached */
+  int heat_on;
+  hydro_heat_desc hd;
+  double* T[4];            /* temperature layers */
+  double* kc;              /* mixture conductivity (hydro2d.hpp:1428) */
+  double* tbval;           /* boundary temperature of box faces */
+  unsigned char* tbder;    /* boundary faces with zero derivative */
   /* scratch */
   double* fw[10];   /* face arrays */
   double* cw[24];   /* cell arrays */
@@ -642,6 +649,8 @@ int oracle_destroy(oracle_ctx* x) {
   free(x->pcorr); free(x->Dc);
   for (int k = 0; k < 3; ++k) free(x->bcu[k]);
   for (int k = 0; k < 3; ++k) { free(x->mrows[k]); free(x->mrowc[k]); }
+  for (int l = 0; l < 4; ++l) free(x->T[l]);
+  free(x->kc); free(x->tbval); free(x->tbder);
   for (int i = 0; i < HYDRO_MAX_PHASES; ++i) free(x->qin[i]);
   for (int i = 0; i < 10; ++i) free(x->fw[i]);
   for (int i = 0; i < 24; ++i) free(x->cw[i]);
@@ -781,6 +790,14 @@ int oracle_update_properties(oracle_ctx* x) {
     }
   }
   for (int k = 0; k < dim; ++k) smooth(m, x->force[k], d->force_smooth_times, x->fw[0]);
+  if (x->heat_on) {
+    /* fc_conductivity = sum_i alpha_i k_i (hydro2d.hpp:1428) */
+    for (long c = 0; c < m->nc; ++c) {
+      double s = 0.;
+      for (int i = 0; i < nph; ++i) s += x->hd.conductivity[i] * x->alpha[i][c];
+      x->kc[c] = s;
+    }
+  }
   return HYDRO_OK;
 }
 
@@ -879,19 +896,46 @@ static void bdf_coeffs(double dt, int second, double* co) {
 /* One velocity component: ConvectionDiffusionScalarImplicit::MakeIteration
  * (conv_diff.hpp:130-251) assembly.  Writes rows/rowc (delta form, relaxed)
  * and returns nothing; u_prev is the iteration's starting field. */
+/* Scalar form: scaling (NULL = 1) multiplies the unsteady and convective
+ * terms, dfr is the face diffusion rate, bcval the per-face boundary
+ * values; bcderiv (NULL = none) marks boundary faces with a zero-derivative
+ * condition instead (InterpolationBoundaryFaceNearestCell /
+ * DerivativeBoundaryFacePlain, solver.hpp:246-341). */
+static void assemble_scalar(oracle_ctx* x, const double* u_prev, const double* u_tc,
+                            const double* u_tp, const double* Fp, const double* dfr,
+                            const double* src, const double* scaling, const double* bcval,
+                            const unsigned char* bcderiv, double dt, int second_order,
+                            double relax);
+
 static void assemble_momentum(oracle_ctx* x, int n, const double* u_prev,
                               const double* u_tc, const double* u_tp,
                               const double* Fp, const double* muf,
                               const double* src) {
+  assemble_scalar(x, u_prev, u_tc, u_tp, Fp, muf, src, x->rho, x->bcu[n], NULL, x->dt,
+                  x->d.time_second_order, x->d.velocity_relaxation_factor);
+}
+
+static void assemble_scalar(oracle_ctx* x, const double* u_prev, const double* u_tc,
+                            const double* u_tp, const double* Fp, const double* muf,
+                            const double* src, const double* scaling, const double* bcval,
+                            const unsigned char* bcderiv, double dt, int second_order,
+                            double relax) {
   const Mesh* m = &x->m;
   int dim = m->dim, w = 2 * dim + 1;
   double* ff = x->fw[5];
   double* gc[3] = {x->cw[3], x->cw[4], x->cw[5]};
-  interp(m, u_prev, ff, BC_FACE, x->bcu[n], 0);
+  interp(m, u_prev, ff, BC_FACE, bcval, 0);
+  if (bcderiv)
+    for (long f = 0; f < m->nf; ++f)
+      if (bcderiv[f]) {
+        int dd;
+        long mi[3], cm, cp;
+        fdecode(m, f, &dd, mi, &cm, &cp);
+        ff[f] = u_prev[cm >= 0 ? cm : cp];
+      }
   gradient(m, ff, gc);
   double co[3];
-  bdf_coeffs(x->dt, x->d.time_second_order, co);
-  double relax = x->d.velocity_relaxation_factor;
+  bdf_coeffs(dt, second_order, co);
   long c;
 #pragma omp parallel for num_threads(g_threads)
   for (c = 0; c < m->nc; ++c) {
@@ -928,10 +972,14 @@ static void assemble_momentum(oracle_ctx* x, int n, const double* u_prev,
         double mA = -muf[fq];
         dfl[sm] += ((-al) * mA * m->A[d]) * s;
         dfl[sp] += ((al) * mA * m->A[d]) * s;
+      } else if (bcderiv && bcderiv[fq]) {
+        /* boundary with a zero-derivative condition: the face value is
+           the cell's (coefficient 1), no diffusive flux */
+        cfl[sc] += (1. * Ff) * s;
       } else {
         /* boundary: InterpolationBoundaryFaceNearestCell /
            DerivativeBoundaryFacePlain with a value condition */
-        double val = x->bcu[n][fq];
+        double val = bcval[fq];
         cconst += (val * Ff) * s;
         double factor = side ? 1. : -1.;  /* id 0 when cm is the valid cell */
         double al = 1. / (0.5 * m->h[d]) * factor;
@@ -940,7 +988,7 @@ static void assemble_momentum(oracle_ctx* x, int n, const double* u_prev,
         dfl[sc] += ((-al) * mA * m->A[d]) * s;
       }
     }
-    double rho = x->rho[c];
+    double rho = scaling ? scaling[c] : 1.;
     double a[MAXW];
     for (int t = 0; t < w; ++t) {
       double un = (t == sc) ? co[2] : 0.;
@@ -971,6 +1019,20 @@ static double coeff_sum(const Mesh* m, const double* rows, long c) {
   double s = 0.;
   for (int t = 0; t < w; ++t) s += rows[c * w + t];
   return s;
+}
+
+static int linear_solve_k(oracle_ctx* x, int kind, double tol, int lim, double om, double* sol,
+                          int* iters) {
+  const Mesh* m = &x->m;
+  switch (kind) {
+    case HYDRO_LINEAR_GAUSS_SEIDEL:
+      return solve_gs(m, x->rows, x->rowc, sol, tol, lim, om, iters);
+    case HYDRO_LINEAR_JACOBI:
+      return solve_jacobi(m, x->rows, x->rowc, sol, x->cw[23], tol, lim, om, iters);
+    case HYDRO_LINEAR_LU:
+      return solve_lu(m, x->rows, x->rowc, sol, iters);
+  }
+  return HYDRO_ERR_ARG;
 }
 
 static int linear_solve(oracle_ctx* x, int which, double* sol, int* iters) {
@@ -1604,6 +1666,11 @@ int oracle_step(oracle_ctx* x, hydro_step_stats* st) {
   rc = oracle_finish_step(x);
   if (rc) return rc;
   if (d->advection_enable) oracle_advection_step(x, &s.advection_substeps);
+  /* heat after advection (hydro2d.hpp:1607-1613) */
+  if (x->heat_on) {
+    int hr = oracle_heat_step(x);
+    if (hr) return hr;
+  }
   oracle_update_properties(x);
   s.dt = x->dt;
   s.dt_advection = x->adv_dt;
@@ -1669,5 +1736,81 @@ int oracle_calc_stat(oracle_ctx* x, hydro_stat* out) {
     out->volume_flux_in[i] = fin;
     out->volume_flux_out[i] = fout;
   }
+  return HYDRO_OK;
+}
+
+
+/* ---------------------------------------------------------------- heat -- */
+
+/* hydro<Mesh>::InitHeatSolver (hydro2d.hpp:650-687): temperature layers,
+ * boundary faces in the box hold its temperature, the others zero
+ * derivative (Rect::IsInside is inclusive, vect.hpp:239-246). */
+int oracle_heat_create(oracle_ctx* x, const hydro_heat_desc* hd) {
+  if (!x || !hd) return HYDRO_ERR_ARG;
+  const Mesh* m = &x->m;
+  x->hd = *hd;
+  for (int l = 0; l < 4; ++l) {
+    if (!x->T[l]) x->T[l] = alloc0(m->nc);
+    for (long c = 0; c < m->nc; ++c) x->T[l][c] = hd->temperature_initial;
+  }
+  if (!x->kc) x->kc = alloc0(m->nc);
+  if (!x->tbval) x->tbval = alloc0(m->nf);
+  if (!x->tbder) x->tbder = (unsigned char*)calloc((size_t)m->nf, 1);
+  for (long f = 0; f < m->nf; ++f) {
+    int d;
+    long mi[3], cm, cp;
+    fdecode(m, f, &d, mi, &cm, &cp);
+    x->tbder[f] = 0;
+    if (cm >= 0 && cp >= 0) continue;
+    double xc[3] = {0, 0, 0};
+    for (int k = 0; k < m->dim; ++k)
+      xc[k] = k == d ? m->lo[k] + mi[k] * m->h[k] : m->lo[k] + (mi[k] + 0.5) * m->h[k];
+    int in = 1;
+    for (int k = 0; k < m->dim; ++k)
+      if (xc[k] < hd->box_lo[k] || hd->box_hi[k] < xc[k]) in = 0;
+    if (in) x->tbval[f] = hd->box_temperature;
+    else x->tbder[f] = 1;
+  }
+  x->heat_on = 1;
+  /* mixture conductivity from the current volume fractions */
+  for (long c = 0; c < m->nc; ++c) {
+    double s = 0.;
+    for (int i = 0; i < x->nph; ++i) s += hd->conductivity[i] * x->alpha[i][c];
+    x->kc[c] = s;
+  }
+  return HYDRO_OK;
+}
+
+int oracle_heat_get_temperature(oracle_ctx* x, double* out, size_t n) {
+  if (!x || !x->heat_on || !out || (long)n != x->m.nc) return HYDRO_ERR_ARG;
+  memcpy(out, x->T[HYDRO_TIME_CURR], sizeof(double) * n);
+  return HYDRO_OK;
+}
+
+/* HeatSolver StartStep, one MakeIteration (ConvectionDiffusionScalarImplicit,
+ * conv_diff.hpp:130-251, unit scaling, conductivity as diffusion rate,
+ * the fluid's iter_curr fluxes), FinishStep. */
+int oracle_heat_step(oracle_ctx* x) {
+  if (!x || !x->heat_on) return HYDRO_ERR_ARG;
+  const Mesh* m = &x->m;
+  long nc = m->nc;
+  double** T = x->T;
+  memcpy(T[HYDRO_ITER_CURR], T[HYDRO_TIME_CURR], sizeof(double) * nc);
+  memcpy(T[HYDRO_ITER_PREV], T[HYDRO_ITER_CURR], sizeof(double) * nc);
+  double* kf = x->fw[0];
+  interp(m, x->kc, kf, BC_ZERODER, NULL, 0);
+  double* src = x->cw[22];
+  for (long c = 0; c < nc; ++c) src[c] = 0.;
+  assemble_scalar(x, T[HYDRO_ITER_PREV], T[HYDRO_TIME_CURR], T[HYDRO_TIME_PREV],
+                  x->F[HYDRO_ITER_CURR], kf, src, NULL, x->tbval, x->tbder, x->hd.dt,
+                  x->hd.time_second_order, x->hd.relaxation_factor);
+  double* corr = x->cw[20];
+  for (long c = 0; c < nc; ++c) corr[c] = 0.;
+  int it = 0;
+  int st = linear_solve_k(x, x->hd.solver, x->hd.tolerance, x->hd.iters_limit, 1., corr, &it);
+  if (st != HYDRO_OK && st != HYDRO_NOT_CONVERGED) return st;
+  for (long c = 0; c < nc; ++c) T[HYDRO_ITER_CURR][c] = T[HYDRO_ITER_PREV][c] + corr[c];
+  memcpy(T[HYDRO_TIME_PREV], T[HYDRO_TIME_CURR], sizeof(double) * nc);
+  memcpy(T[HYDRO_TIME_CURR], T[HYDRO_ITER_CURR], sizeof(double) * nc);
   return HYDRO_OK;
 }

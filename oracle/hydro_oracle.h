@@ -42,6 +42,11 @@ int oracle_get_time(oracle_ctx* ctx, double* fluid_time, double* advection_time)
 int oracle_advection_step(oracle_ctx* ctx, int* substeps);
 int oracle_advection_substep(oracle_ctx* ctx);
 int oracle_step(oracle_ctx* ctx, hydro_step_stats* stats);
+/* HeatSolver (heat.hpp:18-94) attached to the case; oracle_step then runs
+ * one heat step after advection (hydro2d.hpp:1607-1613). */
+int oracle_heat_create(oracle_ctx* ctx, const hydro_heat_desc* hd);
+int oracle_heat_step(oracle_ctx* ctx);
+int oracle_heat_get_temperature(oracle_ctx* ctx, double* out, size_t n);
 int oracle_calc_stat(oracle_ctx* ctx, hydro_stat* out);
 /* GetSmoothField (solver.hpp:636-656) on a cell array, in place. */
 int oracle_smooth_field(oracle_ctx* ctx, double* field, int repeat);

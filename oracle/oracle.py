@@ -39,6 +39,12 @@ def lib():
         _oracle.oracle_smooth_field.restype = ctypes.c_int
         _oracle.oracle_set_threads.argtypes = [ctypes.c_int]
         _oracle.oracle_set_threads.restype = ctypes.c_int
+        _oracle.oracle_heat_create.argtypes = [ctypes.c_void_p, ctypes.POINTER(capi.HeatDesc)]
+        _oracle.oracle_heat_create.restype = ctypes.c_int
+        _oracle.oracle_heat_get_temperature.argtypes = [ctypes.c_void_p,
+                                                        ctypes.POINTER(ctypes.c_double),
+                                                        ctypes.c_size_t]
+        _oracle.oracle_heat_get_temperature.restype = ctypes.c_int
     return _oracle
 
 
@@ -60,6 +66,10 @@ def ref_lib(variant=""):
             lib.ref_run.argtypes = [ctypes.POINTER(capi.HydroDesc), D, D, ctypes.c_int,
                                     D, D, D, D, ctypes.POINTER(capi.StepStats)]
             lib.ref_run.restype = ctypes.c_int
+            lib.ref_run_heat.argtypes = [ctypes.POINTER(capi.HydroDesc),
+                                         ctypes.POINTER(capi.HeatDesc), D, D, ctypes.c_int,
+                                         D, D, D, D, D, ctypes.POINTER(capi.StepStats)]
+            lib.ref_run_heat.restype = ctypes.c_int
             _ref_variants[variant] = lib
         return _ref_variants[variant]
     if _ref is None:
@@ -70,6 +80,10 @@ def ref_lib(variant=""):
         _ref.ref_run.restype = ctypes.c_int
         _ref.ref_smooth.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), D, ctypes.c_int]
         _ref.ref_smooth.restype = ctypes.c_int
+        _ref.ref_run_heat.argtypes = [ctypes.POINTER(capi.HydroDesc),
+                                      ctypes.POINTER(capi.HeatDesc), D, D, ctypes.c_int,
+                                      D, D, D, D, D, ctypes.POINTER(capi.StepStats)]
+        _ref.ref_run_heat.restype = ctypes.c_int
         C = ctypes.c_char_p
         _ref.ref_write_vts.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), D, D,
                                        ctypes.c_int, ctypes.POINTER(C), ctypes.POINTER(D),
@@ -188,6 +202,15 @@ class Oracle:
         self._call("calc_stat", ctypes.byref(s))
         return s
 
+    def heat_create(self, heat):
+        self.heat = capi.HeatDesc.from_buffer_copy(heat)
+        self._call("heat_create", ctypes.byref(self.heat))
+
+    def temperature(self):
+        a = np.empty(self.nc, dtype=np.float64)
+        self._call("heat_get_temperature", _dp(a), a.size)
+        return a
+
     def smooth(self, field, repeat):
         a = np.ascontiguousarray(field, dtype=np.float64).copy()
         self._call("smooth_field", _dp(a), repeat)
@@ -209,10 +232,9 @@ def stencil_solve(dim, n, face_coeff, shift, pinned_cell, pinned_value, rhs, tol
     return st, x, it.value, res.value
 
 
-def ref_run(desc, u0, q0, nsteps):
-    """Run the reference's own FluidSimple + AdvectionSolverMultiExplicit for
-    nsteps steps; returns (u, p, F, q, stats list).  Periodic directions x
-    (and z in 3D) select the harness built with PERX (PERZ)."""
+def _ref_for(desc):
+    """Harness build for the case's periodic directions: x selects PERX,
+    x and z (3D) PERX+PERZ."""
     per = tuple(bool(desc.periodic[k]) for k in range(3))
     variants = {(False, False, False): "", (True, False, False): "perx",
                 (True, False, True): "perxz"}
@@ -220,7 +242,14 @@ def ref_run(desc, u0, q0, nsteps):
         per = (per[0], per[1], False)
     if per not in variants:
         raise ValueError("the reference switches periodicity on x (PERX) and x+z (PERZ) only")
-    R = ref_lib(variants[per])
+    return ref_lib(variants[per])
+
+
+def ref_run(desc, u0, q0, nsteps):
+    """Run the reference's own FluidSimple + AdvectionSolverMultiExplicit for
+    nsteps steps; returns (u, p, F, q, stats list).  Periodic directions x
+    (and z in 3D) select the harness built with PERX (PERZ)."""
+    R = _ref_for(desc)
     nc, nf, dim = desc.ncells, desc.nfaces, desc.dim
     nph = desc.num_phases
     u0 = np.ascontiguousarray(u0, dtype=np.float64).ravel()
@@ -235,6 +264,22 @@ def ref_run(desc, u0, q0, nsteps):
                    _dp(q), stats)
     _check(st, "ref_run")
     return u, p, F, q, [stats[i].as_dict() for i in range(nsteps)]
+
+
+def ref_run_heat(desc, heat, u0, q0, nsteps):
+    """ref_run with the reference's HeatSolver attached (hydro2d.hpp:650-687,
+    1607-1613); returns (u, p, F, q, T, stats list)."""
+    R = _ref_for(desc)
+    nc, nf, dim, nph = desc.ncells, desc.nfaces, desc.dim, desc.num_phases
+    u0 = np.ascontiguousarray(u0, dtype=np.float64).ravel()
+    q0 = np.ascontiguousarray(q0, dtype=np.float64).ravel()
+    u, p, F, q, T = (np.empty(nc * dim), np.empty(nc), np.empty(nf), np.empty(nc * nph),
+                     np.empty(nc))
+    stats = (capi.StepStats * max(nsteps, 1))()
+    d, h = desc.copy(), capi.HeatDesc.from_buffer_copy(heat)
+    _check(R.ref_run_heat(ctypes.byref(d), ctypes.byref(h), _dp(u0), _dp(q0), nsteps, _dp(u),
+                          _dp(p), _dp(F), _dp(q), _dp(T), stats), "ref_run_heat")
+    return u, p, F, q, T, [stats[i].as_dict() for i in range(nsteps)]
 
 
 def ref_write_vts(dim, n, lo, hi, node_fields, cell_fields, base, times):

@@ -20,6 +20,7 @@
 #include "mesh3d.hpp"
 #include "fluid.hpp"
 #include "advection.hpp"
+#include "heat.hpp"
 
 // The ParaView session names its files with an integer-to-text helper from
 // the reference's common library (not part of these headers); the harness
@@ -63,6 +64,11 @@ struct Case {
   MultiTimer<std::string> timer;
   std::shared_ptr<solver::FluidSimple<Mesh>> fluid;
   std::shared_ptr<solver::AdvectionSolverMultiExplicit<Mesh, FieldFace<Scal>>> adv;
+  // heat (hydro2d.hpp:650-687), when hd is given
+  const hydro_heat_desc* hd = nullptr;
+  FieldCell<Scal> fc_conductivity, fc_temperature_source;
+  std::shared_ptr<solver::HeatSolver<Mesh>> heat;
+  std::shared_ptr<const solver::LinearSolverFactory> fheat;
 
   static std::shared_ptr<const solver::LinearSolverFactory> Factory(
       int kind, double tol, int limit, double omega) {
@@ -94,7 +100,9 @@ struct Case {
     return 2 * int(dir) + 1;
   }
 
-  Case(const hydro_desc& desc, const double* u0, const double* q0) : d(desc) {
+  Case(const hydro_desc& desc, const double* u0, const double* q0,
+       const hydro_heat_desc* heat_desc = nullptr)
+      : d(desc), hd(heat_desc) {
     MIdx size;
     Vect lo, hi;
     for (size_t i = 0; i < dim; ++i) {
@@ -189,6 +197,24 @@ struct Case {
         v_p_ff_volume_flux_slip, v_p_fc_mass_source, 0.,
         d.dt * d.advection_dt_factor, d.tvd_split != 0, d.sharp, rho);
     UpdateProperties();
+    if (hd) {
+      geom::MapFace<std::shared_ptr<solver::ConditionFace>> tcond;
+      geom::Rect<Vect> box(V3(hd->box_lo), V3(hd->box_hi));
+      for (auto f : mesh.Faces()) {
+        if (mesh.IsInner(f)) continue;
+        if (box.IsInside(mesh.GetCenter(f)))
+          tcond[f] = std::make_shared<solver::ConditionFaceValueFixed<Scal>>(hd->box_temperature);
+        else
+          tcond[f] = std::make_shared<solver::ConditionFaceDerivativeFixed<Scal>>(0.);
+      }
+      fc_temperature_source.Reinit(mesh, 0.);
+      fheat = Factory(hd->solver, hd->tolerance, hd->iters_limit, 1.);
+      heat = std::make_shared<solver::HeatSolver<Mesh>>(
+          mesh, FieldCell<Scal>(mesh, hd->temperature_initial), tcond, hd->relaxation_factor,
+          &fc_conductivity, &fc_temperature_source,
+          &fluid->GetVolumeFlux(solver::Layers::iter_curr), 0., hd->dt, *fheat, 0.5, 1,
+          hd->time_second_order != 0);
+    }
   }
 
   // UpdateFluidProperties (hydro2d.hpp:1404-1430), mass sources zero.
@@ -247,6 +273,12 @@ struct Case {
       }
     }
     fc_force = solver::GetSmoothField(fc_force, mesh, d.force_smooth_times);
+    if (hd) {
+      fc_conductivity.Reinit(mesh, 0.);
+      for (size_t i = 0; i < nph; ++i)
+        for (size_t c = 0; c < nc; ++c)
+          fc_conductivity[IdxCell(c)] += hd->conductivity[i] * v_fc_volume_fraction[i][IdxCell(c)];
+    }
   }
 
   // hydro<Mesh>::step (hydro2d.hpp:1531-1621)
@@ -276,6 +308,11 @@ struct Case {
       }
     }
     st->advection_substeps = ns;
+    if (heat) {
+      heat->StartStep();
+      heat->CalcStep();
+      heat->FinishStep();
+    }
     st->dt = fluid->GetTimeStep();
     st->dt_advection = adv->GetTimeStep();
     st->time = fluid->GetTime();
@@ -299,15 +336,20 @@ struct Case {
 
 template <class Mesh>
 int Run(const hydro_desc* d, const double* u0, const double* q0, int nsteps,
-        double* u, double* p, double* F, double* q, hydro_step_stats* stats) {
+        double* u, double* p, double* F, double* q, hydro_step_stats* stats,
+        const hydro_heat_desc* hd = nullptr, double* T = nullptr) {
   // The reference's linear solvers print one line per solve
   // (linear.hpp:647,712,779); keep it off the test output.
   std::streambuf* saved = std::cout.rdbuf(nullptr);
   int rc = HYDRO_OK;
   try {
-    Case<Mesh> cs(*d, u0, q0);
+    Case<Mesh> cs(*d, u0, q0, hd);
     for (int s = 0; s < nsteps; ++s) cs.Step(&stats[s]);
     cs.Dump(u, p, F, q);
+    if (hd && T) {
+      const auto& t = cs.heat->GetTemperature();
+      for (size_t c = 0; c < cs.mesh.GetNumCells(); ++c) T[c] = t[geom::IdxCell(c)];
+    }
   } catch (const std::string& e) {
     rc = HYDRO_ERR_NAN;
   } catch (...) {
@@ -332,6 +374,15 @@ extern "C" int ref_run(const hydro_desc* d, const double* u0, const double* q0,
 
 // GetSmoothField (solver.hpp:636-656) of a cell field, for pinning the
 // initialisation helpers.
+extern "C" int ref_run_heat(const hydro_desc* d, const hydro_heat_desc* hd, const double* u0,
+                            const double* q0, int nsteps, double* u, double* p, double* F,
+                            double* q, double* T, hydro_step_stats* stats) {
+  if (d->dim == 2)
+    return Run<geom::geom2d::MeshStructured<double>>(d, u0, q0, nsteps, u, p, F, q, stats, hd,
+                                                     T);
+  return Run<geom::geom3d::MeshStructured<double>>(d, u0, q0, nsteps, u, p, F, q, stats, hd, T);
+}
+
 extern "C" int ref_smooth(int dim, const int* n, double* field, int repeat) {
   if (dim == 2) {
     using Mesh = geom::geom2d::MeshStructured<double>;

@@ -46,6 +46,22 @@ def tight(d, solver=capi.LINEAR_GAUSS_SEIDEL, p_tol=1e-14):
     return d
 
 
+def heat(dt, lo, hi, second_order=1, relax=1.0):
+    """Temperature of the heat goldens: 0.25 initially, the given box at 1,
+    conductivities 0.6 / 0.025, Gauss-Seidel to 1e-15 (tight)."""
+    h = capi.default_heat_desc(dt)
+    h.temperature_initial = 0.25
+    h.conductivity[0], h.conductivity[1] = 0.6, 0.025
+    for k in range(3):
+        h.box_lo[k], h.box_hi[k] = lo[k], hi[k]
+    h.box_temperature = 1.0
+    h.time_second_order = second_order
+    h.relaxation_factor = relax
+    h.solver = capi.LINEAR_GAUSS_SEIDEL
+    h.tolerance, h.iters_limit = 1e-15, 1000000
+    return h
+
+
 def golden_cases():
     out = []
     d, u0, q0 = cases.cavity(n=16, mu=0.01, dt=1e-2)
@@ -140,6 +156,29 @@ def golden_cases():
     d.pressure_fixed_cell = 30
     out.append(("dam2d_simpler_pinned", d, u0, q0, 2, True))
 
+    # HeatSolver attached (hydro2d.hpp:650-687): the temperature is the
+    # eighth element of the case tuple
+    d, u0, q0 = cases.broken_dam(nx=24, ny=12, dt_auto=False, dt=1e-3, smooth_times=2)
+    tight(d, p_tol=1e-10)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    h = heat(d.dt, lo=(-1.0, -1.0, -1.0), hi=(0.3, 0.02, 10.0))
+    out.append(("heat_dam2d", d, u0, q0, 3, True, h))
+
+    d, u0, q0 = cases.channel(nx=12, ny=6, nz=4, dim=3, dt=1e-2, two_phase=True)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 2
+    # box over the inlet side (x = 0, lower half in y): inflow carries T = 1
+    h = heat(d.dt, lo=(-1.0, -1.0, -1.0), hi=(0.0, 0.5, 10.0), second_order=0, relax=0.9)
+    h.conductivity[1] = 0.2
+    out.append(("heat_channel3d", d, u0, q0, 3, True, h))
+
+    d, u0, q0 = cases.broken_dam(nx=16, ny=8, dt_auto=False, dt=1e-3, smooth_times=2)
+    tight(d, p_tol=1e-10)
+    d.periodic[0] = 1
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 2
+    h = heat(d.dt, lo=(0.25, -1.0, -1.0), hi=(0.6, 0.0, 10.0))
+    out.append(("heat_dam2d_periodic_x", d, u0, q0, 2, True, h))
+
     # reference defaults for the linear solvers: one LU sweep for velocity
     # (an approximate solve; CPU-only semantics), SOR pressure
     d, u0, q0 = cases.broken_dam(nx=16, ny=8, dt_auto=False, dt=2e-3, smooth_times=2)
@@ -153,12 +192,18 @@ def golden_cases():
 
 
 def make_cases():
-    for name, d, u0, q0, nsteps, gpu_ok in golden_cases():
-        u, p, F, q, stats = O.ref_run(d, u0, q0, nsteps)
+    for case in golden_cases():
+        name, d, u0, q0, nsteps, gpu_ok = case[:6]
+        extra = {}
+        if len(case) > 6:
+            u, p, F, q, T, stats = O.ref_run_heat(d, case[6], u0, q0, nsteps)
+            extra = {"heat": json.dumps(capi.heat_to_dict(case[6])), "T": T}
+        else:
+            u, p, F, q, stats = O.ref_run(d, u0, q0, nsteps)
         path = os.path.join(HERE, name + ".npz")
         np.savez_compressed(
             path, desc=json.dumps(capi.desc_to_dict(d)), u0=u0, q0=q0, nsteps=nsteps,
-            gpu_comparable=gpu_ok, u=u, p=p, F=F, q=q,
+            gpu_comparable=gpu_ok, u=u, p=p, F=F, q=q, **extra,
             outer_iterations=np.array([s["outer_iterations"] for s in stats]),
             indicator=np.array([s["convergence_indicator"] for s in stats]),
             dt=np.array([s["dt"] for s in stats]),

@@ -26,6 +26,7 @@ def load(name):
     g["desc"] = capi.desc_from_dict(json.loads(str(z["desc"])))
     g["nsteps"] = int(z["nsteps"])
     g["gpu_comparable"] = bool(z["gpu_comparable"])
+    g["heat"] = capi.heat_from_dict(json.loads(str(z["heat"]))) if "heat" in z.files else None
     return g
 
 

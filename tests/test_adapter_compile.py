@@ -15,11 +15,14 @@ SRC = r'''
 #include "mesh3d.hpp"
 #include "fluid.hpp"
 #include "advection.hpp"
+#include "conv_diff.hpp"
 #include "fluid_simple_gpu.hpp"
 template class solver::FluidSimpleGpu<geom::geom2d::MeshStructured<double>>;
 template class solver::FluidSimpleGpu<geom::geom3d::MeshStructured<double>>;
 template class solver::AdvectionSolverMultiGpu<geom::geom2d::MeshStructured<double>>;
 template class solver::AdvectionSolverMultiGpu<geom::geom3d::MeshStructured<double>>;
+template class solver::HeatSolverGpu<geom::geom2d::MeshStructured<double>>;
+template class solver::HeatSolverGpu<geom::geom3d::MeshStructured<double>>;
 int main() { return 0; }
 '''
 

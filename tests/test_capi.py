@@ -46,6 +46,10 @@ def test_struct_layout_matches_header(tmp_path):
              '  printf("%zu %zu %zu\\n", sizeof(hydro_desc), sizeof(hydro_step_stats), sizeof(hydro_stat));']
     for f in fields:
         lines.append('  printf("%%zu\\n", offsetof(hydro_desc, %s));' % f)
+    hfields = [f for f, _ in capi.HeatDesc._fields_]
+    lines.append('  printf("%zu\\n", sizeof(hydro_heat_desc));')
+    for f in hfields:
+        lines.append('  printf("%%zu\\n", offsetof(hydro_heat_desc, %s));' % f)
     lines.append("  return 0; }")
     src.write_text("\n".join(lines))
     exe = tmp_path / "layout"
@@ -54,8 +58,12 @@ def test_struct_layout_matches_header(tmp_path):
     assert int(out[0]) == ctypes.sizeof(capi.HydroDesc)
     assert int(out[1]) == ctypes.sizeof(capi.StepStats)
     assert int(out[2]) == ctypes.sizeof(capi.Stat)
-    for f, off in zip(fields, out[3:]):
+    for f, off in zip(fields, out[3:3 + len(fields)]):
         assert getattr(capi.HydroDesc, f).offset == int(off), f
+    rest = out[3 + len(fields):]
+    assert int(rest[0]) == ctypes.sizeof(capi.HeatDesc)
+    for f, off in zip(hfields, rest[1:]):
+        assert getattr(capi.HeatDesc, f).offset == int(off), f
 
 
 def test_desc_default_matches_python(lib):

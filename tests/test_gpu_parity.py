@@ -210,7 +210,11 @@ def test_gpu_matches_reference_golden(built, name):
     d.pressure_solver = capi.LINEAR_CG
     d.velocity_tolerance, d.velocity_iters_limit = 1e-14, 20000
     d.pressure_tolerance, d.pressure_iters_limit = 1e-13, 20000
-    out = run(Hydro(d), g["u0"], g["q0"], g["nsteps"])
+    heat = g["heat"]
+    if heat is not None:
+        heat = capi.HeatDesc.from_buffer_copy(heat)
+        heat.solver, heat.tolerance, heat.iters_limit = capi.LINEAR_JACOBI, 1e-15, 20000
+    out = run(Hydro(d), g["u0"], g["q0"], g["nsteps"], heat=heat)
     errs = compare(out, g)
     assert all(v <= 1e-9 for v in errs.values()), errs
     assert [s["outer_iterations"] for s in out["stats"]] == list(g["outer_iterations"])

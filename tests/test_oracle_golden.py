@@ -19,7 +19,7 @@ def oracle_lib():
 @pytest.mark.parametrize("name", goldens.names())
 def test_oracle_matches_reference(oracle_lib, name):
     g = goldens.load(name)
-    o = run(oracle_lib.Oracle(g["desc"]), g["u0"], g["q0"], g["nsteps"])
+    o = run(oracle_lib.Oracle(g["desc"]), g["u0"], g["q0"], g["nsteps"], heat=g["heat"])
     errs = compare(o, g)
     assert all(v <= 1e-10 for v in errs.values()), errs
     assert [s["outer_iterations"] for s in o["stats"]] == list(g["outer_iterations"])

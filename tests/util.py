@@ -24,10 +24,12 @@ def tight(d, omega_p=1.0):
     return d
 
 
-def run(solver, u0, q0, nsteps):
+def run(solver, u0, q0, nsteps, heat=None):
     solver.set_field(capi.F_VELOCITY, u0)
     solver.set_field(capi.F_PARTIAL_DENSITY, q0)
     solver.init_state()
+    if heat is not None:
+        solver.heat_create(heat)
     stats = [solver.step() for _ in range(nsteps)]
     out = {
         "u": solver.get_field(capi.F_VELOCITY),
@@ -37,13 +39,18 @@ def run(solver, u0, q0, nsteps):
         "rho": solver.get_field(capi.F_DENSITY),
         "stats": stats,
     }
+    if heat is not None:
+        out["T"] = solver.temperature()
     return out
 
 
 def compare(a, b):
-    return {
+    out = {
         "u": rel(a["u"], b["u"]),
         "p": rel(demean(a["p"]), demean(b["p"])),
         "F": rel(a["F"], b["F"]),
         "q": rel(a["q"], b["q"]),
     }
+    if "T" in a and "T" in b:
+        out["T"] = rel(a["T"], b["T"])
+    return out
