@@ -22,31 +22,33 @@ __device__ __forceinline__ double superbee(double p, double q) {
   return 0.;
 }
 
-// Superbee value on the inner face between P (low side) and E (high side)
-// with flux Ff; fP = value of P's other (low) face, fE = value of E's other
-// (high) face, as the Green-Gauss cell gradients of P and E use them.
-__device__ __forceinline__ double superbee_face(double qP, double qE, double fP, double fE,
-                                                double Ff, double h, double inv_h) {
-  if (Ff > 1e-8) {
-    double gP = (avg(qP, qE) - fP) * inv_h;
-    double dq = qE - qP;
-    return qP + 0.5 * superbee(dq, -4. * (gP * (-0.5 * h)) - dq);
-  } else if (Ff < -1e-8) {
-    double gE = (fE - avg(qP, qE)) * inv_h;
-    double dq = qE - qP;
-    return qE - 0.5 * superbee(dq, 4. * (gE * (0.5 * h)) - dq);
-  }
-  return 0.5 * (qP + qE);
+// Superbee value on the inner face between P (low side) and E (high side):
+// flow from P (Ff > 1e-8) with fP the value of P's other (low) face, flow
+// from E (Ff < -1e-8) with fE the value of E's other (high) face, as the
+// Green-Gauss cell gradients of P and E use them; the mean otherwise.  Only
+// the upwind cell's other face is read.
+__device__ __forceinline__ double superbee_from_p(double qP, double qE, double fP, double h,
+                                                  double inv_h) {
+  double gP = (avg(qP, qE) - fP) * inv_h;
+  double dq = qE - qP;
+  return qP + 0.5 * superbee(dq, -4. * (gP * (-0.5 * h)) - dq);
+}
+__device__ __forceinline__ double superbee_from_e(double qP, double qE, double fE, double h,
+                                                  double inv_h) {
+  double gE = (fE - avg(qP, qE)) * inv_h;
+  double dq = qE - qP;
+  return qE - 0.5 * superbee(dq, 4. * (gE * (0.5 * h)) - dq);
 }
 
 // inlet_mask: bit q set when side q (xm, xp, ym, ...) is an inlet; qin
 // holds the inlet values on those boundary faces.  Boundary faces carry
 // the advection condition (the inlet value, else zero derivative: the
 // cell's own value); across a periodic end the faces are inner.
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void k_adv_faces(Mesh m, Geo g, int nph, int stage, int nstages, const double* F,
                             CP<HYDRO_MAXPH> q, int inlet_mask, CP<HYDRO_MAXPH> qin,
                             WP<HYDRO_MAXPH> qflux, int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
@@ -59,11 +61,11 @@ __global__ void k_adv_faces(Mesh m, Geo g, int nph, int stage, int nstages, cons
     // the low-side face value of cell c (index ic along d) and the
     // high-side face value, for the cell gradients
     auto lo_face = [&](const double* qa, const double* qi, long long c, int ic, long long fc) {
-      if (has_lo(m, d, ic)) return avg(qa[nb_lo(m, d, ic, c, s)], qa[c]);
+      if (has_lo_p<PER>(m, d, ic)) return avg(qa[nb_lo_p<PER>(m, d, ic, c, s)], qa[c]);
       return in_lo ? qi[fc] : qa[c];
     };
     auto hi_face = [&](const double* qa, const double* qi, long long c, int ic, long long fc) {
-      if (has_hi(m, d, ic)) return avg(qa[c], qa[nb_hi(m, d, ic, c, s)]);
+      if (has_hi_p<PER>(m, d, ic)) return avg(qa[c], qa[nb_hi_p<PER>(m, d, ic, c, s)]);
       return in_hi ? qi[fc] : qa[c];
     };
     // inner face between P (index ip) and E (index ie) with face index ff
@@ -71,9 +73,12 @@ __global__ void k_adv_faces(Mesh m, Geo g, int nph, int stage, int nstages, cons
                      long long ff, double Ff) {
       // P's low face is ff - fs unless P wraps (then the periodic end face);
       // E's high face is ff + fs likewise
-      double fP = lo_face(qa, qi, P, ip, ff - fs);
-      double fE = hi_face(qa, qi, E, ie, ff + fs);
-      return superbee_face(qa[P], qa[E], fP, fE, Ff, g.h[d], g.inv_h[d]);
+      const double qP = qa[P], qE = qa[E];
+      if (Ff > 1e-8) return superbee_from_p(qP, qE, lo_face(qa, qi, P, ip, ff - fs), g.h[d],
+                                            g.inv_h[d]);
+      if (Ff < -1e-8) return superbee_from_e(qP, qE, hi_face(qa, qi, E, ie, ff + fs), g.h[d],
+                                             g.inv_h[d]);
+      return 0.5 * (qP + qE);
     };
     double Ff = F[f];
     for (int i = 0; i < nph; ++i) {
@@ -91,7 +96,7 @@ __global__ void k_adv_faces(Mesh m, Geo g, int nph, int stage, int nstages, cons
       double Fh = F[fh];
       for (int i = 0; i < nph; ++i) {
         double qf;
-        if (m.per[d]) qf = inner(q.a[i], qin.a[i], X.c, id, NB_HI(d, s), 0, fh, Fh);
+        if (PER && m.per[d]) qf = inner(q.a[i], qin.a[i], X.c, id, NB_HI(d, s), 0, fh, Fh);
         else qf = in_hi ? qin.a[i][fh] : q.a[i][X.c];
         qflux.a[i][fh] = qf * Fh;
       }
@@ -123,9 +128,10 @@ __global__ void k_adv_update(Mesh m, int nph, int stage, int nstages, double mdt
 // the face gradient of q (zero-derivative boundaries), on faces where
 // |gf| >= 1: n = gf/(|gf|+1e-6), ff = |F n_d| n_d (sharp A |gf| - a (1 -
 // a/amax)); q += dt/V sum_f s_f ff.
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void k_sharpen(Mesh m, Geo g, double sharp, double amax, double dtv, const double* F,
                           const double* q, C3 G, double* qout, int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
   double sh = 0.;
 #pragma unroll
@@ -158,8 +164,9 @@ __global__ void k_sharpen(Mesh m, Geo g, double sharp, double amax, double dtv, 
   CELL_LOOP_END
 }
 
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void k_grad0(Mesh m, Geo g, const double* a, W3 G, int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
   double vc = a[X.c];
 #pragma unroll
@@ -179,12 +186,7 @@ cudaError_t launch_adv_faces(const Mesh& m, int nph, int stage, int nstages, con
                              WP<HYDRO_MAXPH> qflux, cudaStream_t st) {
   Launch L = cell_launch(m);
   Geo g = make_geo(m);
-  if (m.dim == 3)
-    k_adv_faces<3><<<L.grid, L.block, 0, st>>>(m, g, nph, stage, nstages, F, q, inlet_mask, qin,
-                                               qflux, L.kch);
-  else
-    k_adv_faces<2><<<L.grid, L.block, 0, st>>>(m, g, nph, stage, nstages, F, q, inlet_mask, qin,
-                                               qflux, L.kch);
+  CELL_LAUNCH_P(m, L, st, k_adv_faces, m, g, nph, stage, nstages, F, q, inlet_mask, qin, qflux);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -213,13 +215,8 @@ cudaError_t launch_adv_sharpen(const Mesh& m, int phase, double sharp, double am
   Geo g = make_geo(m);
   C3 Gc = {{G.a[0], G.a[1], G.a[2]}};
   double dtv = dt / m.V;
-  if (m.dim == 3) {
-    k_grad0<3><<<L.grid, L.block, 0, st>>>(m, g, q, G, L.kch);
-    k_sharpen<3><<<L.grid, L.block, 0, st>>>(m, g, sharp, amax, dtv, F, q, Gc, qtmp, L.kch);
-  } else {
-    k_grad0<2><<<L.grid, L.block, 0, st>>>(m, g, q, G, L.kch);
-    k_sharpen<2><<<L.grid, L.block, 0, st>>>(m, g, sharp, amax, dtv, F, q, Gc, qtmp, L.kch);
-  }
+  CELL_LAUNCH_P(m, L, st, k_grad0, m, g, q, G);
+  CELL_LAUNCH_P(m, L, st, k_sharpen, m, g, sharp, amax, dtv, F, q, Gc, qtmp);
   cudaMemcpyAsync(q, qtmp, sizeof(double) * m.nc, cudaMemcpyDeviceToDevice, st);
   count_launches(2);
   return cudaGetLastError();

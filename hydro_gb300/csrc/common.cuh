@@ -41,15 +41,38 @@ __host__ __device__ inline long long face_stride(const Mesh& m, int d) {
 // Neighbours along d of the cell c with index i along d.  A neighbour exists
 // inside the block, or across the end of a periodic direction (both end
 // faces then join cells n-1 and 0, mesh3d.hpp:348-392); s = cell_stride.
-__host__ __device__ inline bool has_lo(const Mesh& m, int d, int i) { return i > 0 || m.per[d]; }
-__host__ __device__ inline bool has_hi(const Mesh& m, int d, int i) {
-  return i < m.n[d] - 1 || m.per[d];
+// P is a compile-time switch: kernels are instantiated with P = false for
+// blocks without a periodic direction, where these reduce to the plain
+// bounds test and c -/+ s (no wrap arithmetic in the hot loops).
+template <bool P>
+__host__ __device__ inline bool has_lo_p(const Mesh& m, int d, int i) {
+  return i > 0 || (P && m.per[d]);
 }
+template <bool P>
+__host__ __device__ inline bool has_hi_p(const Mesh& m, int d, int i) {
+  return i < m.n[d] - 1 || (P && m.per[d]);
+}
+// (I: the index type of the caller, int inside one CTA's shared memory)
+template <bool P, class I>
+__host__ __device__ inline I nb_lo_p(const Mesh& m, int d, int i, I c, I s) {
+  return (!P || i > 0) ? c - s : c + (I)(m.n[d] - 1) * s;
+}
+template <bool P, class I>
+__host__ __device__ inline I nb_hi_p(const Mesh& m, int d, int i, I c, I s) {
+  return (!P || i < m.n[d] - 1) ? c + s : c - (I)(m.n[d] - 1) * s;
+}
+__host__ __device__ inline bool has_lo(const Mesh& m, int d, int i) { return has_lo_p<true>(m, d, i); }
+__host__ __device__ inline bool has_hi(const Mesh& m, int d, int i) { return has_hi_p<true>(m, d, i); }
 __host__ __device__ inline long long nb_lo(const Mesh& m, int d, int i, long long c, long long s) {
-  return i > 0 ? c - s : c + (long long)(m.n[d] - 1) * s;
+  return nb_lo_p<true, long long>(m, d, i, c, s);
 }
 __host__ __device__ inline long long nb_hi(const Mesh& m, int d, int i, long long c, long long s) {
-  return i < m.n[d] - 1 ? c + s : c - (long long)(m.n[d] - 1) * s;
+  return nb_hi_p<true, long long>(m, d, i, c, s);
+}
+inline bool any_periodic(const Mesh& m) {
+  for (int d = 0; d < m.dim; ++d)
+    if (m.per[d]) return true;
+  return false;
 }
 
 // Launch geometry: blocks of 32x8 threads over (i, j); each block marches

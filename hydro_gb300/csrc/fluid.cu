@@ -80,14 +80,14 @@ __global__ void k_d2f(long long n, const double* in, float* out) {
 // ------------------------------------------------------- velocity grads --
 // G[n*DIM+m] = d u_n / d x_m at cells, faces carrying the velocity value
 // condition (Gradient(Interpolate(u_n, cond_n)), solver.hpp:392-470,658-677).
-template <int DIM, class T>
+template <int DIM, class T, bool PER>
 __global__ void k_vel_grad(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T, 3> bv,
                            WT<T, 9> G, int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     long long s = cell_stride(m, d);
-    int id = X.i[d], nd = m.n[d];
     long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
 #pragma unroll
     for (int n = 0; n < DIM; ++n) {
@@ -107,11 +107,12 @@ __global__ void k_vel_grad(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T
 // plus the "restored" external force (fluid.hpp:612-625), surface-tension
 // force and the volume-source momentum term.  Also stores the restored
 // force and the FP64 cell pressure gradient for the Rhie-Chow kernel.
-template <int DIM, class T>
+template <int DIM, class T, bool PER>
 __global__ void k_force(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T, 9> G,
                         const double* p, Geo g64, const T* mu, const T* rho,
                         RT<T, 3> force, RT<T, 3> stforce, const T* Sv, const T* Sm,
                         WT<T, 3> fo, WT<T, 3> fres, W3 gp64, int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
   T acc[DIM];
 #pragma unroll
@@ -120,7 +121,6 @@ __global__ void k_force(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T, 9
 #pragma unroll
   for (int n = 0; n < DIM; ++n) {
     long long s = cell_stride(m, n);
-    int id = X.i[n], nd = m.n[n];
     T mlo, mhi;
     T glo[DIM], ghi[DIM];
     if (HAS_LO(n)) {
@@ -152,10 +152,10 @@ __global__ void k_force(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T, 9
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
     long long s = cell_stride(m, k);
-    int id = X.i[k], nd = m.n[k];
+    int id = X.i[k];
     // the pressure gradient stays FP64: p carries the hydrostatic level,
     // whose FP32 rounding would swamp differences across a cell
-    double gpd = grad_extrap_m(m, p, X.c, k, id, s, g64.inv_h[k]);
+    double gpd = grad_extrap_m<PER>(m, p, X.c, k, id, s, g64.inv_h[k]);
     gp64.a[k][X.c] = gpd;
     T gp = (T)gpd;
     T fcv = force.a[k][X.c];
@@ -184,11 +184,12 @@ __global__ void k_force(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T, 9
 // not multiplied, and the deferred correction's factor is formed once for
 // the DIM components.  The BDF time difference of the residual is formed
 // in FP64 from the FP64 layers (us) whatever T is.
-template <int DIM, class T>
+template <int DIM, class T, bool PER>
 __global__ void k_mom_assemble(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> up, RT<T, 3> utc,
                                RT<T, 3> utp, RT<T, 9> G, const T* F, const T* rho, const T* mu,
                                RT<T, 3> fo, Unsteady64 us, RT<T, 3> bv, WT<T, 7> coef,
                                WT<T, 3> res, T* Dc, int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
   const T rhoc = rho[X.c], muc = mu[X.c];
   T aPc = T(0);  // convective and diffusive part of the diagonal
@@ -202,7 +203,6 @@ __global__ void k_mom_assemble(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> up,
   for (int d = 0; d < DIM; ++d) {
     long long s = cell_stride(m, d);
     long long fs = face_stride(m, d);
-    int id = X.i[d], nd = m.n[d];
     long long flo = face_id(m, d, X.i[0], X.i[1], X.i[2]);
     const T hh = T(0.5) * g.h[d];
 #pragma unroll
@@ -275,11 +275,12 @@ __global__ void k_mom_assemble(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> up,
 // |value - du| is reduced into ds->red[RS_MOM_DIFF].  A launch after
 // convergence or after `limit` sweeps returns at once; the first sweep
 // (count 0) starts from du = 0.
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void __launch_bounds__(NT) k_mom_sweep(Mesh m, double omega, double tol,
                                                   CP<7> coef, C3 res, C3 din, W3 dout,
                                                   int limit, double* partials, DevScalars* ds,
                                                   int kch) {
+  constexpr bool kPerT = PER;
   if (ds->flag[FL_MOM_DONE] || ds->flag[FL_MOM_SWEEPS] >= limit) return;
   const bool first = ds->flag[FL_MOM_SWEEPS] == 0;
   double dmax = 0.;
@@ -320,10 +321,11 @@ __global__ void __launch_bounds__(NT) k_mom_sweep(Mesh m, double omega, double t
 // The same Jacobi sweep on the FP32 coefficients and residuals of the
 // mixed-precision path (o32 of k_mom_assemble: inverse diagonal, 2*DIM
 // off-diagonals, DIM residuals): FP32 arithmetic, FP64 only for the max.
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void __launch_bounds__(NT) k_mom_sweep32(Mesh m, float omega, double tol, FP<10> c,
                                                     FP<3> din, FP<3> dout, int limit,
                                                     double* partials, DevScalars* ds, int kch) {
+  constexpr bool kPerT = PER;
   if (ds->flag[FL_MOM_DONE] || ds->flag[FL_MOM_SWEEPS] >= limit) return;
   const bool first = ds->flag[FL_MOM_SWEEPS] == 0;
   float dmax = 0.f;
@@ -377,10 +379,11 @@ __global__ void k_f2d3(long long n, int dim, FP<3> in, W3 out) {
 // The face velocity and the pressure part of the correction are FP64 (up,
 // p, gp are the FP64 iterate and cell pressure gradient); D_f, the force
 // terms and du are in T.
-template <int DIM, class T>
+template <int DIM, class T, bool PER>
 __global__ void k_rhie_chow(Mesh m, Geo g64, GeoT<T> g, FluidCoef fc64, FluidCoefT<T> fc, C3 up,
                             RT<T, 3> du, const double* p, C3 gp, RT<T, 3> force, RT<T, 3> fres,
                             const T* Dc, C3 bv, double* Fs, double* kf, float* kf32, int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
@@ -415,7 +418,7 @@ __global__ void k_rhie_chow(Mesh m, Geo g64, GeoT<T> g, FluidCoef fc64, FluidCoe
     }
     if (id == nd - 1) {
       long long fh = f + face_stride(m, d);
-      if (m.per[d]) {
+      if (PER && m.per[d]) {
         inner(X.c, NB_HI(d, s), fh);
       } else {
         Fs[fh] = bv.a[d][fh] * A - mv;
@@ -452,7 +455,7 @@ __global__ void k_pressure_rhs(Mesh m, Geo g, const double* Fs, const double* Sv
 // velocity correction du and D_c come in FP32 (du32, Dc32 non-null), the
 // update itself is FP64, and the FP32 shadows of the new iterate (u32,
 // p32, F32) are written beside it.
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void __launch_bounds__(NT) k_correct(Mesh m, Geo g, FluidCoef fc, C3 up, C3 du,
                                                 RT<float, 3> du32, const float* Dc32, W3 uic,
                                                 const double* pip, double* pic,
@@ -460,6 +463,7 @@ __global__ void __launch_bounds__(NT) k_correct(Mesh m, Geo g, FluidCoef fc, C3 
                                                 const double* Fs, const double* kf,
                                                 double* Fic, FP<3> u32, float* p32, float* F32,
                                                 double* partials, DevScalars* ds, int kch) {
+  constexpr bool kPerT = PER;
   double dmax = 0.;
   CELL_LOOP_BEGIN(m, kch)
   double pn = pip[X.c] + fc.relax_p * pc[X.c];
@@ -470,7 +474,7 @@ __global__ void __launch_bounds__(NT) k_correct(Mesh m, Geo g, FluidCoef fc, C3 
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
     long long s = cell_stride(m, k);
-    double gpc = grad_extrap_m(m, pc, X.c, k, X.i[k], s, g.inv_h[k]);
+    double gpc = grad_extrap_m<PER>(m, pc, X.c, k, X.i[k], s, g.inv_h[k]);
     double u0 = up.a[k][X.c];
     double duk = du32.a[0] ? (double)du32.a[k][X.c] : du.a[k][X.c];
     double un = (u0 + duk) + gpc * idc;
@@ -505,9 +509,10 @@ __global__ void __launch_bounds__(NT) k_correct(Mesh m, Geo g, FluidCoef fc, C3 
 // (relaxed diagonal 1/iaP, off-diagonals, delta-form constants) evaluated
 // at the velocity change of the iteration, plus the restored force minus
 // the iteration's cell pressure gradient.
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void k_simpler_eval(Mesh m, CP<7> coef, C3 res, C3 uic, C3 up, C3 fres, C3 gp, W3 ev,
                                int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
   const double aPr = 1. / coef.a[0][X.c];
 #pragma unroll
@@ -535,11 +540,12 @@ __global__ void k_simpler_eval(Mesh m, CP<7> coef, C3 res, C3 uic, C3 up, C3 fre
 // the system is solved in delta form around the corrected pressure p:
 // A x = sum_f s_f r_f - A' p (A' without the pinned cell's coupling, whose
 // row becomes x = value - p).
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void k_simpler_rhs(Mesh m, Geo g, FluidCoef fc, C3 ev, C3 force, const double* Dc,
                               const double* Fic, C3 uic, const double* kf, const double* dg,
                               const double* p, long long pin, double pin_value, double* f,
                               int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
   if (X.c == pin) {
     f[X.c] = pin_value - p[X.c];
@@ -650,8 +656,9 @@ __global__ void k_props(Mesh m, int nph, PhaseProps pp, CP<HYDRO_MAXPH> q,
 // One pass of GetSmoothField (solver.hpp:636-656): face averages with
 // zero-derivative boundaries, then the average over the 2*DIM faces
 // (solver.hpp:621-634).
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void k_smooth(Mesh m, const double* in, double* out, int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
   double vc = in[X.c];
   double sum = 0.;
@@ -666,8 +673,9 @@ __global__ void k_smooth(Mesh m, const double* in, double* out, int kch) {
 }
 
 // Cell gradient of a scalar with zero-derivative boundary faces.
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void k_scal_grad(Mesh m, Geo g, const double* a, W3 G, int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
   double vc = a[X.c];
 #pragma unroll
@@ -683,8 +691,9 @@ __global__ void k_scal_grad(Mesh m, Geo g, const double* a, W3 G, int kch) {
 // Surface-tension force (hydro2d.hpp:1318-1370): g the face gradient of the
 // phase-1 volume fraction, n = g/(|g|+1e-6),
 // f_c = sigma/V sum_f [ g (S.n) - S |g| ].
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void k_stforce(Mesh m, Geo g, double sigma, C3 G, W3 out, int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
   double f[DIM];
 #pragma unroll
@@ -769,8 +778,9 @@ __global__ void __launch_bounds__(NT) k_stat(Mesh m, Geo g, const double* q, con
 
 // Initial volume fluxes of the FluidSimple ctor (fluid.hpp:770-784):
 // F = u_f.S - meshvel.S with the velocity value condition on boundaries.
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void k_init_flux(Mesh m, Geo g, FluidCoef fc, C3 u, C3 bv, double* F, int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
@@ -907,6 +917,20 @@ __global__ void k_outlet_set(Mesh m, BcSpec sp, W3 bv, FP<3> bv32, const DevScal
     count_launches(1);                                                   \
     return cudaGetLastError();                                           \
   } while (0)
+#define DISPATCH_DIM_P(m, KERNEL, ...)                                   \
+  do {                                                                   \
+    Launch L = cell_launch(m);                                           \
+    CELL_LAUNCH_P(m, L, st, KERNEL, __VA_ARGS__);                        \
+    count_launches(1);                                                   \
+    return cudaGetLastError();                                           \
+  } while (0)
+#define DISPATCH_DIM_TP(m, KERNEL, T, ...)                               \
+  do {                                                                   \
+    Launch L = cell_launch(m);                                           \
+    CELL_LAUNCH_TP(m, L, st, KERNEL, T, __VA_ARGS__);                    \
+    count_launches(1);                                                   \
+    return cudaGetLastError();                                           \
+  } while (0)
 #define DISPATCH_DIM_T(m, KERNEL, T, ...)                                \
   do {                                                                   \
     Launch L = cell_launch(m);                                           \
@@ -957,7 +981,7 @@ cudaError_t launch_start_step(const Mesh& m, double ge, W3 u_ic, C3 u_tc, C3 u_t
 
 cudaError_t launch_init_flux(const Mesh& m, const FluidCoef& fc, C3 u, C3 bv, double* F,
                              cudaStream_t st) {
-  DISPATCH_DIM(m, k_init_flux, m, make_geo(m), fc, u, bv, F);
+  DISPATCH_DIM_P(m, k_init_flux, m, make_geo(m), fc, u, bv, F);
 }
 
 cudaError_t launch_bc_fill(const Mesh& m, const BcSpec& sp, W3 bv, FP<3> bv32, cudaStream_t st) {
@@ -988,7 +1012,7 @@ cudaError_t launch_outlet_update(const Mesh& m, const BcSpec& sp, C3 u, W3 bv, F
 template <class T>
 cudaError_t launch_vel_grad(const Mesh& m, const FluidCoef& fc, RT<T, 3> u, RT<T, 3> bv,
                             WT<T, 9> G, cudaStream_t st) {
-  DISPATCH_DIM_T(m, k_vel_grad, T, m, make_geo<T>(m), coef_as<T>(fc), u, bv, G);
+  DISPATCH_DIM_TP(m, k_vel_grad, T, m, make_geo<T>(m), coef_as<T>(fc), u, bv, G);
 }
 
 template <class T>
@@ -996,7 +1020,7 @@ cudaError_t launch_force(const Mesh& m, const FluidCoef& fc, RT<T, 3> u, RT<T, 9
                          const double* p, const T* mu, const T* rho, RT<T, 3> force,
                          RT<T, 3> stforce, const T* Sv, const T* Sm, WT<T, 3> fo,
                          WT<T, 3> fres, W3 gp, cudaStream_t st) {
-  DISPATCH_DIM_T(m, k_force, T, m, make_geo<T>(m), coef_as<T>(fc), u, G, p, make_geo(m), mu,
+  DISPATCH_DIM_TP(m, k_force, T, m, make_geo<T>(m), coef_as<T>(fc), u, G, p, make_geo(m), mu,
                  rho, force, stforce, Sv, Sm, fo, fres, gp);
 }
 
@@ -1013,7 +1037,7 @@ cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, RT<T, 3> u_p
     us.utc[k] = utc64.a[k];
     us.utp[k] = utp64.a[k];
   }
-  DISPATCH_DIM_T(m, k_mom_assemble, T, m, make_geo<T>(m), coef_as<T>(fc), u_prev, u_tc, u_tp,
+  DISPATCH_DIM_TP(m, k_mom_assemble, T, m, make_geo<T>(m), coef_as<T>(fc), u_prev, u_tc, u_tp,
                  G, F, rho, mu, fo, us, bv, coef, res, Dc);
 }
 
@@ -1022,7 +1046,7 @@ cudaError_t launch_rhie_chow(const Mesh& m, const FluidCoef& fc, C3 u_prev, RT<T
                              const double* p, C3 gp, RT<T, 3> force, RT<T, 3> fres,
                              const T* Dc, C3 bv, double* Fs, double* kf, float* kf32,
                              cudaStream_t st) {
-  DISPATCH_DIM_T(m, k_rhie_chow, T, m, make_geo(m), make_geo<T>(m), fc, coef_as<T>(fc), u_prev,
+  DISPATCH_DIM_TP(m, k_rhie_chow, T, m, make_geo(m), make_geo<T>(m), fc, coef_as<T>(fc), u_prev,
                  du, p, gp, force, fres, Dc, bv, Fs, kf, kf32);
 }
 
@@ -1053,7 +1077,7 @@ cudaError_t launch_d2f(long long n, const double* in, float* out, cudaStream_t s
 cudaError_t launch_mom_sweep32(const Mesh& m, double omega, double tol, FP<10> c, FP<3> din,
                                FP<3> dout, int limit, double* partials, DevScalars* ds,
                                cudaStream_t st) {
-  DISPATCH_DIM(m, k_mom_sweep32, m, (float)omega, tol, c, din, dout, limit, partials, ds);
+  DISPATCH_DIM_P(m, k_mom_sweep32, m, (float)omega, tol, c, din, dout, limit, partials, ds);
 }
 
 cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st) {
@@ -1065,7 +1089,7 @@ cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st) {
 cudaError_t launch_mom_sweep(const Mesh& m, double omega, double tol, CP<7> coef, C3 res,
                              C3 din, W3 dout, int limit, double* partials, DevScalars* ds,
                              cudaStream_t st) {
-  DISPATCH_DIM(m, k_mom_sweep, m, omega, tol, coef, res, din, dout, limit, partials, ds);
+  DISPATCH_DIM_P(m, k_mom_sweep, m, omega, tol, coef, res, din, dout, limit, partials, ds);
 }
 
 cudaError_t launch_pressure_rhs(const Mesh& m, const double* Fs, const double* Sv, double* f,
@@ -1078,7 +1102,7 @@ cudaError_t launch_correct(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du,
                            double* p_ic, const double* pc, const double* Dc, const double* Fs,
                            const double* kf, double* F_ic, FP<3> u32, float* p32, float* F32,
                            double* partials, DevScalars* ds, cudaStream_t st) {
-  DISPATCH_DIM(m, k_correct, m, make_geo(m), fc, u_prev, du, du32, Dc32, u_ic, p_ip, p_ic, pc,
+  DISPATCH_DIM_P(m, k_correct, m, make_geo(m), fc, u_prev, du, du32, Dc32, u_ic, p_ip, p_ic, pc,
                Dc, Fs, kf, F_ic, u32, p32, F32, partials, ds);
 }
 
@@ -1091,15 +1115,9 @@ cudaError_t launch_simpler_rhs(const Mesh& m, const FluidCoef& fc, CP<7> coef, C
   Geo g = make_geo(m);
   C3 evc{};
   for (int k = 0; k < 3; ++k) evc.a[k] = ev.a[k];
-  if (m.dim == 3) {
-    k_simpler_eval<3><<<L.grid, L.block, 0, st>>>(m, coef, res, uic, up, fres, gp, ev, L.kch);
-    k_simpler_rhs<3><<<L.grid, L.block, 0, st>>>(m, g, fc, evc, force, Dc, Fic, uic, kf, dg, p,
-                                                 pin, pin_value, f, L.kch);
-  } else {
-    k_simpler_eval<2><<<L.grid, L.block, 0, st>>>(m, coef, res, uic, up, fres, gp, ev, L.kch);
-    k_simpler_rhs<2><<<L.grid, L.block, 0, st>>>(m, g, fc, evc, force, Dc, Fic, uic, kf, dg, p,
-                                                 pin, pin_value, f, L.kch);
-  }
+  CELL_LAUNCH_P(m, L, st, k_simpler_eval, m, coef, res, uic, up, fres, gp, ev);
+  CELL_LAUNCH_P(m, L, st, k_simpler_rhs, m, g, fc, evc, force, Dc, Fic, uic, kf, dg, p, pin,
+                pin_value, f);
   count_launches(2);
   return cudaGetLastError();
 }
@@ -1131,7 +1149,7 @@ cudaError_t launch_props(const Mesh& m, int nph, const PhaseProps& pp, CP<HYDRO_
 }
 
 cudaError_t launch_smooth(const Mesh& m, const double* in, double* out, cudaStream_t st) {
-  DISPATCH_DIM(m, k_smooth, m, in, out);
+  DISPATCH_DIM_P(m, k_smooth, m, in, out);
 }
 
 cudaError_t launch_stforce(const Mesh& m, double sigma, const double* alpha1, W3 G, W3 out,
@@ -1139,13 +1157,8 @@ cudaError_t launch_stforce(const Mesh& m, double sigma, const double* alpha1, W3
   Launch L = cell_launch(m);
   Geo g = make_geo(m);
   C3 Gc = {{G.a[0], G.a[1], G.a[2]}};
-  if (m.dim == 3) {
-    k_scal_grad<3><<<L.grid, L.block, 0, st>>>(m, g, alpha1, G, L.kch);
-    k_stforce<3><<<L.grid, L.block, 0, st>>>(m, g, sigma, Gc, out, L.kch);
-  } else {
-    k_scal_grad<2><<<L.grid, L.block, 0, st>>>(m, g, alpha1, G, L.kch);
-    k_stforce<2><<<L.grid, L.block, 0, st>>>(m, g, sigma, Gc, out, L.kch);
-  }
+  CELL_LAUNCH_P(m, L, st, k_scal_grad, m, g, alpha1, G);
+  CELL_LAUNCH_P(m, L, st, k_stforce, m, g, sigma, Gc, out);
   count_launches(2);
   return cudaGetLastError();
 }

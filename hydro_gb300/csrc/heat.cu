@@ -39,8 +39,9 @@ __global__ void k_heat_conductivity(Mesh m, int nph, HeatCoef hc, CP<HYDRO_MAXPH
 // mean of their cells, boundary faces the box temperature or (zero
 // derivative) the cell's own value (Gradient(Interpolate(T, cond)),
 // solver.hpp:246-341, 392-470).
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void k_heat_grad(Mesh m, Geo g, HeatBc bc, const double* T, W3 G, int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
   const double tc = T[X.c];
 #pragma unroll
@@ -63,10 +64,11 @@ __global__ void k_heat_grad(Mesh m, Geo g, HeatBc bc, const double* T, W3 G, int
 // time difference.  Boundary faces: the box temperature gives a convective
 // constant and a half-cell diffusive coupling; a zero-derivative face
 // convects the cell value and has no diffusive flux.
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void k_heat_assemble(Mesh m, Geo g, HeatBc bc, HeatCoef hc, const double* Tp,
                                 const double* Ttc, const double* Ttp, const double* F,
                                 const double* kc, C3 G, WP<7> coef, double* res, int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
   const double kcc = kc[X.c];
   double aPc = 0.;  // convective and diffusive part of the diagonal
@@ -127,11 +129,12 @@ __global__ void k_heat_assemble(Mesh m, Geo g, HeatBc bc, HeatCoef hc, const dou
 }
 
 // Jacobi::Solve (linear.hpp:750-782) with omega 1 on one component.
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void __launch_bounds__(NT) k_heat_sweep(Mesh m, double tol, CP<7> coef,
                                                    const double* res, const double* din,
                                                    double* dout, int limit, double* partials,
                                                    DevScalars* ds, int kch) {
+  constexpr bool kPerT = PER;
   if (ds->flag[FL_HEAT_DONE] || ds->flag[FL_HEAT_SWEEPS] >= limit) return;
   const bool first = ds->flag[FL_HEAT_SWEEPS] == 0;
   double dmax = 0.;
@@ -184,6 +187,13 @@ __global__ void k_heat_finish(long long n, double* tc, double* tp, const double*
     count_launches(1);                                               \
     return cudaGetLastError();                                       \
   } while (0)
+#define HEAT_DISPATCH_P(m, KERNEL, ...)                              \
+  do {                                                               \
+    Launch L = cell_launch(m);                                       \
+    CELL_LAUNCH_P(m, L, st, KERNEL, __VA_ARGS__);                    \
+    count_launches(1);                                               \
+    return cudaGetLastError();                                       \
+  } while (0)
 
 cudaError_t launch_heat_conductivity(const Mesh& m, int nph, const HeatCoef& hc,
                                      CP<HYDRO_MAXPH> alpha, double* kc, cudaStream_t st) {
@@ -192,20 +202,20 @@ cudaError_t launch_heat_conductivity(const Mesh& m, int nph, const HeatCoef& hc,
 
 cudaError_t launch_heat_grad(const Mesh& m, const HeatBc& bc, const double* T, W3 G,
                              cudaStream_t st) {
-  HEAT_DISPATCH(m, k_heat_grad, m, make_geo(m), bc, T, G);
+  HEAT_DISPATCH_P(m, k_heat_grad, m, make_geo(m), bc, T, G);
 }
 
 cudaError_t launch_heat_assemble(const Mesh& m, const HeatBc& bc, const HeatCoef& hc,
                                  const double* Tp, const double* Ttc, const double* Ttp,
                                  const double* F, const double* kc, C3 G, WP<7> coef,
                                  double* res, cudaStream_t st) {
-  HEAT_DISPATCH(m, k_heat_assemble, m, make_geo(m), bc, hc, Tp, Ttc, Ttp, F, kc, G, coef, res);
+  HEAT_DISPATCH_P(m, k_heat_assemble, m, make_geo(m), bc, hc, Tp, Ttc, Ttp, F, kc, G, coef, res);
 }
 
 cudaError_t launch_heat_sweep(const Mesh& m, double tol, CP<7> coef, const double* res,
                               const double* din, double* dout, int limit, double* partials,
                               DevScalars* ds, cudaStream_t st) {
-  HEAT_DISPATCH(m, k_heat_sweep, m, tol, coef, res, din, dout, limit, partials, ds);
+  HEAT_DISPATCH_P(m, k_heat_sweep, m, tol, coef, res, din, dout, limit, partials, ds);
 }
 
 cudaError_t launch_heat_finish(long long n, double* tc, double* tp, const double* du0,

@@ -32,23 +32,18 @@ namespace {
 
 // Matrix-free stencil product (A p)_c = diag_c p_c - sum_f kf_f p_nb with a
 // pinned cell's row the identity and its value excluded from neighbours'.
-template <int DIM, class T>
+template <int DIM, bool PER, class T>
 __device__ __forceinline__ T stencil_row(const Mesh& m, const Cell& X, const T* kf,
                                          const T* dg, const T* p, long long pin) {
+  constexpr bool kPerT = PER;
   if (X.c == pin) return p[X.c];
   T acc = dg[X.c] * p[X.c];
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     long long s = cell_stride(m, d);
     long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
-    if (HAS_LO(d)) {
-      const long long cl = NB_LO(d, s);
-      if (cl != pin) acc -= kf[fl] * p[cl];
-    }
-    if (HAS_HI(d)) {
-      const long long ch = NB_HI(d, s);
-      if (ch != pin) acc -= kf[fl + face_stride(m, d)] * p[ch];
-    }
+    if (HAS_LO(d) && NB_LO(d, s) != pin) acc -= kf[fl] * p[NB_LO(d, s)];
+    if (HAS_HI(d) && NB_HI(d, s) != pin) acc -= kf[fl + face_stride(m, d)] * p[NB_HI(d, s)];
   }
   return acc;
 }
@@ -99,7 +94,7 @@ __global__ void k_sub_mean(long long n, double* x, const double* sum) {
 
 // r = f - mean(f) - A x (x == 0 unless use_guess), z = r/diag, p = z;
 // reduces <r,z>, <r,r>, <f',f'> and sets the tolerance and done flag.
-template <int DIM, class T>
+template <int DIM, class T, bool PER>
 __global__ void __launch_bounds__(NT) k_cg_init(Mesh m, const T* kf, const T* dg, const T* idg,
                                                 const double* f, const double* fmean_sum,
                                                 const T* x, int use_guess, long long pin,
@@ -111,7 +106,7 @@ __global__ void __launch_bounds__(NT) k_cg_init(Mesh m, const T* kf, const T* dg
   CELL_LOOP_BEGIN(m, kch)
   double fc = f[X.c] - mean;
   double rc = fc;
-  if (use_guess) rc -= (double)stencil_row<DIM>(m, X, kf, dg, x, pin);
+  if (use_guess) rc -= (double)stencil_row<DIM, PER>(m, X, kf, dg, x, pin);
   T rt = (T)rc;
   T zt = rt * idg[X.c];
   r[X.c] = rt;
@@ -146,14 +141,14 @@ __global__ void k_cg_dir(long long n, const T* z, T* p, const DevScalars* ds) {
     p[i] = z[i] + beta * p[i];
 }
 
-template <int DIM, class T>
+template <int DIM, class T, bool PER>
 __global__ void __launch_bounds__(NT) k_cg_spmv(Mesh m, const T* kf, const T* dg, const T* p,
                                                 T* Ap, long long pin, double* partials,
                                                 DevScalars* ds, int kch) {
   if (ds->flag[FL_PCG_DONE]) return;
   double s = 0.;
   CELL_LOOP_BEGIN(m, kch)
-  T a = stencil_row<DIM>(m, X, kf, dg, p, pin);
+  T a = stencil_row<DIM, PER>(m, X, kf, dg, p, pin);
   Ap[X.c] = a;
   s += (double)p[X.c] * (double)a;
   CELL_LOOP_END
@@ -202,7 +197,7 @@ __global__ void __launch_bounds__(NT) k_cg_update(long long n, TX* x, T* r, T* z
 
 // FP64 residual of the refinement loop: r = f' - A x (f' = f - mean when
 // singular), <r,r> reduced; r also written as FP32 for the inner solve.
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void __launch_bounds__(NT) k_ir_residual(Mesh m, const double* kf, const double* dg,
                                                     const double* f, const double* fmean_sum,
                                                     const double* x, long long pin, double* r,
@@ -210,7 +205,7 @@ __global__ void __launch_bounds__(NT) k_ir_residual(Mesh m, const double* kf, co
   double s = 0.;
   double mean = fmean_sum ? *fmean_sum / (double)m.nc : 0.;
   CELL_LOOP_BEGIN(m, kch)
-  double rc = (f[X.c] - mean) - stencil_row<DIM>(m, X, kf, dg, x, pin);
+  double rc = (f[X.c] - mean) - stencil_row<DIM, PER>(m, X, kf, dg, x, pin);
   r[X.c] = rc;
   s += rc * rc;
   CELL_LOOP_END
@@ -231,20 +226,8 @@ int flat_blocks_l(long long n) {
 }  // namespace
 
 // ---------------------------------------------------------- drivers ------
-#define LAUNCH_DIM(KERNEL, ...)                                        \
-  do {                                                                 \
-    if (m.dim == 3)                                                    \
-      KERNEL<3><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);       \
-    else                                                               \
-      KERNEL<2><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);       \
-  } while (0)
-#define LAUNCH_DIM_T(KERNEL, T, ...)                                   \
-  do {                                                                 \
-    if (m.dim == 3)                                                    \
-      KERNEL<3, T><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);    \
-    else                                                               \
-      KERNEL<2, T><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);    \
-  } while (0)
+#define LAUNCH_DIM(KERNEL, ...) CELL_LAUNCH_P(m, L, st, KERNEL, __VA_ARGS__)
+#define LAUNCH_DIM_T(KERNEL, T, ...) CELL_LAUNCH_TP(m, L, st, KERNEL, T, __VA_ARGS__)
 
 cudaError_t pcg_prepare(const Mesh& m, const double* kf, double shift, PcgWork& w, int fp32,
                         cudaStream_t st) {
@@ -362,12 +345,13 @@ struct DFAcc {
 
 // p_new = z + beta p_old (p_new = z on the first iteration) evaluated at the
 // cell and its neighbours, A p_new, <p_new, A p_new> -> alpha.
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void __launch_bounds__(NT) k_cg32_dir_spmv(Mesh m, const float* kf, const float* dg,
                                                       const float* z, const float* pold,
                                                       float* pnew, float* Ap, long long pin,
                                                       double* partials, DevScalars* ds,
                                                       int kch) {
+  constexpr bool kPerT = PER;
   if (ds->flag[FL_PCG_DONE]) return;
   const bool first = ds->flag[FL_PCG_ITERS] == 0;
   const float beta = first ? 0.f : (float)ds->red[RS_PCG_BETA];
@@ -385,14 +369,9 @@ __global__ void __launch_bounds__(NT) k_cg32_dir_spmv(Mesh m, const float* kf, c
     for (int d = 0; d < DIM; ++d) {
       long long s = cell_stride(m, d);
       long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
-      if (HAS_LO(d)) {
-        const long long cl = NB_LO(d, s);
-        if (cl != pin) a = fmaf(-kf[fl], P(cl), a);
-      }
-      if (HAS_HI(d)) {
-        const long long ch = NB_HI(d, s);
-        if (ch != pin) a = fmaf(-kf[fl + face_stride(m, d)], P(ch), a);
-      }
+      if (HAS_LO(d) && NB_LO(d, s) != pin) a = fmaf(-kf[fl], P(NB_LO(d, s)), a);
+      if (HAS_HI(d) && NB_HI(d, s) != pin)
+        a = fmaf(-kf[fl + face_stride(m, d)], P(NB_HI(d, s)), a);
     }
   }
   Ap[X.c] = a;
@@ -448,12 +427,7 @@ cudaError_t cg32_dir_spmv(const Mesh& m, const float* kf, const float* dg, const
                           const float* pold, float* pnew, float* Ap, long long pin,
                           double* partials, DevScalars* ds, cudaStream_t st) {
   Launch L = cell_launch(m);
-  if (m.dim == 3)
-    k_cg32_dir_spmv<3><<<L.grid, L.block, 0, st>>>(m, kf, dg, z, pold, pnew, Ap, pin, partials,
-                                                   ds, L.kch);
-  else
-    k_cg32_dir_spmv<2><<<L.grid, L.block, 0, st>>>(m, kf, dg, z, pold, pnew, Ap, pin, partials,
-                                                   ds, L.kch);
+  CELL_LAUNCH_P(m, L, st, k_cg32_dir_spmv, m, kf, dg, z, pold, pnew, Ap, pin, partials, ds);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -467,12 +441,8 @@ cudaError_t f32_pcg_iterate(const Mesh& m, int chunk, PcgWork& w, cudaStream_t s
     float* pold = (w.p32_parity & 1) ? w.p32b : w.p32;
     float* pnew = (w.p32_parity & 1) ? w.p32 : w.p32b;
     if (w.prof) w.prof->begin(PG_CG_SPMV, st);
-    if (m.dim == 3)
-      k_cg32_dir_spmv<3><<<L.grid, L.block, 0, st>>>(m, w.kf32, w.dg32, w.z32, pold, pnew, w.Ap32,
-                                                     w.pin, w.partials, w.ds, L.kch);
-    else
-      k_cg32_dir_spmv<2><<<L.grid, L.block, 0, st>>>(m, w.kf32, w.dg32, w.z32, pold, pnew, w.Ap32,
-                                                     w.pin, w.partials, w.ds, L.kch);
+    CELL_LAUNCH_P(m, L, st, k_cg32_dir_spmv, m, w.kf32, w.dg32, w.z32, pold, pnew, w.Ap32, w.pin,
+                  w.partials, w.ds);
     if (w.prof) w.prof->end(PG_CG_SPMV, st);
     if (w.prof) w.prof->begin(PG_CG_UPDATE, st);
     k_cg32_update<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.x32, w.r32, w.z32, pnew, w.Ap32, w.idg32,

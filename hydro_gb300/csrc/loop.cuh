@@ -52,19 +52,49 @@ __device__ __forceinline__ T grad_extrap(const T* p, long long c, int id, int nd
   return (p[c] - p[c - s]) * inv_h;
 }
 // The same along direction d of mesh m, central across a periodic end.
-template <class T>
+template <bool P, class T>
 __device__ __forceinline__ T grad_extrap_m(const Mesh& m, const T* p, long long c, int d,
                                            int id, long long s, T inv_h) {
-  if (m.per[d])
-    return (p[nb_hi(m, d, id, c, s)] - p[nb_lo(m, d, id, c, s)]) * (T(0.5) * inv_h);
+  if (P && m.per[d])
+    return (p[nb_hi_p<P>(m, d, id, c, s)] - p[nb_lo_p<P>(m, d, id, c, s)]) *
+           (T(0.5) * inv_h);
   return grad_extrap(p, c, id, m.n[d], s, inv_h);
 }
 
 // Shorthands inside CELL_LOOP bodies: neighbours of the cell X along d.
-#define HAS_LO(d) has_lo(m, (d), X.i[d])
-#define HAS_HI(d) has_hi(m, (d), X.i[d])
-#define NB_LO(d, s) nb_lo(m, (d), X.i[d], X.c, (s))
-#define NB_HI(d, s) nb_hi(m, (d), X.i[d], X.c, (s))
+// kPerT is the periodic switch of the enclosing kernel: a kernel
+// instantiated per periodicity declares `constexpr bool kPerT = PER;`,
+// others see this default (wrap test always compiled in).
+constexpr bool kPerT = true;
+#define HAS_LO(d) (kPerT ? has_lo(m, (d), X.i[d]) : X.i[d] > 0)
+#define HAS_HI(d) (kPerT ? has_hi(m, (d), X.i[d]) : X.i[d] < m.n[d] - 1)
+#define NB_LO(d, s) (kPerT ? nb_lo(m, (d), X.i[d], X.c, (s)) : X.c - (s))
+#define NB_HI(d, s) (kPerT ? nb_hi(m, (d), X.i[d], X.c, (s)) : X.c + (s))
+
+// Launch KERNEL<dim[, T], periodic> on the cell grid L for the mesh's
+// dimension and periodicity (kernels with a trailing `bool PER` parameter).
+#define CELL_LAUNCH_P(m, L, st, KERNEL, ...)                                         \
+  do {                                                                               \
+    const bool p_ = any_periodic(m);                                                 \
+    if ((m).dim == 3) {                                                              \
+      if (p_) KERNEL<3, true><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch); \
+      else KERNEL<3, false><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);   \
+    } else {                                                                         \
+      if (p_) KERNEL<2, true><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch); \
+      else KERNEL<2, false><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);   \
+    }                                                                                \
+  } while (0)
+#define CELL_LAUNCH_TP(m, L, st, KERNEL, T, ...)                                        \
+  do {                                                                                  \
+    const bool p_ = any_periodic(m);                                                    \
+    if ((m).dim == 3) {                                                                 \
+      if (p_) KERNEL<3, T, true><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch); \
+      else KERNEL<3, T, false><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);   \
+    } else {                                                                            \
+      if (p_) KERNEL<2, T, true><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch); \
+      else KERNEL<2, T, false><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);   \
+    }                                                                                   \
+  } while (0)
 
 template <class T>
 struct GeoT {

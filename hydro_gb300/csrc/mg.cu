@@ -35,7 +35,7 @@ namespace {
 // x + cx(parent): the prolongation of the coarse correction fused into the
 // first post-smoothing half-sweep (the cells of the other color are
 // overwritten by the next half-sweep, which never reads their old value).
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void k_mg_smooth(Mesh m, const float* kf, const float* idg, const float* b, float* x,
                             int color, int zero, long long pin, const float* cx, int cnx,
                             int cny, const DevScalars* ds, int kch) {
@@ -62,16 +62,17 @@ __global__ void k_mg_smooth(Mesh m, const float* kf, const float* idg, const flo
         long long fl = face_id(m, d, i, j, k);
 #pragma unroll
         for (int side = 0; side < 2; ++side) {
-          bool in = side ? has_hi(m, d, id[d]) : has_lo(m, d, id[d]);
-          if (!in) continue;
-          long long nb = side ? nb_hi(m, d, id[d], c, s) : nb_lo(m, d, id[d], c, s);
-          if (nb == pin) continue;
+          bool in = side ? has_hi_p<PER>(m, d, id[d]) : has_lo_p<PER>(m, d, id[d]);
+          long long nb = side ? nb_hi_p<PER>(m, d, id[d], c, s) : nb_lo_p<PER>(m, d, id[d], c, s);
+          if (!in || nb == pin) continue;
           float xv = x[nb];
           if (cx) {
             int q[3] = {i, j, k};
             q[d] += side ? 1 : -1;
-            if (q[d] < 0) q[d] = m.n[d] - 1;
-            if (q[d] >= m.n[d]) q[d] = 0;
+            if (PER) {
+              if (q[d] < 0) q[d] = m.n[d] - 1;
+              if (q[d] >= m.n[d]) q[d] = 0;
+            }
             xv += cx[(q[0] >> 1) + (long long)cnx * ((q[1] >> 1) + (long long)cny * (q[2] >> 1))];
           }
           acc = fmaf(kf[side ? fl + face_stride(m, d) : fl], xv, acc);
@@ -132,7 +133,7 @@ __global__ void k_mg_diag(Mesh m, const float* kf, float* dg, float* idg, int kc
 
 // Coarse right-hand side = sum over the 2^DIM children of the fine residual
 // b - A x; also clears the coarse correction.
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void k_mg_restrict(Mesh fm, Mesh cm, const float* kf, const float* dg, const float* b,
                               const float* x, float* cb, float* cx, long long pin,
                               const DevScalars* ds, int kch) {
@@ -156,14 +157,11 @@ __global__ void k_mg_restrict(Mesh fm, Mesh cm, const float* kf, const float* dg
           for (int d = 0; d < DIM; ++d) {
             long long s = cell_stride(fm, d);
             long long fl = face_id(fm, d, id[0], id[1], id[2]);
-            if (has_lo(fm, d, id[d])) {
-              const long long cl = nb_lo(fm, d, id[d], c, s);
-              if (cl != pin) ax = fmaf(-kf[fl], x[cl], ax);
-            }
-            if (has_hi(fm, d, id[d])) {
-              const long long ch = nb_hi(fm, d, id[d], c, s);
-              if (ch != pin) ax = fmaf(-kf[fl + face_stride(fm, d)], x[ch], ax);
-            }
+            const long long cl = nb_lo_p<PER>(fm, d, id[d], c, s);
+            const long long ch = nb_hi_p<PER>(fm, d, id[d], c, s);
+            if (has_lo_p<PER>(fm, d, id[d]) && cl != pin) ax = fmaf(-kf[fl], x[cl], ax);
+            if (has_hi_p<PER>(fm, d, id[d]) && ch != pin)
+              ax = fmaf(-kf[fl + face_stride(fm, d)], x[ch], ax);
           }
           r = b[c] - ax;
         }
@@ -202,7 +200,7 @@ __device__ __forceinline__ void blk_ijk(const Mesh& m, int c, int* id) {
   id[2] = DIM == 3 ? r / m.n[1] : 0;
 }
 
-template <int DIM>
+template <int DIM, bool PER>
 __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const float* b,
                          float* x, int color, bool zero, long long pin) {
   const int n = (int)m.nc;
@@ -220,14 +218,11 @@ __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const
       for (int d = 0; d < DIM; ++d) {
         int s = (int)cell_stride(m, d);
         int fl = (int)face_id(m, d, id[0], id[1], id[2]);
-        if (has_lo(m, d, id[d])) {
-          const int cl = (int)nb_lo(m, d, id[d], c, s);
-          if (cl != pin) acc = fmaf(kf[fl], x[cl], acc);
-        }
-        if (has_hi(m, d, id[d])) {
-          const int ch = (int)nb_hi(m, d, id[d], c, s);
-          if (ch != pin) acc = fmaf(kf[fl + (int)face_stride(m, d)], x[ch], acc);
-        }
+        const int cl = nb_lo_p<PER>(m, d, id[d], c, s);
+        const int ch = nb_hi_p<PER>(m, d, id[d], c, s);
+        if (has_lo_p<PER>(m, d, id[d]) && cl != pin) acc = fmaf(kf[fl], x[cl], acc);
+        if (has_hi_p<PER>(m, d, id[d]) && ch != pin)
+          acc = fmaf(kf[fl + (int)face_stride(m, d)], x[ch], acc);
       }
     }
     x[c] = acc * idg[c];
@@ -236,7 +231,7 @@ __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const
 }
 
 // coarse rhs = sum over the children of the fine residual b - A x
-template <int DIM>
+template <int DIM, bool PER>
 __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, const float* b,
                              const float* x, float* cb, long long pin) {
   const int n = (int)cm.nc;
@@ -263,14 +258,10 @@ __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, co
               int fl = (int)face_id(fm, d, id[0], id[1], id[2]);
               float klo = kf[fl], khi = kf[fl + (int)face_stride(fm, d)];
               dg += klo + khi;
-              if (has_lo(fm, d, id[d])) {
-                const int cl = (int)nb_lo(fm, d, id[d], c, s);
-                if (cl != pin) off = fmaf(klo, x[cl], off);
-              }
-              if (has_hi(fm, d, id[d])) {
-                const int ch = (int)nb_hi(fm, d, id[d], c, s);
-                if (ch != pin) off = fmaf(khi, x[ch], off);
-              }
+              const int cl = nb_lo_p<PER>(fm, d, id[d], c, s);
+              const int ch = nb_hi_p<PER>(fm, d, id[d], c, s);
+              if (has_lo_p<PER>(fm, d, id[d]) && cl != pin) off = fmaf(klo, x[cl], off);
+              if (has_hi_p<PER>(fm, d, id[d]) && ch != pin) off = fmaf(khi, x[ch], off);
             }
             r = b[c] - (dg * x[c] - off);
           }
@@ -281,7 +272,7 @@ __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, co
   __syncthreads();
 }
 
-template <int DIM>
+template <int DIM, bool PER>
 __global__ void __launch_bounds__(kBlkThreads)
     k_mg_block_vcycle(MgBlock B, const float* btop, float* xtop, const DevScalars* ds) {
   if (ds->flag[FL_PCG_DONE]) return;
@@ -302,10 +293,10 @@ __global__ void __launch_bounds__(kBlkThreads)
     const float *kf = sm + B.ok[l], *idg = sm + B.oi[l], *b = sm + B.ob[l];
     float* x = sm + B.ox[l];
     for (int s = 0; s < ns; ++s) {
-      blk_half<DIM>(m, kf, idg, b, x, 0, s == 0, lp);
-      blk_half<DIM>(m, kf, idg, b, x, 1, false, lp);
+      blk_half<DIM, PER>(m, kf, idg, b, x, 0, s == 0, lp);
+      blk_half<DIM, PER>(m, kf, idg, b, x, 1, false, lp);
     }
-    blk_restrict<DIM>(m, B.m[l + 1], kf, b, x, sm + B.ob[l + 1], lp);
+    blk_restrict<DIM, PER>(m, B.m[l + 1], kf, b, x, sm + B.ob[l + 1], lp);
   }
   {
     const int l = B.nl - 1;
@@ -334,12 +325,12 @@ __global__ void __launch_bounds__(kBlkThreads)
     }
     const int half = B.coarse_sweeps / 2 > 0 ? B.coarse_sweeps / 2 : 1;
     for (int s = 0; s < half; ++s) {
-      blk_half<DIM>(m, kf, idg, b, x, 0, s == 0, lp);
-      blk_half<DIM>(m, kf, idg, b, x, 1, false, lp);
+      blk_half<DIM, PER>(m, kf, idg, b, x, 0, s == 0, lp);
+      blk_half<DIM, PER>(m, kf, idg, b, x, 1, false, lp);
     }
     for (int s = 0; s < half; ++s) {
-      blk_half<DIM>(m, kf, idg, b, x, 1, false, lp);
-      blk_half<DIM>(m, kf, idg, b, x, 0, false, lp);
+      blk_half<DIM, PER>(m, kf, idg, b, x, 1, false, lp);
+      blk_half<DIM, PER>(m, kf, idg, b, x, 0, false, lp);
     }
   }
   for (int l = B.nl - 2; l >= 0; --l) {
@@ -356,8 +347,8 @@ __global__ void __launch_bounds__(kBlkThreads)
     }
     __syncthreads();
     for (int s = 0; s < ns; ++s) {
-      blk_half<DIM>(m, kf, idg, b, x, 1, false, lp);
-      blk_half<DIM>(m, kf, idg, b, x, 0, false, lp);
+      blk_half<DIM, PER>(m, kf, idg, b, x, 1, false, lp);
+      blk_half<DIM, PER>(m, kf, idg, b, x, 0, false, lp);
     }
   }
   for (int q = tid; q < (int)B.m[0].nc; q += nt) xtop[q] = sm[B.ox[0] + q];
@@ -510,6 +501,18 @@ int mg_levels_for(const Mesh& m) {
       KERNEL<2><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);          \
     count_launches(1);                                                          \
   } while (0)
+// the same for kernels instantiated per periodicity (P: any periodic direction)
+#define MG_LAUNCH_P(KERNEL, L, P, ...)                                          \
+  do {                                                                          \
+    if (dim == 3) {                                                             \
+      if (P) KERNEL<3, true><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);   \
+      else KERNEL<3, false><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);   \
+    } else {                                                                    \
+      if (P) KERNEL<2, true><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);   \
+      else KERNEL<2, false><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);   \
+    }                                                                           \
+    count_launches(1);                                                          \
+  } while (0)
 
 // First level handled inside one CTA and that CTA's shared memory (x, b,
 // inverse diagonal and couplings of every level from there down, each
@@ -548,11 +551,13 @@ cudaError_t mg_prepare(MgWork& mg) {
   mg_plan_block(mg);
   if (mg.nlev > 0 && mg.top < mg.nlev) {
     if (mg.smem_bytes > 227 * 1024) return cudaErrorInvalidValue;
-    return mg.lev[0].m.dim == 3
-               ? cudaFuncSetAttribute(k_mg_block_vcycle<3>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, mg.smem_bytes)
-               : cudaFuncSetAttribute(k_mg_block_vcycle<2>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, mg.smem_bytes);
+    const bool per = any_periodic(mg.lev[0].m);
+    const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    if (mg.lev[0].m.dim == 3)
+      return per ? cudaFuncSetAttribute(k_mg_block_vcycle<3, true>, attr, mg.smem_bytes)
+                 : cudaFuncSetAttribute(k_mg_block_vcycle<3, false>, attr, mg.smem_bytes);
+    return per ? cudaFuncSetAttribute(k_mg_block_vcycle<2, true>, attr, mg.smem_bytes)
+               : cudaFuncSetAttribute(k_mg_block_vcycle<2, false>, attr, mg.smem_bytes);
   }
   return cudaSuccess;
 }
@@ -563,6 +568,7 @@ cudaError_t mg_prepare(MgWork& mg) {
 cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevScalars* ds,
                       cudaStream_t st) {
   int dim = mg.lev[0].m.dim;
+  const bool per = any_periodic(mg.lev[0].m);
   mg.lev[0].b = const_cast<float*>(r);
   mg.lev[0].x = z;
   const int ns = mg.nsweep;
@@ -572,12 +578,12 @@ cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevSc
     long long lp = l == 0 ? pin : -1;
     Launch H = half_launch(f.m);
     for (int s = 0; s < ns; ++s) {
-      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 0, s == 0, lp, nullptr, 0, 0, ds);
-      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, nullptr, 0, 0, ds);
+      MG_LAUNCH_P(k_mg_smooth, H, per, f.m, f.kf, f.idg, f.b, f.x, 0, s == 0, lp, nullptr, 0, 0, ds);
+      MG_LAUNCH_P(k_mg_smooth, H, per, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, nullptr, 0, 0, ds);
     }
     MgLevel& c = mg.lev[l + 1];
     Launch L = cell_launch(c.m);
-    MG_LAUNCH(k_mg_restrict, L, f.m, c.m, f.kf, f.dg, f.b, f.x, c.b, c.x, lp, ds);
+    MG_LAUNCH_P(k_mg_restrict, L, per, f.m, c.m, f.kf, f.dg, f.b, f.x, c.b, c.x, lp, ds);
   }
   if (mg.top < mg.nlev) {
     MgBlock B;
@@ -598,10 +604,13 @@ cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevSc
       B.ok[q] = off; off += f4;
     }
     MgLevel& t = mg.lev[mg.top];
-    if (dim == 3)
-      k_mg_block_vcycle<3><<<1, kBlkThreads, mg.smem_bytes, st>>>(B, t.b, t.x, ds);
-    else
-      k_mg_block_vcycle<2><<<1, kBlkThreads, mg.smem_bytes, st>>>(B, t.b, t.x, ds);
+    if (dim == 3) {
+      if (per) k_mg_block_vcycle<3, true><<<1, kBlkThreads, mg.smem_bytes, st>>>(B, t.b, t.x, ds);
+      else k_mg_block_vcycle<3, false><<<1, kBlkThreads, mg.smem_bytes, st>>>(B, t.b, t.x, ds);
+    } else {
+      if (per) k_mg_block_vcycle<2, true><<<1, kBlkThreads, mg.smem_bytes, st>>>(B, t.b, t.x, ds);
+      else k_mg_block_vcycle<2, false><<<1, kBlkThreads, mg.smem_bytes, st>>>(B, t.b, t.x, ds);
+    }
     count_launches(1);
   } else {
     // large coarsest level (odd dimensions) or a single level: symmetric
@@ -611,12 +620,12 @@ cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevSc
     Launch H = half_launch(cl.m);
     const int half = mg.coarse_sweeps_large / 2 > 0 ? mg.coarse_sweeps_large / 2 : 1;
     for (int s = 0; s < half; ++s) {
-      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, s == 0, lp, nullptr, 0, 0, ds);
-      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 1, 0, lp, nullptr, 0, 0, ds);
+      MG_LAUNCH_P(k_mg_smooth, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, s == 0, lp, nullptr, 0, 0, ds);
+      MG_LAUNCH_P(k_mg_smooth, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 1, 0, lp, nullptr, 0, 0, ds);
     }
     for (int s = 0; s < half; ++s) {
-      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 1, 0, lp, nullptr, 0, 0, ds);
-      MG_LAUNCH(k_mg_smooth, H, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, 0, lp, nullptr, 0, 0, ds);
+      MG_LAUNCH_P(k_mg_smooth, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 1, 0, lp, nullptr, 0, 0, ds);
+      MG_LAUNCH_P(k_mg_smooth, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, 0, lp, nullptr, 0, 0, ds);
     }
   }
   for (int l = top - 1; l >= 0; --l) {
@@ -627,8 +636,8 @@ cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevSc
     for (int s = 0; s < ns; ++s) {
       // the first half-sweep adds the coarse correction on the fly
       const float* cx = s == 0 ? c.x : nullptr;
-      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, cx, c.m.n[0], c.m.n[1], ds);
-      MG_LAUNCH(k_mg_smooth, H, f.m, f.kf, f.idg, f.b, f.x, 0, 0, lp, nullptr, 0, 0, ds);
+      MG_LAUNCH_P(k_mg_smooth, H, per, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, cx, c.m.n[0], c.m.n[1], ds);
+      MG_LAUNCH_P(k_mg_smooth, H, per, f.m, f.kf, f.idg, f.b, f.x, 0, 0, lp, nullptr, 0, 0, ds);
     }
   }
   return cudaGetLastError();
@@ -650,9 +659,7 @@ cudaError_t mgcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, MgW
 }
 
 cudaError_t mgcg_iterate(const Mesh& m, int chunk, PcgWork& w, MgWork& mg, cudaStream_t st) {
-  Launch L = cell_launch(m);
   int fb = flat_blocks_mg(m.nc);
-  int dim = m.dim;
   for (int it = 0; it < chunk; ++it) {
     float* pold = (w.p32_parity & 1) ? w.p32b : w.p32;
     float* pnew = (w.p32_parity & 1) ? w.p32 : w.p32b;
@@ -672,8 +679,6 @@ cudaError_t mgcg_iterate(const Mesh& m, int chunk, PcgWork& w, MgWork& mg, cudaS
     count_launches(2);
     w.p32_parity ^= 1;
   }
-  (void)L;
-  (void)dim;
   return cudaGetLastError();
 }
 
