@@ -94,6 +94,9 @@ class HydroDesc(ctypes.Structure):
         ("sharp", ctypes.c_double),
         ("stream", ctypes.c_void_p),
         ("periodic", ctypes.c_int * 3),
+        ("rigid_box", ctypes.c_int),
+        ("rigid_box_lo", ctypes.c_double * 3),
+        ("rigid_box_hi", ctypes.c_double * 3),
     ]
 
     @property
@@ -376,6 +379,23 @@ def _declare(lib, prefix):
                             ctypes.c_double, D, D, I, ctypes.c_double, I,
                             ctypes.POINTER(I), D]
     stencil.restype = I
+
+
+def fluid_mask(d):
+    """Cells outside the rigid box (centre not in [rigid_box_lo,
+    rigid_box_hi], inclusive), or None when the case has no box."""
+    if not d.rigid_box:
+        return None
+    import numpy as np
+    n = [d.n[k] if k < d.dim else 1 for k in range(3)]
+    idx = np.arange(n[0] * n[1] * n[2])
+    mi = [idx % n[0], (idx // n[0]) % n[1], idx // (n[0] * n[1])]
+    inside = np.ones(idx.size, dtype=bool)
+    for k in range(d.dim):
+        h = (d.hi[k] - d.lo[k]) / d.n[k]
+        xc = d.lo[k] + (mi[k] + 0.5) * h
+        inside &= (d.rigid_box_lo[k] <= xc) & (xc <= d.rigid_box_hi[k])
+    return ~inside
 
 
 def desc_to_dict(d):

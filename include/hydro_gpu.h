@@ -181,6 +181,14 @@ typedef struct hydro_desc {
    * and are solved as inner faces.  Multigrid needs an even cell count
    * along a periodic direction to coarsen it. */
   int periodic[3];
+  /* rigid box (hydro2d.hpp:306-423, keys box_A / box_B): cells whose centre
+   * lies in [rigid_box_lo, rigid_box_hi] (inclusive) are excluded
+   * (mesh3d.hpp:183-215): identity rows in the momentum and pressure
+   * systems, their state left as it is; the faces between them and the
+   * fluid are no-slip walls at rest; faces between excluded cells, and
+   * boundary faces of excluded cells, carry nothing.  0: no box. */
+  int rigid_box;
+  double rigid_box_lo[3], rigid_box_hi[3];
 } hydro_desc;
 
 typedef struct hydro_step_stats {

@@ -33,6 +33,10 @@ typedef struct {
   double h[3], V, A[3];
   double lo[3];
   int per[3]; /* periodic directions (mesh2d.hpp / mesh3d.hpp PERX, PERZ) */
+  /* excluded cells (rigid box, mesh3d.hpp:183-215), NULL = none: a face
+   * touching an excluded cell is not inner, and the excluded cell is not
+   * its neighbour; a face with no valid neighbour is excluded */
+  const unsigned char* ex;
 } Mesh;
 
 struct oracle_ctx {
@@ -116,8 +120,11 @@ static long cnb(const Mesh* m, const long* mi, int q) {
     if (!m->per[d]) return -1;
     a[d] = a[d] < 0 ? m->n[d] - 1 : 0;
   }
-  return cidx(m, a[0], a[1], a[2]);
+  long nb = cidx(m, a[0], a[1], a[2]);
+  if (m->ex && (m->ex[cidx(m, mi[0], mi[1], mi[2])] || m->ex[nb])) return -1;
+  return nb;
 }
+static int cex(const Mesh* m, long c) { return m->ex && m->ex[c]; }
 /* Decode face f: direction, multi-index, neighbour cells cm (id 0) and cp (id 1). */
 static void fdecode(const Mesh* m, long f, int* dir, long* mi, long* cm, long* cp) {
   int d = 0;
@@ -140,12 +147,22 @@ static void fdecode(const Mesh* m, long f, int* dir, long* mi, long* cm, long* c
     b[d] = 0;
     *cp = cidx(m, b[0], b[1], b[2]);
   }
+  if (m->ex) {
+    if (*cm >= 0 && m->ex[*cm]) *cm = -1;
+    if (*cp >= 0 && m->ex[*cp]) *cp = -1;
+  }
 }
 /* Side (enum hydro_side) of a boundary face, or -1 for an inner face. */
 static int fside(const Mesh* m, int d, const long* mi) {
   if (mi[d] == 0) return 2 * d;
   if (mi[d] == m->n[d]) return 2 * d + 1;
   return -1;
+}
+/* Condition kind of a boundary face: its side's, or a wall for a face
+ * between the rigid box and the fluid ("wall 0 0 0", hydro2d.hpp:386-396). */
+static int fkind(const hydro_desc* d, const Mesh* m, int dir, const long* mi) {
+  int side = fside(m, dir, mi);
+  return side < 0 ? HYDRO_BC_WALL : d->bc_kind[side];
 }
 static double outward(int q) { return (q % 2) ? 1. : -1.; }
 
@@ -189,12 +206,13 @@ static void interp(const Mesh* m, const double* fc, double* ff, int bc,
     long mi[3], cm, cp;
     fdecode(m, f, &d, mi, &cm, &cp);
     if (cm >= 0 && cp >= 0) continue;
+    if (cm < 0 && cp < 0) continue;  /* excluded face: no condition, 0 */
     int side = fside(m, d, mi);
     long cc = cm >= 0 ? cm : cp;
     double factor = cm >= 0 ? 1. : -1.;
     double dist = 0.5 * m->h[d];
     if (bc == BC_VALUE) {
-      ff[f] = bcval[side];
+      ff[f] = side >= 0 ? bcval[side] : 0.;
     } else if (bc == BC_FACE) {
       ff[f] = bcval[f];
     } else if (bc == BC_ZERODER) {
@@ -242,9 +260,11 @@ static void interp_vec(const Mesh* m, double* const* fc, double* const* ff, int 
       double an = sqrt(n2);
       for (int k = 0; k < dim; ++k)
         ff[k][f] = an < 1e-8 ? av[k] : av[k] / an * sqrt(sqrt(na) * sqrt(nb));
-    } else {
+    } else if (cm >= 0 || cp >= 0) {
       long cc = cm >= 0 ? cm : cp;
       for (int k = 0; k < dim; ++k) ff[k][f] = fc[k][cc];
+    } else {
+      for (int k = 0; k < dim; ++k) ff[k][f] = 0.;
     }
   }
 }
@@ -257,6 +277,10 @@ static void gradient(const Mesh* m, const double* ff, double* const* gc) {
     long mi[3];
     cmidx(m, c, mi);
     for (int d = 0; d < m->dim; ++d) {
+      if (cex(m, c)) {  /* excluded cells keep zero */
+        gc[d][c] = 0.;
+        continue;
+      }
       long flo = cface(m, mi, 2 * d), fhi = cface(m, mi, 2 * d + 1);
       double sum = (-m->A[d]) * ff[flo];
       sum += m->A[d] * ff[fhi];
@@ -406,7 +430,7 @@ static void stencil_apply(const Mesh* m, const double* k, double shift,
   long c;
 #pragma omp parallel for num_threads(g_threads)
   for (c = 0; c < m->nc; ++c) {
-    if (c == pin) {
+    if (c == pin || cex(m, c)) {  /* identity rows */
       y[c] = x[c];
       continue;
     }
@@ -427,7 +451,7 @@ static void stencil_apply(const Mesh* m, const double* k, double shift,
 static void stencil_diag(const Mesh* m, const double* k, double shift, long pin,
                          double* dg) {
   for (long c = 0; c < m->nc; ++c) {
-    if (c == pin) {
+    if (c == pin || cex(m, c)) {
       dg[c] = 1.;
       continue;
     }
@@ -451,12 +475,16 @@ static int pcg(const Mesh* m, const double* k, double shift, long pin,
   int singular = (shift == 0. && pin < 0);
   stencil_diag(m, k, shift, pin, dg);
   /* r = f (projected when singular) */
+  /* mean over the cells that are not excluded (the singular block) */
   double mean = 0.;
+  long nin = 0;
+  for (long i = 0; i < n; ++i) nin += !cex(m, i);
   if (singular) {
-    for (long i = 0; i < n; ++i) mean += f_in[i];
-    mean /= (double)n;
+    for (long i = 0; i < n; ++i)
+      if (!cex(m, i)) mean += f_in[i];
+    mean /= (double)nin;
   }
-  for (long i = 0; i < n; ++i) r[i] = f_in[i] - mean;
+  for (long i = 0; i < n; ++i) r[i] = cex(m, i) ? f_in[i] : f_in[i] - mean;
   double fnorm = sqrt(dotp(n, r, r));
   if (!use_guess) {
     for (long i = 0; i < n; ++i) x[i] = 0.;
@@ -493,9 +521,11 @@ static int pcg(const Mesh* m, const double* k, double shift, long pin,
   }
   if (singular) {
     double xm = 0.;
-    for (long i = 0; i < n; ++i) xm += x[i];
-    xm /= (double)n;
-    for (long i = 0; i < n; ++i) x[i] -= xm;
+    for (long i = 0; i < n; ++i)
+      if (!cex(m, i)) xm += x[i];
+    xm /= (double)nin;
+    for (long i = 0; i < n; ++i)
+      if (!cex(m, i)) x[i] -= xm;
   }
   *iters = it;
   *res = rnorm / fnorm;
@@ -581,6 +611,34 @@ int oracle_create(const hydro_desc* desc, oracle_ctx** out) {
     return HYDRO_ERR_ARG;
   }
   for (int d = 0; d < desc->dim; ++d) x->m.per[d] = desc->periodic[d] != 0;
+  if (desc->rigid_box) {
+    /* cells whose centre lies in the box (Rect::IsInside, inclusive) */
+    if (desc->simpler) {
+      free(x);
+      return HYDRO_ERR_UNSUPPORTED;
+    }
+    unsigned char* ex = (unsigned char*)calloc((size_t)x->m.nc, 1);
+    long any = 0;
+    for (long c = 0; c < x->m.nc; ++c) {
+      long mi[3];
+      cmidx(&x->m, c, mi);
+      int in = 1;
+      for (int k = 0; k < desc->dim; ++k) {
+        double xc = x->m.lo[k] + (mi[k] + 0.5) * x->m.h[k];
+        if (xc < desc->rigid_box_lo[k] || desc->rigid_box_hi[k] < xc) in = 0;
+      }
+      ex[c] = (unsigned char)in;
+      any += in;
+    }
+    if (desc->pressure_fixed_cell >= 0 && desc->pressure_fixed_cell < x->m.nc &&
+        ex[desc->pressure_fixed_cell]) {
+      free(ex);
+      free(x);
+      return HYDRO_ERR_ARG;
+    }
+    if (any) x->m.ex = ex;
+    else free(ex);
+  }
   for (int s = 0; s < 2 * desc->dim; ++s)
     if (desc->bc_kind[s] < HYDRO_BC_WALL || desc->bc_kind[s] > HYDRO_BC_OUTLET) {
       free(x);
@@ -621,7 +679,9 @@ int oracle_create(const hydro_desc* desc, oracle_ctx** out) {
     long mi[3], cm, cp;
     fdecode(m, f, &d, mi, &cm, &cp);
     if (cm >= 0 && cp >= 0) continue;
+    if (cm < 0 && cp < 0) continue;  /* excluded face */
     int side = fside(m, d, mi);
+    if (side < 0) continue;          /* rigid-box wall at rest */
     for (int k = 0; k < desc->dim; ++k)
       x->bcu[k][f] = desc->bc_kind[side] == HYDRO_BC_OUTLET ? 0. : desc->bc_velocity[side][k];
   }
@@ -655,6 +715,7 @@ int oracle_destroy(oracle_ctx* x) {
   for (int i = 0; i < 10; ++i) free(x->fw[i]);
   for (int i = 0; i < 24; ++i) free(x->cw[i]);
   free(x->rows); free(x->rowc);
+  free((void*)x->m.ex);
   free(x);
   return HYDRO_OK;
 }
@@ -827,7 +888,8 @@ int oracle_init_state(oracle_ctx* x) {
     long mi[3], cm, cp;
     fdecode(m, f, &d, mi, &cm, &cp);
     if (cm >= 0 && cp >= 0) continue;
-    if (x->d.bc_kind[fside(m, d, mi)] != HYDRO_BC_INLET) continue;
+    if (cm < 0 && cp < 0) continue;
+    if (fkind(&x->d, m, d, mi) != HYDRO_BC_INLET) continue;
     for (int i = 0; i < x->nph; ++i) x->qin[i][f] = x->q[i][cm >= 0 ? cm : cp];
   }
   for (int k = 0; k < dim; ++k) {
@@ -931,7 +993,7 @@ static void assemble_scalar(oracle_ctx* x, const double* u_prev, const double* u
         int dd;
         long mi[3], cm, cp;
         fdecode(m, f, &dd, mi, &cm, &cp);
-        ff[f] = u_prev[cm >= 0 ? cm : cp];
+        if (cm >= 0 || cp >= 0) ff[f] = u_prev[cm >= 0 ? cm : cp];
       }
   gradient(m, ff, gc);
   double co[3];
@@ -941,6 +1003,13 @@ static void assemble_scalar(oracle_ctx* x, const double* u_prev, const double* u
   for (c = 0; c < m->nc; ++c) {
     long mi[3];
     cmidx(m, c, mi);
+    if (cex(m, c)) {
+      /* excluded cell: identity row, zero constant (conv_diff.hpp:222-226) */
+      for (int t = 0; t < w; ++t) x->rows[c * w + t] = 0.;
+      x->rows[c * w + slot_c(dim)] = 1.;
+      x->rowc[c] = 0.;
+      continue;
+    }
     double cfl[MAXW] = {0}, dfl[MAXW] = {0};
     double cconst = 0., dconst = 0.;
     int sc = slot_c(dim);
@@ -1072,7 +1141,8 @@ static void update_outlets(oracle_ctx* x) {
     long mi[3], cm, cp;
     fdecode(m, f, &dd, mi, &cm, &cp);
     if (cm >= 0 && cp >= 0) continue;
-    int kind = d->bc_kind[fside(m, dd, mi)];
+    if (cm < 0 && cp < 0) continue;
+    int kind = fkind(d, m, dd, mi);
     int id = cm >= 0 ? 0 : 1;
     long cc = id == 0 ? cm : cp;
     if (kind == HYDRO_BC_OUTLET) {
@@ -1092,7 +1162,8 @@ static void update_outlets(oracle_ctx* x) {
     long mi[3], cm, cp;
     fdecode(m, f, &dd, mi, &cm, &cp);
     if (cm >= 0 && cp >= 0) continue;
-    if (d->bc_kind[fside(m, dd, mi)] != HYDRO_BC_OUTLET) continue;
+    if (cm < 0 && cp < 0) continue;
+    if (fkind(d, m, dd, mi) != HYDRO_BC_OUTLET) continue;
     double factor = cm >= 0 ? 1. : -1.;
     x->bcu[dd][f] = x->bcu[dd][f] + corr * factor;
   }
@@ -1237,10 +1308,17 @@ int oracle_make_iteration(oracle_ctx* x) {
     }
   }
 
-  /* pressure-correction system (fluid.hpp:972-1014) */
+  /* pressure-correction system (fluid.hpp:972-1014); excluded cells:
+   * identity rows with zero constant */
   for (long c = 0; c < nc; ++c) {
     long mi[3];
     cmidx(m, c, mi);
+    if (cex(m, c)) {
+      for (int t = 0; t < w; ++t) x->rows[c * w + t] = 0.;
+      x->rows[c * w + slot_c(dim)] = 1.;
+      x->rowc[c] = 0.;
+      continue;
+    }
     double a[MAXW] = {0};
     double cst = 0.;
     int sc = slot_c(dim);
@@ -1475,6 +1553,7 @@ int oracle_get_auto_time_step(oracle_ctx* x, double* out) {
   double dt = 1e10;
   const double* F = x->F[HYDRO_TIME_CURR];
   for (long c = 0; c < m->nc; ++c) {
+    if (cex(m, c)) continue;  /* fluid.hpp:1195 */
     long mi[3];
     cmidx(m, c, mi);
     for (int q = 0; q < 2 * m->dim; ++q) {
@@ -1538,7 +1617,8 @@ static void advection_iteration(oracle_ctx* x) {
         long mi[3], P, E;
         fdecode(m, f, &dd, mi, &P, &E);
         if (P >= 0 && E >= 0) continue;
-        if (d->bc_kind[fside(m, dd, mi)] == HYDRO_BC_INLET) ff[f] = x->qin[i][f];
+        if (P < 0 && E < 0) continue;
+        if (fkind(d, m, dd, mi) == HYDRO_BC_INLET) ff[f] = x->qin[i][f];
       }
       gradient(m, ff, gc);
       /* InterpolateSuperbee (solver.hpp:560-619) */
@@ -1557,7 +1637,9 @@ static void advection_iteration(oracle_ctx* x) {
           } else {
             qf[f] = 0.5 * (cur[P] + cur[E]);
           }
-        } else if (d->bc_kind[fside(m, dd, mi)] == HYDRO_BC_INLET) {
+        } else if (P < 0 && E < 0) {
+          qf[f] = 0.;  /* excluded face: no condition */
+        } else if (fkind(d, m, dd, mi) == HYDRO_BC_INLET) {
           qf[f] = x->qin[i][f];
         } else {
           qf[f] = cur[P >= 0 ? P : E] + 0. * (0.5 * m->h[dd]);

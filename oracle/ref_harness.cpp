@@ -114,8 +114,15 @@ struct Case {
     nph = d.num_phases;
     size_t nc = mesh.GetNumCells();
 
-    // fluid conditions: one per boundary face (hydro2d.hpp:357-383)
+    // fluid conditions: one per boundary face (hydro2d.hpp:357-383); with a
+    // rigid box, "wall 0 0 0" on the faces between box and fluid cells,
+    // then the box cells are excluded and the conditions of excluded faces
+    // erased (hydro2d.hpp:306-423)
     geom::MapFace<std::shared_ptr<solver::ConditionFaceFluid>> fluid_cond;
+    geom::Rect<Vect> rigid_box(V3(d.rigid_box_lo), V3(d.rigid_box_hi));
+    auto in_box = [&](IdxCell c) {
+      return d.rigid_box && !c.IsNone() && rigid_box.IsInside(mesh.GetCenter(c));
+    };
     for (auto f : mesh.Faces()) {
       if (!mesh.IsInner(f)) {
         int s = Side(f);
@@ -130,7 +137,18 @@ struct Case {
           fluid_cond[f] =
               std::make_shared<solver::fluid_condition::NoSlipWallFixed<Mesh>>(vel);
         }
+      } else if (in_box(mesh.GetNeighbourCell(f, 0)) != in_box(mesh.GetNeighbourCell(f, 1))) {
+        fluid_cond[f] =
+            std::make_shared<solver::fluid_condition::NoSlipWallFixed<Mesh>>(Vect(0));
       }
+    }
+    if (d.rigid_box) {
+      std::vector<IdxCell> excluded;
+      for (auto c : mesh.Cells())
+        if (in_box(c)) excluded.push_back(c);
+      mesh.ExcludeCells(excluded);
+      for (auto f : mesh.Faces())
+        if (mesh.IsExcluded(f)) fluid_cond.erase(f);
     }
     geom::MapCell<std::shared_ptr<solver::ConditionCellFluid>> mc_cond;
     if (d.pressure_fixed_cell >= 0) {
@@ -179,15 +197,15 @@ struct Case {
       v_p_fc_mass_source[i] = &v_fc_mass_source[i];
       q_init[i].Reinit(mesh);
       for (size_t c = 0; c < nc; ++c) q_init[i][IdxCell(c)] = q0[i * nc + c];
-      for (auto f : mesh.Faces()) {
-        if (!mesh.IsInner(f)) {
-          if (d.bc_kind[Side(f)] == HYDRO_BC_INLET) {
-            IdxCell cc = mesh.GetNeighbourCell(f, mesh.GetValidNeighbourCellId(f));
-            v_cond[i][f] = std::make_shared<solver::ConditionFaceValueFixed<Scal>>(
-                q_init[i][cc]);
-          } else {
-            v_cond[i][f] = std::make_shared<solver::ConditionFaceDerivativeFixed<Scal>>(0.);
-          }
+      // one per fluid condition (hydro2d.hpp:563-583): inlets hold the
+      // initial value of their cell, the others zero derivative
+      for (auto it = fluid_cond.cbegin(); it != fluid_cond.cend(); ++it) {
+        IdxFace f = it->GetIdx();
+        if (dynamic_cast<solver::fluid_condition::Inlet<Mesh>*>(it->GetValue().get())) {
+          IdxCell cc = mesh.GetNeighbourCell(f, mesh.GetValidNeighbourCellId(f));
+          v_cond[i][f] = std::make_shared<solver::ConditionFaceValueFixed<Scal>>(q_init[i][cc]);
+        } else {
+          v_cond[i][f] = std::make_shared<solver::ConditionFaceDerivativeFixed<Scal>>(0.);
         }
       }
     }

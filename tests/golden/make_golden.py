@@ -179,6 +179,38 @@ def golden_cases():
     h = heat(d.dt, lo=(0.25, -1.0, -1.0), hi=(0.6, 0.0, 10.0))
     out.append(("heat_dam2d_periodic_x", d, u0, q0, 2, True, h))
 
+    # rigid box (hydro2d.hpp:306-423): excluded cells, walls at rest
+    # around them; in a channel (obstacle in the stream), touching the
+    # bottom wall of a cavity, on the floor under a breaking dam, in 3D
+    def box(d, lo, hi):
+        d.rigid_box = 1
+        for k in range(3):
+            d.rigid_box_lo[k], d.rigid_box_hi[k] = lo[k], hi[k]
+        return d
+
+    d, u0, q0 = cases.channel(nx=24, ny=12, dt=1e-2, two_phase=True)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    out.append(("box_channel2d", box(d, (0.3, 0.3, 0), (0.5, 0.6, 0)), u0, q0, 3, True))
+
+    d, u0, q0 = cases.cavity(n=16, mu=0.01, dt=1e-2)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    out.append(("box_cavity2d", box(d, (0.3, 0.0, 0), (0.55, 0.4, 0)), u0, q0, 3, True))
+
+    d, u0, q0 = cases.broken_dam(nx=24, ny=12, dt_auto=False, dt=1e-3, smooth_times=2)
+    tight(d, p_tol=1e-10)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    out.append(("box_dam2d", box(d, (1.8, -1.0, 0), (2.4, 0.45, 0)), u0, q0, 2, True))
+
+    d, u0, q0 = cases.cavity(n=8, dim=3, dt=1e-2)
+    d.n[0], d.n[2] = 10, 6
+    u0, q0 = np.zeros(d.ncells * 3), np.ones(d.ncells)
+    u0[: d.ncells] = 0.1 * np.sin(2 * np.pi * (np.arange(d.ncells) % 10) / 10.0)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    out.append(("box_cavity3d", box(d, (0.3, 0.2, 0.3), (0.65, 0.6, 0.7)), u0, q0, 2, True))
+
     # reference defaults for the linear solvers: one LU sweep for velocity
     # (an approximate solve; CPU-only semantics), SOR pressure
     d, u0, q0 = cases.broken_dam(nx=16, ny=8, dt_auto=False, dt=2e-3, smooth_times=2)

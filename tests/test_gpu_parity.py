@@ -215,7 +215,7 @@ def test_gpu_matches_reference_golden(built, name):
         heat = capi.HeatDesc.from_buffer_copy(heat)
         heat.solver, heat.tolerance, heat.iters_limit = capi.LINEAR_JACOBI, 1e-15, 20000
     out = run(Hydro(d), g["u0"], g["q0"], g["nsteps"], heat=heat)
-    errs = compare(out, g)
+    errs = compare(out, g, capi.fluid_mask(d))
     assert all(v <= 1e-9 for v in errs.values()), errs
     assert [s["outer_iterations"] for s in out["stats"]] == list(g["outer_iterations"])
 
