@@ -60,13 +60,14 @@ __global__ void k_adv_faces(Mesh m, Geo g, int nph, int stage, int nstages, cons
     const bool in_lo = (inlet_mask >> (2 * d)) & 1, in_hi = (inlet_mask >> (2 * d + 1)) & 1;
     // the low-side face value of cell c (index ic along d) and the
     // high-side face value, for the cell gradients
+    // (a boundary face inside the block is a rigid-box wall: zero derivative)
     auto lo_face = [&](const double* qa, const double* qi, long long c, int ic, long long fc) {
-      if (has_lo_p<PER>(m, d, ic)) return avg(qa[nb_lo_p<PER>(m, d, ic, c, s)], qa[c]);
-      return in_lo ? qi[fc] : qa[c];
+      if (has_lo_p<PER>(m, d, ic, c, s)) return avg(qa[nb_lo_p<PER>(m, d, ic, c, s)], qa[c]);
+      return (in_lo && ic == 0) ? qi[fc] : qa[c];
     };
     auto hi_face = [&](const double* qa, const double* qi, long long c, int ic, long long fc) {
-      if (has_hi_p<PER>(m, d, ic)) return avg(qa[c], qa[nb_hi_p<PER>(m, d, ic, c, s)]);
-      return in_hi ? qi[fc] : qa[c];
+      if (has_hi_p<PER>(m, d, ic, c, s)) return avg(qa[c], qa[nb_hi_p<PER>(m, d, ic, c, s)]);
+      return (in_hi && ic == nd - 1) ? qi[fc] : qa[c];
     };
     // inner face between P (index ip) and E (index ie) with face index ff
     auto inner = [&](const double* qa, const double* qi, long long P, int ip, long long E, int ie,
@@ -87,7 +88,7 @@ __global__ void k_adv_faces(Mesh m, Geo g, int nph, int stage, int nstages, cons
         const int ip = id > 0 ? id - 1 : nd - 1;
         qf = inner(q.a[i], qin.a[i], NB_LO(d, s), ip, X.c, id, f, Ff);
       } else {
-        qf = in_lo ? qin.a[i][f] : q.a[i][X.c];
+        qf = (in_lo && id == 0) ? qin.a[i][f] : q.a[i][X.c];
       }
       qflux.a[i][f] = qf * Ff;
     }
@@ -96,7 +97,7 @@ __global__ void k_adv_faces(Mesh m, Geo g, int nph, int stage, int nstages, cons
       double Fh = F[fh];
       for (int i = 0; i < nph; ++i) {
         double qf;
-        if (PER && m.per[d]) qf = inner(q.a[i], qin.a[i], X.c, id, NB_HI(d, s), 0, fh, Fh);
+        if (PER && HAS_HI(d)) qf = inner(q.a[i], qin.a[i], X.c, id, NB_HI(d, s), 0, fh, Fh);
         else qf = in_hi ? qin.a[i][fh] : q.a[i][X.c];
         qflux.a[i][fh] = qf * Fh;
       }

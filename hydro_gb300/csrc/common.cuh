@@ -21,6 +21,11 @@ struct Mesh {
   double h[3], V, A[3];
   double lo[3];
   int per[3];         // periodic directions: cells n-1 and 0 are neighbours
+  // excluded cells (rigid box, mesh3d.hpp:183-215), device mask, null for
+  // none: a face touching an excluded cell is not inner; nfluid = cells
+  // not excluded
+  const unsigned char* ex;
+  long long nfluid;
 };
 
 __host__ __device__ inline long long cell_id(const Mesh& m, int i, int j, int k) {
@@ -38,20 +43,13 @@ __host__ __device__ inline long long face_stride(const Mesh& m, int d) {
   return d == 0 ? 1 : (d == 1 ? (long long)m.fnx[1] : (long long)m.fnx[2] * m.fny[2]);
 }
 
-// Neighbours along d of the cell c with index i along d.  A neighbour exists
-// inside the block, or across the end of a periodic direction (both end
-// faces then join cells n-1 and 0, mesh3d.hpp:348-392); s = cell_stride.
-// P is a compile-time switch: kernels are instantiated with P = false for
-// blocks without a periodic direction, where these reduce to the plain
-// bounds test and c -/+ s (no wrap arithmetic in the hot loops).
-template <bool P>
-__host__ __device__ inline bool has_lo_p(const Mesh& m, int d, int i) {
-  return i > 0 || (P && m.per[d]);
-}
-template <bool P>
-__host__ __device__ inline bool has_hi_p(const Mesh& m, int d, int i) {
-  return i < m.n[d] - 1 || (P && m.per[d]);
-}
+// Neighbours along d of the cell c with index i along d (s = cell_stride).
+// A neighbour exists inside the block, or across the end of a periodic
+// direction (both end faces then join cells n-1 and 0, mesh3d.hpp:348-392),
+// unless the cell or the neighbour is excluded.  P is a compile-time
+// switch: kernels are instantiated with P = false for plain blocks (no
+// periodic direction, no excluded cell), where these reduce to the bounds
+// test and c -/+ s (no wrap or mask arithmetic in the hot loops).
 // (I: the index type of the caller, int inside one CTA's shared memory)
 template <bool P, class I>
 __host__ __device__ inline I nb_lo_p(const Mesh& m, int d, int i, I c, I s) {
@@ -61,15 +59,39 @@ template <bool P, class I>
 __host__ __device__ inline I nb_hi_p(const Mesh& m, int d, int i, I c, I s) {
   return (!P || i < m.n[d] - 1) ? c + s : c - (I)(m.n[d] - 1) * s;
 }
-__host__ __device__ inline bool has_lo(const Mesh& m, int d, int i) { return has_lo_p<true>(m, d, i); }
-__host__ __device__ inline bool has_hi(const Mesh& m, int d, int i) { return has_hi_p<true>(m, d, i); }
+template <bool P, class I>
+__host__ __device__ inline bool has_lo_p(const Mesh& m, int d, int i, I c, I s) {
+  if (!P) return i > 0;
+  if (!(i > 0 || m.per[d])) return false;
+  return !m.ex || !(m.ex[c] || m.ex[nb_lo_p<P>(m, d, i, c, s)]);
+}
+template <bool P, class I>
+__host__ __device__ inline bool has_hi_p(const Mesh& m, int d, int i, I c, I s) {
+  if (!P) return i < m.n[d] - 1;
+  if (!(i < m.n[d] - 1 || m.per[d])) return false;
+  return !m.ex || !(m.ex[c] || m.ex[nb_hi_p<P>(m, d, i, c, s)]);
+}
+__host__ __device__ inline bool has_lo(const Mesh& m, int d, int i, long long c, long long s) {
+  return has_lo_p<true, long long>(m, d, i, c, s);
+}
+__host__ __device__ inline bool has_hi(const Mesh& m, int d, int i, long long c, long long s) {
+  return has_hi_p<true, long long>(m, d, i, c, s);
+}
 __host__ __device__ inline long long nb_lo(const Mesh& m, int d, int i, long long c, long long s) {
   return nb_lo_p<true, long long>(m, d, i, c, s);
 }
 __host__ __device__ inline long long nb_hi(const Mesh& m, int d, int i, long long c, long long s) {
   return nb_hi_p<true, long long>(m, d, i, c, s);
 }
+// is the cell excluded (general instantiations only)
+template <bool P, class I>
+__host__ __device__ inline bool excluded_p(const Mesh& m, I c) {
+  return P && m.ex && m.ex[c];
+}
+// Kernels take their general instantiation for periodic directions or
+// excluded cells.
 inline bool any_periodic(const Mesh& m) {
+  if (m.ex) return true;
   for (int d = 0; d < m.dim; ++d)
     if (m.per[d]) return true;
   return false;

@@ -155,6 +155,7 @@ struct hydro_ctx {
   BcSpec bc{};
   double* bcu = nullptr;
   float* bcu32 = nullptr;
+  unsigned char* exmask = nullptr;  // excluded cells (rigid box), device
   double* qin = nullptr;
   int inlet_mask = 0, has_outlet = 0;
   // mixed path: FP32 shadows of the state and mixture fields read by the
@@ -284,6 +285,7 @@ int init_mesh(Mesh& m, int dim, const int* n, const double* lo, const double* hi
     if (d < dim) off += (long long)m.fnx[d] * m.fny[d] * (m.n[2] + (d == 2));
   }
   m.nf = off;
+  m.nfluid = m.nc;
   m.V = 1.;
   for (int d = 0; d < dim; ++d) m.V *= m.h[d];
   for (int d = 0; d < 3; ++d) m.A[d] = d < dim ? m.V / m.h[d] : 0.;
@@ -735,6 +737,33 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
     }
   }
   if (desc->pressure_fixed_cell >= x->m.nc) { delete x; return HYDRO_ERR_ARG; }
+  // rigid box: cells whose centre lies in it (Rect::IsInside, inclusive)
+  std::vector<unsigned char> exmask;
+  if (desc->rigid_box) {
+    if (desc->simpler) { delete x; return HYDRO_ERR_UNSUPPORTED; }
+    exmask.assign((size_t)x->m.nc, 0);
+    long long nex = 0;
+    for (long long c = 0; c < x->m.nc; ++c) {
+      long long r = c;
+      int in = 1;
+      for (int d = 0; d < 3; ++d) {
+        long long i = r % x->m.n[d];
+        r /= x->m.n[d];
+        if (d >= desc->dim) continue;
+        double xc = x->m.lo[d] + (i + 0.5) * x->m.h[d];
+        if (xc < desc->rigid_box_lo[d] || desc->rigid_box_hi[d] < xc) in = 0;
+      }
+      exmask[(size_t)c] = (unsigned char)in;
+      nex += in;
+    }
+    if (nex == x->m.nc ||
+        (desc->pressure_fixed_cell >= 0 && exmask[(size_t)desc->pressure_fixed_cell])) {
+      delete x;
+      return HYDRO_ERR_ARG;
+    }
+    if (nex == 0) exmask.clear();
+    x->m.nfluid = x->m.nc - nex;
+  }
   const Mesh& m = x->m;
   x->dim = desc->dim;
   x->nph = desc->num_phases;
@@ -795,6 +824,7 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
     }
     x->gp = a.take<double>(nc * dim);
     x->bcu = a.take<double>(nf * dim);
+    x->exmask = exmask.empty() ? nullptr : a.take<unsigned char>(nc);
     if (desc->precision == HYDRO_MIXED) x->bcu32 = a.take<float>(nf * dim);
     x->qin = a.take<double>(nf * nph);
     x->Dc = a.take<double>(nc);
@@ -860,6 +890,17 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
       cudaStreamSynchronize(x->st) != cudaSuccess) {
     hydro_gpu_destroy(x);
     return HYDRO_ERR_CUDA;
+  }
+  if (x->exmask) {
+    // the mask of the context's mesh; multigrid levels keep none (their
+    // couplings carry the exclusion)
+    if (cudaMemcpyAsync(x->exmask, exmask.data(), exmask.size(), cudaMemcpyHostToDevice,
+                        x->st) != cudaSuccess ||
+        cudaStreamSynchronize(x->st) != cudaSuccess) {
+      hydro_gpu_destroy(x);
+      return HYDRO_ERR_CUDA;
+    }
+    x->m.ex = x->exmask;
   }
   x->pw.pin = desc->pressure_fixed_cell;
   x->pw.prof = &x->prof;
@@ -1782,6 +1823,10 @@ int hydro_gpu_heat_create(hydro_ctx* x, const hydro_heat_desc* hd) {
     }
     bc.side_in[2 * k] = inside(k, m.lo[k]);
     bc.side_in[2 * k + 1] = inside(k, m.lo[k] + m.n[k] * m.h[k]);
+  }
+  for (int k = 0; k < 3; ++k) {
+    bc.lo[k] = hd->box_lo[k];
+    bc.hi[k] = hd->box_hi[k];
   }
   bc.value = hd->box_temperature;
   h.bc = bc;

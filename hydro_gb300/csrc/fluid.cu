@@ -191,6 +191,16 @@ __global__ void k_mom_assemble(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> up,
                                WT<T, 3> res, T* Dc, int kch) {
   constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
+  if (EXCLUDED()) {
+    // identity row, zero constant (conv_diff.hpp:222-226); CoeffSum 1
+    coef.a[0][X.c] = T(1);
+#pragma unroll
+    for (int q = 0; q < 2 * DIM; ++q) coef.a[1 + q][X.c] = T(0);
+#pragma unroll
+    for (int n = 0; n < DIM; ++n) res.a[n][X.c] = T(0);
+    Dc[X.c] = T(1);
+    continue;
+  }
   const T rhoc = rho[X.c], muc = mu[X.c];
   T aPc = T(0);  // convective and diffusive part of the diagonal
   T aq[2 * DIM];
@@ -804,6 +814,8 @@ __global__ void k_init_flux(Mesh m, Geo g, FluidCoef fc, C3 u, C3 bv, double* F,
 template <int DIM>
 __global__ void k_bc_fill(Mesh m, BcSpec sp, W3 bv, FP<3> bv32, int kch) {
   CELL_LOOP_BEGIN(m, kch)
+  // boundary faces of an excluded cell carry no condition (velocity 0)
+  const bool exc = m.ex && m.ex[X.c];
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
@@ -813,7 +825,7 @@ __global__ void k_bc_fill(Mesh m, BcSpec sp, W3 bv, FP<3> bv32, int kch) {
       long long fb = side ? f + face_stride(m, d) : f;
       int q = 2 * d + side;
       for (int k = 0; k < DIM; ++k) {
-        double v = sp.kind[q] == HYDRO_BC_OUTLET ? 0. : sp.vel[q][k];
+        double v = (exc || sp.kind[q] == HYDRO_BC_OUTLET) ? 0. : sp.vel[q][k];
         bv.a[k][fb] = v;
         if (bv32.a[0]) bv32.a[k][fb] = (float)v;
       }
@@ -853,8 +865,10 @@ __global__ void __launch_bounds__(NT) k_outlet_sums(Mesh m, Geo g, BcSpec sp, C3
   double sm[4] = {0., 0., 0., 0.};
   CELL_LOOP_BEGIN(m, kch)
   if (Sv) sm[3] += Sv[X.c] * g.V;
+  const bool exc = m.ex && m.ex[X.c];  // excluded boundary faces: no condition
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
+    if (exc) continue;
     long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
@@ -888,8 +902,10 @@ __global__ void k_outlet_set(Mesh m, BcSpec sp, W3 bv, FP<3> bv32, const DevScal
                              int kch) {
   const double corr = (ds->red[RS_IN_FLUX] - ds->red[RS_OUT_FLUX]) / ds->red[RS_OUT_AREA];
   CELL_LOOP_BEGIN(m, kch)
+  const bool exc = m.ex && m.ex[X.c];
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
+    if (exc) continue;
     long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
 #pragma unroll
     for (int side = 0; side < 2; ++side) {

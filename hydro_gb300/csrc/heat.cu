@@ -13,9 +13,20 @@ namespace hg {
 namespace {
 
 // Does the boundary face on side (d, side) of the cell with indices i carry
-// the box temperature?
+// the box temperature?  A face of the block's own boundary by the side
+// table, a face beside an excluded cell by its centre.
 template <int DIM>
-__device__ __forceinline__ bool heat_value_face(const HeatBc& b, int d, int side, const int* i) {
+__device__ __forceinline__ bool heat_value_face(const Mesh& m, const HeatBc& b, int d, int side,
+                                                const int* i) {
+  const bool domain = !m.per[d] && (side ? i[d] == m.n[d] - 1 : i[d] == 0);
+  if (!domain) {
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      double x = k == d ? m.lo[k] + (i[k] + side) * m.h[k] : m.lo[k] + (i[k] + 0.5) * m.h[k];
+      if (x < b.lo[k] || b.hi[k] < x) return false;
+    }
+    return true;
+  }
   if (!b.side_in[2 * d + side]) return false;
 #pragma unroll
   for (int k = 0; k < DIM; ++k)
@@ -48,9 +59,9 @@ __global__ void k_heat_grad(Mesh m, Geo g, HeatBc bc, const double* T, W3 G, int
   for (int d = 0; d < DIM; ++d) {
     long long s = cell_stride(m, d);
     double flo = HAS_LO(d) ? avg(T[NB_LO(d, s)], tc)
-                           : (heat_value_face<DIM>(bc, d, 0, X.i) ? bc.value : tc);
+                           : (heat_value_face<DIM>(m, bc, d, 0, X.i) ? bc.value : tc);
     double fhi = HAS_HI(d) ? avg(tc, T[NB_HI(d, s)])
-                           : (heat_value_face<DIM>(bc, d, 1, X.i) ? bc.value : tc);
+                           : (heat_value_face<DIM>(m, bc, d, 1, X.i) ? bc.value : tc);
     G.a[d][X.c] = (fhi - flo) * g.inv_h[d];
   }
   CELL_LOOP_END
@@ -70,6 +81,13 @@ __global__ void k_heat_assemble(Mesh m, Geo g, HeatBc bc, HeatCoef hc, const dou
                                 const double* kc, C3 G, WP<7> coef, double* res, int kch) {
   constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
+  if (EXCLUDED()) {  // identity row, zero constant
+    coef.a[0][X.c] = 1.;
+#pragma unroll
+    for (int q = 0; q < 2 * DIM; ++q) coef.a[1 + q][X.c] = 0.;
+    res[X.c] = 0.;
+    continue;
+  }
   const double kcc = kc[X.c];
   double aPc = 0.;  // convective and diffusive part of the diagonal
   double aq[2 * DIM];
@@ -102,7 +120,7 @@ __global__ void k_heat_assemble(Mesh m, Geo g, HeatBc bc, HeatCoef hc, const dou
           long long cu = own_up ? X.c : nb;
           cst += G.a[d][cu] * ((up_m ? hh : -hh) * Fo);
         }
-      } else if (heat_value_face<DIM>(bc, d, side, X.i)) {
+      } else if (heat_value_face<DIM>(m, bc, d, side, X.i)) {
         double dif = 2. * kcc * g.inv_h2[d];
         aPc += dif;
         aq[2 * d + side] = 0.;

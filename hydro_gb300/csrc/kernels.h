@@ -190,10 +190,12 @@ cudaError_t launch_stat(const Mesh& m, const double* q, const double* alpha, C3 
 // Face centres on a side share that side's coordinate and the transverse
 // cell-centre coordinates, so the faces inside are: the sides whose plane
 // meets the box (side_in) and, on them, transverse cell indices i_k in
-// [a[k], b[k]).
+// [a[k], b[k]).  Faces beside excluded cells (rigid box) are tested by
+// their centre against [lo, hi].
 struct HeatBc {
   int side_in[6];
   int a[3], b[3];
+  double lo[3], hi[3];
   double value;
 };
 struct HeatCoef {

@@ -65,7 +65,7 @@ __global__ void k_diag(Mesh m, const double* kf, double shift, long long pin, T*
       if (X.i[d] == m.n[d] - 1) kf32[fl + face_stride(m, d)] = (T)kf[fl + face_stride(m, d)];
     }
   }
-  if (X.c == pin) s = 1.;
+  if (X.c == pin || EXCLUDED()) s = 1.;  // identity rows
   dg[X.c] = (T)s;
   idg[X.c] = (T)(1. / s);
   CELL_LOOP_END
@@ -73,23 +73,25 @@ __global__ void k_diag(Mesh m, const double* kf, double shift, long long pin, T*
 
 // sum of a vector (for the mean projection of singular systems).
 template <class T>
-__global__ void __launch_bounds__(NT) k_sum(long long n, const T* a, double* partials,
-                                            double* out, unsigned* ticket) {
+__global__ void __launch_bounds__(NT) k_sum(long long n, const T* a, const unsigned char* ex,
+                                            double* partials, double* out, unsigned* ticket) {
   double s = 0.;
   long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
   for (long long i = blockIdx.x * (long long)NT + tid; i < n; i += (long long)gridDim.x * NT)
-    s += (double)a[i];
+    if (!ex || !ex[i]) s += (double)a[i];
   double v[1] = {s};
   __shared__ double o[1];
   if (grid_reduce<RED_SUM, 1>(v, partials, ticket, o))
     if (tid == 0) *out = o[0];
 }
 
-__global__ void k_sub_mean(long long n, double* x, const double* sum) {
-  double mean = *sum / (double)n;
+// x -= mean over the cells that are not excluded (nfluid of them)
+__global__ void k_sub_mean(long long n, long long nfluid, const unsigned char* ex, double* x,
+                           const double* sum) {
+  double mean = *sum / (double)nfluid;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    x[i] -= mean;
+    if (!ex || !ex[i]) x[i] -= mean;
 }
 
 // r = f - mean(f) - A x (x == 0 unless use_guess), z = r/diag, p = z;
@@ -102,9 +104,9 @@ __global__ void __launch_bounds__(NT) k_cg_init(Mesh m, const T* kf, const T* dg
                                                 int dev_params, double* partials,
                                                 DevScalars* ds, int kch) {
   double s[3] = {0., 0., 0.};
-  double mean = fmean_sum ? *fmean_sum / (double)m.nc : 0.;
+  double mean = fmean_sum ? *fmean_sum / (double)m.nfluid : 0.;
   CELL_LOOP_BEGIN(m, kch)
-  double fc = f[X.c] - mean;
+  double fc = EXCLUDED() ? f[X.c] : f[X.c] - mean;
   double rc = fc;
   if (use_guess) rc -= (double)stencil_row<DIM, PER>(m, X, kf, dg, x, pin);
   T rt = (T)rc;
@@ -203,9 +205,9 @@ __global__ void __launch_bounds__(NT) k_ir_residual(Mesh m, const double* kf, co
                                                     const double* x, long long pin, double* r,
                                                     double* partials, DevScalars* ds, int kch) {
   double s = 0.;
-  double mean = fmean_sum ? *fmean_sum / (double)m.nc : 0.;
+  double mean = fmean_sum ? *fmean_sum / (double)m.nfluid : 0.;
   CELL_LOOP_BEGIN(m, kch)
-  double rc = (f[X.c] - mean) - stencil_row<DIM, PER>(m, X, kf, dg, x, pin);
+  double rc = (EXCLUDED() ? f[X.c] : f[X.c] - mean) - stencil_row<DIM, PER>(m, X, kf, dg, x, pin);
   r[X.c] = rc;
   s += rc * rc;
   CELL_LOOP_END
@@ -248,7 +250,7 @@ cudaError_t pcg_prepare(const Mesh& m, const double* kf, double shift, PcgWork& 
 }
 
 cudaError_t mean_sum(const Mesh& m, const double* f, PcgWork& w, cudaStream_t st) {
-  k_sum<double><<<flat_blocks_l(m.nc), dim3(BX, BY), 0, st>>>(m.nc, f, w.partials,
+  k_sum<double><<<flat_blocks_l(m.nc), dim3(BX, BY), 0, st>>>(m.nc, f, m.ex, w.partials,
                                                              &w.ds->red[RS_MEAN],
                                                              &w.ds->ticket[TK_MEAN]);
   count_launches(1);
@@ -256,10 +258,10 @@ cudaError_t mean_sum(const Mesh& m, const double* f, PcgWork& w, cudaStream_t st
 }
 
 cudaError_t sub_mean(const Mesh& m, double* x, PcgWork& w, cudaStream_t st) {
-  k_sum<double><<<flat_blocks_l(m.nc), dim3(BX, BY), 0, st>>>(m.nc, x, w.partials,
+  k_sum<double><<<flat_blocks_l(m.nc), dim3(BX, BY), 0, st>>>(m.nc, x, m.ex, w.partials,
                                                              &w.ds->red[RS_XMEAN],
                                                              &w.ds->ticket[TK_MEAN2]);
-  k_sub_mean<<<flat_blocks_l(m.nc), NT, 0, st>>>(m.nc, x, &w.ds->red[RS_XMEAN]);
+  k_sub_mean<<<flat_blocks_l(m.nc), NT, 0, st>>>(m.nc, m.nfluid, m.ex, x, &w.ds->red[RS_XMEAN]);
   count_launches(2);
   return cudaGetLastError();
 }
@@ -486,8 +488,9 @@ __global__ void k_pin_rhs(Mesh m, const double* kf, double* f, long long pin, do
   for (int d = 0; d < m.dim; ++d) {
     long long s = cell_stride(m, d);
     long long fl = face_id(m, d, i[0], i[1], i[2]);
-    if (has_lo(m, d, i[d])) f[nb_lo(m, d, i[d], pin, s)] += kf[fl] * value;
-    if (has_hi(m, d, i[d])) f[nb_hi(m, d, i[d], pin, s)] += kf[fl + face_stride(m, d)] * value;
+    if (has_lo(m, d, i[d], pin, s)) f[nb_lo(m, d, i[d], pin, s)] += kf[fl] * value;
+    if (has_hi(m, d, i[d], pin, s))
+      f[nb_hi(m, d, i[d], pin, s)] += kf[fl + face_stride(m, d)] * value;
   }
   f[pin] = value;
 }

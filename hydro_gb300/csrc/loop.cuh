@@ -51,14 +51,23 @@ __device__ __forceinline__ T grad_extrap(const T* p, long long c, int id, int nd
   if (id == 0) return (p[c + s] - p[c]) * inv_h;
   return (p[c] - p[c - s]) * inv_h;
 }
-// The same along direction d of mesh m, central across a periodic end.
+// The same along direction d of mesh m in the general form: central
+// across a periodic end; beside an excluded cell the face is a boundary
+// face; a cell between two boundary faces along d gets what the
+// reference's in-order extrapolation leaves there (the low face first,
+// reading 0 for the not yet extrapolated high face: p_lo = 2 p_c, then
+// p_hi = 2 p_c - p_lo = 0, gradient -2 p_c / h); an excluded cell 0.
 template <bool P, class T>
 __device__ __forceinline__ T grad_extrap_m(const Mesh& m, const T* p, long long c, int d,
                                            int id, long long s, T inv_h) {
-  if (P && m.per[d])
-    return (p[nb_hi_p<P>(m, d, id, c, s)] - p[nb_lo_p<P>(m, d, id, c, s)]) *
-           (T(0.5) * inv_h);
-  return grad_extrap(p, c, id, m.n[d], s, inv_h);
+  if (!P) return grad_extrap(p, c, id, m.n[d], s, inv_h);
+  if (m.ex && m.ex[c]) return T(0);
+  const bool lo = has_lo_p<P>(m, d, id, c, s), hi = has_hi_p<P>(m, d, id, c, s);
+  if (lo && hi)
+    return (p[nb_hi_p<P>(m, d, id, c, s)] - p[nb_lo_p<P>(m, d, id, c, s)]) * (T(0.5) * inv_h);
+  if (hi) return (p[nb_hi_p<P>(m, d, id, c, s)] - p[c]) * inv_h;
+  if (lo) return (p[c] - p[nb_lo_p<P>(m, d, id, c, s)]) * inv_h;
+  return T(-2) * p[c] * inv_h;
 }
 
 // Shorthands inside CELL_LOOP bodies: neighbours of the cell X along d.
@@ -66,8 +75,9 @@ __device__ __forceinline__ T grad_extrap_m(const Mesh& m, const T* p, long long 
 // instantiated per periodicity declares `constexpr bool kPerT = PER;`,
 // others see this default (wrap test always compiled in).
 constexpr bool kPerT = true;
-#define HAS_LO(d) (kPerT ? has_lo(m, (d), X.i[d]) : X.i[d] > 0)
-#define HAS_HI(d) (kPerT ? has_hi(m, (d), X.i[d]) : X.i[d] < m.n[d] - 1)
+#define HAS_LO(d) (kPerT ? has_lo(m, (d), X.i[d], X.c, cell_stride(m, (d))) : X.i[d] > 0)
+#define HAS_HI(d) (kPerT ? has_hi(m, (d), X.i[d], X.c, cell_stride(m, (d))) : X.i[d] < m.n[d] - 1)
+#define EXCLUDED() (kPerT && m.ex && m.ex[X.c])
 #define NB_LO(d, s) (kPerT ? nb_lo(m, (d), X.i[d], X.c, (s)) : X.c - (s))
 #define NB_HI(d, s) (kPerT ? nb_hi(m, (d), X.i[d], X.c, (s)) : X.c + (s))
 

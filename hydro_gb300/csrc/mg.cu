@@ -62,7 +62,7 @@ __global__ void k_mg_smooth(Mesh m, const float* kf, const float* idg, const flo
         long long fl = face_id(m, d, i, j, k);
 #pragma unroll
         for (int side = 0; side < 2; ++side) {
-          bool in = side ? has_hi_p<PER>(m, d, id[d]) : has_lo_p<PER>(m, d, id[d]);
+          bool in = side ? has_hi_p<PER>(m, d, id[d], c, s) : has_lo_p<PER>(m, d, id[d], c, s);
           long long nb = side ? nb_hi_p<PER>(m, d, id[d], c, s) : nb_lo_p<PER>(m, d, id[d], c, s);
           if (!in || nb == pin) continue;
           float xv = x[nb];
@@ -110,7 +110,7 @@ __global__ void k_mg_coarsen(Mesh fm, Mesh cm, const float* fkf, float* ckf, int
       }
       return sum;
     };
-    ckf[cf] = has_lo(cm, d, X.i[d]) ? 0.5f * fsum(X.i[d]) : 0.f;
+    ckf[cf] = has_lo(cm, d, X.i[d], X.c, cell_stride(cm, d)) ? 0.5f * fsum(X.i[d]) : 0.f;
     if (X.i[d] == cm.n[d] - 1)
       ckf[cf + face_stride(cm, d)] = cm.per[d] ? 0.5f * fsum(X.i[d] + 1) : 0.f;
   }
@@ -159,8 +159,8 @@ __global__ void k_mg_restrict(Mesh fm, Mesh cm, const float* kf, const float* dg
             long long fl = face_id(fm, d, id[0], id[1], id[2]);
             const long long cl = nb_lo_p<PER>(fm, d, id[d], c, s);
             const long long ch = nb_hi_p<PER>(fm, d, id[d], c, s);
-            if (has_lo_p<PER>(fm, d, id[d]) && cl != pin) ax = fmaf(-kf[fl], x[cl], ax);
-            if (has_hi_p<PER>(fm, d, id[d]) && ch != pin)
+            if (has_lo_p<PER>(fm, d, id[d], c, s) && cl != pin) ax = fmaf(-kf[fl], x[cl], ax);
+            if (has_hi_p<PER>(fm, d, id[d], c, s) && ch != pin)
               ax = fmaf(-kf[fl + face_stride(fm, d)], x[ch], ax);
           }
           r = b[c] - ax;
@@ -220,8 +220,8 @@ __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const
         int fl = (int)face_id(m, d, id[0], id[1], id[2]);
         const int cl = nb_lo_p<PER>(m, d, id[d], c, s);
         const int ch = nb_hi_p<PER>(m, d, id[d], c, s);
-        if (has_lo_p<PER>(m, d, id[d]) && cl != pin) acc = fmaf(kf[fl], x[cl], acc);
-        if (has_hi_p<PER>(m, d, id[d]) && ch != pin)
+        if (has_lo_p<PER>(m, d, id[d], c, s) && cl != pin) acc = fmaf(kf[fl], x[cl], acc);
+        if (has_hi_p<PER>(m, d, id[d], c, s) && ch != pin)
           acc = fmaf(kf[fl + (int)face_stride(m, d)], x[ch], acc);
       }
     }
@@ -260,8 +260,8 @@ __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, co
               dg += klo + khi;
               const int cl = nb_lo_p<PER>(fm, d, id[d], c, s);
               const int ch = nb_hi_p<PER>(fm, d, id[d], c, s);
-              if (has_lo_p<PER>(fm, d, id[d]) && cl != pin) off = fmaf(klo, x[cl], off);
-              if (has_hi_p<PER>(fm, d, id[d]) && ch != pin) off = fmaf(khi, x[ch], off);
+              if (has_lo_p<PER>(fm, d, id[d], c, s) && cl != pin) off = fmaf(klo, x[cl], off);
+              if (has_hi_p<PER>(fm, d, id[d], c, s) && ch != pin) off = fmaf(khi, x[ch], off);
             }
             r = b[c] - (dg * x[c] - off);
           }
@@ -459,6 +459,7 @@ Launch half_launch(const Mesh& m) {
 
 Mesh mg_coarse_mesh(const Mesh& f) {
   Mesh c = f;
+  c.ex = nullptr;  // a coarse level carries the exclusion in its couplings
   for (int d = 0; d < f.dim; ++d) {
     c.n[d] = f.n[d] / 2;
     c.h[d] = f.h[d] * 2.;

@@ -211,6 +211,14 @@ def golden_cases():
     d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
     out.append(("box_cavity3d", box(d, (0.3, 0.2, 0.3), (0.65, 0.6, 0.7)), u0, q0, 2, True))
 
+    # a box across the periodic end of x (harness built with PERX)
+    d, u0, q0, _ = cases.rising_drops(n=12, seed=5, dt_max=5e-3)
+    d.periodic[0] = 1
+    tight(d, p_tol=1e-12)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 2
+    out.append(("box_drops3d_periodic_x", box(d, (-1.0, 0.2, 0.3), (0.25, 0.45, 0.6)), u0, q0, 2,
+                True))
+
     # reference defaults for the linear solvers: one LU sweep for velocity
     # (an approximate solve; CPU-only semantics), SOR pressure
     d, u0, q0 = cases.broken_dam(nx=16, ny=8, dt_auto=False, dt=2e-3, smooth_times=2)
