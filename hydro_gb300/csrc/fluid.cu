@@ -428,7 +428,7 @@ __global__ void k_rhie_chow(Mesh m, Geo g64, GeoT<T> g, FluidCoef fc64, FluidCoe
     }
     if (id == nd - 1) {
       long long fh = f + face_stride(m, d);
-      if (PER && m.per[d]) {
+      if (PER && HAS_HI(d)) {  // across a periodic end, unless excluded
         inner(X.c, NB_HI(d, s), fh);
       } else {
         Fs[fh] = bv.a[d][fh] * A - mv;
@@ -500,7 +500,7 @@ __global__ void __launch_bounds__(NT) k_correct(Mesh m, Geo g, FluidCoef fc, C3 
       // high end face: a boundary face, or across a periodic end the face
       // between this cell (cm) and the first cell (cp)
       long long fh = f + face_stride(m, k);
-      double fvh = m.per[k] ? Fs[fh] + kf[fh] * (pc[X.c] - pc[NB_HI(k, s)]) : Fs[fh];
+      double fvh = HAS_HI(k) ? Fs[fh] + kf[fh] * (pc[X.c] - pc[NB_HI(k, s)]) : Fs[fh];
       Fic[fh] = fvh;
       if (F32) F32[fh] = (float)fvh;
     }
@@ -801,7 +801,7 @@ __global__ void k_init_flux(Mesh m, Geo g, FluidCoef fc, C3 u, C3 bv, double* F,
     else F[f] = bv.a[d][f] * g.A[d] - mv;
     if (X.i[d] == m.n[d] - 1)
       F[f + face_stride(m, d)] =
-          m.per[d] ? avg(u.a[d][X.c], u.a[d][NB_HI(d, s)]) * g.A[d] - mv
+          HAS_HI(d) ? avg(u.a[d][X.c], u.a[d][NB_HI(d, s)]) * g.A[d] - mv
                    : bv.a[d][f + face_stride(m, d)] * g.A[d] - mv;
   }
   CELL_LOOP_END
