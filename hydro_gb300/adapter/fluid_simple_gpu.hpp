@@ -178,6 +178,12 @@ class FluidSimpleGpu : public FluidSolver<Mesh> {
       }
       size_t dir = mesh.GetDirection(f);
       auto mi = mesh.GetBlockFaces().GetMIdx(f);
+      if (mi[dir] != 0 && mi[dir] != mesh.GetBlockCells().GetDimensions()[dir]) {
+        // a face inside the block: the rigid box's wall at rest
+        if (kind != HYDRO_BC_WALL || !(v == Vect(0)))
+          throw std::runtime_error("FluidSimpleGpu: inner faces must be walls at rest");
+        continue;
+      }
       int side = 2 * (int)dir + (mi[dir] == 0 ? 0 : 1);
       if (seen[side] && d.bc_kind[side] != kind)
         throw std::runtime_error("FluidSimpleGpu: one condition kind per side");
@@ -188,6 +194,36 @@ class FluidSimpleGpu : public FluidSolver<Mesh> {
       }
       d.bc_kind[side] = kind;
       seen[side] = true;
+    }
+    // excluded cells (mesh.ExcludeCells, the rigid box of hydro2d.hpp:306-423):
+    // the box is the bounding box of their centres, checked to select
+    // exactly them
+    {
+      bool any = false;
+      Vect lo(0), hi(0);
+      for (auto c : mesh.Cells()) {
+        if (!mesh.IsExcluded(c)) continue;
+        Vect x = mesh.GetCenter(c);
+        for (size_t k = 0; k < dim; ++k) {
+          lo[k] = any ? std::min(lo[k], x[k]) : x[k];
+          hi[k] = any ? std::max(hi[k], x[k]) : x[k];
+        }
+        any = true;
+      }
+      if (any) {
+        for (auto c : mesh.Cells()) {
+          Vect x = mesh.GetCenter(c);
+          bool in = true;
+          for (size_t k = 0; k < dim; ++k) in = in && lo[k] <= x[k] && x[k] <= hi[k];
+          if (in != mesh.IsExcluded(c))
+            throw std::runtime_error("FluidSimpleGpu: excluded cells must form a box");
+        }
+        d.rigid_box = 1;
+        for (size_t k = 0; k < dim; ++k) {
+          d.rigid_box_lo[k] = lo[k];
+          d.rigid_box_hi[k] = hi[k];
+        }
+      }
     }
     for (auto it = mc_cond.cbegin(); it != mc_cond.cend(); ++it) {
       auto* gp = dynamic_cast<GivenPressure<Mesh>*>(it->GetValue().get());
