@@ -345,6 +345,15 @@ def measure(args, form, rank, world, local, stream, e2e=True):
     return out
 
 
+# DRAM traffic (ncu dram__bytes_read.sum + dram__bytes_write.sum) per cell of
+# one launch of a group, measured on smaller cases of the same workload
+# (rising drops, cold cache as ncu replays it) and applied per cell:
+#   mg_vcycle: one V-cycle at 128^3 (28 kernel launches) read 479.5 MB,
+#              wrote ~0 (the iterate stays in L2) -> 228.6 B/cell
+#   cg_spmv:   k_cg_spmv<3, double> at 150^3: 134.9 + 16.0 MB -> 44.7 B/cell
+TRAFFIC_PER_CELL = {"mg_vcycle": 479.5e6 / 128 ** 3, "cg_spmv": 150.9e6 / 150 ** 3}
+
+
 def roofline(res):
     """Roofline figure of the dominant kernel group of one measured form."""
     peak, peak_kind = measured_peaks()
@@ -366,8 +375,10 @@ def roofline(res):
         eff = sum(s["velocity_sweeps"] for s in stats)
     bytes_launch = per_cell * N
     achieved = bytes_launch * eff / (tms / 1e3) / 1e9
+    tpc = TRAFFIC_PER_CELL.get(name)
     return {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
-            "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+            "unit": "GB/s", "frac": round(achieved / peak, 4),
+            "traffic": round(tpc * N) if tpc else None,
             "peak_source": peak_kind, "bytes_per_launch": bytes_launch, "launches": nl,
             "effective_launches": eff, "avg_launch_us": round(tms * 1e3 / max(eff, 1), 2)}
 
@@ -507,7 +518,8 @@ def main():
                     help="headline form: mixed precision + multigrid CG, or plain FP64")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 measurement reported beside the headline")
-    ap.add_argument("--n", type=int, default=192)
+    ap.add_argument("--n", "--grid", dest="n", type=int, default=192,
+                    help="cells per side (--grid under torchrun, whose parser claims --n)")
     ap.add_argument("--outer", type=int, default=5, help="SIMPLE iterations per step")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
