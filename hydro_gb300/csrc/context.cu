@@ -1201,13 +1201,15 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
     PK(x, HYDRO_PROF_CORRECT,
        launch_correct(m, x->fc, up, du, x->vf<RT<float, 3>>(x->du32[x->du_cur], dim), s3.Dc,
                       x->uw3(HYDRO_ITER_CURR), pip, x->p[HYDRO_ITER_CURR], x->pc, x->Dc, x->Fs,
-                      x->kf, x->F[HYDRO_ITER_CURR], x->vf<FP<3>>(s3.u[HYDRO_ITER_CURR], dim),
-                      nullptr, s3.F[HYDRO_ITER_CURR], x->pw.partials, x->pw.ds, x->st));
+                      x->kf, x->pw.kf32, x->F[HYDRO_ITER_CURR],
+                      x->vf<FP<3>>(s3.u[HYDRO_ITER_CURR], dim), nullptr, s3.F[HYDRO_ITER_CURR],
+                      x->pw.partials, x->pw.ds, x->st));
   else
     PK(x, HYDRO_PROF_CORRECT,
        launch_correct(m, x->fc, up, du, RT<float, 3>{}, nullptr, x->uw3(HYDRO_ITER_CURR), pip,
-                      x->p[HYDRO_ITER_CURR], x->pc, x->Dc, x->Fs, x->kf, x->F[HYDRO_ITER_CURR],
-                      FP<3>{}, nullptr, nullptr, x->pw.partials, x->pw.ds, x->st));
+                      x->p[HYDRO_ITER_CURR], x->pc, x->Dc, x->Fs, x->kf, nullptr,
+                      x->F[HYDRO_ITER_CURR], FP<3>{}, nullptr, nullptr, x->pw.partials, x->pw.ds,
+                      x->st));
   if (d.simpler) {
     // SIMPLER pressure (fluid.hpp:1059-1155): a second solve with the same
     // matrix, in delta form around the corrected pressure

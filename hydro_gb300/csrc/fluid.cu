@@ -461,56 +461,83 @@ __global__ void k_pressure_rhs(Mesh m, Geo g, const double* Fs, const double* Sv
 // fluid.hpp:1033-1057: p += alpha_p p'; u = u* - grad p'/D_c (p' faces
 // extrapolated); F = F* + kf (p'_cm - p'_cp).  Reduces the SIMPLE
 // convergence indicator max_c |u_c - u_prev,c| (CalcDiff,
-// solver.hpp:804-813) into ds->red[RS_INDICATOR].  Mixed precision: the
-// velocity correction du and D_c come in FP32 (du32, Dc32 non-null), the
-// update itself is FP64, and the FP32 shadows of the new iterate (u32,
-// p32, F32) are written beside it.
-template <int DIM, bool PER>
+// solver.hpp:804-813) into ds->red[RS_INDICATOR], the square root taken
+// once on the maximum.  MIX (mixed path): the velocity and flux increments
+// are formed in FP32 from the FP32 momentum correction, diagonal and
+// couplings and added to the FP64 state (the p' differences stay FP64);
+// the FP32 shadows of the new iterate (u32, p32, F32) are written beside it.
+template <int DIM, bool MIX, bool PER>
 __global__ void __launch_bounds__(NT) k_correct(Mesh m, Geo g, FluidCoef fc, C3 up, C3 du,
                                                 RT<float, 3> du32, const float* Dc32, W3 uic,
                                                 const double* pip, double* pic,
                                                 const double* pc, const double* Dc,
                                                 const double* Fs, const double* kf,
-                                                double* Fic, FP<3> u32, float* p32, float* F32,
-                                                double* partials, DevScalars* ds, int kch) {
+                                                const float* kf32, double* Fic, FP<3> u32,
+                                                float* p32, float* F32, double* partials,
+                                                DevScalars* ds, int kch) {
   constexpr bool kPerT = PER;
   double dmax = 0.;
   CELL_LOOP_BEGIN(m, kch)
   double pn = pip[X.c] + fc.relax_p * pc[X.c];
   pic[X.c] = pn;
   if (p32) p32[X.c] = (float)pn;
-  double idc = -1. / (Dc32 ? (double)Dc32[X.c] : Dc[X.c]);
   double d2 = 0.;
+  if (MIX) {
+    const float idc = -1.f / Dc32[X.c];
+    float e2 = 0.f;
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) {
-    long long s = cell_stride(m, k);
-    double gpc = grad_extrap_m<PER>(m, pc, X.c, k, X.i[k], s, g.inv_h[k]);
-    double u0 = up.a[k][X.c];
-    double duk = du32.a[0] ? (double)du32.a[k][X.c] : du.a[k][X.c];
-    double un = (u0 + duk) + gpc * idc;
-    uic.a[k][X.c] = un;
-    if (u32.a[0]) u32.a[k][X.c] = (float)un;
-    double dd = un - u0;
-    d2 += dd * dd;
-    long long f = face_id(m, k, X.i[0], X.i[1], X.i[2]);
-    double fv = HAS_LO(k) ? Fs[f] + kf[f] * (pc[NB_LO(k, s)] - pc[X.c]) : Fs[f];
-    Fic[f] = fv;
-    if (F32) F32[f] = (float)fv;
-    if (X.i[k] == m.n[k] - 1) {
-      // high end face: a boundary face, or across a periodic end the face
-      // between this cell (cm) and the first cell (cp)
-      long long fh = f + face_stride(m, k);
-      double fvh = HAS_HI(k) ? Fs[fh] + kf[fh] * (pc[X.c] - pc[NB_HI(k, s)]) : Fs[fh];
-      Fic[fh] = fvh;
-      if (F32) F32[fh] = (float)fvh;
+    for (int k = 0; k < DIM; ++k) {
+      long long s = cell_stride(m, k);
+      const float gpc = (float)grad_extrap_m<PER>(m, pc, X.c, k, X.i[k], s, g.inv_h[k]);
+      const float inc = fmaf(gpc, idc, du32.a[k][X.c]);
+      const double un = up.a[k][X.c] + (double)inc;
+      uic.a[k][X.c] = un;
+      u32.a[k][X.c] = (float)un;
+      e2 = fmaf(inc, inc, e2);
+      long long f = face_id(m, k, X.i[0], X.i[1], X.i[2]);
+      const double fv =
+          HAS_LO(k) ? Fs[f] + (double)(kf32[f] * (float)(pc[NB_LO(k, s)] - pc[X.c])) : Fs[f];
+      Fic[f] = fv;
+      F32[f] = (float)fv;
+      if (X.i[k] == m.n[k] - 1) {
+        long long fh = f + face_stride(m, k);
+        const double fvh =
+            HAS_HI(k) ? Fs[fh] + (double)(kf32[fh] * (float)(pc[X.c] - pc[NB_HI(k, s)]))
+                      : Fs[fh];
+        Fic[fh] = fvh;
+        F32[fh] = (float)fvh;
+      }
+    }
+    d2 = e2;
+  } else {
+    const double idc = -1. / Dc[X.c];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      long long s = cell_stride(m, k);
+      double gpc = grad_extrap_m<PER>(m, pc, X.c, k, X.i[k], s, g.inv_h[k]);
+      double u0 = up.a[k][X.c];
+      double un = (u0 + du.a[k][X.c]) + gpc * idc;
+      uic.a[k][X.c] = un;
+      double dd = un - u0;
+      d2 += dd * dd;
+      long long f = face_id(m, k, X.i[0], X.i[1], X.i[2]);
+      double fv = HAS_LO(k) ? Fs[f] + kf[f] * (pc[NB_LO(k, s)] - pc[X.c]) : Fs[f];
+      Fic[f] = fv;
+      if (X.i[k] == m.n[k] - 1) {
+        // high end face: a boundary face, or across a periodic end the face
+        // between this cell (cm) and the first cell (cp)
+        long long fh = f + face_stride(m, k);
+        double fvh = HAS_HI(k) ? Fs[fh] + kf[fh] * (pc[X.c] - pc[NB_HI(k, s)]) : Fs[fh];
+        Fic[fh] = fvh;
+      }
     }
   }
-  dmax = fmax(dmax, sqrt(d2));
+  dmax = fmax(dmax, d2);
   CELL_LOOP_END
   double v[1] = {dmax};
   __shared__ double out[1];
   if (grid_reduce<RED_MAX, 1>(v, partials, &ds->ticket[TK_IND], out)) {
-    if (threadIdx.x == 0 && threadIdx.y == 0) ds->red[RS_INDICATOR] = out[0];
+    if (threadIdx.x == 0 && threadIdx.y == 0) ds->red[RS_INDICATOR] = sqrt(out[0]);
   }
 }
 
@@ -1116,10 +1143,18 @@ cudaError_t launch_pressure_rhs(const Mesh& m, const double* Fs, const double* S
 cudaError_t launch_correct(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du,
                            RT<float, 3> du32, const float* Dc32, W3 u_ic, const double* p_ip,
                            double* p_ic, const double* pc, const double* Dc, const double* Fs,
-                           const double* kf, double* F_ic, FP<3> u32, float* p32, float* F32,
-                           double* partials, DevScalars* ds, cudaStream_t st) {
-  DISPATCH_DIM_P(m, k_correct, m, make_geo(m), fc, u_prev, du, du32, Dc32, u_ic, p_ip, p_ic, pc,
-               Dc, Fs, kf, F_ic, u32, p32, F32, partials, ds);
+                           const double* kf, const float* kf32, double* F_ic, FP<3> u32,
+                           float* p32, float* F32, double* partials, DevScalars* ds,
+                           cudaStream_t st) {
+  Launch L = cell_launch(m);
+  if (du32.a[0])
+    CELL_LAUNCH_TP(m, L, st, k_correct, true, m, make_geo(m), fc, u_prev, du, du32, Dc32, u_ic,
+                   p_ip, p_ic, pc, Dc, Fs, kf, kf32, F_ic, u32, p32, F32, partials, ds);
+  else
+    CELL_LAUNCH_TP(m, L, st, k_correct, false, m, make_geo(m), fc, u_prev, du, du32, Dc32, u_ic,
+                   p_ip, p_ic, pc, Dc, Fs, kf, kf32, F_ic, u32, p32, F32, partials, ds);
+  count_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_simpler_rhs(const Mesh& m, const FluidCoef& fc, CP<7> coef, C3 res, C3 uic,

@@ -151,8 +151,9 @@ cudaError_t launch_pressure_rhs(const Mesh& m, const double* Fs, const double* S
 cudaError_t launch_correct(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du,
                            RT<float, 3> du32, const float* Dc32, W3 u_ic, const double* p_ip,
                            double* p_ic, const double* pc, const double* Dc, const double* Fs,
-                           const double* kf, double* F_ic, FP<3> u32, float* p32, float* F32,
-                           double* partials, DevScalars* ds, cudaStream_t st);
+                           const double* kf, const float* kf32, double* F_ic, FP<3> u32,
+                           float* p32, float* F32, double* partials, DevScalars* ds,
+                           cudaStream_t st);
 cudaError_t launch_auto_dt(const Mesh& m, const double* F, double* partials, DevScalars* ds,
                            cudaStream_t st);
 // SIMPLER (FP64 path): right-hand side f of the delta-form pressure solve

@@ -48,26 +48,34 @@ __device__ __forceinline__ T stencil_row(const Mesh& m, const Cell& X, const T* 
   return acc;
 }
 
-// diag = sum of the inner-face couplings + shift (1 on the pinned row);
-// idg = 1/diag.
-template <int DIM, class T>
-__global__ void k_diag(Mesh m, const double* kf, double shift, long long pin, T* dg, T* idg,
-                       T* kf32, int kch) {
+// diag = sum of the inner-face couplings + shift (1 on the pinned row and
+// on excluded cells); idg = 1/diag in FP64, and with dg32 set the same in
+// FP32 plus the FP32 couplings (the mixed path's copy), from one read of kf.
+template <int DIM, bool PER>
+__global__ void k_diag(Mesh m, const double* kf, double shift, long long pin, double* dg,
+                       double* idg, float* dg32, float* idg32, float* kf32, int kch) {
+  constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
   double s = shift;
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
-    if (HAS_LO(d)) s += kf[fl];
+    const double klo = kf[fl];
+    if (HAS_LO(d)) s += klo;
     if (HAS_HI(d)) s += kf[fl + face_stride(m, d)];
     if (kf32) {
-      kf32[fl] = (T)kf[fl];
-      if (X.i[d] == m.n[d] - 1) kf32[fl + face_stride(m, d)] = (T)kf[fl + face_stride(m, d)];
+      kf32[fl] = (float)klo;
+      if (X.i[d] == m.n[d] - 1) kf32[fl + face_stride(m, d)] = (float)kf[fl + face_stride(m, d)];
     }
   }
   if (X.c == pin || EXCLUDED()) s = 1.;  // identity rows
-  dg[X.c] = (T)s;
-  idg[X.c] = (T)(1. / s);
+  const double is = 1. / s;
+  dg[X.c] = s;
+  idg[X.c] = is;
+  if (dg32) {
+    dg32[X.c] = (float)s;
+    idg32[X.c] = (float)is;
+  }
   CELL_LOOP_END
 }
 
@@ -234,18 +242,9 @@ int flat_blocks_l(long long n) {
 cudaError_t pcg_prepare(const Mesh& m, const double* kf, double shift, PcgWork& w, int fp32,
                         cudaStream_t st) {
   Launch L = cell_launch(m);
-  if (m.dim == 3) {
-    k_diag<3, double><<<L.grid, L.block, 0, st>>>(m, kf, shift, w.pin, w.dg, w.idg, nullptr, L.kch);
-    if (fp32)
-      k_diag<3, float><<<L.grid, L.block, 0, st>>>(m, kf, shift, w.pin, w.dg32, w.idg32, w.kf32,
-                                                   L.kch);
-  } else {
-    k_diag<2, double><<<L.grid, L.block, 0, st>>>(m, kf, shift, w.pin, w.dg, w.idg, nullptr, L.kch);
-    if (fp32)
-      k_diag<2, float><<<L.grid, L.block, 0, st>>>(m, kf, shift, w.pin, w.dg32, w.idg32, w.kf32,
-                                                   L.kch);
-  }
-  count_launches(fp32 ? 2 : 1);
+  CELL_LAUNCH_P(m, L, st, k_diag, m, kf, shift, w.pin, w.dg, w.idg, fp32 ? w.dg32 : nullptr,
+                fp32 ? w.idg32 : nullptr, fp32 ? w.kf32 : nullptr);
+  count_launches(1);
   return cudaGetLastError();
 }
 
