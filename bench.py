@@ -9,15 +9,17 @@ Synthetic seeded inputs of that shape (no external data).
 
 Metric: Mcell-updates/s = cells x time steps / wall seconds, whole job.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--form mixed_mg|fp64]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--form mixed_mg|fp64|fp64_mg]
                   [--no-plain] [--no-cpu-baseline]
   python bench.py --impl reference ...   # the reference algorithm on the CPU
 
-The headline form is "mixed_mg": FP64 iterative refinement around an FP32
-conjugate-gradient pressure solve preconditioned by geometric multigrid, with
-FP32 momentum sweeps (FP64 assembly, residuals and corrections).  The plain
-FP64 form (Jacobi-preconditioned CG, FP64 sweeps) is timed beside it in the
-same run as "plain_fp64" unless --no-plain is given.
+The headline form is "mixed_mg": FP32 assembly and momentum sweeps (FP64
+kept where the arithmetic cancels) and FP64 iterative refinement around an
+FP32 conjugate-gradient pressure solve preconditioned by geometric multigrid.
+Timed beside it in the same run unless --no-plain is given: the plain FP64
+form ("plain_fp64": every kernel FP64, Jacobi-preconditioned CG) and the FP64
+form with the multigrid-preconditioned refinement ("fp64_multigrid": FP64
+kernels and system, FP32 inner corrections).
 
 Multi-GPU: replicas only (the reference's MPI mode runs redundant replicas;
 the path has no exchange step here) -- each rank advances its own seeded
@@ -261,15 +263,17 @@ def cpu_sample(n, seed, outer, sweeps=(4, 12), threads=None):
 # ---------------------------------------------------------------- our arm --
 def measure(args, form, rank, world, local, stream, e2e=True):
     """Times args.steps steps of one form ("mixed_mg": mixed precision with
-    the multigrid CG, "fp64": plain FP64 with Jacobi CG) after args.warmup
-    untimed steps; returns a dict of results."""
+    the multigrid CG, "fp64": plain FP64 with Jacobi CG, "fp64_mg": FP64
+    with the multigrid-preconditioned refinement) after args.warmup untimed
+    steps; returns a dict of results."""
     import numpy as np
     import torch
 
     from hydro_gb300 import capi
     from hydro_gb300 import solver as S
 
-    precision, solver = ("mixed", "mgcg") if form == "mixed_mg" else ("fp64", "cg")
+    precision, solver = {"mixed_mg": ("mixed", "mgcg"), "fp64": ("fp64", "cg"),
+                         "fp64_mg": ("fp64", "mgcg")}[form]
     d, u0, q0, drops = workload(args.n, args.seed + rank, precision, args.outer, solver)
     h = S.make(d, u0, q0, stream=stream.cuda_stream)
     N = d.ncells
@@ -398,8 +402,11 @@ def run_ours(args, rank, world, local):
     stream = torch.cuda.Stream()
     head = measure(args, args.form, rank, world, local, stream)
     plain = None
+    fp64mg = None
     if args.form != "fp64" and not args.no_plain:
         plain = measure(args, "fp64", rank, world, local, stream, e2e=False)
+        if args.form != "fp64_mg":
+            fp64mg = measure(args, "fp64_mg", rank, world, local, stream, e2e=False)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -468,6 +475,16 @@ def run_ours(args, rank, world, local):
             "clocks": plain["clocks"],
             "profile_ms": {k: round(v[1], 3) for k, v in sorted(plain["prof"].items())},
         }
+    if fp64mg:
+        out["fp64_multigrid"] = {
+            "value": round(fp64mg["value"], 4),
+            "ms_per_step": round(fp64mg["ms"] / args.steps, 3),
+            "pressure_iterations": [s["pressure_iterations"] for s in fp64mg["stats"]],
+            "note": "FP64 kernels and FP64 system; pressure by FP64 iterative refinement "
+                    "around the FP32 multigrid-preconditioned CG",
+            "clocks": fp64mg["clocks"],
+            "profile_ms": {k: round(v[1], 3) for k, v in sorted(fp64mg["prof"].items())},
+        }
     print(json.dumps(out))
 
 
@@ -514,7 +531,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="mixed_mg", choices=["mixed_mg", "fp64"],
+    ap.add_argument("--form", default="mixed_mg", choices=["mixed_mg", "fp64", "fp64_mg"],
                     help="headline form: mixed precision + multigrid CG, or plain FP64")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 measurement reported beside the headline")

@@ -562,7 +562,10 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
   w.pin = d.pressure_fixed_cell;
   if (w.pin >= 0 && apply_pin)
     CK(pin_rhs(m, x->kf, x->prhs, w.pin, d.pressure_fixed_value, x->st));
-  int mixed = (d.precision == HYDRO_MIXED);
+  // FP64 iterative refinement around an FP32 inner solve: the mixed path,
+  // and the FP64 path with the multigrid preconditioner (the FP64 system is
+  // still solved to the FP64 tolerance; only the inner corrections are FP32)
+  int mixed = (d.precision == HYDRO_MIXED) || d.pressure_solver == HYDRO_LINEAR_MGCG;
   CK(pcg_prepare(m, x->kf, 0., w, mixed, x->st));
   if (x->graph_mode) return solve_pressure_graph(x, singular, mixed);
   int rc;
@@ -719,8 +722,6 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
       return HYDRO_ERR_ARG;
   if (desc->velocity_omega <= 0. || desc->velocity_relaxation_factor <= 0.)
     return HYDRO_ERR_ARG;
-  if (desc->pressure_solver == HYDRO_LINEAR_MGCG && desc->precision != HYDRO_MIXED)
-    return HYDRO_ERR_UNSUPPORTED;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return HYDRO_ERR_NO_DEVICE;
   hydro_ctx* x = new (std::nothrow) hydro_ctx();

@@ -85,11 +85,16 @@ enum hydro_linear {
   HYDRO_LINEAR_CG = 2,           /* new: no Krylov solver in the reference */
   HYDRO_LINEAR_LU = 3,           /* linear.hpp:527-567 (one symmetric sweep) */
   HYDRO_LINEAR_MGCG = 4          /* new: CG preconditioned by a geometric multigrid
-                                    V-cycle (GPU: mixed precision only) */
+                                    V-cycle, in FP32, inside an FP64 iterative
+                                    refinement (both precisions: the FP64 system
+                                    is solved to the FP64 tolerance) */
 };
 
-/* Arithmetic of the pressure solve.  MIXED runs the PCG in FP32 inside an
- * FP64 iterative-refinement loop whose residual, dots and norms stay FP64. */
+/* Arithmetic of the SIMPLE iteration.  FP64: every kernel in FP64.  MIXED:
+ * the assembly, the momentum sweeps and the pressure Krylov solve in FP32,
+ * FP64 kept where the arithmetic cancels (BDF difference, pressure
+ * gradients, face velocity, state updates) and for the refinement residual,
+ * dots and norms of the pressure solve. */
 enum hydro_precision { HYDRO_FP64 = 0, HYDRO_MIXED = 1 };
 
 /* Field ids for get/set.  Vector fields have dim components (component-major). */
