@@ -866,6 +866,7 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
       lv.x = a.take<float>(lv.m.nc);
       lv.b = a.take<float>(lv.m.nc);
     }
+    mg.cinv = mg.nlev >= 2 ? a.take<float>(kMgCoarseTarget * kMgCoarseTarget) : nullptr;
     w.ds = a.take<DevScalars>(1);
     x->stat_out = a.take<double>(16);
     x->stat_ticket = a.take<unsigned>(4);

@@ -310,6 +310,11 @@ struct MgWork {
   int coarse_sweeps;       // sweeps of the coarsest solve inside the CTA
   int coarse_sweeps_large; // sweeps when the coarsest level stays large
   MgLevel lev[kMgMaxLevels];
+  // inverse of the coarsest level's operator (rank-one completed for its
+  // constant null space), dense, when that level has <= kMgCoarseTarget
+  // cells and is not the top level; null otherwise
+  float* cinv;
+  bool cdense;
 };
 Mesh mg_coarse_mesh(const Mesh& fine);
 int mg_levels_for(const Mesh& m);

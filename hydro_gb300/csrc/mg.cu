@@ -83,6 +83,78 @@ __global__ void k_mg_smooth(Mesh m, const float* kf, const float* idg, const flo
   }
 }
 
+// Dense inverse of the operator of a small coarsest level (n <= 64 cells),
+// one CTA, FP64 in shared memory: A = couplings (diagonal = their sum), cells
+// without couplings (inside a rigid box) decoupled as identity rows, the
+// constant mode of the others completed by 1/m (A + e e^T / m is SPD, and
+// for a zero-mean right-hand side its solution is the zero-mean solution
+// of A x = b); in-place Gauss-Jordan, symmetrised, stored in FP32.
+constexpr int kMgDense = (int)kMgCoarseTarget;
+template <int DIM>
+__global__ void __launch_bounds__(256) k_mg_coarse_inv(Mesh m, const float* kf, float* P) {
+  __shared__ double A[kMgDense][kMgDense];
+  __shared__ int iso[kMgDense];
+  __shared__ int niso;
+  const int n = (int)m.nc, tid = threadIdx.x, nt = blockDim.x;
+  for (int q = tid; q < kMgDense * kMgDense; q += nt) A[q / kMgDense][q % kMgDense] = 0.;
+  if (tid == 0) niso = 0;
+  __syncthreads();
+  for (int c = tid; c < n; c += nt) {
+    int id[3];
+    id[0] = c % m.n[0];
+    id[1] = (c / m.n[0]) % m.n[1];
+    id[2] = DIM == 3 ? c / (m.n[0] * m.n[1]) : 0;
+    double dg = 0.;
+    for (int d = 0; d < DIM; ++d) {
+      const long long s = cell_stride(m, d);
+      const long long fl = face_id(m, d, id[0], id[1], id[2]);
+      if (has_lo(m, d, id[d], c, s)) {
+        const double k = kf[fl];
+        dg += k;
+        A[c][nb_lo(m, d, id[d], c, s)] -= k;
+      }
+      if (has_hi(m, d, id[d], c, s)) {
+        const double k = kf[fl + face_stride(m, d)];
+        dg += k;
+        A[c][nb_hi(m, d, id[d], c, s)] -= k;
+      }
+    }
+    A[c][c] += dg;
+    iso[c] = dg > 0. ? 0 : 1;
+    if (iso[c]) atomicAdd(&niso, 1);
+  }
+  __syncthreads();
+  const double rm = 1. / (double)(n - niso > 0 ? n - niso : 1);
+  for (int q = tid; q < n * n; q += nt) {
+    const int i = q / n, j = q % n;
+    if (iso[i] || iso[j]) A[i][j] = (i == j) ? 1. : 0.;
+    else A[i][j] += rm;
+  }
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    const double piv = A[k][k];
+    const double ip = fabs(piv) > 1e-300 ? 1. / piv : 0.;
+    __syncthreads();
+    for (int j = tid; j < n; j += nt) A[k][j] = (j == k) ? ip : A[k][j] * ip;
+    __syncthreads();
+    for (int q = tid; q < n * n; q += nt) {
+      const int i = q / n, j = q % n;
+      if (i == k) continue;
+      const double f = A[i][k];
+      if (j == k) continue;
+      A[i][j] -= f * A[k][j];
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += nt)
+      if (i != k) A[i][k] = -A[i][k] * A[k][k];
+    __syncthreads();
+  }
+  for (int q = tid; q < n * n; q += nt) {
+    const int i = q / n, j = q % n;
+    P[q] = (float)(0.5 * (A[i][j] + A[j][i]));
+  }
+}
+
 // Coarse couplings: 1/2 of the sum of the fine couplings of each coarse face
 // (zero on boundary faces; across a periodic end the coarse face joins the
 // last and first coarse cells like the fine one).
@@ -185,6 +257,7 @@ constexpr int kBlkThreads = 1024;
 struct MgBlock {
   int nl;  // levels in the CTA, top first
   int nsweep, coarse_sweeps;
+  const float* cinv;  // dense inverse of the coarsest level, or null (sweeps)
   long long pin;  // pinned cell of the top level (-1: none)
   Mesh m[kMgMaxLevels];
   const float* kf[kMgMaxLevels];
@@ -323,14 +396,25 @@ __global__ void __launch_bounds__(kBlkThreads)
       for (int c = tid; c < n; c += nt) b[c] -= mean;
       __syncthreads();
     }
-    const int half = B.coarse_sweeps / 2 > 0 ? B.coarse_sweeps / 2 : 1;
-    for (int s = 0; s < half; ++s) {
-      blk_half<DIM, PER>(m, kf, idg, b, x, 0, s == 0, lp);
-      blk_half<DIM, PER>(m, kf, idg, b, x, 1, false, lp);
-    }
-    for (int s = 0; s < half; ++s) {
-      blk_half<DIM, PER>(m, kf, idg, b, x, 1, false, lp);
-      blk_half<DIM, PER>(m, kf, idg, b, x, 0, false, lp);
+    if (B.cinv && lp < 0) {
+      // exact coarsest solve: x = P b, P the symmetric inverse of the level's
+      // operator completed by the constant mode (b has zero mean)
+      for (int c = tid; c < n; c += nt) {
+        float acc = 0.f;
+        for (int q = 0; q < n; ++q) acc = fmaf(B.cinv[c * n + q], b[q], acc);
+        x[c] = acc;
+      }
+      __syncthreads();
+    } else {
+      const int half = B.coarse_sweeps / 2 > 0 ? B.coarse_sweeps / 2 : 1;
+      for (int s = 0; s < half; ++s) {
+        blk_half<DIM, PER>(m, kf, idg, b, x, 0, s == 0, lp);
+        blk_half<DIM, PER>(m, kf, idg, b, x, 1, false, lp);
+      }
+      for (int s = 0; s < half; ++s) {
+        blk_half<DIM, PER>(m, kf, idg, b, x, 1, false, lp);
+        blk_half<DIM, PER>(m, kf, idg, b, x, 0, false, lp);
+      }
     }
   }
   for (int l = B.nl - 2; l >= 0; --l) {
@@ -545,11 +629,21 @@ cudaError_t mg_setup(MgWork& mg, PcgWork& w, cudaStream_t st) {
     MG_LAUNCH(k_mg_coarsen, L, f.m, c.m, f.kf, c.kf);
     MG_LAUNCH(k_mg_diag, L, c.m, c.kf, c.dg, c.idg);
   }
+  if (mg.cdense) {
+    const MgLevel& cl = mg.lev[mg.nlev - 1];
+    if (dim == 3) k_mg_coarse_inv<3><<<1, 256, 0, st>>>(cl.m, cl.kf, mg.cinv);
+    else k_mg_coarse_inv<2><<<1, 256, 0, st>>>(cl.m, cl.kf, mg.cinv);
+    count_launches(1);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t mg_prepare(MgWork& mg) {
   mg_plan_block(mg);
+  // the coarsest level is solved exactly when it is small and below the top
+  // level of the in-CTA cycle (a coarse level: singular, unpinned)
+  mg.cdense = mg.cinv && mg.nlev >= 2 && mg.top < mg.nlev && mg.top < mg.nlev - 1 &&
+              mg.lev[mg.nlev - 1].m.nc <= kMgCoarseTarget;
   if (mg.nlev > 0 && mg.top < mg.nlev) {
     if (mg.smem_bytes > 227 * 1024) return cudaErrorInvalidValue;
     const bool per = any_periodic(mg.lev[0].m);
@@ -591,6 +685,7 @@ cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevSc
     B.nl = mg.nlev - mg.top;
     B.nsweep = ns;
     B.coarse_sweeps = mg.coarse_sweeps;
+    B.cinv = mg.cdense ? mg.cinv : nullptr;
     B.pin = mg.top == 0 ? pin : -1;
     int off = 0;
     for (int q = 0; q < B.nl; ++q) {

@@ -1,0 +1,125 @@
+"""The five configurations of the workload at their full sizes, through
+properties that do not depend on size: the plain FP64 path against the
+oracle where the oracle finishes in seconds (the 64^2 cavity over its 200
+steps, the 512x256 breaking dam over two steps), the mixed forms against
+the FP64 path at 8.4 M and 7.1 M cells, conservation of every phase over
+many steps, and the 512-case batch against its cases stepped alone."""
+import numpy as np
+import pytest
+
+from hydro_gb300 import capi, cases
+from tests.util import compare, rel, run, tight
+
+pytestmark = pytest.mark.gpu
+
+
+def _pinned(d, iters):
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, iters
+    return d
+
+
+def test_c1_cavity_64_over_200_steps_vs_oracle(built):
+    """Lid-driven cavity, 64^2, Re 100, dt 1e-3, 200 steps (outer iterations
+    pinned at 2 per step for the comparison)."""
+    from hydro_gb300.solver import Hydro
+    from oracle.oracle import Oracle
+    d, u0, q0 = cases.cavity(n=64, mu=0.01, dt=1e-3)
+    _pinned(tight(d), 2)
+    a = run(Hydro(d), u0, q0, 200)
+    do = d.copy()
+    do.pressure_solver = capi.LINEAR_CG
+    b = run(Oracle(do, threads=8), u0, q0, 200)
+    errs = compare(a, b)
+    assert all(v <= 1e-10 for v in errs.values()), errs
+    assert np.abs(a["u"]).max() > 0.5  # the lid drove the flow
+
+
+def test_c2_dam_512x256_vs_oracle_and_conservation(built):
+    """Breaking dam at 512x256: two steps against the oracle, then 15 steps
+    conserving the partial mass of both phases.  (With the example scripts'
+    smoothing; at this resolution and the default loose velocity tolerance
+    the SIMPLE loop stops converging after ~20 steps and the run diverges
+    near step 27 identically in FP64 and mixed precision, as the reference
+    algorithm does in the oracle.)"""
+    from hydro_gb300.solver import Hydro
+    from oracle.oracle import Oracle
+    d, u0, q0 = cases.broken_dam(nx=512, ny=256, dt_auto=True, dt_max=1e-3, smooth_times=2)
+    _pinned(tight(d, 1.0), 2)
+    d.pressure_tolerance = 1e-12
+    a = run(Hydro(d), u0, q0, 2)
+    do = d.copy()
+    do.pressure_solver = capi.LINEAR_CG
+    b = run(Oracle(do, threads=8), u0, q0, 2)
+    errs = compare(a, b)
+    assert all(v <= 1e-9 for v in errs.values()), errs
+    d2, u0, q0 = cases.broken_dam(nx=512, ny=256, dt_auto=True, dt_max=1e-3, smooth_times=2)
+    d2.precision = capi.MIXED
+    d2.pressure_solver = capi.LINEAR_MGCG
+    h = Hydro(d2)
+    run(h, u0, q0, 0)
+    m0 = h.calc_stat()
+    stats = [h.step() for _ in range(15)]
+    m1 = h.calc_stat()
+    assert all(s["status"] == 0 for s in stats)
+    for i in range(2):
+        assert abs(m1.partial_mass[i] - m0.partial_mass[i]) <= 1e-11 * abs(m0.partial_mass[i])
+    q = h.get_field(capi.F_PARTIAL_DENSITY)
+    assert np.all(np.isfinite(q))
+
+
+@pytest.mark.parametrize("config", ["c3_rt_128x128x512", "c4_drops_192"])
+def test_mixed_forms_vs_fp64_full_size(built, config):
+    """Mixed precision with the multigrid CG against the FP64 path (FP64
+    kernels, multigrid-preconditioned refinement) at full size: 2 steps of
+    3 outer iterations, fields within the mixed tolerance."""
+    from hydro_gb300.solver import Hydro
+    if config.startswith("c3"):
+        d, u0, q0 = cases.rayleigh_taylor(seed=0)[:3]
+    else:
+        d, u0, q0, _ = cases.rising_drops(n=192, seed=0, dt_max=2e-3)
+    _pinned(d, 3)
+    d.velocity_tolerance, d.velocity_iters_limit = 1e-10, 400
+    d.pressure_tolerance, d.pressure_iters_limit = 1e-10, 20000
+    d.precision = capi.FP64
+    d.pressure_solver = capi.LINEAR_MGCG
+    a = run(Hydro(d), u0, q0, 2)
+    dm = d.copy()
+    dm.precision = capi.MIXED
+    b = run(Hydro(dm), u0, q0, 2)
+    errs = compare(b, a)
+    assert errs["u"] <= 1e-6 and errs["F"] <= 1e-6 and errs["q"] <= 1e-6, errs
+    assert errs["p"] <= 5e-6, errs
+    for s in a["stats"] + b["stats"]:
+        assert s["status"] == 0 and s["pressure_residual"] <= 1e-10
+
+
+def test_c5_batch_512_cavities(built):
+    """512 cavities of 64^2..256^2 (13.4 M cells) in one batch, mixed with the
+    multigrid CG, SIMPLE converged per case: two batch steps, and four cases
+    of every size stepped alone give the same fields."""
+    from hydro_gb300.solver import Batch, Hydro
+    specs = cases.cavity_batch(ncases=512, seed=0)
+    descs = []
+    for d, u0, q0, _ in specs:
+        d = d.copy()
+        d.precision = capi.MIXED
+        d.pressure_solver = capi.LINEAR_MGCG
+        descs.append(d)
+    b = Batch(descs)
+    for c, (d, u0, q0, _) in zip(b.cases, specs):
+        c.set_field(capi.F_VELOCITY, u0)
+        c.set_field(capi.F_PARTIAL_DENSITY, q0)
+    b.init_state()
+    st = [b.step() for _ in range(2)]
+    assert all(s["status"] == 0 for step in st for s in step)
+    picked = {}
+    for i, d in enumerate(descs):
+        picked.setdefault(d.n[0], [])
+        if len(picked[d.n[0]]) < 4:
+            picked[d.n[0]].append(i)
+    for n, idx in picked.items():
+        for i in idx:
+            d, u0, q0, _ = specs[i]
+            alone = run(Hydro(descs[i]), u0, q0, 2)
+            u = b.cases[i].get_field(capi.F_VELOCITY)
+            assert rel(u, alone["u"]) <= 1e-12, (n, i)
