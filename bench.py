@@ -147,6 +147,7 @@ def workload(n, seed, precision, outer, solver="cg"):
     d, u0, q0, drops = cases.rising_drops(n=n, seed=seed, dt_max=2e-3)
     d.convergence_tolerance = 0.0
     d.num_iterations_limit = outer
+    d.velocity_solver = capi.LINEAR_GAUSS_SEIDEL  # red-black on the GPU
     d.velocity_tolerance = 1e-8
     d.velocity_iters_limit = 200
     d.pressure_tolerance = 1e-8

@@ -169,6 +169,10 @@ struct hydro_ctx {
     float *G = nullptr, *fo = nullptr, *fres = nullptr, *Dc = nullptr;
   } s32;
   bool mixed = false;
+  // momentum solver: red-black Gauss-Seidel (velocity_solver GAUSS_SEIDEL;
+  // the FP32 path then stores its rows color-blocked, which needs an even
+  // Nx) or Jacobi
+  bool mom_gs = false;
   // graph-captured step (hydro_gpu_step_graph): capture state and the
   // instantiated step with the values it was captured for
   bool graph_mode = false;
@@ -400,6 +404,46 @@ int solve_momentum(hydro_ctx* x) {
     for (int k = 0; k < dim; ++k) r.a[k] = base + (size_t)k * x->m.nc;
     return r;
   };
+  if (x->mom_gs) {
+    // red-black Gauss-Seidel, in place on du[0] / du32[0]
+    auto gs_sweep = [&]() -> int {
+      for (int color = 0; color < 2; ++color) {
+        if (f32)
+          PK(x, HYDRO_PROF_MOM_SWEEP,
+             launch_mom_rbgs32(x->m, d.velocity_omega, d.velocity_tolerance, x->o32p(),
+                               fp3(x->du32[0]), color, limit, x->pw.partials, x->pw.ds, x->st));
+        else
+          PK(x, HYDRO_PROF_MOM_SWEEP,
+             launch_mom_rbgs(x->m, d.velocity_omega, d.velocity_tolerance, cc, resc,
+                             x->vec<W3>(x->du[0], dim, x->m.nc), color, limit, x->pw.partials,
+                             x->pw.ds, x->st));
+      }
+      return HYDRO_OK;
+    };
+    x->du_cur = 0;
+    if (x->graph_mode) {
+      cudaGraphConditionalHandle h;
+      if ((rc = new_handle(x, 1, &h))) return rc;
+      return add_loop(x, h, [&]() -> int {
+        int r;
+        if ((r = gs_sweep()) || (r = gs_sweep())) return r;
+        CK(launch_ctl_sweeps(x->pw.ds, limit, h, 1, x->st));
+        return HYDRO_OK;
+      });
+    }
+    int queued = 0;
+    for (;;) {
+      int n = std::min(kSweepChunk, limit - queued);
+      for (int s = 0; s < n; ++s)
+        if ((rc = gs_sweep())) return rc;
+      queued += n;
+      rc = sync_scalars(x);
+      if (rc) return rc;
+      if (x->hds->flag[FL_MOM_DONE] || queued >= limit) break;
+    }
+    x->vel_sweeps += x->hds->flag[FL_MOM_SWEEPS];
+    return HYDRO_OK;
+  }
   auto sweep = [&](int k) -> int {
     if (f32) {
       PK(x, HYDRO_PROF_MOM_SWEEP,
@@ -769,6 +813,8 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
   x->dim = desc->dim;
   x->nph = desc->num_phases;
   x->mixed = desc->precision == HYDRO_MIXED;
+  x->mom_gs = desc->velocity_solver == HYDRO_LINEAR_GAUSS_SEIDEL &&
+              (!x->mixed || x->m.n[0] % 2 == 0);
   cudaGetDevice(&x->device);
   if (desc->stream) {
     x->st = (cudaStream_t)desc->stream;
@@ -1160,7 +1206,7 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
                                   x->vf<RT<float, 9>>(s3.G, dim * dim), s3.F[HYDRO_ITER_PREV],
                                   s3.rho, s3.mu, x->vf<R3>(s3.fo, dim), up,
                                   x->uc3(HYDRO_TIME_CURR), x->uc3(HYDRO_TIME_PREV), bv32,
-                                  coef32, res32, s3.Dc, x->st));
+                                  coef32, res32, s3.Dc, x->mom_gs ? 1 : 0, x->st));
     rc = solve_momentum(x);
     if (rc) return rc;
     x->cd_iter_count++;
@@ -1186,7 +1232,7 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
                                    x->vec<C3>(x->fo, dim, m.nc), up, x->uc3(HYDRO_TIME_CURR),
                                    x->uc3(HYDRO_TIME_PREV), bv64,
                                    x->vec<WP<7>>(x->coef, 2 * dim + 1, m.nc),
-                                   x->vec<W3>(x->res, dim, m.nc), x->Dc, x->st));
+                                   x->vec<W3>(x->res, dim, m.nc), x->Dc, 0, x->st));
     rc = solve_momentum(x);
     if (rc) return rc;
     C3 du = x->vec<C3>(x->du[x->du_cur], dim, m.nc);

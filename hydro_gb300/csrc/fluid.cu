@@ -188,16 +188,20 @@ template <int DIM, class T, bool PER>
 __global__ void k_mom_assemble(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> up, RT<T, 3> utc,
                                RT<T, 3> utp, RT<T, 9> G, const T* F, const T* rho, const T* mu,
                                RT<T, 3> fo, Unsteady64 us, RT<T, 3> bv, WT<T, 7> coef,
-                               WT<T, 3> res, T* Dc, int kch) {
+                               WT<T, 3> res, T* Dc, int split, int kch) {
   constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
+  // row index of the coefficients and residuals: natural, or color-blocked
+  // for the red-black Gauss-Seidel sweeps
+  const long long oi =
+      split ? ((X.i[0] + X.i[1] + X.i[2]) & 1) * (m.nc / 2) + (X.c >> 1) : X.c;
   if (EXCLUDED()) {
     // identity row, zero constant (conv_diff.hpp:222-226); CoeffSum 1
-    coef.a[0][X.c] = T(1);
+    coef.a[0][oi] = T(1);
 #pragma unroll
-    for (int q = 0; q < 2 * DIM; ++q) coef.a[1 + q][X.c] = T(0);
+    for (int q = 0; q < 2 * DIM; ++q) coef.a[1 + q][oi] = T(0);
 #pragma unroll
-    for (int n = 0; n < DIM; ++n) res.a[n][X.c] = T(0);
+    for (int n = 0; n < DIM; ++n) res.a[n][oi] = T(0);
     Dc[X.c] = T(1);
     continue;
   }
@@ -269,13 +273,13 @@ __global__ void k_mom_assemble(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> up,
       if (HAS_LO(d)) r += aq[2 * d] * up.a[n][NB_LO(d, s)];
       if (HAS_HI(d)) r += aq[2 * d + 1] * up.a[n][NB_HI(d, s)];
     }
-    res.a[n][X.c] = r;
+    res.a[n][oi] = r;
   }
   T aPr = aP / fc.relax_u;
   // the sweep multiplies by the inverse diagonal
-  coef.a[0][X.c] = T(1) / aPr;
+  coef.a[0][oi] = T(1) / aPr;
 #pragma unroll
-  for (int q = 0; q < 2 * DIM; ++q) coef.a[1 + q][X.c] = aq[q];
+  for (int q = 0; q < 2 * DIM; ++q) coef.a[1 + q][oi] = aq[q];
   Dc[X.c] = cs - aP + aPr;
   CELL_LOOP_END
 }
@@ -324,6 +328,71 @@ __global__ void __launch_bounds__(NT) k_mom_sweep(Mesh m, double omega, double t
       ds->red[RS_MOM_DIFF] = out[0];
       ds->flag[FL_MOM_SWEEPS] += 1;
       if (!(out[0] > tol)) ds->flag[FL_MOM_DONE] = 1;
+    }
+  }
+}
+
+// Red-black Gauss-Seidel half-sweep (see launch_mom_rbgs).  Thread (x, y)
+// owns the color cell of the pair (2x, 2x+1) in row (j, k).  The first sweep
+// starts from du = 0: its red half reads no neighbours and the own old value
+// of both halves is 0.
+template <int DIM, bool PER, class T, bool SPLIT>
+__global__ void __launch_bounds__(NT) k_mom_rbgs(Mesh m, T omega, double tol, RT<T, 7> cf,
+                                                 RT<T, 3> rs, WT<T, 3> du, int color, int limit,
+                                                 double* partials, DevScalars* ds, int kch) {
+  if (ds->flag[FL_MOM_DONE] || ds->flag[FL_MOM_SWEEPS] >= limit) return;
+  const bool first = ds->flag[FL_MOM_SWEEPS] == 0;
+  const int ih = blockIdx.x * BX + threadIdx.x;
+  const int j = blockIdx.y * BY + threadIdx.y;
+  const int nz = DIM == 3 ? m.n[2] : 1;
+  const int k0 = blockIdx.z * kch, k1 = min(k0 + kch, nz);
+  const long long half = m.nc / 2;
+  T dmax = T(0);
+  if (j < m.n[1]) {
+    for (int k = k0; k < k1; ++k) {
+      Cell X;
+      X.i[0] = 2 * ih + ((j + k + color) & 1);
+      X.i[1] = j;
+      X.i[2] = k;
+      if (X.i[0] >= m.n[0]) continue;
+      X.c = cell_id(m, X.i[0], X.i[1], X.i[2]);
+      const long long ci = SPLIT ? color * half + (X.c >> 1) : X.c;
+      const T iaP = cf.a[0][ci];
+      T a[2 * DIM];
+#pragma unroll
+      for (int q = 0; q < 2 * DIM; ++q) a[q] = cf.a[1 + q][ci];
+      constexpr bool kPerT = PER;
+#pragma unroll
+      for (int n = 0; n < DIM; ++n) {
+        T sum = T(0), cur = T(0);
+        if (!first) cur = du.a[n][X.c];
+        if (!(first && color == 0)) {
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) {
+            long long s = cell_stride(m, d);
+            if (HAS_LO(d)) sum += a[2 * d] * du.a[n][NB_LO(d, s)];
+            if (HAS_HI(d)) sum += a[2 * d + 1] * du.a[n][NB_HI(d, s)];
+          }
+        }
+        const T value = -(rs.a[n][ci] + sum) * iaP;
+        const T corr = value - cur;
+        dmax = fmax(dmax, fabs(corr));
+        du.a[n][X.c] = cur + corr * omega;
+      }
+    }
+  }
+  double v[1] = {(double)dmax};
+  __shared__ double out[1];
+  if (grid_reduce<RED_MAX, 1>(v, partials, &ds->ticket[color == 0 ? TK_MOM_RED : TK_MOM], out)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      if (color == 0) {
+        ds->red[RS_MOM_DIFF_RED] = out[0];
+      } else {
+        const double mx = fmax(out[0], ds->red[RS_MOM_DIFF_RED]);
+        ds->red[RS_MOM_DIFF] = mx;
+        ds->flag[FL_MOM_SWEEPS] += 1;
+        if (!(mx > tol)) ds->flag[FL_MOM_DONE] = 1;
+      }
     }
   }
 }
@@ -1072,7 +1141,7 @@ cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, RT<T, 3> u_p
                                 RT<T, 3> u_tc, RT<T, 3> u_tp, RT<T, 9> G, const T* F,
                                 const T* rho, const T* mu, RT<T, 3> fo, C3 up64, C3 utc64,
                                 C3 utp64, RT<T, 3> bv, WT<T, 7> coef, WT<T, 3> res, T* Dc,
-                                cudaStream_t st) {
+                                int split, cudaStream_t st) {
   Unsteady64 us;
   for (int k = 0; k < 3; ++k) {
     us.co[k] = fc.co[k];
@@ -1081,7 +1150,7 @@ cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, RT<T, 3> u_p
     us.utp[k] = utp64.a[k];
   }
   DISPATCH_DIM_TP(m, k_mom_assemble, T, m, make_geo<T>(m), coef_as<T>(fc), u_prev, u_tc, u_tp,
-                 G, F, rho, mu, fo, us, bv, coef, res, Dc);
+                 G, F, rho, mu, fo, us, bv, coef, res, Dc, split);
 }
 
 template <class T>
@@ -1103,7 +1172,8 @@ cudaError_t launch_rhie_chow(const Mesh& m, const FluidCoef& fc, C3 u_prev, RT<T
   template cudaError_t launch_mom_assemble<T>(const Mesh&, const FluidCoef&, RT<T, 3>,        \
                                               RT<T, 3>, RT<T, 3>, RT<T, 9>, const T*,         \
                                               const T*, const T*, RT<T, 3>, C3, C3, C3,       \
-                                              RT<T, 3>, WT<T, 7>, WT<T, 3>, T*, cudaStream_t);\
+                                              RT<T, 3>, WT<T, 7>, WT<T, 3>, T*, int,          \
+                                              cudaStream_t);                                  \
   template cudaError_t launch_rhie_chow<T>(const Mesh&, const FluidCoef&, C3, RT<T, 3>,       \
                                            const double*, C3, RT<T, 3>, RT<T, 3>, const T*,   \
                                            C3, double*, double*, float*, cudaStream_t);
@@ -1125,6 +1195,51 @@ cudaError_t launch_mom_sweep32(const Mesh& m, double omega, double tol, FP<10> c
 
 cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st) {
   k_f2d3<<<flat_blocks(m.nc), NT, 0, st>>>(m.nc, m.dim, in, out);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+namespace {
+Launch rb_launch(const Mesh& m) {
+  Launch L = cell_launch(m);
+  L.grid.x = ((m.n[0] + 1) / 2 + BX - 1) / BX;
+  return L;
+}
+}  // namespace
+
+cudaError_t launch_mom_rbgs(const Mesh& m, double omega, double tol, CP<7> coef, C3 res, W3 du,
+                            int color, int limit, double* partials, DevScalars* ds,
+                            cudaStream_t st) {
+  Launch L = rb_launch(m);
+  const bool p = any_periodic(m);
+  if (m.dim == 3) {
+    if (p) k_mom_rbgs<3, true, double, false><<<L.grid, L.block, 0, st>>>(m, omega, tol, coef, res, du, color, limit, partials, ds, L.kch);
+    else k_mom_rbgs<3, false, double, false><<<L.grid, L.block, 0, st>>>(m, omega, tol, coef, res, du, color, limit, partials, ds, L.kch);
+  } else {
+    if (p) k_mom_rbgs<2, true, double, false><<<L.grid, L.block, 0, st>>>(m, omega, tol, coef, res, du, color, limit, partials, ds, L.kch);
+    else k_mom_rbgs<2, false, double, false><<<L.grid, L.block, 0, st>>>(m, omega, tol, coef, res, du, color, limit, partials, ds, L.kch);
+  }
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mom_rbgs32(const Mesh& m, double omega, double tol, FP<10> c, FP<3> du,
+                              int color, int limit, double* partials, DevScalars* ds,
+                              cudaStream_t st) {
+  RT<float, 7> cf{};
+  RT<float, 3> rs{};
+  for (int q = 0; q < 7; ++q) cf.a[q] = c.a[q];
+  for (int k = 0; k < 3; ++k) rs.a[k] = c.a[7 + k];
+  Launch L = rb_launch(m);
+  const bool p = any_periodic(m);
+  const float om = (float)omega;
+  if (m.dim == 3) {
+    if (p) k_mom_rbgs<3, true, float, true><<<L.grid, L.block, 0, st>>>(m, om, tol, cf, rs, du, color, limit, partials, ds, L.kch);
+    else k_mom_rbgs<3, false, float, true><<<L.grid, L.block, 0, st>>>(m, om, tol, cf, rs, du, color, limit, partials, ds, L.kch);
+  } else {
+    if (p) k_mom_rbgs<2, true, float, true><<<L.grid, L.block, 0, st>>>(m, om, tol, cf, rs, du, color, limit, partials, ds, L.kch);
+    else k_mom_rbgs<2, false, float, true><<<L.grid, L.block, 0, st>>>(m, om, tol, cf, rs, du, color, limit, partials, ds, L.kch);
+  }
   count_launches(1);
   return cudaGetLastError();
 }

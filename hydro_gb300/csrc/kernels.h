@@ -73,7 +73,8 @@ enum {
   RS_P_RES = 16,         // relative pressure residual of the last solve
   RS_IR_FF = 17,         // refinement: ||f||^2 of the first residual
   RS_OUT_FLUX = 18, RS_OUT_AREA = 19, RS_IN_FLUX = 20,  // outlet rebalancing sums
-  RS_HEAT_DIFF = 21      // max |update| of the last temperature sweep
+  RS_HEAT_DIFF = 21,     // max |update| of the last temperature sweep
+  RS_MOM_DIFF_RED = 22   // max |update| of the red half of a Gauss-Seidel sweep
 };
 enum {
   FL_MOM_DONE = 0, FL_MOM_SWEEPS = 1, FL_PCG_DONE = 2, FL_PCG_ITERS = 3, FL_NAN = 4,
@@ -91,7 +92,7 @@ enum {
   TK_MOM = 0, TK_PCG_A = 1, TK_PCG_B = 2, TK_PCG_INIT = 3, TK_IND = 4, TK_DT = 5,
   TK_MEAN = 6, TK_MEAN2 = 7, TK_STAT = 8, TK_STAT2 = 9, TK_STAT3 = 10, TK_IR = 11,
   TK_NAN = 12, TK_PCG_INIT2 = 13, TK_F32_A = 14, TK_F32_B = 15, TK_F32_INIT = 16,
-  TK_OUTLET = 17, TK_HEAT = 18
+  TK_OUTLET = 17, TK_HEAT = 18, TK_MOM_RED = 19
 };
 
 // ---------------------------------------------------------------- fluid --
@@ -127,7 +128,7 @@ cudaError_t launch_mom_assemble(const Mesh& m, const FluidCoef& fc, RT<T, 3> u_p
                                 RT<T, 3> u_tc, RT<T, 3> u_tp, RT<T, 9> G, const T* F,
                                 const T* rho, const T* mu, RT<T, 3> fo, C3 up64, C3 utc64,
                                 C3 utp64, RT<T, 3> bv, WT<T, 7> coef, WT<T, 3> res, T* Dc,
-                                cudaStream_t st);
+                                int split, cudaStream_t st);
 // u_prev, p, gp (cell pressure gradient from launch_force) are FP64
 template <class T>
 cudaError_t launch_rhie_chow(const Mesh& m, const FluidCoef& fc, C3 u_prev, RT<T, 3> du,
@@ -141,6 +142,20 @@ cudaError_t launch_mom_sweep32(const Mesh& m, double omega, double tol, FP<10> c
                                FP<3> dout, int limit, double* partials, DevScalars* ds,
                                cudaStream_t st);
 cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st);
+// Red-black Gauss-Seidel half-sweep of the momentum corrections (the
+// parallel ordering of GaussSeidel::Solve, linear.hpp:671-716), in place on
+// du: the cells of `color` ((i+j+k) % 2) from the other color's current
+// values, x += omega (value - x).  The red half keeps its max |value - x| in
+// RS_MOM_DIFF_RED, the black half completes the sweep's max and the exit
+// rules of launch_mom_sweep.  split: the coefficients and residuals are
+// stored color-blocked (index color * nc/2 + c/2; nx even), the layout the
+// FP32 assembly writes for this solver.
+cudaError_t launch_mom_rbgs(const Mesh& m, double omega, double tol, CP<7> coef, C3 res, W3 du,
+                            int color, int limit, double* partials, DevScalars* ds,
+                            cudaStream_t st);
+cudaError_t launch_mom_rbgs32(const Mesh& m, double omega, double tol, FP<10> c, FP<3> du,
+                              int color, int limit, double* partials, DevScalars* ds,
+                              cudaStream_t st);
 cudaError_t launch_mom_sweep(const Mesh& m, double omega, double tol, CP<7> coef, C3 res,
                              C3 din, W3 dout, int limit, double* partials, DevScalars* ds,
                              cudaStream_t st);

@@ -188,6 +188,56 @@ def test_fp64_multigrid_refinement_matches_oracle(built):
     assert all(v <= 1e-12 for v in errs.values()), errs
 
 
+def test_gauss_seidel_momentum(built):
+    """velocity_solver GAUSS_SEIDEL: red-black Gauss-Seidel sweeps in place
+    (FP64 rows natural, FP32 rows color-blocked).  Tight solves reach the
+    oracle's (lexicographic Gauss-Seidel) fields; fewer sweeps than Jacobi;
+    the mixed form within its tolerance; the graph step equals the host
+    step."""
+    from hydro_gb300.solver import Hydro
+    from oracle.oracle import Oracle
+    d, u0, q0, _ = cases.rising_drops(n=24, seed=4, dt_max=5e-3)
+    d.n[0], d.n[1], d.n[2] = 24, 20, 16  # nz != nx: the color-blocked index
+    from hydro_gb300.cases import cell_centers, two_phase_q
+    d.hi[0], d.hi[1], d.hi[2] = 1.5, 1.25, 1.0
+    x, y, z = cell_centers(d)
+    alpha1 = (((x - 0.7) ** 2 + (y - 0.6) ** 2 + (z - 0.4) ** 2) < 0.2 ** 2).astype(float)
+    q0 = two_phase_q(d, alpha1, 2)
+    u0 = np.zeros(d.ncells * 3)
+    u0[: d.ncells] = 0.05 * np.sin(2 * np.pi * x)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    d.velocity_solver = capi.LINEAR_GAUSS_SEIDEL
+    d.pressure_solver = capi.LINEAR_MGCG
+    a = run(Hydro(d), u0, q0, 3)
+    do = d.copy()
+    do.pressure_solver = capi.LINEAR_CG
+    b = run(Oracle(do), u0, q0, 3)
+    errs = compare(a, b)
+    assert all(v <= 1e-10 for v in errs.values()), errs
+    dj = d.copy()
+    dj.velocity_solver = capi.LINEAR_JACOBI
+    c = run(Hydro(dj), u0, q0, 3)
+    assert sum(s["velocity_sweeps"] for s in a["stats"]) < sum(
+        s["velocity_sweeps"] for s in c["stats"])
+    dm = d.copy()
+    dm.precision = capi.MIXED
+    dm.velocity_tolerance = 1e-9
+    e = run(Hydro(dm), u0, q0, 3)
+    errs = compare(e, a)
+    assert errs["u"] <= 1e-6 and errs["F"] <= 1e-6 and errs["q"] <= 1e-6, errs
+    h = Hydro(dm)
+    h.set_field(capi.F_VELOCITY, u0)
+    h.set_field(capi.F_PARTIAL_DENSITY, q0)
+    h.init_state()
+    for _ in range(3):
+        h.step_graph()
+    g = {"u": h.get_field(capi.F_VELOCITY), "p": h.get_field(capi.F_PRESSURE),
+         "F": h.get_field(capi.F_VOLUME_FLUX), "q": h.get_field(capi.F_PARTIAL_DENSITY)}
+    errs = compare(g, e)
+    assert all(v <= 1e-12 for v in errs.values()), errs
+
+
 def test_stencil_solve_matches_oracle(built):
     from hydro_gb300.solver import stencil_solve
     from oracle import oracle as O
