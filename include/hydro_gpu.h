@@ -152,9 +152,11 @@ typedef struct hydro_desc {
   int num_iterations_limit;     /* SIMPLE outer iterations per step */
   int simpler;                  /* SIMPLER pressure (fluid.hpp:1059-1155); FP64 only */
 
-  int velocity_solver;          /* enum hydro_linear; the GPU sweeps Jacobi for all three
-                                   (the parallel one): with a tight velocity_tolerance the
-                                   three reach the same solution */
+  int velocity_solver;          /* enum hydro_linear: GAUSS_SEIDEL sweeps red-black
+                                   Gauss-Seidel in place (mixed precision: when n[0] is
+                                   even, else Jacobi); JACOBI and LU sweep Jacobi (LU is
+                                   sequential).  With a tight velocity_tolerance all reach
+                                   the same solution */
   double velocity_tolerance;    /* max |update| per sweep */
   int velocity_iters_limit;
   double velocity_omega;        /* relaxation of the sweep */
