@@ -173,6 +173,7 @@ struct hydro_ctx {
   // the FP32 path then stores its rows color-blocked, which needs an even
   // Nx) or Jacobi
   bool mom_gs = false;
+  bool mom_split64 = false;
   // graph-captured step (hydro_gpu_step_graph): capture state and the
   // instantiated step with the values it was captured for
   bool graph_mode = false;
@@ -415,8 +416,8 @@ int solve_momentum(hydro_ctx* x) {
         else
           PK(x, HYDRO_PROF_MOM_SWEEP,
              launch_mom_rbgs(x->m, d.velocity_omega, d.velocity_tolerance, cc, resc,
-                             x->vec<W3>(x->du[0], dim, x->m.nc), color, limit, x->pw.partials,
-                             x->pw.ds, x->st));
+                             x->vec<W3>(x->du[0], dim, x->m.nc), color, x->mom_split64 ? 1 : 0,
+                             limit, x->pw.partials, x->pw.ds, x->st));
       }
       return HYDRO_OK;
     };
@@ -815,6 +816,8 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
   x->mixed = desc->precision == HYDRO_MIXED;
   x->mom_gs = desc->velocity_solver == HYDRO_LINEAR_GAUSS_SEIDEL &&
               (!x->mixed || x->m.n[0] % 2 == 0);
+  // FP64 rows color-blocked too, unless SIMPLER reads them in cell order
+  x->mom_split64 = x->mom_gs && !x->mixed && !desc->simpler && x->m.n[0] % 2 == 0;
   cudaGetDevice(&x->device);
   if (desc->stream) {
     x->st = (cudaStream_t)desc->stream;
@@ -1232,7 +1235,8 @@ int hydro_gpu_make_iteration(hydro_ctx* x) {
                                    x->vec<C3>(x->fo, dim, m.nc), up, x->uc3(HYDRO_TIME_CURR),
                                    x->uc3(HYDRO_TIME_PREV), bv64,
                                    x->vec<WP<7>>(x->coef, 2 * dim + 1, m.nc),
-                                   x->vec<W3>(x->res, dim, m.nc), x->Dc, 0, x->st));
+                                   x->vec<W3>(x->res, dim, m.nc), x->Dc,
+                                   x->mom_split64 ? 1 : 0, x->st));
     rc = solve_momentum(x);
     if (rc) return rc;
     C3 du = x->vec<C3>(x->du[x->du_cur], dim, m.nc);

@@ -357,27 +357,34 @@ __global__ void __launch_bounds__(NT) k_mom_rbgs(Mesh m, T omega, double tol, RT
       if (X.i[0] >= m.n[0]) continue;
       X.c = cell_id(m, X.i[0], X.i[1], X.i[2]);
       const long long ci = SPLIT ? color * half + (X.c >> 1) : X.c;
+      // every load of the cell before its first store: the three components'
+      // rows and neighbours are in flight together
       const T iaP = cf.a[0][ci];
-      T a[2 * DIM];
+      T a[2 * DIM], r[DIM], cur[DIM], nb[DIM][2 * DIM];
 #pragma unroll
       for (int q = 0; q < 2 * DIM; ++q) a[q] = cf.a[1 + q][ci];
       constexpr bool kPerT = PER;
+      const bool rd = !(first && color == 0);
 #pragma unroll
       for (int n = 0; n < DIM; ++n) {
-        T sum = T(0), cur = T(0);
-        if (!first) cur = du.a[n][X.c];
-        if (!(first && color == 0)) {
+        r[n] = rs.a[n][ci];
+        cur[n] = first ? T(0) : du.a[n][X.c];
 #pragma unroll
-          for (int d = 0; d < DIM; ++d) {
-            long long s = cell_stride(m, d);
-            if (HAS_LO(d)) sum += a[2 * d] * du.a[n][NB_LO(d, s)];
-            if (HAS_HI(d)) sum += a[2 * d + 1] * du.a[n][NB_HI(d, s)];
-          }
+        for (int d = 0; d < DIM; ++d) {
+          long long s = cell_stride(m, d);
+          nb[n][2 * d] = rd && HAS_LO(d) ? du.a[n][NB_LO(d, s)] : T(0);
+          nb[n][2 * d + 1] = rd && HAS_HI(d) ? du.a[n][NB_HI(d, s)] : T(0);
         }
-        const T value = -(rs.a[n][ci] + sum) * iaP;
-        const T corr = value - cur;
+      }
+#pragma unroll
+      for (int n = 0; n < DIM; ++n) {
+        T sum = T(0);
+#pragma unroll
+        for (int q = 0; q < 2 * DIM; ++q) sum += a[q] * nb[n][q];
+        const T value = -(r[n] + sum) * iaP;
+        const T corr = value - cur[n];
         dmax = fmax(dmax, fabs(corr));
-        du.a[n][X.c] = cur + corr * omega;
+        du.a[n][X.c] = cur[n] + corr * omega;
       }
     }
   }
@@ -1200,25 +1207,31 @@ cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st) {
 }
 
 namespace {
+// Grid of a red-black half-sweep: one thread per cell pair along x, sized
+// like a cell launch over the half-width mesh.
 Launch rb_launch(const Mesh& m) {
-  Launch L = cell_launch(m);
-  L.grid.x = ((m.n[0] + 1) / 2 + BX - 1) / BX;
-  return L;
+  Mesh h = m;
+  h.n[0] = (m.n[0] + 1) / 2;
+  return cell_launch(h);
 }
 }  // namespace
 
 cudaError_t launch_mom_rbgs(const Mesh& m, double omega, double tol, CP<7> coef, C3 res, W3 du,
-                            int color, int limit, double* partials, DevScalars* ds,
+                            int color, int split, int limit, double* partials, DevScalars* ds,
                             cudaStream_t st) {
   Launch L = rb_launch(m);
   const bool p = any_periodic(m);
+#define RBGS64(D, P, S) \
+  k_mom_rbgs<D, P, double, S><<<L.grid, L.block, 0, st>>>(m, omega, tol, coef, res, du, color, \
+                                                          limit, partials, ds, L.kch)
   if (m.dim == 3) {
-    if (p) k_mom_rbgs<3, true, double, false><<<L.grid, L.block, 0, st>>>(m, omega, tol, coef, res, du, color, limit, partials, ds, L.kch);
-    else k_mom_rbgs<3, false, double, false><<<L.grid, L.block, 0, st>>>(m, omega, tol, coef, res, du, color, limit, partials, ds, L.kch);
+    if (split) { if (p) RBGS64(3, true, true); else RBGS64(3, false, true); }
+    else { if (p) RBGS64(3, true, false); else RBGS64(3, false, false); }
   } else {
-    if (p) k_mom_rbgs<2, true, double, false><<<L.grid, L.block, 0, st>>>(m, omega, tol, coef, res, du, color, limit, partials, ds, L.kch);
-    else k_mom_rbgs<2, false, double, false><<<L.grid, L.block, 0, st>>>(m, omega, tol, coef, res, du, color, limit, partials, ds, L.kch);
+    if (split) { if (p) RBGS64(2, true, true); else RBGS64(2, false, true); }
+    else { if (p) RBGS64(2, true, false); else RBGS64(2, false, false); }
   }
+#undef RBGS64
   count_launches(1);
   return cudaGetLastError();
 }

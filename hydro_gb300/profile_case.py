@@ -2,10 +2,12 @@
 
     python -m hydro_gb300.profile_case [--n 150] [--precision fp64|mixed]
                                        [--solver cg|mgcg] [--outer 1] [--cg 40]
+                                       [--velocity jacobi|gs]
 
 Builds the rising-drops case at n^3, runs one time step with `outer` SIMPLE
 iterations and at most `cg` pressure-CG iterations per solve, and exits
-(`--solver mgcg`, mixed precision only: CG preconditioned by multigrid).
+(`--solver mgcg`: CG preconditioned by multigrid; `--velocity gs`:
+red-black Gauss-Seidel momentum sweeps instead of Jacobi).
 At n = 150 the arrays of one CG iteration (p, couplings, diagonal, A p)
 exceed the 129 MB L2 while the whole context stays near 2 GB, and the run
 issues a few hundred kernel launches -- small enough for ncu captures to end
@@ -22,6 +24,7 @@ def main(argv=None):
     ap.add_argument("--solver", default="cg", choices=["cg", "mgcg"])
     ap.add_argument("--outer", type=int, default=1)
     ap.add_argument("--cg", type=int, default=40)
+    ap.add_argument("--velocity", default="jacobi", choices=["jacobi", "gs"])
     args = ap.parse_args(argv)
     from . import capi, cases
     from .solver import launch_count, make
@@ -30,6 +33,8 @@ def main(argv=None):
     d.num_iterations_limit = args.outer
     d.velocity_tolerance = 1e-8
     d.velocity_iters_limit = 50
+    if args.velocity == "gs":
+        d.velocity_solver = capi.LINEAR_GAUSS_SEIDEL
     d.pressure_tolerance = 1e-30
     d.pressure_iters_limit = args.cg
     d.precision = capi.MIXED if args.precision == "mixed" else capi.FP64

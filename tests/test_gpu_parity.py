@@ -238,6 +238,33 @@ def test_gauss_seidel_momentum(built):
     assert all(v <= 1e-12 for v in errs.values()), errs
 
 
+@pytest.mark.parametrize("nx", [25, 24])
+def test_gauss_seidel_momentum_2d_cavity(built, nx):
+    """Red-black Gauss-Seidel in 2D with rows in cell order (odd nx: FP64
+    natural, the mixed form falls back to Jacobi) and color-blocked (even
+    nx) against the oracle's lexicographic Gauss-Seidel."""
+    from hydro_gb300.solver import Hydro
+    from oracle.oracle import Oracle
+    d, u0, q0 = cases.cavity(n=20, mu=0.01, dt=1e-2)
+    d.n[0] = nx
+    d.hi[0] = nx / 20.0
+    u0 = np.zeros(d.ncells * 2)
+    q0 = np.ones(d.ncells)
+    tight(d)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    d.velocity_solver = capi.LINEAR_GAUSS_SEIDEL
+    a = run(Hydro(d), u0, q0, 3)
+    b = run(Oracle(d), u0, q0, 3)
+    errs = compare(a, b)
+    assert all(v <= 1e-10 for v in errs.values()), errs
+    dm = d.copy()
+    dm.precision = capi.MIXED
+    dm.velocity_tolerance = 1e-9
+    e = run(Hydro(dm), u0, q0, 3)
+    errs = compare(e, a)
+    assert errs["u"] <= 1e-6 and errs["F"] <= 1e-6, errs
+
+
 def test_stencil_solve_matches_oracle(built):
     from hydro_gb300.solver import stencil_solve
     from oracle import oracle as O
