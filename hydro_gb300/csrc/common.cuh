@@ -122,6 +122,37 @@ inline Launch cell_launch(const Mesh& m, int target_blocks = 152 * 16) {
   return L;
 }
 
+// CTAs of `kernel` (NT threads, no dynamic shared memory) resident on the
+// whole GPU at once; queried once per kernel.
+int resident_ctas(const void* kernel);
+
+// Cell launch sized in whole waves: a CTA marches kch planes, and a grid of
+// C CTAs with R resident takes ceil(C / R) rounds of kch planes plus a
+// fixed cost per CTA (start, block reduction: about two planes); among the
+// grids that fill the GPU at least once, the cheapest (ties: fewer CTAs),
+// so that no nearly empty last wave holds the whole GPU for a full march.
+inline Launch cell_launch_waves(const Mesh& m, int resident) {
+  Launch L = cell_launch(m);
+  if (resident <= 0) return L;
+  const int nz = m.dim == 3 ? m.n[2] : 1;
+  const long long per = (long long)L.grid.x * L.grid.y;
+  if (per * nz < resident) return L;
+  long long best = -1;
+  for (int gz = 1; gz <= nz; ++gz) {
+    const int kch = (nz + gz - 1) / gz;
+    if ((nz + kch - 1) / kch != gz) continue;  // same march as a smaller grid
+    if (per * gz < resident) continue;
+    if (per * gz > (1 << 17)) break;
+    const long long cost = (per * gz + resident - 1) / resident * (kch + 2);
+    if (best < 0 || cost < best) {
+      best = cost;
+      L.kch = kch;
+      L.grid.z = (unsigned)gz;
+    }
+  }
+  return L;
+}
+
 // ------------------------------------------------------------ reductions --
 // Deterministic grid reduction: every block writes its partial, the last
 // block to arrive (atomic ticket) combines the partials in index order and
@@ -213,14 +244,23 @@ __device__ inline bool grid_reduce(T (&v)[NV], T* partials, unsigned* ticket, T*
   if (!last) return false;
   __threadfence();
   // fixed-order combine: thread t folds partials t, t+nthr, ... in order,
-  // then a fixed tree over threads
+  // then a fixed tree over threads.  The partials are read from L2 (ld.cg:
+  // written by other blocks, made visible by their fences), eight in flight
+  // per thread before they are folded.
   T acc[NV];
 #pragma unroll
   for (int a = 0; a < NV; ++a) {
-    const volatile T* pa = partials + (size_t)a * nb;
-    T x = (tid < (int)nb) ? pa[tid] : T(0);
-    for (unsigned b = tid + nthr; b < nb; b += nthr) x = red_combine<OP>(x, (T)pa[b]);
-    if (tid >= (int)nb) x = (OP == RED_SUM) ? T(0) : (T)pa[0];
+    const T* pa = partials + (size_t)a * nb;
+    T x = (OP == RED_SUM) ? T(0) : __ldcg(pa);
+    unsigned b = tid;
+    for (; b + 7u * nthr < nb; b += 8u * nthr) {
+      T y[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) y[u] = __ldcg(pa + b + u * nthr);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) x = red_combine<OP>(x, y[u]);
+    }
+    for (; b < nb; b += nthr) x = red_combine<OP>(x, __ldcg(pa + b));
     acc[a] = x;
   }
   block_reduce<OP, NV>(acc, sh);

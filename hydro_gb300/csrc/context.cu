@@ -18,7 +18,9 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <mutex>
 #include <new>
+#include <unordered_map>
 #include <utility>
 #include <vector>
 
@@ -31,6 +33,22 @@ using namespace hg;
 namespace hg {
 static std::atomic<long long> g_launches{0};
 void count_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int resident_ctas(const void* kernel) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, int> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(kernel);
+  if (it != cache.end()) return it->second;
+  int dev = 0, sms = 0, per_sm = 0;
+  int r = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess &&
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, NT, 0) == cudaSuccess)
+    r = per_sm * sms;
+  cache[kernel] = r;
+  return r;
+}
 }  // namespace hg
 
 namespace {
@@ -59,6 +77,7 @@ struct EventProfiler : Profiler {
   }
   void begin(int, cudaStream_t st) override {
     if (!on) return;
+    if (open) pool.push_back(open);  // an inner group replaces an open outer one
     open = get();
     cudaEventRecord(open, st);
   }
@@ -87,6 +106,12 @@ struct EventProfiler : Profiler {
       launches[g] = 0;
       ms[g] = 0.;
     }
+  }
+  // bracketed launches that found the solve converged and exited at once
+  // (queued past convergence by the chunked host loop): kept in the time,
+  // taken out of the count
+  void uncount(int g, long long n) {
+    if (on && n > 0) launches[g] -= n;
   }
   ~EventProfiler() {
     for (auto& p : pending) {
@@ -668,6 +693,7 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
         if (rc) return rc;
         if (x->hds->flag[FL_PCG_DONE] || queued >= w.limit) break;
       }
+      if (mgcg) x->prof.uncount(HYDRO_PROF_MG_VCYCLE, queued - x->hds->flag[FL_PCG_ITERS]);
       total += x->hds->flag[FL_PCG_ITERS];
       CK(f32_accumulate(m, x->pc, w, x->st));
     }

@@ -1208,22 +1208,24 @@ cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st) {
 
 namespace {
 // Grid of a red-black half-sweep: one thread per cell pair along x, sized
-// like a cell launch over the half-width mesh.
-Launch rb_launch(const Mesh& m) {
+// in whole waves over the half-width mesh.
+Launch rb_launch(const Mesh& m, const void* kernel) {
   Mesh h = m;
   h.n[0] = (m.n[0] + 1) / 2;
-  return cell_launch(h);
+  return cell_launch_waves(h, resident_ctas(kernel));
 }
 }  // namespace
 
 cudaError_t launch_mom_rbgs(const Mesh& m, double omega, double tol, CP<7> coef, C3 res, W3 du,
                             int color, int split, int limit, double* partials, DevScalars* ds,
                             cudaStream_t st) {
-  Launch L = rb_launch(m);
   const bool p = any_periodic(m);
-#define RBGS64(D, P, S) \
-  k_mom_rbgs<D, P, double, S><<<L.grid, L.block, 0, st>>>(m, omega, tol, coef, res, du, color, \
-                                                          limit, partials, ds, L.kch)
+#define RBGS64(D, P, S)                                                                       \
+  do {                                                                                        \
+    Launch L = rb_launch(m, (const void*)k_mom_rbgs<D, P, double, S>);                        \
+    k_mom_rbgs<D, P, double, S><<<L.grid, L.block, 0, st>>>(m, omega, tol, coef, res, du,     \
+                                                            color, limit, partials, ds, L.kch); \
+  } while (0)
   if (m.dim == 3) {
     if (split) { if (p) RBGS64(3, true, true); else RBGS64(3, false, true); }
     else { if (p) RBGS64(3, true, false); else RBGS64(3, false, false); }
@@ -1243,16 +1245,20 @@ cudaError_t launch_mom_rbgs32(const Mesh& m, double omega, double tol, FP<10> c,
   RT<float, 3> rs{};
   for (int q = 0; q < 7; ++q) cf.a[q] = c.a[q];
   for (int k = 0; k < 3; ++k) rs.a[k] = c.a[7 + k];
-  Launch L = rb_launch(m);
   const bool p = any_periodic(m);
   const float om = (float)omega;
+#define RBGS32(D, P)                                                                        \
+  do {                                                                                      \
+    Launch L = rb_launch(m, (const void*)k_mom_rbgs<D, P, float, true>);                    \
+    k_mom_rbgs<D, P, float, true><<<L.grid, L.block, 0, st>>>(m, om, tol, cf, rs, du, color, \
+                                                              limit, partials, ds, L.kch);  \
+  } while (0)
   if (m.dim == 3) {
-    if (p) k_mom_rbgs<3, true, float, true><<<L.grid, L.block, 0, st>>>(m, om, tol, cf, rs, du, color, limit, partials, ds, L.kch);
-    else k_mom_rbgs<3, false, float, true><<<L.grid, L.block, 0, st>>>(m, om, tol, cf, rs, du, color, limit, partials, ds, L.kch);
+    if (p) RBGS32(3, true); else RBGS32(3, false);
   } else {
-    if (p) k_mom_rbgs<2, true, float, true><<<L.grid, L.block, 0, st>>>(m, om, tol, cf, rs, du, color, limit, partials, ds, L.kch);
-    else k_mom_rbgs<2, false, float, true><<<L.grid, L.block, 0, st>>>(m, om, tol, cf, rs, du, color, limit, partials, ds, L.kch);
+    if (p) RBGS32(2, true); else RBGS32(2, false);
   }
+#undef RBGS32
   count_launches(1);
   return cudaGetLastError();
 }

@@ -347,9 +347,12 @@ struct DFAcc {
 // p_new = z + beta p_old (p_new = z on the first iteration) evaluated at the
 // cell and its neighbours, A p_new, <p_new, A p_new> -> alpha.
 template <int DIM, bool PER>
-__global__ void __launch_bounds__(NT) k_cg32_dir_spmv(Mesh m, const float* kf, const float* dg,
-                                                      const float* z, const float* pold,
-                                                      float* pnew, float* Ap, long long pin,
+__global__ void __launch_bounds__(NT) k_cg32_dir_spmv(Mesh m, const float* __restrict__ kf,
+                                                      const float* __restrict__ dg,
+                                                      const float* __restrict__ z,
+                                                      const float* __restrict__ pold,
+                                                      float* __restrict__ pnew,
+                                                      float* __restrict__ Ap, long long pin,
                                                       double* partials, DevScalars* ds,
                                                       int kch) {
   constexpr bool kPerT = PER;
@@ -427,14 +430,14 @@ __global__ void __launch_bounds__(NT) k_cg32_update(long long n, float* x, float
 cudaError_t cg32_dir_spmv(const Mesh& m, const float* kf, const float* dg, const float* z,
                           const float* pold, float* pnew, float* Ap, long long pin,
                           double* partials, DevScalars* ds, cudaStream_t st) {
-  Launch L = cell_launch(m);
+  Launch L = cell_launch_waves(m, resident_ctas(CELL_KERNEL_P(m, k_cg32_dir_spmv)));
   CELL_LAUNCH_P(m, L, st, k_cg32_dir_spmv, m, kf, dg, z, pold, pnew, Ap, pin, partials, ds);
   count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t f32_pcg_iterate(const Mesh& m, int chunk, PcgWork& w, cudaStream_t st) {
-  Launch L = cell_launch(m);
+  Launch L = cell_launch_waves(m, resident_ctas(CELL_KERNEL_P(m, k_cg32_dir_spmv)));
   int fb = flat_blocks_l(m.nc);
   for (int it = 0; it < chunk; ++it) {
     // p lives in w.p32 / w.p32b alternately; its parity only matters while

@@ -94,6 +94,13 @@ constexpr bool kPerT = true;
       else KERNEL<2, false><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);   \
     }                                                                                \
   } while (0)
+// The instantiation CELL_LAUNCH_P launches, as a pointer for occupancy
+// queries.
+#define CELL_KERNEL_P(m, KERNEL)                                                       \
+  ((m).dim == 3 ? (any_periodic(m) ? (const void*)KERNEL<3, true>                      \
+                                   : (const void*)KERNEL<3, false>)                    \
+                : (any_periodic(m) ? (const void*)KERNEL<2, true>                      \
+                                   : (const void*)KERNEL<2, false>))
 #define CELL_LAUNCH_TP(m, L, st, KERNEL, T, ...)                                        \
   do {                                                                                  \
     const bool p_ = any_periodic(m);                                                    \

@@ -452,14 +452,33 @@ struct DFAcc2 {
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
+// The vector kernels of the inner solve step four cells per thread with
+// 16-byte loads (every vector is 256-byte aligned, the launchers check);
+// the last n % 4 cells are taken one by one by the first threads of the
+// grid.
+
 // Inner-solve start: r = FP32 copy of the FP64 refinement residual; ||r||^2
 // sets the stop test.
-__global__ void __launch_bounds__(NT) k_mgcg_init(long long n, const double* r64, float* r,
-                                                  float* x, double tol, int limit, int dev_params,
+__global__ void __launch_bounds__(NT) k_mgcg_init(long long n, const double* __restrict__ r64,
+                                                  float* __restrict__ r, float* __restrict__ x,
+                                                  double tol, int limit, int dev_params,
                                                   double* partials, DevScalars* ds) {
   double s = 0.;
-  long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
-  for (long long i = blockIdx.x * (long long)NT + tid; i < n; i += (long long)gridDim.x * NT) {
+  const long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
+  const long long g = blockIdx.x * (long long)NT + tid, stride = (long long)gridDim.x * NT;
+  const long long n4 = n >> 2;
+  const double2* r2 = reinterpret_cast<const double2*>(r64);
+#pragma unroll 2
+  for (long long i = g; i < n4; i += stride) {
+    const double2 a = r2[2 * i], b = r2[2 * i + 1];
+    reinterpret_cast<float4*>(r)[i] = make_float4((float)a.x, (float)a.y, (float)b.x, (float)b.y);
+    reinterpret_cast<float4*>(x)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    s += a.x * a.x;
+    s += a.y * a.y;
+    s += b.x * b.x;
+    s += b.y * b.y;
+  }
+  for (long long i = 4 * n4 + g; i < n; i += stride) {
     double v = r64[i];
     r[i] = (float)v;
     x[i] = 0.f;
@@ -481,14 +500,39 @@ __global__ void __launch_bounds__(NT) k_mgcg_init(long long n, const double* r64
 }
 
 // x += alpha p, r -= alpha Ap; ||r||^2 and the stop test.
-__global__ void __launch_bounds__(NT) k_mgcg_update(long long n, float* x, float* r,
-                                                    const float* p, const float* Ap,
+__global__ void __launch_bounds__(NT) k_mgcg_update(long long n, float* __restrict__ x,
+                                                    float* __restrict__ r,
+                                                    const float* __restrict__ p,
+                                                    const float* __restrict__ Ap,
                                                     double* partials, DevScalars* ds) {
   if (ds->flag[FL_PCG_DONE]) return;
   const float at = (float)ds->red[RS_PCG_ALPHA];
   DFAcc2 rr;
-  long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
-  for (long long i = blockIdx.x * (long long)NT + tid; i < n; i += (long long)gridDim.x * NT) {
+  const long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
+  const long long g = blockIdx.x * (long long)NT + tid, stride = (long long)gridDim.x * NT;
+  const long long n4 = n >> 2;
+#pragma unroll 2
+  for (long long i = g; i < n4; i += stride) {
+    float4 xv = reinterpret_cast<const float4*>(x)[i];
+    float4 rv = reinterpret_cast<const float4*>(r)[i];
+    const float4 pv = reinterpret_cast<const float4*>(p)[i];
+    const float4 av = reinterpret_cast<const float4*>(Ap)[i];
+    xv.x = fmaf(at, pv.x, xv.x);
+    xv.y = fmaf(at, pv.y, xv.y);
+    xv.z = fmaf(at, pv.z, xv.z);
+    xv.w = fmaf(at, pv.w, xv.w);
+    rv.x = fmaf(-at, av.x, rv.x);
+    rv.y = fmaf(-at, av.y, rv.y);
+    rv.z = fmaf(-at, av.z, rv.z);
+    rv.w = fmaf(-at, av.w, rv.w);
+    reinterpret_cast<float4*>(x)[i] = xv;
+    reinterpret_cast<float4*>(r)[i] = rv;
+    rr.add_prod(rv.x, rv.x);
+    rr.add_prod(rv.y, rv.y);
+    rr.add_prod(rv.z, rv.z);
+    rr.add_prod(rv.w, rv.w);
+  }
+  for (long long i = 4 * n4 + g; i < n; i += stride) {
     x[i] = fmaf(at, p[i], x[i]);
     float ri = fmaf(-at, Ap[i], r[i]);
     r[i] = ri;
@@ -508,13 +552,24 @@ __global__ void __launch_bounds__(NT) k_mgcg_update(long long n, float* x, float
 }
 
 // <r, z> -> beta = <r,z>/<r,z>_old (first: only stores <r,z>).
-__global__ void __launch_bounds__(NT) k_mgcg_dot(long long n, const float* r, const float* z,
-                                                 int first, double* partials, DevScalars* ds) {
+__global__ void __launch_bounds__(NT) k_mgcg_dot(long long n, const float* __restrict__ r,
+                                                 const float* __restrict__ z, int first,
+                                                 double* partials, DevScalars* ds) {
   if (ds->flag[FL_PCG_DONE]) return;
   DFAcc2 rz;
-  long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
-  for (long long i = blockIdx.x * (long long)NT + tid; i < n; i += (long long)gridDim.x * NT)
-    rz.add_prod(r[i], z[i]);
+  const long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
+  const long long g = blockIdx.x * (long long)NT + tid, stride = (long long)gridDim.x * NT;
+  const long long n4 = n >> 2;
+#pragma unroll 4
+  for (long long i = g; i < n4; i += stride) {
+    const float4 a = reinterpret_cast<const float4*>(r)[i];
+    const float4 b = reinterpret_cast<const float4*>(z)[i];
+    rz.add_prod(a.x, b.x);
+    rz.add_prod(a.y, b.y);
+    rz.add_prod(a.z, b.z);
+    rz.add_prod(a.w, b.w);
+  }
+  for (long long i = 4 * n4 + g; i < n; i += stride) rz.add_prod(r[i], z[i]);
   double s[1] = {rz.value()};
   __shared__ double o[1];
   if (grid_reduce<RED_SUM, 1>(s, partials, &ds->ticket[TK_PCG_INIT2], o)) {
@@ -524,6 +579,8 @@ __global__ void __launch_bounds__(NT) k_mgcg_dot(long long n, const float* r, co
     }
   }
 }
+
+bool aligned16(const void* a) { return (reinterpret_cast<uintptr_t>(a) & 15) == 0; }
 
 int flat_blocks_mg(long long n) {
   long long b = (n + NT - 1) / NT;
@@ -742,6 +799,9 @@ cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevSc
 cudaError_t mgcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, MgWork& mg,
                       cudaStream_t st) {
   int fb = flat_blocks_mg(m.nc);
+  if (!aligned16(w.r) || !aligned16(w.r32) || !aligned16(w.x32) || !aligned16(w.z32) ||
+      !aligned16(w.p32) || !aligned16(w.p32b) || !aligned16(w.Ap32))
+    return cudaErrorInvalidValue;
   w.p32_parity = 0;
   k_mgcg_init<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.r, w.r32, w.x32, tol, w.limit, dev_params,
                                            w.partials, w.ds);

@@ -447,7 +447,9 @@ int hydro_gpu_stencil_solve_noalloc(int dim, int nx, int ny, int nz,
  * there).  With profiling on, every launch of the groups below is
  * bracketed by CUDA events on the context's stream; get_profile returns
  * the launches and summed device milliseconds of one group since the last
- * reset.  The launch count covers every kernel this library enqueued. */
+ * reset (multigrid V-cycles queued past the convergence of their Krylov
+ * solve exit at once: their time is kept, their count is not).  The launch
+ * count covers every kernel this library enqueued. */
 enum hydro_prof_group {
   HYDRO_PROF_VEL_GRAD = 0, HYDRO_PROF_FORCE, HYDRO_PROF_MOM_ASSEMBLE, HYDRO_PROF_MOM_SWEEP,
   HYDRO_PROF_RHIE_CHOW, HYDRO_PROF_PRESSURE_RHS, HYDRO_PROF_CG_INIT, HYDRO_PROF_CG_SPMV,
