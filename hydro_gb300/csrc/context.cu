@@ -450,24 +450,32 @@ int solve_momentum(hydro_ctx* x) {
     if (x->graph_mode) {
       cudaGraphConditionalHandle h;
       if ((rc = new_handle(x, 1, &h))) return rc;
-      return add_loop(x, h, [&]() -> int {
+      rc = add_loop(x, h, [&]() -> int {
         int r;
         if ((r = gs_sweep()) || (r = gs_sweep())) return r;
         CK(launch_ctl_sweeps(x->pw.ds, limit, h, 1, x->st));
         return HYDRO_OK;
       });
-    }
-    int queued = 0;
-    for (;;) {
-      int n = std::min(kSweepChunk, limit - queued);
-      for (int s = 0; s < n; ++s)
-        if ((rc = gs_sweep())) return rc;
-      queued += n;
-      rc = sync_scalars(x);
       if (rc) return rc;
-      if (x->hds->flag[FL_MOM_DONE] || queued >= limit) break;
+    } else {
+      int queued = 0;
+      for (;;) {
+        int n = std::min(kSweepChunk, limit - queued);
+        for (int s = 0; s < n; ++s)
+          if ((rc = gs_sweep())) return rc;
+        queued += n;
+        rc = sync_scalars(x);
+        if (rc) return rc;
+        if (x->hds->flag[FL_MOM_DONE] || queued >= limit) break;
+      }
+      x->vel_sweeps += x->hds->flag[FL_MOM_SWEEPS];
     }
-    x->vel_sweeps += x->hds->flag[FL_MOM_SWEEPS];
+    if (f32) {
+      // the FP32 corrections are color-blocked: cell order in du32[1] for the
+      // Rhie-Chow and correction kernels
+      CK(launch_unsplit3(x->m, fp3(x->du32[0]), fp3(x->du32[1]), x->st));
+      x->du_cur = 1;
+    }
     return HYDRO_OK;
   }
   auto sweep = [&](int k) -> int {

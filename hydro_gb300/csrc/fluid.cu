@@ -335,8 +335,10 @@ __global__ void __launch_bounds__(NT) k_mom_sweep(Mesh m, double omega, double t
 // Red-black Gauss-Seidel half-sweep (see launch_mom_rbgs).  Thread (x, y)
 // owns the color cell of the pair (2x, 2x+1) in row (j, k).  The first sweep
 // starts from du = 0: its red half reads no neighbours and the own old value
-// of both halves is 0.
-template <int DIM, bool PER, class T, bool SPLIT>
+// of both halves is 0.  SDU: du itself is stored color-blocked like the rows
+// (a neighbour nb of the other color at (1 - color) * nc/2 + nb/2), so that a
+// warp's neighbour loads are unit-stride.
+template <int DIM, bool PER, class T, bool SPLIT, bool SDU>
 __global__ void __launch_bounds__(NT) k_mom_rbgs(Mesh m, T omega, double tol, RT<T, 7> cf,
                                                  RT<T, 3> rs, WT<T, 3> du, int color, int limit,
                                                  double* partials, DevScalars* ds, int kch) {
@@ -365,15 +367,18 @@ __global__ void __launch_bounds__(NT) k_mom_rbgs(Mesh m, T omega, double tol, RT
       for (int q = 0; q < 2 * DIM; ++q) a[q] = cf.a[1 + q][ci];
       constexpr bool kPerT = PER;
       const bool rd = !(first && color == 0);
+      const long long own = SDU ? ci : X.c;
+      const long long obase = SDU ? (1 - color) * half : 0;
+      auto nbi = [&](long long nb) { return SDU ? obase + (nb >> 1) : nb; };
 #pragma unroll
       for (int n = 0; n < DIM; ++n) {
         r[n] = rs.a[n][ci];
-        cur[n] = first ? T(0) : du.a[n][X.c];
+        cur[n] = first ? T(0) : du.a[n][own];
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
           long long s = cell_stride(m, d);
-          nb[n][2 * d] = rd && HAS_LO(d) ? du.a[n][NB_LO(d, s)] : T(0);
-          nb[n][2 * d + 1] = rd && HAS_HI(d) ? du.a[n][NB_HI(d, s)] : T(0);
+          nb[n][2 * d] = rd && HAS_LO(d) ? du.a[n][nbi(NB_LO(d, s))] : T(0);
+          nb[n][2 * d + 1] = rd && HAS_HI(d) ? du.a[n][nbi(NB_HI(d, s))] : T(0);
         }
       }
 #pragma unroll
@@ -384,7 +389,7 @@ __global__ void __launch_bounds__(NT) k_mom_rbgs(Mesh m, T omega, double tol, RT
         const T value = -(r[n] + sum) * iaP;
         const T corr = value - cur[n];
         dmax = fmax(dmax, fabs(corr));
-        du.a[n][X.c] = cur[n] + corr * omega;
+        du.a[n][own] = cur[n] + corr * omega;
       }
     }
   }
@@ -1207,6 +1212,42 @@ cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st) {
 }
 
 namespace {
+// Color-blocked (index color * nc/2 + c/2, nx even) to cell order: thread
+// (x, y) takes the pair (2x, 2x+1) of row (j, k), whose first cell has color
+// (j + k) % 2; both cells share the blocked index c/2.
+template <int DIM>
+__global__ void __launch_bounds__(NT) k_unsplit3(Mesh m, FP<3> in, FP<3> out, int kch) {
+  const int ih = blockIdx.x * BX + threadIdx.x;
+  const int j = blockIdx.y * BY + threadIdx.y;
+  const int nz = DIM == 3 ? m.n[2] : 1;
+  const int k0 = blockIdx.z * kch, k1 = min(k0 + kch, nz);
+  if (2 * ih >= m.n[0] || j >= m.n[1]) return;
+  const long long half = m.nc / 2;
+  for (int k = k0; k < k1; ++k) {
+    const long long c = cell_id(m, 2 * ih, j, k);
+    const long long h = c >> 1;
+    const int a = (j + k) & 1;
+#pragma unroll
+    for (int n = 0; n < DIM; ++n) {
+      const float e = in.a[n][a * half + h], o = in.a[n][(1 - a) * half + h];
+      *reinterpret_cast<float2*>(out.a[n] + c) = make_float2(e, o);
+    }
+  }
+}
+}  // namespace
+
+cudaError_t launch_unsplit3(const Mesh& m, FP<3> in, FP<3> out, cudaStream_t st) {
+  if (m.n[0] % 2) return cudaErrorInvalidValue;
+  Mesh h = m;
+  h.n[0] = m.n[0] / 2;
+  Launch L = cell_launch(h);
+  if (m.dim == 3) k_unsplit3<3><<<L.grid, L.block, 0, st>>>(m, in, out, L.kch);
+  else k_unsplit3<2><<<L.grid, L.block, 0, st>>>(m, in, out, L.kch);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+namespace {
 // Grid of a red-black half-sweep: one thread per cell pair along x, sized
 // in whole waves over the half-width mesh.
 Launch rb_launch(const Mesh& m, const void* kernel) {
@@ -1222,8 +1263,8 @@ cudaError_t launch_mom_rbgs(const Mesh& m, double omega, double tol, CP<7> coef,
   const bool p = any_periodic(m);
 #define RBGS64(D, P, S)                                                                       \
   do {                                                                                        \
-    Launch L = rb_launch(m, (const void*)k_mom_rbgs<D, P, double, S>);                        \
-    k_mom_rbgs<D, P, double, S><<<L.grid, L.block, 0, st>>>(m, omega, tol, coef, res, du,     \
+    Launch L = rb_launch(m, (const void*)k_mom_rbgs<D, P, double, S, false>);                        \
+    k_mom_rbgs<D, P, double, S, false><<<L.grid, L.block, 0, st>>>(m, omega, tol, coef, res, du,     \
                                                             color, limit, partials, ds, L.kch); \
   } while (0)
   if (m.dim == 3) {
@@ -1249,9 +1290,10 @@ cudaError_t launch_mom_rbgs32(const Mesh& m, double omega, double tol, FP<10> c,
   const float om = (float)omega;
 #define RBGS32(D, P)                                                                        \
   do {                                                                                      \
-    Launch L = rb_launch(m, (const void*)k_mom_rbgs<D, P, float, true>);                    \
-    k_mom_rbgs<D, P, float, true><<<L.grid, L.block, 0, st>>>(m, om, tol, cf, rs, du, color, \
-                                                              limit, partials, ds, L.kch);  \
+    Launch L = rb_launch(m, (const void*)k_mom_rbgs<D, P, float, true, true>);              \
+    k_mom_rbgs<D, P, float, true, true><<<L.grid, L.block, 0, st>>>(m, om, tol, cf, rs, du,  \
+                                                                    color, limit, partials, \
+                                                                    ds, L.kch);             \
   } while (0)
   if (m.dim == 3) {
     if (p) RBGS32(3, true); else RBGS32(3, false);

@@ -150,10 +150,13 @@ cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st);
 // rules of launch_mom_sweep.  split: the coefficients and residuals are
 // stored color-blocked (index color * nc/2 + c/2; nx even), the layout the
 // assembly writes for this solver (FP32 always, FP64 without SIMPLER);
-// launch_mom_rbgs32 is always split.
+// launch_mom_rbgs32 is always split, and keeps du color-blocked too.
 cudaError_t launch_mom_rbgs(const Mesh& m, double omega, double tol, CP<7> coef, C3 res, W3 du,
                             int color, int split, int limit, double* partials, DevScalars* ds,
                             cudaStream_t st);
+// Color-blocked FP32 vectors (the momentum corrections of launch_mom_rbgs32)
+// back to cell order; nx even.
+cudaError_t launch_unsplit3(const Mesh& m, FP<3> in, FP<3> out, cudaStream_t st);
 cudaError_t launch_mom_rbgs32(const Mesh& m, double omega, double tol, FP<10> c, FP<3> du,
                               int color, int limit, double* partials, DevScalars* ds,
                               cudaStream_t st);
