@@ -60,9 +60,9 @@ ALG_BYTES_PER_CELL_FP32 = {
     "cg_update": 4 * (4 + 2),              # read x, r, p, Ap; write x, r
     "mom_sweep": 4 * (10 + 3 + 3),         # read coef[7]+res[3], du[3]; write du[3]
     # one V-cycle: finest level 4 red-black sweeps (x r/w, b, kf[3], 1/diag)
-    # + restriction (x, b, kf[3], diag) + prolongation (x r/w), coarser
-    # levels 1/8 per level
-    "mg_vcycle": int(round(4 * (4 * 7 + 6 + 2) * 8 / 7)),
+    # + restriction of the red residuals (x, kf[3]; b and diag of the red
+    # half) + prolongation (x r/w), coarser levels 1/8 per level
+    "mg_vcycle": int(round(4 * (4 * 7 + 5 + 2) * 8 / 7)),
 }
 
 

@@ -701,7 +701,13 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
         if (rc) return rc;
         if (x->hds->flag[FL_PCG_DONE] || queued >= w.limit) break;
       }
-      if (mgcg) x->prof.uncount(HYDRO_PROF_MG_VCYCLE, queued - x->hds->flag[FL_PCG_ITERS]);
+      if (mgcg) {
+        // brackets: the start and `queued` iterations; V-cycles that ran: the
+        // start and every iteration but a converging last one
+        const int it = x->hds->flag[FL_PCG_ITERS];
+        x->prof.uncount(HYDRO_PROF_MG_VCYCLE,
+                        1 + queued - (x->hds->flag[FL_PCG_DONE] && it > 0 ? it : it + 1));
+      }
       total += x->hds->flag[FL_PCG_ITERS];
       CK(f32_accumulate(m, x->pc, w, x->st));
     }
@@ -1035,6 +1041,7 @@ int hydro_gpu_destroy(hydro_ctx* x) {
   if (!x) return HYDRO_OK;
   if (x->st) cudaStreamSynchronize(x->st);
   if (x->sg.exec) cudaGraphExecDestroy(x->sg.exec);
+  mg_release(x->mg);
   for (auto& cs : x->cap_streams)
     if (cs) cudaStreamDestroy(cs);
   if (x->arena.base) cudaFree(x->arena.base);

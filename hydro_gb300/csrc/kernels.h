@@ -334,6 +334,15 @@ struct MgWork {
   // cells and is not the top level; null otherwise
   float* cinv;
   bool cdense;
+  int smem_cinv_off;  // offset (floats) of its copy in the CTA's shared memory
+  // host-driven steps replay the launches of one V-cycle as a CUDA graph,
+  // instantiated for these vectors (null until the first V-cycle)
+  cudaGraphExec_t vc_exec;
+  const float* vc_r;
+  float* vc_z;
+  long long vc_pin;
+  DevScalars* vc_ds;
+  int vc_kernels;
 };
 Mesh mg_coarse_mesh(const Mesh& fine);
 int mg_levels_for(const Mesh& m);
@@ -342,8 +351,12 @@ int mg_levels_for(const Mesh& m);
 cudaError_t mg_prepare(MgWork& mg);
 // Coarse couplings and diagonals from level 0 (w.kf32 / dg32 / idg32).
 cudaError_t mg_setup(MgWork& mg, PcgWork& w, cudaStream_t st);
+// z = M^-1 r.  Inside a stream capture the launches join the capture;
+// otherwise they are replayed as one graph (kernels back to back without a
+// host launch between them).
 cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevScalars* ds,
                       cudaStream_t st);
+void mg_release(MgWork& mg);
 // Inner solve of the mixed path with the V-cycle as preconditioner:
 // init from the FP64 residual in w.r, chunks of iterations into w.x32.
 cudaError_t mgcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, MgWork& mg,

@@ -204,7 +204,10 @@ __global__ void k_mg_diag(Mesh m, const float* kf, float* dg, float* idg, int kc
 }
 
 // Coarse right-hand side = sum over the 2^DIM children of the fine residual
-// b - A x; also clears the coarse correction.
+// b - A x; also clears the coarse correction.  The pre-smoothing ends with
+// a black half-sweep, which leaves the residual of every black cell zero
+// (up to rounding), so only the red children are summed: a coarse cell's
+// children (2I + ci, 2J + cj, 2K + ck) are red when ci + cj + ck is even.
 template <int DIM, bool PER>
 __global__ void k_mg_restrict(Mesh fm, Mesh cm, const float* kf, const float* dg, const float* b,
                               const float* x, float* cb, float* cx, long long pin,
@@ -218,6 +221,7 @@ __global__ void k_mg_restrict(Mesh fm, Mesh cm, const float* kf, const float* dg
     for (int cj = 0; cj < 2; ++cj)
 #pragma unroll
       for (int ci = 0; ci < 2; ++ci) {
+        if ((ci + cj + ck) & 1) continue;
         int id[3] = {2 * X.i[0] + ci, 2 * X.i[1] + cj, DIM == 3 ? 2 * X.i[2] + ck : 0};
         long long c = cell_id(fm, id[0], id[1], id[2]);
         float r;
@@ -258,6 +262,7 @@ struct MgBlock {
   int nl;  // levels in the CTA, top first
   int nsweep, coarse_sweeps;
   const float* cinv;  // dense inverse of the coarsest level, or null (sweeps)
+  int oc;             // its place in shared memory
   long long pin;  // pinned cell of the top level (-1: none)
   Mesh m[kMgMaxLevels];
   const float* kf[kMgMaxLevels];
@@ -358,6 +363,10 @@ __global__ void __launch_bounds__(kBlkThreads)
     for (int q = tid; q < nc; q += nt) sm[B.oi[l] + q] = B.idg[l][q];
   }
   for (int q = tid; q < (int)B.m[0].nc; q += nt) sm[B.ob[0] + q] = btop[q];
+  if (B.cinv) {
+    const int n = (int)B.m[B.nl - 1].nc;
+    for (int q = tid; q < n * n; q += nt) sm[B.oc + q] = B.cinv[q];
+  }
   __syncthreads();
   const int ns = B.nsweep;
   for (int l = 0; l + 1 < B.nl; ++l) {
@@ -398,11 +407,15 @@ __global__ void __launch_bounds__(kBlkThreads)
     }
     if (B.cinv && lp < 0) {
       // exact coarsest solve: x = P b, P the symmetric inverse of the level's
-      // operator completed by the constant mode (b has zero mean)
-      for (int c = tid; c < n; c += nt) {
+      // operator completed by the constant mode (b has zero mean); one warp
+      // per row of P (n <= 64)
+      const float* P = sm + B.oc;
+      const int lane = tid & 31;
+      for (int c = tid >> 5; c < n; c += nt >> 5) {
         float acc = 0.f;
-        for (int q = 0; q < n; ++q) acc = fmaf(B.cinv[c * n + q], b[q], acc);
-        x[c] = acc;
+        for (int q = lane; q < n; q += 32) acc = fmaf(P[c * n + q], b[q], acc);
+        acc = warp_sum(acc);
+        if (lane == 0) x[c] = acc;
       }
       __syncthreads();
     } else {
@@ -701,6 +714,12 @@ cudaError_t mg_prepare(MgWork& mg) {
   // level of the in-CTA cycle (a coarse level: singular, unpinned)
   mg.cdense = mg.cinv && mg.nlev >= 2 && mg.top < mg.nlev && mg.top < mg.nlev - 1 &&
               mg.lev[mg.nlev - 1].m.nc <= kMgCoarseTarget;
+  if (mg.cdense) {
+    // the dense inverse joins the CTA's shared memory after the levels
+    const long long n = mg.lev[mg.nlev - 1].m.nc;
+    mg.smem_cinv_off = mg.smem_bytes / (int)sizeof(float);
+    mg.smem_bytes += (int)(n * n * sizeof(float));
+  }
   if (mg.nlev > 0 && mg.top < mg.nlev) {
     if (mg.smem_bytes > 227 * 1024) return cudaErrorInvalidValue;
     const bool per = any_periodic(mg.lev[0].m);
@@ -714,11 +733,12 @@ cudaError_t mg_prepare(MgWork& mg) {
   return cudaSuccess;
 }
 
+namespace {
 // z = M^-1 r: one V-cycle with `nsweep` (red, black) sweeps before and
 // (black, red) sweeps after each coarse correction.  Levels above `top`
 // are grid launches; `top` and below run in one CTA.
-cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevScalars* ds,
-                      cudaStream_t st) {
+cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin,
+                             DevScalars* ds, cudaStream_t st) {
   int dim = mg.lev[0].m.dim;
   const bool per = any_periodic(mg.lev[0].m);
   mg.lev[0].b = const_cast<float*>(r);
@@ -743,6 +763,7 @@ cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevSc
     B.nsweep = ns;
     B.coarse_sweeps = mg.coarse_sweeps;
     B.cinv = mg.cdense ? mg.cinv : nullptr;
+    B.oc = mg.smem_cinv_off;
     B.pin = mg.top == 0 ? pin : -1;
     int off = 0;
     for (int q = 0; q < B.nl; ++q) {
@@ -796,6 +817,49 @@ cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevSc
   return cudaGetLastError();
 }
 
+}  // namespace
+
+cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevScalars* ds,
+                      cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(st, &cs);
+  if (e != cudaSuccess) return e;
+  if (cs != cudaStreamCaptureStatusNone) return mg_vcycle_launch(mg, r, z, pin, ds, st);
+  if (!mg.vc_exec || mg.vc_r != r || mg.vc_z != z || mg.vc_pin != pin || mg.vc_ds != ds) {
+    mg_release(mg);
+    cudaGraph_t g = nullptr;
+    if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed)) != cudaSuccess) return e;
+    cudaError_t el = mg_vcycle_launch(mg, r, z, pin, ds, st);
+    e = cudaStreamEndCapture(st, &g);
+    if (el != cudaSuccess || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return el != cudaSuccess ? el : e;
+    }
+    size_t nodes = 0;
+    cudaGraphGetNodes(g, nullptr, &nodes);
+    e = cudaGraphInstantiate(&mg.vc_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      mg.vc_exec = nullptr;
+      return e;
+    }
+    // the capture counted its kernels; each replay counts them
+    mg.vc_kernels = (int)nodes;
+    count_launches(-mg.vc_kernels);
+    mg.vc_r = r;
+    mg.vc_z = z;
+    mg.vc_pin = pin;
+    mg.vc_ds = ds;
+  }
+  count_launches(mg.vc_kernels);
+  return cudaGraphLaunch(mg.vc_exec, st);
+}
+
+void mg_release(MgWork& mg) {
+  if (mg.vc_exec) cudaGraphExecDestroy(mg.vc_exec);
+  mg.vc_exec = nullptr;
+}
+
 cudaError_t mgcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, MgWork& mg,
                       cudaStream_t st) {
   int fb = flat_blocks_mg(m.nc);
@@ -807,8 +871,9 @@ cudaError_t mgcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, MgW
                                            w.partials, w.ds);
   count_launches(1);
   if (w.prof) w.prof->begin(HYDRO_PROF_MG_VCYCLE, st);
-  mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st);
+  cudaError_t e = mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st);
   if (w.prof) w.prof->end(HYDRO_PROF_MG_VCYCLE, st);
+  if (e != cudaSuccess) return e;
   k_mgcg_dot<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.r32, w.z32, 1, w.partials, w.ds);
   count_launches(1);
   return cudaGetLastError();
@@ -829,8 +894,9 @@ cudaError_t mgcg_iterate(const Mesh& m, int chunk, PcgWork& w, MgWork& mg, cudaS
                                                w.ds);
     if (w.prof) w.prof->end(HYDRO_PROF_CG_UPDATE, st);
     if (w.prof) w.prof->begin(HYDRO_PROF_MG_VCYCLE, st);
-    mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st);
+    e = mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st);
     if (w.prof) w.prof->end(HYDRO_PROF_MG_VCYCLE, st);
+    if (e != cudaSuccess) return e;
     k_mgcg_dot<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.r32, w.z32, 0, w.partials, w.ds);
     count_launches(2);
     w.p32_parity ^= 1;
