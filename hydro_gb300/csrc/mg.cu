@@ -208,10 +208,12 @@ __global__ void k_mg_diag(Mesh m, const float* kf, float* dg, float* idg, int kc
 // a black half-sweep, which leaves the residual of every black cell zero
 // (up to rounding), so only the red children are summed: a coarse cell's
 // children (2I + ci, 2J + cj, 2K + ck) are red when ci + cj + ck is even.
+// With cidg the coarse level's first half-sweep (red, from x = 0: x = b /
+// diag) is done here as well; without it the coarse iterate is cleared.
 template <int DIM, bool PER>
 __global__ void k_mg_restrict(Mesh fm, Mesh cm, const float* kf, const float* dg, const float* b,
-                              const float* x, float* cb, float* cx, long long pin,
-                              const DevScalars* ds, int kch) {
+                              const float* x, float* cb, float* cx, const float* cidg,
+                              long long pin, const DevScalars* ds, int kch) {
   if (ds->flag[FL_PCG_DONE]) return;
   CELL_LOOP_BEGIN(cm, kch)
   float sum = 0.f;
@@ -244,7 +246,7 @@ __global__ void k_mg_restrict(Mesh fm, Mesh cm, const float* kf, const float* dg
         sum += r;
       }
   cb[X.c] = sum;
-  cx[X.c] = 0.f;
+  cx[X.c] = cidg && ((X.i[0] + X.i[1] + X.i[2]) & 1) == 0 ? sum * cidg[X.c] : 0.f;
   CELL_LOOP_END
 }
 
@@ -750,12 +752,16 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
     long long lp = l == 0 ? pin : -1;
     Launch H = half_launch(f.m);
     for (int s = 0; s < ns; ++s) {
-      MG_LAUNCH_P(k_mg_smooth, H, per, f.m, f.kf, f.idg, f.b, f.x, 0, s == 0, lp, nullptr, 0, 0, ds);
+      // below the finest level the first (red, from zero) half-sweep was
+      // done by the restriction
+      if (s > 0 || l == 0)
+        MG_LAUNCH_P(k_mg_smooth, H, per, f.m, f.kf, f.idg, f.b, f.x, 0, s == 0, lp, nullptr, 0, 0, ds);
       MG_LAUNCH_P(k_mg_smooth, H, per, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, nullptr, 0, 0, ds);
     }
     MgLevel& c = mg.lev[l + 1];
     Launch L = cell_launch(c.m);
-    MG_LAUNCH_P(k_mg_restrict, L, per, f.m, c.m, f.kf, f.dg, f.b, f.x, c.b, c.x, lp, ds);
+    const float* cidg = l + 1 < top && ns > 0 ? c.idg : nullptr;
+    MG_LAUNCH_P(k_mg_restrict, L, per, f.m, c.m, f.kf, f.dg, f.b, f.x, c.b, c.x, cidg, lp, ds);
   }
   if (mg.top < mg.nlev) {
     MgBlock B;
