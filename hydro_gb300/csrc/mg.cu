@@ -36,7 +36,7 @@ namespace {
 // first post-smoothing half-sweep (the cells of the other color are
 // overwritten by the next half-sweep, which never reads their old value).
 template <int DIM, bool PER>
-__global__ void k_mg_smooth(Mesh m, const float* kf, const float* idg, const float* b, float* x,
+__global__ void __launch_bounds__(NT, PER ? 6 : 8) k_mg_smooth(Mesh m, const float* kf, const float* idg, const float* b, float* x,
                             int color, int zero, long long pin, const float* cx, int cnx,
                             int cny, const DevScalars* ds, int kch) {
   if (ds->flag[FL_PCG_DONE]) return;
@@ -604,11 +604,15 @@ int flat_blocks_mg(long long n) {
   return (int)b;
 }
 
+// Grid of a red-black half-sweep: one thread per cell pair along x, sized
+// in whole waves over the half-width mesh.
 Launch half_launch(const Mesh& m) {
-  Launch L = cell_launch(m);
-  int halfx = (m.n[0] + 1) / 2;
-  L.grid.x = (halfx + BX - 1) / BX;
-  return L;
+  const bool per = any_periodic(m);
+  const void* k = m.dim == 3 ? (per ? (const void*)k_mg_smooth<3, true> : (const void*)k_mg_smooth<3, false>)
+                             : (per ? (const void*)k_mg_smooth<2, true> : (const void*)k_mg_smooth<2, false>);
+  Mesh h = m;
+  h.n[0] = (m.n[0] + 1) / 2;
+  return cell_launch_waves(h, resident_ctas(k));
 }
 
 }  // namespace
