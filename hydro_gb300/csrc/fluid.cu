@@ -409,6 +409,91 @@ __global__ void __launch_bounds__(NT) k_mom_rbgs(Mesh m, T omega, double tol, RT
   }
 }
 
+// k_mom_rbgs for the FP32 color-blocked rows and corrections of a block
+// without periodic directions or excluded cells, in 32-bit index arithmetic
+// (nc < 2^31): with n0 even, the blocked index of cell c is c/2 within its
+// color's half, and its neighbours across y and z sit n0/2 and n0 n1/2
+// blocked entries away.  Same loads, order of the sum and results as the
+// general form.
+template <int DIM>
+__global__ void __launch_bounds__(NT) k_mom_rbgs_f32(Mesh m, float omega, double tol,
+                                                     RT<float, 7> cf, RT<float, 3> rs, FP<3> du,
+                                                     int color, int limit, double* partials,
+                                                     DevScalars* ds, int kch) {
+  if (ds->flag[FL_MOM_DONE] || ds->flag[FL_MOM_SWEEPS] >= limit) return;
+  const bool first = ds->flag[FL_MOM_SWEEPS] == 0;
+  const int ih = blockIdx.x * BX + threadIdx.x;
+  const int j = blockIdx.y * BY + threadIdx.y;
+  const int n0 = m.n[0], n1 = m.n[1];
+  const int nz = DIM == 3 ? m.n[2] : 1;
+  const int k0 = blockIdx.z * kch, k1 = min(k0 + kch, nz);
+  const int half = (int)(m.nc / 2);
+  const int hy = n0 / 2, hz = n0 / 2 * n1;
+  const int ob = (1 - color) * half;
+  const bool rd = !(first && color == 0);
+  float dmax = 0.f;
+  if (j < n1) {
+    for (int k = k0; k < k1; ++k) {
+      const int i = 2 * ih + ((j + k + color) & 1);
+      if (i >= n0) continue;
+      const int c = i + n0 * (j + n1 * k);
+      const int h = c >> 1;
+      const int ci = color * half + h;
+      const float iaP = cf.a[0][ci];
+      float a[2 * DIM], r[DIM], cur[DIM], nb[DIM][2 * DIM];
+#pragma unroll
+      for (int q = 0; q < 2 * DIM; ++q) a[q] = cf.a[1 + q][ci];
+      bool in[2 * DIM];
+      int nbi[2 * DIM];
+      in[0] = rd && i > 0;
+      nbi[0] = ob + ((c - 1) >> 1);
+      in[1] = rd && i < n0 - 1;
+      nbi[1] = ob + ((c + 1) >> 1);
+      in[2] = rd && j > 0;
+      nbi[2] = ob + h - hy;
+      in[3] = rd && j < n1 - 1;
+      nbi[3] = ob + h + hy;
+      if (DIM == 3) {
+        in[2 * DIM - 2] = rd && k > 0;
+        nbi[2 * DIM - 2] = ob + h - hz;
+        in[2 * DIM - 1] = rd && k < nz - 1;
+        nbi[2 * DIM - 1] = ob + h + hz;
+      }
+#pragma unroll
+      for (int n = 0; n < DIM; ++n) {
+        r[n] = rs.a[n][ci];
+        cur[n] = first ? 0.f : du.a[n][ci];
+#pragma unroll
+        for (int q = 0; q < 2 * DIM; ++q) nb[n][q] = in[q] ? du.a[n][nbi[q]] : 0.f;
+      }
+#pragma unroll
+      for (int n = 0; n < DIM; ++n) {
+        float sum = 0.f;
+#pragma unroll
+        for (int q = 0; q < 2 * DIM; ++q) sum += a[q] * nb[n][q];
+        const float value = -(r[n] + sum) * iaP;
+        const float corr = value - cur[n];
+        dmax = fmaxf(dmax, fabsf(corr));
+        du.a[n][ci] = cur[n] + corr * omega;
+      }
+    }
+  }
+  double v[1] = {(double)dmax};
+  __shared__ double out[1];
+  if (grid_reduce<RED_MAX, 1>(v, partials, &ds->ticket[color == 0 ? TK_MOM_RED : TK_MOM], out)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      if (color == 0) {
+        ds->red[RS_MOM_DIFF_RED] = out[0];
+      } else {
+        const double mx = fmax(out[0], ds->red[RS_MOM_DIFF_RED]);
+        ds->red[RS_MOM_DIFF] = mx;
+        ds->flag[FL_MOM_SWEEPS] += 1;
+        if (!(mx > tol)) ds->flag[FL_MOM_DONE] = 1;
+      }
+    }
+  }
+}
+
 // The same Jacobi sweep on the FP32 coefficients and residuals of the
 // mixed-precision path (o32 of k_mom_assemble: inverse diagonal, 2*DIM
 // off-diagonals, DIM residuals): FP32 arithmetic, FP64 only for the max.
@@ -1295,7 +1380,16 @@ cudaError_t launch_mom_rbgs32(const Mesh& m, double omega, double tol, FP<10> c,
                                                                     color, limit, partials, \
                                                                     ds, L.kch);             \
   } while (0)
-  if (m.dim == 3) {
+  if (!p && m.nc < (1LL << 31)) {
+#define RBGSF(D)                                                                            \
+  do {                                                                                      \
+    Launch L = rb_launch(m, (const void*)k_mom_rbgs_f32<D>);                                \
+    k_mom_rbgs_f32<D><<<L.grid, L.block, 0, st>>>(m, om, tol, cf, rs, du, color, limit,     \
+                                                  partials, ds, L.kch);                     \
+  } while (0)
+    if (m.dim == 3) RBGSF(3); else RBGSF(2);
+#undef RBGSF
+  } else if (m.dim == 3) {
     if (p) RBGS32(3, true); else RBGS32(3, false);
   } else {
     if (p) RBGS32(2, true); else RBGS32(2, false);
