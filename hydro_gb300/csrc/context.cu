@@ -1025,6 +1025,7 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
   x->fc.sources = 0;
   for (int i = 0; i < HYDRO_MAXPH; ++i) {
     x->pp.dens[i] = desc->density[i];
+    x->pp.idens[i] = 1. / desc->density[i];
     x->pp.visc[i] = desc->viscosity[i];
   }
   for (int k = 0; k < 3; ++k) {

@@ -787,18 +787,28 @@ __global__ void k_add(long long n, double* a, const double* b) {
 // --------------------------------------------------------- auto time step --
 // FluidSimple::GetAutoTimeStep (fluid.hpp:1191-1206): min over faces with
 // F != 0 of |V/F|, 1e10 when there is none.
+// min over faces with F != 0 of V / |F| (at most 1e10), formed as
+// V / max |F|: correctly rounded division is monotonic, so this is the same
+// number, with one division instead of one per face.  The maximum runs on
+// the bit patterns of |F| (ordered like the values for non-negative
+// doubles; NaNs skipped), which keeps the reduction off the FP64 pipe.
 __global__ void __launch_bounds__(NT) k_auto_dt(long long nf, double V, const double* F,
                                                 double* partials, DevScalars* ds) {
-  double dmin = 1e10;
+  constexpr unsigned long long kAbs = 0x7fffffffffffffffULL, kInf = 0x7ff0000000000000ULL;
+  unsigned long long bmax = 0;
   long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
   for (long long f = blockIdx.x * (long long)NT + tid; f < nf; f += (long long)gridDim.x * NT) {
-    double fl = F[f];
-    if (fl != 0.) dmin = fmin(dmin, fabs(V / fl));
+    const unsigned long long b = (unsigned long long)__double_as_longlong(F[f]) & kAbs;
+    if (b <= kInf && b > bmax) bmax = b;
   }
-  double v[1] = {dmin};
-  __shared__ double out[1];
-  if (grid_reduce<RED_MIN, 1>(v, partials, &ds->ticket[TK_DT], out)) {
-    if (tid == 0) ds->red[RS_AUTO_DT] = out[0];
+  unsigned long long v[1] = {bmax};
+  __shared__ unsigned long long out[1];
+  if (grid_reduce<RED_MAX, 1>(v, reinterpret_cast<unsigned long long*>(partials),
+                              &ds->ticket[TK_DT], out)) {
+    if (tid == 0) {
+      const double fmax_abs = __longlong_as_double((long long)out[0]);
+      ds->red[RS_AUTO_DT] = fmax_abs > 0. ? fmin(1e10, V / fmax_abs) : 1e10;
+    }
   }
 }
 
@@ -830,15 +840,17 @@ __global__ void k_props(Mesh m, int nph, PhaseProps pp, CP<HYDRO_MAXPH> q,
 #pragma unroll
   for (int i = 0; i < HYDRO_MAXPH; ++i) {
     if (i < nph) {
-      a[i] = q.a[i][X.c] / pp.dens[i];
+      a[i] = q.a[i][X.c] * pp.idens[i];
       sum += a[i];
     }
   }
   double rr = 0., mm = 0.;
+  // one FP64 division per cell (GB300's FP64 rate makes each one count)
+  const double isum = 1. / sum;
 #pragma unroll
   for (int i = 0; i < HYDRO_MAXPH; ++i) {
     if (i < nph) {
-      a[i] /= sum;
+      a[i] *= isum;
       alpha.a[i][X.c] = a[i];
       rr += pp.dens[i] * a[i];
     }
@@ -871,7 +883,7 @@ __global__ void k_smooth(Mesh m, const double* in, double* out, int kch) {
     sum += HAS_LO(d) ? avg(in[NB_LO(d, s)], vc) : vc;
     sum += HAS_HI(d) ? avg(vc, in[NB_HI(d, s)]) : vc;
   }
-  out[X.c] = sum / (2. * DIM);
+  out[X.c] = sum * (1. / (2. * DIM));  // a product: an FP64 division costs ~20 FP64 issues
   CELL_LOOP_END
 }
 

@@ -188,7 +188,7 @@ cudaError_t launch_nan_count(long long n, const double* a, double* partials, Dev
 
 // ----------------------------------------------------------- properties --
 struct PhaseProps {
-  double dens[HYDRO_MAXPH], visc[HYDRO_MAXPH], grav[3], f0[3];
+  double dens[HYDRO_MAXPH], idens[HYDRO_MAXPH], visc[HYDRO_MAXPH], grav[3], f0[3];
 };
 cudaError_t launch_props(const Mesh& m, int nph, const PhaseProps& pp,
                          CP<HYDRO_MAXPH> q, WP<HYDRO_MAXPH> alpha, double* rho_raw,

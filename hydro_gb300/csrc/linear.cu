@@ -69,12 +69,12 @@ __global__ void k_diag(Mesh m, const double* kf, double shift, long long pin, do
     }
   }
   if (X.c == pin || EXCLUDED()) s = 1.;  // identity rows
-  const double is = 1. / s;
   dg[X.c] = s;
-  idg[X.c] = is;
+  if (idg) idg[X.c] = 1. / s;  // FP64 Jacobi-PCG only
   if (dg32) {
-    dg32[X.c] = (float)s;
-    idg32[X.c] = (float)is;
+    const float s32 = (float)s;
+    dg32[X.c] = s32;
+    idg32[X.c] = 1.f / s32;
   }
   CELL_LOOP_END
 }
@@ -242,7 +242,8 @@ int flat_blocks_l(long long n) {
 cudaError_t pcg_prepare(const Mesh& m, const double* kf, double shift, PcgWork& w, int fp32,
                         cudaStream_t st) {
   Launch L = cell_launch(m);
-  CELL_LAUNCH_P(m, L, st, k_diag, m, kf, shift, w.pin, w.dg, w.idg, fp32 ? w.dg32 : nullptr,
+  CELL_LAUNCH_P(m, L, st, k_diag, m, kf, shift, w.pin, w.dg, fp32 ? nullptr : w.idg,
+                fp32 ? w.dg32 : nullptr,
                 fp32 ? w.idg32 : nullptr, fp32 ? w.kf32 : nullptr);
   count_launches(1);
   return cudaGetLastError();
