@@ -64,7 +64,7 @@ enum {
   RS_PCG_ALPHA = 6, RS_PCG_BETA = 7,
   RS_INDICATOR = 8,      // SIMPLE convergence indicator
   RS_AUTO_DT = 9,
-  RS_MEAN = 10,          // sum used for mean projection
+  RS_MEAN = 10,          // mean of the right-hand side (singular systems)
   RS_PCG_TOL2 = 11,      // tol^2 * ||f||^2
   RS_IR_RR = 12,         // refinement residual norm^2
   RS_NAN = 13,
@@ -294,7 +294,7 @@ cudaError_t pcg_init(const Mesh& m, const double* kf, const double* f, double* x
                      double tol, int singular, PcgWork& w, cudaStream_t st);
 cudaError_t pcg_iterate(const Mesh& m, const double* kf, double* x, int chunk, PcgWork& w,
                         cudaStream_t st);
-// sum(f) into ds->red[RS_MEAN]; x -= mean(x).
+// mean(f) into ds->red[RS_MEAN]; x -= mean(x).
 cudaError_t mean_sum(const Mesh& m, const double* f, PcgWork& w, cudaStream_t st);
 cudaError_t sub_mean(const Mesh& m, double* x, PcgWork& w, cudaStream_t st);
 // Mixed precision: FP64 residual r = f' - A x (||r||^2 in ds->red[RS_IR_RR]),

@@ -79,10 +79,12 @@ __global__ void k_diag(Mesh m, const double* kf, double shift, long long pin, do
   CELL_LOOP_END
 }
 
-// sum of a vector (for the mean projection of singular systems).
+// mean of a vector over the cells that are not excluded (nfluid of them),
+// for the mean projection of singular systems: the sum, divided once.
 template <class T>
-__global__ void __launch_bounds__(NT) k_sum(long long n, const T* a, const unsigned char* ex,
-                                            double* partials, double* out, unsigned* ticket) {
+__global__ void __launch_bounds__(NT) k_mean(long long n, long long nfluid, const T* a,
+                                             const unsigned char* ex, double* partials,
+                                             double* out, unsigned* ticket) {
   double s = 0.;
   long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
   for (long long i = blockIdx.x * (long long)NT + tid; i < n; i += (long long)gridDim.x * NT)
@@ -90,13 +92,12 @@ __global__ void __launch_bounds__(NT) k_sum(long long n, const T* a, const unsig
   double v[1] = {s};
   __shared__ double o[1];
   if (grid_reduce<RED_SUM, 1>(v, partials, ticket, o))
-    if (tid == 0) *out = o[0];
+    if (tid == 0) *out = o[0] / (double)nfluid;
 }
 
-// x -= mean over the cells that are not excluded (nfluid of them)
-__global__ void k_sub_mean(long long n, long long nfluid, const unsigned char* ex, double* x,
-                           const double* sum) {
-  double mean = *sum / (double)nfluid;
+// x -= mean over the cells that are not excluded
+__global__ void k_sub_mean(long long n, const unsigned char* ex, double* x, const double* xmean) {
+  const double mean = *xmean;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     if (!ex || !ex[i]) x[i] -= mean;
@@ -106,13 +107,13 @@ __global__ void k_sub_mean(long long n, long long nfluid, const unsigned char* e
 // reduces <r,z>, <r,r>, <f',f'> and sets the tolerance and done flag.
 template <int DIM, class T, bool PER>
 __global__ void __launch_bounds__(NT) k_cg_init(Mesh m, const T* kf, const T* dg, const T* idg,
-                                                const double* f, const double* fmean_sum,
+                                                const double* f, const double* fmean,
                                                 const T* x, int use_guess, long long pin,
                                                 T* r, T* z, T* p, double tol, int limit,
                                                 int dev_params, double* partials,
                                                 DevScalars* ds, int kch) {
   double s[3] = {0., 0., 0.};
-  double mean = fmean_sum ? *fmean_sum / (double)m.nfluid : 0.;
+  const double mean = fmean ? *fmean : 0.;
   CELL_LOOP_BEGIN(m, kch)
   double fc = EXCLUDED() ? f[X.c] : f[X.c] - mean;
   double rc = fc;
@@ -209,11 +210,11 @@ __global__ void __launch_bounds__(NT) k_cg_update(long long n, TX* x, T* r, T* z
 // singular), <r,r> reduced; r also written as FP32 for the inner solve.
 template <int DIM, bool PER>
 __global__ void __launch_bounds__(NT) k_ir_residual(Mesh m, const double* kf, const double* dg,
-                                                    const double* f, const double* fmean_sum,
+                                                    const double* f, const double* fmean,
                                                     const double* x, long long pin, double* r,
                                                     double* partials, DevScalars* ds, int kch) {
   double s = 0.;
-  double mean = fmean_sum ? *fmean_sum / (double)m.nfluid : 0.;
+  const double mean = fmean ? *fmean : 0.;
   CELL_LOOP_BEGIN(m, kch)
   double rc = (EXCLUDED() ? f[X.c] : f[X.c] - mean) - stencil_row<DIM, PER>(m, X, kf, dg, x, pin);
   r[X.c] = rc;
@@ -250,18 +251,18 @@ cudaError_t pcg_prepare(const Mesh& m, const double* kf, double shift, PcgWork& 
 }
 
 cudaError_t mean_sum(const Mesh& m, const double* f, PcgWork& w, cudaStream_t st) {
-  k_sum<double><<<flat_blocks_l(m.nc), dim3(BX, BY), 0, st>>>(m.nc, f, m.ex, w.partials,
-                                                             &w.ds->red[RS_MEAN],
-                                                             &w.ds->ticket[TK_MEAN]);
+  k_mean<double><<<flat_blocks_l(m.nc), dim3(BX, BY), 0, st>>>(m.nc, m.nfluid, f, m.ex,
+                                                              w.partials, &w.ds->red[RS_MEAN],
+                                                              &w.ds->ticket[TK_MEAN]);
   count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t sub_mean(const Mesh& m, double* x, PcgWork& w, cudaStream_t st) {
-  k_sum<double><<<flat_blocks_l(m.nc), dim3(BX, BY), 0, st>>>(m.nc, x, m.ex, w.partials,
-                                                             &w.ds->red[RS_XMEAN],
-                                                             &w.ds->ticket[TK_MEAN2]);
-  k_sub_mean<<<flat_blocks_l(m.nc), NT, 0, st>>>(m.nc, m.nfluid, m.ex, x, &w.ds->red[RS_XMEAN]);
+  k_mean<double><<<flat_blocks_l(m.nc), dim3(BX, BY), 0, st>>>(m.nc, m.nfluid, x, m.ex,
+                                                              w.partials, &w.ds->red[RS_XMEAN],
+                                                              &w.ds->ticket[TK_MEAN2]);
+  k_sub_mean<<<flat_blocks_l(m.nc), NT, 0, st>>>(m.nc, m.ex, x, &w.ds->red[RS_XMEAN]);
   count_launches(2);
   return cudaGetLastError();
 }
