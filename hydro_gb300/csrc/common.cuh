@@ -5,7 +5,20 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "fpconv.h"
+
 namespace hg {
+
+// Widening / narrowing between a kernel's arithmetic type and FP64 through
+// the integer-pipe conversions (fpconv.h); identities for FP64 kernels.
+__device__ __forceinline__ double to_d(float v) { return f2d(v); }
+__device__ __forceinline__ double to_d(double v) { return v; }
+template <class T>
+__device__ __forceinline__ T to_t(double v);
+template <>
+__device__ __forceinline__ float to_t<float>(double v) { return d2f(v); }
+template <>
+__device__ __forceinline__ double to_t<double>(double v) { return v; }
 
 // Uniform Cartesian block.  Cells: i + nx*(j + ny*k); faces direction-
 // blocked, x-fastest over (n_d+1) in their own direction (the reference's

@@ -74,7 +74,7 @@ __global__ void k_axpy_extrap(long long n, double ge, double* out, const double*
 __global__ void k_d2f(long long n, const double* in, float* out) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    out[i] = (float)in[i];
+    out[i] = d2f(in[i]);
 }
 
 // ------------------------------------------------------- velocity grads --
@@ -542,7 +542,7 @@ __global__ void __launch_bounds__(NT) k_mom_sweep32(Mesh m, float omega, double 
 __global__ void k_f2d3(long long n, int dim, FP<3> in, W3 out) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    for (int k = 0; k < dim; ++k) out.a[k][i] = (double)in.a[k][i];
+    for (int k = 0; k < dim; ++k) out.a[k][i] = f2d(in.a[k][i]);
 }
 
 // ------------------------------------------------------------ Rhie-Chow --
@@ -572,7 +572,7 @@ __global__ void k_rhie_chow(Mesh m, Geo g64, GeoT<T> g, FluidCoef fc64, FluidCoe
     auto inner = [&](long long cm, long long cp, long long ff) {
       // FP64: the interpolated velocity and the difference of the wide and
       // compact pressure gradients (the cell gradients come from k_force)
-      double uf = avg(up.a[d][cm] + (double)du.a[d][cm], up.a[d][cp] + (double)du.a[d][cp]);
+      double uf = avg(up.a[d][cm] + to_d(du.a[d][cm]), up.a[d][cp] + to_d(du.a[d][cp]));
       double vfi = uf * A;
       double gpf = avg(gp.a[d][cm], gp.a[d][cp]);
       double dpw = gpf - (p[cp] - p[cm]) * g64.inv_h[d];
@@ -580,9 +580,9 @@ __global__ void k_rhie_chow(Mesh m, Geo g64, GeoT<T> g, FluidCoef fc64, FluidCoe
       T fxf = face_vec<DIM, T>(force, cm, cp, d, fc.geometric);
       T iDf = T(1) / avg(Dc[cm], Dc[cp]);
       T k = g.A[d] * g.inv_h[d] * iDf;
-      T corr = fc.rc * (((T)dpw + (fxf - frf)) * g.A[d]) * iDf;
-      Fs[ff] = vfi + (double)corr - mv;
-      kf[ff] = (double)k;
+      T corr = fc.rc * ((to_t<T>(dpw) + (fxf - frf)) * g.A[d]) * iDf;
+      Fs[ff] = vfi + to_d(corr) - mv;
+      kf[ff] = to_d(k);
       if (kf32) kf32[ff] = (float)k;
     };
     if (HAS_LO(d)) {
@@ -646,7 +646,7 @@ __global__ void __launch_bounds__(NT) k_correct(Mesh m, Geo g, FluidCoef fc, C3 
   CELL_LOOP_BEGIN(m, kch)
   double pn = pip[X.c] + fc.relax_p * pc[X.c];
   pic[X.c] = pn;
-  if (p32) p32[X.c] = (float)pn;
+  if (p32) p32[X.c] = d2f(pn);
   double d2 = 0.;
   if (MIX) {
     const float idc = -1.f / Dc32[X.c];
@@ -654,24 +654,23 @@ __global__ void __launch_bounds__(NT) k_correct(Mesh m, Geo g, FluidCoef fc, C3 
 #pragma unroll
     for (int k = 0; k < DIM; ++k) {
       long long s = cell_stride(m, k);
-      const float gpc = (float)grad_extrap_m<PER>(m, pc, X.c, k, X.i[k], s, g.inv_h[k]);
+      const float gpc = d2f(grad_extrap_m<PER>(m, pc, X.c, k, X.i[k], s, g.inv_h[k]));
       const float inc = fmaf(gpc, idc, du32.a[k][X.c]);
-      const double un = up.a[k][X.c] + (double)inc;
+      const double un = up.a[k][X.c] + f2d(inc);
       uic.a[k][X.c] = un;
-      u32.a[k][X.c] = (float)un;
+      u32.a[k][X.c] = d2f(un);
       e2 = fmaf(inc, inc, e2);
       long long f = face_id(m, k, X.i[0], X.i[1], X.i[2]);
       const double fv =
-          HAS_LO(k) ? Fs[f] + (double)(kf32[f] * (float)(pc[NB_LO(k, s)] - pc[X.c])) : Fs[f];
+          HAS_LO(k) ? Fs[f] + f2d(kf32[f] * d2f(pc[NB_LO(k, s)] - pc[X.c])) : Fs[f];
       Fic[f] = fv;
-      F32[f] = (float)fv;
+      F32[f] = d2f(fv);
       if (X.i[k] == m.n[k] - 1) {
         long long fh = f + face_stride(m, k);
         const double fvh =
-            HAS_HI(k) ? Fs[fh] + (double)(kf32[fh] * (float)(pc[X.c] - pc[NB_HI(k, s)]))
-                      : Fs[fh];
+            HAS_HI(k) ? Fs[fh] + f2d(kf32[fh] * d2f(pc[X.c] - pc[NB_HI(k, s)])) : Fs[fh];
         Fic[fh] = fvh;
-        F32[fh] = (float)fvh;
+        F32[fh] = d2f(fvh);
       }
     }
     d2 = e2;

@@ -64,15 +64,15 @@ __global__ void k_diag(Mesh m, const double* kf, double shift, long long pin, do
     if (HAS_LO(d)) s += klo;
     if (HAS_HI(d)) s += kf[fl + face_stride(m, d)];
     if (kf32) {
-      kf32[fl] = (float)klo;
-      if (X.i[d] == m.n[d] - 1) kf32[fl + face_stride(m, d)] = (float)kf[fl + face_stride(m, d)];
+      kf32[fl] = d2f(klo);
+      if (X.i[d] == m.n[d] - 1) kf32[fl + face_stride(m, d)] = d2f(kf[fl + face_stride(m, d)]);
     }
   }
   if (X.c == pin || EXCLUDED()) s = 1.;  // identity rows
   dg[X.c] = s;
   if (idg) idg[X.c] = 1. / s;  // FP64 Jacobi-PCG only
   if (dg32) {
-    const float s32 = (float)s;
+    const float s32 = d2f(s);
     dg32[X.c] = s32;
     idg32[X.c] = 1.f / s32;
   }
@@ -464,7 +464,7 @@ namespace {
 __global__ void k_accumulate(long long n, double* x, const float* e) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    x[i] += (double)e[i];
+    x[i] += f2d(e[i]);
 }
 }  // namespace
 

@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(NT) k_mgcg_init(long long n, const double* __r
 #pragma unroll 2
   for (long long i = g; i < n4; i += stride) {
     const double2 a = r2[2 * i], b = r2[2 * i + 1];
-    reinterpret_cast<float4*>(r)[i] = make_float4((float)a.x, (float)a.y, (float)b.x, (float)b.y);
+    reinterpret_cast<float4*>(r)[i] = make_float4(d2f(a.x), d2f(a.y), d2f(b.x), d2f(b.y));
     reinterpret_cast<float4*>(x)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     s += a.x * a.x;
     s += a.y * a.y;
@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(NT) k_mgcg_init(long long n, const double* __r
   }
   for (long long i = 4 * n4 + g; i < n; i += stride) {
     double v = r64[i];
-    r[i] = (float)v;
+    r[i] = d2f(v);
     x[i] = 0.f;
     s += v * v;
   }
