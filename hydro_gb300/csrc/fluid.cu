@@ -1127,9 +1127,11 @@ __global__ void k_outlet_set(Mesh m, BcSpec sp, W3 bv, FP<3> bv32, const DevScal
 }  // namespace
 
 // ------------------------------------------------------------ launchers --
+// Cell kernels are launched in whole waves of their own occupancy
+// (cell_launch_waves).
 #define DISPATCH_DIM(m, KERNEL, ...)                                     \
   do {                                                                   \
-    Launch L = cell_launch(m);                                           \
+    Launch L = cell_launch_waves(m, resident_ctas((m).dim == 3 ? (const void*)KERNEL<3> : (const void*)KERNEL<2>)); \
     if ((m).dim == 3)                                                    \
       KERNEL<3><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);         \
     else                                                                 \
@@ -1139,21 +1141,21 @@ __global__ void k_outlet_set(Mesh m, BcSpec sp, W3 bv, FP<3> bv32, const DevScal
   } while (0)
 #define DISPATCH_DIM_P(m, KERNEL, ...)                                   \
   do {                                                                   \
-    Launch L = cell_launch(m);                                           \
+    Launch L = cell_launch_waves(m, resident_ctas(CELL_KERNEL_P(m, KERNEL))); \
     CELL_LAUNCH_P(m, L, st, KERNEL, __VA_ARGS__);                        \
     count_launches(1);                                                   \
     return cudaGetLastError();                                           \
   } while (0)
 #define DISPATCH_DIM_TP(m, KERNEL, T, ...)                               \
   do {                                                                   \
-    Launch L = cell_launch(m);                                           \
+    Launch L = cell_launch_waves(m, resident_ctas(CELL_KERNEL_TP(m, KERNEL, T))); \
     CELL_LAUNCH_TP(m, L, st, KERNEL, T, __VA_ARGS__);                    \
     count_launches(1);                                                   \
     return cudaGetLastError();                                           \
   } while (0)
 #define DISPATCH_DIM_T(m, KERNEL, T, ...)                                \
   do {                                                                   \
-    Launch L = cell_launch(m);                                           \
+    Launch L = cell_launch_waves(m, resident_ctas((m).dim == 3 ? (const void*)KERNEL<3, T> : (const void*)KERNEL<2, T>)); \
     if ((m).dim == 3)                                                    \
       KERNEL<3, T><<<L.grid, L.block, 0, st>>>(__VA_ARGS__, L.kch);      \
     else                                                                 \
@@ -1427,7 +1429,8 @@ cudaError_t launch_correct(const Mesh& m, const FluidCoef& fc, C3 u_prev, C3 du,
                            const double* kf, const float* kf32, double* F_ic, FP<3> u32,
                            float* p32, float* F32, double* partials, DevScalars* ds,
                            cudaStream_t st) {
-  Launch L = cell_launch(m);
+  Launch L = cell_launch_waves(m, resident_ctas(du32.a[0] ? CELL_KERNEL_TP(m, k_correct, true)
+                                                          : CELL_KERNEL_TP(m, k_correct, false)));
   if (du32.a[0])
     CELL_LAUNCH_TP(m, L, st, k_correct, true, m, make_geo(m), fc, u_prev, du, du32, Dc32, u_ic,
                    p_ip, p_ic, pc, Dc, Fs, kf, kf32, F_ic, u32, p32, F32, partials, ds);

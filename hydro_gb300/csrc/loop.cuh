@@ -101,6 +101,11 @@ constexpr bool kPerT = true;
                                    : (const void*)KERNEL<3, false>)                    \
                 : (any_periodic(m) ? (const void*)KERNEL<2, true>                      \
                                    : (const void*)KERNEL<2, false>))
+#define CELL_KERNEL_TP(m, KERNEL, T)                                                   \
+  ((m).dim == 3 ? (any_periodic(m) ? (const void*)KERNEL<3, T, true>                   \
+                                   : (const void*)KERNEL<3, T, false>)                 \
+                : (any_periodic(m) ? (const void*)KERNEL<2, T, true>                   \
+                                   : (const void*)KERNEL<2, T, false>))
 #define CELL_LAUNCH_TP(m, L, st, KERNEL, T, ...)                                        \
   do {                                                                                  \
     const bool p_ = any_periodic(m);                                                    \
