@@ -604,7 +604,7 @@ int solve_pressure_graph(hydro_ctx* x, int singular, int mixed) {
     cudaGraphConditionalHandle hr, hk;
     if ((rc = new_handle(x, 0, &hr))) return rc;
     if ((rc = new_handle(x, 1, &hk))) return rc;
-    CK(ir_residual(m, x->kf, x->prhs, x->pc, singular, w, x->st));
+    CK(ir_residual(m, x->kf, x->prhs, nullptr, singular, w, x->st));
     CK(launch_ctl_refine(w.ds, d.pressure_tolerance, inner_min, d.pressure_iters_limit, hr, 1,
                          x->st));
     rc = add_while(x, hr, [&]() -> int {
@@ -675,7 +675,7 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
     int total = 0;
     const double inner_tol = mgcg ? 1e-5 : 1e-4;
     for (int outer = 0; outer < 50; ++outer) {
-      CK(ir_residual(m, x->kf, x->prhs, x->pc, singular, w, x->st));
+      CK(ir_residual(m, x->kf, x->prhs, outer ? x->pc : nullptr, singular, w, x->st));
       rc = sync_scalars(x);
       if (rc) return rc;
       double rr = x->hds->red[RS_IR_RR];

@@ -566,22 +566,22 @@ __global__ void k_rhie_chow(Mesh m, Geo g64, GeoT<T> g, FluidCoef fc64, FluidCoe
     long long s = cell_stride(m, d);
     int id = X.i[d], nd = m.n[d];
     long long f = face_id(m, d, X.i[0], X.i[1], X.i[2]);
-    const double A = g64.A[d];
+    const double A = g64.A[d], hA = 0.5 * A;
     const double mv = fc64.meshvel[d] * A;
     // inner face between cm (low side) and cp (high side)
     auto inner = [&](long long cm, long long cp, long long ff) {
       // FP64: the interpolated velocity and the difference of the wide and
-      // compact pressure gradients (the cell gradients come from k_force)
-      double uf = avg(up.a[d][cm] + to_d(du.a[d][cm]), up.a[d][cp] + to_d(du.a[d][cp]));
-      double vfi = uf * A;
-      double gpf = avg(gp.a[d][cm], gp.a[d][cp]);
+      // compact pressure gradients (the cell gradients come from k_force);
+      // the two corrections are summed in T, the two velocities in FP64
+      double vfi = ((up.a[d][cm] + up.a[d][cp]) + to_d(du.a[d][cm] + du.a[d][cp])) * hA;
+      double gpf = (gp.a[d][cm] + gp.a[d][cp]) * 0.5;
       double dpw = gpf - (p[cp] - p[cm]) * g64.inv_h[d];
       T frf = face_vec<DIM, T>(fres, cm, cp, d, fc.geometric);
       T fxf = face_vec<DIM, T>(force, cm, cp, d, fc.geometric);
       T iDf = T(1) / avg(Dc[cm], Dc[cp]);
       T k = g.A[d] * g.inv_h[d] * iDf;
       T corr = fc.rc * ((to_t<T>(dpw) + (fxf - frf)) * g.A[d]) * iDf;
-      Fs[ff] = vfi + to_d(corr) - mv;
+      Fs[ff] = mv != 0. ? vfi + to_d(corr) - mv : vfi + to_d(corr);
       kf[ff] = to_d(k);
       if (kf32) kf32[ff] = (float)k;
     };

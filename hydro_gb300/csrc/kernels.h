@@ -297,8 +297,9 @@ cudaError_t pcg_iterate(const Mesh& m, const double* kf, double* x, int chunk, P
 // mean(f) into ds->red[RS_MEAN]; x -= mean(x).
 cudaError_t mean_sum(const Mesh& m, const double* f, PcgWork& w, cudaStream_t st);
 cudaError_t sub_mean(const Mesh& m, double* x, PcgWork& w, cudaStream_t st);
-// Mixed precision: FP64 residual r = f' - A x (||r||^2 in ds->red[RS_IR_RR]),
-// FP32 PCG for A e = r to a relative tolerance, x += e.
+// Mixed precision: FP64 residual r = f' - A x (||r||^2 in ds->red[RS_IR_RR];
+// x null when the iterate is zero), FP32 PCG for A e = r to a relative
+// tolerance, x += e.
 cudaError_t ir_residual(const Mesh& m, const double* kf, const double* f, const double* x,
                         int singular, PcgWork& w, cudaStream_t st);
 // Inner-solve start.  dev_params = 0: tolerance `tol` and limit `w.limit`

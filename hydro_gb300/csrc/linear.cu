@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(NT) k_cg_update(long long n, TX* x, T* r, T* z
 }
 
 // FP64 residual of the refinement loop: r = f' - A x (f' = f - mean when
-// singular), <r,r> reduced; r also written as FP32 for the inner solve.
+// singular; x null: the iterate is zero and r = f'), <r,r> reduced.
 template <int DIM, bool PER>
 __global__ void __launch_bounds__(NT) k_ir_residual(Mesh m, const double* kf, const double* dg,
                                                     const double* f, const double* fmean,
@@ -216,7 +216,8 @@ __global__ void __launch_bounds__(NT) k_ir_residual(Mesh m, const double* kf, co
   double s = 0.;
   const double mean = fmean ? *fmean : 0.;
   CELL_LOOP_BEGIN(m, kch)
-  double rc = (EXCLUDED() ? f[X.c] : f[X.c] - mean) - stencil_row<DIM, PER>(m, X, kf, dg, x, pin);
+  double rc = EXCLUDED() ? f[X.c] : f[X.c] - mean;
+  if (x) rc -= stencil_row<DIM, PER>(m, X, kf, dg, x, pin);
   r[X.c] = rc;
   s += rc * rc;
   CELL_LOOP_END
