@@ -394,6 +394,62 @@ __global__ void __launch_bounds__(NT) k_cg32_dir_spmv(Mesh m, const float* __res
   }
 }
 
+// k_cg32_dir_spmv for a block without periodic directions or excluded cells
+// in 32-bit index arithmetic (faces < 2^31): same loads, order of the sums
+// and results.
+template <int DIM>
+__global__ void __launch_bounds__(NT) k_cg32_dir_spmv_i32(Mesh m, const float* __restrict__ kf,
+                                                          const float* __restrict__ dg,
+                                                          const float* __restrict__ z,
+                                                          const float* __restrict__ pold,
+                                                          float* __restrict__ pnew,
+                                                          float* __restrict__ Ap, int pin,
+                                                          double* partials, DevScalars* ds,
+                                                          int kch) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  const bool first = ds->flag[FL_PCG_ITERS] == 0;
+  const float beta = first ? 0.f : (float)ds->red[RS_PCG_BETA];
+  DFAcc acc;
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int j = blockIdx.y * BY + threadIdx.y;
+  const int n0 = m.n[0], n1 = m.n[1];
+  const int nz = DIM == 3 ? m.n[2] : 1;
+  const int k0 = blockIdx.z * kch, k1 = min(k0 + kch, nz);
+  const int cs[3] = {1, n0, n0 * n1};
+  const int fs[3] = {1, (int)m.fnx[1], (int)(m.fnx[2] * m.fny[2])};
+  auto P = [&](int c) { return first ? z[c] : fmaf(beta, pold[c], z[c]); };
+  if (i < n0 && j < n1) {
+    for (int k = k0; k < k1; ++k) {
+      const int id[3] = {i, j, k};
+      const int c = i + n0 * (j + n1 * k);
+      const float pc = P(c);
+      pnew[c] = pc;
+      float a;
+      if (c == pin) {
+        a = pc;
+      } else {
+        a = dg[c] * pc;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          const int fl = (int)m.fofs[d] + i + (int)m.fnx[d] * (j + (int)m.fny[d] * k);
+          if (id[d] > 0 && c - cs[d] != pin) a = fmaf(-kf[fl], P(c - cs[d]), a);
+          if (id[d] < m.n[d] - 1 && c + cs[d] != pin) a = fmaf(-kf[fl + fs[d]], P(c + cs[d]), a);
+        }
+      }
+      Ap[c] = a;
+      acc.add_prod(pc, a);
+    }
+  }
+  double v[1] = {acc.value()};
+  __shared__ double o[1];
+  if (grid_reduce<RED_SUM, 1>(v, partials, &ds->ticket[TK_F32_A], o)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      ds->red[RS_PCG_PAP] = o[0];
+      ds->red[RS_PCG_ALPHA] = ds->red[RS_PCG_RZ] / o[0];
+    }
+  }
+}
+
 // x += alpha p, r -= alpha Ap, z = r/diag; <r,z>, <r,r> -> beta, stop test.
 __global__ void __launch_bounds__(NT) k_cg32_update(long long n, float* x, float* r, float* z,
                                                     const float* p, const float* Ap,
@@ -433,6 +489,19 @@ __global__ void __launch_bounds__(NT) k_cg32_update(long long n, float* x, float
 cudaError_t cg32_dir_spmv(const Mesh& m, const float* kf, const float* dg, const float* z,
                           const float* pold, float* pnew, float* Ap, long long pin,
                           double* partials, DevScalars* ds, cudaStream_t st) {
+  if (!any_periodic(m) && m.nf < (1LL << 31)) {
+    const void* k = m.dim == 3 ? (const void*)k_cg32_dir_spmv_i32<3>
+                               : (const void*)k_cg32_dir_spmv_i32<2>;
+    Launch L = cell_launch_waves(m, resident_ctas(k));
+    if (m.dim == 3)
+      k_cg32_dir_spmv_i32<3><<<L.grid, L.block, 0, st>>>(m, kf, dg, z, pold, pnew, Ap, (int)pin,
+                                                         partials, ds, L.kch);
+    else
+      k_cg32_dir_spmv_i32<2><<<L.grid, L.block, 0, st>>>(m, kf, dg, z, pold, pnew, Ap, (int)pin,
+                                                         partials, ds, L.kch);
+    count_launches(1);
+    return cudaGetLastError();
+  }
   Launch L = cell_launch_waves(m, resident_ctas(CELL_KERNEL_P(m, k_cg32_dir_spmv)));
   CELL_LAUNCH_P(m, L, st, k_cg32_dir_spmv, m, kf, dg, z, pold, pnew, Ap, pin, partials, ds);
   count_launches(1);

@@ -740,6 +740,13 @@ cudaError_t mg_prepare(MgWork& mg) {
 }
 
 namespace {
+// One red-black half-sweep of a level (k_mg_smooth).
+void mg_smooth(int dim, const Launch& H, bool per, const Mesh& m, const float* kf,
+               const float* idg, const float* b, float* x, int color, int zero, long long pin,
+               const float* cx, int cnx, int cny, const DevScalars* ds, cudaStream_t st) {
+  MG_LAUNCH_P(k_mg_smooth, H, per, m, kf, idg, b, x, color, zero, pin, cx, cnx, cny, ds);
+}
+
 // z = M^-1 r: one V-cycle with `nsweep` (red, black) sweeps before and
 // (black, red) sweeps after each coarse correction.  Levels above `top`
 // are grid launches; `top` and below run in one CTA.
@@ -759,8 +766,8 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
       // below the finest level the first (red, from zero) half-sweep was
       // done by the restriction
       if (s > 0 || l == 0)
-        MG_LAUNCH_P(k_mg_smooth, H, per, f.m, f.kf, f.idg, f.b, f.x, 0, s == 0, lp, nullptr, 0, 0, ds);
-      MG_LAUNCH_P(k_mg_smooth, H, per, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, nullptr, 0, 0, ds);
+        mg_smooth(dim, H, per, f.m, f.kf, f.idg, f.b, f.x, 0, s == 0, lp, nullptr, 0, 0, ds, st);
+      mg_smooth(dim, H, per, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, nullptr, 0, 0, ds, st);
     }
     MgLevel& c = mg.lev[l + 1];
     Launch L = cell_launch(c.m);
@@ -804,12 +811,12 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
     Launch H = half_launch(cl.m);
     const int half = mg.coarse_sweeps_large / 2 > 0 ? mg.coarse_sweeps_large / 2 : 1;
     for (int s = 0; s < half; ++s) {
-      MG_LAUNCH_P(k_mg_smooth, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, s == 0, lp, nullptr, 0, 0, ds);
-      MG_LAUNCH_P(k_mg_smooth, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 1, 0, lp, nullptr, 0, 0, ds);
+      mg_smooth(dim, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, s == 0, lp, nullptr, 0, 0, ds, st);
+      mg_smooth(dim, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 1, 0, lp, nullptr, 0, 0, ds, st);
     }
     for (int s = 0; s < half; ++s) {
-      MG_LAUNCH_P(k_mg_smooth, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 1, 0, lp, nullptr, 0, 0, ds);
-      MG_LAUNCH_P(k_mg_smooth, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, 0, lp, nullptr, 0, 0, ds);
+      mg_smooth(dim, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 1, 0, lp, nullptr, 0, 0, ds, st);
+      mg_smooth(dim, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, 0, lp, nullptr, 0, 0, ds, st);
     }
   }
   for (int l = top - 1; l >= 0; --l) {
@@ -820,8 +827,8 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
     for (int s = 0; s < ns; ++s) {
       // the first half-sweep adds the coarse correction on the fly
       const float* cx = s == 0 ? c.x : nullptr;
-      MG_LAUNCH_P(k_mg_smooth, H, per, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, cx, c.m.n[0], c.m.n[1], ds);
-      MG_LAUNCH_P(k_mg_smooth, H, per, f.m, f.kf, f.idg, f.b, f.x, 0, 0, lp, nullptr, 0, 0, ds);
+      mg_smooth(dim, H, per, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, cx, c.m.n[0], c.m.n[1], ds, st);
+      mg_smooth(dim, H, per, f.m, f.kf, f.idg, f.b, f.x, 0, 0, lp, nullptr, 0, 0, ds, st);
     }
   }
   return cudaGetLastError();
