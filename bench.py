@@ -388,12 +388,43 @@ def roofline(res):
             "effective_launches": eff, "avg_launch_us": round(tms * 1e3 / max(eff, 1), 2)}
 
 
+def gpu_local_cpus(local):
+    """CPUs attached to the GPU's PCI root (sysfs local_cpulist), or None."""
+    try:
+        import torch
+        prop = torch.cuda.get_device_properties(local)
+        dom = getattr(prop, "pci_domain_id", 0)
+        bus, dev = getattr(prop, "pci_bus_id"), getattr(prop, "pci_device_id")
+        path = "/sys/bus/pci/devices/%04x:%02x:%02x.0/local_cpulist" % (dom, bus, dev)
+        with open(path) as f:
+            text = f.read().strip()
+        cpus = set()
+        for part in text.split(","):
+            if "-" in part:
+                a, b = part.split("-")
+                cpus.update(range(int(a), int(b) + 1))
+            elif part:
+                cpus.add(int(part))
+        return cpus or None
+    except Exception:
+        return None
+
+
 def run_ours(args, rank, world, local):
     import torch
 
     from hydro_gb300 import capi
 
     torch.cuda.set_device(local)
+    # host threads and the pinned host buffers of the end-to-end leg on the
+    # GPU's own NUMA node (first touch), when sysfs says which CPUs those are
+    cpus = gpu_local_cpus(local)
+    avail = os.sched_getaffinity(0) if hasattr(os, "sched_getaffinity") else None
+    if cpus and avail and cpus & avail and cpus & avail != avail:
+        try:
+            os.sched_setaffinity(0, cpus & avail)
+        except OSError:
+            pass
     try:
         capi.load()
     except RuntimeError:
@@ -408,6 +439,11 @@ def run_ours(args, rank, world, local):
         plain = measure(args, "fp64", rank, world, local, stream, e2e=False)
         if args.form != "fp64_mg":
             fp64mg = measure(args, "fp64_mg", rank, world, local, stream, e2e=False)
+    if avail:
+        try:
+            os.sched_setaffinity(0, avail)  # the CPU baseline uses every host core
+        except OSError:
+            pass
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
