@@ -1187,6 +1187,12 @@ static int flat_blocks(long long n) {
   if (b < 1) b = 1;
   return (int)b;
 }
+// grid of a grid-stride reduction: 16 blocks per SM at most, so that the
+// last block folds a few thousand partials, not one per 256 elements
+static int flat_blocks_red(long long n) {
+  const int b = flat_blocks(n);
+  return b < 152 * 16 ? b : 152 * 16;
+}
 
 cudaError_t launch_start_step(const Mesh& m, double ge, W3 u_ic, C3 u_tc, C3 u_tp,
                               double* p_ic, const double* p_tc, const double* p_tp,
@@ -1465,14 +1471,14 @@ cudaError_t launch_add(long long n, double* a, const double* b, cudaStream_t st)
 
 cudaError_t launch_auto_dt(const Mesh& m, const double* F, double* partials, DevScalars* ds,
                            cudaStream_t st) {
-  k_auto_dt<<<flat_blocks(m.nf), dim3(BX, BY), 0, st>>>(m.nf, m.V, F, partials, ds);
+  k_auto_dt<<<flat_blocks_red(m.nf), dim3(BX, BY), 0, st>>>(m.nf, m.V, F, partials, ds);
   count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_nan_count(long long n, const double* a, double* partials, DevScalars* ds,
                              cudaStream_t st) {
-  k_nan_count<<<flat_blocks(n), dim3(BX, BY), 0, st>>>(n, a, partials, ds);
+  k_nan_count<<<flat_blocks_red(n), dim3(BX, BY), 0, st>>>(n, a, partials, ds);
   count_launches(1);
   return cudaGetLastError();
 }
