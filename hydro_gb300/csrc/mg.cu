@@ -211,7 +211,7 @@ __global__ void k_mg_diag(Mesh m, const float* kf, float* dg, float* idg, int kc
 // With cidg the coarse level's first half-sweep (red, from x = 0: x = b /
 // diag) is done here as well; without it the coarse iterate is cleared.
 template <int DIM, bool PER>
-__global__ void k_mg_restrict(Mesh fm, Mesh cm, const float* kf, const float* dg, const float* b,
+__global__ void __launch_bounds__(NT, 4) k_mg_restrict(Mesh fm, Mesh cm, const float* kf, const float* dg, const float* b,
                               const float* x, float* cb, float* cx, const float* cidg,
                               long long pin, const DevScalars* ds, int kch) {
   if (ds->flag[FL_PCG_DONE]) return;
