@@ -108,7 +108,7 @@ __global__ void k_vel_grad(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T
 // force and the volume-source momentum term.  Also stores the restored
 // force and the FP64 cell pressure gradient for the Rhie-Chow kernel.
 template <int DIM, class T, bool PER>
-__global__ void __launch_bounds__(NT, 6) k_force(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T, 9> G,
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 6 : 1) k_force(Mesh m, GeoT<T> g, FluidCoefT<T> fc, RT<T, 3> u, RT<T, 9> G,
                         const double* p, Geo g64, const T* mu, const T* rho,
                         RT<T, 3> force, RT<T, 3> stforce, const T* Sv, const T* Sm,
                         WT<T, 3> fo, WT<T, 3> fres, W3 gp64, int kch) {
