@@ -874,15 +874,18 @@ template <int DIM, bool PER>
 __global__ void k_smooth(Mesh m, const double* in, double* out, int kch) {
   constexpr bool kPerT = PER;
   CELL_LOOP_BEGIN(m, kch)
+  // mean over the 2 DIM faces of the face averages (the cell's own value on
+  // a boundary face) = half the cell value + half the mean of the face
+  // neighbours: 2 DIM + 1 FP64 operations instead of three per face
   double vc = in[X.c];
   double sum = 0.;
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     long long s = cell_stride(m, d);
-    sum += HAS_LO(d) ? avg(in[NB_LO(d, s)], vc) : vc;
-    sum += HAS_HI(d) ? avg(vc, in[NB_HI(d, s)]) : vc;
+    sum += HAS_LO(d) ? in[NB_LO(d, s)] : vc;
+    sum += HAS_HI(d) ? in[NB_HI(d, s)] : vc;
   }
-  out[X.c] = sum * (1. / (2. * DIM));  // a product: an FP64 division costs ~20 FP64 issues
+  out[X.c] = fma(sum, 0.5 / (2. * DIM), 0.5 * vc);
   CELL_LOOP_END
 }
 
