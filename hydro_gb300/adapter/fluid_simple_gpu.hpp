@@ -68,7 +68,9 @@ class GpuHotPath {
   size_t nf() const { return mesh_.GetNumFaces(); }
 
   static void Check(int st, const char* where) {
-    if (st == HYDRO_OK) return;
+    // a solve stopped at its iteration limit is not an error: the reference
+    // goes on past a solver's limit (linear.hpp:690-710)
+    if (st == HYDRO_OK || st == HYDRO_NOT_CONVERGED) return;
     if (st == HYDRO_ERR_NAN) throw std::string("NaN pressure");
     throw std::runtime_error(std::string(where) + ": hydro_gpu status " + std::to_string(st));
   }

@@ -97,6 +97,7 @@ class HydroDesc(ctypes.Structure):
         ("rigid_box", ctypes.c_int),
         ("rigid_box_lo", ctypes.c_double * 3),
         ("rigid_box_hi", ctypes.c_double * 3),
+        ("substitute_solvers", ctypes.c_int),
     ]
 
     @property
@@ -134,6 +135,7 @@ class StepStats(ctypes.Structure):
         ("dt", ctypes.c_double),
         ("dt_advection", ctypes.c_double),
         ("time", ctypes.c_double),
+        ("pressure_unconverged", ctypes.c_int),
     ]
 
     def as_dict(self):

@@ -231,6 +231,7 @@ struct hydro_ctx {
   double time = 0., dt = 0., adv_time = 0., adv_dt = 0.;
   int iter_count = 0, cd_iter_count = 0;
   int vel_sweeps = 0, p_iters = 0;
+  int p_unconv = 0;  // pressure solves of the step that stopped above their tolerance
   double p_res = 0., indicator = 1.;
   int du_cur = 0;
   int status = HYDRO_OK;
@@ -664,6 +665,7 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
     x->p_iters += it;
     double ff = x->hds->red[RS_PCG_FF];
     x->p_res = ff > 0. ? sqrt(x->hds->red[RS_PCG_RR] / ff) : 0.;
+    if (!(x->hds->red[RS_PCG_RR] <= x->hds->red[RS_PCG_TOL2])) x->p_unconv++;
   } else {
     // FP64 iterative refinement around an FP32 PCG (Jacobi or multigrid
     // preconditioned)
@@ -673,6 +675,7 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
     CK(cudaMemsetAsync(x->pc, 0, sizeof(double) * m.nc, x->st));
     double ff = -1.;
     int total = 0;
+    bool conv = false;
     const double inner_tol = mgcg ? 1e-5 : 1e-4;
     for (int outer = 0; outer < 50; ++outer) {
       CK(ir_residual(m, x->kf, x->prhs, outer ? x->pc : nullptr, singular, w, x->st));
@@ -681,7 +684,10 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
       double rr = x->hds->red[RS_IR_RR];
       if (ff < 0.) ff = rr;
       x->p_res = ff > 0. ? sqrt(rr / ff) : 0.;
-      if (ff == 0. || rr <= d.pressure_tolerance * d.pressure_tolerance * ff) break;
+      if (ff == 0. || rr <= d.pressure_tolerance * d.pressure_tolerance * ff) {
+        conv = true;
+        break;
+      }
       if (total >= d.pressure_iters_limit) break;
       w.limit = d.pressure_iters_limit - total;
       double tol = std::max(inner_tol, 0.5 * d.pressure_tolerance * sqrt(ff / rr));
@@ -712,6 +718,7 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
       CK(f32_accumulate(m, x->pc, w, x->st));
     }
     x->p_iters += total;
+    if (!conv) x->p_unconv++;
   }
   if (singular) CK(sub_mean(m, x->pc, w, x->st));
   return HYDRO_OK;
@@ -807,6 +814,17 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
       return HYDRO_ERR_ARG;
   if (desc->velocity_omega <= 0. || desc->velocity_relaxation_factor <= 0.)
     return HYDRO_ERR_ARG;
+  // solvers the GPU does not have are substituted only on request
+  {
+    const int vs = desc->velocity_solver, ps = desc->pressure_solver;
+    const bool v_ok = vs == HYDRO_LINEAR_GAUSS_SEIDEL || vs == HYDRO_LINEAR_JACOBI;
+    const bool p_ok = ps == HYDRO_LINEAR_CG || ps == HYDRO_LINEAR_MGCG;
+    const bool v_known = v_ok || vs == HYDRO_LINEAR_LU;
+    const bool p_known = p_ok || ps == HYDRO_LINEAR_GAUSS_SEIDEL || ps == HYDRO_LINEAR_JACOBI ||
+                         ps == HYDRO_LINEAR_LU;
+    if (!v_known || !p_known) return HYDRO_ERR_ARG;
+    if ((!v_ok || !p_ok) && !desc->substitute_solvers) return HYDRO_ERR_UNSUPPORTED;
+  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return HYDRO_ERR_NO_DEVICE;
   hydro_ctx* x = new (std::nothrow) hydro_ctx();
@@ -1174,6 +1192,7 @@ int hydro_gpu_start_step(hydro_ctx* x) {
   x->cd_iter_count = 0;
   x->vel_sweeps = 0;
   x->p_iters = 0;
+  x->p_unconv = 0;
   x->p_res = 0.;
   x->indicator = 1.;
   bdf_coeffs(x->dt, x->d.time_second_order, x->fc.co);
@@ -1481,9 +1500,13 @@ int hydro_gpu_step(hydro_ctx* x, hydro_step_stats* stats) {
   s.dt = x->dt;
   s.dt_advection = x->adv_dt;
   s.time = x->time;
-  s.status = HYDRO_OK;
+  // a pressure solve that stopped at its limit does not stop the step (the
+  // reference goes on past a solver's limit, linear.hpp:690-710); the
+  // status reports it once the step is complete
+  s.pressure_unconverged = x->p_unconv;
+  s.status = x->p_unconv ? HYDRO_NOT_CONVERGED : HYDRO_OK;
   if (stats) *stats = s;
-  return HYDRO_OK;
+  return s.status;
 }
 
 // ------------------------------------------------------ graph-captured step --
@@ -1508,7 +1531,7 @@ int advection_substeps(const hydro_ctx* x, double dt, double* t_out) {
 // not run); restored once the capture is complete.
 struct HostSnapshot {
   double time, adv_time, p_res, indicator;
-  int iter_count, cd_iter_count, vel_sweeps, p_iters;
+  int iter_count, cd_iter_count, vel_sweeps, p_iters, p_unconv;
   bool prof;
 };
 
@@ -1516,7 +1539,7 @@ int begin_capture_of(hydro_ctx* x, HostSnapshot* s) {
   for (int i = 0; i < 4; ++i)
     if (!x->cap_streams[i]) CK(cudaStreamCreateWithFlags(&x->cap_streams[i], cudaStreamNonBlocking));
   *s = {x->time, x->adv_time, x->p_res, x->indicator, x->iter_count, x->cd_iter_count,
-        x->vel_sweeps, x->p_iters, x->prof.on};
+        x->vel_sweeps, x->p_iters, x->p_unconv, x->prof.on};
   x->prof.on = false;
   x->graph_mode = true;
   return HYDRO_OK;
@@ -1534,6 +1557,7 @@ void end_capture_of(hydro_ctx* x, const HostSnapshot& s) {
   x->cd_iter_count = s.cd_iter_count;
   x->vel_sweeps = s.vel_sweeps;
   x->p_iters = s.p_iters;
+  x->p_unconv = s.p_unconv;
 }
 
 // Enqueues one whole step (StartStep, SIMPLE loop, FinishStep, advection
@@ -1549,6 +1573,7 @@ int enqueue_step_body(hydro_ctx* x, int substeps) {
   double* q0 = x->q;
     int r;
     if ((r = reset_flags(x, FL_STEP_SWEEPS, 3))) return r;  // sweeps, p iterations, SIMPLE
+    if ((r = reset_flags(x, FL_STEP_PUNCONV, 1))) return r;
     if ((r = hydro_gpu_start_step(x))) return r;
     const int limit = d.num_iterations_limit;
     const double tol = d.convergence_tolerance;
@@ -1691,7 +1716,11 @@ int finish_graph_step(hydro_ctx* x, int substeps, double adv_end, hydro_step_sta
   s.dt = x->dt;
   s.dt_advection = x->adv_dt;
   s.time = x->time;
-  s.status = (h.red[RS_NAN] > 0. || isnan(x->indicator)) ? HYDRO_ERR_NAN : HYDRO_OK;
+  x->p_unconv = h.flag[FL_STEP_PUNCONV];
+  s.pressure_unconverged = x->p_unconv;
+  s.status = (h.red[RS_NAN] > 0. || isnan(x->indicator)) ? HYDRO_ERR_NAN
+             : x->p_unconv                                 ? HYDRO_NOT_CONVERGED
+                                                           : HYDRO_OK;
   if (stats) *stats = s;
   return s.status;
 }
@@ -1885,6 +1914,10 @@ int hydro_gpu_heat_create(hydro_ctx* x, const hydro_heat_desc* hd) {
   if (hd->solver != HYDRO_LINEAR_JACOBI && hd->solver != HYDRO_LINEAR_GAUSS_SEIDEL &&
       hd->solver != HYDRO_LINEAR_LU)
     return HYDRO_ERR_ARG;
+  // the temperature rows are swept by Jacobi; another solver is substituted
+  // only on request
+  if (hd->solver != HYDRO_LINEAR_JACOBI && !x->d.substitute_solvers)
+    return HYDRO_ERR_UNSUPPORTED;
   const Mesh& m = x->m;
   auto& h = x->heat;
   if (!h.mem) {
@@ -2070,6 +2103,9 @@ int hydro_gpu_stencil_solve(int dim, int nx, int ny, int nz, const double* face_
   double res = ff > 0. ? sqrt(rr / ff) : 0.;
   if (iterations) *iterations = h.flag[FL_PCG_ITERS];
   if (residual) *residual = res;
+  // a zero row (no couplings, no shift) or a non-finite input ends the
+  // iteration with a NaN residual: reported, never taken as converged
+  if (std::isnan(rr) || std::isnan(ff)) return HYDRO_ERR_NAN;
   return (ff > 0. && rr > tolerance * tolerance * ff) ? HYDRO_NOT_CONVERGED : HYDRO_OK;
 }
 

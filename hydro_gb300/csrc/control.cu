@@ -45,6 +45,7 @@ __global__ void k_ctl_krylov_done(DevScalars* ds) {
   double ff = ds->red[RS_PCG_FF];
   ds->red[RS_P_RES] = ff > 0. ? sqrt(ds->red[RS_PCG_RR] / ff) : 0.;
   ds->flag[FL_STEP_PITERS] += ds->flag[FL_PCG_ITERS];
+  if (!(ds->red[RS_PCG_RR] <= ds->red[RS_PCG_TOL2])) ds->flag[FL_STEP_PUNCONV] += 1;
 }
 
 // Iterative refinement (the mixed pressure solve): called after every FP64
@@ -74,6 +75,8 @@ __global__ void k_ctl_refine(DevScalars* ds, double tol, double inner_min, int l
     double t = 0.5 * tol * sqrt(ff / rr);
     ds->red[RS_INNER_TOL] = t > inner_min ? t : inner_min;
     ds->flag[FL_PCG_LIMIT] = limit - total;
+  } else if (!conv) {
+    ds->flag[FL_STEP_PUNCONV] += 1;  // stopped at a limit (or NaN) above the tolerance
   }
   decide(ds, cont, h, use);
 }

@@ -86,7 +86,8 @@ enum {
   FL_ITERS = 10,         // SIMPLE iterations of the step
   FL_IR_OUTER = 11,      // refinement cycles
   FL_CONT = 12,          // last loop decision
-  FL_HEAT_DONE = 13, FL_HEAT_SWEEPS = 14  // temperature solve
+  FL_HEAT_DONE = 13, FL_HEAT_SWEEPS = 14,  // temperature solve
+  FL_STEP_PUNCONV = 15   // pressure solves of the step that stopped above their tolerance
 };
 enum {
   TK_MOM = 0, TK_PCG_A = 1, TK_PCG_B = 2, TK_PCG_INIT = 3, TK_IND = 4, TK_DT = 5,

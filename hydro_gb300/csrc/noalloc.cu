@@ -6,11 +6,14 @@
 // a file-scope device array of this library: every GPU that loads the
 // library holds it until the process exits.  Host code cannot pass the
 // array's name to a kernel (on the host that name is only a stand-in, not a
-// device address), so the first call on each device looks the address up
-// with cudaGetSymbolAddress, with that device current, and caches it.
+// device address), so every call looks the address up with
+// cudaGetSymbolAddress, with the calling device and context current.  The
+// address belongs to a CUDA context, not to a device number: a lookup per
+// call stays right after cudaDeviceReset or when the host application
+// makes its own context current, where a cached address would point into
+// a context that no longer exists.  The lookup is a host-side table query
+// and allocates nothing.
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "../../include/hydro_gpu.h"
 #include "kernels.h"
@@ -30,26 +33,20 @@ constexpr size_t kScratchBytes =
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-void* g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of g_noalloc_scratch on the current device (set up once).
+// Device address of g_noalloc_scratch in the current context.
 int scratch_address(void** out) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return HYDRO_ERR_NO_DEVICE;
-  if (dev < 0 || dev >= kMaxDevices) return HYDRO_ERR_ARG;
-  std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      cudaGetLastError();
-      return HYDRO_ERR_CUDA;
-    }
-    g_scratch_ptr[dev] = p;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return HYDRO_ERR_NO_DEVICE;
   }
-  *out = g_scratch_ptr[dev];
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    cudaGetLastError();
+    return HYDRO_ERR_CUDA;
+  }
+  *out = p;
   return HYDRO_OK;
 }
 

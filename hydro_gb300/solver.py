@@ -155,15 +155,27 @@ class Hydro:
         self._call("advection_step", ctypes.byref(n))
         return n.value
 
+    @staticmethod
+    def _check_step(st, where):
+        # HYDRO_NOT_CONVERGED: the step is complete, a pressure solve stopped
+        # at its iteration limit (the reference goes on past a solver's limit
+        # too); the stats carry the status and the count of such solves
+        if st not in (capi.OK, capi.NOT_CONVERGED):
+            raise capi.HydroError(st, where)
+
     def step(self):
+        """One time step (hydro_gpu_step); returns its stats.  A step in
+        which a pressure solve stopped at its limit returns normally with
+        ``status`` HYDRO_NOT_CONVERGED; every other error raises."""
         st = capi.StepStats()
-        self._call("step", ctypes.byref(st))
+        self._check_step(self.lib.hydro_gpu_step(self.ctx, ctypes.byref(st)), "hydro_gpu_step")
         return st.as_dict()
 
     def step_graph(self):
         """The same step as one CUDA-graph launch (hydro_gpu_step_graph)."""
         st = capi.StepStats()
-        self._call("step_graph", ctypes.byref(st))
+        self._check_step(self.lib.hydro_gpu_step_graph(self.ctx, ctypes.byref(st)),
+                         "hydro_gpu_step_graph")
         return st.as_dict()
 
     def calc_stat(self):
@@ -235,7 +247,7 @@ class Batch:
 
     def step(self):
         st = (capi.StepStats * len(self.cases))()
-        Hydro._check(self.lib.hydro_gpu_batch_step(self.b, st), "hydro_gpu_batch_step")
+        Hydro._check_step(self.lib.hydro_gpu_batch_step(self.b, st), "hydro_gpu_batch_step")
         return [s.as_dict() for s in st]
 
     def close(self):

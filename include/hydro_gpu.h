@@ -62,7 +62,12 @@ enum hydro_status {
   HYDRO_ERR_ARG = 1,          /* invalid argument / unsupported size */
   HYDRO_ERR_CUDA = 2,         /* a CUDA runtime call failed */
   HYDRO_ERR_NAN = 3,          /* NaN in pressure or velocity (fluid.hpp:795-797,1164-1166) */
-  HYDRO_NOT_CONVERGED = 4,    /* a linear solve hit its iteration limit */
+  HYDRO_NOT_CONVERGED = 4,    /* a linear solve stopped at its iteration limit above its
+                                 tolerance: the stencil solve; or a step (host-driven,
+                                 graph-captured, batch) in which a pressure solve did so.
+                                 Such a step is complete -- the reference goes on past a
+                                 solver's limit too (linear.hpp:690-710) -- and its stats
+                                 count the solves (pressure_unconverged) */
   HYDRO_ERR_UNSUPPORTED = 5,  /* option the GPU path does not implement */
   HYDRO_ERR_NOMEM = 6,        /* device allocation failed */
   HYDRO_ERR_NO_DEVICE = 7,    /* no CUDA device visible */
@@ -76,9 +81,10 @@ enum hydro_side { HYDRO_XM = 0, HYDRO_XP, HYDRO_YM, HYDRO_YP, HYDRO_ZM, HYDRO_ZP
 /* Fluid boundary condition kinds (fluid.hpp:259-337, parsed at 392-417). */
 enum hydro_bc_kind { HYDRO_BC_WALL = 0, HYDRO_BC_INLET = 1, HYDRO_BC_OUTLET = 2 };
 
-/* Linear solvers.  GAUSS_SEIDEL and LU exist only on the CPU side (oracle);
- * the GPU runs JACOBI for velocity and CG (Jacobi-preconditioned conjugate
- * gradients) for pressure. */
+/* Linear solvers.  The GPU has: for velocity GAUSS_SEIDEL (red-black sweeps)
+ * and JACOBI; for pressure CG (Jacobi-preconditioned conjugate gradients)
+ * and MGCG; for temperature JACOBI.  Any other choice is the reference's
+ * CPU solver (the oracle has them all) and needs substitute_solvers. */
 enum hydro_linear {
   HYDRO_LINEAR_GAUSS_SEIDEL = 0, /* linear.hpp:671-716 */
   HYDRO_LINEAR_JACOBI = 1,       /* linear.hpp:736-783 */
@@ -196,6 +202,18 @@ typedef struct hydro_desc {
    * boundary faces of excluded cells, carry nothing.  0: no box. */
   int rigid_box;
   double rigid_box_lo[3], rigid_box_hi[3];
+  /* Solvers the GPU does not have: velocity LU (the reference's one-sweep
+   * sequential approximate solve, linear.hpp:527-567), pressure
+   * GAUSS_SEIDEL / JACOBI / LU (stopping on the max update,
+   * linear.hpp:671-783), temperature GAUSS_SEIDEL / LU.  With 0 (the
+   * default) such a description gives HYDRO_ERR_UNSUPPORTED (from
+   * hydro_gpu_create, hydro_gpu_heat_create, hydro_gpu_batch_create); with
+   * 1 the GPU substitutes Jacobi sweeps to velocity_tolerance (velocity,
+   * temperature) and CG to the relative residual pressure_tolerance
+   * (pressure).  A substitute reaches the reference's numbers only with
+   * tight tolerances: with the reference's loose defaults (one LU sweep,
+   * SOR to a max update of 1e-3) the fields differ. */
+  int substitute_solvers;
 } hydro_desc;
 
 typedef struct hydro_step_stats {
@@ -207,6 +225,8 @@ typedef struct hydro_step_stats {
   double pressure_residual;     /* last relative residual of the pressure solve */
   int advection_substeps;
   double dt, dt_advection, time;
+  int pressure_unconverged;     /* pressure solves of the step that stopped at their
+                                   iteration limit above their tolerance (CG, MGCG) */
 } hydro_step_stats;
 
 typedef struct hydro_stat {
@@ -399,7 +419,9 @@ int hydro_scalar_output_close(hydro_scalar_output* out);
  *               treatment of a fixed-pressure cell, fluid.hpp:996-1014).
  * Singular (shift == 0, no pinned cell) systems are solved in the subspace
  * orthogonal to the constants and return the zero-mean solution.  Returns HYDRO_NOT_CONVERGED when the limit is
- * hit; *iterations and *residual report the relative residual reached. */
+ * hit; *iterations and *residual report the relative residual reached.
+ * Returns HYDRO_ERR_NAN when the residual is not a number (a non-finite
+ * input, or a row with neither couplings nor shift). */
 size_t hydro_gpu_stencil_workspace_size(int dim, int nx, int ny, int nz);
 int hydro_gpu_stencil_solve(int dim, int nx, int ny, int nz,
                             const double* face_coeff, double shift,
@@ -425,9 +447,13 @@ int hydro_gpu_stencil_solve(int dim, int nx, int ny, int nz,
  * Limits and rules:
  *  - at most HYDRO_NOALLOC_MAX_CELLS cells; larger blocks return
  *    HYDRO_ERR_ARG without touching the GPU;
- *  - the first call on each device looks up the array's device address
- *    (cudaGetSymbolAddress, with that device current) and caches it; make
- *    that first call before any stream capture;
+ *  - every call looks up the array's device address in the calling
+ *    thread's current device and context (cudaGetSymbolAddress), so the
+ *    call follows cudaDeviceReset and contexts the host application makes
+ *    current; the lookup allocates nothing;
+ *  - like hydro_gpu_stencil_solve, the call waits for `stream` between
+ *    chunks of iterations (it reads the convergence flags back to the
+ *    host) and returns with the stream's work complete;
  *  - all calls share the one array, which keeps the last call's contents
  *    (each call clears what must start at zero itself); calls that overlap
  *    on the GPU -- two streams or host threads at once -- race on it, so

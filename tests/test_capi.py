@@ -105,3 +105,29 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(capi, "lib_path", lambda: str(tmp_path / "absent.so"))
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         capi.load()
+
+
+def test_create_needs_opt_in_for_substituted_solvers(lib):
+    """Solvers the GPU does not have (velocity LU, pressure Gauss-Seidel /
+    Jacobi / LU) are an explicit request: without substitute_solvers the
+    description is refused before any device work (no GPU needed)."""
+    ctx = ctypes.c_void_p()
+    for field, value in (("velocity_solver", capi.LINEAR_LU),
+                         ("pressure_solver", capi.LINEAR_GAUSS_SEIDEL),
+                         ("pressure_solver", capi.LINEAR_JACOBI),
+                         ("pressure_solver", capi.LINEAR_LU)):
+        d = capi.default_desc()
+        setattr(d, field, value)
+        assert lib.hydro_gpu_create(ctypes.byref(d), ctypes.byref(ctx)) == capi.ERR_UNSUPPORTED
+    d = capi.default_desc()
+    d.velocity_solver = 17
+    assert lib.hydro_gpu_create(ctypes.byref(d), ctypes.byref(ctx)) == capi.ERR_ARG
+    # with the opt-in the description passes validation (and without a GPU
+    # here stops at the device check)
+    d = capi.default_desc()
+    d.velocity_solver = capi.LINEAR_LU
+    d.substitute_solvers = 1
+    st = lib.hydro_gpu_create(ctypes.byref(d), ctypes.byref(ctx))
+    assert st in (capi.ERR_NO_DEVICE, capi.OK)
+    if st == capi.OK:
+        lib.hydro_gpu_destroy(ctx)

@@ -7,9 +7,10 @@ device synchronisation or out-of-memory failure.  It solves the same rows
 as hydro_gpu_stencil_solve but takes its scratch from a fixed device array
 of the library instead of a caller workspace.
 
-Two calls in a row (a 2D singular system, then a 3D system with a pinned
-cell), each through the C-ABI, must give the existing entry point's answer
-within the tolerance of the other stencil-solve tests.  This file is named
+Two calls in a row on each of two systems (a 2D singular system, then a 3D
+system with a pinned cell), each through the C-ABI, must give the existing
+entry point's answer within the tolerance of the other stencil-solve tests;
+the second call of each must leave the device's free memory unchanged.  This file is named
 so that pytest collects it last; it also passes alone in a fresh process.
 """
 import ctypes
@@ -55,18 +56,30 @@ def test_noalloc_matches_workspace_solve_twice(built):
                                            dc.data_ptr(), x_ref.data_ptr(), 0, 1e-12, 5000,
                                            ws.data_ptr(), None, ctypes.byref(it_a),
                                            ctypes.byref(res_a))
-        it_b, res_b = ctypes.c_int(), ctypes.c_double()
-        st_b = lib.hydro_gpu_stencil_solve_noalloc(dim, n[0], n[1], nz, dk.data_ptr(), 0.0, pin,
-                                                   pval, dc.data_ptr(), x_new.data_ptr(), 0,
-                                                   1e-12, 5000, None, ctypes.byref(it_b),
-                                                   ctypes.byref(res_b))
-        torch.cuda.synchronize()
-        assert st_a == capi.OK and st_b == capi.OK, (st_a, st_b)
         a = x_ref.cpu().numpy()
-        b = x_new.cpu().numpy()
-        rel = np.linalg.norm(b - a) / np.linalg.norm(a)
-        assert rel <= 1e-9, (dim, n, rel)
-        assert res_b.value <= 1e-12 and it_b.value == it_a.value
+        assert st_a == capi.OK, st_a
+        for call in range(2):
+            # the second call of a case (every kernel it launches already
+            # loaded) must leave the device's free memory and torch's
+            # allocations unchanged: the entry point allocates nothing
+            x_new.fill_(0.0)
+            torch.cuda.synchronize()
+            free0 = torch.cuda.mem_get_info()[0]
+            held0 = torch.cuda.memory_allocated()
+            it_b, res_b = ctypes.c_int(), ctypes.c_double()
+            st_b = lib.hydro_gpu_stencil_solve_noalloc(dim, n[0], n[1], nz, dk.data_ptr(), 0.0,
+                                                       pin, pval, dc.data_ptr(), x_new.data_ptr(),
+                                                       0, 1e-12, 5000, None, ctypes.byref(it_b),
+                                                       ctypes.byref(res_b))
+            torch.cuda.synchronize()
+            if call == 1:
+                assert torch.cuda.mem_get_info()[0] == free0
+                assert torch.cuda.memory_allocated() == held0
+            assert st_b == capi.OK, st_b
+            b = x_new.cpu().numpy()
+            rel = np.linalg.norm(b - a) / np.linalg.norm(a)
+            assert rel <= 1e-9, (dim, n, call, rel)
+            assert res_b.value <= 1e-12 and it_b.value == it_a.value
 
 
 def test_noalloc_rejects_oversize(built):
