@@ -14,6 +14,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["fluid.cu", "linear.cu", "mg.cu", "advection.cu", "control.cu", "context.cu", "heat.cu",
+           "conv.cu", "net.cu",
            "noalloc.cu", "output.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
@@ -30,7 +31,8 @@ def _compile(src):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
     srcp = os.path.join(CSRC, src)
     deps = [srcp] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
-    deps.append(os.path.join(ROOT, "include", "hydro_gpu.h"))
+    inc = os.path.join(ROOT, "include")
+    deps += [os.path.join(inc, h) for h in os.listdir(inc) if h.endswith(".h")]
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc()] + ARCH + NVCC_FLAGS + ["-c", srcp, "-o", obj]

@@ -35,14 +35,14 @@ FP64, MIXED = range(2)
 (F_VELOCITY, F_PRESSURE, F_VOLUME_FLUX, F_PARTIAL_DENSITY, F_VOLUME_FRACTION,
  F_DENSITY, F_VISCOSITY, F_FORCE, F_VOLUME_SOURCE, F_MASS_SOURCE,
  F_PRESSURE_CORRECTION, F_DIAG_COEFF, F_SURFACE_FORCE, F_TEMPERATURE,
- F_CONDUCTIVITY) = range(15)
+ F_CONDUCTIVITY, F_PRESSURE_RHS) = range(16)
 VECTOR_FIELDS = (F_VELOCITY, F_FORCE, F_SURFACE_FORCE)
 # enum hydro_layer (solver::Layers order)
 TIME_CURR, TIME_PREV, ITER_CURR, ITER_PREV = range(4)
 # enum hydro_prof_group
 PROF_GROUPS = ["vel_grad", "force", "mom_assemble", "mom_sweep", "rhie_chow", "pressure_rhs",
                "cg_init", "cg_spmv", "cg_update", "cg_dir", "ir_residual", "correct",
-               "adv_faces", "adv_update", "props", "mg_vcycle", "other"]
+               "adv_faces", "adv_update", "props", "mg_vcycle", "other", "guess"]
 
 
 class HydroDesc(ctypes.Structure):
@@ -371,11 +371,32 @@ def _declare(lib, prefix):
             "hydro_scalar_output_open": [P, C, ctypes.POINTER(P)],
             "hydro_scalar_output_write": [P, ctypes.c_double, I],
             "hydro_scalar_output_close": [P],
+            # learned pressure guess (include/hydro_net.h)
+            "hydro_net_create": [I, I, I, I, ctypes.c_ulonglong, ctypes.POINTER(P)],
+            "hydro_net_destroy": [P],
+            "hydro_net_num_params": [P, ctypes.POINTER(ctypes.c_size_t)],
+            "hydro_net_get_params": [P, ctypes.POINTER(ctypes.c_float), ctypes.c_size_t],
+            "hydro_net_set_params": [P, ctypes.POINTER(ctypes.c_float), ctypes.c_size_t],
+            "hydro_net_pack_sample": [P, P, P, P, ctypes.c_double, P, P],
+            "hydro_net_train_step": [P, ctypes.POINTER(P), I, ctypes.c_double, D, P],
+            "hydro_net_gradient": [P, ctypes.POINTER(P), I, ctypes.POINTER(ctypes.c_float),
+                                   ctypes.c_size_t, D, P],
+            "hydro_net_eval_loss": [P, ctypes.POINTER(P), I, D, P],
+            "hydro_net_predict": [P, P, P, ctypes.c_double, P, P],
+            "hydro_net_last_predict": [P, D, ctypes.POINTER(I)],
+            "hydro_gpu_set_pressure_guess": [P, P, I, ctypes.c_double],
+            "hydro_gpu_get_guess_stats": [P, ctypes.POINTER(ctypes.c_longlong),
+                                          ctypes.POINTER(ctypes.c_longlong)],
+            "hydro_conv3d_forward": [I, I, I, I, I, I, P, P, P, P, I, P, P],
+            "hydro_conv3d_backward_data": [I, I, I, I, I, I, P, P, P, P, P, P],
+            "hydro_conv3d_backward_weight": [I, I, I, I, I, I, P, P, P, P, P],
         }
         for name, args in extra.items():
             fn = getattr(lib, name)
             fn.argtypes = args
             fn.restype = I
+        lib.hydro_net_sample_bytes.argtypes = [P]
+        lib.hydro_net_sample_bytes.restype = ctypes.c_size_t
     else:
         stencil.argtypes = [I, I, I, I, D, ctypes.c_double, ctypes.c_long,
                             ctypes.c_double, D, D, I, ctypes.c_double, I,

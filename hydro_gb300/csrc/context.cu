@@ -25,7 +25,14 @@
 #include <vector>
 
 #include "../../include/hydro_gpu.h"
+#include "../../include/hydro_net.h"
 #include "kernels.h"
+
+// the network of the learned pressure guess (net.cu)
+int net_predict_async(hydro_net* net, const double* rhs, const double* rho, double rho_scale,
+                      double* out, cudaStream_t st);
+int net_check_grid(const hydro_net* net, int dim, const int* n);
+int net_error(hydro_net* net, cudaStream_t st);
 #include "loop.cuh"
 
 using namespace hg;
@@ -33,6 +40,7 @@ using namespace hg;
 namespace hg {
 static std::atomic<long long> g_launches{0};
 void count_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_total() { return g_launches.load(); }
 
 int resident_ctas(const void* kernel) {
   static std::mutex mu;
@@ -232,6 +240,10 @@ struct hydro_ctx {
   int iter_count = 0, cd_iter_count = 0;
   int vel_sweeps = 0, p_iters = 0;
   int p_unconv = 0;  // pressure solves of the step that stopped above their tolerance
+  // learned initial guess of the first net_iters pressure solves of a step
+  hydro_net* net = nullptr;
+  int net_iters = 0;
+  double net_rho_scale = 1.;
   double p_res = 0., indicator = 1.;
   int du_cur = 0;
   int status = HYDRO_OK;
@@ -576,9 +588,25 @@ int heat_step(hydro_ctx* x) {
 }
 
 // ------------------------------------------------------------- pressure --
+// The network's initial guess of the refinement iterate x->pc, after the
+// residual of the zero guess (RS_IR_RR = ||f'||^2) has been reduced:
+// predict, project (singular), Galerkin-scale, its residual, keep or drop.
+int apply_guess(hydro_ctx* x, int singular) {
+  const Mesh& m = x->m;
+  PcgWork& w = x->pw;
+  CK(launch_store_ff(w.ds, x->st));
+  int rc = net_predict_async(x->net, x->prhs, x->rho, x->net_rho_scale, x->pc, x->st);
+  if (rc) return rc;
+  if (singular) CK(sub_mean(m, x->pc, w, x->st));
+  CK(guess_scale(m, x->kf, x->prhs, x->pc, singular, w, x->st));
+  CK(ir_residual(m, x->kf, x->prhs, x->pc, singular, w, x->st));
+  CK(guess_accept(m, x->prhs, x->pc, singular, w, x->st));
+  return HYDRO_OK;
+}
+
 // Graph-captured form of the pressure solve: the refinement and Krylov loops
 // become WHILE nodes steered by the control kernels.
-int solve_pressure_graph(hydro_ctx* x, int singular, int mixed) {
+int solve_pressure_graph(hydro_ctx* x, int singular, int mixed, bool apply_pin_guess) {
   const hydro_desc& d = x->d;
   const Mesh& m = x->m;
   PcgWork& w = x->pw;
@@ -608,6 +636,20 @@ int solve_pressure_graph(hydro_ctx* x, int singular, int mixed) {
     CK(ir_residual(m, x->kf, x->prhs, nullptr, singular, w, x->st));
     CK(launch_ctl_refine(w.ds, d.pressure_tolerance, inner_min, d.pressure_iters_limit, hr, 1,
                          x->st));
+    if (x->net && x->net_iters > 0 && apply_pin_guess) {
+      // the learned guess, for the first net_iters SIMPLE iterations
+      cudaGraphConditionalHandle hg2;
+      if ((rc = new_handle(x, 0, &hg2))) return rc;
+      CK(launch_ctl_guess_gate(w.ds, x->net_iters, hg2, x->st));
+      rc = add_if(x, hg2, [&]() -> int {
+        int r;
+        if ((r = apply_guess(x, singular))) return r;
+        CK(launch_ctl_guess(w.ds, d.pressure_tolerance, inner_min, d.pressure_iters_limit, hr,
+                            x->st));
+        return HYDRO_OK;
+      });
+      if (rc) return rc;
+    }
     rc = add_while(x, hr, [&]() -> int {
       int r;
       if (mgcg) CK(mgcg_init(m, 0., 1, w, x->mg, x->st));
@@ -646,7 +688,7 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
   // still solved to the FP64 tolerance; only the inner corrections are FP32)
   int mixed = (d.precision == HYDRO_MIXED) || d.pressure_solver == HYDRO_LINEAR_MGCG;
   CK(pcg_prepare(m, x->kf, 0., w, mixed, x->st));
-  if (x->graph_mode) return solve_pressure_graph(x, singular, mixed);
+  if (x->graph_mode) return solve_pressure_graph(x, singular, mixed, apply_pin);
   int rc;
   if (!mixed) {
     w.limit = d.pressure_iters_limit;
@@ -665,6 +707,7 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
     x->p_iters += it;
     double ff = x->hds->red[RS_PCG_FF];
     x->p_res = ff > 0. ? sqrt(x->hds->red[RS_PCG_RR] / ff) : 0.;
+    if (std::isnan(x->hds->red[RS_PCG_RR])) return HYDRO_ERR_NAN;
     if (!(x->hds->red[RS_PCG_RR] <= x->hds->red[RS_PCG_TOL2])) x->p_unconv++;
   } else {
     // FP64 iterative refinement around an FP32 PCG (Jacobi or multigrid
@@ -682,7 +725,17 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
       rc = sync_scalars(x);
       if (rc) return rc;
       double rr = x->hds->red[RS_IR_RR];
+      if (std::isnan(rr)) return HYDRO_ERR_NAN;  // a NaN in the system (fluid.hpp:1164-1166)
       if (ff < 0.) ff = rr;
+      if (outer == 0 && apply_pin && x->net && x->iter_count < x->net_iters && ff > 0.) {
+        // start from the network's guess when it beats the zero guess
+        x->prof.begin(HYDRO_PROF_GUESS, x->st);
+        rc = apply_guess(x, singular);
+        x->prof.end(HYDRO_PROF_GUESS, x->st);
+        if (rc) return rc;
+        if ((rc = sync_scalars(x))) return rc;
+        rr = x->hds->red[RS_IR_RR];
+      }
       x->p_res = ff > 0. ? sqrt(rr / ff) : 0.;
       if (ff == 0. || rr <= d.pressure_tolerance * d.pressure_tolerance * ff) {
         conv = true;
@@ -747,6 +800,7 @@ int fluid_field(hydro_ctx* x, int field, int layer, double** ptr, long long* n) 
     case HYDRO_FIELD_VOLUME_SOURCE: *ptr = x->Sv; return HYDRO_OK;
     case HYDRO_FIELD_MASS_SOURCE: *ptr = x->Sm; return HYDRO_OK;
     case HYDRO_FIELD_PRESSURE_CORRECTION: *ptr = x->pc; return HYDRO_OK;
+    case HYDRO_FIELD_PRESSURE_RHS: *ptr = x->prhs; return HYDRO_OK;
     case HYDRO_FIELD_DIAG_COEFF: *ptr = x->Dc; return HYDRO_OK;
     case HYDRO_FIELD_SURFACE_FORCE: *ptr = x->stforce; *n = m.nc * x->dim; return HYDRO_OK;
     case HYDRO_FIELD_TEMPERATURE:
@@ -1573,7 +1627,7 @@ int enqueue_step_body(hydro_ctx* x, int substeps) {
   double* q0 = x->q;
     int r;
     if ((r = reset_flags(x, FL_STEP_SWEEPS, 3))) return r;  // sweeps, p iterations, SIMPLE
-    if ((r = reset_flags(x, FL_STEP_PUNCONV, 1))) return r;
+    if ((r = reset_flags(x, FL_STEP_PUNCONV, 2))) return r;  // unconverged solves, NaN
     if ((r = hydro_gpu_start_step(x))) return r;
     const int limit = d.num_iterations_limit;
     const double tol = d.convergence_tolerance;
@@ -1718,7 +1772,7 @@ int finish_graph_step(hydro_ctx* x, int substeps, double adv_end, hydro_step_sta
   s.time = x->time;
   x->p_unconv = h.flag[FL_STEP_PUNCONV];
   s.pressure_unconverged = x->p_unconv;
-  s.status = (h.red[RS_NAN] > 0. || isnan(x->indicator)) ? HYDRO_ERR_NAN
+  s.status = (h.red[RS_NAN] > 0. || isnan(x->indicator) || h.flag[FL_STEP_NAN]) ? HYDRO_ERR_NAN
              : x->p_unconv                                 ? HYDRO_NOT_CONVERGED
                                                            : HYDRO_OK;
   if (stats) *stats = s;
@@ -2107,6 +2161,41 @@ int hydro_gpu_stencil_solve(int dim, int nx, int ny, int nz, const double* face_
   // iteration with a NaN residual: reported, never taken as converged
   if (std::isnan(rr) || std::isnan(ff)) return HYDRO_ERR_NAN;
   return (ff > 0. && rr > tolerance * tolerance * ff) ? HYDRO_NOT_CONVERGED : HYDRO_OK;
+}
+
+// ------------------------------------------------- learned guess ------
+int hydro_gpu_set_pressure_guess(hydro_ctx* x, hydro_net* net, int iterations,
+                                 double rho_scale) {
+  if (!x || iterations < 0 || !(rho_scale > 0.)) return HYDRO_ERR_ARG;
+  if (!net || iterations == 0) {
+    x->net = nullptr;
+    x->net_iters = 0;
+    return HYDRO_OK;
+  }
+  const bool refine = x->d.precision == HYDRO_MIXED || x->d.pressure_solver == HYDRO_LINEAR_MGCG;
+  if (!refine || !net_check_grid(net, x->dim, x->m.n)) return HYDRO_ERR_UNSUPPORTED;
+  // one forward pass outside any capture: kernel attributes and module
+  // loading happen here, not inside a captured step
+  int rc = net_predict_async(net, x->prhs, x->rho, rho_scale, x->pc, x->st);
+  if (rc) return rc;
+  if ((rc = net_error(net, x->st))) return rc;
+  x->net = net;
+  x->net_iters = iterations;
+  x->net_rho_scale = rho_scale;
+  if (x->sg.exec) {  // a captured step without (or with another) guess
+    cudaGraphExecDestroy(x->sg.exec);
+    x->sg.exec = nullptr;
+  }
+  return HYDRO_OK;
+}
+
+int hydro_gpu_get_guess_stats(hydro_ctx* x, long long* used, long long* dropped) {
+  if (!x) return HYDRO_ERR_ARG;
+  int rc = sync_scalars(x);
+  if (rc) return rc;
+  if (used) *used = x->hds->flag[FL_GUESS_USED];
+  if (dropped) *dropped = x->hds->flag[FL_GUESS_DROPPED];
+  return reset_flags(x, FL_GUESS_USED, 2);
 }
 
 }  // extern "C"

@@ -46,6 +46,7 @@ __global__ void k_ctl_krylov_done(DevScalars* ds) {
   ds->red[RS_P_RES] = ff > 0. ? sqrt(ds->red[RS_PCG_RR] / ff) : 0.;
   ds->flag[FL_STEP_PITERS] += ds->flag[FL_PCG_ITERS];
   if (!(ds->red[RS_PCG_RR] <= ds->red[RS_PCG_TOL2])) ds->flag[FL_STEP_PUNCONV] += 1;
+  if (isnan(ds->red[RS_PCG_RR])) ds->flag[FL_STEP_NAN] = 1;
 }
 
 // Iterative refinement (the mixed pressure solve): called after every FP64
@@ -69,6 +70,7 @@ __global__ void k_ctl_refine(DevScalars* ds, double tol, double inner_min, int l
   }
   double ff = ds->red[RS_IR_FF];
   ds->red[RS_P_RES] = ff > 0. ? sqrt(rr / ff) : 0.;
+  if (isnan(rr)) ds->flag[FL_STEP_NAN] = 1;  // a NaN in the system (fluid.hpp:1164-1166)
   int conv = (ff == 0. || rr <= tol * tol * ff);
   int cont = !conv && !isnan(rr) && total < limit && ds->flag[FL_IR_OUTER] < 50;
   if (cont) {
@@ -79,6 +81,32 @@ __global__ void k_ctl_refine(DevScalars* ds, double tol, double inner_min, int l
     ds->flag[FL_STEP_PUNCONV] += 1;  // stopped at a limit (or NaN) above the tolerance
   }
   decide(ds, cont, h, use);
+}
+
+__global__ void k_ctl_guess_gate(DevScalars* ds, int limit, cudaGraphConditionalHandle h) {
+  if (threadIdx.x != 0) return;
+  cudaGraphSetConditional(h, ds->flag[FL_ITERS] < limit ? 1u : 0u);
+}
+
+// The refinement loop's first decision, again, from the residual of the
+// accepted guess (no inner iterations yet: the whole limit is left).
+__global__ void k_ctl_guess(DevScalars* ds, double tol, double inner_min, int limit,
+                            cudaGraphConditionalHandle h) {
+  if (threadIdx.x != 0) return;
+  const double rr = ds->red[RS_IR_RR], ff = ds->red[RS_IR_FF];
+  ds->red[RS_P_RES] = ff > 0. ? sqrt(rr / ff) : 0.;
+  const int conv = (ff == 0. || rr <= tol * tol * ff);
+  const int cont = !conv && !isnan(rr) && limit > 0;
+  if (cont) {
+    const double t = 0.5 * tol * sqrt(ff / rr);
+    ds->red[RS_INNER_TOL] = t > inner_min ? t : inner_min;
+    ds->flag[FL_PCG_LIMIT] = limit;
+  }
+  decide(ds, cont, h, 1);
+}
+
+__global__ void k_store_ff(DevScalars* ds) {
+  if (threadIdx.x == 0) ds->red[RS_IR_FF] = ds->red[RS_IR_RR];
 }
 
 __global__ void k_ctl_simple(DevScalars* ds, int limit, double tol,
@@ -162,6 +190,26 @@ cudaError_t launch_ctl_krylov(DevScalars* ds, cudaGraphConditionalHandle h, int 
 cudaError_t launch_ctl_refine(DevScalars* ds, double tol, double inner_min, int limit,
                               cudaGraphConditionalHandle h, int use, cudaStream_t st) {
   k_ctl_refine<<<1, 32, 0, st>>>(ds, tol, inner_min, limit, h, use);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ctl_guess_gate(DevScalars* ds, int limit, cudaGraphConditionalHandle h,
+                                  cudaStream_t st) {
+  k_ctl_guess_gate<<<1, 32, 0, st>>>(ds, limit, h);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ctl_guess(DevScalars* ds, double tol, double inner_min, int limit,
+                             cudaGraphConditionalHandle h, cudaStream_t st) {
+  k_ctl_guess<<<1, 32, 0, st>>>(ds, tol, inner_min, limit, h);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_store_ff(DevScalars* ds, cudaStream_t st) {
+  k_store_ff<<<1, 32, 0, st>>>(ds);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -74,7 +74,8 @@ enum {
   RS_IR_FF = 17,         // refinement: ||f||^2 of the first residual
   RS_OUT_FLUX = 18, RS_OUT_AREA = 19, RS_IN_FLUX = 20,  // outlet rebalancing sums
   RS_HEAT_DIFF = 21,     // max |update| of the last temperature sweep
-  RS_MOM_DIFF_RED = 22   // max |update| of the red half of a Gauss-Seidel sweep
+  RS_MOM_DIFF_RED = 22,  // max |update| of the red half of a Gauss-Seidel sweep
+  RS_GUESS_S0 = 23, RS_GUESS_S1 = 24  // <x, f'>, <x, A x> of a learned initial guess
 };
 enum {
   FL_MOM_DONE = 0, FL_MOM_SWEEPS = 1, FL_PCG_DONE = 2, FL_PCG_ITERS = 3, FL_NAN = 4,
@@ -87,13 +88,15 @@ enum {
   FL_IR_OUTER = 11,      // refinement cycles
   FL_CONT = 12,          // last loop decision
   FL_HEAT_DONE = 13, FL_HEAT_SWEEPS = 14,  // temperature solve
-  FL_STEP_PUNCONV = 15   // pressure solves of the step that stopped above their tolerance
+  FL_STEP_PUNCONV = 15,  // pressure solves of the step that stopped above their tolerance
+  FL_STEP_NAN = 16,      // a pressure solve of the step met a NaN residual
+  FL_GUESS_USED = 17, FL_GUESS_DROPPED = 18  // learned initial guesses kept / dropped
 };
 enum {
   TK_MOM = 0, TK_PCG_A = 1, TK_PCG_B = 2, TK_PCG_INIT = 3, TK_IND = 4, TK_DT = 5,
   TK_MEAN = 6, TK_MEAN2 = 7, TK_STAT = 8, TK_STAT2 = 9, TK_STAT3 = 10, TK_IR = 11,
   TK_NAN = 12, TK_PCG_INIT2 = 13, TK_F32_A = 14, TK_F32_B = 15, TK_F32_INIT = 16,
-  TK_OUTLET = 17, TK_HEAT = 18, TK_MOM_RED = 19
+  TK_OUTLET = 17, TK_HEAT = 18, TK_MOM_RED = 19, TK_GUESS = 20
 };
 
 // ---------------------------------------------------------------- fluid --
@@ -275,6 +278,8 @@ struct Profiler {
 };
 // Kernel launches issued by this library since load (all contexts).
 void count_launches(int n);
+// Kernels this library enqueued so far (every launcher counts its own).
+long long launch_total();
 
 struct PcgWork {
   double *r, *z, *p, *Ap, *dg, *idg;                     // FP64 vectors
@@ -303,6 +308,16 @@ cudaError_t sub_mean(const Mesh& m, double* x, PcgWork& w, cudaStream_t st);
 // tolerance, x += e.
 cudaError_t ir_residual(const Mesh& m, const double* kf, const double* f, const double* x,
                         int singular, PcgWork& w, cudaStream_t st);
+// Learned initial guess x of A x = f' (pc of the refinement): Galerkin
+// scaling x *= alpha, alpha = <x, f'> / <x, A x> (x = 0 when alpha is not
+// positive and finite), then -- after ir_residual(x) -- keep it only when its
+// residual is below ||f'|| (ds->red[RS_IR_FF]); otherwise x = 0 and the
+// residual vector and RS_IR_RR are those of the zero guess.  Counts in
+// FL_GUESS_USED / FL_GUESS_DROPPED.
+cudaError_t guess_scale(const Mesh& m, const double* kf, const double* f, double* x, int singular,
+                        PcgWork& w, cudaStream_t st);
+cudaError_t guess_accept(const Mesh& m, const double* f, double* x, int singular, PcgWork& w,
+                         cudaStream_t st);
 // Inner-solve start.  dev_params = 0: tolerance `tol` and limit `w.limit`
 // from the host (stored on the device); 1: both already on the device
 // (RS_INNER_TOL, FL_PCG_LIMIT, set by launch_ctl_refine).
@@ -393,6 +408,15 @@ cudaError_t launch_ctl_krylov(DevScalars* ds, cudaGraphConditionalHandle h, int 
 cudaError_t launch_ctl_refine(DevScalars* ds, double tol, double inner_min, int limit,
                               cudaGraphConditionalHandle h, int use, cudaStream_t st);
 // End of a FP64 Krylov solve: RS_P_RES and FL_STEP_PITERS.
+// Learned guess in a captured step: the IF node around it runs while the
+// SIMPLE iteration count of the step is below `limit`; after the guess, the
+// refinement loop's condition is decided again from the guess's residual.
+cudaError_t launch_ctl_guess_gate(DevScalars* ds, int limit, cudaGraphConditionalHandle h,
+                                  cudaStream_t st);
+cudaError_t launch_ctl_guess(DevScalars* ds, double tol, double inner_min, int limit,
+                             cudaGraphConditionalHandle h, cudaStream_t st);
+// RS_IR_FF = RS_IR_RR (the residual of the zero guess, before a guess).
+cudaError_t launch_store_ff(DevScalars* ds, cudaStream_t st);
 cudaError_t launch_ctl_krylov_done(DevScalars* ds, cudaStream_t st);
 // SIMPLE loop after an iteration: FL_ITERS += 1; continue while below
 // `limit` and the indicator is not below `tol`.

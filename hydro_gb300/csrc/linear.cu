@@ -227,6 +227,66 @@ __global__ void __launch_bounds__(NT) k_ir_residual(Mesh m, const double* kf, co
     if (threadIdx.x == 0 && threadIdx.y == 0) ds->red[RS_IR_RR] = o[0];
 }
 
+// <x, f'> and <x, A x> of a guess x (f' = f - mean on a singular system).
+template <int DIM, bool PER>
+__global__ void __launch_bounds__(NT) k_guess_dots(Mesh m, const double* kf, const double* dg,
+                                                   const double* f, const double* fmean,
+                                                   const double* x, long long pin,
+                                                   double* partials, DevScalars* ds, int kch) {
+  double s[2] = {0., 0.};
+  const double mean = fmean ? *fmean : 0.;
+  CELL_LOOP_BEGIN(m, kch)
+  const double fc = EXCLUDED() ? f[X.c] : f[X.c] - mean;
+  const double xc = x[X.c];
+  s[0] += xc * fc;
+  s[1] += xc * stencil_row<DIM, PER>(m, X, kf, dg, x, pin);
+  CELL_LOOP_END
+  __shared__ double o[2];
+  if (grid_reduce<RED_SUM, 2>(s, partials, &ds->ticket[TK_GUESS], o)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      ds->red[RS_GUESS_S0] = o[0];
+      ds->red[RS_GUESS_S1] = o[1];
+    }
+  }
+}
+
+__global__ void k_guess_scale(long long n, double* x, const DevScalars* ds) {
+  double a = ds->red[RS_GUESS_S0] / ds->red[RS_GUESS_S1];
+  if (!(a > 0. && a < 1e300)) a = 0.;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] *= a;
+}
+
+// After the residual of the scaled guess: keep it when its residual is
+// below that of the zero guess, else restore x = 0, r = f' and RS_IR_RR.
+__global__ void k_guess_accept(long long n, const unsigned char* ex, const double* f,
+                               const double* fmean, double* x, double* r, DevScalars* ds) {
+  const double a = ds->red[RS_GUESS_S0] / ds->red[RS_GUESS_S1];
+  const bool keep = (a > 0. && a < 1e300) && ds->red[RS_IR_RR] < ds->red[RS_IR_FF];
+  if (!keep) {
+    const double mean = fmean ? *fmean : 0.;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+      x[i] = 0.;
+      r[i] = (ex && ex[i]) ? f[i] : f[i] - mean;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (keep) {
+      ds->flag[FL_GUESS_USED] += 1;
+    } else {
+      ds->flag[FL_GUESS_DROPPED] += 1;
+    }
+  }
+}
+
+__global__ void k_guess_rr(DevScalars* ds) {
+  const double a = ds->red[RS_GUESS_S0] / ds->red[RS_GUESS_S1];
+  const bool keep = (a > 0. && a < 1e300) && ds->red[RS_IR_RR] < ds->red[RS_IR_FF];
+  if (threadIdx.x == 0 && !keep) ds->red[RS_IR_RR] = ds->red[RS_IR_FF];
+}
+
 int flat_blocks_l(long long n) {
   long long b = (n + NT - 1) / NT;
   if (b > kMaxBlocks) b = kMaxBlocks;
@@ -312,6 +372,27 @@ cudaError_t ir_residual(const Mesh& m, const double* kf, const double* f, const 
   LAUNCH_DIM(k_ir_residual, m, kf, w.dg, f, msum, x, w.pin, w.r, w.partials, w.ds);
   if (w.prof) w.prof->end(PG_IR_RESIDUAL, st);
   count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t guess_scale(const Mesh& m, const double* kf, const double* f, double* x, int singular,
+                        PcgWork& w, cudaStream_t st) {
+  Launch L = cell_launch(m);
+  const double* msum = singular ? &w.ds->red[RS_MEAN] : nullptr;
+  LAUNCH_DIM(k_guess_dots, m, kf, w.dg, f, msum, x, w.pin, w.partials, w.ds);
+  k_guess_scale<<<flat_blocks_l(m.nc), NT, 0, st>>>(m.nc, x, w.ds);
+  count_launches(2);
+  return cudaGetLastError();
+}
+
+cudaError_t guess_accept(const Mesh& m, const double* f, double* x, int singular, PcgWork& w,
+                         cudaStream_t st) {
+  const double* msum = singular ? &w.ds->red[RS_MEAN] : nullptr;
+  // RS_IR_RR is rewritten only by the next kernel, after every block of
+  // k_guess_accept has read it
+  k_guess_accept<<<flat_blocks_l(m.nc), NT, 0, st>>>(m.nc, m.ex, f, msum, x, w.r, w.ds);
+  k_guess_rr<<<1, 32, 0, st>>>(w.ds);
+  count_launches(2);
   return cudaGetLastError();
 }
 

@@ -83,6 +83,12 @@ class Hydro:
         self._call("field_ptr", field, layer, ctypes.byref(p))
         return ctypes.cast(p, ctypes.c_void_p).value
 
+    def stream_ptr(self):
+        """The context's cudaStream_t (hydro_gpu_get_stream)."""
+        p = ctypes.c_void_p()
+        self._call("get_stream", ctypes.byref(p))
+        return p.value
+
     def GetVelocity(self, layer="time_curr"):
         return self.get_field(capi.F_VELOCITY, Layers[layer]).reshape(self.dim, self.nc)
 

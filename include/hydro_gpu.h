@@ -121,8 +121,12 @@ enum hydro_field {
   HYDRO_FIELD_TEMPERATURE = 13,    /* cells, layers TIME_CURR / TIME_PREV, after
                                       hydro_gpu_heat_create (HeatSolver::GetTemperature,
                                       heat.hpp:88-93) */
-  HYDRO_FIELD_CONDUCTIVITY = 14    /* cells, after hydro_gpu_heat_create: mixture
+  HYDRO_FIELD_CONDUCTIVITY = 14,   /* cells, after hydro_gpu_heat_create: mixture
                                       conductivity (fc_conductivity, hydro2d.hpp:1428) */
+  HYDRO_FIELD_PRESSURE_RHS = 15    /* cells: right-hand side f of the last pressure-
+                                      correction solve, A p' = f (the pinned row
+                                      included); with PRESSURE_CORRECTION and DENSITY
+                                      the snapshot the learned guess trains on */
 };
 
 /* Same order as solver::Layers (solver.hpp:762). */
@@ -482,6 +486,7 @@ enum hydro_prof_group {
   HYDRO_PROF_CG_UPDATE, HYDRO_PROF_CG_DIR, HYDRO_PROF_IR_RESIDUAL, HYDRO_PROF_CORRECT,
   HYDRO_PROF_ADV_FACES, HYDRO_PROF_ADV_UPDATE, HYDRO_PROF_PROPS, HYDRO_PROF_MG_VCYCLE,
   HYDRO_PROF_OTHER,
+  HYDRO_PROF_GUESS,  /* learned initial guess of a pressure solve (hydro_net.h) */
   HYDRO_PROF_COUNT
 };
 int hydro_gpu_set_profiling(hydro_ctx* ctx, int on);
