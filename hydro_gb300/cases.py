@@ -266,3 +266,25 @@ def channel(nx=40, ny=20, nz=1, dim=2, length=2.0, u_in=1.0, mu=0.01, dt=1e-2, r
     else:
         q0 = np.ones(nc) * d.density[0]
     return d, u0, q0
+
+
+def hydrostatic_pressure(desc, rho):
+    """Pressure in hydrostatic balance with the cell density rho (raw order)
+    for gravity along one axis: dp/dx_a = rho g_a integrated cell to cell
+    with the face density (the mean of the two cells), zero mean.  The
+    fluid at rest then starts without the one-off pressure build-up of its
+    first step.  Zeros when gravity is zero or not along one axis."""
+    dim = desc.dim
+    g = [desc.gravity[k] for k in range(dim)]
+    axes = [k for k in range(dim) if g[k] != 0.0]
+    shape = tuple(desc.n[k] for k in reversed(range(dim)))
+    if len(axes) != 1:
+        return np.zeros(int(np.prod(shape)))
+    a = axes[0]
+    ax = dim - 1 - a  # numpy axis of direction a (arrays are (z,) y, x)
+    r = np.asarray(rho, dtype=np.float64).reshape(shape)
+    h = (desc.hi[a] - desc.lo[a]) / desc.n[a]
+    face = 0.5 * (r.take(range(1, shape[ax]), axis=ax) + r.take(range(0, shape[ax] - 1), axis=ax))
+    inc = np.cumsum(face * (g[a] * h), axis=ax)
+    p = np.concatenate([np.zeros_like(r.take([0], axis=ax)), inc], axis=ax)
+    return (p - p.mean()).ravel()
