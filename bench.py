@@ -582,6 +582,40 @@ def run_reference(args, rank, world):
     print(json.dumps(out))
 
 
+def run_profile_case(args):
+    """A short, bounded run of the hot path for profiler captures: the
+    rising-drops case at --n^3, one time step of --outer SIMPLE iterations
+    with at most --cg-limit pressure-CG iterations per solve, then exit.  At
+    n = 150 the arrays of one CG iteration exceed the 129 MB L2 while the
+    context stays near 2 GB and the run issues a few hundred kernel launches:
+    small enough for ncu captures to end by themselves."""
+    from hydro_gb300 import capi
+    from hydro_gb300.solver import Hydro, launch_count
+    d, u0, q0, _ = workload(args.n, args.seed, args.precision, args.outer,
+                            "mgcg" if args.solver == "mgcg" else "cg")
+    d.velocity_iters_limit = 50
+    if args.velocity == "jacobi":
+        d.velocity_solver = capi.LINEAR_JACOBI
+    d.pressure_tolerance = 1e-30
+    d.pressure_iters_limit = args.cg_limit
+    if args.hydrostatic:
+        h = init_case(Hydro(d), d, u0, q0)
+    else:  # at rest with zero pressure
+        h = Hydro(d)
+        h.set_field(capi.F_VELOCITY, u0)
+        h.set_field(capi.F_PARTIAL_DENSITY, q0)
+        h.init_state()
+    if args.weights:
+        from hydro_gb300.net import Net, attach
+        from hydro_gb300.train_guess import RHO_SCALE
+        net = Net((args.n,) * 3, batch=1)
+        net.load(args.weights)
+        attach(h, net, 1, RHO_SCALE)
+    st = h.step()
+    print("profile case n=%d %s %s: %s launches=%d"
+          % (args.n, args.precision, args.solver, st, launch_count()))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -600,7 +634,24 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=150.0,
                     help="seconds of complete CPU steps (reference arm; the cpu_baseline leg "
                          "times one step)")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="one bounded step for profiler captures (see run_profile_case)")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="--profile-case: arithmetic of the SIMPLE iteration")
+    ap.add_argument("--solver", default="cg", choices=["cg", "mgcg"],
+                    help="--profile-case: pressure solver")
+    ap.add_argument("--cg-limit", type=int, default=40,
+                    help="--profile-case: pressure iterations per solve")
+    ap.add_argument("--velocity", default="gs", choices=["jacobi", "gs"],
+                    help="--profile-case: momentum sweeps")
+    ap.add_argument("--hydrostatic", action="store_true",
+                    help="--profile-case: start from the hydrostatic pressure (default: zero)")
+    ap.add_argument("--weights", default=None,
+                    help="--profile-case: attach the learned guess with these parameters")
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local = init_dist()

@@ -213,6 +213,13 @@ class FluidSimpleGpu : public FluidSolver<Mesh> {
         any = true;
       }
       if (any) {
+        // widen by a quarter cell: the library recomputes the centres with
+        // its own formula, which may differ from the mesh's in the last bit
+        for (size_t k = 0; k < dim; ++k) {
+          const double h = (d.hi[k] - d.lo[k]) / d.n[k];
+          lo[k] -= 0.25 * h;
+          hi[k] += 0.25 * h;
+        }
         for (auto c : mesh.Cells()) {
           Vect x = mesh.GetCenter(c);
           bool in = true;

@@ -14,7 +14,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["fluid.cu", "linear.cu", "mg.cu", "advection.cu", "control.cu", "context.cu", "heat.cu",
-           "conv.cu", "net.cu",
+           "conv.cu", "net.cu", "desc.cpp",
            "noalloc.cu", "output.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
@@ -28,7 +28,7 @@ def nvcc():
 
 
 def _compile(src):
-    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")  # .cu and host-only .cpp
     srcp = os.path.join(CSRC, src)
     deps = [srcp] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
     inc = os.path.join(ROOT, "include")

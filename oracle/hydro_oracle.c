@@ -486,6 +486,9 @@ static int pcg(const Mesh* m, const double* k, double shift, long pin,
   }
   for (long i = 0; i < n; ++i) r[i] = cex(m, i) ? f_in[i] : f_in[i] - mean;
   double fnorm = sqrt(dotp(n, r, r));
+  /* a NaN in the system is reported, as the library does (the reference's
+     Gauss-Seidel would carry it into p and throw, fluid.hpp:1164-1166) */
+  if (isnan(fnorm)) return HYDRO_ERR_NAN;
   if (!use_guess) {
     for (long i = 0; i < n; ++i) x[i] = 0.;
   } else {

@@ -245,11 +245,13 @@ def _ref_for(desc):
     return ref_lib(variants[per])
 
 
-def ref_run(desc, u0, q0, nsteps):
+def ref_run(desc, u0, q0, nsteps, variant=None):
     """Run the reference's own FluidSimple + AdvectionSolverMultiExplicit for
     nsteps steps; returns (u, p, F, q, stats list).  Periodic directions x
-    (and z in 3D) select the harness built with PERX (PERZ)."""
-    R = _ref_for(desc)
+    (and z in 3D) select the harness built with PERX (PERZ).  variant
+    "adapter": the harness with the reference-side adapter classes in their
+    place, the C-ABI forwarded to this oracle (oracle/adapter_shim.c)."""
+    R = ref_lib(variant) if variant else _ref_for(desc)
     nc, nf, dim = desc.ncells, desc.nfaces, desc.dim
     nph = desc.num_phases
     u0 = np.ascontiguousarray(u0, dtype=np.float64).ravel()

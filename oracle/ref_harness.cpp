@@ -36,6 +36,15 @@ static std::string IntToStr(size_t a) {
 
 #include "../include/hydro_gpu.h"
 
+// HYDRO_ADAPTER: the same harness with the reference-side adapter classes
+// (FluidSimpleGpu, AdvectionSolverMultiGpu) in place of FluidSimple and
+// AdvectionSolverMultiExplicit, constructed with the same arguments and
+// stepped through the same FluidSolver / AdvectionSolverMulti calls; linked
+// with adapter_shim.c, which forwards the C-ABI to the CPU oracle.
+#ifdef HYDRO_ADAPTER
+#include "../hydro_gb300/adapter/fluid_simple_gpu.hpp"
+#endif
+
 namespace {
 
 template <class Mesh>
@@ -62,8 +71,15 @@ struct Case {
   FieldFace<Vect> ff_stforce;
   std::vector<geom::MapFace<std::shared_ptr<solver::ConditionFace>>> v_cond;
   MultiTimer<std::string> timer;
-  std::shared_ptr<solver::FluidSimple<Mesh>> fluid;
-  std::shared_ptr<solver::AdvectionSolverMultiExplicit<Mesh, FieldFace<Scal>>> adv;
+#ifdef HYDRO_ADAPTER
+  using Fluid = solver::FluidSimpleGpu<Mesh>;
+  using Adv = solver::AdvectionSolverMultiGpu<Mesh>;
+#else
+  using Fluid = solver::FluidSimple<Mesh>;
+  using Adv = solver::AdvectionSolverMultiExplicit<Mesh, FieldFace<Scal>>;
+#endif
+  std::shared_ptr<Fluid> fluid;
+  std::shared_ptr<Adv> adv;
   // heat (hydro2d.hpp:650-687), when hd is given
   const hydro_heat_desc* hd = nullptr;
   FieldCell<Scal> fc_conductivity, fc_temperature_source;
@@ -172,7 +188,7 @@ struct Case {
                       d.velocity_iters_limit, d.velocity_omega);
     auto fp = Factory(d.pressure_solver, d.pressure_tolerance,
                       d.pressure_iters_limit, d.pressure_omega);
-    fluid = std::make_shared<solver::FluidSimple<Mesh>>(
+    fluid = std::make_shared<Fluid>(
         mesh, fc_vel0, fluid_cond, mc_cond, d.velocity_relaxation_factor,
         d.pressure_relaxation_factor, d.rhie_chow_factor, &fc_density_smooth,
         &fc_viscosity_smooth, &fc_force, &fc_stforce, &ff_stforce,
@@ -180,6 +196,10 @@ struct Case {
         d.convergence_tolerance, d.num_iterations_limit, &timer,
         d.time_second_order != 0, d.simpler != 0, d.force_geometric_average != 0,
         d.guess_extrapolation, V3(d.meshvel));
+#ifdef HYDRO_ADAPTER
+    fluid->SetLinearTolerances(d.velocity_tolerance, d.velocity_iters_limit,
+                               d.pressure_tolerance, d.pressure_iters_limit);
+#endif
 
     // advection (hydro2d.hpp:483-600): zero-derivative walls, value inlets
     v_fc_mass_source.resize(nph);
@@ -210,11 +230,21 @@ struct Case {
       }
     }
     std::vector<Scal> rho(d.density, d.density + nph);
-    adv = std::make_shared<solver::AdvectionSolverMultiExplicit<Mesh, FieldFace<Scal>>>(
+#ifdef HYDRO_ADAPTER
+    // the adapters share one context: the fluxes stay on its side
+    adv = std::make_shared<Adv>(*fluid, mesh, q_init, v_cond, nullptr, v_p_ff_volume_flux_slip,
+                                v_p_fc_mass_source, 0., d.dt * d.advection_dt_factor,
+                                d.tvd_split != 0, d.sharp, rho);
+#else
+    adv = std::make_shared<Adv>(
         mesh, q_init, v_cond, &fluid->GetVolumeFlux(solver::Layers::iter_curr),
         v_p_ff_volume_flux_slip, v_p_fc_mass_source, 0.,
         d.dt * d.advection_dt_factor, d.tvd_split != 0, d.sharp, rho);
+#endif
     UpdateProperties();
+#ifdef HYDRO_ADAPTER
+    if (hd) throw std::runtime_error("the adapter variant runs no temperature");
+#endif
     if (hd) {
       geom::MapFace<std::shared_ptr<solver::ConditionFace>> tcond;
       geom::Rect<Vect> box(V3(hd->box_lo), V3(hd->box_hi));

@@ -4,7 +4,7 @@ Run in a container that holds the reference tree (default /root/reference;
 override with HYDRO_REFERENCE):
 
     make -C oracle            # builds oracle/_ref/libhydro_ref.so from it
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]   # all, or the named cases
 
 1. For each case below, the reference's own FluidSimple +
    AdvectionSolverMultiExplicit (driven by oracle/ref_harness.cpp) runs
@@ -228,12 +228,22 @@ def golden_cases():
     d.convergence_tolerance, d.num_iterations_limit = 1e-2, 10
     d.sharp = 0.5
     out.append(("dam2d_lu_sor_sharp", d, u0, q0, 3, False))
+
+    # interface sharpening (advection.hpp:481-530) with tight linear solves
+    # (Jacobi velocity sweeps), which the GPU path reproduces
+    d, u0, q0 = cases.broken_dam(nx=24, ny=12, dt_auto=False, dt=2e-3, smooth_times=2)
+    tight(d, solver=capi.LINEAR_JACOBI, p_tol=1e-10)
+    d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
+    d.sharp = 0.5
+    out.append(("dam2d_sharp", d, u0, q0, 3, True))
     return out
 
 
-def make_cases():
+def make_cases(only=None):
     for case in golden_cases():
         name, d, u0, q0, nsteps, gpu_ok = case[:6]
+        if only and name not in only:
+            continue
         extra = {}
         if len(case) > 6:
             u, p, F, q, T, stats = O.ref_run_heat(d, case[6], u0, q0, nsteps)
@@ -318,6 +328,9 @@ def make_vts():
 if __name__ == "__main__":
     if not O.ref_available():
         O.build(ref=True)
-    make_cases()
-    make_vts()
-    make_sample()
+    # optional: names of solver cases to (re)write, e.g. dam2d_sharp
+    only = set(sys.argv[1:])
+    make_cases(only)
+    if not only:
+        make_vts()
+        make_sample()

@@ -68,6 +68,7 @@ def test_box_mixed_multigrid_and_graph(built):
     dm.pressure_solver = capi.LINEAR_MGCG
     b = run(Hydro(dm), u0, q0, 3)
     errs = compare(b, a, mask)
+    print("mixed vs FP64", errs)
     assert errs["u"] <= 1e-6 and errs["F"] <= 1e-6 and errs["q"] <= 1e-6, errs
     assert errs["p"] <= 5e-6, errs
     h = Hydro(dm)

@@ -1,9 +1,10 @@
 """The five configurations of the workload at their full sizes, through
 properties that do not depend on size: the plain FP64 path against the
 oracle where the oracle finishes in seconds (the 64^2 cavity over its 200
-steps, the 512x256 breaking dam over two steps), the mixed forms against
-the FP64 path at 8.4 M and 7.1 M cells, conservation of every phase over
-many steps, and the 512-case batch against its cases stepped alone."""
+steps, the 512x256 breaking dam over ten steps), the mixed forms against
+the FP64 path at 8.4 M and 7.1 M cells over 50 steps, conservation of every
+phase over many steps, and the 512-case batch against its cases stepped
+alone."""
 import numpy as np
 import pytest
 
@@ -34,24 +35,38 @@ def test_c1_cavity_64_over_200_steps_vs_oracle(built):
     assert np.abs(a["u"]).max() > 0.5  # the lid drove the flow
 
 
+def _fields(s):
+    return {"u": s.get_field(capi.F_VELOCITY), "p": s.get_field(capi.F_PRESSURE),
+            "F": s.get_field(capi.F_VOLUME_FLUX), "q": s.get_field(capi.F_PARTIAL_DENSITY)}
+
+
 def test_c2_dam_512x256_vs_oracle_and_conservation(built):
-    """Breaking dam at 512x256: two steps against the oracle, then 15 steps
-    conserving the partial mass of both phases.  (With the example scripts'
-    smoothing; at this resolution and the default loose velocity tolerance
-    the SIMPLE loop stops converging after ~20 steps and the run diverges
-    near step 27 identically in FP64 and mixed precision, as the reference
-    algorithm does in the oracle.)"""
+    """Breaking dam at 512x256: ten steps against the oracle, compared after
+    every step (the errors stay at rounding level, they do not grow), then
+    15 steps of the mixed form conserving the partial mass of both phases.
+    (With the example scripts' smoothing; at this resolution and the default
+    loose velocity tolerance the SIMPLE loop stops converging after ~20 steps
+    and the run diverges near step 27 identically in FP64 and mixed
+    precision, as the reference algorithm does in the oracle.)"""
     from hydro_gb300.solver import Hydro
     from oracle.oracle import Oracle
     d, u0, q0 = cases.broken_dam(nx=512, ny=256, dt_auto=True, dt_max=1e-3, smooth_times=2)
     _pinned(tight(d, 1.0), 2)
     d.pressure_tolerance = 1e-12
-    a = run(Hydro(d), u0, q0, 2)
     do = d.copy()
     do.pressure_solver = capi.LINEAR_CG
-    b = run(Oracle(do, threads=8), u0, q0, 2)
-    errs = compare(a, b)
-    assert all(v <= 1e-9 for v in errs.values()), errs
+    a, b = Hydro(d), Oracle(do, threads=16)
+    run(a, u0, q0, 0)
+    run(b, u0, q0, 0)
+    history = []
+    for step in range(10):
+        sa, sb = a.step(), b.step()
+        assert sa["outer_iterations"] == sb["outer_iterations"]
+        assert sa["dt"] == pytest.approx(sb["dt"], rel=1e-12)
+        errs = compare(_fields(a), _fields(b))
+        history.append(max(errs.values()))
+        assert all(v <= 1e-9 for v in errs.values()), (step, errs)
+    print("C2 per-step max relative error vs oracle:", ["%.1e" % e for e in history])
     d2, u0, q0 = cases.broken_dam(nx=512, ny=256, dt_auto=True, dt_max=1e-3, smooth_times=2)
     d2.precision = capi.MIXED
     d2.pressure_solver = capi.LINEAR_MGCG
@@ -70,8 +85,13 @@ def test_c2_dam_512x256_vs_oracle_and_conservation(built):
 @pytest.mark.parametrize("config", ["c3_rt_128x128x512", "c4_drops_192"])
 def test_mixed_forms_vs_fp64_full_size(built, config):
     """Mixed precision with the multigrid CG against the FP64 path (FP64
-    kernels, multigrid-preconditioned refinement) at full size: 2 steps of
-    3 outer iterations, fields within the mixed tolerance."""
+    kernels, multigrid-preconditioned refinement) at full size over 50 steps
+    of 3 SIMPLE iterations, compared after every step: every field --
+    velocity, pressure (up to its constant), fluxes, partial densities --
+    within 1e-6 relative L2 at every step, every pressure solve at its
+    tolerance.  (Measured: u <= 3.2e-7, p <= 3.1e-9 over 30 steps at 192^3;
+    u <= 5.6e-7, p <= 1.3e-9 for Rayleigh-Taylor; the velocity error grows
+    by about 1e-8 a step.)"""
     from hydro_gb300.solver import Hydro
     if config.startswith("c3"):
         d, u0, q0 = cases.rayleigh_taylor(seed=0)[:3]
@@ -82,15 +102,21 @@ def test_mixed_forms_vs_fp64_full_size(built, config):
     d.pressure_tolerance, d.pressure_iters_limit = 1e-10, 20000
     d.precision = capi.FP64
     d.pressure_solver = capi.LINEAR_MGCG
-    a = run(Hydro(d), u0, q0, 2)
     dm = d.copy()
     dm.precision = capi.MIXED
-    b = run(Hydro(dm), u0, q0, 2)
-    errs = compare(b, a)
-    assert errs["u"] <= 1e-6 and errs["F"] <= 1e-6 and errs["q"] <= 1e-6, errs
-    assert errs["p"] <= 5e-6, errs
-    for s in a["stats"] + b["stats"]:
-        assert s["status"] == 0 and s["pressure_residual"] <= 1e-10
+    a, b = Hydro(d), Hydro(dm)
+    run(a, u0, q0, 0)
+    run(b, u0, q0, 0)
+    worst = {}
+    for step in range(50):
+        sa, sb = a.step(), b.step()
+        for s in (sa, sb):
+            assert s["status"] == 0 and s["pressure_residual"] <= 1e-10
+        errs = compare(_fields(b), _fields(a))
+        for k, v in errs.items():
+            worst[k] = max(worst.get(k, 0.0), v)
+        assert all(v <= 1e-6 for v in errs.values()), (step, errs)
+    print(config, "largest relative error over 50 steps:", {k: "%.1e" % v for k, v in worst.items()})
 
 
 def test_c5_batch_512_cavities(built):

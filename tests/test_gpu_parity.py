@@ -374,6 +374,7 @@ def test_channel_mixed_and_graph(built):
     dm.pressure_solver = capi.LINEAR_MGCG
     b = run(Hydro(dm), u0, q0, 3)
     errs = compare(b, a)
+    print("mixed vs FP64", errs)
     # velocity and fluxes within the mixed bar; the pressure of a channel
     # started from rest carries the FP32 rounding of the assembled momentum
     # fluxes relative to its own (smaller) scale: measured 1.6e-6
