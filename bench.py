@@ -281,9 +281,20 @@ def measure(args, form, rank, world, local, stream, e2e=True):
     from hydro_gb300 import solver as S
 
     precision, solver = {"mixed_mg": ("mixed", "mgcg"), "fp64": ("fp64", "cg"),
-                         "fp64_mg": ("fp64", "mgcg")}[form]
+                         "fp64_mg": ("fp64", "mgcg"),
+                         "learned_mixed_mg": ("mixed", "mgcg")}[form]
     d, u0, q0, drops = workload(args.n, args.seed + rank, precision, args.outer, solver)
     h = init_case(S.Hydro(d, stream=stream.cuda_stream), d, u0, q0)
+    net = None
+    if form.startswith("learned"):
+        from hydro_gb300.net import Net, attach
+        from hydro_gb300.train_guess import RHO_SCALE
+        if not os.path.exists(args.weights_file):
+            raise RuntimeError("learned form: no trained weights at %s (train them with "
+                               "python -m hydro_gb300.train_guess)" % args.weights_file)
+        net = Net((args.n,) * 3, batch=1)
+        net.load(args.weights_file)
+        attach(h, net, args.guess_iterations, RHO_SCALE)
     N = d.ncells
     for _ in range(args.warmup):
         h.step()
@@ -306,8 +317,16 @@ def measure(args, form, rank, world, local, stream, e2e=True):
     ms = e0.elapsed_time(e1)
     prof = h.profile()
     h.set_profiling(False)
+    guess = None
+    if net is not None:
+        from hydro_gb300.net import guess_stats
+        used, dropped = guess_stats(h)
+        pms, plaunch = net.last_predict()
+        guess = {"used": used, "dropped": dropped, "predict_ms": round(pms, 4),
+                 "predict_launches": plaunch, "iterations_guessed": args.guess_iterations}
     ms_max = max_over_ranks(ms, world)
     out = {"form": form, "precision": precision, "solver": solver, "N": N, "drops": len(drops),
+           "guess": guess,
            "ms": ms_max, "value": world * N * args.steps / (ms_max / 1e3) / 1e6,
            "launches": launches, "clocks": clk, "stats": stats, "prof": prof, "desc": d}
     if e2e:
@@ -354,6 +373,8 @@ def measure(args, form, rank, world, local, stream, e2e=True):
                       "h2d_bytes_per_step": (d.dim + nph) * N * 8,
                       "d2h_bytes_per_step": (d.dim + 1 + nph) * N * 8}
     h.close()
+    if net is not None:
+        net.close()
     return out
 
 
@@ -442,6 +463,10 @@ def run_ours(args, rank, world, local):
     head = measure(args, args.form, rank, world, local, stream)
     plain = None
     fp64mg = None
+    mixed = None
+    if args.form.startswith("learned") and not args.no_plain:
+        # the same form without the network: what the learned guess gains
+        mixed = measure(args, "mixed_mg", rank, world, local, stream, e2e=False)
     if args.form != "fp64" and not args.no_plain:
         plain = measure(args, "fp64", rank, world, local, stream, e2e=False)
         if args.form != "fp64_mg":
@@ -512,6 +537,19 @@ def run_ours(args, rank, world, local):
             "pressure_iterations": [s["pressure_iterations"] for s in head["graph"]["stats"]],
         },
     }
+    if head.get("guess"):
+        out["learned_guess"] = dict(head["guess"])
+        out["learned_guess"]["weights"] = os.path.relpath(args.weights_file, ROOT)
+    if mixed:
+        out["mixed_multigrid"] = {
+            "value": round(mixed["value"], 4),
+            "ms_per_step": round(mixed["ms"] / args.steps, 3),
+            "pressure_iterations": [s["pressure_iterations"] for s in mixed["stats"]],
+            "speedup_of_headline": round(head["value"] / mixed["value"], 3),
+            "note": "the headline form without the learned guess: what the network gains",
+            "clocks": mixed["clocks"],
+            "profile_ms": {k: round(v[1], 3) for k, v in sorted(mixed["prof"].items())},
+        }
     if plain:
         out["plain_fp64"] = {
             "value": round(plain["value"], 4),
@@ -622,14 +660,22 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="mixed_mg", choices=["mixed_mg", "fp64", "fp64_mg"],
+    ap.add_argument("--weights-file", default=os.path.join(ROOT, "hydro_gb300", "weights",
+                                                           "rising_drops_192.npy"),
+                    help="parameters of the learned pressure guess (learned_mixed_mg)")
+    ap.add_argument("--guess-iterations", type=int, default=1,
+                    help="SIMPLE iterations per step whose pressure solve starts from the "
+                         "network's guess (learned_mixed_mg)")
+    ap.add_argument("--form", default="mixed_mg",
+                    choices=["learned_mixed_mg", "mixed_mg", "fp64", "fp64_mg"],
                     help="headline form: mixed precision + multigrid CG, or plain FP64")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 measurement reported beside the headline")
     ap.add_argument("--n", "--grid", dest="n", type=int, default=192,
                     help="cells per side (--grid under torchrun, whose parser claims --n)")
     ap.add_argument("--outer", type=int, default=5, help="SIMPLE iterations per step")
-    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--seed", type=int, default=40,
+                    help="drop seed (40: the first held-out seed of the learned guess)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=150.0,
                     help="seconds of complete CPU steps (reference arm; the cpu_baseline leg "

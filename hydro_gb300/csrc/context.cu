@@ -993,6 +993,19 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
       lv.b = a.take<float>(lv.m.nc);
     }
     mg.cinv = mg.nlev >= 2 ? a.take<float>(kMgCoarseTarget * kMgCoarseTarget) : nullptr;
+    // colour-blocked FP16 finest level (plain 3D block, even n[0])
+    const bool plain = !m.per[0] && !m.per[1] && !m.per[2] && exmask.empty();
+    if (mg.nlev >= 2 && m.dim == 3 && plain && m.n[0] % 2 == 0 && m.nc < (1LL << 30)) {
+      const long long n0 = m.n[0], n1 = m.n[1], n2 = m.n[2];
+      mg.k16[0] = a.take<unsigned short>((n0 + 1) * n1 * n2);
+      mg.k16[1] = a.take<unsigned short>(n0 * (n1 + 1) * n2);
+      mg.k16[2] = a.take<unsigned short>(n0 * n1 * (n2 + 1));
+      mg.b0 = a.take<float>(nc);
+      mg.x0 = a.take<float>(nc);
+      mg.idg0 = a.take<float>(nc);
+    } else {
+      mg.k16[0] = mg.k16[1] = mg.k16[2] = nullptr;
+    }
     w.ds = a.take<DevScalars>(1);
     x->stat_out = a.take<double>(16);
     x->stat_ticket = a.take<unsigned>(4);

@@ -75,7 +75,8 @@ enum {
   RS_OUT_FLUX = 18, RS_OUT_AREA = 19, RS_IN_FLUX = 20,  // outlet rebalancing sums
   RS_HEAT_DIFF = 21,     // max |update| of the last temperature sweep
   RS_MOM_DIFF_RED = 22,  // max |update| of the red half of a Gauss-Seidel sweep
-  RS_GUESS_S0 = 23, RS_GUESS_S1 = 24  // <x, f'>, <x, A x> of a learned initial guess
+  RS_GUESS_S0 = 23, RS_GUESS_S1 = 24,  // <x, f'>, <x, A x> of a learned initial guess
+  RS_MG0_SCALE = 25      // power-of-two scale of the FP16 finest-level couplings
 };
 enum {
   FL_MOM_DONE = 0, FL_MOM_SWEEPS = 1, FL_PCG_DONE = 2, FL_PCG_ITERS = 3, FL_NAN = 4,
@@ -96,7 +97,7 @@ enum {
   TK_MOM = 0, TK_PCG_A = 1, TK_PCG_B = 2, TK_PCG_INIT = 3, TK_IND = 4, TK_DT = 5,
   TK_MEAN = 6, TK_MEAN2 = 7, TK_STAT = 8, TK_STAT2 = 9, TK_STAT3 = 10, TK_IR = 11,
   TK_NAN = 12, TK_PCG_INIT2 = 13, TK_F32_A = 14, TK_F32_B = 15, TK_F32_INIT = 16,
-  TK_OUTLET = 17, TK_HEAT = 18, TK_MOM_RED = 19, TK_GUESS = 20
+  TK_OUTLET = 17, TK_HEAT = 18, TK_MOM_RED = 19, TK_GUESS = 20, TK_MG0 = 21
 };
 
 // ---------------------------------------------------------------- fluid --
@@ -346,6 +347,17 @@ struct MgWork {
   int coarse_sweeps;       // sweeps of the coarsest solve inside the CTA
   int coarse_sweeps_large; // sweeps when the coarsest level stays large
   MgLevel lev[kMgMaxLevels];
+  // Finest level of a plain 3D block (no periodic direction, no excluded
+  // cell, even n[0]) solved without a pinned cell: the iterate, right-hand
+  // side and inverse diagonal stored colour-blocked (cell c at
+  // colour * nc/2 + c/2, colour = (i+j+k) mod 2) and the face couplings in
+  // FP16 scaled by a power of two, so that a half-sweep streams its own
+  // colour's rows, the other colour's iterate and 2-byte couplings.  k16
+  // null: not allocated (the mesh does not allow it); fast0: in use for
+  // the current solve (set by mg_setup).
+  unsigned short* k16[3];
+  float *b0, *x0, *idg0;
+  bool fast0;
   // inverse of the coarsest level's operator (rank-one completed for its
   // constant null space), dense, when that level has <= kMgCoarseTarget
   // cells and is not the top level; null otherwise
@@ -359,6 +371,7 @@ struct MgWork {
   float* vc_z;
   long long vc_pin;
   DevScalars* vc_ds;
+  bool vc_fast0;
   int vc_kernels;
 };
 Mesh mg_coarse_mesh(const Mesh& fine);

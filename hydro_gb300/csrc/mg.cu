@@ -19,6 +19,7 @@
 //                      on the zero-mean right-hand side).
 // All kernels return at once when the CG's done flag is set, so iterations
 // can be queued in chunks like the other solvers.
+#include <cuda_fp16.h>
 #include <math.h>
 
 #include "kernels.h"
@@ -597,6 +598,221 @@ __global__ void __launch_bounds__(NT) k_mgcg_dot(long long n, const float* __res
 
 bool aligned16(const void* a) { return (reinterpret_cast<uintptr_t>(a) & 15) == 0; }
 
+// ------------------------------------------ colour-blocked finest level --
+// A plain 3D block (no periodic direction, no excluded cell) with an even
+// n0, solved without a pinned cell.  Cell c = i + n0 (j + n1 k) of colour
+// q = (i+j+k) mod 2 sits at q * nc/2 + c/2 in the iterate, right-hand side
+// and inverse diagonal: with n0 even the two cells of a pair (2h, 2h+1)
+// have opposite colours, so c/2 = h + n0/2 (j + n1 k) and a warp of one
+// colour reads and writes consecutive words.  The neighbours of a cell at
+// blocked index p are p - 1 + (i odd) and p + (i odd) along x, p -/+ n0/2
+// along y and p -/+ n0 n1/2 along z in the other colour's half.  The face
+// couplings are stored in FP16 (as bit patterns) divided by 2^e, e chosen
+// so that the largest coupling lies in [2^13, 2^14); the inverse diagonal
+// is formed from the rounded couplings, so every row still sums to zero.
+// The V-cycle stays symmetric: one face value serves both of its cells.
+struct Fast0 {
+  int n0, n1, n2;
+  const unsigned short *kx, *ky, *kz;
+};
+
+__device__ __forceinline__ float h2f(const unsigned short* a, long long i) {
+  return __half2float(__ushort_as_half(a[i]));
+}
+
+// Largest face coupling -> the power-of-two scale 2^e (RS_MG0_SCALE).
+__global__ void __launch_bounds__(NT) k_mg0_scale(long long nf, const float* kf,
+                                                  double* partials, DevScalars* ds) {
+  double mx = 0.;
+  for (long long i = blockIdx.x * (long long)NT + threadIdx.x + BX * threadIdx.y; i < nf;
+       i += (long long)gridDim.x * NT)
+    mx = fmax(mx, (double)kf[i]);
+  double v[1] = {mx};
+  __shared__ double o[1];
+  if (grid_reduce<RED_MAX, 1>(v, partials, &ds->ticket[TK_MG0], o)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      int e = 0;
+      frexp(o[0], &e);  // o = f 2^e, f in [0.5, 1)
+      ds->red[RS_MG0_SCALE] = o[0] > 0. ? ldexp(1.0, e - 14) : 1.0;
+    }
+  }
+}
+
+// Face couplings of the level (direction-blocked FP32) -> three FP16 arrays.
+__global__ void k_mg0_pack(Mesh m, const float* kf, const DevScalars* ds, unsigned short* kx,
+                           unsigned short* ky, unsigned short* kz) {
+  const float inv = (float)(1. / ds->red[RS_MG0_SCALE]);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m.nf;
+       i += (long long)gridDim.x * blockDim.x) {
+    const unsigned short v = __half_as_ushort(__float2half_rn(kf[i] * inv));
+    if (i < m.fofs[1]) kx[i] = v;
+    else if (i < m.fofs[2]) ky[i - m.fofs[1]] = v;
+    else kz[i - m.fofs[2]] = v;
+  }
+}
+
+// Inverse diagonal of the rounded operator, colour-blocked (one thread per
+// cell pair).
+__global__ void k_mg0_diag(Fast0 f, const DevScalars* ds, float* idg0) {
+  const double scale = ds->red[RS_MG0_SCALE];
+  const int h0 = f.n0 / 2;
+  const long long half = (long long)h0 * f.n1 * f.n2;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < half;
+       p += (long long)gridDim.x * blockDim.x) {
+    const long long row = p / h0;
+    const int ih = (int)(p - row * h0);
+    const int j = (int)(row % f.n1), k = (int)(row / f.n1);
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int i = 2 * ih + e;
+      const long long fx = i + (long long)(f.n0 + 1) * (j + (long long)f.n1 * k);
+      const long long fy = i + (long long)f.n0 * (j + (long long)(f.n1 + 1) * k);
+      const long long fz = i + (long long)f.n0 * (j + (long long)f.n1 * k);
+      const float sk = h2f(f.kx, fx) + h2f(f.kx, fx + 1) + h2f(f.ky, fy) +
+                       h2f(f.ky, fy + f.n0) + h2f(f.kz, fz) +
+                       h2f(f.kz, fz + (long long)f.n0 * f.n1);
+      const double dg = (double)sk * scale;
+      const int q = (i + j + k) & 1;
+      idg0[q * half + p] = dg > 0. ? (float)(1. / dg) : 0.f;
+    }
+  }
+}
+
+// Start of a V-cycle: the CG residual r (cell order) into the blocked
+// right-hand side, and the first half-sweep (red, from x = 0: x = b / diag).
+__global__ void k_mg0_split(Fast0 f, const float* r, const float* idg0, float* b0, float* x0,
+                            const DevScalars* ds) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  const int h0 = f.n0 / 2;
+  const long long half = (long long)h0 * f.n1 * f.n2;
+  const float2* r2 = reinterpret_cast<const float2*>(r);
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < half;
+       p += (long long)gridDim.x * blockDim.x) {
+    const long long row = p / h0;
+    const int q = (int)((row % f.n1 + row / f.n1) & 1);  // colour of cell 2p
+    const float2 v = r2[p];
+    b0[q * half + p] = v.x;
+    b0[(1 - q) * half + p] = v.y;
+    x0[p] = (q == 0 ? v.x : v.y) * idg0[p];
+  }
+}
+
+// Red-black half-sweep of one colour on the blocked arrays.  PROLONG: the
+// neighbours are read as x + cx(parent) (the injected coarse correction,
+// first post-smoothing half-sweep).  ZOUT: the new values also go to z in
+// cell order (the last half-sweep of each colour: the preconditioned
+// residual the CG reads).
+template <bool PROLONG, bool ZOUT>
+__global__ void __launch_bounds__(NT) k_mg0_smooth(Fast0 f, const float* idg0, const float* b0,
+                                                   float* x0, int color, const float* cx,
+                                                   float* z, const DevScalars* ds, int kch) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  const int h0 = f.n0 / 2;
+  const int ih = blockIdx.x * BX + threadIdx.x;
+  const int j = blockIdx.y * BY + threadIdx.y;
+  if (ih >= h0 || j >= f.n1) return;
+  const int k0 = blockIdx.z * kch, k1 = min(k0 + kch, f.n2);
+  const int half = h0 * f.n1 * f.n2;
+  const int hz = h0 * f.n1;
+  const int own = color * half, oth = (1 - color) * half;
+  const float scale = (float)ds->red[RS_MG0_SCALE];
+  const int cnx = f.n0 / 2, cny = f.n1 / 2;
+  for (int k = k0; k < k1; ++k) {
+    const int i = 2 * ih + ((j + k + color) & 1);
+    const int odd = i & 1;
+    const int p = ih + h0 * (j + f.n1 * k);
+    const int fx = i + (f.n0 + 1) * (j + f.n1 * k);
+    const int fy = i + f.n0 * (j + (f.n1 + 1) * k);
+    const int fz = i + f.n0 * (j + f.n1 * k);
+    float xs[6], ks[6];
+    bool in[6];
+    int nb[6];
+    in[0] = i > 0;
+    nb[0] = p - 1 + odd;
+    ks[0] = h2f(f.kx, fx);
+    in[1] = i < f.n0 - 1;
+    nb[1] = p + odd;
+    ks[1] = h2f(f.kx, fx + 1);
+    in[2] = j > 0;
+    nb[2] = p - h0;
+    ks[2] = h2f(f.ky, fy);
+    in[3] = j < f.n1 - 1;
+    nb[3] = p + h0;
+    ks[3] = h2f(f.ky, fy + f.n0);
+    in[4] = k > 0;
+    nb[4] = p - hz;
+    ks[4] = h2f(f.kz, fz);
+    in[5] = k < f.n2 - 1;
+    nb[5] = p + hz;
+    ks[5] = h2f(f.kz, fz + f.n0 * f.n1);
+#pragma unroll
+    for (int q = 0; q < 6; ++q) xs[q] = in[q] ? x0[oth + nb[q]] : 0.f;
+    if (PROLONG) {
+      const int ci = i >> 1, cj = j >> 1, ck = k >> 1;
+      const int pc = ci + cnx * (cj + cny * ck);
+      // parents of the six neighbours: the own parent or the next one
+      if (in[0]) xs[0] += cx[odd ? pc : pc - 1];
+      if (in[1]) xs[1] += cx[odd ? pc + 1 : pc];
+      if (in[2]) xs[2] += cx[(j & 1) ? pc : pc - cnx];
+      if (in[3]) xs[3] += cx[(j & 1) ? pc + cnx : pc];
+      if (in[4]) xs[4] += cx[(k & 1) ? pc : pc - cnx * cny];
+      if (in[5]) xs[5] += cx[(k & 1) ? pc + cnx * cny : pc];
+    }
+    const float bb = b0[own + p], ig = idg0[own + p];
+    float acc = 0.f;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) acc = fmaf(ks[q], xs[q], acc);
+    const float xn = fmaf(scale, acc, bb) * ig;
+    x0[own + p] = xn;
+    if (ZOUT) z[i + f.n0 * (j + f.n1 * k)] = xn;
+  }
+}
+
+// Coarse right-hand side = sum of the red children's residuals (the
+// pre-smoothing ends with a black half-sweep, which leaves the black
+// residuals zero up to rounding): r = b + 2^e sum_f k_f (x_nb - x_c).
+// With cidg the coarse level's first half-sweep (red, from zero) as well,
+// else the coarse iterate is cleared.
+__global__ void __launch_bounds__(NT, 4) k_mg0_restrict(Fast0 f, Mesh cm, const float* b0,
+                                                        const float* x0, float* cb, float* cx,
+                                                        const float* cidg, const DevScalars* ds,
+                                                        int kch) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  const int h0 = f.n0 / 2;
+  const int half = h0 * f.n1 * f.n2;
+  const int hz = h0 * f.n1;
+  const float scale = (float)ds->red[RS_MG0_SCALE];
+  CELL_LOOP_BEGIN(cm, kch)
+  float sum = 0.f;
+#pragma unroll
+  for (int ck = 0; ck < 2; ++ck)
+#pragma unroll
+    for (int cj = 0; cj < 2; ++cj)
+#pragma unroll
+      for (int ci = 0; ci < 2; ++ci) {
+        if ((ci + cj + ck) & 1) continue;
+        const int i = 2 * X.i[0] + ci, j = 2 * X.i[1] + cj, k = 2 * X.i[2] + ck;
+        const int odd = i & 1;
+        const int p = (i >> 1) + h0 * (j + f.n1 * k);  // red: colour 0
+        const int fx = i + (f.n0 + 1) * (j + f.n1 * k);
+        const int fy = i + f.n0 * (j + (f.n1 + 1) * k);
+        const int fz = i + f.n0 * (j + f.n1 * k);
+        const float xc = x0[p];
+        float acc = 0.f;
+        if (i > 0) acc = fmaf(h2f(f.kx, fx), x0[half + p - 1 + odd] - xc, acc);
+        if (i < f.n0 - 1) acc = fmaf(h2f(f.kx, fx + 1), x0[half + p + odd] - xc, acc);
+        if (j > 0) acc = fmaf(h2f(f.ky, fy), x0[half + p - h0] - xc, acc);
+        if (j < f.n1 - 1) acc = fmaf(h2f(f.ky, fy + f.n0), x0[half + p + h0] - xc, acc);
+        if (k > 0) acc = fmaf(h2f(f.kz, fz), x0[half + p - hz] - xc, acc);
+        if (k < f.n2 - 1)
+          acc = fmaf(h2f(f.kz, fz + f.n0 * f.n1), x0[half + p + hz] - xc, acc);
+        sum += fmaf(scale, acc, b0[p]);
+      }
+  cb[X.c] = sum;
+  cx[X.c] = cidg && ((X.i[0] + X.i[1] + X.i[2]) & 1) == 0 ? sum * cidg[X.c] : 0.f;
+  CELL_LOOP_END
+}
+
 int flat_blocks_mg(long long n) {
   long long b = (n + NT - 1) / NT;
   if (b > 152 * 16) b = 152 * 16;
@@ -606,6 +822,12 @@ int flat_blocks_mg(long long n) {
 
 // Grid of a red-black half-sweep: one thread per cell pair along x, sized
 // in whole waves over the half-width mesh.
+Launch fast0_launch(const Mesh& m) {
+  Mesh h = m;
+  h.n[0] = m.n[0] / 2;
+  return cell_launch_waves(h, resident_ctas((const void*)k_mg0_smooth<false, false>));
+}
+
 Launch half_launch(const Mesh& m) {
   const bool per = any_periodic(m);
   const void* k = m.dim == 3 ? (per ? (const void*)k_mg_smooth<3, true> : (const void*)k_mg_smooth<3, false>)
@@ -698,6 +920,18 @@ cudaError_t mg_setup(MgWork& mg, PcgWork& w, cudaStream_t st) {
   mg.lev[0].kf = w.kf32;
   mg.lev[0].dg = w.dg32;
   mg.lev[0].idg = w.idg32;
+  // the colour-blocked FP16 finest level: allocated for this mesh, no
+  // pinned cell in this solve, and a grid level (not the in-CTA cycle)
+  mg.fast0 = mg.k16[0] != nullptr && w.pin < 0 && mg.nlev >= 2 && mg.top >= 1;
+  if (mg.fast0) {
+    const Mesh& m = mg.lev[0].m;
+    Fast0 f{m.n[0], m.n[1], m.n[2], mg.k16[0], mg.k16[1], mg.k16[2]};
+    k_mg0_scale<<<flat_blocks_mg(m.nf), dim3(BX, BY), 0, st>>>(m.nf, w.kf32, w.partials, w.ds);
+    k_mg0_pack<<<flat_blocks_mg(m.nf), NT, 0, st>>>(m, w.kf32, w.ds, mg.k16[0], mg.k16[1],
+                                                    mg.k16[2]);
+    k_mg0_diag<<<flat_blocks_mg(m.nc / 2), NT, 0, st>>>(f, w.ds, mg.idg0);
+    count_launches(3);
+  }
   for (int l = 1; l < mg.nlev; ++l) {
     MgLevel& f = mg.lev[l - 1];
     MgLevel& c = mg.lev[l];
@@ -758,7 +992,32 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
   mg.lev[0].x = z;
   const int ns = mg.nsweep;
   const int top = mg.top < mg.nlev ? mg.top : mg.nlev - 1;
-  for (int l = 0; l < top; ++l) {
+  const bool fast0 = mg.fast0 && top >= 1 && ns >= 1;
+  const Mesh& m0 = mg.lev[0].m;
+  const Fast0 f0{m0.n[0], m0.n[1], m0.n[2], mg.k16[0], mg.k16[1], mg.k16[2]};
+  if (fast0) {
+    // level 0 on the colour-blocked arrays: split (+ red from zero), then
+    // black, (red, black)^(ns-1), restriction of the red residuals
+    const Launch H = fast0_launch(m0);
+    k_mg0_split<<<flat_blocks_mg(m0.nc / 2), NT, 0, st>>>(f0, r, mg.idg0, mg.b0, mg.x0, ds);
+    count_launches(1);
+    for (int s = 0; s < ns; ++s) {
+      if (s > 0) {
+        k_mg0_smooth<false, false><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 0,
+                                                              nullptr, nullptr, ds, H.kch);
+        count_launches(1);
+      }
+      k_mg0_smooth<false, false><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 1,
+                                                            nullptr, nullptr, ds, H.kch);
+      count_launches(1);
+    }
+    MgLevel& c = mg.lev[1];
+    Launch L = cell_launch(c.m);
+    const float* cidg = 1 < top ? c.idg : nullptr;
+    k_mg0_restrict<<<L.grid, L.block, 0, st>>>(f0, c.m, mg.b0, mg.x0, c.b, c.x, cidg, ds, L.kch);
+    count_launches(1);
+  }
+  for (int l = fast0 ? 1 : 0; l < top; ++l) {
     MgLevel& f = mg.lev[l];
     long long lp = l == 0 ? pin : -1;
     Launch H = half_launch(f.m);
@@ -819,7 +1078,7 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
       mg_smooth(dim, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, 0, lp, nullptr, 0, 0, ds, st);
     }
   }
-  for (int l = top - 1; l >= 0; --l) {
+  for (int l = top - 1; l >= (fast0 ? 1 : 0); --l) {
     MgLevel& f = mg.lev[l];
     MgLevel& c = mg.lev[l + 1];
     long long lp = l == 0 ? pin : -1;
@@ -829,6 +1088,34 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
       const float* cx = s == 0 ? c.x : nullptr;
       mg_smooth(dim, H, per, f.m, f.kf, f.idg, f.b, f.x, 1, 0, lp, cx, c.m.n[0], c.m.n[1], ds, st);
       mg_smooth(dim, H, per, f.m, f.kf, f.idg, f.b, f.x, 0, 0, lp, nullptr, 0, 0, ds, st);
+    }
+  }
+  if (fast0) {
+    // (black + injected correction, red), (black, red)^(ns-1); the last
+    // half-sweep of each colour writes z in cell order
+    const Launch H = fast0_launch(m0);
+    const float* cx = mg.lev[1].x;
+    for (int s = 0; s < ns; ++s) {
+      const bool last = s == ns - 1;
+      if (s == 0 && last)
+        k_mg0_smooth<true, true><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 1, cx,
+                                                            z, ds, H.kch);
+      else if (s == 0)
+        k_mg0_smooth<true, false><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 1, cx,
+                                                             nullptr, ds, H.kch);
+      else if (last)
+        k_mg0_smooth<false, true><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 1,
+                                                             nullptr, z, ds, H.kch);
+      else
+        k_mg0_smooth<false, false><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 1,
+                                                              nullptr, nullptr, ds, H.kch);
+      if (last)
+        k_mg0_smooth<false, true><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 0,
+                                                             nullptr, z, ds, H.kch);
+      else
+        k_mg0_smooth<false, false><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 0,
+                                                              nullptr, nullptr, ds, H.kch);
+      count_launches(2);
     }
   }
   return cudaGetLastError();
@@ -842,7 +1129,8 @@ cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevSc
   cudaError_t e = cudaStreamIsCapturing(st, &cs);
   if (e != cudaSuccess) return e;
   if (cs != cudaStreamCaptureStatusNone) return mg_vcycle_launch(mg, r, z, pin, ds, st);
-  if (!mg.vc_exec || mg.vc_r != r || mg.vc_z != z || mg.vc_pin != pin || mg.vc_ds != ds) {
+  if (!mg.vc_exec || mg.vc_r != r || mg.vc_z != z || mg.vc_pin != pin || mg.vc_ds != ds ||
+      mg.vc_fast0 != mg.fast0) {
     mg_release(mg);
     cudaGraph_t g = nullptr;
     if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed)) != cudaSuccess) return e;
@@ -867,6 +1155,7 @@ cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevSc
     mg.vc_z = z;
     mg.vc_pin = pin;
     mg.vc_ds = ds;
+    mg.vc_fast0 = mg.fast0;
   }
   count_launches(mg.vc_kernels);
   return cudaGraphLaunch(mg.vc_exec, st);
