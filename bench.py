@@ -320,9 +320,10 @@ def measure(args, form, rank, world, local, stream, e2e=True):
     guess = None
     if net is not None:
         from hydro_gb300.net import guess_stats
-        used, dropped = guess_stats(h)
+        used, dropped, skipped = guess_stats(h)
         pms, plaunch = net.last_predict()
-        guess = {"used": used, "dropped": dropped, "predict_ms": round(pms, 4),
+        guess = {"used": used, "dropped": dropped, "skipped_steps": skipped,
+                 "predict_ms": round(pms, 4),
                  "predict_launches": plaunch, "iterations_guessed": args.guess_iterations}
     ms_max = max_over_ranks(ms, world)
     out = {"form": form, "precision": precision, "solver": solver, "N": N, "drops": len(drops),

@@ -386,6 +386,7 @@ def _declare(lib, prefix):
             "hydro_net_last_predict": [P, D, ctypes.POINTER(I)],
             "hydro_gpu_set_pressure_guess": [P, P, I, ctypes.c_double],
             "hydro_gpu_get_guess_stats": [P, ctypes.POINTER(ctypes.c_longlong),
+                                          ctypes.POINTER(ctypes.c_longlong),
                                           ctypes.POINTER(ctypes.c_longlong)],
             "hydro_conv3d_forward": [I, I, I, I, I, I, P, P, P, P, I, P, P],
             "hydro_conv3d_backward_data": [I, I, I, I, I, I, P, P, P, P, P, P],

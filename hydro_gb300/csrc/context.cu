@@ -244,6 +244,7 @@ struct hydro_ctx {
   hydro_net* net = nullptr;
   int net_iters = 0;
   double net_rho_scale = 1.;
+  bool guess_off = false;  // host-driven step: this step skips the guess (back-off)
   double p_res = 0., indicator = 1.;
   int du_cur = 0;
   int status = HYDRO_OK;
@@ -640,7 +641,7 @@ int solve_pressure_graph(hydro_ctx* x, int singular, int mixed, bool apply_pin_g
       // the learned guess, for the first net_iters SIMPLE iterations
       cudaGraphConditionalHandle hg2;
       if ((rc = new_handle(x, 0, &hg2))) return rc;
-      CK(launch_ctl_guess_gate(w.ds, x->net_iters, hg2, x->st));
+      CK(launch_ctl_guess_gate(w.ds, x->net_iters, hg2, 1, x->st));
       rc = add_if(x, hg2, [&]() -> int {
         int r;
         if ((r = apply_guess(x, singular))) return r;
@@ -727,7 +728,18 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
       double rr = x->hds->red[RS_IR_RR];
       if (std::isnan(rr)) return HYDRO_ERR_NAN;  // a NaN in the system (fluid.hpp:1164-1166)
       if (ff < 0.) ff = rr;
-      if (outer == 0 && apply_pin && x->net && x->iter_count < x->net_iters && ff > 0.) {
+      bool guess = outer == 0 && apply_pin && x->net && x->iter_count < x->net_iters;
+      if (guess) {
+        // the back-off (the device flags as of the last read-back, which
+        // follows the last guess): the same decision the gate kernel
+        // applies on the device
+        if (x->iter_count == 0) {
+          x->guess_off = x->hds->flag[FL_GUESS_SKIP] > 0;
+          CK(launch_ctl_guess_gate(w.ds, x->net_iters, cudaGraphConditionalHandle{}, 0, x->st));
+        }
+        guess = !x->guess_off && ff > 0.;
+      }
+      if (guess) {
         // start from the network's guess when it beats the zero guess
         x->prof.begin(HYDRO_PROF_GUESS, x->st);
         rc = apply_guess(x, singular);
@@ -2160,6 +2172,10 @@ int hydro_gpu_set_pressure_guess(hydro_ctx* x, hydro_net* net, int iterations,
   x->net = net;
   x->net_iters = iterations;
   x->net_rho_scale = rho_scale;
+  x->guess_off = false;
+  if ((rc = reset_flags(x, FL_GUESS_USED, 2)) || (rc = reset_flags(x, FL_GUESS_SKIP, 4)))
+    return rc;
+  if ((rc = sync_scalars(x))) return rc;
   if (x->sg.exec) {  // a captured step without (or with another) guess
     cudaGraphExecDestroy(x->sg.exec);
     x->sg.exec = nullptr;
@@ -2167,13 +2183,16 @@ int hydro_gpu_set_pressure_guess(hydro_ctx* x, hydro_net* net, int iterations,
   return HYDRO_OK;
 }
 
-int hydro_gpu_get_guess_stats(hydro_ctx* x, long long* used, long long* dropped) {
+int hydro_gpu_get_guess_stats(hydro_ctx* x, long long* used, long long* dropped,
+                              long long* skipped) {
   if (!x) return HYDRO_ERR_ARG;
   int rc = sync_scalars(x);
   if (rc) return rc;
   if (used) *used = x->hds->flag[FL_GUESS_USED];
   if (dropped) *dropped = x->hds->flag[FL_GUESS_DROPPED];
-  return reset_flags(x, FL_GUESS_USED, 2);
+  if (skipped) *skipped = x->hds->flag[FL_GUESS_SKIPPED];
+  if ((rc = reset_flags(x, FL_GUESS_USED, 2))) return rc;
+  return reset_flags(x, FL_GUESS_SKIPPED, 1);
 }
 
 }  // extern "C"

@@ -83,9 +83,24 @@ __global__ void k_ctl_refine(DevScalars* ds, double tol, double inner_min, int l
   decide(ds, cont, h, use);
 }
 
-__global__ void k_ctl_guess_gate(DevScalars* ds, int limit, cudaGraphConditionalHandle h) {
+// Whether this SIMPLE iteration's pressure solve starts from the learned
+// guess: the first `limit` iterations of a step, unless the step is one the
+// back-off skips (decided at its first iteration).
+// use = 0 (host-driven step): called at the step's first iteration only,
+// for the back-off bookkeeping.
+__global__ void k_ctl_guess_gate(DevScalars* ds, int limit, cudaGraphConditionalHandle h,
+                                 int use) {
   if (threadIdx.x != 0) return;
-  cudaGraphSetConditional(h, ds->flag[FL_ITERS] < limit ? 1u : 0u);
+  const int it = use ? ds->flag[FL_ITERS] : 0;
+  if (it == 0) {
+    const int off = ds->flag[FL_GUESS_SKIP] > 0;
+    if (off) {
+      ds->flag[FL_GUESS_SKIP] -= 1;
+      ds->flag[FL_GUESS_SKIPPED] += 1;
+    }
+    ds->flag[FL_GUESS_OFF] = off;
+  }
+  if (use) cudaGraphSetConditional(h, (it < limit && !ds->flag[FL_GUESS_OFF]) ? 1u : 0u);
 }
 
 // The refinement loop's first decision, again, from the residual of the
@@ -195,8 +210,8 @@ cudaError_t launch_ctl_refine(DevScalars* ds, double tol, double inner_min, int 
 }
 
 cudaError_t launch_ctl_guess_gate(DevScalars* ds, int limit, cudaGraphConditionalHandle h,
-                                  cudaStream_t st) {
-  k_ctl_guess_gate<<<1, 32, 0, st>>>(ds, limit, h);
+                                  int use, cudaStream_t st) {
+  k_ctl_guess_gate<<<1, 32, 0, st>>>(ds, limit, h, use);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -12,8 +12,8 @@
 //    views into it -- the A operand of tap (dx, dy, dz) starts dx + 10 dy +
 //    180 dz rows into the tile, with its 8-row core matrices 10 rows (160 B)
 //    apart -- so the input crosses HBM once per tile, not 27 times.  The
-//    weights of one tap ([ci/8][co][8] BF16, K-major) stream through a
-//    three-stage ring by bulk copies.  One thread issues tcgen05.mma
+//    weights of one tap ([ci/8][co][8] BF16, K-major) are bulk copies: all
+//    27 resident for the 16/32-channel layers, else a ring of 9 (or 3).  One thread issues tcgen05.mma
 //    (M = 128, N = Cout, K = 16) into four accumulators of Cout columns in
 //    TMEM; the four warps read them back with tcgen05.ld and apply the
 //    epilogue (bias, addend, ReLU, mask) before a 16-byte-vector store.
@@ -42,7 +42,16 @@ namespace nn {
 
 namespace {
 
-constexpr int kNStage = 3;                 // weight ring stages (forward)
+// Weight stages of the forward kernel: all 27 taps resident in shared
+// memory when they take at most 28 KB (the 16- and 32-channel layers of the
+// finest levels: no wait on the tensor pipe between taps), else a ring of 9
+// (a bulk copy's latency is hidden behind the MMAs of 8 taps) where the
+// shared memory allows, else 3.
+constexpr int stages_for(int cin, int cout) {
+  return 27 * cin * cout * 2 <= 28 * 1024                          ? 27
+         : (cin / 8) * kRegion + 9 * cin * cout * 2 <= 212 * 1024 ? 9
+                                                                   : 3;
+}
 constexpr long kWaitPolls = 1L << 24;      // bounded mbarrier waits (~1 s)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -197,7 +206,7 @@ __device__ __forceinline__ float bf(__nv_bfloat16 v) { return __bfloat162float(v
 // ------------------------------------------------------------ forward --
 // out[p][co] = epi(sum_tap sum_ci x[p + off(tap)][ci] w[tap][co][ci]).
 // w: [27][CIN/8][COUT][8] BF16 (K-major core matrices per tap).
-template <int CIN, int COUT>
+template <int CIN, int COUT, int kNStage>
 __global__ void __launch_bounds__(128) k_conv(const __grid_constant__ CUtensorMap xin,
                                               ConvDims dm, const __nv_bfloat16* __restrict__ w,
                                               Epilogue ep, __nv_bfloat16* __restrict__ out,
@@ -510,8 +519,8 @@ EncodeTiled encoder() {
 }
 
 int fwd_smem(int cin, int cout) {
-  return 1024 + (cin / 8) * kRegion + kNStage * cin * cout * 2 + 8 * (3 + 2 * kNStage) + 16 +
-         4 * 64;
+  const int ns = stages_for(cin, cout);
+  return 1024 + (cin / 8) * kRegion + ns * cin * cout * 2 + 8 * (3 + 2 * ns) + 16 + 4 * 64;
 }
 
 int wgrad_smem(int cin, int cout) {
@@ -521,17 +530,18 @@ int wgrad_smem(int cin, int cout) {
 template <int CIN, int COUT>
 cudaError_t run_conv(const CUtensorMap& map, ConvDims dm, const __nv_bfloat16* w, Epilogue ep,
                      __nv_bfloat16* out, int* err, cudaStream_t st) {
+  constexpr int NS = stages_for(CIN, COUT);
   const int smem = fwd_smem(CIN, COUT);
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_conv<CIN, COUT>,
+    cudaError_t e = cudaFuncSetAttribute(k_conv<CIN, COUT, NS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     attr = true;
   }
   dim3 grid((dm.nx + kTX - 1) / kTX, (dm.ny + kTY - 1) / kTY,
             ((dm.nz + kTZ - 1) / kTZ) * dm.nb);
-  k_conv<CIN, COUT><<<grid, 128, smem, st>>>(map, dm, w, ep, out, err);
+  k_conv<CIN, COUT, NS><<<grid, 128, smem, st>>>(map, dm, w, ep, out, err);
   return cudaGetLastError();
 }
 

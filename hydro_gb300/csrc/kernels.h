@@ -91,7 +91,12 @@ enum {
   FL_HEAT_DONE = 13, FL_HEAT_SWEEPS = 14,  // temperature solve
   FL_STEP_PUNCONV = 15,  // pressure solves of the step that stopped above their tolerance
   FL_STEP_NAN = 16,      // a pressure solve of the step met a NaN residual
-  FL_GUESS_USED = 17, FL_GUESS_DROPPED = 18  // learned initial guesses kept / dropped
+  FL_GUESS_USED = 17, FL_GUESS_DROPPED = 18,  // learned initial guesses kept / dropped
+  // back-off of the learned guess: after a dropped guess the next
+  // FL_GUESS_SKIP steps run without it (1, 2, 4, ... 16 steps; a kept guess
+  // resets it); FL_GUESS_OFF: the current step skips it
+  FL_GUESS_SKIP = 19, FL_GUESS_BACKOFF = 20, FL_GUESS_OFF = 21,
+  FL_GUESS_SKIPPED = 22  // steps that skipped the guess
 };
 enum {
   TK_MOM = 0, TK_PCG_A = 1, TK_PCG_B = 2, TK_PCG_INIT = 3, TK_IND = 4, TK_DT = 5,
@@ -425,7 +430,7 @@ cudaError_t launch_ctl_refine(DevScalars* ds, double tol, double inner_min, int 
 // SIMPLE iteration count of the step is below `limit`; after the guess, the
 // refinement loop's condition is decided again from the guess's residual.
 cudaError_t launch_ctl_guess_gate(DevScalars* ds, int limit, cudaGraphConditionalHandle h,
-                                  cudaStream_t st);
+                                  int use, cudaStream_t st);
 cudaError_t launch_ctl_guess(DevScalars* ds, double tol, double inner_min, int limit,
                              cudaGraphConditionalHandle h, cudaStream_t st);
 // RS_IR_FF = RS_IR_RR (the residual of the zero guess, before a guess).

@@ -275,8 +275,13 @@ __global__ void k_guess_accept(long long n, const unsigned char* ex, const doubl
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     if (keep) {
       ds->flag[FL_GUESS_USED] += 1;
+      ds->flag[FL_GUESS_BACKOFF] = 0;
     } else {
+      // back off: skip the guess in the next 1, 2, 4, ... 16 steps
       ds->flag[FL_GUESS_DROPPED] += 1;
+      const int b = ds->flag[FL_GUESS_BACKOFF];
+      ds->flag[FL_GUESS_BACKOFF] = b ? (2 * b < 16 ? 2 * b : 16) : 1;
+      ds->flag[FL_GUESS_SKIP] = ds->flag[FL_GUESS_BACKOFF];
     }
   }
 }

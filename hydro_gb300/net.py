@@ -126,11 +126,13 @@ def attach(hydro, net, iterations=1, rho_scale=1.0):
 
 
 def guess_stats(hydro):
-    used, dropped = ctypes.c_longlong(), ctypes.c_longlong()
-    st = hydro.lib.hydro_gpu_get_guess_stats(hydro.ctx, ctypes.byref(used), ctypes.byref(dropped))
+    """(kept, dropped, skipped) since the last call (hydro_gpu_get_guess_stats)."""
+    used, dropped, skipped = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+    st = hydro.lib.hydro_gpu_get_guess_stats(hydro.ctx, ctypes.byref(used), ctypes.byref(dropped),
+                                             ctypes.byref(skipped))
     if st != capi.OK:
         raise capi.HydroError(st, "hydro_gpu_get_guess_stats")
-    return used.value, dropped.value
+    return used.value, dropped.value, skipped.value
 
 
 def snapshot_step(hydro, net, rho_scale, dst_ptr):

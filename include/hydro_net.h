@@ -97,9 +97,12 @@ int hydro_net_last_predict(hydro_net* net, double* ms, int* launches);
 int hydro_gpu_set_pressure_guess(hydro_ctx* ctx, hydro_net* net, int iterations,
                                  double rho_scale);
 /* Counters since the last call: pressure solves that started from the
- * network's guess and solves whose guess was dropped (alpha not positive,
- * or a residual not below the zero guess's). */
-int hydro_gpu_get_guess_stats(hydro_ctx* ctx, long long* used, long long* dropped);
+ * network's guess, solves whose guess was dropped (alpha not positive, or a
+ * residual not below the zero guess's), and steps that skipped the guess.
+ * Back-off: a dropped guess makes the next 1, 2, 4, 8 and then 16 steps run
+ * without the network (no forward pass); a kept guess resets it. */
+int hydro_gpu_get_guess_stats(hydro_ctx* ctx, long long* used, long long* dropped,
+                              long long* skipped);
 
 /* ---- single layers, for checks against a CPU convolution -------------
  * Device buffers; x, y, g*: BF16 [nb][nz][ny][nx][c] with c in {16,32,64};

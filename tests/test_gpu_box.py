@@ -69,8 +69,8 @@ def test_box_mixed_multigrid_and_graph(built):
     b = run(Hydro(dm), u0, q0, 3)
     errs = compare(b, a, mask)
     print("mixed vs FP64", errs)
-    assert errs["u"] <= 1e-6 and errs["F"] <= 1e-6 and errs["q"] <= 1e-6, errs
-    assert errs["p"] <= 5e-6, errs
+    # measured: u 1.2e-7, p 2.3e-9
+    assert all(v <= 1e-6 for v in errs.values()), errs
     h = Hydro(dm)
     h.set_field(capi.F_VELOCITY, u0)
     h.set_field(capi.F_PARTIAL_DENSITY, q0)

@@ -36,7 +36,7 @@ def _run(seed, net=None):
     out = {"u": h.get_field(capi.F_VELOCITY), "p": h.get_field(capi.F_PRESSURE),
            "F": h.get_field(capi.F_VOLUME_FLUX), "q": h.get_field(capi.F_PARTIAL_DENSITY),
            "stats": stats}
-    out["guess"] = guess_stats(h) if net is not None else (0, 0)
+    out["guess"] = guess_stats(h) if net is not None else (0, 0, 0)
     h.close()
     return out
 
@@ -60,11 +60,13 @@ def test_learned_guess_held_out(built):
         it_b = [s["pressure_iterations"] for s in base["stats"]]
         it_l = [s["pressure_iterations"] for s in lrn["stats"]]
         print("seed %d: pressure iterations per step without / with the guess %s / %s, "
-              "guesses kept / dropped %s, field differences %s"
+              "guesses kept / dropped / skipped steps %s, field differences %s"
               % (seed, it_b, it_l, lrn["guess"], {k: "%.1e" % v for k, v in errs.items()}))
         assert all(v <= 1e-6 for v in errs.values()), errs
         for s in base["stats"] + lrn["stats"]:
             assert s["status"] == capi.OK and s["pressure_residual"] <= 1e-8
-        used, dropped = lrn["guess"]
-        assert used + dropped == STEPS and used >= 1
+        used, dropped, skipped = lrn["guess"]
+        # every step either tried the guess (kept or dropped) or skipped it
+        # (back-off after a dropped guess)
+        assert used + dropped + skipped == STEPS and used >= 1
     net.close()
