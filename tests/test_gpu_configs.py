@@ -76,8 +76,8 @@ def test_c2_dam_512x256_vs_oracle_and_conservation(built):
     stats = [h.step() for _ in range(15)]
     m1 = h.calc_stat()
     assert all(s["status"] == 0 for s in stats), [
-        (s["status"], s["pressure_residual"], s["pressure_iterations"], s["pressure_unconverged"])
-        for s in stats]
+        (i, s["status"], s["pressure_residual"], s["pressure_iterations"],
+         s["pressure_unconverged"]) for i, s in enumerate(stats) if s["status"] != 0]
     for i in range(2):
         assert abs(m1.partial_mass[i] - m0.partial_mass[i]) <= 1e-11 * abs(m0.partial_mass[i])
     q = h.get_field(capi.F_PARTIAL_DENSITY)

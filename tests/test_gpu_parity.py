@@ -368,17 +368,33 @@ def test_channel_mixed_and_graph(built):
     d, u0, q0 = cases.channel(nx=16, ny=8, nz=8, dim=3, dt=1e-2, reverse=True)
     d.pressure_tolerance, d.velocity_tolerance = 1e-10, 1e-12
     d.convergence_tolerance, d.num_iterations_limit = 0.0, 3
-    a = run(Hydro(d), u0, q0, 3)
     dm = d.copy()
     dm.precision = capi.MIXED
     dm.pressure_solver = capi.LINEAR_MGCG
-    b = run(Hydro(dm), u0, q0, 3)
+    ha, hb = Hydro(d), Hydro(dm)
+    run(ha, u0, q0, 0)
+    run(hb, u0, q0, 0)
+    pscale = 0.0
+    for _ in range(3):
+        ha.step()
+        hb.step()
+        pa = ha.get_field(capi.F_PRESSURE)
+        pscale = max(pscale, float(np.linalg.norm(pa - pa.mean())))
+    fields = lambda h: {"u": h.get_field(capi.F_VELOCITY), "p": h.get_field(capi.F_PRESSURE),  # noqa: E731
+                        "F": h.get_field(capi.F_VOLUME_FLUX),
+                        "q": h.get_field(capi.F_PARTIAL_DENSITY)}
+    a, b = fields(ha), fields(hb)
     errs = compare(b, a)
-    print("mixed vs FP64", errs)
-    # velocity and fluxes within the mixed bar; the pressure of a channel
-    # started from rest carries the FP32 rounding of the assembled momentum
-    # fluxes relative to its own (smaller) scale: measured 1.6e-6
+    pa, pb = a["p"] - a["p"].mean(), b["p"] - b["p"].mean()
+    p_run = float(np.linalg.norm(pb - pa)) / pscale
+    print("mixed vs FP64", errs, "pressure error / largest pressure of the run", p_run)
+    # The channel starts from rest: its first step builds a pressure 260x
+    # the steady one (rms 87 -> 0.33), and the FP32 rounding of that
+    # transient (7e-9 relative) stays in p as an absolute offset, 1.6e-6 of
+    # the small steady pressure.  Against the pressure scale of the run it
+    # is ~1e-8; velocity and fluxes are within the 1e-6 bar.
     assert errs["u"] <= 1e-6 and errs["F"] <= 1e-6 and errs["q"] <= 1e-6, errs
+    assert p_run <= 1e-6, p_run
     assert errs["p"] <= 5e-6, errs
     h = Hydro(dm)
     h.set_field(capi.F_VELOCITY, u0)
