@@ -76,7 +76,8 @@ enum {
   RS_HEAT_DIFF = 21,     // max |update| of the last temperature sweep
   RS_MOM_DIFF_RED = 22,  // max |update| of the red half of a Gauss-Seidel sweep
   RS_GUESS_S0 = 23, RS_GUESS_S1 = 24,  // <x, f'>, <x, A x> of a learned initial guess
-  RS_MG0_SCALE = 25      // power-of-two scale of the FP16 finest-level couplings
+  RS_MG0_SCALE = 25,     // power-of-two scale of the FP16 finest-level couplings
+  RS_PCG_RRREF = 26      // inner multigrid CG: ||r||^2 at its last halving
 };
 enum {
   FL_MOM_DONE = 0, FL_MOM_SWEEPS = 1, FL_PCG_DONE = 2, FL_PCG_ITERS = 3, FL_NAN = 4,
@@ -96,7 +97,8 @@ enum {
   // FL_GUESS_SKIP steps run without it (1, 2, 4, ... 16 steps; a kept guess
   // resets it); FL_GUESS_OFF: the current step skips it
   FL_GUESS_SKIP = 19, FL_GUESS_BACKOFF = 20, FL_GUESS_OFF = 21,
-  FL_GUESS_SKIPPED = 22  // steps that skipped the guess
+  FL_GUESS_SKIPPED = 22, // steps that skipped the guess
+  FL_PCG_REFIT = 23      // inner multigrid CG: iteration of its last halving of ||r||
 };
 enum {
   TK_MOM = 0, TK_PCG_A = 1, TK_PCG_B = 2, TK_PCG_INIT = 3, TK_IND = 4, TK_DT = 5,

@@ -509,11 +509,22 @@ __global__ void __launch_bounds__(NT) k_mgcg_init(long long n, const double* __r
       ds->red[RS_PCG_FF] = o[0];
       ds->red[RS_PCG_RR] = o[0];
       ds->red[RS_PCG_TOL2] = tol * tol * o[0];
+      ds->red[RS_PCG_RRREF] = o[0];
       ds->flag[FL_PCG_ITERS] = 0;
+      ds->flag[FL_PCG_REFIT] = 0;
       ds->flag[FL_PCG_DONE] = (o[0] == 0. || ds->flag[FL_PCG_LIMIT] <= 0) ? 1 : 0;
     }
   }
 }
+
+// Iterations without a halving of ||r|| after which the inner solve stops
+// and hands the FP64 refinement a fresh residual: a multigrid-preconditioned
+// CG halves ||r|| every iteration or two, and in FP32 on a singular
+// (all-Neumann) system the recursive residual picks up a constant component
+// from rounding that the operator cannot remove, so the recursion can
+// stall above the requested inner tolerance.  The restart from the
+// projected FP64 residual removes it.
+constexpr int kStallIters = 40;
 
 // x += alpha p, r -= alpha Ap; ||r||^2 and the stop test.
 __global__ void __launch_bounds__(NT) k_mgcg_update(long long n, float* __restrict__ x,
@@ -561,7 +572,12 @@ __global__ void __launch_bounds__(NT) k_mgcg_update(long long n, float* __restri
       ds->red[RS_PCG_RR] = o[0];
       int it = ds->flag[FL_PCG_ITERS] + 1;
       ds->flag[FL_PCG_ITERS] = it;
-      if (o[0] <= ds->red[RS_PCG_TOL2] || it >= ds->flag[FL_PCG_LIMIT] || isnan(o[0]))
+      if (o[0] <= 0.25 * ds->red[RS_PCG_RRREF]) {
+        ds->red[RS_PCG_RRREF] = o[0];
+        ds->flag[FL_PCG_REFIT] = it;
+      }
+      if (o[0] <= ds->red[RS_PCG_TOL2] || it >= ds->flag[FL_PCG_LIMIT] || isnan(o[0]) ||
+          it - ds->flag[FL_PCG_REFIT] >= kStallIters)
         ds->flag[FL_PCG_DONE] = 1;
     }
   }
