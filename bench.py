@@ -626,11 +626,17 @@ def run_batch(args):
     256^2 cells (Re log-uniform in [100, 5000], dt 1e-3, SIMPLE converged
     per case to max |du| 1e-8 within 20 iterations), mixed precision with
     the multigrid CG, all cases advanced by one CUDA-graph launch per batch
-    step (hydro_gpu_batch_step).  Prints one JSON line: Mcell-updates/s =
-    cells of all cases x batch steps / seconds."""
+    step (hydro_gpu_batch_step).  The launch shape of each case's linear
+    solves (grid-wide, or one CTA of 256 / 512 / 1024 threads per solve) is
+    chosen per grid size by the autotuner (hydro_gb300/autotune.py) before
+    the run, unless --cta-threads fixes it.  The process runs with
+    CUDA_DEVICE_MAX_CONNECTIONS=32 (set before CUDA starts), so that the
+    GPU takes up to 32 of the graph's independent branches at once instead
+    of 8.  Prints one JSON line: Mcell-updates/s = cells of all cases x
+    batch steps / seconds."""
     import torch
 
-    from hydro_gb300 import capi, cases
+    from hydro_gb300 import autotune, capi, cases
     from hydro_gb300.solver import Batch, launch_count
     specs = cases.cavity_batch(ncases=args.cases, seed=0)
     descs = []
@@ -639,6 +645,16 @@ def run_batch(args):
         d.precision = capi.MIXED
         d.pressure_solver = capi.LINEAR_MGCG
         descs.append(d)
+    if args.cta_threads is None:
+        t0 = time.perf_counter()
+        table = autotune.tune([(d, u0, q0) for d, (_, u0, q0, _) in zip(descs, specs)])
+        tuning = {"by": "hydro_gb300/autotune.py", "seconds": round(time.perf_counter() - t0, 1),
+                  "choices": table}
+        autotune.apply(descs, table)
+    else:
+        for d in descs:
+            d.cta_threads = args.cta_threads
+        tuning = {"by": "--cta-threads", "cta_threads": args.cta_threads}
     b = Batch(descs)
     for c, (d, u0, q0, _) in zip(b.cases, specs):
         c.set_field(capi.F_VELOCITY, u0)
@@ -662,7 +678,10 @@ def run_batch(args):
            "ms_per_step": round(sec * 1e3 / args.steps, 2), "higher_is_better": True,
            "dtype": "f64+f32", "data": "synthetic: seeded cavity sizes and Reynolds numbers",
            "config": {"workload": "cavity_batch_%d" % args.cases, "cells": cells,
-                      "form": "mixed_mg, one graph launch per batch step"},
+                      "form": "mixed_mg, one graph launch per batch step",
+                      "cuda_device_max_connections":
+                          os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
+                      "tuning": tuning},
            "gpu_launches": launch_count() - l0, "clocks": clk,
            "simple_iterations_mean": round(sum(iters) / len(iters), 2),
            "status_ok": all(s["status"] == 0 for st in stats for s in st)}
@@ -747,8 +766,13 @@ def main():
     ap.add_argument("--workload", default="drops", choices=["drops", "batch"],
                     help="batch: the 512-cavity batch (its own JSON line)")
     ap.add_argument("--cases", type=int, default=512, help="--workload batch: cases")
+    ap.add_argument("--cta-threads", type=int, default=None,
+                    help="--workload batch: launch shape of every case's solves (0: grid-wide; "
+                         "default: chosen per grid size by the autotuner)")
     args = ap.parse_args()
     if args.workload == "batch":
+        # before anything starts CUDA in this process
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
         run_batch(args)
         return
     if args.profile_case:

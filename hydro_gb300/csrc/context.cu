@@ -492,6 +492,24 @@ int solve_momentum(hydro_ctx* x) {
     }
     return HYDRO_OK;
   }
+  if (f32 && d.cta_threads > 0) {
+    // the whole Jacobi loop by one CTA
+    CK(launch_cta_mom_jacobi32(x->m, d.velocity_omega, d.velocity_tolerance, x->o32p(),
+                               fp3(x->du32[0]), fp3(x->du32[1]), limit, x->graph_mode ? 1 : 0,
+                               d.cta_threads, x->pw.ds, x->st));
+    if (x->graph_mode) {
+      const long long n = x->m.nc * dim;
+      CK(launch_select_sweep(n, nullptr, x->du[0], x->du32[1], x->du32[0], x->pw.ds, x->st));
+      x->du_cur = 0;
+      return HYDRO_OK;
+    }
+    rc = sync_scalars(x);
+    if (rc) return rc;
+    const int sweeps = x->hds->flag[FL_MOM_SWEEPS];
+    x->vel_sweeps += sweeps;
+    x->du_cur = sweeps > 0 ? (sweeps - 1) % 2 : 0;
+    return HYDRO_OK;
+  }
   auto sweep = [&](int k) -> int {
     if (f32) {
       PK(x, HYDRO_PROF_MOM_SWEEP,
@@ -689,6 +707,23 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
   // still solved to the FP64 tolerance; only the inner corrections are FP32)
   int mixed = (d.precision == HYDRO_MIXED) || d.pressure_solver == HYDRO_LINEAR_MGCG;
   CK(pcg_prepare(m, x->kf, 0., w, mixed, x->st));
+  if (d.cta_threads > 0) {
+    // the whole solve by one CTA
+    CK(mg_setup(x->mg, w, x->st));
+    CK(cta_pressure(m, x->kf, x->prhs, x->pc, singular, d.pressure_tolerance, 1e-5,
+                    d.pressure_iters_limit, x->graph_mode ? 1 : 0, d.cta_threads, w, x->mg,
+                    x->st));
+    if (x->graph_mode) return HYDRO_OK;
+    int rc = sync_scalars(x);
+    if (rc) return rc;
+    x->p_iters += x->hds->flag[FL_PCG_ITERS];
+    x->p_res = x->hds->red[RS_P_RES];
+    if (!x->hds->flag[FL_PCG_DONE]) {
+      if (std::isnan(x->hds->red[RS_IR_RR])) return HYDRO_ERR_NAN;
+      x->p_unconv++;
+    }
+    return HYDRO_OK;
+  }
   if (x->graph_mode) return solve_pressure_graph(x, singular, mixed, apply_pin);
   int rc;
   if (!mixed) {
@@ -856,6 +891,15 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
     if (!v_known || !p_known) return HYDRO_ERR_ARG;
     if ((!v_ok || !p_ok) && !desc->substitute_solvers) return HYDRO_ERR_UNSUPPORTED;
   }
+  if (desc->cta_threads != 0) {
+    const int t = desc->cta_threads;
+    if (t < 32 || t > 1024 || t % 32) return HYDRO_ERR_ARG;
+    if (desc->precision != HYDRO_MIXED || desc->pressure_solver != HYDRO_LINEAR_MGCG ||
+        desc->rigid_box)
+      return HYDRO_ERR_UNSUPPORTED;
+    for (int d = 0; d < desc->dim && d < 3; ++d)
+      if (desc->periodic[d]) return HYDRO_ERR_UNSUPPORTED;
+  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return HYDRO_ERR_NO_DEVICE;
   hydro_ctx* x = new (std::nothrow) hydro_ctx();
@@ -1007,7 +1051,8 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
     mg.cinv = mg.nlev >= 2 ? a.take<float>(kMgCoarseTarget * kMgCoarseTarget) : nullptr;
     // colour-blocked FP16 finest level (plain 3D block, even n[0])
     const bool plain = !m.per[0] && !m.per[1] && !m.per[2] && exmask.empty();
-    if (mg.nlev >= 2 && m.dim == 3 && plain && m.n[0] % 2 == 0 && m.nc < (1LL << 30)) {
+    if (mg.nlev >= 2 && m.dim == 3 && plain && m.n[0] % 2 == 0 && m.nc < (1LL << 30) &&
+        !desc->cta_threads) {
       const long long n0 = m.n[0], n1 = m.n[1], n2 = m.n[2];
       mg.k16[0] = a.take<unsigned short>((n0 + 1) * n1 * n2);
       mg.k16[1] = a.take<unsigned short>(n0 * (n1 + 1) * n2);
@@ -1057,6 +1102,7 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
   }
   x->pw.pin = desc->pressure_fixed_cell;
   x->pw.prof = &x->prof;
+  x->mg.cta = desc->cta_threads > 0;
   if (mg_prepare(x->mg) != cudaSuccess) {
     hydro_gpu_destroy(x);
     return HYDRO_ERR_CUDA;
@@ -2163,7 +2209,8 @@ int hydro_gpu_set_pressure_guess(hydro_ctx* x, hydro_net* net, int iterations,
     return HYDRO_OK;
   }
   const bool refine = x->d.precision == HYDRO_MIXED || x->d.pressure_solver == HYDRO_LINEAR_MGCG;
-  if (!refine || !net_check_grid(net, x->dim, x->m.n)) return HYDRO_ERR_UNSUPPORTED;
+  if (!refine || x->d.cta_threads > 0 || !net_check_grid(net, x->dim, x->m.n))
+    return HYDRO_ERR_UNSUPPORTED;
   // one forward pass outside any capture: kernel attributes and module
   // loading happen here, not inside a captured step
   int rc = net_predict_async(net, x->prhs, x->rho, rho_scale, x->pc, x->st);

@@ -539,6 +539,83 @@ __global__ void __launch_bounds__(NT) k_mom_sweep32(Mesh m, float omega, double 
   }
 }
 
+// The whole Jacobi loop of k_mom_sweep32 by ONE CTA on a plain block (no
+// periodic direction, no excluded cell): sweep k reads d[(k+1) % 2] and
+// writes d[k % 2] as the grid launches do, with the same per-cell
+// arithmetic and the same stop test on the largest correction (a maximum,
+// so the result does not depend on the CTA's order), up to `limit` sweeps.
+// For small cases run many at once: each takes one SM instead of queueing
+// two launches per sweep.
+template <int DIM>
+__global__ void __launch_bounds__(1024) k_cta_mom_jacobi32(Mesh m, float omega, double tol,
+                                                           FP<10> c, FP<3> d0, FP<3> d1,
+                                                           int limit, int graph,
+                                                           DevScalars* ds) {
+  constexpr bool kPerT = false;
+  __shared__ float red[33];
+  const int n = (int)m.nc, tid = threadIdx.x, nt = blockDim.x;
+  int sweeps = 0;
+  float dall = 0.f;
+  bool done = false;
+  for (int k = 0; k < limit; ++k) {
+    const FP<3>& din = (k & 1) ? d0 : d1;
+    const FP<3>& dout = (k & 1) ? d1 : d0;
+    const bool first = k == 0;
+    float dmax = 0.f;
+    for (int q = tid; q < n; q += nt) {
+      Cell X;
+      X.c = q;
+      X.i[0] = q % m.n[0];
+      const int r = q / m.n[0];
+      X.i[1] = DIM == 3 ? r % m.n[1] : r;
+      X.i[2] = DIM == 3 ? r / m.n[1] : 0;
+      float iaP = c.a[0][X.c];
+      float a[2 * DIM];
+#pragma unroll
+      for (int e = 0; e < 2 * DIM; ++e) a[e] = c.a[1 + e][X.c];
+#pragma unroll
+      for (int v = 0; v < DIM; ++v) {
+        float sum = 0.f, cur = 0.f;
+        if (!first) {
+          cur = din.a[v][X.c];
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) {
+            long long s = cell_stride(m, d);
+            if (HAS_LO(d)) sum = fmaf(a[2 * d], din.a[v][NB_LO(d, s)], sum);
+            if (HAS_HI(d)) sum = fmaf(a[2 * d + 1], din.a[v][NB_HI(d, s)], sum);
+          }
+        }
+        float value = -(c.a[7 + v][X.c] + sum) * iaP;
+        float corr = value - cur;
+        dmax = fmaxf(dmax, fabsf(corr));
+        dout.a[v][X.c] = fmaf(corr, omega, cur);
+      }
+    }
+    dmax = warp_max(dmax);
+    if ((tid & 31) == 0) red[tid >> 5] = dmax;
+    __syncthreads();
+    if (tid < 32) {
+      float v = tid < (nt + 31) / 32 ? red[tid] : 0.f;
+      v = warp_max(v);
+      if (tid == 0) red[32] = v;
+    }
+    __syncthreads();
+    dall = red[32];
+    __syncthreads();
+    sweeps = k + 1;
+    if (!((double)dall > tol)) {
+      done = true;
+      break;
+    }
+  }
+  if (tid == 0) {
+    ds->red[RS_MOM_DIFF] = (double)dall;
+    ds->flag[FL_MOM_SWEEPS] = sweeps;
+    ds->flag[FL_MOM_DONE] = done ? 1 : 0;
+    if (graph) ds->flag[FL_STEP_SWEEPS] += sweeps;
+  }
+}
+
 __global__ void k_f2d3(long long n, int dim, FP<3> in, W3 out) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
@@ -1310,6 +1387,19 @@ cudaError_t launch_mom_sweep32(const Mesh& m, double omega, double tol, FP<10> c
                                FP<3> dout, int limit, double* partials, DevScalars* ds,
                                cudaStream_t st) {
   DISPATCH_DIM_P(m, k_mom_sweep32, m, (float)omega, tol, c, din, dout, limit, partials, ds);
+}
+
+cudaError_t launch_cta_mom_jacobi32(const Mesh& m, double omega, double tol, FP<10> c, FP<3> d0,
+                                    FP<3> d1, int limit, int graph, int threads, DevScalars* ds,
+                                    cudaStream_t st) {
+  if (any_periodic(m) || m.nc >= (1LL << 31) || threads < 32 || threads > 1024 || threads % 32)
+    return cudaErrorInvalidValue;
+  if (m.dim == 3)
+    k_cta_mom_jacobi32<3><<<1, threads, 0, st>>>(m, (float)omega, tol, c, d0, d1, limit, graph, ds);
+  else
+    k_cta_mom_jacobi32<2><<<1, threads, 0, st>>>(m, (float)omega, tol, c, d0, d1, limit, graph, ds);
+  count_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_f2d3(const Mesh& m, FP<3> in, W3 out, cudaStream_t st) {

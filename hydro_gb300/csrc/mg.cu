@@ -353,43 +353,43 @@ __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, co
   __syncthreads();
 }
 
+// The levels of one V-cycle run by one CTA, by pointer (shared or global
+// memory): b[0] is the right-hand side, x[0] receives M^-1 b.
+struct CtaLevels {
+  int nl;  // levels, finest first
+  int nsweep, coarse_sweeps;
+  const float* cinv;  // dense inverse of the coarsest level, or null (sweeps)
+  long long pin;      // pinned cell of the finest level (-1: none)
+  Mesh m[kMgMaxLevels];
+  const float* kf[kMgMaxLevels];
+  const float* idg[kMgMaxLevels];
+  float* x[kMgMaxLevels];
+  float* b[kMgMaxLevels];
+};
+
+// One V-cycle by the calling CTA (all its threads; red: 32 floats of shared
+// scratch).  Ends with a __syncthreads.
 template <int DIM, bool PER>
-__global__ void __launch_bounds__(kBlkThreads)
-    k_mg_block_vcycle(MgBlock B, const float* btop, float* xtop, const DevScalars* ds) {
-  if (ds->flag[FL_PCG_DONE]) return;
-  extern __shared__ float sm[];
-  __shared__ float red[32];
+__device__ void cta_vcycle(const CtaLevels& B, float* red) {
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int l = 0; l < B.nl; ++l) {
-    const int nf = (int)B.m[l].nf, nc = (int)B.m[l].nc;
-    for (int q = tid; q < nf; q += nt) sm[B.ok[l] + q] = B.kf[l][q];
-    for (int q = tid; q < nc; q += nt) sm[B.oi[l] + q] = B.idg[l][q];
-  }
-  for (int q = tid; q < (int)B.m[0].nc; q += nt) sm[B.ob[0] + q] = btop[q];
-  if (B.cinv) {
-    const int n = (int)B.m[B.nl - 1].nc;
-    for (int q = tid; q < n * n; q += nt) sm[B.oc + q] = B.cinv[q];
-  }
-  __syncthreads();
   const int ns = B.nsweep;
   for (int l = 0; l + 1 < B.nl; ++l) {
     const Mesh& m = B.m[l];
     long long lp = l == 0 ? B.pin : -1;
-    const float *kf = sm + B.ok[l], *idg = sm + B.oi[l], *b = sm + B.ob[l];
-    float* x = sm + B.ox[l];
     for (int s = 0; s < ns; ++s) {
-      blk_half<DIM, PER>(m, kf, idg, b, x, 0, s == 0, lp);
-      blk_half<DIM, PER>(m, kf, idg, b, x, 1, false, lp);
+      blk_half<DIM, PER>(m, B.kf[l], B.idg[l], B.b[l], B.x[l], 0, s == 0, lp);
+      blk_half<DIM, PER>(m, B.kf[l], B.idg[l], B.b[l], B.x[l], 1, false, lp);
     }
-    blk_restrict<DIM, PER>(m, B.m[l + 1], kf, b, x, sm + B.ob[l + 1], lp);
+    blk_restrict<DIM, PER>(m, B.m[l + 1], B.kf[l], B.b[l], B.x[l], B.b[l + 1], lp);
   }
   {
     const int l = B.nl - 1;
     const Mesh& m = B.m[l];
     long long lp = l == 0 ? B.pin : -1;
-    const float *kf = sm + B.ok[l], *idg = sm + B.oi[l];
-    float* b = sm + B.ob[l];
-    float* x = sm + B.ox[l];
+    const float* kf = B.kf[l];
+    const float* idg = B.idg[l];
+    float* b = B.b[l];
+    float* x = B.x[l];
     const int n = (int)m.nc;
     if (lp < 0) {
       // singular Neumann block: project the right-hand side to zero mean
@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(kBlkThreads)
       // exact coarsest solve: x = P b, P the symmetric inverse of the level's
       // operator completed by the constant mode (b has zero mean); one warp
       // per row of P (n <= 64)
-      const float* P = sm + B.oc;
+      const float* P = B.cinv;
       const int lane = tid & 31;
       for (int c = tid >> 5; c < n; c += nt >> 5) {
         float acc = 0.f;
@@ -437,9 +437,8 @@ __global__ void __launch_bounds__(kBlkThreads)
     const Mesh& m = B.m[l];
     const Mesh& cm = B.m[l + 1];
     long long lp = l == 0 ? B.pin : -1;
-    const float *kf = sm + B.ok[l], *idg = sm + B.oi[l], *b = sm + B.ob[l];
-    float* x = sm + B.ox[l];
-    const float* cx = sm + B.ox[l + 1];
+    float* x = B.x[l];
+    const float* cx = B.x[l + 1];
     for (int c = tid; c < (int)m.nc; c += nt) {
       int id[3];
       blk_ijk<DIM>(m, c, id);
@@ -447,10 +446,53 @@ __global__ void __launch_bounds__(kBlkThreads)
     }
     __syncthreads();
     for (int s = 0; s < ns; ++s) {
-      blk_half<DIM, PER>(m, kf, idg, b, x, 1, false, lp);
-      blk_half<DIM, PER>(m, kf, idg, b, x, 0, false, lp);
+      blk_half<DIM, PER>(m, B.kf[l], B.idg[l], B.b[l], x, 1, false, lp);
+      blk_half<DIM, PER>(m, B.kf[l], B.idg[l], B.b[l], x, 0, false, lp);
     }
   }
+}
+
+// The levels from `top` down, staged into shared memory (MgBlock offsets),
+// as a CtaLevels set (built by thread 0; the caller synchronises).
+__device__ void cta_stage_levels(const MgBlock& B, float* sm, CtaLevels* V, int first = 0) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int l = 0; l < B.nl; ++l) {
+    const int nf = (int)B.m[l].nf, nc = (int)B.m[l].nc;
+    for (int q = tid; q < nf; q += nt) sm[B.ok[l] + q] = B.kf[l][q];
+    for (int q = tid; q < nc; q += nt) sm[B.oi[l] + q] = B.idg[l][q];
+  }
+  if (B.cinv) {
+    const int n = (int)B.m[B.nl - 1].nc;
+    for (int q = tid; q < n * n; q += nt) sm[B.oc + q] = B.cinv[q];
+  }
+  if (tid == 0) {
+    V->nl = first + B.nl;
+    V->nsweep = B.nsweep;
+    V->coarse_sweeps = B.coarse_sweeps;
+    V->cinv = B.cinv ? sm + B.oc : nullptr;
+    V->pin = B.pin;
+    for (int l = 0; l < B.nl; ++l) {
+      V->m[first + l] = B.m[l];
+      V->kf[first + l] = sm + B.ok[l];
+      V->idg[first + l] = sm + B.oi[l];
+      V->x[first + l] = sm + B.ox[l];
+      V->b[first + l] = sm + B.ob[l];
+    }
+  }
+}
+
+template <int DIM, bool PER>
+__global__ void __launch_bounds__(kBlkThreads)
+    k_mg_block_vcycle(MgBlock B, const float* btop, float* xtop, const DevScalars* ds) {
+  if (ds->flag[FL_PCG_DONE]) return;
+  extern __shared__ float sm[];
+  __shared__ float red[32];
+  __shared__ CtaLevels V;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  cta_stage_levels(B, sm, &V);
+  for (int q = tid; q < (int)B.m[0].nc; q += nt) sm[B.ob[0] + q] = btop[q];
+  __syncthreads();
+  cta_vcycle<DIM, PER>(V, red);
   for (int q = tid; q < (int)B.m[0].nc; q += nt) xtop[q] = sm[B.ox[0] + q];
 }
 
@@ -829,6 +871,256 @@ __global__ void __launch_bounds__(NT, 4) k_mg0_restrict(Fast0 f, Mesh cm, const 
   CELL_LOOP_END
 }
 
+// ----------------------------------------- one CTA per pressure solve --
+// The whole mixed pressure solve of a small plain block (no periodic
+// direction, no excluded cell) by ONE CTA: FP64 iterative refinement around
+// the multigrid-preconditioned FP32 CG, the same algorithm as the grid
+// launches (k_ir_residual / k_ctl_refine / k_mgcg_* / the V-cycle), with
+// __syncthreads between the passes instead of kernel boundaries and
+// CTA-wide sums in FP64 in a fixed order.  Hundreds of small cases then
+// each take one SM for their solve instead of queueing a few hundred tiny
+// grid launches apiece.  The levels above `top` stay in global memory (L2
+// for a small case); `top` and below are staged into shared memory once
+// per solve, as the block V-cycle stages them.
+struct CtaPressure {
+  Mesh m;
+  const double *kf, *dg, *f;  // FP64 couplings, diagonal, right-hand side
+  double *x, *r;              // correction (out), FP64 residual
+  const float *kf32, *dg32;   // FP32 level-0 operator
+  float *x32, *r32, *z32, *p, *pb, *Ap;
+  long long pin;
+  int singular, limit, graph;
+  double tol, inner_min;
+  int nl, top;  // levels; first level in shared memory (nl: none)
+  MgBlock blk;  // the staged levels (valid when top < nl)
+  Mesh gm[kMgMaxLevels];
+  const float *gkf[kMgMaxLevels], *gidg[kMgMaxLevels];
+  float *gx[kMgMaxLevels], *gb[kMgMaxLevels];
+  int nsweep, coarse_sweeps;
+  DevScalars* ds;
+};
+
+// CTA-wide FP64 sum, the same value in every thread (sd: 33 doubles).
+__device__ double cta_sum(double v, double* sd) {
+  v = warp_sum(v);
+  const int nw = (blockDim.x + 31) >> 5;
+  if ((threadIdx.x & 31) == 0) sd[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = (int)threadIdx.x < nw ? sd[threadIdx.x] : 0.;
+    t = warp_sum(t);
+    if (threadIdx.x == 0) sd[32] = t;
+  }
+  __syncthreads();
+  const double r = sd[32];
+  __syncthreads();
+  return r;
+}
+
+// z = M^-1 r on the CTA's level set (the finest level staged or not).
+template <int DIM>
+__device__ void cta_precondition(const CtaPressure& P, CtaLevels& V, float* sm, float* red) {
+  const int n = (int)P.m.nc;
+  if (P.top == 0) {
+    for (int c = threadIdx.x; c < n; c += blockDim.x) V.b[0][c] = P.r32[c];
+    __syncthreads();
+  }
+  cta_vcycle<DIM, false>(V, red);
+  if (P.top == 0) {
+    for (int c = threadIdx.x; c < n; c += blockDim.x) P.z32[c] = V.x[0][c];
+    __syncthreads();
+  }
+}
+
+// Inner MG-CG for A e = r (FP32, e in x32) to relative tolerance t within
+// `lim` iterations, stopping on a stall as k_mgcg_update does; returns the
+// iterations.
+template <int DIM>
+__device__ int cta_mgcg(const CtaPressure& P, CtaLevels& V, float* sm, float* red, double* sd,
+                        double t, int lim) {
+  const Mesh& m = P.m;
+  const int n = (int)m.nc, tid = threadIdx.x, nt = blockDim.x;
+  double s = 0.;
+  for (int c = tid; c < n; c += nt) {
+    const double v = P.r[c];
+    P.r32[c] = d2f(v);
+    P.x32[c] = 0.f;
+    s += v * v;
+  }
+  const double rr0 = cta_sum(s, sd);
+  if (rr0 == 0. || lim <= 0) return 0;
+  const double tol2 = t * t * rr0;
+  cta_precondition<DIM>(P, V, sm, red);
+  s = 0.;
+  for (int c = tid; c < n; c += nt) s += (double)P.r32[c] * (double)P.z32[c];
+  double rz = cta_sum(s, sd);
+  double rref = rr0, beta = 0.;
+  int it = 0, refit = 0;
+  float* pold = P.p;
+  float* pnew = P.pb;
+  const int cs[3] = {1, m.n[0], m.n[0] * m.n[1]};
+  const int fs[3] = {1, (int)m.fnx[1], (int)(m.fnx[2] * m.fny[2])};
+  const int pin = (int)P.pin;
+  for (;;) {
+    // p = z + beta p_old (z on the first), Ap, <p, Ap> (k_cg32_dir_spmv)
+    const bool first = it == 0;
+    const float bt = (float)beta;
+    auto Pv = [&](int c) { return first ? P.z32[c] : fmaf(bt, pold[c], P.z32[c]); };
+    s = 0.;
+    for (int c = tid; c < n; c += nt) {
+      int id[3];
+      blk_ijk<DIM>(m, c, id);
+      const float pc = Pv(c);
+      pnew[c] = pc;
+      float a;
+      if (c == pin) {
+        a = pc;
+      } else {
+        a = P.dg32[c] * pc;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          const int fl = (int)m.fofs[d] + id[0] + m.fnx[d] * (id[1] + m.fny[d] * id[2]);
+          if (id[d] > 0 && c - cs[d] != pin) a = fmaf(-P.kf32[fl], Pv(c - cs[d]), a);
+          if (id[d] < m.n[d] - 1 && c + cs[d] != pin) a = fmaf(-P.kf32[fl + fs[d]], Pv(c + cs[d]), a);
+        }
+      }
+      P.Ap[c] = a;
+      s += (double)pc * (double)a;
+    }
+    const double pAp = cta_sum(s, sd);
+    const float at = (float)(rz / pAp);
+    s = 0.;
+    for (int c = tid; c < n; c += nt) {
+      P.x32[c] = fmaf(at, pnew[c], P.x32[c]);
+      const float rc = fmaf(-at, P.Ap[c], P.r32[c]);
+      P.r32[c] = rc;
+      s += (double)rc * (double)rc;
+    }
+    const double rr = cta_sum(s, sd);
+    ++it;
+    if (rr <= 0.25 * rref) {
+      rref = rr;
+      refit = it;
+    }
+    if (rr <= tol2 || it >= lim || isnan(rr) || it - refit >= kStallIters) break;
+    cta_precondition<DIM>(P, V, sm, red);
+    s = 0.;
+    for (int c = tid; c < n; c += nt) s += (double)P.r32[c] * (double)P.z32[c];
+    const double rz1 = cta_sum(s, sd);
+    beta = rz1 / rz;
+    rz = rz1;
+    float* tmp = pold;
+    pold = pnew;
+    pnew = tmp;
+  }
+  return it;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kBlkThreads)
+    k_cta_pressure(const __grid_constant__ CtaPressure P) {
+  extern __shared__ float sm[];
+  __shared__ float red[32];
+  __shared__ double sd[33];
+  __shared__ CtaLevels V;
+  const Mesh& m = P.m;
+  const int n = (int)m.nc, tid = threadIdx.x, nt = blockDim.x;
+  // level set: global levels above top, shared from top
+  if (P.top < P.nl) cta_stage_levels(P.blk, sm, &V, P.top);
+  if (tid == 0) {
+    V.nl = P.nl;
+    V.nsweep = P.nsweep;
+    V.coarse_sweeps = P.coarse_sweeps;
+    V.pin = P.pin;
+    if (P.top >= P.nl) V.cinv = nullptr;
+    for (int l = 0; l < P.top && l < P.nl; ++l) {
+      V.m[l] = P.gm[l];
+      V.kf[l] = P.gkf[l];
+      V.idg[l] = P.gidg[l];
+      V.x[l] = P.gx[l];
+      V.b[l] = P.gb[l];
+    }
+  }
+  double mean = 0.;
+  if (P.singular) {
+    double s = 0.;
+    for (int c = tid; c < n; c += nt) s += P.f[c];
+    mean = cta_sum(s, sd) / (double)n;  // also orders the staging above
+  } else {
+    __syncthreads();
+  }
+  for (int c = tid; c < n; c += nt) P.x[c] = 0.;
+  const int cs[3] = {1, m.n[0], m.n[0] * m.n[1]};
+  const int fs[3] = {1, (int)m.fnx[1], (int)(m.fnx[2] * m.fny[2])};
+  const long long pin = P.pin;
+  double ff = -1., pres = 0., last = 0.;
+  int total = 0, outer = 0;
+  bool conv = false, nan = false;
+  for (;;) {
+    // FP64 residual r = f - mean - A x (x = 0 on the first pass)
+    double s = 0.;
+    for (int c = tid; c < n; c += nt) {
+      double rc = P.f[c] - mean;
+      if (outer > 0) {
+        double acc;
+        if (c == pin) {
+          acc = P.x[c];
+        } else {
+          int id[3];
+          blk_ijk<DIM>(m, c, id);
+          acc = P.dg[c] * P.x[c];
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) {
+            const int fl = (int)m.fofs[d] + id[0] + m.fnx[d] * (id[1] + m.fny[d] * id[2]);
+            if (id[d] > 0 && c - cs[d] != pin) acc -= P.kf[fl] * P.x[c - cs[d]];
+            if (id[d] < m.n[d] - 1 && c + cs[d] != pin) acc -= P.kf[fl + fs[d]] * P.x[c + cs[d]];
+          }
+        }
+        rc -= acc;
+      }
+      P.r[c] = rc;
+      s += rc * rc;
+    }
+    const double rr = cta_sum(s, sd);
+    last = rr;
+    if (isnan(rr)) {
+      nan = true;
+      break;
+    }
+    if (ff < 0.) ff = rr;
+    pres = ff > 0. ? sqrt(rr / ff) : 0.;
+    if (ff == 0. || rr <= P.tol * P.tol * ff) {
+      conv = true;
+      break;
+    }
+    if (total >= P.limit || outer >= 50) break;
+    const double t = fmax(0.5 * P.tol * sqrt(ff / rr), P.inner_min);
+    total += cta_mgcg<DIM>(P, V, sm, red, sd, t, P.limit - total);
+    for (int c = tid; c < n; c += nt) P.x[c] += (double)P.x32[c];
+    ++outer;
+    __syncthreads();
+  }
+  if (P.singular) {
+    double s = 0.;
+    for (int c = tid; c < n; c += nt) s += P.x[c];
+    const double xm = cta_sum(s, sd) / (double)n;
+    for (int c = tid; c < n; c += nt) P.x[c] -= xm;
+  }
+  if (tid == 0) {
+    DevScalars* ds = P.ds;
+    ds->red[RS_P_RES] = pres;
+    ds->red[RS_IR_RR] = last;  // NaN when the system held one
+    ds->flag[FL_PCG_ITERS] = total;
+    ds->flag[FL_IR_OUTER] = outer;
+    ds->flag[FL_PCG_DONE] = conv ? 1 : 0;
+    if (P.graph) {
+      ds->flag[FL_STEP_PITERS] += total;
+      if (!conv) ds->flag[FL_STEP_PUNCONV] += 1;
+      if (nan) ds->flag[FL_STEP_NAN] = 1;
+    }
+  }
+}
+
 int flat_blocks_mg(long long n) {
   long long b = (n + NT - 1) / NT;
   if (b > 152 * 16) b = 152 * 16;
@@ -938,7 +1230,7 @@ cudaError_t mg_setup(MgWork& mg, PcgWork& w, cudaStream_t st) {
   mg.lev[0].idg = w.idg32;
   // the colour-blocked FP16 finest level: allocated for this mesh, no
   // pinned cell in this solve, and a grid level (not the in-CTA cycle)
-  mg.fast0 = mg.k16[0] != nullptr && w.pin < 0 && mg.nlev >= 2 && mg.top >= 1;
+  mg.fast0 = mg.k16[0] != nullptr && w.pin < 0 && mg.nlev >= 2 && mg.top >= 1 && !mg.cta;
   if (mg.fast0) {
     const Mesh& m = mg.lev[0].m;
     Fast0 f{m.n[0], m.n[1], m.n[2], mg.k16[0], mg.k16[1], mg.k16[2]};
@@ -977,9 +1269,16 @@ cudaError_t mg_prepare(MgWork& mg) {
     mg.smem_bytes += (int)(n * n * sizeof(float));
   }
   if (mg.nlev > 0 && mg.top < mg.nlev) {
-    if (mg.smem_bytes > 227 * 1024) return cudaErrorInvalidValue;
+    // (the kernels' static shared memory adds a few KB)
+    if (mg.smem_bytes > 220 * 1024) return cudaErrorInvalidValue;
     const bool per = any_periodic(mg.lev[0].m);
     const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    if (mg.cta && !per) {
+      cudaError_t e = mg.lev[0].m.dim == 3
+                          ? cudaFuncSetAttribute(k_cta_pressure<3>, attr, mg.smem_bytes)
+                          : cudaFuncSetAttribute(k_cta_pressure<2>, attr, mg.smem_bytes);
+      if (e != cudaSuccess) return e;
+    }
     if (mg.lev[0].m.dim == 3)
       return per ? cudaFuncSetAttribute(k_mg_block_vcycle<3, true>, attr, mg.smem_bytes)
                  : cudaFuncSetAttribute(k_mg_block_vcycle<3, false>, attr, mg.smem_bytes);
@@ -1180,6 +1479,74 @@ cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevSc
 void mg_release(MgWork& mg) {
   if (mg.vc_exec) cudaGraphExecDestroy(mg.vc_exec);
   mg.vc_exec = nullptr;
+}
+
+cudaError_t cta_pressure(const Mesh& m, const double* kf, const double* f, double* x,
+                         int singular, double tol, double inner_min, int limit, int graph,
+                         int threads, PcgWork& w, MgWork& mg, cudaStream_t st) {
+  if (any_periodic(m) || m.nf >= (1LL << 31) || mg.nlev < 1 || threads < 32 || threads > 1024 ||
+      threads % 32)
+    return cudaErrorInvalidValue;
+  CtaPressure P{};
+  P.m = m;
+  P.kf = kf;
+  P.dg = w.dg;
+  P.f = f;
+  P.x = x;
+  P.r = w.r;
+  P.kf32 = w.kf32;
+  P.dg32 = w.dg32;
+  P.x32 = w.x32;
+  P.r32 = w.r32;
+  P.z32 = w.z32;
+  P.p = w.p32;
+  P.pb = w.p32b;
+  P.Ap = w.Ap32;
+  P.pin = w.pin;
+  P.singular = singular;
+  P.limit = limit;
+  P.graph = graph;
+  P.tol = tol;
+  P.inner_min = inner_min;
+  P.nl = mg.nlev;
+  P.top = mg.top < mg.nlev ? mg.top : mg.nlev;
+  P.nsweep = mg.nsweep;
+  P.coarse_sweeps = mg.top < mg.nlev ? mg.coarse_sweeps : mg.coarse_sweeps_large;
+  for (int l = 0; l < P.top; ++l) {
+    const MgLevel& lv = mg.lev[l];
+    P.gm[l] = lv.m;
+    P.gkf[l] = l == 0 ? w.kf32 : lv.kf;
+    P.gidg[l] = l == 0 ? w.idg32 : lv.idg;
+    P.gx[l] = l == 0 ? w.z32 : lv.x;
+    P.gb[l] = l == 0 ? w.r32 : lv.b;
+  }
+  if (P.top < P.nl) {
+    MgBlock& B = P.blk;
+    B.nl = mg.nlev - mg.top;
+    B.nsweep = mg.nsweep;
+    B.coarse_sweeps = mg.coarse_sweeps;
+    B.cinv = mg.cdense ? mg.cinv : nullptr;
+    B.oc = mg.smem_cinv_off;
+    B.pin = mg.top == 0 ? w.pin : -1;
+    int off = 0;
+    for (int q = 0; q < B.nl; ++q) {
+      const MgLevel& lv = mg.lev[mg.top + q];
+      B.m[q] = lv.m;
+      B.kf[q] = mg.top + q == 0 ? w.kf32 : lv.kf;
+      B.idg[q] = mg.top + q == 0 ? w.idg32 : lv.idg;
+      const int c4 = (int)((lv.m.nc + 3) / 4 * 4), f4 = (int)((lv.m.nf + 3) / 4 * 4);
+      B.ox[q] = off; off += c4;
+      B.ob[q] = off; off += c4;
+      B.oi[q] = off; off += c4;
+      B.ok[q] = off; off += f4;
+    }
+  }
+  P.ds = w.ds;
+  const int smem = P.top < P.nl ? mg.smem_bytes : 0;
+  if (m.dim == 3) k_cta_pressure<3><<<1, threads, smem, st>>>(P);
+  else k_cta_pressure<2><<<1, threads, smem, st>>>(P);
+  count_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t mgcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, MgWork& mg,

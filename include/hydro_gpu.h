@@ -218,6 +218,19 @@ typedef struct hydro_desc {
    * tight tolerances: with the reference's loose defaults (one LU sweep,
    * SOR to a max update of 1e-3) the fields differ. */
   int substitute_solvers;
+  /* Linear solves of a small case by ONE CTA each: with 0 (the default)
+   * every sweep and every Krylov iteration is a grid-wide launch; with a
+   * thread count (32..1024, a multiple of 32) the whole velocity Jacobi
+   * loop and the whole pressure solve (FP64 refinement around the
+   * multigrid CG, with CTA-wide FP64 sums in place of the grid reductions)
+   * each run as one launch of one CTA of that many threads.  For batches of
+   * many small cases (hydro_gpu_batch_*), where each case then holds one SM
+   * per solve instead of queueing hundreds of tiny launches.  Needs
+   * precision MIXED, pressure solver MGCG, no periodic direction and no
+   * rigid box (HYDRO_ERR_UNSUPPORTED otherwise); a Gauss-Seidel velocity
+   * solve stays grid-wide.  Results agree with the grid-wide form to the
+   * solver tolerances, not bit for bit (other summation order). */
+  int cta_threads;
 } hydro_desc;
 
 typedef struct hydro_step_stats {

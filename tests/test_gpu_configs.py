@@ -121,10 +121,13 @@ def test_mixed_forms_vs_fp64_full_size(built, config):
     print(config, "largest relative error over 50 steps:", {k: "%.1e" % v for k, v in worst.items()})
 
 
-def test_c5_batch_512_cavities(built):
+@pytest.mark.parametrize("cta_threads", [0, 512])
+def test_c5_batch_512_cavities(built, cta_threads):
     """512 cavities of 64^2..256^2 (13.4 M cells) in one batch, mixed with the
     multigrid CG, SIMPLE converged per case: two batch steps, and four cases
-    of every size stepped alone give the same fields."""
+    of every size stepped alone give the same fields -- with grid-wide
+    solver launches, and with every linear solve by one CTA of 512
+    threads."""
     from hydro_gb300.solver import Batch, Hydro
     specs = cases.cavity_batch(ncases=512, seed=0)
     descs = []
@@ -132,6 +135,7 @@ def test_c5_batch_512_cavities(built):
         d = d.copy()
         d.precision = capi.MIXED
         d.pressure_solver = capi.LINEAR_MGCG
+        d.cta_threads = cta_threads
         descs.append(d)
     b = Batch(descs)
     for c, (d, u0, q0, _) in zip(b.cases, specs):
@@ -151,3 +155,67 @@ def test_c5_batch_512_cavities(built):
             alone = run(Hydro(descs[i]), u0, q0, 2)
             u = b.cases[i].get_field(capi.F_VELOCITY)
             assert rel(u, alone["u"]) <= 1e-12, (n, i)
+
+
+@pytest.mark.parametrize("n,threads", [(64, 256), (96, 512), (256, 1024)])
+def test_cta_solvers_match_grid_solvers(built, n, threads):
+    """The one-CTA linear solves against the grid-wide ones on a cavity
+    (Re 1000, mixed, multigrid CG): same SIMPLE iteration counts, velocity
+    and pressure within 1e-6 of the run's scale after 5 steps (both solve
+    to a pressure residual of 1e-10 and a velocity update of 1e-10; only
+    the summation order differs), and every step converged."""
+    from hydro_gb300.solver import Hydro
+    d, u0, q0 = cases.cavity(n=n, mu=1e-3, dt=1e-3)
+    d.precision = capi.MIXED
+    d.pressure_solver = capi.LINEAR_MGCG
+    d.pressure_tolerance = 1e-10
+    d.velocity_tolerance = 1e-10
+    dc = d.copy()
+    dc.cta_threads = threads
+    a, b = Hydro(d), Hydro(dc)
+    for h in (a, b):
+        h.set_field(capi.F_VELOCITY, u0)
+        h.set_field(capi.F_PARTIAL_DENSITY, q0)
+        h.init_state()
+    for step in range(5):
+        sa = a.step()
+        sb = b.step_graph() if step % 2 else b.step()
+        assert sa["status"] == 0 and sb["status"] == 0, (sa, sb)
+        assert sb["pressure_unconverged"] == 0
+        assert abs(sa["outer_iterations"] - sb["outer_iterations"]) <= 1, (sa, sb)
+    ua, ub = a.get_field(capi.F_VELOCITY), b.get_field(capi.F_VELOCITY)
+    pa, pb = a.get_field(capi.F_PRESSURE), b.get_field(capi.F_PRESSURE)
+    assert np.abs(ua - ub).max() <= 1e-6 * np.abs(ua).max()
+    assert np.abs(pa - pb).max() <= 1e-6 * np.abs(pa).max()
+
+
+def test_cta_solvers_limits_and_nan(built):
+    """The one-CTA pressure solve reports a pressure iteration limit as
+    HYDRO_NOT_CONVERGED (host-driven and graph-captured) and a NaN in the
+    system as HYDRO_ERR_NAN; a rigid box or a periodic direction with
+    cta_threads set is refused."""
+    from hydro_gb300.solver import Hydro, make
+    d, u0, q0 = cases.cavity(n=64, mu=1e-2, dt=1e-3)
+    d.precision = capi.MIXED
+    d.pressure_solver = capi.LINEAR_MGCG
+    d.cta_threads = 256
+    d.pressure_tolerance, d.pressure_iters_limit = 1e-12, 1
+    for graph in (False, True):
+        h = make(d, u0, q0)
+        st = h.step_graph() if graph else h.step()
+        assert st["status"] == capi.NOT_CONVERGED and st["pressure_unconverged"] >= 1, st
+        assert np.all(np.isfinite(h.get_field(capi.F_PRESSURE)))
+    d.pressure_iters_limit = 20000
+    h = make(d, u0, q0)
+    assert h.step()["status"] == capi.OK
+    u = h.get_field(capi.F_VELOCITY)
+    u[d.ncells // 2] = np.nan
+    h.set_field(capi.F_VELOCITY, u)
+    with pytest.raises(capi.HydroError) as e:
+        h.step()
+    assert e.value.status == capi.ERR_NAN
+    bad = d.copy()
+    bad.periodic[0] = 1
+    with pytest.raises(capi.HydroError) as e:
+        Hydro(bad)
+    assert e.value.status == capi.ERR_UNSUPPORTED
