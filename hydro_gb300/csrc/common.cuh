@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 #include "fpconv.h"
 
 namespace hg {
@@ -109,6 +111,38 @@ inline bool any_periodic(const Mesh& m) {
     if (m.per[d]) return true;
   return false;
 }
+
+// Programmatic dependent launch: a kernel launched with pdl() may be
+// scheduled onto SMs while the kernel before it in the stream drains.  Such
+// a kernel calls pdl_wait() before its first memory access -- it returns
+// once the previous kernel has completed and its writes are visible, so the
+// dependency is that of a plain launch -- and pdl_trigger() to let the next
+// one be scheduled in turn (it takes effect once every CTA of this kernel
+// has started or exited, so waiting CTAs never displace this kernel's
+// own).  What overlaps is the launch latency between dependent kernels:
+// a few microseconds each in the chains of small multigrid and Krylov
+// kernels.  Both are no-ops for a plain launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+template <class... P, class... A>
+inline cudaError_t pdl(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       A&&... a) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<A>(a)...);
+}
+// pdl() whose error, like a <<<>>> launch's, is left to cudaGetLastError
+#define PDL(...) ((void)pdl(__VA_ARGS__))
 
 // Launch geometry: blocks of 32x8 threads over (i, j); each block marches
 // KCH planes in k so that the grid stays a few waves deep on 152 SMs.

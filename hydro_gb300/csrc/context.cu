@@ -22,6 +22,7 @@
 #include <new>
 #include <unordered_map>
 #include <utility>
+#include <array>
 #include <vector>
 
 #include "../../include/hydro_gpu.h"
@@ -217,6 +218,10 @@ struct hydro_ctx {
     cudaGraphExec_t exec = nullptr;
     double dt = -1., adv_dt = -1.;
     int substeps = -1, sources = -1, heat_gen = -1;
+    // the time and iteration layers the graph was captured on: a
+    // host-driven step rotates them, after which the graph is captured
+    // again
+    std::array<const void*, 30> layers{};
   } sg;
   // temperature (HeatSolver, heat.hpp:18-94; hydro_gpu_heat_create): its
   // two time layers and the mixture conductivity; the step's gradient,
@@ -1770,12 +1775,31 @@ int next_dt(hydro_ctx* x) {
   return HYDRO_OK;
 }
 
+std::array<const void*, 30> layer_key(const hydro_ctx* x) {
+  std::array<const void*, 30> k{};
+  int n = 0;
+  for (int l = 0; l < 4; ++l) {
+    k[n++] = x->u[l];
+    k[n++] = x->p[l];
+    k[n++] = x->F[l];
+    k[n++] = x->s32.u[l];
+    k[n++] = x->s32.F[l];
+  }
+  k[n++] = x->q;
+  k[n++] = x->qtmp;
+  k[n++] = x->heat.tc;
+  k[n++] = x->heat.tp;
+  return k;
+}
+
 bool graph_stale(const hydro_ctx* x, int substeps) {
   return x->sg.dt != x->dt || x->sg.adv_dt != x->adv_dt || x->sg.substeps != substeps ||
-         x->sg.sources != x->fc.sources || x->sg.heat_gen != x->heat.gen;
+         x->sg.sources != x->fc.sources || x->sg.heat_gen != x->heat.gen ||
+         x->sg.layers != layer_key(x);
 }
 
 void graph_key(hydro_ctx* x, int substeps) {
+  x->sg.layers = layer_key(x);
   x->sg.dt = x->dt;
   x->sg.adv_dt = x->adv_dt;
   x->sg.substeps = substeps;

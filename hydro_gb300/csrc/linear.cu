@@ -444,6 +444,8 @@ __global__ void __launch_bounds__(NT) k_cg32_dir_spmv(Mesh m, const float* __res
                                                       float* __restrict__ Ap, long long pin,
                                                       double* partials, DevScalars* ds,
                                                       int kch) {
+  pdl_wait();
+  pdl_trigger();
   constexpr bool kPerT = PER;
   if (ds->flag[FL_PCG_DONE]) return;
   const bool first = ds->flag[FL_PCG_ITERS] == 0;
@@ -492,6 +494,8 @@ __global__ void __launch_bounds__(NT) k_cg32_dir_spmv_i32(Mesh m, const float* _
                                                           float* __restrict__ Ap, int pin,
                                                           double* partials, DevScalars* ds,
                                                           int kch) {
+  pdl_wait();
+  pdl_trigger();
   if (ds->flag[FL_PCG_DONE]) return;
   const bool first = ds->flag[FL_PCG_ITERS] == 0;
   const float beta = first ? 0.f : (float)ds->red[RS_PCG_BETA];
@@ -580,11 +584,11 @@ cudaError_t cg32_dir_spmv(const Mesh& m, const float* kf, const float* dg, const
                                : (const void*)k_cg32_dir_spmv_i32<2>;
     Launch L = cell_launch_waves(m, resident_ctas(k));
     if (m.dim == 3)
-      k_cg32_dir_spmv_i32<3><<<L.grid, L.block, 0, st>>>(m, kf, dg, z, pold, pnew, Ap, (int)pin,
-                                                         partials, ds, L.kch);
+      PDL(k_cg32_dir_spmv_i32<3>, L.grid, L.block, 0, st, m, kf, dg, z, pold, pnew, Ap, (int)pin,
+          partials, ds, L.kch);
     else
-      k_cg32_dir_spmv_i32<2><<<L.grid, L.block, 0, st>>>(m, kf, dg, z, pold, pnew, Ap, (int)pin,
-                                                         partials, ds, L.kch);
+      PDL(k_cg32_dir_spmv_i32<2>, L.grid, L.block, 0, st, m, kf, dg, z, pold, pnew, Ap, (int)pin,
+          partials, ds, L.kch);
     count_launches(1);
     return cudaGetLastError();
   }

@@ -40,6 +40,8 @@ template <int DIM, bool PER>
 __global__ void __launch_bounds__(NT, PER ? 6 : 8) k_mg_smooth(Mesh m, const float* kf, const float* idg, const float* b, float* x,
                             int color, int zero, long long pin, const float* cx, int cnx,
                             int cny, const DevScalars* ds, int kch) {
+  pdl_wait();
+  pdl_trigger();
   if (ds->flag[FL_PCG_DONE]) return;
   const int ih = blockIdx.x * BX + threadIdx.x;
   const int j = blockIdx.y * BY + threadIdx.y;
@@ -161,6 +163,8 @@ __global__ void __launch_bounds__(256) k_mg_coarse_inv(Mesh m, const float* kf, 
 // last and first coarse cells like the fine one).
 template <int DIM>
 __global__ void k_mg_coarsen(Mesh fm, Mesh cm, const float* fkf, float* ckf, int kch) {
+  pdl_wait();
+  pdl_trigger();
   CELL_LOOP_BEGIN(cm, kch)
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
@@ -192,6 +196,8 @@ __global__ void k_mg_coarsen(Mesh fm, Mesh cm, const float* fkf, float* ckf, int
 
 template <int DIM>
 __global__ void k_mg_diag(Mesh m, const float* kf, float* dg, float* idg, int kch) {
+  pdl_wait();
+  pdl_trigger();
   CELL_LOOP_BEGIN(m, kch)
   float s = 0.f;
 #pragma unroll
@@ -215,6 +221,8 @@ template <int DIM, bool PER>
 __global__ void __launch_bounds__(NT, 4) k_mg_restrict(Mesh fm, Mesh cm, const float* kf, const float* dg, const float* b,
                               const float* x, float* cb, float* cx, const float* cidg,
                               long long pin, const DevScalars* ds, int kch) {
+  pdl_wait();
+  pdl_trigger();
   if (ds->flag[FL_PCG_DONE]) return;
   CELL_LOOP_BEGIN(cm, kch)
   float sum = 0.f;
@@ -484,6 +492,8 @@ __device__ void cta_stage_levels(const MgBlock& B, float* sm, CtaLevels* V, int 
 template <int DIM, bool PER>
 __global__ void __launch_bounds__(kBlkThreads)
     k_mg_block_vcycle(MgBlock B, const float* btop, float* xtop, const DevScalars* ds) {
+  pdl_wait();
+  pdl_trigger();
   if (ds->flag[FL_PCG_DONE]) return;
   extern __shared__ float sm[];
   __shared__ float red[32];
@@ -521,6 +531,8 @@ __global__ void __launch_bounds__(NT) k_mgcg_init(long long n, const double* __r
                                                   float* __restrict__ r, float* __restrict__ x,
                                                   double tol, int limit, int dev_params,
                                                   double* partials, DevScalars* ds) {
+  pdl_wait();
+  pdl_trigger();
   double s = 0.;
   const long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
   const long long g = blockIdx.x * (long long)NT + tid, stride = (long long)gridDim.x * NT;
@@ -574,6 +586,8 @@ __global__ void __launch_bounds__(NT) k_mgcg_update(long long n, float* __restri
                                                     const float* __restrict__ p,
                                                     const float* __restrict__ Ap,
                                                     double* partials, DevScalars* ds) {
+  pdl_wait();
+  pdl_trigger();
   if (ds->flag[FL_PCG_DONE]) return;
   const float at = (float)ds->red[RS_PCG_ALPHA];
   DFAcc2 rr;
@@ -629,6 +643,8 @@ __global__ void __launch_bounds__(NT) k_mgcg_update(long long n, float* __restri
 __global__ void __launch_bounds__(NT) k_mgcg_dot(long long n, const float* __restrict__ r,
                                                  const float* __restrict__ z, int first,
                                                  double* partials, DevScalars* ds) {
+  pdl_wait();
+  pdl_trigger();
   if (ds->flag[FL_PCG_DONE]) return;
   DFAcc2 rz;
   const long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
@@ -740,6 +756,8 @@ __global__ void k_mg0_diag(Fast0 f, const DevScalars* ds, float* idg0) {
 // right-hand side, and the first half-sweep (red, from x = 0: x = b / diag).
 __global__ void k_mg0_split(Fast0 f, const float* r, const float* idg0, float* b0, float* x0,
                             const DevScalars* ds) {
+  pdl_wait();
+  pdl_trigger();
   if (ds->flag[FL_PCG_DONE]) return;
   const int h0 = f.n0 / 2;
   const long long half = (long long)h0 * f.n1 * f.n2;
@@ -764,6 +782,8 @@ template <bool PROLONG, bool ZOUT>
 __global__ void __launch_bounds__(NT) k_mg0_smooth(Fast0 f, const float* idg0, const float* b0,
                                                    float* x0, int color, const float* cx,
                                                    float* z, const DevScalars* ds, int kch) {
+  pdl_wait();
+  pdl_trigger();
   if (ds->flag[FL_PCG_DONE]) return;
   const int h0 = f.n0 / 2;
   const int ih = blockIdx.x * BX + threadIdx.x;
@@ -835,6 +855,8 @@ __global__ void __launch_bounds__(NT, 4) k_mg0_restrict(Fast0 f, Mesh cm, const 
                                                         const float* x0, float* cb, float* cx,
                                                         const float* cidg, const DevScalars* ds,
                                                         int kch) {
+  pdl_wait();
+  pdl_trigger();
   if (ds->flag[FL_PCG_DONE]) return;
   const int h0 = f.n0 / 2;
   const int half = h0 * f.n1 * f.n2;
@@ -1187,20 +1209,20 @@ int mg_levels_for(const Mesh& m) {
 #define MG_LAUNCH(KERNEL, L, ...)                                               \
   do {                                                                          \
     if (dim == 3)                                                               \
-      KERNEL<3><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);          \
+      PDL(KERNEL<3>, (L).grid, (L).block, 0, st, __VA_ARGS__, (L).kch);         \
     else                                                                        \
-      KERNEL<2><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);          \
+      PDL(KERNEL<2>, (L).grid, (L).block, 0, st, __VA_ARGS__, (L).kch);         \
     count_launches(1);                                                          \
   } while (0)
 // the same for kernels instantiated per periodicity (P: any periodic direction)
 #define MG_LAUNCH_P(KERNEL, L, P, ...)                                          \
   do {                                                                          \
     if (dim == 3) {                                                             \
-      if (P) KERNEL<3, true><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);   \
-      else KERNEL<3, false><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);   \
+      if (P) PDL(KERNEL<3, true>, (L).grid, (L).block, 0, st, __VA_ARGS__, (L).kch);   \
+      else PDL(KERNEL<3, false>, (L).grid, (L).block, 0, st, __VA_ARGS__, (L).kch);   \
     } else {                                                                    \
-      if (P) KERNEL<2, true><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);   \
-      else KERNEL<2, false><<<(L).grid, (L).block, 0, st>>>(__VA_ARGS__, (L).kch);   \
+      if (P) PDL(KERNEL<2, true>, (L).grid, (L).block, 0, st, __VA_ARGS__, (L).kch);   \
+      else PDL(KERNEL<2, false>, (L).grid, (L).block, 0, st, __VA_ARGS__, (L).kch);   \
     }                                                                           \
     count_launches(1);                                                          \
   } while (0)
@@ -1314,22 +1336,22 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
     // level 0 on the colour-blocked arrays: split (+ red from zero), then
     // black, (red, black)^(ns-1), restriction of the red residuals
     const Launch H = fast0_launch(m0);
-    k_mg0_split<<<flat_blocks_mg(m0.nc / 2), NT, 0, st>>>(f0, r, mg.idg0, mg.b0, mg.x0, ds);
+    PDL(k_mg0_split, flat_blocks_mg(m0.nc / 2), NT, 0, st, f0, r, mg.idg0, mg.b0, mg.x0, ds);
     count_launches(1);
     for (int s = 0; s < ns; ++s) {
       if (s > 0) {
-        k_mg0_smooth<false, false><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 0,
+        PDL(k_mg0_smooth<false, false>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 0,
                                                               nullptr, nullptr, ds, H.kch);
         count_launches(1);
       }
-      k_mg0_smooth<false, false><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 1,
+      PDL(k_mg0_smooth<false, false>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 1,
                                                             nullptr, nullptr, ds, H.kch);
       count_launches(1);
     }
     MgLevel& c = mg.lev[1];
     Launch L = cell_launch(c.m);
     const float* cidg = 1 < top ? c.idg : nullptr;
-    k_mg0_restrict<<<L.grid, L.block, 0, st>>>(f0, c.m, mg.b0, mg.x0, c.b, c.x, cidg, ds, L.kch);
+    PDL(k_mg0_restrict, L.grid, L.block, 0, st, f0, c.m, mg.b0, mg.x0, c.b, c.x, cidg, ds, L.kch);
     count_launches(1);
   }
   for (int l = fast0 ? 1 : 0; l < top; ++l) {
@@ -1370,11 +1392,11 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
     }
     MgLevel& t = mg.lev[mg.top];
     if (dim == 3) {
-      if (per) k_mg_block_vcycle<3, true><<<1, kBlkThreads, mg.smem_bytes, st>>>(B, t.b, t.x, ds);
-      else k_mg_block_vcycle<3, false><<<1, kBlkThreads, mg.smem_bytes, st>>>(B, t.b, t.x, ds);
+      if (per) PDL(k_mg_block_vcycle<3, true>, 1, kBlkThreads, mg.smem_bytes, st, B, t.b, t.x, ds);
+      else PDL(k_mg_block_vcycle<3, false>, 1, kBlkThreads, mg.smem_bytes, st, B, t.b, t.x, ds);
     } else {
-      if (per) k_mg_block_vcycle<2, true><<<1, kBlkThreads, mg.smem_bytes, st>>>(B, t.b, t.x, ds);
-      else k_mg_block_vcycle<2, false><<<1, kBlkThreads, mg.smem_bytes, st>>>(B, t.b, t.x, ds);
+      if (per) PDL(k_mg_block_vcycle<2, true>, 1, kBlkThreads, mg.smem_bytes, st, B, t.b, t.x, ds);
+      else PDL(k_mg_block_vcycle<2, false>, 1, kBlkThreads, mg.smem_bytes, st, B, t.b, t.x, ds);
     }
     count_launches(1);
   } else {
@@ -1413,22 +1435,22 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
     for (int s = 0; s < ns; ++s) {
       const bool last = s == ns - 1;
       if (s == 0 && last)
-        k_mg0_smooth<true, true><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 1, cx,
+        PDL(k_mg0_smooth<true, true>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 1, cx,
                                                             z, ds, H.kch);
       else if (s == 0)
-        k_mg0_smooth<true, false><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 1, cx,
+        PDL(k_mg0_smooth<true, false>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 1, cx,
                                                              nullptr, ds, H.kch);
       else if (last)
-        k_mg0_smooth<false, true><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 1,
+        PDL(k_mg0_smooth<false, true>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 1,
                                                              nullptr, z, ds, H.kch);
       else
-        k_mg0_smooth<false, false><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 1,
+        PDL(k_mg0_smooth<false, false>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 1,
                                                               nullptr, nullptr, ds, H.kch);
       if (last)
-        k_mg0_smooth<false, true><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 0,
+        PDL(k_mg0_smooth<false, true>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 0,
                                                              nullptr, z, ds, H.kch);
       else
-        k_mg0_smooth<false, false><<<H.grid, H.block, 0, st>>>(f0, mg.idg0, mg.b0, mg.x0, 0,
+        PDL(k_mg0_smooth<false, false>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 0,
                                                               nullptr, nullptr, ds, H.kch);
       count_launches(2);
     }
@@ -1556,14 +1578,14 @@ cudaError_t mgcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, MgW
       !aligned16(w.p32) || !aligned16(w.p32b) || !aligned16(w.Ap32))
     return cudaErrorInvalidValue;
   w.p32_parity = 0;
-  k_mgcg_init<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.r, w.r32, w.x32, tol, w.limit, dev_params,
-                                           w.partials, w.ds);
+  PDL(k_mgcg_init, fb, dim3(BX, BY), 0, st, m.nc, w.r, w.r32, w.x32, tol, w.limit, dev_params,
+      w.partials, w.ds);
   count_launches(1);
   if (w.prof) w.prof->begin(HYDRO_PROF_MG_VCYCLE, st);
   cudaError_t e = mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st);
   if (w.prof) w.prof->end(HYDRO_PROF_MG_VCYCLE, st);
   if (e != cudaSuccess) return e;
-  k_mgcg_dot<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.r32, w.z32, 1, w.partials, w.ds);
+  PDL(k_mgcg_dot, fb, dim3(BX, BY), 0, st, m.nc, w.r32, w.z32, 1, w.partials, w.ds);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -1579,14 +1601,14 @@ cudaError_t mgcg_iterate(const Mesh& m, int chunk, PcgWork& w, MgWork& mg, cudaS
     if (w.prof) w.prof->end(HYDRO_PROF_CG_SPMV, st);
     if (e != cudaSuccess) return e;
     if (w.prof) w.prof->begin(HYDRO_PROF_CG_UPDATE, st);
-    k_mgcg_update<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.x32, w.r32, pnew, w.Ap32, w.partials,
-                                               w.ds);
+    PDL(k_mgcg_update, fb, dim3(BX, BY), 0, st, m.nc, w.x32, w.r32, pnew, w.Ap32, w.partials,
+        w.ds);
     if (w.prof) w.prof->end(HYDRO_PROF_CG_UPDATE, st);
     if (w.prof) w.prof->begin(HYDRO_PROF_MG_VCYCLE, st);
     e = mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st);
     if (w.prof) w.prof->end(HYDRO_PROF_MG_VCYCLE, st);
     if (e != cudaSuccess) return e;
-    k_mgcg_dot<<<fb, dim3(BX, BY), 0, st>>>(m.nc, w.r32, w.z32, 0, w.partials, w.ds);
+    PDL(k_mgcg_dot, fb, dim3(BX, BY), 0, st, m.nc, w.r32, w.z32, 0, w.partials, w.ds);
     count_launches(2);
     w.p32_parity ^= 1;
   }

@@ -185,8 +185,8 @@ def test_cta_solvers_match_grid_solvers(built, n, threads):
         assert abs(sa["outer_iterations"] - sb["outer_iterations"]) <= 1, (sa, sb)
     ua, ub = a.get_field(capi.F_VELOCITY), b.get_field(capi.F_VELOCITY)
     pa, pb = a.get_field(capi.F_PRESSURE), b.get_field(capi.F_PRESSURE)
-    assert np.abs(ua - ub).max() <= 1e-6 * np.abs(ua).max()
-    assert np.abs(pa - pb).max() <= 1e-6 * np.abs(pa).max()
+    assert np.abs(ua - ub).max() <= 1e-6 * np.abs(ua).max(), np.abs(ua - ub).max()
+    assert np.abs(pa - pb).max() <= 1e-6 * np.abs(pa).max(), np.abs(pa - pb).max()
 
 
 def test_cta_solvers_limits_and_nan(built):

@@ -109,3 +109,27 @@ def test_graph_step_simpler_channel(built):
     d.convergence_tolerance = 1e-5
     d.num_iterations_limit = 7
     _check(d, u0, q0, 3)
+
+
+@pytest.mark.parametrize("pattern", ["HGHG", "GHGH", "GGHHG"])
+def test_graph_and_host_steps_interleaved(built, pattern):
+    """Host-driven and graph-captured steps interleaved on one context give
+    the host-only run: a host step rotates the time and iteration layers
+    (pointer swaps), after which the graph is captured again instead of
+    replaying launches on the layers it was captured on."""
+    from hydro_gb300.solver import Hydro
+    d, u0, q0 = cases.cavity(n=32, mu=1e-3, dt=1e-3)
+    d.precision = capi.MIXED
+    d.pressure_solver = capi.LINEAR_MGCG
+    ref = _run(d, u0, q0, len(pattern), graph=False)
+    h = Hydro(d)
+    h.set_field(capi.F_VELOCITY, u0)
+    h.set_field(capi.F_PARTIAL_DENSITY, q0)
+    h.init_state()
+    for ch in pattern:
+        st = h.step_graph() if ch == "G" else h.step()
+        assert st["status"] == capi.OK
+    got = {"u": h.get_field(capi.F_VELOCITY), "p": h.get_field(capi.F_PRESSURE),
+           "F": h.get_field(capi.F_VOLUME_FLUX), "q": h.get_field(capi.F_PARTIAL_DENSITY)}
+    errs = compare(got, {k: ref[k] for k in got})
+    assert all(v <= 1e-12 for v in errs.values()), errs
