@@ -19,6 +19,7 @@
 //                      on the zero-mean right-hand side).
 // All kernels return at once when the CG's done flag is set, so iterations
 // can be queued in chunks like the other solvers.
+#include <cooperative_groups.h>
 #include <cuda_fp16.h>
 #include <math.h>
 
@@ -281,6 +282,24 @@ struct MgBlock {
   int ox[kMgMaxLevels], ob[kMgMaxLevels], oi[kMgMaxLevels], ok[kMgMaxLevels];
 };
 
+// Thread groups of the in-CTA helpers: one CTA (__syncthreads) or one
+// thread-block cluster (its CTAs' threads numbered CTA-major, a cluster
+// barrier, which orders the global-memory accesses of its CTAs as well).
+struct CtaG {
+  __device__ int rank() const { return threadIdx.x; }
+  __device__ int size() const { return blockDim.x; }
+  __device__ void sync() const { __syncthreads(); }
+};
+struct ClusterG {
+  int r, n;
+  __device__ ClusterG()
+      : r((int)(cooperative_groups::this_cluster().block_rank() * blockDim.x + threadIdx.x)),
+        n((int)(cooperative_groups::this_cluster().num_blocks() * blockDim.x)) {}
+  __device__ int rank() const { return r; }
+  __device__ int size() const { return n; }
+  __device__ void sync() const { cooperative_groups::this_cluster().sync(); }
+};
+
 template <int DIM>
 __device__ __forceinline__ void blk_ijk(const Mesh& m, int c, int* id) {
   id[0] = c % m.n[0];
@@ -289,14 +308,22 @@ __device__ __forceinline__ void blk_ijk(const Mesh& m, int c, int* id) {
   id[2] = DIM == 3 ? r / m.n[1] : 0;
 }
 
-template <int DIM, bool PER>
+// One red-black half-sweep by the group: slot t of row (j, k) is the cell
+// i = 2t + ((j + k + color) & 1); the cells of one colour are independent,
+// so the order does not change the result.
+template <int DIM, bool PER, class G = CtaG>
 __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const float* b,
-                         float* x, int color, bool zero, long long pin) {
-  const int n = (int)m.nc;
-  for (int c = threadIdx.x; c < n; c += blockDim.x) {
+                         float* x, int color, bool zero, long long pin, const G& g = G()) {
+  const int hx = (m.n[0] + 1) >> 1;
+  const int n = hx * m.n[1] * (DIM == 3 ? m.n[2] : 1);
+  for (int q = g.rank(); q < n; q += g.size()) {
+    const int row = q / hx;
     int id[3];
-    blk_ijk<DIM>(m, c, id);
-    if (((id[0] + id[1] + id[2]) & 1) != color) continue;
+    id[1] = DIM == 3 ? row % m.n[1] : row;
+    id[2] = DIM == 3 ? row / m.n[1] : 0;
+    id[0] = 2 * (q - row * hx) + ((id[1] + id[2] + color) & 1);
+    if (id[0] >= m.n[0]) continue;
+    const int c = id[0] + m.n[0] * row;
     if (c == pin) {
       x[c] = b[c];
       continue;
@@ -316,15 +343,15 @@ __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const
     }
     x[c] = acc * idg[c];
   }
-  __syncthreads();
+  g.sync();
 }
 
 // coarse rhs = sum over the children of the fine residual b - A x
-template <int DIM, bool PER>
+template <int DIM, bool PER, class G = CtaG>
 __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, const float* b,
-                             const float* x, float* cb, long long pin) {
+                             const float* x, float* cb, long long pin, const G& g = G()) {
   const int n = (int)cm.nc;
-  for (int C = threadIdx.x; C < n; C += blockDim.x) {
+  for (int C = g.rank(); C < n; C += g.size()) {
     int I[3];
     blk_ijk<DIM>(cm, C, I);
     float sum = 0.f;
@@ -358,7 +385,7 @@ __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, co
         }
     cb[C] = sum;
   }
-  __syncthreads();
+  g.sync();
 }
 
 // The levels of one V-cycle run by one CTA, by pointer (shared or global
@@ -485,6 +512,81 @@ __device__ void cta_stage_levels(const MgBlock& B, float* sm, CtaLevels* V, int 
       V->idg[first + l] = sm + B.oi[l];
       V->x[first + l] = sm + B.ox[l];
       V->b[first + l] = sm + B.ob[l];
+    }
+  }
+}
+
+// The small grid levels of a V-cycle and the in-CTA levels below them by
+// ONE thread-block cluster: the cluster smooths and restricts its global
+// levels (each a few thousand to tens of thousands of cells, where a grid
+// launch per half-sweep is mostly launch latency) with cluster barriers
+// between the passes, CTA 0 runs the sub-V-cycle of the staged levels in
+// its shared memory while the others wait at the barrier, and the cluster
+// prolongs and post-smooths back up.  Same smoother and transfers as the
+// grid and in-CTA levels.
+constexpr int kClusterCtas = 8;
+constexpr long long kClusterMaxCells = 32768;  // levels this small join the cluster
+struct ClusterVc {
+  int ng;      // global levels of the cluster, finest first
+  int nsweep;
+  long long pin;  // pinned cell of its finest level (-1: none)
+  Mesh m[kMgMaxLevels];
+  const float* kf[kMgMaxLevels];
+  const float* idg[kMgMaxLevels];
+  float* x[kMgMaxLevels];
+  float* b[kMgMaxLevels];
+  Mesh mtop;  // the first staged level, exchanged through global memory
+  float *btop, *xtop;
+  MgBlock blk;  // the staged levels
+};
+
+template <int DIM, bool PER>
+__global__ void __launch_bounds__(kBlkThreads)
+    k_mg_cluster_vcycle(const __grid_constant__ ClusterVc C, const DevScalars* ds) {
+  pdl_wait();
+  pdl_trigger();
+  if (ds->flag[FL_PCG_DONE]) return;  // the same in every CTA of the cluster
+  extern __shared__ float sm[];
+  __shared__ float red[32];
+  __shared__ CtaLevels V;
+  const ClusterG g;
+  const bool lead = cooperative_groups::this_cluster().block_rank() == 0;
+  if (lead) cta_stage_levels(C.blk, sm, &V);
+  const int ns = C.nsweep;
+  for (int l = 0; l < C.ng; ++l) {
+    const long long lp = l == 0 ? C.pin : -1;
+    for (int s = 0; s < ns; ++s) {
+      blk_half<DIM, PER>(C.m[l], C.kf[l], C.idg[l], C.b[l], C.x[l], 0, s == 0, lp, g);
+      blk_half<DIM, PER>(C.m[l], C.kf[l], C.idg[l], C.b[l], C.x[l], 1, false, lp, g);
+    }
+    const bool last = l + 1 == C.ng;
+    blk_restrict<DIM, PER>(C.m[l], last ? C.mtop : C.m[l + 1], C.kf[l], C.b[l], C.x[l],
+                           last ? C.btop : C.b[l + 1], lp, g);
+  }
+  if (lead) {
+    const int n = (int)C.mtop.nc;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) sm[C.blk.ob[0] + q] = C.btop[q];
+    __syncthreads();
+    cta_vcycle<DIM, PER>(V, red);
+    for (int q = threadIdx.x; q < n; q += blockDim.x) C.xtop[q] = sm[C.blk.ox[0] + q];
+  }
+  g.sync();
+  for (int l = C.ng - 1; l >= 0; --l) {
+    const long long lp = l == 0 ? C.pin : -1;
+    const bool last = l + 1 == C.ng;
+    const Mesh& m = C.m[l];
+    const Mesh& cm = last ? C.mtop : C.m[l + 1];
+    const float* cx = last ? C.xtop : C.x[l + 1];
+    float* x = C.x[l];
+    for (int c = g.rank(); c < (int)m.nc; c += g.size()) {
+      int id[3];
+      blk_ijk<DIM>(m, c, id);
+      x[c] += cx[(int)cell_id(cm, id[0] >> 1, id[1] >> 1, id[2] >> 1)];
+    }
+    g.sync();
+    for (int s = 0; s < ns; ++s) {
+      blk_half<DIM, PER>(m, C.kf[l], C.idg[l], C.b[l], x, 1, false, lp, g);
+      blk_half<DIM, PER>(m, C.kf[l], C.idg[l], C.b[l], x, 0, false, lp, g);
     }
   }
 }
@@ -1301,9 +1403,17 @@ cudaError_t mg_prepare(MgWork& mg) {
                           : cudaFuncSetAttribute(k_cta_pressure<2>, attr, mg.smem_bytes);
       if (e != cudaSuccess) return e;
     }
-    if (mg.lev[0].m.dim == 3)
+    cudaError_t e;
+    if (mg.lev[0].m.dim == 3) {
+      e = per ? cudaFuncSetAttribute(k_mg_cluster_vcycle<3, true>, attr, mg.smem_bytes)
+              : cudaFuncSetAttribute(k_mg_cluster_vcycle<3, false>, attr, mg.smem_bytes);
+      if (e != cudaSuccess) return e;
       return per ? cudaFuncSetAttribute(k_mg_block_vcycle<3, true>, attr, mg.smem_bytes)
                  : cudaFuncSetAttribute(k_mg_block_vcycle<3, false>, attr, mg.smem_bytes);
+    }
+    e = per ? cudaFuncSetAttribute(k_mg_cluster_vcycle<2, true>, attr, mg.smem_bytes)
+            : cudaFuncSetAttribute(k_mg_cluster_vcycle<2, false>, attr, mg.smem_bytes);
+    if (e != cudaSuccess) return e;
     return per ? cudaFuncSetAttribute(k_mg_block_vcycle<2, true>, attr, mg.smem_bytes)
                : cudaFuncSetAttribute(k_mg_block_vcycle<2, false>, attr, mg.smem_bytes);
   }
@@ -1330,6 +1440,16 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
   const int ns = mg.nsweep;
   const int top = mg.top < mg.nlev ? mg.top : mg.nlev - 1;
   const bool fast0 = mg.fast0 && top >= 1 && ns >= 1;
+  // the first level run by the cluster kernel (small grid levels above the
+  // in-CTA levels), or none
+  int ctop = -1;
+  if (mg.top < mg.nlev)
+    for (int l = fast0 ? 1 : 0; l < mg.top; ++l)
+      if (mg.lev[l].m.nc <= kClusterMaxCells) {
+        ctop = l;
+        break;
+      }
+  const int gtop = ctop >= 0 ? ctop : top;  // grid levels: [0, gtop)
   const Mesh& m0 = mg.lev[0].m;
   const Fast0 f0{m0.n[0], m0.n[1], m0.n[2], mg.k16[0], mg.k16[1], mg.k16[2]};
   if (fast0) {
@@ -1350,11 +1470,11 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
     }
     MgLevel& c = mg.lev[1];
     Launch L = cell_launch(c.m);
-    const float* cidg = 1 < top ? c.idg : nullptr;
+    const float* cidg = 1 < gtop ? c.idg : nullptr;
     PDL(k_mg0_restrict, L.grid, L.block, 0, st, f0, c.m, mg.b0, mg.x0, c.b, c.x, cidg, ds, L.kch);
     count_launches(1);
   }
-  for (int l = fast0 ? 1 : 0; l < top; ++l) {
+  for (int l = fast0 ? 1 : 0; l < gtop; ++l) {
     MgLevel& f = mg.lev[l];
     long long lp = l == 0 ? pin : -1;
     Launch H = half_launch(f.m);
@@ -1367,7 +1487,7 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
     }
     MgLevel& c = mg.lev[l + 1];
     Launch L = cell_launch(c.m);
-    const float* cidg = l + 1 < top && ns > 0 ? c.idg : nullptr;
+    const float* cidg = l + 1 < gtop && ns > 0 ? c.idg : nullptr;
     MG_LAUNCH_P(k_mg_restrict, L, per, f.m, c.m, f.kf, f.dg, f.b, f.x, c.b, c.x, cidg, lp, ds);
   }
   if (mg.top < mg.nlev) {
@@ -1391,7 +1511,31 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
       B.ok[q] = off; off += f4;
     }
     MgLevel& t = mg.lev[mg.top];
-    if (dim == 3) {
+    if (ctop >= 0) {
+      ClusterVc C;
+      C.ng = mg.top - ctop;
+      C.nsweep = ns;
+      C.pin = ctop == 0 ? pin : -1;
+      for (int q = 0; q < C.ng; ++q) {
+        const MgLevel& lv = mg.lev[ctop + q];
+        C.m[q] = lv.m;
+        C.kf[q] = lv.kf;
+        C.idg[q] = lv.idg;
+        C.x[q] = lv.x;
+        C.b[q] = lv.b;
+      }
+      C.mtop = t.m;
+      C.btop = t.b;
+      C.xtop = t.x;
+      C.blk = B;
+      if (dim == 3) {
+        if (per) PDL_CLUSTER(k_mg_cluster_vcycle<3, true>, kClusterCtas, kBlkThreads, mg.smem_bytes, st, C, ds);
+        else PDL_CLUSTER(k_mg_cluster_vcycle<3, false>, kClusterCtas, kBlkThreads, mg.smem_bytes, st, C, ds);
+      } else {
+        if (per) PDL_CLUSTER(k_mg_cluster_vcycle<2, true>, kClusterCtas, kBlkThreads, mg.smem_bytes, st, C, ds);
+        else PDL_CLUSTER(k_mg_cluster_vcycle<2, false>, kClusterCtas, kBlkThreads, mg.smem_bytes, st, C, ds);
+      }
+    } else if (dim == 3) {
       if (per) PDL(k_mg_block_vcycle<3, true>, 1, kBlkThreads, mg.smem_bytes, st, B, t.b, t.x, ds);
       else PDL(k_mg_block_vcycle<3, false>, 1, kBlkThreads, mg.smem_bytes, st, B, t.b, t.x, ds);
     } else {
@@ -1415,7 +1559,7 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
       mg_smooth(dim, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, 0, lp, nullptr, 0, 0, ds, st);
     }
   }
-  for (int l = top - 1; l >= (fast0 ? 1 : 0); --l) {
+  for (int l = gtop - 1; l >= (fast0 ? 1 : 0); --l) {
     MgLevel& f = mg.lev[l];
     MgLevel& c = mg.lev[l + 1];
     long long lp = l == 0 ? pin : -1;
