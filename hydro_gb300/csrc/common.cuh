@@ -143,27 +143,7 @@ inline cudaError_t pdl(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cuda
 }
 // pdl() whose error, like a <<<>>> launch's, is left to cudaGetLastError
 #define PDL(...) ((void)pdl(__VA_ARGS__))
-// The same for one thread-block cluster of `ctas` CTAs (the whole grid).
-template <class... P, class... A>
-inline cudaError_t pdl_cluster(void (*k)(P...), int ctas, int threads, size_t smem,
-                               cudaStream_t st, A&&... a) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(ctas);
-  cfg.blockDim = dim3(threads);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute at[2];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  at[1].id = cudaLaunchAttributeClusterDimension;
-  at[1].val.clusterDim.x = ctas;
-  at[1].val.clusterDim.y = 1;
-  at[1].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 2;
-  return cudaLaunchKernelEx(&cfg, k, std::forward<A>(a)...);
-}
-#define PDL_CLUSTER(...) ((void)pdl_cluster(__VA_ARGS__))
+
 
 // Launch geometry: blocks of 32x8 threads over (i, j); each block marches
 // KCH planes in k so that the grid stays a few waves deep on 152 SMs.

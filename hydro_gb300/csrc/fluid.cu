@@ -562,33 +562,47 @@ __global__ void __launch_bounds__(1024) k_cta_mom_jacobi32(Mesh m, float omega, 
     const FP<3>& dout = (k & 1) ? d1 : d0;
     const bool first = k == 0;
     float dmax = 0.f;
-    for (int q = tid; q < n; q += nt) {
-      Cell X;
-      X.c = q;
-      X.i[0] = q % m.n[0];
-      const int r = q / m.n[0];
-      X.i[1] = DIM == 3 ? r % m.n[1] : r;
-      X.i[2] = DIM == 3 ? r / m.n[1] : 0;
-      float iaP = c.a[0][X.c];
-      float a[2 * DIM];
+    // two cells per thread per pass, every load before the stores (the
+    // sweep reads din and writes dout)
+    for (int q0 = tid; q0 < n; q0 += 2 * nt) {
+      float out[2][DIM];
 #pragma unroll
-      for (int e = 0; e < 2 * DIM; ++e) a[e] = c.a[1 + e][X.c];
+      for (int u = 0; u < 2; ++u) {
+        Cell X;
+        X.c = q0 + u * nt;
+        if (X.c >= n) continue;
+        X.i[0] = (int)(X.c % m.n[0]);
+        const int r = (int)(X.c / m.n[0]);
+        X.i[1] = DIM == 3 ? r % m.n[1] : r;
+        X.i[2] = DIM == 3 ? r / m.n[1] : 0;
+        float iaP = c.a[0][X.c];
+        float a[2 * DIM];
 #pragma unroll
-      for (int v = 0; v < DIM; ++v) {
-        float sum = 0.f, cur = 0.f;
-        if (!first) {
-          cur = din.a[v][X.c];
+        for (int e = 0; e < 2 * DIM; ++e) a[e] = c.a[1 + e][X.c];
 #pragma unroll
-          for (int d = 0; d < DIM; ++d) {
-            long long s = cell_stride(m, d);
-            if (HAS_LO(d)) sum = fmaf(a[2 * d], din.a[v][NB_LO(d, s)], sum);
-            if (HAS_HI(d)) sum = fmaf(a[2 * d + 1], din.a[v][NB_HI(d, s)], sum);
+        for (int v = 0; v < DIM; ++v) {
+          float sum = 0.f, cur = 0.f;
+          if (!first) {
+            cur = din.a[v][X.c];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+              long long s = cell_stride(m, d);
+              if (HAS_LO(d)) sum = fmaf(a[2 * d], din.a[v][NB_LO(d, s)], sum);
+              if (HAS_HI(d)) sum = fmaf(a[2 * d + 1], din.a[v][NB_HI(d, s)], sum);
+            }
           }
+          float value = -(c.a[7 + v][X.c] + sum) * iaP;
+          float corr = value - cur;
+          dmax = fmaxf(dmax, fabsf(corr));
+          out[u][v] = fmaf(corr, omega, cur);
         }
-        float value = -(c.a[7 + v][X.c] + sum) * iaP;
-        float corr = value - cur;
-        dmax = fmaxf(dmax, fabsf(corr));
-        dout.a[v][X.c] = fmaf(corr, omega, cur);
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int q = q0 + u * nt;
+        if (q >= n) continue;
+#pragma unroll
+        for (int v = 0; v < DIM; ++v) dout.a[v][q] = out[u][v];
       }
     }
     dmax = warp_max(dmax);

