@@ -735,9 +735,10 @@ def main():
     ap.add_argument("--guess-iterations", type=int, default=1,
                     help="SIMPLE iterations per step whose pressure solve starts from the "
                          "network's guess (learned_mixed_mg)")
-    ap.add_argument("--form", default="mixed_mg",
+    ap.add_argument("--form", default="learned_mixed_mg",
                     choices=["learned_mixed_mg", "mixed_mg", "fp64", "fp64_mg"],
-                    help="headline form: mixed precision + multigrid CG, or plain FP64")
+                    help="headline form: the learned guess + mixed precision + multigrid CG "
+                         "(the metric's form), without the guess, or FP64")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 measurement reported beside the headline")
     ap.add_argument("--n", "--grid", dest="n", type=int, default=192,

@@ -685,7 +685,8 @@ int solve_pressure_graph(hydro_ctx* x, int singular, int mixed, bool apply_pin_g
         return HYDRO_OK;
       });
       if (r) return r;
-      CK(f32_accumulate(m, x->pc, w, x->st));
+      if (mgcg) CK(mgcg_accumulate(m, x->pc, w, x->mg, x->st));
+      else CK(f32_accumulate(m, x->pc, w, x->st));
       CK(ir_residual(m, x->kf, x->prhs, x->pc, singular, w, x->st));
       CK(launch_ctl_refine(w.ds, d.pressure_tolerance, inner_min, d.pressure_iters_limit, hr, 1,
                            x->st));
@@ -820,7 +821,8 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
                         1 + queued - (x->hds->flag[FL_PCG_DONE] && it > 0 ? it : it + 1));
       }
       total += x->hds->flag[FL_PCG_ITERS];
-      CK(f32_accumulate(m, x->pc, w, x->st));
+      if (mgcg) CK(mgcg_accumulate(m, x->pc, w, x->mg, x->st));
+      else CK(f32_accumulate(m, x->pc, w, x->st));
     }
     x->p_iters += total;
     if (!conv) x->p_unconv++;
@@ -1062,8 +1064,6 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
       mg.k16[0] = a.take<unsigned short>((n0 + 1) * n1 * n2);
       mg.k16[1] = a.take<unsigned short>(n0 * (n1 + 1) * n2);
       mg.k16[2] = a.take<unsigned short>(n0 * n1 * (n2 + 1));
-      mg.b0 = a.take<float>(nc);
-      mg.x0 = a.take<float>(nc);
       mg.idg0 = a.take<float>(nc);
     } else {
       mg.k16[0] = mg.k16[1] = mg.k16[2] = nullptr;

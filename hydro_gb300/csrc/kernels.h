@@ -369,7 +369,7 @@ struct MgWork {
   // null: not allocated (the mesh does not allow it); fast0: in use for
   // the current solve (set by mg_setup).
   unsigned short* k16[3];
-  float *b0, *x0, *idg0;
+  float* idg0;
   bool fast0;
   // inverse of the coarsest level's operator (rank-one completed for its
   // constant null space), dense, when that level has <= kMgCoarseTarget
@@ -417,6 +417,9 @@ cudaError_t mgcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, MgW
                       cudaStream_t st);
 cudaError_t mgcg_iterate(const Mesh& m, int chunk, PcgWork& w, MgWork& mg, cudaStream_t st);
 cudaError_t f32_accumulate(const Mesh& m, double* x, PcgWork& w, cudaStream_t st);
+// x += the inner multigrid CG's result (in the finest level's colour-blocked
+// order when that level is in use, mg.fast0).
+cudaError_t mgcg_accumulate(const Mesh& m, double* x, PcgWork& w, MgWork& mg, cudaStream_t st);
 cudaError_t scale_vector(long long n, double* a, double s, cudaStream_t st);
 // Right-hand side of a pinned cell (fluid.hpp:996-1014): f[pin] = value and
 // the pinned value moved into the neighbours' rows.

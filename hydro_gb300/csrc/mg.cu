@@ -809,36 +809,33 @@ __global__ void k_mg0_diag(Fast0 f, const DevScalars* ds, float* idg0) {
   }
 }
 
-// Start of a V-cycle: the CG residual r (cell order) into the blocked
-// right-hand side, and the first half-sweep (red, from x = 0: x = b / diag).
-__global__ void k_mg0_split(Fast0 f, const float* r, const float* idg0, float* b0, float* x0,
-                            const DevScalars* ds) {
+// Start of a V-cycle on the colour-blocked finest level, whose right-hand
+// side is the inner CG's residual itself (kept colour-blocked): the first
+// half-sweep, red from x = 0, is x = b / diag on the red half.
+__global__ void __launch_bounds__(NT) k_mg0_red0(long long half, const float* __restrict__ b0,
+                                                 const float* __restrict__ idg0,
+                                                 float* __restrict__ x0, const DevScalars* ds) {
   pdl_wait();
   pdl_trigger();
   if (ds->flag[FL_PCG_DONE]) return;
-  const int h0 = f.n0 / 2;
-  const long long half = (long long)h0 * f.n1 * f.n2;
-  const float2* r2 = reinterpret_cast<const float2*>(r);
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < half;
-       p += (long long)gridDim.x * blockDim.x) {
-    const long long row = p / h0;
-    const int q = (int)((row % f.n1 + row / f.n1) & 1);  // colour of cell 2p
-    const float2 v = r2[p];
-    b0[q * half + p] = v.x;
-    b0[(1 - q) * half + p] = v.y;
-    x0[p] = (q == 0 ? v.x : v.y) * idg0[p];
+  const long long n4 = half >> 2;
+  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = g; i < n4; i += stride) {
+    const float4 b = reinterpret_cast<const float4*>(b0)[i];
+    const float4 d = reinterpret_cast<const float4*>(idg0)[i];
+    reinterpret_cast<float4*>(x0)[i] = make_float4(b.x * d.x, b.y * d.y, b.z * d.z, b.w * d.w);
   }
+  for (long long i = 4 * n4 + g; i < half; i += stride) x0[i] = b0[i] * idg0[i];
 }
 
 // Red-black half-sweep of one colour on the blocked arrays.  PROLONG: the
 // neighbours are read as x + cx(parent) (the injected coarse correction,
-// first post-smoothing half-sweep).  ZOUT: the new values also go to z in
-// cell order (the last half-sweep of each colour: the preconditioned
-// residual the CG reads).
-template <bool PROLONG, bool ZOUT>
+// first post-smoothing half-sweep).
+template <bool PROLONG>
 __global__ void __launch_bounds__(NT) k_mg0_smooth(Fast0 f, const float* idg0, const float* b0,
                                                    float* x0, int color, const float* cx,
-                                                   float* z, const DevScalars* ds, int kch) {
+                                                   const DevScalars* ds, int kch) {
   pdl_wait();
   pdl_trigger();
   if (ds->flag[FL_PCG_DONE]) return;
@@ -899,7 +896,6 @@ __global__ void __launch_bounds__(NT) k_mg0_smooth(Fast0 f, const float* idg0, c
     for (int q = 0; q < 6; ++q) acc = fmaf(ks[q], xs[q], acc);
     const float xn = fmaf(scale, acc, bb) * ig;
     x0[own + p] = xn;
-    if (ZOUT) z[i + f.n0 * (j + f.n1 * k)] = xn;
   }
 }
 
@@ -948,6 +944,129 @@ __global__ void __launch_bounds__(NT, 4) k_mg0_restrict(Fast0 f, Mesh cm, const 
   cb[X.c] = sum;
   cx[X.c] = cidg && ((X.i[0] + X.i[1] + X.i[2]) & 1) == 0 ? sum * cidg[X.c] : 0.f;
   CELL_LOOP_END
+}
+
+// ---- inner CG in the colour-blocked order of the finest level (fast0) --
+// With the colour-blocked finest level the inner CG keeps r, z, p, Ap and
+// x in that order (cell c of colour q at q * nc/2 + c/2), so the V-cycle
+// reads r and writes z in place: no reordering pass at either end of it.
+// The FP64 side stays in cell order; these kernels convert at the borders.
+
+// r = FP32 of the FP64 residual (cell order -> blocked), x = 0; ||r||^2.
+__global__ void __launch_bounds__(NT) k_mgcg_init_blk(Fast0 f, const double* __restrict__ r64,
+                                                      float* __restrict__ r,
+                                                      float* __restrict__ x, double tol,
+                                                      int limit, int dev_params,
+                                                      double* partials, DevScalars* ds) {
+  pdl_wait();
+  pdl_trigger();
+  const int h0 = f.n0 / 2;
+  const long long half = (long long)h0 * f.n1 * f.n2;
+  const double2* r2 = reinterpret_cast<const double2*>(r64);
+  const long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
+  double s = 0.;
+  for (long long p = blockIdx.x * (long long)NT + tid; p < half; p += (long long)gridDim.x * NT) {
+    const long long row = p / h0;
+    const int q = (int)((row % f.n1 + row / f.n1) & 1);  // colour of cell 2p
+    const double2 v = r2[p];                              // cells 2p, 2p + 1
+    r[q * half + p] = d2f(v.x);
+    r[(1 - q) * half + p] = d2f(v.y);
+    x[p] = 0.f;
+    x[half + p] = 0.f;
+    s += v.x * v.x;
+    s += v.y * v.y;
+  }
+  double v[1] = {s};
+  __shared__ double o[1];
+  if (grid_reduce<RED_SUM, 1>(v, partials, &ds->ticket[TK_F32_INIT], o)) {
+    if (tid == 0) {
+      if (dev_params) tol = ds->red[RS_INNER_TOL];
+      else ds->flag[FL_PCG_LIMIT] = limit;
+      ds->red[RS_PCG_FF] = o[0];
+      ds->red[RS_PCG_RR] = o[0];
+      ds->red[RS_PCG_TOL2] = tol * tol * o[0];
+      ds->red[RS_PCG_RRREF] = o[0];
+      ds->flag[FL_PCG_ITERS] = 0;
+      ds->flag[FL_PCG_REFIT] = 0;
+      ds->flag[FL_PCG_DONE] = (o[0] == 0. || ds->flag[FL_PCG_LIMIT] <= 0) ? 1 : 0;
+    }
+  }
+}
+
+// p = z + beta p_old (z on the first iteration), Ap = A32 p with the FP32
+// operator (cell-order couplings and diagonal), <p, Ap>: one thread per
+// cell pair (2h, 2h + 1) of a row, both colours.
+__global__ void __launch_bounds__(NT) k_cg32_dir_spmv_blk(Fast0 f, const float* __restrict__ kf,
+                                                          const float* __restrict__ dg,
+                                                          const float* __restrict__ z,
+                                                          const float* __restrict__ pold,
+                                                          float* __restrict__ pnew,
+                                                          float* __restrict__ Ap,
+                                                          long long fofs1, long long fofs2,
+                                                          double* partials, DevScalars* ds) {
+  pdl_wait();
+  pdl_trigger();
+  if (ds->flag[FL_PCG_DONE]) return;
+  const bool first = ds->flag[FL_PCG_ITERS] == 0;
+  const float beta = first ? 0.f : (float)ds->red[RS_PCG_BETA];
+  const int n0 = f.n0, n1 = f.n1, n2 = f.n2, h0 = n0 / 2;
+  const long long half = (long long)h0 * n1 * n2;
+  const long long hz = (long long)h0 * n1;
+  auto P = [&](long long b) { return first ? z[b] : fmaf(beta, pold[b], z[b]); };
+  DFAcc2 acc;
+  const long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
+  for (long long p = blockIdx.x * (long long)NT + tid; p < half; p += (long long)gridDim.x * NT) {
+    const long long row = p / h0;
+    const int ih = (int)(p - row * h0);
+    const int j = (int)(row % n1), k = (int)(row / n1);
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int i = 2 * ih + e;
+      const int q = (i + j + k) & 1;
+      const long long own = q * half + p, oth = (1 - q) * half + p;
+      const long long c = 2 * p + e;
+      const long long fx = i + (long long)(n0 + 1) * row;
+      const long long fy = fofs1 + i + (long long)n0 * (j + (long long)(n1 + 1) * k);
+      const long long fz = fofs2 + c;
+      const float pc = P(own);
+      float a = dg[c] * pc;
+      if (i > 0) a = fmaf(-kf[fx], P(oth - 1 + e), a);
+      if (i < n0 - 1) a = fmaf(-kf[fx + 1], P(oth + e), a);
+      if (j > 0) a = fmaf(-kf[fy], P(oth - h0), a);
+      if (j < n1 - 1) a = fmaf(-kf[fy + n0], P(oth + h0), a);
+      if (k > 0) a = fmaf(-kf[fz], P(oth - hz), a);
+      if (k < n2 - 1) a = fmaf(-kf[fz + (long long)n0 * n1], P(oth + hz), a);
+      pnew[own] = pc;
+      Ap[own] = a;
+      acc.add_prod(pc, a);
+    }
+  }
+  double v[1] = {acc.value()};
+  __shared__ double o[1];
+  if (grid_reduce<RED_SUM, 1>(v, partials, &ds->ticket[TK_F32_A], o)) {
+    if (tid == 0) {
+      ds->red[RS_PCG_PAP] = o[0];
+      ds->red[RS_PCG_ALPHA] = ds->red[RS_PCG_RZ] / o[0];
+    }
+  }
+}
+
+// x64 (cell order) += FP64 of x32 (blocked).
+__global__ void k_accumulate_blk(Fast0 f, double* __restrict__ x, const float* __restrict__ e) {
+  pdl_wait();
+  pdl_trigger();
+  const int h0 = f.n0 / 2;
+  const long long half = (long long)h0 * f.n1 * f.n2;
+  double2* x2 = reinterpret_cast<double2*>(x);
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < half;
+       p += (long long)gridDim.x * blockDim.x) {
+    const long long row = p / h0;
+    const int q = (int)((row % f.n1 + row / f.n1) & 1);
+    double2 v = x2[p];
+    v.x += f2d(e[q * half + p]);
+    v.y += f2d(e[(1 - q) * half + p]);
+    x2[p] = v;
+  }
 }
 
 // ----------------------------------------- one CTA per pressure solve --
@@ -1257,7 +1376,7 @@ int flat_blocks_mg(long long n) {
 Launch fast0_launch(const Mesh& m) {
   Mesh h = m;
   h.n[0] = m.n[0] / 2;
-  return cell_launch_waves(h, resident_ctas((const void*)k_mg0_smooth<false, false>));
+  return cell_launch_waves(h, resident_ctas((const void*)k_mg0_smooth<false>));
 }
 
 Launch half_launch(const Mesh& m) {
@@ -1435,25 +1554,28 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
   const Mesh& m0 = mg.lev[0].m;
   const Fast0 f0{m0.n[0], m0.n[1], m0.n[2], mg.k16[0], mg.k16[1], mg.k16[2]};
   if (fast0) {
-    // level 0 on the colour-blocked arrays: split (+ red from zero), then
-    // black, (red, black)^(ns-1), restriction of the red residuals
+    // level 0 on the colour-blocked arrays, whose right-hand side and
+    // iterate are the inner CG's r and z themselves (kept colour-blocked):
+    // red from zero, then black, (red, black)^(ns-1), restriction of the
+    // red residuals
     const Launch H = fast0_launch(m0);
-    PDL(k_mg0_split, flat_blocks_mg(m0.nc / 2), NT, 0, st, f0, r, mg.idg0, mg.b0, mg.x0, ds);
+    float* x0 = z;
+    const float* b0 = r;
+    PDL(k_mg0_red0, flat_blocks_mg(m0.nc / 8), NT, 0, st, m0.nc / 2, b0, mg.idg0, x0, ds);
     count_launches(1);
     for (int s = 0; s < ns; ++s) {
       if (s > 0) {
-        PDL(k_mg0_smooth<false, false>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 0,
-                                                              nullptr, nullptr, ds, H.kch);
+        PDL(k_mg0_smooth<false>, H.grid, H.block, 0, st, f0, mg.idg0, b0, x0, 0, nullptr, ds,
+            H.kch);
         count_launches(1);
       }
-      PDL(k_mg0_smooth<false, false>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 1,
-                                                            nullptr, nullptr, ds, H.kch);
+      PDL(k_mg0_smooth<false>, H.grid, H.block, 0, st, f0, mg.idg0, b0, x0, 1, nullptr, ds, H.kch);
       count_launches(1);
     }
     MgLevel& c = mg.lev[1];
     Launch L = cell_launch(c.m);
     const float* cidg = 1 < top ? c.idg : nullptr;
-    PDL(k_mg0_restrict, L.grid, L.block, 0, st, f0, c.m, mg.b0, mg.x0, c.b, c.x, cidg, ds, L.kch);
+    PDL(k_mg0_restrict, L.grid, L.block, 0, st, f0, c.m, b0, x0, c.b, c.x, cidg, ds, L.kch);
     count_launches(1);
   }
   for (int l = fast0 ? 1 : 0; l < top; ++l) {
@@ -1530,30 +1652,17 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
     }
   }
   if (fast0) {
-    // (black + injected correction, red), (black, red)^(ns-1); the last
-    // half-sweep of each colour writes z in cell order
+    // (black + injected correction, red), (black, red)^(ns-1): z is the
+    // colour-blocked iterate itself
     const Launch H = fast0_launch(m0);
     const float* cx = mg.lev[1].x;
     for (int s = 0; s < ns; ++s) {
-      const bool last = s == ns - 1;
-      if (s == 0 && last)
-        PDL(k_mg0_smooth<true, true>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 1, cx,
-                                                            z, ds, H.kch);
-      else if (s == 0)
-        PDL(k_mg0_smooth<true, false>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 1, cx,
-                                                             nullptr, ds, H.kch);
-      else if (last)
-        PDL(k_mg0_smooth<false, true>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 1,
-                                                             nullptr, z, ds, H.kch);
+      if (s == 0)
+        PDL(k_mg0_smooth<true>, H.grid, H.block, 0, st, f0, mg.idg0, r, z, 1, cx, ds, H.kch);
       else
-        PDL(k_mg0_smooth<false, false>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 1,
-                                                              nullptr, nullptr, ds, H.kch);
-      if (last)
-        PDL(k_mg0_smooth<false, true>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 0,
-                                                             nullptr, z, ds, H.kch);
-      else
-        PDL(k_mg0_smooth<false, false>, H.grid, H.block, 0, st, f0, mg.idg0, mg.b0, mg.x0, 0,
-                                                              nullptr, nullptr, ds, H.kch);
+        PDL(k_mg0_smooth<false>, H.grid, H.block, 0, st, f0, mg.idg0, r, z, 1, nullptr, ds,
+            H.kch);
+      PDL(k_mg0_smooth<false>, H.grid, H.block, 0, st, f0, mg.idg0, r, z, 0, nullptr, ds, H.kch);
       count_launches(2);
     }
   }
@@ -1680,8 +1789,14 @@ cudaError_t mgcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, MgW
       !aligned16(w.p32) || !aligned16(w.p32b) || !aligned16(w.Ap32))
     return cudaErrorInvalidValue;
   w.p32_parity = 0;
-  PDL(k_mgcg_init, fb, dim3(BX, BY), 0, st, m.nc, w.r, w.r32, w.x32, tol, w.limit, dev_params,
-      w.partials, w.ds);
+  if (mg.fast0) {
+    const Fast0 f{m.n[0], m.n[1], m.n[2], mg.k16[0], mg.k16[1], mg.k16[2]};
+    PDL(k_mgcg_init_blk, flat_blocks_mg(m.nc / 2), dim3(BX, BY), 0, st, f, w.r, w.r32, w.x32,
+        tol, w.limit, dev_params, w.partials, w.ds);
+  } else {
+    PDL(k_mgcg_init, fb, dim3(BX, BY), 0, st, m.nc, w.r, w.r32, w.x32, tol, w.limit,
+        dev_params, w.partials, w.ds);
+  }
   count_launches(1);
   if (w.prof) w.prof->begin(HYDRO_PROF_MG_VCYCLE, st);
   cudaError_t e = mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st);
@@ -1698,8 +1813,17 @@ cudaError_t mgcg_iterate(const Mesh& m, int chunk, PcgWork& w, MgWork& mg, cudaS
     float* pold = (w.p32_parity & 1) ? w.p32b : w.p32;
     float* pnew = (w.p32_parity & 1) ? w.p32 : w.p32b;
     if (w.prof) w.prof->begin(HYDRO_PROF_CG_SPMV, st);
-    cudaError_t e = cg32_dir_spmv(m, w.kf32, w.dg32, w.z32, pold, pnew, w.Ap32, w.pin,
-                                  w.partials, w.ds, st);
+    cudaError_t e;
+    if (mg.fast0) {
+      const Fast0 f{m.n[0], m.n[1], m.n[2], mg.k16[0], mg.k16[1], mg.k16[2]};
+      PDL(k_cg32_dir_spmv_blk, flat_blocks_mg(m.nc / 2), dim3(BX, BY), 0, st, f, w.kf32, w.dg32,
+          w.z32, pold, pnew, w.Ap32, m.fofs[1], m.fofs[2], w.partials, w.ds);
+      count_launches(1);
+      e = cudaGetLastError();
+    } else {
+      e = cg32_dir_spmv(m, w.kf32, w.dg32, w.z32, pold, pnew, w.Ap32, w.pin, w.partials, w.ds,
+                        st);
+    }
     if (w.prof) w.prof->end(HYDRO_PROF_CG_SPMV, st);
     if (e != cudaSuccess) return e;
     if (w.prof) w.prof->begin(HYDRO_PROF_CG_UPDATE, st);
@@ -1714,6 +1838,14 @@ cudaError_t mgcg_iterate(const Mesh& m, int chunk, PcgWork& w, MgWork& mg, cudaS
     count_launches(2);
     w.p32_parity ^= 1;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t mgcg_accumulate(const Mesh& m, double* x, PcgWork& w, MgWork& mg, cudaStream_t st) {
+  if (!mg.fast0) return f32_accumulate(m, x, w, st);
+  const Fast0 f{m.n[0], m.n[1], m.n[2], mg.k16[0], mg.k16[1], mg.k16[2]};
+  PDL(k_accumulate_blk, flat_blocks_mg(m.nc / 2), NT, 0, st, f, x, w.x32);
+  count_launches(1);
   return cudaGetLastError();
 }
 
