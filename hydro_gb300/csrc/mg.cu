@@ -961,13 +961,13 @@ __global__ void __launch_bounds__(NT) k_mgcg_init_blk(Fast0 f, const double* __r
   pdl_wait();
   pdl_trigger();
   const int h0 = f.n0 / 2;
-  const long long half = (long long)h0 * f.n1 * f.n2;
+  const int half = h0 * f.n1 * f.n2;  // < 2^30
   const double2* r2 = reinterpret_cast<const double2*>(r64);
-  const long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
+  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
   double s = 0.;
-  for (long long p = blockIdx.x * (long long)NT + tid; p < half; p += (long long)gridDim.x * NT) {
-    const long long row = p / h0;
-    const int q = (int)((row % f.n1 + row / f.n1) & 1);  // colour of cell 2p
+  for (int p = blockIdx.x * NT + tid; p < half; p += gridDim.x * NT) {
+    const int row = p / h0;
+    const int q = (row % f.n1 + row / f.n1) & 1;  // colour of cell 2p
     const double2 v = r2[p];                              // cells 2p, 2p + 1
     r[q * half + p] = d2f(v.x);
     r[(1 - q) * half + p] = d2f(v.y);
@@ -994,57 +994,61 @@ __global__ void __launch_bounds__(NT) k_mgcg_init_blk(Fast0 f, const double* __r
 }
 
 // p = z + beta p_old (z on the first iteration), Ap = A32 p with the FP32
-// operator (cell-order couplings and diagonal), <p, Ap>: one thread per
-// cell pair (2h, 2h + 1) of a row, both colours.
+// operator (cell-order couplings and diagonal), <p, Ap>: thread (x, y) of
+// block (bx, by, bz) takes the cell pair (2h, 2h + 1), h = bx*BX + x, of
+// row (j, k), j = by*BY + y, for the kch planes k of its block (the
+// half-sweep's grid); 32-bit indices (the blocked level has < 2^30 cells).
 __global__ void __launch_bounds__(NT) k_cg32_dir_spmv_blk(Fast0 f, const float* __restrict__ kf,
                                                           const float* __restrict__ dg,
                                                           const float* __restrict__ z,
                                                           const float* __restrict__ pold,
                                                           float* __restrict__ pnew,
-                                                          float* __restrict__ Ap,
-                                                          long long fofs1, long long fofs2,
-                                                          double* partials, DevScalars* ds) {
+                                                          float* __restrict__ Ap, int fofs1,
+                                                          int fofs2, double* partials,
+                                                          DevScalars* ds, int kch) {
   pdl_wait();
   pdl_trigger();
   if (ds->flag[FL_PCG_DONE]) return;
   const bool first = ds->flag[FL_PCG_ITERS] == 0;
   const float beta = first ? 0.f : (float)ds->red[RS_PCG_BETA];
   const int n0 = f.n0, n1 = f.n1, n2 = f.n2, h0 = n0 / 2;
-  const long long half = (long long)h0 * n1 * n2;
-  const long long hz = (long long)h0 * n1;
-  auto P = [&](long long b) { return first ? z[b] : fmaf(beta, pold[b], z[b]); };
+  const int half = h0 * n1 * n2, hz = h0 * n1;
+  auto P = [&](int b) { return first ? z[b] : fmaf(beta, pold[b], z[b]); };
   DFAcc2 acc;
-  const long long tid = threadIdx.x + blockDim.x * (long long)threadIdx.y;
-  for (long long p = blockIdx.x * (long long)NT + tid; p < half; p += (long long)gridDim.x * NT) {
-    const long long row = p / h0;
-    const int ih = (int)(p - row * h0);
-    const int j = (int)(row % n1), k = (int)(row / n1);
+  const int ih = blockIdx.x * BX + threadIdx.x;
+  const int j = blockIdx.y * BY + threadIdx.y;
+  if (ih < h0 && j < n1) {
+    const int k0 = blockIdx.z * kch, k1 = min(k0 + kch, n2);
+    for (int k = k0; k < k1; ++k) {
+      const int row = j + n1 * k;
+      const int p = ih + h0 * row;
 #pragma unroll
-    for (int e = 0; e < 2; ++e) {
-      const int i = 2 * ih + e;
-      const int q = (i + j + k) & 1;
-      const long long own = q * half + p, oth = (1 - q) * half + p;
-      const long long c = 2 * p + e;
-      const long long fx = i + (long long)(n0 + 1) * row;
-      const long long fy = fofs1 + i + (long long)n0 * (j + (long long)(n1 + 1) * k);
-      const long long fz = fofs2 + c;
-      const float pc = P(own);
-      float a = dg[c] * pc;
-      if (i > 0) a = fmaf(-kf[fx], P(oth - 1 + e), a);
-      if (i < n0 - 1) a = fmaf(-kf[fx + 1], P(oth + e), a);
-      if (j > 0) a = fmaf(-kf[fy], P(oth - h0), a);
-      if (j < n1 - 1) a = fmaf(-kf[fy + n0], P(oth + h0), a);
-      if (k > 0) a = fmaf(-kf[fz], P(oth - hz), a);
-      if (k < n2 - 1) a = fmaf(-kf[fz + (long long)n0 * n1], P(oth + hz), a);
-      pnew[own] = pc;
-      Ap[own] = a;
-      acc.add_prod(pc, a);
+      for (int e = 0; e < 2; ++e) {
+        const int i = 2 * ih + e;
+        const int q = (i + j + k) & 1;
+        const int own = q * half + p, oth = (1 - q) * half + p;
+        const int c = 2 * p + e;
+        const int fx = i + (n0 + 1) * row;
+        const int fy = fofs1 + i + n0 * (j + (n1 + 1) * k);
+        const int fz = fofs2 + c;
+        const float pc = P(own);
+        float a = dg[c] * pc;
+        if (i > 0) a = fmaf(-kf[fx], P(oth - 1 + e), a);
+        if (i < n0 - 1) a = fmaf(-kf[fx + 1], P(oth + e), a);
+        if (j > 0) a = fmaf(-kf[fy], P(oth - h0), a);
+        if (j < n1 - 1) a = fmaf(-kf[fy + n0], P(oth + h0), a);
+        if (k > 0) a = fmaf(-kf[fz], P(oth - hz), a);
+        if (k < n2 - 1) a = fmaf(-kf[fz + n0 * n1], P(oth + hz), a);
+        pnew[own] = pc;
+        Ap[own] = a;
+        acc.add_prod(pc, a);
+      }
     }
   }
   double v[1] = {acc.value()};
   __shared__ double o[1];
   if (grid_reduce<RED_SUM, 1>(v, partials, &ds->ticket[TK_F32_A], o)) {
-    if (tid == 0) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
       ds->red[RS_PCG_PAP] = o[0];
       ds->red[RS_PCG_ALPHA] = ds->red[RS_PCG_RZ] / o[0];
     }
@@ -1056,12 +1060,11 @@ __global__ void k_accumulate_blk(Fast0 f, double* __restrict__ x, const float* _
   pdl_wait();
   pdl_trigger();
   const int h0 = f.n0 / 2;
-  const long long half = (long long)h0 * f.n1 * f.n2;
+  const int half = h0 * f.n1 * f.n2;  // < 2^30
   double2* x2 = reinterpret_cast<double2*>(x);
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < half;
-       p += (long long)gridDim.x * blockDim.x) {
-    const long long row = p / h0;
-    const int q = (int)((row % f.n1 + row / f.n1) & 1);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < half; p += gridDim.x * blockDim.x) {
+    const int row = p / h0;
+    const int q = (row % f.n1 + row / f.n1) & 1;
     double2 v = x2[p];
     v.x += f2d(e[q * half + p]);
     v.y += f2d(e[(1 - q) * half + p]);
@@ -1816,8 +1819,9 @@ cudaError_t mgcg_iterate(const Mesh& m, int chunk, PcgWork& w, MgWork& mg, cudaS
     cudaError_t e;
     if (mg.fast0) {
       const Fast0 f{m.n[0], m.n[1], m.n[2], mg.k16[0], mg.k16[1], mg.k16[2]};
-      PDL(k_cg32_dir_spmv_blk, flat_blocks_mg(m.nc / 2), dim3(BX, BY), 0, st, f, w.kf32, w.dg32,
-          w.z32, pold, pnew, w.Ap32, m.fofs[1], m.fofs[2], w.partials, w.ds);
+      const Launch H = fast0_launch(m);
+      PDL(k_cg32_dir_spmv_blk, H.grid, H.block, 0, st, f, w.kf32, w.dg32, w.z32, pold, pnew,
+          w.Ap32, (int)m.fofs[1], (int)m.fofs[2], w.partials, w.ds, H.kch);
       count_launches(1);
       e = cudaGetLastError();
     } else {
