@@ -994,10 +994,10 @@ __global__ void __launch_bounds__(NT) k_mgcg_init_blk(Fast0 f, const double* __r
 }
 
 // p = z + beta p_old (z on the first iteration), Ap = A32 p with the FP32
-// operator (cell-order couplings and diagonal), <p, Ap>: thread (x, y) of
-// block (bx, by, bz) takes the cell pair (2h, 2h + 1), h = bx*BX + x, of
-// row (j, k), j = by*BY + y, for the kch planes k of its block (the
-// half-sweep's grid); 32-bit indices (the blocked level has < 2^30 cells).
+// operator (cell-order couplings and diagonal), <p, Ap>: one thread per
+// cell on the cell-order grid (thread x of a row is cell i = x, the pair
+// i/2 of colour-blocked index q * half + (i/2 + n0/2 * row)); 32-bit
+// indices (the blocked level has < 2^30 cells).
 __global__ void __launch_bounds__(NT) k_cg32_dir_spmv_blk(Fast0 f, const float* __restrict__ kf,
                                                           const float* __restrict__ dg,
                                                           const float* __restrict__ z,
@@ -1015,34 +1015,31 @@ __global__ void __launch_bounds__(NT) k_cg32_dir_spmv_blk(Fast0 f, const float* 
   const int half = h0 * n1 * n2, hz = h0 * n1;
   auto P = [&](int b) { return first ? z[b] : fmaf(beta, pold[b], z[b]); };
   DFAcc2 acc;
-  const int ih = blockIdx.x * BX + threadIdx.x;
+  const int i = blockIdx.x * BX + threadIdx.x;
   const int j = blockIdx.y * BY + threadIdx.y;
-  if (ih < h0 && j < n1) {
+  if (i < n0 && j < n1) {
+    const int ih = i >> 1, e = i & 1;
     const int k0 = blockIdx.z * kch, k1 = min(k0 + kch, n2);
     for (int k = k0; k < k1; ++k) {
       const int row = j + n1 * k;
       const int p = ih + h0 * row;
-#pragma unroll
-      for (int e = 0; e < 2; ++e) {
-        const int i = 2 * ih + e;
-        const int q = (i + j + k) & 1;
-        const int own = q * half + p, oth = (1 - q) * half + p;
-        const int c = 2 * p + e;
-        const int fx = i + (n0 + 1) * row;
-        const int fy = fofs1 + i + n0 * (j + (n1 + 1) * k);
-        const int fz = fofs2 + c;
-        const float pc = P(own);
-        float a = dg[c] * pc;
-        if (i > 0) a = fmaf(-kf[fx], P(oth - 1 + e), a);
-        if (i < n0 - 1) a = fmaf(-kf[fx + 1], P(oth + e), a);
-        if (j > 0) a = fmaf(-kf[fy], P(oth - h0), a);
-        if (j < n1 - 1) a = fmaf(-kf[fy + n0], P(oth + h0), a);
-        if (k > 0) a = fmaf(-kf[fz], P(oth - hz), a);
-        if (k < n2 - 1) a = fmaf(-kf[fz + n0 * n1], P(oth + hz), a);
-        pnew[own] = pc;
-        Ap[own] = a;
-        acc.add_prod(pc, a);
-      }
+      const int q = (i + j + k) & 1;
+      const int own = q * half + p, oth = (1 - q) * half + p;
+      const int c = i + n0 * row;
+      const int fx = i + (n0 + 1) * row;
+      const int fy = fofs1 + i + n0 * (j + (n1 + 1) * k);
+      const int fz = fofs2 + c;
+      const float pc = P(own);
+      float a = dg[c] * pc;
+      if (i > 0) a = fmaf(-kf[fx], P(oth - 1 + e), a);
+      if (i < n0 - 1) a = fmaf(-kf[fx + 1], P(oth + e), a);
+      if (j > 0) a = fmaf(-kf[fy], P(oth - h0), a);
+      if (j < n1 - 1) a = fmaf(-kf[fy + n0], P(oth + h0), a);
+      if (k > 0) a = fmaf(-kf[fz], P(oth - hz), a);
+      if (k < n2 - 1) a = fmaf(-kf[fz + n0 * n1], P(oth + hz), a);
+      pnew[own] = pc;
+      Ap[own] = a;
+      acc.add_prod(pc, a);
     }
   }
   double v[1] = {acc.value()};
@@ -1819,7 +1816,7 @@ cudaError_t mgcg_iterate(const Mesh& m, int chunk, PcgWork& w, MgWork& mg, cudaS
     cudaError_t e;
     if (mg.fast0) {
       const Fast0 f{m.n[0], m.n[1], m.n[2], mg.k16[0], mg.k16[1], mg.k16[2]};
-      const Launch H = fast0_launch(m);
+      const Launch H = cell_launch_waves(m, resident_ctas((const void*)k_cg32_dir_spmv_blk));
       PDL(k_cg32_dir_spmv_blk, H.grid, H.block, 0, st, f, w.kf32, w.dg32, w.z32, pold, pnew,
           w.Ap32, (int)m.fofs[1], (int)m.fofs[2], w.partials, w.ds, H.kch);
       count_launches(1);
