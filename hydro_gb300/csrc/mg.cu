@@ -904,10 +904,14 @@ __global__ void __launch_bounds__(NT) k_mg0_smooth(Fast0 f, const float* idg0, c
 // residuals zero up to rounding): r = b + 2^e sum_f k_f (x_nb - x_c).
 // With cidg the coarse level's first half-sweep (red, from zero) as well,
 // else the coarse iterate is cleared.
-__global__ void __launch_bounds__(NT, 4) k_mg0_restrict(Fast0 f, Mesh cm, const float* b0,
-                                                        const float* x0, float* cb, float* cx,
-                                                        const float* cidg, const DevScalars* ds,
-                                                        int kch) {
+// Two threads per coarse cell, one per child plane ck (lanes 2t and 2t+1
+// of a warp: 16 coarse cells per warp row): each sums the residuals of
+// its two red children and a lane shuffle adds the pair.  Launched on the
+// coarse grid with its x extent doubled (restrict0_launch).
+__global__ void __launch_bounds__(NT) k_mg0_restrict(Fast0 f, Mesh cm, const float* b0,
+                                                     const float* x0, float* cb, float* cx,
+                                                     const float* cidg, const DevScalars* ds,
+                                                     int kch) {
   pdl_wait();
   pdl_trigger();
   if (ds->flag[FL_PCG_DONE]) return;
@@ -915,16 +919,18 @@ __global__ void __launch_bounds__(NT, 4) k_mg0_restrict(Fast0 f, Mesh cm, const 
   const int half = h0 * f.n1 * f.n2;
   const int hz = h0 * f.n1;
   const float scale = (float)ds->red[RS_MG0_SCALE];
-  CELL_LOOP_BEGIN(cm, kch)
-  float sum = 0.f;
+  const int I = blockIdx.x * (BX / 2) + (threadIdx.x >> 1);
+  const int ck = threadIdx.x & 1;
+  const int J = blockIdx.y * BY + threadIdx.y;
+  const bool act = I < cm.n[0] && J < cm.n[1];
+  const int k0 = blockIdx.z * kch, k1 = min(k0 + kch, cm.n[2]);
+  for (int K = k0; K < k1; ++K) {  // the same trip count in every lane
+    float sum = 0.f;
+    if (act) {
 #pragma unroll
-  for (int ck = 0; ck < 2; ++ck)
-#pragma unroll
-    for (int cj = 0; cj < 2; ++cj)
-#pragma unroll
-      for (int ci = 0; ci < 2; ++ci) {
-        if ((ci + cj + ck) & 1) continue;
-        const int i = 2 * X.i[0] + ci, j = 2 * X.i[1] + cj, k = 2 * X.i[2] + ck;
+      for (int cj = 0; cj < 2; ++cj) {
+        const int ci = (cj + ck) & 1;  // red children: ci + cj + ck even
+        const int i = 2 * I + ci, j = 2 * J + cj, k = 2 * K + ck;
         const int odd = i & 1;
         const int p = (i >> 1) + h0 * (j + f.n1 * k);  // red: colour 0
         const int fx = i + (f.n0 + 1) * (j + f.n1 * k);
@@ -941,9 +947,14 @@ __global__ void __launch_bounds__(NT, 4) k_mg0_restrict(Fast0 f, Mesh cm, const 
           acc = fmaf(h2f(f.kz, fz + f.n0 * f.n1), x0[half + p + hz] - xc, acc);
         sum += fmaf(scale, acc, b0[p]);
       }
-  cb[X.c] = sum;
-  cx[X.c] = cidg && ((X.i[0] + X.i[1] + X.i[2]) & 1) == 0 ? sum * cidg[X.c] : 0.f;
-  CELL_LOOP_END
+    }
+    sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+    if (act && ck == 0) {
+      const int C = I + cm.n[0] * (J + cm.n[1] * K);
+      cb[C] = sum;
+      cx[C] = cidg && ((I + J + K) & 1) == 0 ? sum * cidg[C] : 0.f;
+    }
+  }
 }
 
 // ---- inner CG in the colour-blocked order of the finest level (fast0) --
@@ -1573,7 +1584,9 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
       count_launches(1);
     }
     MgLevel& c = mg.lev[1];
-    Launch L = cell_launch(c.m);
+    Mesh c2 = c.m;  // two threads per coarse cell along x
+    c2.n[0] *= 2;
+    const Launch L = cell_launch_waves(c2, resident_ctas((const void*)k_mg0_restrict));
     const float* cidg = 1 < top ? c.idg : nullptr;
     PDL(k_mg0_restrict, L.grid, L.block, 0, st, f0, c.m, b0, x0, c.b, c.x, cidg, ds, L.kch);
     count_launches(1);
