@@ -924,15 +924,9 @@ __global__ void __launch_bounds__(NT) k_mg0_restrict(Fast0 f, Mesh cm, const flo
   const int J = blockIdx.y * BY + threadIdx.y;
   const bool act = I < cm.n[0] && J < cm.n[1];
   const int k0 = blockIdx.z * kch, k1 = min(k0 + kch, cm.n[2]);
-  // two coarse planes per trip (the same trip count in every lane), both
-  // planes' loads ahead of their stores
-  for (int Kb = k0; Kb < k1; Kb += 2) {
-    float sums[2] = {0.f, 0.f};
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-    const int K = Kb + u;
+  for (int K = k0; K < k1; ++K) {  // the same trip count in every lane
     float sum = 0.f;
-    if (act && K < k1) {
+    if (act) {
 #pragma unroll
       for (int cj = 0; cj < 2; ++cj) {
         const int ci = (cj + ck) & 1;  // red children: ci + cj + ck even
@@ -954,17 +948,11 @@ __global__ void __launch_bounds__(NT) k_mg0_restrict(Fast0 f, Mesh cm, const flo
         sum += fmaf(scale, acc, b0[p]);
       }
     }
-    sums[u] = sum;
-    }
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int K = Kb + u;
-      const float sum = sums[u] + __shfl_xor_sync(0xffffffffu, sums[u], 1);
-      if (act && ck == 0 && K < k1) {
-        const int C = I + cm.n[0] * (J + cm.n[1] * K);
-        cb[C] = sum;
-        cx[C] = cidg && ((I + J + K) & 1) == 0 ? sum * cidg[C] : 0.f;
-      }
+    sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+    if (act && ck == 0) {
+      const int C = I + cm.n[0] * (J + cm.n[1] * K);
+      cb[C] = sum;
+      cx[C] = cidg && ((I + J + K) & 1) == 0 ? sum * cidg[C] : 0.f;
     }
   }
 }
@@ -1043,44 +1031,26 @@ __global__ void __launch_bounds__(NT) k_cg32_dir_spmv_blk(Fast0 f, const float* 
   if (i < n0 && j < n1) {
     const int ih = i >> 1, e = i & 1;
     const int k0 = blockIdx.z * kch, k1 = min(k0 + kch, n2);
-    // two planes per trip, both planes' loads ahead of their stores: the
-    // kernel is load-latency-bound with one cell in flight per thread
-    for (int kb = k0; kb < k1; kb += 2) {
-      float pv[2], av[2];
-      int ov[2];
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int k = kb + u;
-        ov[u] = -1;
-        pv[u] = av[u] = 0.f;
-        if (k >= k1) continue;
-        const int row = j + n1 * k;
-        const int p = ih + h0 * row;
-        const int q = (i + j + k) & 1;
-        const int own = q * half + p, oth = (1 - q) * half + p;
-        const int c = i + n0 * row;
-        const int fx = i + (n0 + 1) * row;
-        const int fy = fofs1 + i + n0 * (j + (n1 + 1) * k);
-        const int fz = fofs2 + c;
-        const float pc = P(own);
-        float a = dg[c] * pc;
-        if (i > 0) a = fmaf(-kf[fx], P(oth - 1 + e), a);
-        if (i < n0 - 1) a = fmaf(-kf[fx + 1], P(oth + e), a);
-        if (j > 0) a = fmaf(-kf[fy], P(oth - h0), a);
-        if (j < n1 - 1) a = fmaf(-kf[fy + n0], P(oth + h0), a);
-        if (k > 0) a = fmaf(-kf[fz], P(oth - hz), a);
-        if (k < n2 - 1) a = fmaf(-kf[fz + n0 * n1], P(oth + hz), a);
-        ov[u] = own;
-        pv[u] = pc;
-        av[u] = a;
-      }
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        if (ov[u] < 0) continue;
-        pnew[ov[u]] = pv[u];
-        Ap[ov[u]] = av[u];
-        acc.add_prod(pv[u], av[u]);
-      }
+    for (int k = k0; k < k1; ++k) {
+      const int row = j + n1 * k;
+      const int p = ih + h0 * row;
+      const int q = (i + j + k) & 1;
+      const int own = q * half + p, oth = (1 - q) * half + p;
+      const int c = i + n0 * row;
+      const int fx = i + (n0 + 1) * row;
+      const int fy = fofs1 + i + n0 * (j + (n1 + 1) * k);
+      const int fz = fofs2 + c;
+      const float pc = P(own);
+      float a = dg[c] * pc;
+      if (i > 0) a = fmaf(-kf[fx], P(oth - 1 + e), a);
+      if (i < n0 - 1) a = fmaf(-kf[fx + 1], P(oth + e), a);
+      if (j > 0) a = fmaf(-kf[fy], P(oth - h0), a);
+      if (j < n1 - 1) a = fmaf(-kf[fy + n0], P(oth + h0), a);
+      if (k > 0) a = fmaf(-kf[fz], P(oth - hz), a);
+      if (k < n2 - 1) a = fmaf(-kf[fz + n0 * n1], P(oth + hz), a);
+      pnew[own] = pc;
+      Ap[own] = a;
+      acc.add_prod(pc, a);
     }
   }
   double v[1] = {acc.value()};
