@@ -1006,9 +1006,10 @@ __global__ void __launch_bounds__(NT) k_mgcg_init_blk(Fast0 f, const double* __r
 
 // p = z + beta p_old (z on the first iteration), Ap = A32 p with the FP32
 // operator (cell-order couplings and diagonal), <p, Ap>: one thread per
-// cell on the cell-order grid (thread x of a row is cell i = x, the pair
-// i/2 of colour-blocked index q * half + (i/2 + n0/2 * row)); 32-bit
-// indices (the blocked level has < 2^30 cells).
+// cell pair (2h, 2h + 1) of a row on the half-width grid, so that every
+// warp-wide load reads 32 consecutive words of one colour; the two cells
+// share their x neighbours (each is the other's), 12 direction values per
+// pair.  32-bit indices (the blocked level has < 2^30 cells).
 __global__ void __launch_bounds__(NT) k_cg32_dir_spmv_blk(Fast0 f, const float* __restrict__ kf,
                                                           const float* __restrict__ dg,
                                                           const float* __restrict__ z,
@@ -1023,34 +1024,53 @@ __global__ void __launch_bounds__(NT) k_cg32_dir_spmv_blk(Fast0 f, const float* 
   const bool first = ds->flag[FL_PCG_ITERS] == 0;
   const float beta = first ? 0.f : (float)ds->red[RS_PCG_BETA];
   const int n0 = f.n0, n1 = f.n1, n2 = f.n2, h0 = n0 / 2;
-  const int half = h0 * n1 * n2, hz = h0 * n1;
+  const int half = h0 * n1 * n2, hz = h0 * n1, nxy = n0 * n1;
   auto P = [&](int b) { return first ? z[b] : fmaf(beta, pold[b], z[b]); };
   DFAcc2 acc;
-  const int i = blockIdx.x * BX + threadIdx.x;
+  const int ih = blockIdx.x * BX + threadIdx.x;
   const int j = blockIdx.y * BY + threadIdx.y;
-  if (i < n0 && j < n1) {
-    const int ih = i >> 1, e = i & 1;
+  if (ih < h0 && j < n1) {
     const int k0 = blockIdx.z * kch, k1 = min(k0 + kch, n2);
     for (int k = k0; k < k1; ++k) {
       const int row = j + n1 * k;
       const int p = ih + h0 * row;
-      const int q = (i + j + k) & 1;
-      const int own = q * half + p, oth = (1 - q) * half + p;
-      const int c = i + n0 * row;
-      const int fx = i + (n0 + 1) * row;
-      const int fy = fofs1 + i + n0 * (j + (n1 + 1) * k);
-      const int fz = fofs2 + c;
-      const float pc = P(own);
-      float a = dg[c] * pc;
-      if (i > 0) a = fmaf(-kf[fx], P(oth - 1 + e), a);
-      if (i < n0 - 1) a = fmaf(-kf[fx + 1], P(oth + e), a);
-      if (j > 0) a = fmaf(-kf[fy], P(oth - h0), a);
-      if (j < n1 - 1) a = fmaf(-kf[fy + n0], P(oth + h0), a);
-      if (k > 0) a = fmaf(-kf[fz], P(oth - hz), a);
-      if (k < n2 - 1) a = fmaf(-kf[fz + n0 * n1], P(oth + hz), a);
-      pnew[own] = pc;
-      Ap[own] = a;
-      acc.add_prod(pc, a);
+      const int q = (j + k) & 1;  // colour of the even cell
+      const int a0 = q * half + p, a1 = (1 - q) * half + p;  // even, odd cell
+      const int c0 = 2 * p;
+      const int i0 = 2 * ih;
+      const int fx = i0 + (n0 + 1) * row;
+      const int fy = fofs1 + i0 + n0 * (j + (n1 + 1) * k);
+      const int fz = fofs2 + c0;
+      const float p0 = P(a0), p1 = P(a1);
+      float s0 = dg[c0] * p0, s1 = dg[c0 + 1] * p1;
+      // x: even cell's low neighbour is the odd cell of the pair before;
+      // the odd cell's high neighbour the even cell of the pair after
+      if (i0 > 0) s0 = fmaf(-kf[fx], P(a1 - 1), s0);
+      s0 = fmaf(-kf[fx + 1], p1, s0);
+      s1 = fmaf(-kf[fx + 1], p0, s1);
+      if (i0 + 2 < n0) s1 = fmaf(-kf[fx + 2], P(a0 + 1), s1);
+      if (j > 0) {
+        s0 = fmaf(-kf[fy], P(a1 - h0), s0);
+        s1 = fmaf(-kf[fy + 1], P(a0 - h0), s1);
+      }
+      if (j < n1 - 1) {
+        s0 = fmaf(-kf[fy + n0], P(a1 + h0), s0);
+        s1 = fmaf(-kf[fy + n0 + 1], P(a0 + h0), s1);
+      }
+      if (k > 0) {
+        s0 = fmaf(-kf[fz], P(a1 - hz), s0);
+        s1 = fmaf(-kf[fz + 1], P(a0 - hz), s1);
+      }
+      if (k < n2 - 1) {
+        s0 = fmaf(-kf[fz + nxy], P(a1 + hz), s0);
+        s1 = fmaf(-kf[fz + nxy + 1], P(a0 + hz), s1);
+      }
+      pnew[a0] = p0;
+      pnew[a1] = p1;
+      Ap[a0] = s0;
+      Ap[a1] = s1;
+      acc.add_prod(p0, s0);
+      acc.add_prod(p1, s1);
     }
   }
   double v[1] = {acc.value()};
@@ -1829,7 +1849,9 @@ cudaError_t mgcg_iterate(const Mesh& m, int chunk, PcgWork& w, MgWork& mg, cudaS
     cudaError_t e;
     if (mg.fast0) {
       const Fast0 f{m.n[0], m.n[1], m.n[2], mg.k16[0], mg.k16[1], mg.k16[2]};
-      const Launch H = cell_launch_waves(m, resident_ctas((const void*)k_cg32_dir_spmv_blk));
+      Mesh hm = m;  // one thread per cell pair
+      hm.n[0] = m.n[0] / 2;
+      const Launch H = cell_launch_waves(hm, resident_ctas((const void*)k_cg32_dir_spmv_blk));
       PDL(k_cg32_dir_spmv_blk, H.grid, H.block, 0, st, f, w.kf32, w.dg32, w.z32, pold, pnew,
           w.Ap32, (int)m.fofs[1], (int)m.fofs[2], w.partials, w.ds, H.kch);
       count_launches(1);
