@@ -809,30 +809,13 @@ __global__ void k_mg0_diag(Fast0 f, const DevScalars* ds, float* idg0) {
   }
 }
 
-// Start of a V-cycle on the colour-blocked finest level, whose right-hand
-// side is the inner CG's residual itself (kept colour-blocked): the first
-// half-sweep, red from x = 0, is x = b / diag on the red half.
-__global__ void __launch_bounds__(NT) k_mg0_red0(long long half, const float* __restrict__ b0,
-                                                 const float* __restrict__ idg0,
-                                                 float* __restrict__ x0, const DevScalars* ds) {
-  pdl_wait();
-  pdl_trigger();
-  if (ds->flag[FL_PCG_DONE]) return;
-  const long long n4 = half >> 2;
-  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = g; i < n4; i += stride) {
-    const float4 b = reinterpret_cast<const float4*>(b0)[i];
-    const float4 d = reinterpret_cast<const float4*>(idg0)[i];
-    reinterpret_cast<float4*>(x0)[i] = make_float4(b.x * d.x, b.y * d.y, b.z * d.z, b.w * d.w);
-  }
-  for (long long i = 4 * n4 + g; i < half; i += stride) x0[i] = b0[i] * idg0[i];
-}
-
 // Red-black half-sweep of one colour on the blocked arrays.  PROLONG: the
 // neighbours are read as x + cx(parent) (the injected coarse correction,
-// first post-smoothing half-sweep).
-template <bool PROLONG>
+// first post-smoothing half-sweep).  FROMZERO (the first black half-sweep
+// of a V-cycle): the red half-sweep from x = 0 before it is folded in --
+// the red neighbours are read as b / diag, and each thread also stores
+// that value for the red cell of its own pair.
+template <bool PROLONG, bool FROMZERO = false>
 __global__ void __launch_bounds__(NT) k_mg0_smooth(Fast0 f, const float* idg0, const float* b0,
                                                    float* x0, int color, const float* cx,
                                                    const DevScalars* ds, int kch) {
@@ -877,8 +860,15 @@ __global__ void __launch_bounds__(NT) k_mg0_smooth(Fast0 f, const float* idg0, c
     in[5] = k < f.n2 - 1;
     nb[5] = p + hz;
     ks[5] = h2f(f.kz, fz + f.n0 * f.n1);
+    if (FROMZERO) {
 #pragma unroll
-    for (int q = 0; q < 6; ++q) xs[q] = in[q] ? x0[oth + nb[q]] : 0.f;
+      for (int q = 0; q < 6; ++q)
+        xs[q] = in[q] ? b0[oth + nb[q]] * idg0[oth + nb[q]] : 0.f;
+      x0[oth + p] = b0[oth + p] * idg0[oth + p];  // the other cell of the pair
+    } else {
+#pragma unroll
+      for (int q = 0; q < 6; ++q) xs[q] = in[q] ? x0[oth + nb[q]] : 0.f;
+    }
     if (PROLONG) {
       const int ci = i >> 1, cj = j >> 1, ck = k >> 1;
       const int pc = ci + cnx * (cj + cny * ck);
@@ -1592,15 +1582,19 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
     const Launch H = fast0_launch(m0);
     float* x0 = z;
     const float* b0 = r;
-    PDL(k_mg0_red0, flat_blocks_mg(m0.nc / 8), NT, 0, st, m0.nc / 2, b0, mg.idg0, x0, ds);
-    count_launches(1);
     for (int s = 0; s < ns; ++s) {
       if (s > 0) {
         PDL(k_mg0_smooth<false>, H.grid, H.block, 0, st, f0, mg.idg0, b0, x0, 0, nullptr, ds,
             H.kch);
         count_launches(1);
       }
-      PDL(k_mg0_smooth<false>, H.grid, H.block, 0, st, f0, mg.idg0, b0, x0, 1, nullptr, ds, H.kch);
+      // the first black half-sweep carries the red one from zero
+      if (s == 0)
+        PDL(k_mg0_smooth<false, true>, H.grid, H.block, 0, st, f0, mg.idg0, b0, x0, 1, nullptr, ds,
+            H.kch);
+      else
+        PDL(k_mg0_smooth<false>, H.grid, H.block, 0, st, f0, mg.idg0, b0, x0, 1, nullptr, ds,
+            H.kch);
       count_launches(1);
     }
     MgLevel& c = mg.lev[1];
