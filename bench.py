@@ -336,6 +336,7 @@ def measure(args, form, rank, world, local, stream, e2e=True):
         h.step_graph()  # capture
         barrier(world)
         torch.cuda.synchronize()
+        g0 = S.launch_count()
         e0.record(stream)
         gstats = [h.step_graph() for _ in range(args.steps)]
         e1.record(stream)
@@ -343,7 +344,7 @@ def measure(args, form, rank, world, local, stream, e2e=True):
         barrier(world)
         gms = max_over_ranks(e0.elapsed_time(e1), world)
         out["graph"] = {"ms": gms, "value": world * N * args.steps / (gms / 1e3) / 1e6,
-                        "stats": gstats}
+                        "stats": gstats, "launches": S.launch_count() - g0}
         # through the public C-ABI with host buffers (the graph-captured step):
         # every step uploads the state from pinned host memory and reads the
         # result back
@@ -536,6 +537,7 @@ def run_ours(args, rank, world, local):
             "note": "same steps, one CUDA-graph launch per step; value above is the "
                     "host-driven step with per-group CUDA events (roofline source)",
             "pressure_iterations": [s["pressure_iterations"] for s in head["graph"]["stats"]],
+            "gpu_launches": head["graph"]["launches"],
         },
     }
     if head.get("guess"):

@@ -40,7 +40,7 @@ using namespace hg;
 
 namespace hg {
 static std::atomic<long long> g_launches{0};
-void count_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launch_total() { return g_launches.load(); }
 
 int resident_ctas(const void* kernel) {
@@ -214,6 +214,13 @@ struct hydro_ctx {
   cudaGraph_t cap_graph = nullptr;
   cudaStream_t cap_streams[4] = {};
   int cap_depth = 0;
+  // kernel counts of a capture: per nesting level (0: the graph itself)
+  // the launch counter at its start and the kernels of the bodies nested
+  // in it; kernels a graph launch runs outside any body; the device body
+  // counter (RS_KEXEC) as last read
+  long long cap_start[5] = {}, cap_nested[5] = {};
+  long long graph_top = 0;
+  double kexec_seen = 0.;
   struct StepGraph {
     cudaGraphExec_t exec = nullptr;
     double dt = -1., adv_dt = -1.;
@@ -380,6 +387,12 @@ int new_handle(hydro_ctx* x, unsigned def, cudaGraphConditionalHandle* h) {
   return HYDRO_OK;
 }
 
+// Kernels of the body being captured up to and including the next launch
+// (its closing control kernel), bodies nested in it excluded.
+int body_kernels(const hydro_ctx* x) {
+  return (int)(launch_total() + 1 - x->cap_start[x->cap_depth] - x->cap_nested[x->cap_depth]);
+}
+
 // Adds a WHILE (or IF) node after the work captured so far on x->st and
 // captures `body` into it on the next capture stream.
 template <class Body>
@@ -404,6 +417,8 @@ int add_conditional(hydro_ctx* x, cudaGraphConditionalHandle h, cudaGraphConditi
                                          cudaStreamSetCaptureDependencies));
   cudaGraph_t bg = p.conditional.phGraph_out[0];
   cudaStream_t inner = x->cap_streams[x->cap_depth++];
+  x->cap_start[x->cap_depth] = launch_total();
+  x->cap_nested[x->cap_depth] = 0;
   CK(cudaStreamBeginCaptureToGraph(inner, bg, nullptr, nullptr, 0,
                                    cudaStreamCaptureModeRelaxed));
   x->st = inner;
@@ -411,7 +426,9 @@ int add_conditional(hydro_ctx* x, cudaGraphConditionalHandle h, cudaGraphConditi
   x->st = outer;
   cudaGraph_t done = nullptr;
   cudaError_t e = cudaStreamEndCapture(inner, &done);
+  const long long inner_kernels = launch_total() - x->cap_start[x->cap_depth];
   x->cap_depth--;
+  x->cap_nested[x->cap_depth] += inner_kernels;
   if (rc) return rc;
   CK(e);
   return HYDRO_OK;
@@ -472,7 +489,7 @@ int solve_momentum(hydro_ctx* x) {
       rc = add_loop(x, h, [&]() -> int {
         int r;
         if ((r = gs_sweep()) || (r = gs_sweep())) return r;
-        CK(launch_ctl_sweeps(x->pw.ds, limit, h, 1, x->st));
+        CK(launch_ctl_sweeps(x->pw.ds, limit, h, 1, x->st, body_kernels(x)));
         return HYDRO_OK;
       });
       if (rc) return rc;
@@ -536,7 +553,7 @@ int solve_momentum(hydro_ctx* x) {
     rc = add_loop(x, h, [&]() -> int {
       int r;
       if ((r = sweep(0)) || (r = sweep(1))) return r;
-      CK(launch_ctl_sweeps(x->pw.ds, limit, h, 1, x->st));
+      CK(launch_ctl_sweeps(x->pw.ds, limit, h, 1, x->st, body_kernels(x)));
       return HYDRO_OK;
     });
     if (rc) return rc;
@@ -592,7 +609,7 @@ int heat_step(hydro_ctx* x) {
     rc = add_loop(x, hc, [&]() -> int {
       int r;
       if ((r = sweep(0)) || (r = sweep(1))) return r;
-      CK(launch_ctl_heat(x->pw.ds, limit, hc, 1, x->st));
+      CK(launch_ctl_heat(x->pw.ds, limit, hc, 1, x->st, body_kernels(x)));
       return HYDRO_OK;
     });
     if (rc) return rc;
@@ -642,7 +659,7 @@ int solve_pressure_graph(hydro_ctx* x, int singular, int mixed, bool apply_pin_g
     if ((rc = new_handle(x, 1, &h))) return rc;
     rc = add_loop(x, h, [&]() -> int {
       CK(pcg_iterate(m, x->kf, x->pc, 4, w, x->st));
-      CK(launch_ctl_krylov(w.ds, h, 1, x->st));
+      CK(launch_ctl_krylov(w.ds, h, 1, x->st, body_kernels(x)));
       return HYDRO_OK;
     });
     if (rc) return rc;
@@ -669,7 +686,7 @@ int solve_pressure_graph(hydro_ctx* x, int singular, int mixed, bool apply_pin_g
         int r;
         if ((r = apply_guess(x, singular))) return r;
         CK(launch_ctl_guess(w.ds, d.pressure_tolerance, inner_min, d.pressure_iters_limit, hr,
-                            x->st));
+                            x->st, body_kernels(x)));
         return HYDRO_OK;
       });
       if (rc) return rc;
@@ -681,7 +698,7 @@ int solve_pressure_graph(hydro_ctx* x, int singular, int mixed, bool apply_pin_g
       r = add_loop(x, hk, [&]() -> int {
         if (mgcg) CK(mgcg_iterate(m, 2, w, x->mg, x->st));
         else CK(f32_pcg_iterate(m, 4, w, x->st));
-        CK(launch_ctl_krylov(w.ds, hk, 1, x->st));
+        CK(launch_ctl_krylov(w.ds, hk, 1, x->st, body_kernels(x)));
         return HYDRO_OK;
       });
       if (r) return r;
@@ -689,7 +706,7 @@ int solve_pressure_graph(hydro_ctx* x, int singular, int mixed, bool apply_pin_g
       else CK(f32_accumulate(m, x->pc, w, x->st));
       CK(ir_residual(m, x->kf, x->prhs, x->pc, singular, w, x->st));
       CK(launch_ctl_refine(w.ds, d.pressure_tolerance, inner_min, d.pressure_iters_limit, hr, 1,
-                           x->st));
+                           x->st, body_kernels(x)));
       return HYDRO_OK;
     });
     if (rc) return rc;
@@ -1635,6 +1652,9 @@ int begin_capture_of(hydro_ctx* x, HostSnapshot* s) {
     if (!x->cap_streams[i]) CK(cudaStreamCreateWithFlags(&x->cap_streams[i], cudaStreamNonBlocking));
   *s = {x->time, x->adv_time, x->p_res, x->indicator, x->iter_count, x->cd_iter_count,
         x->vel_sweeps, x->p_iters, x->p_unconv, x->prof.on};
+  x->cap_depth = 0;
+  x->cap_start[0] = launch_total();
+  x->cap_nested[0] = 0;
   x->prof.on = false;
   x->graph_mode = true;
   return HYDRO_OK;
@@ -1678,11 +1698,11 @@ int enqueue_step_body(hydro_ctx* x, int substeps) {
     r = add_while(x, hw, [&]() -> int {
       int q;
       if ((q = hydro_gpu_make_iteration(x))) return q;
-      CK(launch_ctl_simple2(x->pw.ds, limit, tol, hi, hw, x->st));
+      CK(launch_ctl_simple2(x->pw.ds, limit, tol, hi, hw, x->st, body_kernels(x)));
       return add_if(x, hi, [&]() -> int {
         int z;
         if ((z = hydro_gpu_make_iteration(x))) return z;
-        CK(launch_ctl_simple(x->pw.ds, limit, tol, hw, 1, x->st));
+        CK(launch_ctl_simple(x->pw.ds, limit, tol, hw, 1, x->st, body_kernels(x)));
         return HYDRO_OK;
       });
     });
@@ -1724,6 +1744,14 @@ int enqueue_step_body(hydro_ctx* x, int substeps) {
     return HYDRO_OK;
 }
 
+// After a context's step was captured: what a launch runs outside the
+// bodies, and the captured launches taken off the launch counter (kernels
+// are counted when a graph launch runs them, finish_graph_step).
+void end_capture_count(hydro_ctx* x) {
+  x->graph_top = launch_total() - x->cap_start[0] - x->cap_nested[0];
+  count_launches(-(launch_total() - x->cap_start[0]));
+}
+
 // Captures one step of one context into x->sg.exec.
 int capture_step(hydro_ctx* x, int substeps) {
   if (x->sg.exec) {
@@ -1742,6 +1770,7 @@ int capture_step(hydro_ctx* x, int substeps) {
   if (cudaStreamBeginCaptureToGraph(x->st, g, nullptr, nullptr, 0,
                                     cudaStreamCaptureModeRelaxed) == cudaSuccess) {
     rc = enqueue_step_body(x, substeps);
+    end_capture_count(x);
     cudaGraph_t out = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(x->st, &out);
     if (!rc && e2 != cudaSuccess) rc = HYDRO_ERR_CUDA;
@@ -1812,6 +1841,10 @@ int finish_graph_step(hydro_ctx* x, int substeps, double adv_end, hydro_step_sta
   hydro_step_stats s;
   memset(&s, 0, sizeof(s));
   const DevScalars& h = *x->hds;
+  // the kernels this launch ran: those outside the bodies once, those of
+  // every body run as counted on the device
+  count_launches(x->graph_top + (long long)(h.red[RS_KEXEC] - x->kexec_seen));
+  x->kexec_seen = h.red[RS_KEXEC];
   x->iter_count = h.flag[FL_ITERS];
   x->cd_iter_count = h.flag[FL_ITERS];
   x->indicator = h.red[RS_INDICATOR];
@@ -1968,6 +2001,7 @@ int capture_batch(hydro_batch* b) {
       break;
     }
     rc = enqueue_step_body(x, b->substeps[i]);
+    end_capture_count(x);
     if (!rc && (cudaEventRecord(b->join[i], x->st) != cudaSuccess ||
                 cudaStreamWaitEvent(b->st, b->join[i], 0) != cudaSuccess))
       rc = HYDRO_ERR_CUDA;

@@ -16,28 +16,35 @@ namespace hg {
 
 namespace {
 
+// nk: kernels of the captured body this decision closes (0 outside a
+// graph), added to ds->red[RS_KEXEC] on each run of the body.
 __device__ __forceinline__ void decide(DevScalars* ds, int cont, cudaGraphConditionalHandle h,
-                                       int use) {
+                                       int use, int nk) {
   ds->flag[FL_CONT] = cont;
-  if (use) cudaGraphSetConditional(h, cont ? 1u : 0u);
+  if (use) {
+    cudaGraphSetConditional(h, cont ? 1u : 0u);
+    ds->red[RS_KEXEC] += (double)nk;
+  }
 }
 
-__global__ void k_ctl_sweeps(DevScalars* ds, int limit, cudaGraphConditionalHandle h, int use) {
+__global__ void k_ctl_sweeps(DevScalars* ds, int limit, cudaGraphConditionalHandle h, int use,
+                             int nk) {
   if (threadIdx.x != 0) return;
   int sweeps = ds->flag[FL_MOM_SWEEPS];
   int cont = !(ds->flag[FL_MOM_DONE] || sweeps >= limit);
   if (!cont) ds->flag[FL_STEP_SWEEPS] += sweeps;
-  decide(ds, cont, h, use);
+  decide(ds, cont, h, use, nk);
 }
 
-__global__ void k_ctl_heat(DevScalars* ds, int limit, cudaGraphConditionalHandle h, int use) {
+__global__ void k_ctl_heat(DevScalars* ds, int limit, cudaGraphConditionalHandle h, int use,
+                           int nk) {
   if (threadIdx.x != 0) return;
-  decide(ds, !(ds->flag[FL_HEAT_DONE] || ds->flag[FL_HEAT_SWEEPS] >= limit), h, use);
+  decide(ds, !(ds->flag[FL_HEAT_DONE] || ds->flag[FL_HEAT_SWEEPS] >= limit), h, use, nk);
 }
 
-__global__ void k_ctl_krylov(DevScalars* ds, cudaGraphConditionalHandle h, int use) {
+__global__ void k_ctl_krylov(DevScalars* ds, cudaGraphConditionalHandle h, int use, int nk) {
   if (threadIdx.x != 0) return;
-  decide(ds, !ds->flag[FL_PCG_DONE], h, use);
+  decide(ds, !ds->flag[FL_PCG_DONE], h, use, nk);
 }
 
 __global__ void k_ctl_krylov_done(DevScalars* ds) {
@@ -52,7 +59,7 @@ __global__ void k_ctl_krylov_done(DevScalars* ds) {
 // Iterative refinement (the mixed pressure solve): called after every FP64
 // residual; FL_IR_STATE = 0 marks the first residual of a solve.
 __global__ void k_ctl_refine(DevScalars* ds, double tol, double inner_min, int limit,
-                             cudaGraphConditionalHandle h, int use) {
+                             cudaGraphConditionalHandle h, int use, int nk) {
   if (threadIdx.x != 0) return;
   double rr = ds->red[RS_IR_RR];
   int total;
@@ -80,7 +87,7 @@ __global__ void k_ctl_refine(DevScalars* ds, double tol, double inner_min, int l
   } else if (!conv) {
     ds->flag[FL_STEP_PUNCONV] += 1;  // stopped at a limit (or NaN) above the tolerance
   }
-  decide(ds, cont, h, use);
+  decide(ds, cont, h, use, nk);
 }
 
 // Whether this SIMPLE iteration's pressure solve starts from the learned
@@ -106,7 +113,7 @@ __global__ void k_ctl_guess_gate(DevScalars* ds, int limit, cudaGraphConditional
 // The refinement loop's first decision, again, from the residual of the
 // accepted guess (no inner iterations yet: the whole limit is left).
 __global__ void k_ctl_guess(DevScalars* ds, double tol, double inner_min, int limit,
-                            cudaGraphConditionalHandle h) {
+                            cudaGraphConditionalHandle h, int nk) {
   if (threadIdx.x != 0) return;
   const double rr = ds->red[RS_IR_RR], ff = ds->red[RS_IR_FF];
   ds->red[RS_P_RES] = ff > 0. ? sqrt(rr / ff) : 0.;
@@ -117,7 +124,7 @@ __global__ void k_ctl_guess(DevScalars* ds, double tol, double inner_min, int li
     ds->red[RS_INNER_TOL] = t > inner_min ? t : inner_min;
     ds->flag[FL_PCG_LIMIT] = limit;
   }
-  decide(ds, cont, h, 1);
+  decide(ds, cont, h, 1, nk);
 }
 
 __global__ void k_store_ff(DevScalars* ds) {
@@ -125,19 +132,19 @@ __global__ void k_store_ff(DevScalars* ds) {
 }
 
 __global__ void k_ctl_simple(DevScalars* ds, int limit, double tol,
-                             cudaGraphConditionalHandle h, int use) {
+                             cudaGraphConditionalHandle h, int use, int nk) {
   if (threadIdx.x != 0) return;
   int it = ds->flag[FL_ITERS] + 1;
   ds->flag[FL_ITERS] = it;
   double ind = ds->red[RS_INDICATOR];
   int cont = !(it >= limit || ind < tol);
-  decide(ds, cont, h, use);
+  decide(ds, cont, h, use, nk);
 }
 
 // Same decision, written to two conditionals: the IF node of the second
 // iteration of a loop trip and the WHILE node of the trip.
 __global__ void k_ctl_simple2(DevScalars* ds, int limit, double tol, cudaGraphConditionalHandle h1,
-                              cudaGraphConditionalHandle h2) {
+                              cudaGraphConditionalHandle h2, int nk) {
   if (threadIdx.x != 0) return;
   int it = ds->flag[FL_ITERS] + 1;
   ds->flag[FL_ITERS] = it;
@@ -146,6 +153,7 @@ __global__ void k_ctl_simple2(DevScalars* ds, int limit, double tol, cudaGraphCo
   ds->flag[FL_CONT] = cont;
   cudaGraphSetConditional(h1, cont ? 1u : 0u);
   cudaGraphSetConditional(h2, cont ? 1u : 0u);
+  ds->red[RS_KEXEC] += (double)nk;
 }
 
 // A conditional's default value is applied once per graph launch, so a
@@ -182,29 +190,29 @@ int copy_blocks(long long n) {
 }  // namespace
 
 cudaError_t launch_ctl_sweeps(DevScalars* ds, int limit, cudaGraphConditionalHandle h, int use,
-                              cudaStream_t st) {
-  k_ctl_sweeps<<<1, 32, 0, st>>>(ds, limit, h, use);
+                              cudaStream_t st, int nk) {
+  k_ctl_sweeps<<<1, 32, 0, st>>>(ds, limit, h, use, nk);
   count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_ctl_heat(DevScalars* ds, int limit, cudaGraphConditionalHandle h, int use,
-                            cudaStream_t st) {
-  k_ctl_heat<<<1, 32, 0, st>>>(ds, limit, h, use);
+                            cudaStream_t st, int nk) {
+  k_ctl_heat<<<1, 32, 0, st>>>(ds, limit, h, use, nk);
   count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_ctl_krylov(DevScalars* ds, cudaGraphConditionalHandle h, int use,
-                              cudaStream_t st) {
-  k_ctl_krylov<<<1, 32, 0, st>>>(ds, h, use);
+                              cudaStream_t st, int nk) {
+  k_ctl_krylov<<<1, 32, 0, st>>>(ds, h, use, nk);
   count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_ctl_refine(DevScalars* ds, double tol, double inner_min, int limit,
-                              cudaGraphConditionalHandle h, int use, cudaStream_t st) {
-  k_ctl_refine<<<1, 32, 0, st>>>(ds, tol, inner_min, limit, h, use);
+                              cudaGraphConditionalHandle h, int use, cudaStream_t st, int nk) {
+  k_ctl_refine<<<1, 32, 0, st>>>(ds, tol, inner_min, limit, h, use, nk);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -217,8 +225,8 @@ cudaError_t launch_ctl_guess_gate(DevScalars* ds, int limit, cudaGraphConditiona
 }
 
 cudaError_t launch_ctl_guess(DevScalars* ds, double tol, double inner_min, int limit,
-                             cudaGraphConditionalHandle h, cudaStream_t st) {
-  k_ctl_guess<<<1, 32, 0, st>>>(ds, tol, inner_min, limit, h);
+                             cudaGraphConditionalHandle h, cudaStream_t st, int nk) {
+  k_ctl_guess<<<1, 32, 0, st>>>(ds, tol, inner_min, limit, h, nk);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -236,16 +244,16 @@ cudaError_t launch_ctl_krylov_done(DevScalars* ds, cudaStream_t st) {
 }
 
 cudaError_t launch_ctl_simple(DevScalars* ds, int limit, double tol,
-                              cudaGraphConditionalHandle h, int use, cudaStream_t st) {
-  k_ctl_simple<<<1, 32, 0, st>>>(ds, limit, tol, h, use);
+                              cudaGraphConditionalHandle h, int use, cudaStream_t st, int nk) {
+  k_ctl_simple<<<1, 32, 0, st>>>(ds, limit, tol, h, use, nk);
   count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_ctl_simple2(DevScalars* ds, int limit, double tol,
                                cudaGraphConditionalHandle h1, cudaGraphConditionalHandle h2,
-                               cudaStream_t st) {
-  k_ctl_simple2<<<1, 32, 0, st>>>(ds, limit, tol, h1, h2);
+                               cudaStream_t st, int nk) {
+  k_ctl_simple2<<<1, 32, 0, st>>>(ds, limit, tol, h1, h2, nk);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -77,7 +77,9 @@ enum {
   RS_MOM_DIFF_RED = 22,  // max |update| of the red half of a Gauss-Seidel sweep
   RS_GUESS_S0 = 23, RS_GUESS_S1 = 24,  // <x, f'>, <x, A x> of a learned initial guess
   RS_MG0_SCALE = 25,     // power-of-two scale of the FP16 finest-level couplings
-  RS_PCG_RRREF = 26      // inner multigrid CG: ||r||^2 at its last halving
+  RS_PCG_RRREF = 26,     // inner multigrid CG: ||r||^2 at its last halving
+  RS_KEXEC = 27          // kernels run by the conditional bodies of captured graphs (each
+                         // body's closing control kernel adds its count per run; exact below 2^53)
 };
 enum {
   FL_MOM_DONE = 0, FL_MOM_SWEEPS = 1, FL_PCG_DONE = 2, FL_PCG_ITERS = 3, FL_NAN = 4,
@@ -291,7 +293,7 @@ struct Profiler {
   virtual ~Profiler() {}
 };
 // Kernel launches issued by this library since load (all contexts).
-void count_launches(int n);
+void count_launches(long long n);
 // Kernels this library enqueued so far (every launcher counts its own).
 long long launch_total();
 
@@ -434,19 +436,19 @@ cudaError_t pin_rhs(const Mesh& m, const double* kf, double* f, long long pin, d
 // Momentum sweeps: continue while not converged and fewer than `limit`;
 // accumulates the finished loop's sweeps into FL_STEP_SWEEPS when it stops.
 cudaError_t launch_ctl_sweeps(DevScalars* ds, int limit, cudaGraphConditionalHandle h, int use,
-                              cudaStream_t st);
+                              cudaStream_t st, int nk = 0);
 // Krylov inner loop: continue while not done.
 // The temperature sweep loop (FL_HEAT_DONE / FL_HEAT_SWEEPS).
 cudaError_t launch_ctl_heat(DevScalars* ds, int limit, cudaGraphConditionalHandle h, int use,
-                            cudaStream_t st);
+                            cudaStream_t st, int nk = 0);
 cudaError_t launch_ctl_krylov(DevScalars* ds, cudaGraphConditionalHandle h, int use,
-                              cudaStream_t st);
+                              cudaStream_t st, int nk = 0);
 // Refinement cycle after a residual: records ||f||^2 on the first call,
 // the relative residual in RS_P_RES, adds the finished inner solve's
 // iterations; continues while above `tol`, below `limit` iterations and 50
 // cycles, then sets the next inner tolerance (>= inner_min) and limit.
 cudaError_t launch_ctl_refine(DevScalars* ds, double tol, double inner_min, int limit,
-                              cudaGraphConditionalHandle h, int use, cudaStream_t st);
+                              cudaGraphConditionalHandle h, int use, cudaStream_t st, int nk = 0);
 // End of a FP64 Krylov solve: RS_P_RES and FL_STEP_PITERS.
 // Learned guess in a captured step: the IF node around it runs while the
 // SIMPLE iteration count of the step is below `limit`; after the guess, the
@@ -454,18 +456,18 @@ cudaError_t launch_ctl_refine(DevScalars* ds, double tol, double inner_min, int 
 cudaError_t launch_ctl_guess_gate(DevScalars* ds, int limit, cudaGraphConditionalHandle h,
                                   int use, cudaStream_t st);
 cudaError_t launch_ctl_guess(DevScalars* ds, double tol, double inner_min, int limit,
-                             cudaGraphConditionalHandle h, cudaStream_t st);
+                             cudaGraphConditionalHandle h, cudaStream_t st, int nk = 0);
 // RS_IR_FF = RS_IR_RR (the residual of the zero guess, before a guess).
 cudaError_t launch_store_ff(DevScalars* ds, cudaStream_t st);
 cudaError_t launch_ctl_krylov_done(DevScalars* ds, cudaStream_t st);
 // SIMPLE loop after an iteration: FL_ITERS += 1; continue while below
 // `limit` and the indicator is not below `tol`.
 cudaError_t launch_ctl_simple(DevScalars* ds, int limit, double tol,
-                              cudaGraphConditionalHandle h, int use, cudaStream_t st);
+                              cudaGraphConditionalHandle h, int use, cudaStream_t st, int nk = 0);
 // The same for graph-captured loops with two conditionals (both set).
 cudaError_t launch_ctl_simple2(DevScalars* ds, int limit, double tol,
                                cudaGraphConditionalHandle h1, cudaGraphConditionalHandle h2,
-                               cudaStream_t st);
+                               cudaStream_t st, int nk = 0);
 // Sets a graph conditional (re-arms a loop nested in another loop's body).
 cudaError_t launch_set_cond(cudaGraphConditionalHandle h, unsigned v, cudaStream_t st);
 // Copies src to dst when the momentum sweep count is even (the last sweep

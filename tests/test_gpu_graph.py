@@ -133,3 +133,40 @@ def test_graph_and_host_steps_interleaved(built, pattern):
            "F": h.get_field(capi.F_VOLUME_FLUX), "q": h.get_field(capi.F_PARTIAL_DENSITY)}
     errs = compare(got, {k: ref[k] for k in got})
     assert all(v <= 1e-12 for v in errs.values()), errs
+
+
+def test_graph_launch_counts(built):
+    """Kernels counted for graph launches (the captured bodies count their
+    runs on the device): a batch step runs exactly the kernels of its cases'
+    graph steps run alone."""
+    from hydro_gb300.solver import Batch, Hydro, launch_count
+    specs = [cases.cavity(n=n, mu=1.0 / re, dt=1e-3) for n, re in ((32, 100), (48, 1000), (64, 400))]
+    descs = []
+    for d, _, _ in specs:
+        d = d.copy()
+        d.precision = capi.MIXED
+        d.pressure_solver = capi.LINEAR_MGCG
+        descs.append(d)
+    alone = []
+    for d, (_, u0, q0) in zip(descs, specs):
+        h = Hydro(d)
+        h.set_field(capi.F_VELOCITY, u0)
+        h.set_field(capi.F_PARTIAL_DENSITY, q0)
+        h.init_state()
+        h.step_graph()  # capture
+        c0 = launch_count()
+        st = h.step_graph()
+        alone.append((launch_count() - c0, st["outer_iterations"]))
+        h.close()
+    b = Batch(descs)
+    for c, (_, u0, q0) in zip(b.cases, specs):
+        c.set_field(capi.F_VELOCITY, u0)
+        c.set_field(capi.F_PARTIAL_DENSITY, q0)
+    b.init_state()
+    b.step()  # capture
+    c0 = launch_count()
+    b.step()
+    got = launch_count() - c0
+    b.close()
+    assert all(n > 0 for n, _ in alone), alone
+    assert got == sum(n for n, _ in alone), (got, alone)
