@@ -390,8 +390,6 @@ struct MgWork {
   long long vc_pin;
   DevScalars* vc_ds;
   bool vc_fast0;
-  int vc_dot;
-  const double* vc_partials;
   int vc_kernels;
 };
 Mesh mg_coarse_mesh(const Mesh& fine);
@@ -405,8 +403,7 @@ cudaError_t mg_setup(MgWork& mg, PcgWork& w, cudaStream_t st);
 // otherwise they are replayed as one graph (kernels back to back without a
 // host launch between them).
 cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevScalars* ds,
-                      cudaStream_t st, int dot = 0,
-                      double* partials = nullptr);
+                      cudaStream_t st);
 void mg_release(MgWork& mg);
 // Inner solve of the mixed path with the V-cycle as preconditioner:
 // init from the FP64 residual in w.r, chunks of iterations into w.x32.

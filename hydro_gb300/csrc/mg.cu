@@ -815,25 +815,18 @@ __global__ void k_mg0_diag(Fast0 f, const DevScalars* ds, float* idg0) {
 // of a V-cycle): the red half-sweep from x = 0 before it is folded in --
 // the red neighbours are read as b / diag, and each thread also stores
 // that value for the red cell of its own pair.
-// DOT (the last half-sweep of a V-cycle, red): with the iterate final it
-// also forms the inner CG's <r, z> (r = b0, z = x0, both colours of each
-// pair) -- what k_mgcg_dot does after the V-cycle otherwise; dot = 1: the
-// first (stores <r,z>), 2: later (also beta = <r,z> / <r,z>_old).
-template <bool PROLONG, bool FROMZERO = false, bool DOT = false>
+template <bool PROLONG, bool FROMZERO = false>
 __global__ void __launch_bounds__(NT) k_mg0_smooth(Fast0 f, const float* idg0, const float* b0,
                                                    float* x0, int color, const float* cx,
-                                                   DevScalars* ds, int kch, int dot = 0,
-                                                   double* partials = nullptr) {
+                                                   const DevScalars* ds, int kch) {
   pdl_wait();
   pdl_trigger();
   if (ds->flag[FL_PCG_DONE]) return;
   const int h0 = f.n0 / 2;
   const int ih = blockIdx.x * BX + threadIdx.x;
   const int j = blockIdx.y * BY + threadIdx.y;
-  DFAcc2 rz;
-  const bool act = ih < h0 && j < f.n1;
-  if (!DOT && !act) return;
-  const int k0 = blockIdx.z * kch, k1 = act ? min(k0 + kch, f.n2) : k0;
+  if (ih >= h0 || j >= f.n1) return;
+  const int k0 = blockIdx.z * kch, k1 = min(k0 + kch, f.n2);
   const int half = h0 * f.n1 * f.n2;
   const int hz = h0 * f.n1;
   const int own = color * half, oth = (1 - color) * half;
@@ -893,21 +886,6 @@ __global__ void __launch_bounds__(NT) k_mg0_smooth(Fast0 f, const float* idg0, c
     for (int q = 0; q < 6; ++q) acc = fmaf(ks[q], xs[q], acc);
     const float xn = fmaf(scale, acc, bb) * ig;
     x0[own + p] = xn;
-    if (DOT) {
-      // the pair's other cell is this cell's x neighbour: final x0 already read
-      rz.add_prod(bb, xn);
-      rz.add_prod(b0[oth + p], odd ? xs[0] : xs[1]);
-    }
-  }
-  if (DOT) {
-    double v[1] = {rz.value()};
-    __shared__ double o[1];
-    if (grid_reduce<RED_SUM, 1>(v, partials, &ds->ticket[TK_PCG_INIT2], o)) {
-      if (threadIdx.x == 0 && threadIdx.y == 0) {
-        if (dot == 2) ds->red[RS_PCG_BETA] = o[0] / ds->red[RS_PCG_RZ];
-        ds->red[RS_PCG_RZ] = o[0];
-      }
-    }
   }
 }
 
@@ -1586,7 +1564,7 @@ void mg_smooth(int dim, const Launch& H, bool per, const Mesh& m, const float* k
 // (black, red) sweeps after each coarse correction.  Levels above `top`
 // are grid launches; `top` and below run in one CTA.
 cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin,
-                             DevScalars* ds, cudaStream_t st, int dot, double* partials) {
+                             DevScalars* ds, cudaStream_t st) {
   int dim = mg.lev[0].m.dim;
   const bool per = any_periodic(mg.lev[0].m);
   mg.lev[0].b = const_cast<float*>(r);
@@ -1607,16 +1585,16 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
     for (int s = 0; s < ns; ++s) {
       if (s > 0) {
         PDL(k_mg0_smooth<false>, H.grid, H.block, 0, st, f0, mg.idg0, b0, x0, 0, nullptr, ds,
-            H.kch, 0, nullptr);
+            H.kch);
         count_launches(1);
       }
       // the first black half-sweep carries the red one from zero
       if (s == 0)
         PDL(k_mg0_smooth<false, true>, H.grid, H.block, 0, st, f0, mg.idg0, b0, x0, 1, nullptr, ds,
-            H.kch, 0, nullptr);
+            H.kch);
       else
         PDL(k_mg0_smooth<false>, H.grid, H.block, 0, st, f0, mg.idg0, b0, x0, 1, nullptr, ds,
-            H.kch, 0, nullptr);
+            H.kch);
       count_launches(1);
     }
     MgLevel& c = mg.lev[1];
@@ -1707,16 +1685,11 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
     const float* cx = mg.lev[1].x;
     for (int s = 0; s < ns; ++s) {
       if (s == 0)
-        PDL(k_mg0_smooth<true>, H.grid, H.block, 0, st, f0, mg.idg0, r, z, 1, cx, ds, H.kch, 0, nullptr);
+        PDL(k_mg0_smooth<true>, H.grid, H.block, 0, st, f0, mg.idg0, r, z, 1, cx, ds, H.kch);
       else
         PDL(k_mg0_smooth<false>, H.grid, H.block, 0, st, f0, mg.idg0, r, z, 1, nullptr, ds,
-            H.kch, 0, nullptr);
-      if (dot && s == ns - 1)  // the last half-sweep also forms <r, z>
-        PDL(k_mg0_smooth<false, false, true>, H.grid, H.block, 0, st, f0, mg.idg0, r, z, 0,
-            nullptr, ds, H.kch, dot, partials);
-      else
-        PDL(k_mg0_smooth<false>, H.grid, H.block, 0, st, f0, mg.idg0, r, z, 0, nullptr, ds,
-            H.kch, 0, nullptr);
+            H.kch);
+      PDL(k_mg0_smooth<false>, H.grid, H.block, 0, st, f0, mg.idg0, r, z, 0, nullptr, ds, H.kch);
       count_launches(2);
     }
   }
@@ -1726,17 +1699,17 @@ cudaError_t mg_vcycle_launch(MgWork& mg, const float* r, float* z, long long pin
 }  // namespace
 
 cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevScalars* ds,
-                      cudaStream_t st, int dot, double* partials) {
+                      cudaStream_t st) {
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   cudaError_t e = cudaStreamIsCapturing(st, &cs);
   if (e != cudaSuccess) return e;
-  if (cs != cudaStreamCaptureStatusNone) return mg_vcycle_launch(mg, r, z, pin, ds, st, dot, partials);
+  if (cs != cudaStreamCaptureStatusNone) return mg_vcycle_launch(mg, r, z, pin, ds, st);
   if (!mg.vc_exec || mg.vc_r != r || mg.vc_z != z || mg.vc_pin != pin || mg.vc_ds != ds ||
-      mg.vc_fast0 != mg.fast0 || mg.vc_dot != dot || mg.vc_partials != partials) {
+      mg.vc_fast0 != mg.fast0) {
     mg_release(mg);
     cudaGraph_t g = nullptr;
     if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed)) != cudaSuccess) return e;
-    cudaError_t el = mg_vcycle_launch(mg, r, z, pin, ds, st, dot, partials);
+    cudaError_t el = mg_vcycle_launch(mg, r, z, pin, ds, st);
     e = cudaStreamEndCapture(st, &g);
     if (el != cudaSuccess || e != cudaSuccess) {
       if (g) cudaGraphDestroy(g);
@@ -1758,8 +1731,6 @@ cudaError_t mg_vcycle(MgWork& mg, const float* r, float* z, long long pin, DevSc
     mg.vc_pin = pin;
     mg.vc_ds = ds;
     mg.vc_fast0 = mg.fast0;
-    mg.vc_dot = dot;
-    mg.vc_partials = partials;
   }
   count_launches(mg.vc_kernels);
   return cudaGraphLaunch(mg.vc_exec, st);
@@ -1855,15 +1826,11 @@ cudaError_t mgcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, MgW
   }
   count_launches(1);
   if (w.prof) w.prof->begin(HYDRO_PROF_MG_VCYCLE, st);
-  // on the colour-blocked finest level the V-cycle's last half-sweep forms
-  // <r, z> itself
-  cudaError_t e = mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st, mg.fast0 ? 1 : 0, w.partials);
+  cudaError_t e = mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st);
   if (w.prof) w.prof->end(HYDRO_PROF_MG_VCYCLE, st);
   if (e != cudaSuccess) return e;
-  if (!mg.fast0) {
-    PDL(k_mgcg_dot, fb, dim3(BX, BY), 0, st, m.nc, w.r32, w.z32, 1, w.partials, w.ds);
-    count_launches(1);
-  }
+  PDL(k_mgcg_dot, fb, dim3(BX, BY), 0, st, m.nc, w.r32, w.z32, 1, w.partials, w.ds);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -1894,14 +1861,11 @@ cudaError_t mgcg_iterate(const Mesh& m, int chunk, PcgWork& w, MgWork& mg, cudaS
         w.ds);
     if (w.prof) w.prof->end(HYDRO_PROF_CG_UPDATE, st);
     if (w.prof) w.prof->begin(HYDRO_PROF_MG_VCYCLE, st);
-    e = mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st, mg.fast0 ? 2 : 0, w.partials);
+    e = mg_vcycle(mg, w.r32, w.z32, w.pin, w.ds, st);
     if (w.prof) w.prof->end(HYDRO_PROF_MG_VCYCLE, st);
     if (e != cudaSuccess) return e;
-    if (!mg.fast0) {
-      PDL(k_mgcg_dot, fb, dim3(BX, BY), 0, st, m.nc, w.r32, w.z32, 0, w.partials, w.ds);
-      count_launches(1);
-    }
-    count_launches(1);
+    PDL(k_mgcg_dot, fb, dim3(BX, BY), 0, st, m.nc, w.r32, w.z32, 0, w.partials, w.ds);
+    count_launches(2);
     w.p32_parity ^= 1;
   }
   return cudaGetLastError();
