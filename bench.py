@@ -59,11 +59,22 @@ ALG_BYTES_PER_CELL_FP32 = {
     "cg_spmv": 4 * (6 + 2),                # read z, p_old, kf[3], diag; write p_new, Ap
     "cg_update": 4 * (4 + 2),              # read x, r, p, Ap; write x, r
     "mom_sweep": 4 * (10 + 3 + 3),         # read coef[7]+res[3], du[3]; write du[3]
-    # one V-cycle: finest level 4 red-black sweeps (x r/w, b, kf[3], 1/diag)
-    # + restriction of the red residuals (x, kf[3]; b and diag of the red
-    # half) + prolongation (x r/w), coarser levels 1/8 per level
-    "mg_vcycle": int(round(4 * (4 * 7 + 5 + 2) * 8 / 7)),
+    "mg_vcycle": None,                     # below
 }
+# One V-cycle, bytes per cell of the finest level.  Finest level (colour-
+# blocked, FP16 couplings): a half-sweep reads the couplings (3 faces x 2 B
+# per cell) and, on half of the cells each, its own colour's b and 1/diag,
+# the other colour's x, and writes its own x: 6 + 4 x 2 = 14 B; the first
+# (black) one also carries the red one from zero (reads the red b and
+# 1/diag instead of x, writes the red x: +4 B), the first post-smoothing
+# one reads the coarse correction (+0.5 B); 3 + 4 half-sweeps; restriction:
+# red b and x, black x, couplings, coarse b and x written = 13 B.  Coarser
+# levels (FP32 couplings 12 B per cell): 7 half-sweeps of 20 B, restriction
+# 21 B, prolongation 0.5 B per cell of the level, summed over the levels
+# (1/8 + 1/64 + ...) of the finest level's cells.
+_FINE = (14 + 4) + 14 + 14 + (14 + 0.5) + 3 * 14 + 13
+_COARSE = 7 * 20 + 21 + 0.5
+ALG_BYTES_PER_CELL_FP32["mg_vcycle"] = int(round(_FINE + _COARSE * (1 / 7)))
 
 
 def env_int(name, default):
