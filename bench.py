@@ -394,10 +394,10 @@ def measure(args, form, rank, world, local, stream, e2e=True):
 # DRAM traffic (ncu dram__bytes_read.sum + dram__bytes_write.sum) per cell of
 # one launch of a group, measured on smaller cases of the same workload
 # (rising drops, cold cache as ncu replays it) and applied per cell:
-#   mg_vcycle: one V-cycle at 128^3 (26 kernel launches) read 478.3 MB,
-#              wrote ~0 (the iterate stays in L2) -> 228.1 B/cell
+#   mg_vcycle: one V-cycle at 160^3, summed over per-kernel captures (one
+#              kernel and at most three launches each): 521.0 MB -> 127.2 B/cell
 #   cg_spmv:   k_cg_spmv<3, double> at 150^3: 134.9 + 16.0 MB -> 44.7 B/cell
-TRAFFIC_PER_CELL = {"mg_vcycle": 478.3e6 / 128 ** 3, "cg_spmv": 150.9e6 / 150 ** 3}
+TRAFFIC_PER_CELL = {"mg_vcycle": 521.0e6 / 160 ** 3, "cg_spmv": 150.9e6 / 150 ** 3}
 
 
 def roofline(res):
