@@ -667,7 +667,9 @@ def run_batch(args):
     else:
         for d in descs:
             d.cta_threads = args.cta_threads
-        tuning = {"by": "--cta-threads", "cta_threads": args.cta_threads}
+            d.cta_cluster = args.cta_cluster
+        tuning = {"by": "--cta-threads", "cta_threads": args.cta_threads,
+                  "cta_cluster": args.cta_cluster}
     b = Batch(descs)
     for c, (d, u0, q0, _) in zip(b.cases, specs):
         c.set_field(capi.F_VELOCITY, u0)
@@ -783,6 +785,8 @@ def main():
     ap.add_argument("--cta-threads", type=int, default=None,
                     help="--workload batch: launch shape of every case's solves (0: grid-wide; "
                          "default: chosen per grid size by the autotuner)")
+    ap.add_argument("--cta-cluster", type=int, default=0,
+                    help="--workload batch with --cta-threads: CTAs per solve's cluster")
     args = ap.parse_args()
     if args.workload == "batch":
         # before anything starts CUDA in this process

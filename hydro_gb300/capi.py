@@ -99,6 +99,7 @@ class HydroDesc(ctypes.Structure):
         ("rigid_box_hi", ctypes.c_double * 3),
         ("substitute_solvers", ctypes.c_int),
         ("cta_threads", ctypes.c_int),
+        ("cta_cluster", ctypes.c_int),
     ]
 
     @property

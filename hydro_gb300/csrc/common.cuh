@@ -2,6 +2,7 @@
 // shared by the sm_103a kernels of the hydro hot path.
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -144,6 +145,24 @@ inline cudaError_t pdl(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cuda
 // pdl() whose error, like a <<<>>> launch's, is left to cudaGetLastError
 #define PDL(...) ((void)pdl(__VA_ARGS__))
 
+
+// Thread groups of the in-CTA helpers: one CTA (__syncthreads) or one
+// thread-block cluster (its CTAs' threads numbered CTA-major; the cluster
+// barrier also orders the CTAs' global-memory accesses).
+struct CtaG {
+  __device__ int rank() const { return threadIdx.x; }
+  __device__ int size() const { return blockDim.x; }
+  __device__ void sync() const { __syncthreads(); }
+};
+struct ClusterG {
+  int r, n;
+  __device__ ClusterG()
+      : r((int)(cooperative_groups::this_cluster().block_rank() * blockDim.x + threadIdx.x)),
+        n((int)(cooperative_groups::this_cluster().num_blocks() * blockDim.x)) {}
+  __device__ int rank() const { return r; }
+  __device__ int size() const { return n; }
+  __device__ void sync() const { cooperative_groups::this_cluster().sync(); }
+};
 
 // Launch geometry: blocks of 32x8 threads over (i, j); each block marches
 // KCH planes in k so that the grid stays a few waves deep on 152 SMs.

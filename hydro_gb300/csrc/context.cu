@@ -518,7 +518,8 @@ int solve_momentum(hydro_ctx* x) {
     // the whole Jacobi loop by one CTA
     CK(launch_cta_mom_jacobi32(x->m, d.velocity_omega, d.velocity_tolerance, x->o32p(),
                                fp3(x->du32[0]), fp3(x->du32[1]), limit, x->graph_mode ? 1 : 0,
-                               d.cta_threads, x->pw.ds, x->st));
+                               d.cta_threads, d.cta_cluster > 1 ? d.cta_cluster : 1, x->pw.ds,
+                               x->st));
     if (x->graph_mode) {
       const long long n = x->m.nc * dim;
       CK(launch_select_sweep(n, nullptr, x->du[0], x->du32[1], x->du32[0], x->pw.ds, x->st));
@@ -734,8 +735,8 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
     // the whole solve by one CTA
     CK(mg_setup(x->mg, w, x->st));
     CK(cta_pressure(m, x->kf, x->prhs, x->pc, singular, d.pressure_tolerance, 1e-5,
-                    d.pressure_iters_limit, x->graph_mode ? 1 : 0, d.cta_threads, w, x->mg,
-                    x->st));
+                    d.pressure_iters_limit, x->graph_mode ? 1 : 0, d.cta_threads,
+                    d.cta_cluster > 1 ? d.cta_cluster : 1, w, x->mg, x->st));
     if (x->graph_mode) return HYDRO_OK;
     int rc = sync_scalars(x);
     if (rc) return rc;
@@ -915,6 +916,10 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
     if (!v_known || !p_known) return HYDRO_ERR_ARG;
     if ((!v_ok || !p_ok) && !desc->substitute_solvers) return HYDRO_ERR_UNSUPPORTED;
   }
+  if (desc->cta_cluster != 0 && desc->cta_cluster != 1 && desc->cta_cluster != 2 &&
+      desc->cta_cluster != 4 && desc->cta_cluster != 8)
+    return HYDRO_ERR_ARG;
+  if (desc->cta_cluster > 1 && desc->cta_threads == 0) return HYDRO_ERR_ARG;
   if (desc->cta_threads != 0) {
     const int t = desc->cta_threads;
     if (t < 32 || t > 1024 || t % 32) return HYDRO_ERR_ARG;
@@ -1128,6 +1133,11 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
   if (mg_prepare(x->mg) != cudaSuccess) {
     hydro_gpu_destroy(x);
     return HYDRO_ERR_CUDA;
+  }
+  if (x->mg.cta && x->mg.top >= x->mg.nlev) {
+    // the one-CTA solve runs its coarse levels in shared memory
+    hydro_gpu_destroy(x);
+    return HYDRO_ERR_UNSUPPORTED;
   }
   for (int q = 0; q < 6; ++q) {
     // the sides of a periodic direction carry no condition

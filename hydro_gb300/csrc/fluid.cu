@@ -539,21 +539,51 @@ __global__ void __launch_bounds__(NT) k_mom_sweep32(Mesh m, float omega, double 
   }
 }
 
-// The whole Jacobi loop of k_mom_sweep32 by ONE CTA on a plain block (no
-// periodic direction, no excluded cell): sweep k reads d[(k+1) % 2] and
+// The whole Jacobi loop of k_mom_sweep32 by ONE CTA (or one thread-block
+// cluster, G = ClusterG) on a plain block (no periodic direction, no
+// excluded cell): sweep k reads d[(k+1) % 2] and
 // writes d[k % 2] as the grid launches do, with the same per-cell
 // arithmetic and the same stop test on the largest correction (a maximum,
 // so the result does not depend on the CTA's order), up to `limit` sweeps.
 // For small cases run many at once: each takes one SM instead of queueing
 // two launches per sweep.
-template <int DIM>
+// Group-wide largest correction, the same in every thread (red: 34 floats).
+__device__ float grp_max(float v, float* red, const CtaG&) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  v = warp_max(v);
+  if ((tid & 31) == 0) red[tid >> 5] = v;
+  __syncthreads();
+  if (tid < 32) {
+    float w = tid < (nt + 31) / 32 ? red[tid] : 0.f;
+    w = warp_max(w);
+    if (tid == 0) red[32] = w;
+  }
+  __syncthreads();
+  const float r = red[32];
+  __syncthreads();
+  return r;
+}
+__device__ float grp_max(float v, float* red, const ClusterG&) {
+  const float b = grp_max(v, red, CtaG());
+  if (threadIdx.x == 0) red[33] = b;
+  auto cl = cooperative_groups::this_cluster();
+  cl.sync();
+  float t = 0.f;
+  const int nb = (int)cl.num_blocks();
+  for (int q = 0; q < nb; ++q) t = fmaxf(t, *cl.map_shared_rank(&red[33], q));
+  cl.sync();  // before red[33] is written again
+  return t;
+}
+
+template <int DIM, class G>
 __global__ void __launch_bounds__(1024) k_cta_mom_jacobi32(Mesh m, float omega, double tol,
                                                            FP<10> c, FP<3> d0, FP<3> d1,
                                                            int limit, int graph,
                                                            DevScalars* ds) {
   constexpr bool kPerT = false;
-  __shared__ float red[33];
-  const int n = (int)m.nc, tid = threadIdx.x, nt = blockDim.x;
+  __shared__ float red[34];
+  const G g;
+  const int n = (int)m.nc, tid = g.rank(), nt = g.size();
   int sweeps = 0;
   float dall = 0.f;
   bool done = false;
@@ -605,17 +635,7 @@ __global__ void __launch_bounds__(1024) k_cta_mom_jacobi32(Mesh m, float omega, 
         for (int v = 0; v < DIM; ++v) dout.a[v][q] = out[u][v];
       }
     }
-    dmax = warp_max(dmax);
-    if ((tid & 31) == 0) red[tid >> 5] = dmax;
-    __syncthreads();
-    if (tid < 32) {
-      float v = tid < (nt + 31) / 32 ? red[tid] : 0.f;
-      v = warp_max(v);
-      if (tid == 0) red[32] = v;
-    }
-    __syncthreads();
-    dall = red[32];
-    __syncthreads();
+    dall = grp_max(dmax, red, g);  // also the barrier between sweeps
     sweeps = k + 1;
     if (!((double)dall > tol)) {
       done = true;
@@ -1404,14 +1424,37 @@ cudaError_t launch_mom_sweep32(const Mesh& m, double omega, double tol, FP<10> c
 }
 
 cudaError_t launch_cta_mom_jacobi32(const Mesh& m, double omega, double tol, FP<10> c, FP<3> d0,
-                                    FP<3> d1, int limit, int graph, int threads, DevScalars* ds,
-                                    cudaStream_t st) {
-  if (any_periodic(m) || m.nc >= (1LL << 31) || threads < 32 || threads > 1024 || threads % 32)
+                                    FP<3> d1, int limit, int graph, int threads, int cluster,
+                                    DevScalars* ds, cudaStream_t st) {
+  if (any_periodic(m) || m.nc >= (1LL << 31) || threads < 32 || threads > 1024 || threads % 32 ||
+      cluster < 1 || cluster > 8)
     return cudaErrorInvalidValue;
-  if (m.dim == 3)
-    k_cta_mom_jacobi32<3><<<1, threads, 0, st>>>(m, (float)omega, tol, c, d0, d1, limit, graph, ds);
-  else
-    k_cta_mom_jacobi32<2><<<1, threads, 0, st>>>(m, (float)omega, tol, c, d0, d1, limit, graph, ds);
+  const float om = (float)omega;
+  if (cluster == 1) {
+    if (m.dim == 3)
+      k_cta_mom_jacobi32<3, CtaG><<<1, threads, 0, st>>>(m, om, tol, c, d0, d1, limit, graph, ds);
+    else
+      k_cta_mom_jacobi32<2, CtaG><<<1, threads, 0, st>>>(m, om, tol, c, d0, d1, limit, graph, ds);
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cluster);
+    cfg.blockDim = dim3(threads);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaError_t e =
+        m.dim == 3
+            ? cudaLaunchKernelEx(&cfg, k_cta_mom_jacobi32<3, ClusterG>, m, om, tol, c, d0, d1, limit,
+                                 graph, ds)
+            : cudaLaunchKernelEx(&cfg, k_cta_mom_jacobi32<2, ClusterG>, m, om, tol, c, d0, d1, limit,
+                                 graph, ds);
+    if (e != cudaSuccess) return e;
+  }
   count_launches(1);
   return cudaGetLastError();
 }

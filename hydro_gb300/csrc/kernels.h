@@ -153,11 +153,12 @@ cudaError_t launch_d2f(long long n, const double* in, float* out, cudaStream_t s
 // Mixed path: FP32 Jacobi sweep on the o32 output of the assembly
 // (o32 = {1/diag, 2*DIM off-diagonals, DIM residuals}); FP32 -> FP64 copy.
 // The whole Jacobi loop of launch_mom_sweep32 (sweeps until converged or
-// `limit`) by one CTA of `threads` threads, for a plain block; with graph
+// `limit`) by one CTA of `threads` threads (or a cluster of `cluster` such
+// CTAs), for a plain block; with graph
 // set it also adds its sweeps to FL_STEP_SWEEPS.
 cudaError_t launch_cta_mom_jacobi32(const Mesh& m, double omega, double tol, FP<10> c, FP<3> d0,
-                                    FP<3> d1, int limit, int graph, int threads, DevScalars* ds,
-                                    cudaStream_t st);
+                                    FP<3> d1, int limit, int graph, int threads, int cluster,
+                                    DevScalars* ds, cudaStream_t st);
 cudaError_t launch_mom_sweep32(const Mesh& m, double omega, double tol, FP<10> c, FP<3> din,
                                FP<3> dout, int limit, double* partials, DevScalars* ds,
                                cudaStream_t st);
@@ -409,12 +410,14 @@ void mg_release(MgWork& mg);
 // init from the FP64 residual in w.r, chunks of iterations into w.x32.
 // The whole mixed pressure solve (FP64 refinement around the multigrid CG,
 // x = the correction, mean-free when singular) by one CTA of `threads`
-// threads, for a plain block, after pcg_prepare(fp32) and mg_setup.  Leaves
+// threads, or one cluster of `cluster` such CTAs, for a plain block whose
+// coarse levels fit the CTA's shared memory (mg.top < mg.nlev), after
+// pcg_prepare(fp32) and mg_setup.  Leaves
 // RS_P_RES, FL_PCG_ITERS (inner iterations), FL_PCG_DONE (converged) and
 // with graph set adds to FL_STEP_PITERS / FL_STEP_PUNCONV / FL_STEP_NAN.
 cudaError_t cta_pressure(const Mesh& m, const double* kf, const double* f, double* x,
                          int singular, double tol, double inner_min, int limit, int graph,
-                         int threads, PcgWork& w, MgWork& mg, cudaStream_t st);
+                         int threads, int cluster, PcgWork& w, MgWork& mg, cudaStream_t st);
 cudaError_t mgcg_init(const Mesh& m, double tol, int dev_params, PcgWork& w, MgWork& mg,
                       cudaStream_t st);
 cudaError_t mgcg_iterate(const Mesh& m, int chunk, PcgWork& w, MgWork& mg, cudaStream_t st);

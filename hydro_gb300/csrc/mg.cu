@@ -281,12 +281,6 @@ struct MgBlock {
   int ox[kMgMaxLevels], ob[kMgMaxLevels], oi[kMgMaxLevels], ok[kMgMaxLevels];
 };
 
-// Thread group of the in-CTA helpers (the CTA, __syncthreads).
-struct CtaG {
-  __device__ int rank() const { return threadIdx.x; }
-  __device__ int size() const { return blockDim.x; }
-  __device__ void sync() const { __syncthreads(); }
-};
 
 template <int DIM>
 __device__ __forceinline__ void blk_ijk(const Mesh& m, int c, int* id) {
@@ -1090,17 +1084,21 @@ __global__ void k_accumulate_blk(Fast0 f, double* __restrict__ x, const float* _
   }
 }
 
-// ----------------------------------------- one CTA per pressure solve --
+// ------------------------------- one CTA or cluster per pressure solve --
 // The whole mixed pressure solve of a small plain block (no periodic
-// direction, no excluded cell) by ONE CTA: FP64 iterative refinement around
-// the multigrid-preconditioned FP32 CG, the same algorithm as the grid
-// launches (k_ir_residual / k_ctl_refine / k_mgcg_* / the V-cycle), with
-// __syncthreads between the passes instead of kernel boundaries and
-// CTA-wide sums in FP64 in a fixed order.  Hundreds of small cases then
-// each take one SM for their solve instead of queueing a few hundred tiny
-// grid launches apiece.  The levels above `top` stay in global memory (L2
-// for a small case); `top` and below are staged into shared memory once
-// per solve, as the block V-cycle stages them.
+// direction, no excluded cell) by ONE CTA or ONE thread-block cluster: FP64
+// iterative refinement around the multigrid-preconditioned FP32 CG, the
+// same algorithm as the grid launches (k_ir_residual / k_ctl_refine /
+// k_mgcg_* / the V-cycle), with group barriers (__syncthreads, or the
+// cluster barrier, which orders the CTAs' global-memory accesses) between
+// the passes instead of kernel boundaries, and group-wide sums in FP64 in
+// a fixed order.  Hundreds of small cases then each hold one SM (or a few)
+// for their solve instead of queueing a few hundred tiny grid launches
+// apiece.  The levels above `top` stay in global memory (L2 for a small
+// case) and are swept by the whole group; `top` and below are staged into
+// CTA 0's shared memory once per solve and run there as one sub-V-cycle
+// while the other CTAs wait at the barrier (the right-hand side and the
+// result of level `top` pass through its global arrays).
 struct CtaPressure {
   Mesh m;
   const double *kf, *dg, *f;  // FP64 couplings, diagonal, right-hand side
@@ -1110,16 +1108,18 @@ struct CtaPressure {
   long long pin;
   int singular, limit, graph;
   double tol, inner_min;
-  int nl, top;  // levels; first level in shared memory (nl: none)
-  MgBlock blk;  // the staged levels (valid when top < nl)
+  int nl, top;  // levels; first level in shared memory (< nl)
+  MgBlock blk;  // the staged levels
+  Mesh mtop;    // level `top`, exchanged through global memory
+  float *btop, *xtop;
   Mesh gm[kMgMaxLevels];
   const float *gkf[kMgMaxLevels], *gidg[kMgMaxLevels];
   float *gx[kMgMaxLevels], *gb[kMgMaxLevels];
-  int nsweep, coarse_sweeps;
+  int nsweep;
   DevScalars* ds;
 };
 
-// CTA-wide FP64 sum, the same value in every thread (sd: 33 doubles).
+// CTA-wide FP64 sum, the same value in every thread (sd: >= 34 doubles).
 __device__ double cta_sum(double v, double* sd) {
   v = warp_sum(v);
   const int nw = (blockDim.x + 31) >> 5;
@@ -1135,30 +1135,77 @@ __device__ double cta_sum(double v, double* sd) {
   __syncthreads();
   return r;
 }
+__device__ double grp_sum(double v, double* sd, const CtaG&) { return cta_sum(v, sd); }
+// Cluster-wide: every CTA's sum read from its shared memory in rank order.
+__device__ double grp_sum(double v, double* sd, const ClusterG& g) {
+  const double b = cta_sum(v, sd);
+  if (threadIdx.x == 0) sd[33] = b;
+  auto cl = cooperative_groups::this_cluster();
+  cl.sync();
+  double t = 0.;
+  const int nb = (int)cl.num_blocks();
+  for (int q = 0; q < nb; ++q) t += *cl.map_shared_rank(&sd[33], q);
+  cl.sync();  // before sd[33] is written again
+  return t;
+}
+__device__ bool grp_lead(const CtaG&) { return true; }
+__device__ bool grp_lead(const ClusterG&) {
+  return cooperative_groups::this_cluster().block_rank() == 0;
+}
 
-// z = M^-1 r on the CTA's level set (the finest level staged or not).
-template <int DIM>
-__device__ void cta_precondition(const CtaPressure& P, CtaLevels& V, float* sm, float* red) {
-  const int n = (int)P.m.nc;
-  if (P.top == 0) {
-    for (int c = threadIdx.x; c < n; c += blockDim.x) V.b[0][c] = P.r32[c];
-    __syncthreads();
+// z = M^-1 r by the group: the global levels swept and restricted by all,
+// the staged sub-V-cycle by CTA 0 (its level set V in shared memory).
+template <int DIM, class G>
+__device__ void grp_precondition(const CtaPressure& P, CtaLevels& V, float* sm, float* red,
+                                 const G& g) {
+  const int T = P.top, ns = P.nsweep;
+  for (int l = 0; l < T; ++l) {
+    const long long lp = l == 0 ? P.pin : -1;
+    for (int s = 0; s < ns; ++s) {
+      blk_half<DIM, false>(P.gm[l], P.gkf[l], P.gidg[l], P.gb[l], P.gx[l], 0, s == 0, lp, g);
+      blk_half<DIM, false>(P.gm[l], P.gkf[l], P.gidg[l], P.gb[l], P.gx[l], 1, false, lp, g);
+    }
+    const bool last = l + 1 == T;
+    blk_restrict<DIM, false>(P.gm[l], last ? P.mtop : P.gm[l + 1], P.gkf[l], P.gb[l], P.gx[l],
+                             last ? P.btop : P.gb[l + 1], lp, g);
   }
-  cta_vcycle<DIM, false>(V, red);
-  if (P.top == 0) {
-    for (int c = threadIdx.x; c < n; c += blockDim.x) P.z32[c] = V.x[0][c];
+  if (grp_lead(g)) {
+    const int n = (int)P.mtop.nc;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) V.b[0][q] = P.btop[q];
     __syncthreads();
+    cta_vcycle<DIM, false>(V, red);
+    for (int q = threadIdx.x; q < n; q += blockDim.x) P.xtop[q] = V.x[0][q];
+  }
+  g.sync();
+  for (int l = T - 1; l >= 0; --l) {
+    const long long lp = l == 0 ? P.pin : -1;
+    const bool last = l + 1 == T;
+    const Mesh& m = P.gm[l];
+    const Mesh& cm = last ? P.mtop : P.gm[l + 1];
+    const float* cx = last ? P.xtop : P.gx[l + 1];
+    float* x = P.gx[l];
+    const int nc = (int)m.nc;
+    for (int c = g.rank(); c < nc; c += g.size()) {
+      int id[3];
+      blk_ijk<DIM>(m, c, id);
+      x[c] += cx[(int)cell_id(cm, id[0] >> 1, id[1] >> 1, id[2] >> 1)];
+    }
+    g.sync();
+    for (int s = 0; s < ns; ++s) {
+      blk_half<DIM, false>(m, P.gkf[l], P.gidg[l], P.gb[l], x, 1, false, lp, g);
+      blk_half<DIM, false>(m, P.gkf[l], P.gidg[l], P.gb[l], x, 0, false, lp, g);
+    }
   }
 }
 
 // Inner MG-CG for A e = r (FP32, e in x32) to relative tolerance t within
 // `lim` iterations, stopping on a stall as k_mgcg_update does; returns the
 // iterations.
-template <int DIM>
-__device__ int cta_mgcg(const CtaPressure& P, CtaLevels& V, float* sm, float* red, double* sd,
-                        double t, int lim) {
+template <int DIM, class G>
+__device__ int grp_mgcg(const CtaPressure& P, CtaLevels& V, float* sm, float* red, double* sd,
+                        double t, int lim, const G& g) {
   const Mesh& m = P.m;
-  const int n = (int)m.nc, tid = threadIdx.x, nt = blockDim.x;
+  const int n = (int)m.nc, tid = g.rank(), nt = g.size();
   double s = 0.;
   for (int c = tid; c < n; c += nt) {
     const double v = P.r[c];
@@ -1166,13 +1213,13 @@ __device__ int cta_mgcg(const CtaPressure& P, CtaLevels& V, float* sm, float* re
     P.x32[c] = 0.f;
     s += v * v;
   }
-  const double rr0 = cta_sum(s, sd);
+  const double rr0 = grp_sum(s, sd, g);
   if (rr0 == 0. || lim <= 0) return 0;
   const double tol2 = t * t * rr0;
-  cta_precondition<DIM>(P, V, sm, red);
+  grp_precondition<DIM>(P, V, sm, red, g);
   s = 0.;
   for (int c = tid; c < n; c += nt) s += (double)P.r32[c] * (double)P.z32[c];
-  double rz = cta_sum(s, sd);
+  double rz = grp_sum(s, sd, g);
   double rref = rr0, beta = 0.;
   int it = 0, refit = 0;
   float* pold = P.p;
@@ -1186,7 +1233,7 @@ __device__ int cta_mgcg(const CtaPressure& P, CtaLevels& V, float* sm, float* re
     const float bt = (float)beta;
     auto Pv = [&](int c) { return first ? P.z32[c] : fmaf(bt, pold[c], P.z32[c]); };
     // U cells per thread per pass with every load before the stores (a
-    // CTA alone on a case is latency-bound otherwise)
+    // group alone on a case is latency-bound otherwise)
     constexpr int U = 4;
     s = 0.;
     for (int c0 = tid; c0 < n; c0 += U * nt) {
@@ -1224,7 +1271,7 @@ __device__ int cta_mgcg(const CtaPressure& P, CtaLevels& V, float* sm, float* re
         s += (double)pv[u] * (double)av[u];
       }
     }
-    const double pAp = cta_sum(s, sd);
+    const double pAp = grp_sum(s, sd, g);
     const float at = (float)(rz / pAp);
     s = 0.;
     for (int c0 = tid; c0 < n; c0 += U * nt) {
@@ -1246,17 +1293,17 @@ __device__ int cta_mgcg(const CtaPressure& P, CtaLevels& V, float* sm, float* re
         s += (double)rv[u] * (double)rv[u];
       }
     }
-    const double rr = cta_sum(s, sd);
+    const double rr = grp_sum(s, sd, g);
     ++it;
     if (rr <= 0.25 * rref) {
       rref = rr;
       refit = it;
     }
     if (rr <= tol2 || it >= lim || isnan(rr) || it - refit >= kStallIters) break;
-    cta_precondition<DIM>(P, V, sm, red);
+    grp_precondition<DIM>(P, V, sm, red, g);
     s = 0.;
     for (int c = tid; c < n; c += nt) s += (double)P.r32[c] * (double)P.z32[c];
-    const double rz1 = cta_sum(s, sd);
+    const double rz1 = grp_sum(s, sd, g);
     beta = rz1 / rz;
     rz = rz1;
     float* tmp = pold;
@@ -1266,37 +1313,26 @@ __device__ int cta_mgcg(const CtaPressure& P, CtaLevels& V, float* sm, float* re
   return it;
 }
 
-template <int DIM>
+// The whole solve by the launch's group G: one CTA (CtaG) or the one
+// cluster the grid is (ClusterG).
+template <int DIM, class G>
 __global__ void __launch_bounds__(kBlkThreads)
     k_cta_pressure(const __grid_constant__ CtaPressure P) {
   extern __shared__ float sm[];
   __shared__ float red[32];
-  __shared__ double sd[33];
-  __shared__ CtaLevels V;
+  __shared__ double sd[34];
+  __shared__ CtaLevels V;  // the staged levels (CTA 0)
+  const G g;
   const Mesh& m = P.m;
-  const int n = (int)m.nc, tid = threadIdx.x, nt = blockDim.x;
-  // level set: global levels above top, shared from top
-  if (P.top < P.nl) cta_stage_levels(P.blk, sm, &V, P.top);
-  if (tid == 0) {
-    V.nl = P.nl;
-    V.nsweep = P.nsweep;
-    V.coarse_sweeps = P.coarse_sweeps;
-    V.pin = P.pin;
-    if (P.top >= P.nl) V.cinv = nullptr;
-    for (int l = 0; l < P.top && l < P.nl; ++l) {
-      V.m[l] = P.gm[l];
-      V.kf[l] = P.gkf[l];
-      V.idg[l] = P.gidg[l];
-      V.x[l] = P.gx[l];
-      V.b[l] = P.gb[l];
-    }
-  }
+  const int n = (int)m.nc, tid = g.rank(), nt = g.size();
+  if (grp_lead(g)) cta_stage_levels(P.blk, sm, &V);
   double mean = 0.;
   if (P.singular) {
     double s = 0.;
     for (int c = tid; c < n; c += nt) s += P.f[c];
-    mean = cta_sum(s, sd) / (double)n;  // also orders the staging above
+    mean = grp_sum(s, sd, g) / (double)n;  // also orders the staging above
   } else {
+    g.sync();
     __syncthreads();
   }
   for (int c = tid; c < n; c += nt) P.x[c] = 0.;
@@ -1345,7 +1381,7 @@ __global__ void __launch_bounds__(kBlkThreads)
         s += rv[u] * rv[u];
       }
     }
-    const double rr = cta_sum(s, sd);
+    const double rr = grp_sum(s, sd, g);
     last = rr;
     if (isnan(rr)) {
       nan = true;
@@ -1359,15 +1395,15 @@ __global__ void __launch_bounds__(kBlkThreads)
     }
     if (total >= P.limit || outer >= 50) break;
     const double t = fmax(0.5 * P.tol * sqrt(ff / rr), P.inner_min);
-    total += cta_mgcg<DIM>(P, V, sm, red, sd, t, P.limit - total);
+    total += grp_mgcg<DIM>(P, V, sm, red, sd, t, P.limit - total, g);
     for (int c = tid; c < n; c += nt) P.x[c] += (double)P.x32[c];
     ++outer;
-    __syncthreads();
+    g.sync();
   }
   if (P.singular) {
     double s = 0.;
     for (int c = tid; c < n; c += nt) s += P.x[c];
-    const double xm = cta_sum(s, sd) / (double)n;
+    const double xm = grp_sum(s, sd, g) / (double)n;
     for (int c = tid; c < n; c += nt) P.x[c] -= xm;
   }
   if (tid == 0) {
@@ -1538,9 +1574,14 @@ cudaError_t mg_prepare(MgWork& mg) {
     const bool per = any_periodic(mg.lev[0].m);
     const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
     if (mg.cta && !per) {
-      cudaError_t e = mg.lev[0].m.dim == 3
-                          ? cudaFuncSetAttribute(k_cta_pressure<3>, attr, mg.smem_bytes)
-                          : cudaFuncSetAttribute(k_cta_pressure<2>, attr, mg.smem_bytes);
+      cudaError_t e =
+          mg.lev[0].m.dim == 3
+              ? cudaFuncSetAttribute(k_cta_pressure<3, CtaG>, attr, mg.smem_bytes)
+              : cudaFuncSetAttribute(k_cta_pressure<2, CtaG>, attr, mg.smem_bytes);
+      if (e != cudaSuccess) return e;
+      e = mg.lev[0].m.dim == 3
+              ? cudaFuncSetAttribute(k_cta_pressure<3, ClusterG>, attr, mg.smem_bytes)
+              : cudaFuncSetAttribute(k_cta_pressure<2, ClusterG>, attr, mg.smem_bytes);
       if (e != cudaSuccess) return e;
     }
     if (mg.lev[0].m.dim == 3)
@@ -1743,9 +1784,9 @@ void mg_release(MgWork& mg) {
 
 cudaError_t cta_pressure(const Mesh& m, const double* kf, const double* f, double* x,
                          int singular, double tol, double inner_min, int limit, int graph,
-                         int threads, PcgWork& w, MgWork& mg, cudaStream_t st) {
-  if (any_periodic(m) || m.nf >= (1LL << 31) || mg.nlev < 1 || threads < 32 || threads > 1024 ||
-      threads % 32)
+                         int threads, int cluster, PcgWork& w, MgWork& mg, cudaStream_t st) {
+  if (any_periodic(m) || m.nf >= (1LL << 31) || mg.nlev < 1 || mg.top >= mg.nlev ||
+      threads < 32 || threads > 1024 || threads % 32 || cluster < 1 || cluster > 8)
     return cudaErrorInvalidValue;
   CtaPressure P{};
   P.m = m;
@@ -1769,9 +1810,11 @@ cudaError_t cta_pressure(const Mesh& m, const double* kf, const double* f, doubl
   P.tol = tol;
   P.inner_min = inner_min;
   P.nl = mg.nlev;
-  P.top = mg.top < mg.nlev ? mg.top : mg.nlev;
+  P.top = mg.top;
   P.nsweep = mg.nsweep;
-  P.coarse_sweeps = mg.top < mg.nlev ? mg.coarse_sweeps : mg.coarse_sweeps_large;
+  P.mtop = mg.lev[mg.top].m;
+  P.btop = mg.top == 0 ? w.r32 : mg.lev[mg.top].b;
+  P.xtop = mg.top == 0 ? w.z32 : mg.lev[mg.top].x;
   for (int l = 0; l < P.top; ++l) {
     const MgLevel& lv = mg.lev[l];
     P.gm[l] = lv.m;
@@ -1780,7 +1823,7 @@ cudaError_t cta_pressure(const Mesh& m, const double* kf, const double* f, doubl
     P.gx[l] = l == 0 ? w.z32 : lv.x;
     P.gb[l] = l == 0 ? w.r32 : lv.b;
   }
-  if (P.top < P.nl) {
+  {
     MgBlock& B = P.blk;
     B.nl = mg.nlev - mg.top;
     B.nsweep = mg.nsweep;
@@ -1802,9 +1845,27 @@ cudaError_t cta_pressure(const Mesh& m, const double* kf, const double* f, doubl
     }
   }
   P.ds = w.ds;
-  const int smem = P.top < P.nl ? mg.smem_bytes : 0;
-  if (m.dim == 3) k_cta_pressure<3><<<1, threads, smem, st>>>(P);
-  else k_cta_pressure<2><<<1, threads, smem, st>>>(P);
+  const int smem = mg.smem_bytes;
+  if (cluster == 1) {
+    if (m.dim == 3) k_cta_pressure<3, CtaG><<<1, threads, smem, st>>>(P);
+    else k_cta_pressure<2, CtaG><<<1, threads, smem, st>>>(P);
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cluster);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaError_t e = m.dim == 3 ? cudaLaunchKernelEx(&cfg, k_cta_pressure<3, ClusterG>, P)
+                               : cudaLaunchKernelEx(&cfg, k_cta_pressure<2, ClusterG>, P);
+    if (e != cudaSuccess) return e;
+  }
   count_launches(1);
   return cudaGetLastError();
 }

@@ -231,6 +231,13 @@ typedef struct hydro_desc {
    * solve stays grid-wide.  Results agree with the grid-wide form to the
    * solver tolerances, not bit for bit (other summation order). */
   int cta_threads;
+  /* With cta_threads set: the number of CTAs (1, 2, 4 or 8; 0 means 1) of
+   * the thread-block cluster that runs each of those solves -- the cluster's
+   * threads share the passes, cluster barriers separate them, the coarse
+   * multigrid levels run in the first CTA's shared memory.  A case's
+   * coarse levels must fit that shared memory (HYDRO_ERR_UNSUPPORTED
+   * otherwise). */
+  int cta_cluster;
 } hydro_desc;
 
 typedef struct hydro_step_stats {

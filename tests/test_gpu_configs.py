@@ -121,13 +121,13 @@ def test_mixed_forms_vs_fp64_full_size(built, config):
     print(config, "largest relative error over 50 steps:", {k: "%.1e" % v for k, v in worst.items()})
 
 
-@pytest.mark.parametrize("cta_threads", [0, 512])
-def test_c5_batch_512_cavities(built, cta_threads):
+@pytest.mark.parametrize("cta_threads,cta_cluster", [(0, 0), (512, 1), (1024, 4)])
+def test_c5_batch_512_cavities(built, cta_threads, cta_cluster):
     """512 cavities of 64^2..256^2 (13.4 M cells) in one batch, mixed with the
     multigrid CG, SIMPLE converged per case: two batch steps, and four cases
     of every size stepped alone give the same fields -- with grid-wide
-    solver launches, and with every linear solve by one CTA of 512
-    threads."""
+    solver launches, with every linear solve by one CTA of 512 threads, and
+    by one cluster of four CTAs of 1024 threads."""
     from hydro_gb300.solver import Batch, Hydro
     specs = cases.cavity_batch(ncases=512, seed=0)
     descs = []
@@ -136,6 +136,7 @@ def test_c5_batch_512_cavities(built, cta_threads):
         d.precision = capi.MIXED
         d.pressure_solver = capi.LINEAR_MGCG
         d.cta_threads = cta_threads
+        d.cta_cluster = cta_cluster
         descs.append(d)
     b = Batch(descs)
     for c, (d, u0, q0, _) in zip(b.cases, specs):
@@ -157,9 +158,11 @@ def test_c5_batch_512_cavities(built, cta_threads):
             assert rel(u, alone["u"]) <= 1e-12, (n, i)
 
 
-@pytest.mark.parametrize("n,threads", [(64, 256), (96, 512), (256, 1024)])
-def test_cta_solvers_match_grid_solvers(built, n, threads):
-    """The one-CTA linear solves against the grid-wide ones on a cavity
+@pytest.mark.parametrize("n,threads,cluster",
+                         [(64, 256, 1), (96, 512, 1), (256, 1024, 1), (96, 1024, 4),
+                          (256, 1024, 8)])
+def test_cta_solvers_match_grid_solvers(built, n, threads, cluster):
+    """The one-CTA (or one-cluster) linear solves against the grid-wide ones on a cavity
     (Re 1000, mixed, multigrid CG), host-driven and graph-captured steps
     interleaved: velocity and pressure within 1e-6 of the run's scale after
     5 steps of 5 SIMPLE iterations (both solve to a pressure residual of
@@ -174,6 +177,7 @@ def test_cta_solvers_match_grid_solvers(built, n, threads):
     d.velocity_tolerance = 1e-7
     dc = d.copy()
     dc.cta_threads = threads
+    dc.cta_cluster = cluster
     a, b = Hydro(d), Hydro(dc)
     for h in (a, b):
         h.set_field(capi.F_VELOCITY, u0)
