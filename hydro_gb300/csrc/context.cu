@@ -730,10 +730,9 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
   // and the FP64 path with the multigrid preconditioner (the FP64 system is
   // still solved to the FP64 tolerance; only the inner corrections are FP32)
   int mixed = (d.precision == HYDRO_MIXED) || d.pressure_solver == HYDRO_LINEAR_MGCG;
-  CK(pcg_prepare(m, x->kf, 0., w, mixed, x->st));
   if (d.cta_threads > 0) {
-    // the whole solve by one CTA
-    CK(mg_setup(x->mg, w, x->st));
+    // the whole solve, its set-up (diagonals, coarse levels) included, by
+    // one CTA or cluster
     CK(cta_pressure(m, x->kf, x->prhs, x->pc, singular, d.pressure_tolerance, 1e-5,
                     d.pressure_iters_limit, x->graph_mode ? 1 : 0, d.cta_threads,
                     d.cta_cluster > 1 ? d.cta_cluster : 1, w, x->mg, x->st));
@@ -748,6 +747,7 @@ int solve_pressure(hydro_ctx* x, bool apply_pin = true) {
     }
     return HYDRO_OK;
   }
+  CK(pcg_prepare(m, x->kf, 0., w, mixed, x->st));
   if (x->graph_mode) return solve_pressure_graph(x, singular, mixed, apply_pin);
   int rc;
   if (!mixed) {

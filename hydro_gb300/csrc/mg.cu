@@ -87,99 +87,136 @@ __global__ void __launch_bounds__(NT, PER ? 6 : 8) k_mg_smooth(Mesh m, const flo
 }
 
 // Dense inverse of the operator of a small coarsest level (n <= 64 cells),
-// one CTA, FP64 in shared memory: A = couplings (diagonal = their sum), cells
-// without couplings (inside a rigid box) decoupled as identity rows, the
-// constant mode of the others completed by 1/m (A + e e^T / m is SPD, and
-// for a zero-mean right-hand side its solution is the zero-mean solution
-// of A x = b); in-place Gauss-Jordan, symmetrised, stored in FP32.
+// Dense inverse of a small level (n <= kMgDense cells) by one CTA, FP32 in
+// shared memory (S: kDenseScratch floats).  A = couplings (diagonal = their
+// sum); cells without couplings (inside a rigid box) decoupled as identity
+// rows; the constant mode of the others completed by (d/m) e e^T, d their
+// mean diagonal and m their count: A + (d/m) e e^T is SPD with the constant
+// mode at eigenvalue d, inside A's own range (FP32 keeps the condition
+// number of the Laplacian), and for a zero-mean right-hand side its
+// solution is the zero-mean solution of A x = b.  Gauss-Jordan without
+// pivoting (SPD), one barrier per pivot: the thread owning slot 64 i + j
+// updates element (i, j), and the next pivot row and column are published
+// through double buffers as they are written.  The result is symmetrised.
+// Element ownership does not depend on the thread count, nor does the
+// result.
 constexpr int kMgDense = (int)kMgCoarseTarget;
+static_assert(kMgDense == 64, "slot layout: 64 columns");
+constexpr int kDenseScratch = kMgDense * kMgDense + 5 * kMgDense + 4;
 template <int DIM>
-__global__ void __launch_bounds__(256) k_mg_coarse_inv(Mesh m, const float* kf, float* P) {
-  __shared__ double A[kMgDense][kMgDense];
-  __shared__ int iso[kMgDense];
-  __shared__ int niso;
+__device__ void dense_inverse(const Mesh& m, const float* kf, float* P, float* S) {
+  constexpr int K = kMgDense;
+  float* A = S;                                       // [K][K]
+  float* rowb = A + K * K;                            // [2][K]
+  float* colb = rowb + 2 * K;                         // [2][K]
+  int* iso = reinterpret_cast<int*>(colb + 2 * K);    // [K]
+  float* alpha = reinterpret_cast<float*>(iso + K);   // [1]
   const int n = (int)m.nc, tid = threadIdx.x, nt = blockDim.x;
-  for (int q = tid; q < kMgDense * kMgDense; q += nt) A[q / kMgDense][q % kMgDense] = 0.;
-  if (tid == 0) niso = 0;
+  const int slots = n * K;  // rows 0..n-1 of the slot grid
+  for (int q = tid; q < slots; q += nt) A[q] = 0.f;
   __syncthreads();
   for (int c = tid; c < n; c += nt) {
     int id[3];
     id[0] = c % m.n[0];
     id[1] = (c / m.n[0]) % m.n[1];
     id[2] = DIM == 3 ? c / (m.n[0] * m.n[1]) : 0;
-    double dg = 0.;
+    float dg = 0.f;
     for (int d = 0; d < DIM; ++d) {
       const long long s = cell_stride(m, d);
       const long long fl = face_id(m, d, id[0], id[1], id[2]);
       if (has_lo(m, d, id[d], c, s)) {
-        const double k = kf[fl];
+        const float k = kf[fl];
         dg += k;
-        A[c][nb_lo(m, d, id[d], c, s)] -= k;
+        A[c * K + (int)nb_lo(m, d, id[d], c, s)] -= k;
       }
       if (has_hi(m, d, id[d], c, s)) {
-        const double k = kf[fl + face_stride(m, d)];
+        const float k = kf[fl + face_stride(m, d)];
         dg += k;
-        A[c][nb_hi(m, d, id[d], c, s)] -= k;
+        A[c * K + (int)nb_hi(m, d, id[d], c, s)] -= k;
       }
     }
-    A[c][c] += dg;
-    iso[c] = dg > 0. ? 0 : 1;
-    if (iso[c]) atomicAdd(&niso, 1);
+    A[c * K + c] += dg;
+    iso[c] = dg > 0.f ? 0 : 1;
   }
   __syncthreads();
-  const double rm = 1. / (double)(n - niso > 0 ? n - niso : 1);
-  for (int q = tid; q < n * n; q += nt) {
-    const int i = q / n, j = q % n;
-    if (iso[i] || iso[j]) A[i][j] = (i == j) ? 1. : 0.;
-    else A[i][j] += rm;
+  if (tid < 32) {
+    float sd = 0.f;
+    int cnt = 0;
+    for (int c = tid; c < n; c += 32)
+      if (!iso[c]) {
+        sd += A[c * K + c];
+        ++cnt;
+      }
+    sd = warp_sum(sd);
+    cnt = __reduce_add_sync(0xffffffffu, cnt);
+    if (tid == 0) alpha[0] = cnt > 0 ? sd / (float)cnt / (float)cnt : 0.f;
+  }
+  __syncthreads();
+  const float al = alpha[0];
+  for (int q = tid; q < slots; q += nt) {
+    const int i = q >> 6, j = q & (K - 1);
+    if (j >= n) continue;
+    float a;
+    if (iso[i] || iso[j]) a = i == j ? 1.f : 0.f;
+    else a = A[q] + al;
+    A[q] = a;
+    if (i == 0) rowb[j] = a;
+    if (j == 0) colb[i] = a;
   }
   __syncthreads();
   for (int k = 0; k < n; ++k) {
-    const double piv = A[k][k];
-    const double ip = fabs(piv) > 1e-300 ? 1. / piv : 0.;
-    __syncthreads();
-    for (int j = tid; j < n; j += nt) A[k][j] = (j == k) ? ip : A[k][j] * ip;
-    __syncthreads();
-    for (int q = tid; q < n * n; q += nt) {
-      const int i = q / n, j = q % n;
-      if (i == k) continue;
-      const double f = A[i][k];
-      if (j == k) continue;
-      A[i][j] -= f * A[k][j];
+    const float* rk = rowb + (k & 1) * K;
+    const float* ck = colb + (k & 1) * K;
+    float* rn = rowb + ((k + 1) & 1) * K;
+    float* cn = colb + ((k + 1) & 1) * K;
+    const float piv = rk[k];
+    const float ip = fabsf(piv) > 1e-30f ? 1.f / piv : 0.f;
+    for (int q = tid; q < slots; q += nt) {
+      const int i = q >> 6, j = q & (K - 1);
+      if (j >= n) continue;
+      float a = A[q];
+      if (i == k) a = j == k ? ip : a * ip;
+      else if (j == k) a = -a * ip;
+      else a = fmaf(-ck[i] * ip, rk[j], a);
+      A[q] = a;
+      if (i == k + 1) rn[j] = a;
+      if (j == k + 1) cn[i] = a;
     }
-    __syncthreads();
-    for (int i = tid; i < n; i += nt)
-      if (i != k) A[i][k] = -A[i][k] * A[k][k];
     __syncthreads();
   }
   for (int q = tid; q < n * n; q += nt) {
     const int i = q / n, j = q % n;
-    P[q] = (float)(0.5 * (A[i][j] + A[j][i]));
+    P[q] = 0.5f * (A[i * K + j] + A[j * K + i]);
   }
 }
 
-// Coarse couplings: 1/2 of the sum of the fine couplings of each coarse face
-// (zero on boundary faces; across a periodic end the coarse face joins the
-// last and first coarse cells like the fine one).
 template <int DIM>
-__global__ void k_mg_coarsen(Mesh fm, Mesh cm, const float* fkf, float* ckf, int kch) {
-  pdl_wait();
-  pdl_trigger();
-  CELL_LOOP_BEGIN(cm, kch)
+__global__ void __launch_bounds__(256) k_mg_coarse_inv(Mesh m, const float* kf, float* P) {
+  __shared__ float S[kDenseScratch];
+  dense_inverse<DIM>(m, kf, P, S);
+}
+
+// Coarse couplings of coarse cell c at I: 1/2 of the sum of the fine
+// couplings of each coarse face (zero on boundary faces; across a periodic
+// end the coarse face joins the last and first coarse cells like the fine
+// one).
+template <int DIM>
+__device__ __forceinline__ void coarsen_cell(const Mesh& fm, const Mesh& cm, const float* fkf,
+                                             float* ckf, const int* I, long long c) {
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
-    long long cf = face_id(cm, d, X.i[0], X.i[1], X.i[2]);
+    long long cf = face_id(cm, d, I[0], I[1], I[2]);
     int e1 = (d + 1) % DIM, e2 = (d + 2) % DIM;
-    // fine faces of the coarse face at coarse index I along d: index 2I
-    // along d, 2I' and 2I'+1 across
-    auto fsum = [&](int I) {
+    // fine faces of the coarse face at coarse index J along d: index 2J
+    // along d, 2J' and 2J'+1 across
+    auto fsum = [&](int J) {
       float sum = 0.f;
 #pragma unroll
       for (int a = 0; a < 2; ++a) {
 #pragma unroll
         for (int bq = 0; bq < (DIM == 3 ? 2 : 1); ++bq) {
-          int fi[3] = {2 * X.i[0], 2 * X.i[1], 2 * X.i[2]};
-          fi[d] = 2 * I;
+          int fi[3] = {2 * I[0], 2 * I[1], 2 * I[2]};
+          fi[d] = 2 * J;
           fi[e1] += a;
           if (DIM == 3) fi[e2] += bq;
           sum += fkf[face_id(fm, d, fi[0], fi[1], DIM == 3 ? fi[2] : 0)];
@@ -187,11 +224,31 @@ __global__ void k_mg_coarsen(Mesh fm, Mesh cm, const float* fkf, float* ckf, int
       }
       return sum;
     };
-    ckf[cf] = has_lo(cm, d, X.i[d], X.c, cell_stride(cm, d)) ? 0.5f * fsum(X.i[d]) : 0.f;
-    if (X.i[d] == cm.n[d] - 1)
-      ckf[cf + face_stride(cm, d)] = cm.per[d] ? 0.5f * fsum(X.i[d] + 1) : 0.f;
+    ckf[cf] = has_lo(cm, d, I[d], c, cell_stride(cm, d)) ? 0.5f * fsum(I[d]) : 0.f;
+    if (I[d] == cm.n[d] - 1)
+      ckf[cf + face_stride(cm, d)] = cm.per[d] ? 0.5f * fsum(I[d] + 1) : 0.f;
   }
+}
+
+template <int DIM>
+__global__ void k_mg_coarsen(Mesh fm, Mesh cm, const float* fkf, float* ckf, int kch) {
+  pdl_wait();
+  pdl_trigger();
+  CELL_LOOP_BEGIN(cm, kch)
+  coarsen_cell<DIM>(fm, cm, fkf, ckf, X.i, X.c);
   CELL_LOOP_END
+}
+
+// Diagonal of a coarse level's cell at I: the sum of its face couplings.
+template <int DIM>
+__device__ __forceinline__ float diag_cell(const Mesh& m, const float* kf, const int* I) {
+  float s = 0.f;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    long long fl = face_id(m, d, I[0], I[1], I[2]);
+    s += kf[fl] + kf[fl + face_stride(m, d)];
+  }
+  return s;
 }
 
 template <int DIM>
@@ -199,12 +256,7 @@ __global__ void k_mg_diag(Mesh m, const float* kf, float* dg, float* idg, int kc
   pdl_wait();
   pdl_trigger();
   CELL_LOOP_BEGIN(m, kch)
-  float s = 0.f;
-#pragma unroll
-  for (int d = 0; d < DIM; ++d) {
-    long long fl = face_id(m, d, X.i[0], X.i[1], X.i[2]);
-    s += kf[fl] + kf[fl + face_stride(m, d)];
-  }
+  const float s = diag_cell<DIM>(m, kf, X.i);
   dg[X.c] = s;
   idg[X.c] = s > 0.f ? 1.f / s : 0.f;
   CELL_LOOP_END
@@ -1101,9 +1153,10 @@ __global__ void k_accumulate_blk(Fast0 f, double* __restrict__ x, const float* _
 // result of level `top` pass through its global arrays).
 struct CtaPressure {
   Mesh m;
-  const double *kf, *dg, *f;  // FP64 couplings, diagonal, right-hand side
+  const double *kf, *f;       // FP64 couplings, right-hand side
+  double* dg;                 // FP64 diagonal (set up by the launch)
   double *x, *r;              // correction (out), FP64 residual
-  const float *kf32, *dg32;   // FP32 level-0 operator
+  float *kf32, *dg32, *idg32; // FP32 level-0 operator (set up by the launch)
   float *x32, *r32, *z32, *p, *pb, *Ap;
   long long pin;
   int singular, limit, graph;
@@ -1116,6 +1169,10 @@ struct CtaPressure {
   const float *gkf[kMgMaxLevels], *gidg[kMgMaxLevels];
   float *gx[kMgMaxLevels], *gb[kMgMaxLevels];
   int nsweep;
+  // the set-up's outputs: couplings and inverse diagonal of every level
+  // (level 0: kf32, idg32) and the dense coarsest inverse (null: none)
+  float *lkf[kMgMaxLevels], *lidg[kMgMaxLevels];
+  float* cinv;
   DevScalars* ds;
 };
 
@@ -1151,6 +1208,68 @@ __device__ double grp_sum(double v, double* sd, const ClusterG& g) {
 __device__ bool grp_lead(const CtaG&) { return true; }
 __device__ bool grp_lead(const ClusterG&) {
   return cooperative_groups::this_cluster().block_rank() == 0;
+}
+
+__device__ __forceinline__ const Mesh& lvl_mesh(const CtaPressure& P, int l) {
+  return l < P.top ? P.gm[l] : P.blk.m[l - P.top];
+}
+
+// The per-solve set-up that the grid form launches as separate kernels
+// (k_diag, then k_mg_coarsen / k_mg_diag per level and k_mg_coarse_inv),
+// with the same arithmetic: level 0's FP32 couplings and its FP64 / FP32
+// diagonals (the pinned row an identity row), every coarser level's
+// couplings and inverse diagonal (level l coarsened while level l - 1's
+// diagonal is formed, one barrier per level), and the dense inverse of the
+// coarsest level by CTA 0 with its dynamic shared memory as scratch (the
+// levels are staged there afterwards).  Ends with a group barrier.
+template <int DIM, class G>
+__device__ void grp_setup(const CtaPressure& P, float* sm, const G& g) {
+  const Mesh& m = P.m;
+  const int tid = g.rank(), nt = g.size();
+  const int nf = (int)m.nf, n = (int)m.nc;
+  for (int f = tid; f < nf; f += nt) P.kf32[f] = d2f(P.kf[f]);
+  for (int c = tid; c < n; c += nt) {
+    int id[3];
+    blk_ijk<DIM>(m, c, id);
+    double s = 0.;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const long long fl = face_id(m, d, id[0], id[1], id[2]);
+      if (id[d] > 0) s += P.kf[fl];
+      if (id[d] < m.n[d] - 1) s += P.kf[fl + face_stride(m, d)];
+    }
+    if (c == P.pin) s = 1.;
+    P.dg[c] = s;
+    const float s32 = d2f(s);
+    P.dg32[c] = s32;
+    P.idg32[c] = 1.f / s32;
+  }
+  g.sync();
+  for (int l = 1; l <= P.nl; ++l) {
+    if (l < P.nl) {
+      const Mesh& fm = lvl_mesh(P, l - 1);
+      const Mesh& cm = lvl_mesh(P, l);
+      const int nc = (int)cm.nc;
+      for (int c = tid; c < nc; c += nt) {
+        int I[3];
+        blk_ijk<DIM>(cm, c, I);
+        coarsen_cell<DIM>(fm, cm, P.lkf[l - 1], P.lkf[l], I, c);
+      }
+    }
+    if (l >= 2) {
+      const Mesh& dm = lvl_mesh(P, l - 1);
+      const int nc = (int)dm.nc;
+      for (int c = tid; c < nc; c += nt) {
+        int I[3];
+        blk_ijk<DIM>(dm, c, I);
+        const float s = diag_cell<DIM>(dm, P.lkf[l - 1], I);
+        P.lidg[l - 1][c] = s > 0.f ? 1.f / s : 0.f;
+      }
+    }
+    if (l == P.nl && P.cinv && grp_lead(g))
+      dense_inverse<DIM>(lvl_mesh(P, P.nl - 1), P.lkf[P.nl - 1], P.cinv, sm);
+    g.sync();
+  }
 }
 
 // z = M^-1 r by the group: the global levels swept and restricted by all,
@@ -1325,6 +1444,7 @@ __global__ void __launch_bounds__(kBlkThreads)
   const G g;
   const Mesh& m = P.m;
   const int n = (int)m.nc, tid = g.rank(), nt = g.size();
+  grp_setup<DIM>(P, sm, g);
   if (grp_lead(g)) cta_stage_levels(P.blk, sm, &V);
   double mean = 0.;
   if (P.singular) {
@@ -1567,6 +1687,12 @@ cudaError_t mg_prepare(MgWork& mg) {
     const long long n = mg.lev[mg.nlev - 1].m.nc;
     mg.smem_cinv_off = mg.smem_bytes / (int)sizeof(float);
     mg.smem_bytes += (int)(n * n * sizeof(float));
+  }
+  if (mg.cta && mg.cdense) {
+    // the one-group solve forms the dense inverse in its dynamic shared
+    // memory before staging the levels there
+    const int scratch = (int)(kDenseScratch * sizeof(float));
+    if (mg.smem_bytes < scratch) mg.smem_bytes = scratch;
   }
   if (mg.nlev > 0 && mg.top < mg.nlev) {
     // (the kernels' static shared memory adds a few KB)
@@ -1844,6 +1970,12 @@ cudaError_t cta_pressure(const Mesh& m, const double* kf, const double* f, doubl
       B.ok[q] = off; off += f4;
     }
   }
+  for (int l = 0; l < mg.nlev; ++l) {
+    P.lkf[l] = l == 0 ? w.kf32 : mg.lev[l].kf;
+    P.lidg[l] = l == 0 ? w.idg32 : mg.lev[l].idg;
+  }
+  P.idg32 = w.idg32;
+  P.cinv = mg.cdense ? mg.cinv : nullptr;
   P.ds = w.ds;
   const int smem = mg.smem_bytes;
   if (cluster == 1) {
