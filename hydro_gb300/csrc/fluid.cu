@@ -563,16 +563,21 @@ __device__ float grp_max(float v, float* red, const CtaG&) {
   __syncthreads();
   return r;
 }
+// Cluster-wide: lane q of the first warp reads CTA q's maximum from its
+// shared memory; the warp's maximum goes to the CTA's threads through red[32].
 __device__ float grp_max(float v, float* red, const ClusterG&) {
   const float b = grp_max(v, red, CtaG());
   if (threadIdx.x == 0) red[33] = b;
   auto cl = cooperative_groups::this_cluster();
   cl.sync();
-  float t = 0.f;
-  const int nb = (int)cl.num_blocks();
-  for (int q = 0; q < nb; ++q) t = fmaxf(t, *cl.map_shared_rank(&red[33], q));
-  cl.sync();  // before red[33] is written again
-  return t;
+  if (threadIdx.x < 32) {
+    const int nb = (int)cl.num_blocks(), lane = threadIdx.x;
+    float t = lane < nb ? *cl.map_shared_rank(&red[33], lane) : 0.f;
+    t = warp_max(t);
+    if (lane == 0) red[32] = t;
+  }
+  cl.sync();  // red[32] written; every red[33] read before it is written again
+  return red[32];
 }
 
 template <int DIM, class G>

@@ -342,6 +342,33 @@ __device__ __forceinline__ void blk_ijk(const Mesh& m, int c, int* id) {
   id[2] = DIM == 3 ? r / m.n[1] : 0;
 }
 
+// Index constants of a level held in registers for a pass (the level's
+// Mesh may sit in shared memory beside the arrays the pass writes, and
+// would be re-read after every store otherwise): 32-bit, a level of a
+// one-group solve has fewer than 2^31 faces.
+template <int DIM>
+struct LvIx {
+  // cells, and the offsets of the y and z face blocks; the face layout is
+  // fixed by the cell counts (fnx = nx + (d == 0), fny = ny + (d == 1))
+  int n[3], fo1, fo2;
+  __device__ __forceinline__ explicit LvIx(const Mesh& m) {
+    n[0] = m.n[0];
+    n[1] = m.n[1];
+    n[2] = DIM == 3 ? m.n[2] : 1;
+    fo1 = (int)m.fofs[1];
+    fo2 = DIM == 3 ? (int)m.fofs[2] : 0;
+  }
+  // stride between neighbouring cells along d (= between its two faces)
+  __device__ __forceinline__ int cs(int d) const { return d == 0 ? 1 : (d == 1 ? n[0] : n[0] * n[1]); }
+  __device__ __forceinline__ int fs(int d) const {
+    return d == 0 ? 1 : (d == 1 ? n[0] : n[0] * n[1]);
+  }
+  __device__ __forceinline__ int face(int d, const int* id) const {
+    const int fx = n[0] + (d == 0), fy = n[1] + (d == 1);
+    return (d == 0 ? 0 : d == 1 ? fo1 : fo2) + id[0] + fx * (id[1] + fy * id[2]);
+  }
+};
+
 // One red-black half-sweep by the group: slot t of row (j, k) is the cell
 // i = 2t + ((j + k + color) & 1); the cells of one colour are independent,
 // so the order does not change the result.
@@ -353,8 +380,10 @@ __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const
   // flight: a CTA alone on a level of tens of thousands of cells is
   // latency-bound otherwise
   constexpr int U = DIM == 3 ? 2 : 4;
-  const int hx = (m.n[0] + 1) >> 1;
-  const int n = hx * m.n[1] * (DIM == 3 ? m.n[2] : 1);
+  const LvIx<DIM> L(m);
+  const int pn = (int)pin;
+  const int hx = (L.n[0] + 1) >> 1;
+  const int n = hx * L.n[1] * L.n[2];
   const int step = g.size();
   for (int q0 = g.rank(); q0 < n; q0 += U * step) {
     float val[U];
@@ -367,13 +396,13 @@ __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const
       if (q >= n) continue;
       const int row = q / hx;
       int id[3];
-      id[1] = DIM == 3 ? row % m.n[1] : row;
-      id[2] = DIM == 3 ? row / m.n[1] : 0;
+      id[1] = DIM == 3 ? row % L.n[1] : row;
+      id[2] = DIM == 3 ? row / L.n[1] : 0;
       id[0] = 2 * (q - row * hx) + ((id[1] + id[2] + color) & 1);
-      if (id[0] >= m.n[0]) continue;
-      const int c = id[0] + m.n[0] * row;
+      if (id[0] >= L.n[0]) continue;
+      const int c = id[0] + L.n[0] * row;
       cc[u] = c;
-      if (c == pin) {
+      if (c == pn) {
         val[u] = b[c];
         continue;
       }
@@ -381,13 +410,18 @@ __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const
       if (!zero) {
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
-          int s = (int)cell_stride(m, d);
-          int fl = (int)face_id(m, d, id[0], id[1], id[2]);
-          const int cl = nb_lo_p<PER>(m, d, id[d], c, s);
-          const int ch = nb_hi_p<PER>(m, d, id[d], c, s);
-          if (has_lo_p<PER>(m, d, id[d], c, s) && cl != pin) acc = fmaf(kf[fl], x[cl], acc);
-          if (has_hi_p<PER>(m, d, id[d], c, s) && ch != pin)
-            acc = fmaf(kf[fl + (int)face_stride(m, d)], x[ch], acc);
+          const int s = L.cs(d);
+          const int fl = L.face(d, id);
+          if (PER) {
+            const int cl = nb_lo_p<PER>(m, d, id[d], c, s);
+            const int ch = nb_hi_p<PER>(m, d, id[d], c, s);
+            if (has_lo_p<PER>(m, d, id[d], c, s) && cl != pn) acc = fmaf(kf[fl], x[cl], acc);
+            if (has_hi_p<PER>(m, d, id[d], c, s) && ch != pn)
+              acc = fmaf(kf[fl + L.fs(d)], x[ch], acc);
+          } else {
+            if (id[d] > 0 && c - s != pn) acc = fmaf(kf[fl], x[c - s], acc);
+            if (id[d] < L.n[d] - 1 && c + s != pn) acc = fmaf(kf[fl + L.fs(d)], x[c + s], acc);
+          }
         }
       }
       val[u] = acc * idg[c];
@@ -404,6 +438,9 @@ template <int DIM, bool PER, class G = CtaG>
 __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, const float* b,
                              const float* x, float* cb, long long pin, const G& g = G()) {
   constexpr int U = DIM == 3 ? 2 : 4;  // coarse cells per thread per pass, loads first
+  const LvIx<DIM> L(fm);
+  const int cn0 = cm.n[0], cn1 = cm.n[1];
+  const int pn = (int)pin;
   const int n = (int)cm.nc;
   const int step = g.size();
   for (int C0 = g.rank(); C0 < n; C0 += U * step) {
@@ -414,7 +451,10 @@ __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, co
       sums[u] = 0.f;
       if (C >= n) continue;
       int I[3];
-      blk_ijk<DIM>(cm, C, I);
+      I[0] = C % cn0;
+      const int r = C / cn0;
+      I[1] = DIM == 3 ? r % cn1 : r;
+      I[2] = DIM == 3 ? r / cn1 : 0;
       float sum = 0.f;
 #pragma unroll
       for (int ck = 0; ck < (DIM == 3 ? 2 : 1); ++ck)
@@ -423,22 +463,27 @@ __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, co
 #pragma unroll
           for (int ci = 0; ci < 2; ++ci) {
             int id[3] = {2 * I[0] + ci, 2 * I[1] + cj, DIM == 3 ? 2 * I[2] + ck : 0};
-            int c = (int)cell_id(fm, id[0], id[1], id[2]);
+            const int c = id[0] + L.n[0] * (id[1] + L.n[1] * id[2]);
             float r;
-            if (c == pin) {
+            if (c == pn) {
               r = b[c] - x[c];
             } else {
               float dg = 0.f, off = 0.f;
 #pragma unroll
               for (int d = 0; d < DIM; ++d) {
-                int s = (int)cell_stride(fm, d);
-                int fl = (int)face_id(fm, d, id[0], id[1], id[2]);
-                float klo = kf[fl], khi = kf[fl + (int)face_stride(fm, d)];
+                const int s = L.cs(d);
+                const int fl = L.face(d, id);
+                float klo = kf[fl], khi = kf[fl + L.fs(d)];
                 dg += klo + khi;
-                const int cl = nb_lo_p<PER>(fm, d, id[d], c, s);
-                const int ch = nb_hi_p<PER>(fm, d, id[d], c, s);
-                if (has_lo_p<PER>(fm, d, id[d], c, s) && cl != pin) off = fmaf(klo, x[cl], off);
-                if (has_hi_p<PER>(fm, d, id[d], c, s) && ch != pin) off = fmaf(khi, x[ch], off);
+                if (PER) {
+                  const int cl = nb_lo_p<PER>(fm, d, id[d], c, s);
+                  const int ch = nb_hi_p<PER>(fm, d, id[d], c, s);
+                  if (has_lo_p<PER>(fm, d, id[d], c, s) && cl != pn) off = fmaf(klo, x[cl], off);
+                  if (has_hi_p<PER>(fm, d, id[d], c, s) && ch != pn) off = fmaf(khi, x[ch], off);
+                } else {
+                  if (id[d] > 0 && c - s != pn) off = fmaf(klo, x[c - s], off);
+                  if (id[d] < L.n[d] - 1 && c + s != pn) off = fmaf(khi, x[c + s], off);
+                }
               }
               r = b[c] - (dg * x[c] - off);
             }
@@ -539,7 +584,7 @@ __device__ void cta_vcycle(const CtaLevels& B, float* red) {
     long long lp = l == 0 ? B.pin : -1;
     float* x = B.x[l];
     const float* cx = B.x[l + 1];
-    const int nc = (int)m.nc;
+    const int nc = (int)m.nc, n0 = m.n[0], n1 = m.n[1], cn0 = cm.n[0], cn1 = cm.n[1];
     for (int c0 = tid; c0 < nc; c0 += 4 * nt) {
       float v[4];
 #pragma unroll
@@ -547,9 +592,9 @@ __device__ void cta_vcycle(const CtaLevels& B, float* red) {
         const int c = c0 + u * nt;
         v[u] = 0.f;
         if (c >= nc) continue;
-        int id[3];
-        blk_ijk<DIM>(m, c, id);
-        v[u] = x[c] + cx[(int)cell_id(cm, id[0] >> 1, id[1] >> 1, id[2] >> 1)];
+        const int i = c % n0, r = c / n0;
+        const int j = DIM == 3 ? r % n1 : r, k = DIM == 3 ? r / n1 : 0;
+        v[u] = x[c] + cx[(i >> 1) + cn0 * ((j >> 1) + cn1 * (k >> 1))];
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u)
@@ -565,16 +610,29 @@ __device__ void cta_vcycle(const CtaLevels& B, float* red) {
 
 // The levels from `top` down, staged into shared memory (MgBlock offsets),
 // as a CtaLevels set (built by thread 0; the caller synchronises).
-__device__ void cta_stage_levels(const MgBlock& B, float* sm, CtaLevels* V, int first = 0) {
+// n floats from global to shared memory by the CTA, 4 loads per thread in
+// flight
+__device__ __forceinline__ void cta_copy(float* dst, const float* src, int n) {
   const int tid = threadIdx.x, nt = blockDim.x;
+  for (int q0 = tid; q0 < n; q0 += 4 * nt) {
+    float v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = q0 + u * nt < n ? src[q0 + u * nt] : 0.f;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (q0 + u * nt < n) dst[q0 + u * nt] = v[u];
+  }
+}
+
+__device__ void cta_stage_levels(const MgBlock& B, float* sm, CtaLevels* V, int first = 0) {
+  const int tid = threadIdx.x;
   for (int l = 0; l < B.nl; ++l) {
-    const int nf = (int)B.m[l].nf, nc = (int)B.m[l].nc;
-    for (int q = tid; q < nf; q += nt) sm[B.ok[l] + q] = B.kf[l][q];
-    for (int q = tid; q < nc; q += nt) sm[B.oi[l] + q] = B.idg[l][q];
+    cta_copy(sm + B.ok[l], B.kf[l], (int)B.m[l].nf);
+    cta_copy(sm + B.oi[l], B.idg[l], (int)B.m[l].nc);
   }
   if (B.cinv) {
     const int n = (int)B.m[B.nl - 1].nc;
-    for (int q = tid; q < n * n; q += nt) sm[B.oc + q] = B.cinv[q];
+    cta_copy(sm + B.oc, B.cinv, n * n);
   }
   if (tid == 0) {
     V->nl = first + B.nl;
@@ -1193,17 +1251,23 @@ __device__ double cta_sum(double v, double* sd) {
   return r;
 }
 __device__ double grp_sum(double v, double* sd, const CtaG&) { return cta_sum(v, sd); }
-// Cluster-wide: every CTA's sum read from its shared memory in rank order.
+// Cluster-wide: every CTA's sum read from its shared memory (lane q of the
+// first warp reads CTA q's, all in flight at once) and added in rank order
+// by lane 0, then passed to the CTA's threads through sd[32].
 __device__ double grp_sum(double v, double* sd, const ClusterG& g) {
   const double b = cta_sum(v, sd);
   if (threadIdx.x == 0) sd[33] = b;
   auto cl = cooperative_groups::this_cluster();
   cl.sync();
-  double t = 0.;
-  const int nb = (int)cl.num_blocks();
-  for (int q = 0; q < nb; ++q) t += *cl.map_shared_rank(&sd[33], q);
-  cl.sync();  // before sd[33] is written again
-  return t;
+  if (threadIdx.x < 32) {
+    const int nb = (int)cl.num_blocks(), lane = threadIdx.x;
+    const double mine = lane < nb ? *cl.map_shared_rank(&sd[33], lane) : 0.;
+    double t = 0.;
+    for (int q = 0; q < nb; ++q) t += __shfl_sync(0xffffffffu, mine, q);
+    if (lane == 0) sd[32] = t;
+  }
+  cl.sync();  // sd[32] written; every sd[33] read before it is written again
+  return sd[32];
 }
 __device__ bool grp_lead(const CtaG&) { return true; }
 __device__ bool grp_lead(const ClusterG&) {
@@ -1227,7 +1291,14 @@ __device__ void grp_setup(const CtaPressure& P, float* sm, const G& g) {
   const Mesh& m = P.m;
   const int tid = g.rank(), nt = g.size();
   const int nf = (int)m.nf, n = (int)m.nc;
-  for (int f = tid; f < nf; f += nt) P.kf32[f] = d2f(P.kf[f]);
+  for (int f0 = tid; f0 < nf; f0 += 4 * nt) {
+    double v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = f0 + u * nt < nf ? P.kf[f0 + u * nt] : 0.;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (f0 + u * nt < nf) P.kf32[f0 + u * nt] = d2f(v[u]);
+  }
   for (int c = tid; c < n; c += nt) {
     int id[3];
     blk_ijk<DIM>(m, c, id);
@@ -1326,11 +1397,18 @@ __device__ int grp_mgcg(const CtaPressure& P, CtaLevels& V, float* sm, float* re
   const Mesh& m = P.m;
   const int n = (int)m.nc, tid = g.rank(), nt = g.size();
   double s = 0.;
-  for (int c = tid; c < n; c += nt) {
-    const double v = P.r[c];
-    P.r32[c] = d2f(v);
-    P.x32[c] = 0.f;
-    s += v * v;
+  for (int c0 = tid; c0 < n; c0 += 4 * nt) {
+    double v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = c0 + u * nt < n ? P.r[c0 + u * nt] : 0.;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int c = c0 + u * nt;
+      if (c >= n) continue;
+      P.r32[c] = d2f(v[u]);
+      P.x32[c] = 0.f;
+      s += v[u] * v[u];
+    }
   }
   const double rr0 = grp_sum(s, sd, g);
   if (rr0 == 0. || lim <= 0) return 0;
@@ -1516,7 +1594,17 @@ __global__ void __launch_bounds__(kBlkThreads)
     if (total >= P.limit || outer >= 50) break;
     const double t = fmax(0.5 * P.tol * sqrt(ff / rr), P.inner_min);
     total += grp_mgcg<DIM>(P, V, sm, red, sd, t, P.limit - total, g);
-    for (int c = tid; c < n; c += nt) P.x[c] += (double)P.x32[c];
+    for (int c0 = tid; c0 < n; c0 += 4 * nt) {
+      double v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int c = c0 + u * nt;
+        v[u] = c < n ? P.x[c] + (double)P.x32[c] : 0.;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (c0 + u * nt < n) P.x[c0 + u * nt] = v[u];
+    }
     ++outer;
     g.sync();
   }
