@@ -156,6 +156,9 @@ struct CtaG {
 };
 struct ClusterG {
   int r, n;
+  // parity of the cluster-wide reductions so far (their shared-memory
+  // slots are double-buffered); every thread runs the same sequence
+  mutable int par = 0;
   __device__ ClusterG()
       : r((int)(cooperative_groups::this_cluster().block_rank() * blockDim.x + threadIdx.x)),
         n((int)(cooperative_groups::this_cluster().num_blocks() * blockDim.x)) {}

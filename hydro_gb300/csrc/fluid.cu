@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(NT) k_mom_sweep32(Mesh m, float omega, double 
 // so the result does not depend on the CTA's order), up to `limit` sweeps.
 // For small cases run many at once: each takes one SM instead of queueing
 // two launches per sweep.
-// Group-wide largest correction, the same in every thread (red: 34 floats).
+// Group-wide largest correction, the same in every thread (red: 38 floats).
 __device__ float grp_max(float v, float* red, const CtaG&) {
   const int tid = threadIdx.x, nt = blockDim.x;
   v = warp_max(v);
@@ -563,21 +563,33 @@ __device__ float grp_max(float v, float* red, const CtaG&) {
   __syncthreads();
   return r;
 }
-// Cluster-wide: lane q of the first warp reads CTA q's maximum from its
-// shared memory; the warp's maximum goes to the CTA's threads through red[32].
-__device__ float grp_max(float v, float* red, const ClusterG&) {
-  const float b = grp_max(v, red, CtaG());
-  if (threadIdx.x == 0) red[33] = b;
+// Cluster-wide (red: >= 38 floats): each CTA's maximum goes to red[34 +
+// parity]; after one cluster barrier lane q of the first warp reads CTA q's
+// and the warp's maximum reaches the CTA's threads through red[36 +
+// parity] (slots alternate between calls, as for the FP64 sums of the
+// pressure solve).
+__device__ float grp_max(float v, float* red, const ClusterG& g) {
+  const int tid = threadIdx.x, lane = tid & 31, nw = (blockDim.x + 31) >> 5;
+  const int par = g.par;
+  g.par ^= 1;
+  v = warp_max(v);
+  if (lane == 0) red[tid >> 5] = v;
+  __syncthreads();
+  if (tid < 32) {
+    float w = lane < nw ? red[lane] : 0.f;
+    w = warp_max(w);
+    if (lane == 0) red[34 + par] = w;
+  }
   auto cl = cooperative_groups::this_cluster();
   cl.sync();
-  if (threadIdx.x < 32) {
-    const int nb = (int)cl.num_blocks(), lane = threadIdx.x;
-    float t = lane < nb ? *cl.map_shared_rank(&red[33], lane) : 0.f;
+  if (tid < 32) {
+    const int nb = (int)cl.num_blocks();
+    float t = lane < nb ? *cl.map_shared_rank(&red[34 + par], lane) : 0.f;
     t = warp_max(t);
-    if (lane == 0) red[32] = t;
+    if (lane == 0) red[36 + par] = t;
   }
-  cl.sync();  // red[32] written; every red[33] read before it is written again
-  return red[32];
+  __syncthreads();
+  return red[36 + par];
 }
 
 template <int DIM, class G>
@@ -586,7 +598,7 @@ __global__ void __launch_bounds__(1024) k_cta_mom_jacobi32(Mesh m, float omega, 
                                                            int limit, int graph,
                                                            DevScalars* ds) {
   constexpr bool kPerT = false;
-  __shared__ float red[34];
+  __shared__ float red[38];
   const G g;
   const int n = (int)m.nc, tid = g.rank(), nt = g.size();
   int sweeps = 0;

@@ -103,6 +103,62 @@ __global__ void __launch_bounds__(NT, PER ? 6 : 8) k_mg_smooth(Mesh m, const flo
 constexpr int kMgDense = (int)kMgCoarseTarget;
 static_assert(kMgDense == 64, "slot layout: 64 columns");
 constexpr int kDenseScratch = kMgDense * kMgDense + 5 * kMgDense + 4;
+__device__ __forceinline__ float dense_pivot_inv(float piv) {
+  return fabsf(piv) > 1e-30f ? 1.f / piv : 0.f;
+}
+// Element (i, j) after pivot step k (ip = 1 / pivot, cik and rkj: column k
+// and row k before the step).
+__device__ __forceinline__ float dense_update(float a, int i, int j, int k, float ip, float cik,
+                                              float rkj) {
+  if (i == k) return j == k ? ip : a * ip;
+  if (j == k) return -a * ip;
+  return fmaf(-cik * ip, rkj, a);
+}
+
+// The pivot steps of dense_inverse with the elements in registers: the
+// first 4096 / E threads take part, thread t owning slots t + s (4096 / E)
+// (one column j = t & 63, rows spaced 64 / E apart); A (slot layout) holds
+// the matrix before and after, rowb / colb publish row and column 0.
+template <int E>
+__device__ void dense_pivots_regs(float* A, float* rowb, float* colb, int n) {
+  constexpr int K = kMgDense, NT = K * K / E, RS = NT / K;
+  const int tid = threadIdx.x;
+  const bool in = tid < NT;
+  const int j = tid & (K - 1), i0 = tid >> 6;
+  float a[E];
+#pragma unroll
+  for (int t = 0; t < E; ++t) {
+    const int i = i0 + t * RS;
+    a[t] = in && i < n && j < n ? A[i * K + j] : 0.f;
+  }
+  for (int k = 0; k < n; ++k) {
+    const float* rk = rowb + (k & 1) * K;
+    const float* ck = colb + (k & 1) * K;
+    float* rn = rowb + ((k + 1) & 1) * K;
+    float* cn = colb + ((k + 1) & 1) * K;
+    if (in && j < n) {
+      const float ip = dense_pivot_inv(rk[k]);
+      const float rkj = rk[j];
+#pragma unroll
+      for (int t = 0; t < E; ++t) {
+        const int i = i0 + t * RS;
+        if (i >= n) continue;
+        const float v = dense_update(a[t], i, j, k, ip, ck[i], rkj);
+        a[t] = v;
+        if (i == k + 1) rn[j] = v;
+        if (j == k + 1) cn[i] = v;
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int t = 0; t < E; ++t) {
+    const int i = i0 + t * RS;
+    if (in && i < n && j < n) A[i * K + j] = a[t];
+  }
+  __syncthreads();
+}
+
 template <int DIM>
 __device__ void dense_inverse(const Mesh& m, const float* kf, float* P, float* S) {
   constexpr int K = kMgDense;
@@ -164,25 +220,27 @@ __device__ void dense_inverse(const Mesh& m, const float* kf, float* P, float* S
     if (j == 0) colb[i] = a;
   }
   __syncthreads();
-  for (int k = 0; k < n; ++k) {
-    const float* rk = rowb + (k & 1) * K;
-    const float* ck = colb + (k & 1) * K;
-    float* rn = rowb + ((k + 1) & 1) * K;
-    float* cn = colb + ((k + 1) & 1) * K;
-    const float piv = rk[k];
-    const float ip = fabsf(piv) > 1e-30f ? 1.f / piv : 0.f;
-    for (int q = tid; q < slots; q += nt) {
-      const int i = q >> 6, j = q & (K - 1);
-      if (j >= n) continue;
-      float a = A[q];
-      if (i == k) a = j == k ? ip : a * ip;
-      else if (j == k) a = -a * ip;
-      else a = fmaf(-ck[i] * ip, rk[j], a);
-      A[q] = a;
-      if (i == k + 1) rn[j] = a;
-      if (j == k + 1) cn[i] = a;
+  if (nt >= 512) {
+    dense_pivots_regs<8>(A, rowb, colb, n);
+  } else if (nt >= 256) {
+    dense_pivots_regs<16>(A, rowb, colb, n);
+  } else {
+    for (int k = 0; k < n; ++k) {
+      const float* rk = rowb + (k & 1) * K;
+      const float* ck = colb + (k & 1) * K;
+      float* rn = rowb + ((k + 1) & 1) * K;
+      float* cn = colb + ((k + 1) & 1) * K;
+      const float ip = dense_pivot_inv(rk[k]);
+      for (int q = tid; q < slots; q += nt) {
+        const int i = q >> 6, j = q & (K - 1);
+        if (j >= n) continue;
+        const float a = dense_update(A[q], i, j, k, ip, ck[i], rk[j]);
+        A[q] = a;
+        if (i == k + 1) rn[j] = a;
+        if (j == k + 1) cn[i] = a;
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
   for (int q = tid; q < n * n; q += nt) {
     const int i = q / n, j = q % n;
@@ -1251,23 +1309,36 @@ __device__ double cta_sum(double v, double* sd) {
   return r;
 }
 __device__ double grp_sum(double v, double* sd, const CtaG&) { return cta_sum(v, sd); }
-// Cluster-wide: every CTA's sum read from its shared memory (lane q of the
-// first warp reads CTA q's, all in flight at once) and added in rank order
-// by lane 0, then passed to the CTA's threads through sd[32].
+// Cluster-wide (sd: >= 38 doubles): each CTA's sum goes to sd[34 + parity];
+// after one cluster barrier lane q of the first warp reads CTA q's, all in
+// flight at once, lane 0 adds them in rank order and passes the total to
+// the CTA's threads through sd[36 + parity].  The slots alternate between
+// calls, so a slot is rewritten only after the next call's cluster (or CTA)
+// barrier, which every reader of its previous value has passed; the one
+// cluster barrier also orders the caller's earlier global stores.
 __device__ double grp_sum(double v, double* sd, const ClusterG& g) {
-  const double b = cta_sum(v, sd);
-  if (threadIdx.x == 0) sd[33] = b;
+  const int tid = threadIdx.x, lane = tid & 31, nw = (blockDim.x + 31) >> 5;
+  const int par = g.par;
+  g.par ^= 1;
+  v = warp_sum(v);
+  if (lane == 0) sd[tid >> 5] = v;
+  __syncthreads();
+  if (tid < 32) {
+    double t = lane < nw ? sd[lane] : 0.;
+    t = warp_sum(t);
+    if (lane == 0) sd[34 + par] = t;
+  }
   auto cl = cooperative_groups::this_cluster();
   cl.sync();
-  if (threadIdx.x < 32) {
-    const int nb = (int)cl.num_blocks(), lane = threadIdx.x;
-    const double mine = lane < nb ? *cl.map_shared_rank(&sd[33], lane) : 0.;
+  if (tid < 32) {
+    const int nb = (int)cl.num_blocks();
+    const double mine = lane < nb ? *cl.map_shared_rank(&sd[34 + par], lane) : 0.;
     double t = 0.;
     for (int q = 0; q < nb; ++q) t += __shfl_sync(0xffffffffu, mine, q);
-    if (lane == 0) sd[32] = t;
+    if (lane == 0) sd[36 + par] = t;
   }
-  cl.sync();  // sd[32] written; every sd[33] read before it is written again
-  return sd[32];
+  __syncthreads();
+  return sd[36 + par];
 }
 __device__ bool grp_lead(const CtaG&) { return true; }
 __device__ bool grp_lead(const ClusterG&) {
@@ -1517,7 +1588,7 @@ __global__ void __launch_bounds__(kBlkThreads)
     k_cta_pressure(const __grid_constant__ CtaPressure P) {
   extern __shared__ float sm[];
   __shared__ float red[32];
-  __shared__ double sd[34];
+  __shared__ double sd[38];
   __shared__ CtaLevels V;  // the staged levels (CTA 0)
   const G g;
   const Mesh& m = P.m;
