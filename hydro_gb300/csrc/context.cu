@@ -928,6 +928,9 @@ int hydro_gpu_create(const hydro_desc* desc, hydro_ctx** out) {
       return HYDRO_ERR_UNSUPPORTED;
     for (int d = 0; d < desc->dim && d < 3; ++d)
       if (desc->periodic[d]) return HYDRO_ERR_UNSUPPORTED;
+    long long cells = 1;
+    for (int d = 0; d < desc->dim && d < 3; ++d) cells *= desc->n[d];
+    if (cells >= (1LL << 24)) return HYDRO_ERR_UNSUPPORTED;  // one group's solve
   }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return HYDRO_ERR_NO_DEVICE;

@@ -400,6 +400,36 @@ __device__ __forceinline__ void blk_ijk(const Mesh& m, int c, int* id) {
   id[2] = DIM == 3 ? r / m.n[1] : 0;
 }
 
+// q / d (returned) and q % d (r) for 0 <= q < 2^24 and d >= 1, from rd =
+// 1 / d in FP32: q rd is within 1 of q / d there, so one integer correction
+// makes the quotient exact (a handful of instructions against a signed
+// division's few dozen, per cell of every pass).
+__device__ __forceinline__ int fdivmod(int q, int d, float rd, int& r) {
+  int t = __float2int_rz((float)q * rd);
+  int rem = q - t * d;
+  if (rem < 0) {
+    --t;
+    rem += d;
+  } else if (rem >= d) {
+    ++t;
+    rem -= d;
+  }
+  r = rem;
+  return t;
+}
+
+// (i, j, k) of cell c of an n0 x n1 [x n2] level (r0 = 1 / n0, r1 = 1 / n1).
+template <int DIM>
+__device__ __forceinline__ void blk_ijk(int n0, int n1, float r0, float r1, int c, int* id) {
+  const int row = fdivmod(c, n0, r0, id[0]);
+  if (DIM == 3) {
+    id[2] = fdivmod(row, n1, r1, id[1]);
+  } else {
+    id[1] = row;
+    id[2] = 0;
+  }
+}
+
 // Index constants of a level held in registers for a pass (the level's
 // Mesh may sit in shared memory beside the arrays the pass writes, and
 // would be re-read after every store otherwise): 32-bit, a level of a
@@ -439,10 +469,15 @@ __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const
   // latency-bound otherwise
   constexpr int U = DIM == 3 ? 2 : 4;
   const LvIx<DIM> L(m);
-  const int pn = (int)pin;
   const int hx = (L.n[0] + 1) >> 1;
   const int n = hx * L.n[1] * L.n[2];
+  // a thread without a cell (most of them on a small level) skips the
+  // pass, leaving the issue slots to those that have one; every thread
+  // meets the one barrier at the end
+  if (g.rank() < n) {
+  const int pn = (int)pin;
   const int step = g.size();
+  const float rhx = 1.f / (float)hx, rn1 = 1.f / (float)L.n[1];
   for (int q0 = g.rank(); q0 < n; q0 += U * step) {
     float val[U];
     int cc[U];
@@ -452,11 +487,15 @@ __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const
       cc[u] = -1;
       val[u] = 0.f;
       if (q >= n) continue;
-      const int row = q / hx;
-      int id[3];
-      id[1] = DIM == 3 ? row % L.n[1] : row;
-      id[2] = DIM == 3 ? row / L.n[1] : 0;
-      id[0] = 2 * (q - row * hx) + ((id[1] + id[2] + color) & 1);
+      int id[3], t;
+      const int row = fdivmod(q, hx, rhx, t);
+      if (DIM == 3) {
+        id[2] = fdivmod(row, L.n[1], rn1, id[1]);
+      } else {
+        id[1] = row;
+        id[2] = 0;
+      }
+      id[0] = 2 * t + ((id[1] + id[2] + color) & 1);
       if (id[0] >= L.n[0]) continue;
       const int c = id[0] + L.n[0] * row;
       cc[u] = c;
@@ -488,6 +527,7 @@ __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const
     for (int u = 0; u < U; ++u)
       if (cc[u] >= 0) x[cc[u]] = val[u];
   }
+  }
   g.sync();
 }
 
@@ -496,10 +536,12 @@ template <int DIM, bool PER, class G = CtaG>
 __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, const float* b,
                              const float* x, float* cb, long long pin, const G& g = G()) {
   constexpr int U = DIM == 3 ? 2 : 4;  // coarse cells per thread per pass, loads first
+  const int n = (int)cm.nc;
+  if (g.rank() < n) {  // (threads without a coarse cell skip to the barrier)
   const LvIx<DIM> L(fm);
   const int cn0 = cm.n[0], cn1 = cm.n[1];
+  const float rc0 = 1.f / (float)cn0, rc1 = 1.f / (float)cn1;
   const int pn = (int)pin;
-  const int n = (int)cm.nc;
   const int step = g.size();
   for (int C0 = g.rank(); C0 < n; C0 += U * step) {
     float sums[U];
@@ -509,10 +551,7 @@ __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, co
       sums[u] = 0.f;
       if (C >= n) continue;
       int I[3];
-      I[0] = C % cn0;
-      const int r = C / cn0;
-      I[1] = DIM == 3 ? r % cn1 : r;
-      I[2] = DIM == 3 ? r / cn1 : 0;
+      blk_ijk<DIM>(cn0, cn1, rc0, rc1, C, I);
       float sum = 0.f;
 #pragma unroll
       for (int ck = 0; ck < (DIM == 3 ? 2 : 1); ++ck)
@@ -552,6 +591,7 @@ __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, co
 #pragma unroll
     for (int u = 0; u < U; ++u)
       if (C0 + u * step < n) cb[C0 + u * step] = sums[u];
+  }
   }
   g.sync();
 }
@@ -643,6 +683,7 @@ __device__ void cta_vcycle(const CtaLevels& B, float* red) {
     float* x = B.x[l];
     const float* cx = B.x[l + 1];
     const int nc = (int)m.nc, n0 = m.n[0], n1 = m.n[1], cn0 = cm.n[0], cn1 = cm.n[1];
+    const float r0 = 1.f / (float)n0, r1 = 1.f / (float)n1;
     for (int c0 = tid; c0 < nc; c0 += 4 * nt) {
       float v[4];
 #pragma unroll
@@ -650,9 +691,9 @@ __device__ void cta_vcycle(const CtaLevels& B, float* red) {
         const int c = c0 + u * nt;
         v[u] = 0.f;
         if (c >= nc) continue;
-        const int i = c % n0, r = c / n0;
-        const int j = DIM == 3 ? r % n1 : r, k = DIM == 3 ? r / n1 : 0;
-        v[u] = x[c] + cx[(i >> 1) + cn0 * ((j >> 1) + cn1 * (k >> 1))];
+        int id[3];
+        blk_ijk<DIM>(n0, n1, r0, r1, c, id);
+        v[u] = x[c] + cx[(id[0] >> 1) + cn0 * ((id[1] >> 1) + cn1 * (id[2] >> 1))];
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u)
@@ -1446,9 +1487,10 @@ __device__ void grp_precondition(const CtaPressure& P, CtaLevels& V, float* sm, 
     const float* cx = last ? P.xtop : P.gx[l + 1];
     float* x = P.gx[l];
     const int nc = (int)m.nc;
+    const float r0 = 1.f / (float)m.n[0], r1 = 1.f / (float)m.n[1];
     for (int c = g.rank(); c < nc; c += g.size()) {
       int id[3];
-      blk_ijk<DIM>(m, c, id);
+      blk_ijk<DIM>(m.n[0], m.n[1], r0, r1, c, id);
       x[c] += cx[(int)cell_id(cm, id[0] >> 1, id[1] >> 1, id[2] >> 1)];
     }
     g.sync();
@@ -1495,6 +1537,7 @@ __device__ int grp_mgcg(const CtaPressure& P, CtaLevels& V, float* sm, float* re
   const int cs[3] = {1, m.n[0], m.n[0] * m.n[1]};
   const int fs[3] = {1, (int)m.fnx[1], (int)(m.fnx[2] * m.fny[2])};
   const int pin = (int)P.pin;
+  const float r0 = 1.f / (float)m.n[0], r1 = 1.f / (float)m.n[1];
   for (;;) {
     // p = z + beta p_old (z on the first), Ap, <p, Ap> (k_cg32_dir_spmv)
     const bool first = it == 0;
@@ -1512,7 +1555,7 @@ __device__ int grp_mgcg(const CtaPressure& P, CtaLevels& V, float* sm, float* re
         pv[u] = av[u] = 0.f;
         if (c >= n) continue;
         int id[3];
-        blk_ijk<DIM>(m, c, id);
+        blk_ijk<DIM>(m.n[0], m.n[1], r0, r1, c, id);
         const float pc = Pv(c);
         float a;
         if (c == pin) {
@@ -2070,7 +2113,8 @@ void mg_release(MgWork& mg) {
 cudaError_t cta_pressure(const Mesh& m, const double* kf, const double* f, double* x,
                          int singular, double tol, double inner_min, int limit, int graph,
                          int threads, int cluster, PcgWork& w, MgWork& mg, cudaStream_t st) {
-  if (any_periodic(m) || m.nf >= (1LL << 31) || mg.nlev < 1 || mg.top >= mg.nlev ||
+  // (the group passes index cells through FP32 reciprocals: < 2^24 cells)
+  if (any_periodic(m) || m.nc >= (1LL << 24) || mg.nlev < 1 || mg.top >= mg.nlev ||
       threads < 32 || threads > 1024 || threads % 32 || cluster < 1 || cluster > 8)
     return cudaErrorInvalidValue;
   CtaPressure P{};

@@ -226,8 +226,10 @@ typedef struct hydro_desc {
    * each run as one launch of one CTA of that many threads.  For batches of
    * many small cases (hydro_gpu_batch_*), where each case then holds one SM
    * per solve instead of queueing hundreds of tiny launches.  Needs
-   * precision MIXED, pressure solver MGCG, no periodic direction and no
-   * rigid box (HYDRO_ERR_UNSUPPORTED otherwise); a Gauss-Seidel velocity
+   * precision MIXED, pressure solver MGCG, no periodic direction, no
+   * rigid box and fewer than 2^24 cells (HYDRO_ERR_UNSUPPORTED otherwise);
+   * the pressure solve's set-up (diagonals, coarse levels, the dense
+   * coarsest inverse) runs inside the same launch; a Gauss-Seidel velocity
    * solve stays grid-wide.  Results agree with the grid-wide form to the
    * solver tolerances, not bit for bit (other summation order). */
   int cta_threads;
