@@ -131,3 +131,39 @@ def test_create_needs_opt_in_for_substituted_solvers(lib):
     assert st in (capi.ERR_NO_DEVICE, capi.OK)
     if st == capi.OK:
         lib.hydro_gpu_destroy(ctx)
+
+
+def test_create_checks_one_group_solves(lib):
+    """cta_threads / cta_cluster are validated before any device work: a
+    thread count that is no multiple of 32, a cluster of 3 or a cluster
+    without a thread count is HYDRO_ERR_ARG; FP64, a periodic direction or
+    2^24 cells and more is HYDRO_ERR_UNSUPPORTED (the one-group passes index
+    cells through FP32 reciprocals)."""
+    torch = pytest.importorskip("torch")
+    ctx = ctypes.c_void_p()
+
+    def desc(nx, ny, **kw):
+        d = capi.default_desc()
+        d.dim = 2
+        d.n[0], d.n[1], d.n[2] = nx, ny, 1
+        d.precision = capi.MIXED
+        d.pressure_solver = capi.LINEAR_MGCG
+        d.cta_threads = 1024
+        for k, v in kw.items():
+            setattr(d, k, v)
+        return d
+
+    for kw in ({"cta_threads": 48}, {"cta_cluster": 3}, {"cta_threads": 0, "cta_cluster": 4}):
+        d = desc(64, 64, **kw)
+        assert lib.hydro_gpu_create(ctypes.byref(d), ctypes.byref(ctx)) == capi.ERR_ARG, kw
+    d = desc(64, 64, precision=capi.FP64)
+    assert lib.hydro_gpu_create(ctypes.byref(d), ctypes.byref(ctx)) == capi.ERR_UNSUPPORTED
+    d = desc(64, 64)
+    d.periodic[0] = 1
+    assert lib.hydro_gpu_create(ctypes.byref(d), ctypes.byref(ctx)) == capi.ERR_UNSUPPORTED
+    d = desc(4096, 4096)  # 2^24 cells
+    assert lib.hydro_gpu_create(ctypes.byref(d), ctypes.byref(ctx)) == capi.ERR_UNSUPPORTED
+    if not torch.cuda.is_available():
+        # one cell fewer passes validation and stops at the device check
+        d = desc(4096, 4095)
+        assert lib.hydro_gpu_create(ctypes.byref(d), ctypes.byref(ctx)) == capi.ERR_NO_DEVICE
