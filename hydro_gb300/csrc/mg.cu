@@ -1312,7 +1312,7 @@ struct CtaPressure {
   Mesh m;
   const double *kf, *f;       // FP64 couplings, right-hand side
   double* dg;                 // FP64 diagonal (set up by the launch)
-  double *x, *r;              // correction (out), FP64 residual
+  double* x;                  // correction (out)
   float *kf32, *dg32, *idg32; // FP32 level-0 operator (set up by the launch)
   float *x32, *r32, *z32, *p, *pb, *Ap;
   long long pin;
@@ -1503,27 +1503,14 @@ __device__ void grp_precondition(const CtaPressure& P, CtaLevels& V, float* sm, 
 
 // Inner MG-CG for A e = r (FP32, e in x32) to relative tolerance t within
 // `lim` iterations, stopping on a stall as k_mgcg_update does; returns the
-// iterations.
+// iterations.  The refinement's residual pass has left r in r32 (rounded
+// from FP64), x32 = 0 and rr0 = <r, r> in FP64.
 template <int DIM, class G>
 __device__ int grp_mgcg(const CtaPressure& P, CtaLevels& V, float* sm, float* red, double* sd,
-                        double t, int lim, const G& g) {
+                        double rr0, double t, int lim, const G& g) {
   const Mesh& m = P.m;
   const int n = (int)m.nc, tid = g.rank(), nt = g.size();
-  double s = 0.;
-  for (int c0 = tid; c0 < n; c0 += 4 * nt) {
-    double v[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) v[u] = c0 + u * nt < n ? P.r[c0 + u * nt] : 0.;
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int c = c0 + u * nt;
-      if (c >= n) continue;
-      P.r32[c] = d2f(v[u]);
-      P.x32[c] = 0.f;
-      s += v[u] * v[u];
-    }
-  }
-  const double rr0 = grp_sum(s, sd, g);
+  double s;
   if (rr0 == 0. || lim <= 0) return 0;
   const double tol2 = t * t * rr0;
   grp_precondition<DIM>(P, V, sm, red, g);
@@ -1655,7 +1642,8 @@ __global__ void __launch_bounds__(kBlkThreads)
   int total = 0, outer = 0;
   bool conv = false, nan = false;
   for (;;) {
-    // FP64 residual r = f - mean - A x (x = 0 on the first pass)
+    // FP64 residual r = f - mean - A x (x = 0 on the first pass) and its
+    // FP64 <r, r>; r itself is kept only as the inner CG's FP32 start
     double s = 0.;
     for (int c0 = tid; c0 < n; c0 += 2 * nt) {
       double rv[2];
@@ -1689,7 +1677,9 @@ __global__ void __launch_bounds__(kBlkThreads)
       for (int u = 0; u < 2; ++u) {
         const int c = c0 + u * nt;
         if (c >= n) continue;
-        P.r[c] = rv[u];
+        // the inner CG's start: r rounded to FP32, e = 0
+        P.r32[c] = d2f(rv[u]);
+        P.x32[c] = 0.f;
         s += rv[u] * rv[u];
       }
     }
@@ -1707,7 +1697,7 @@ __global__ void __launch_bounds__(kBlkThreads)
     }
     if (total >= P.limit || outer >= 50) break;
     const double t = fmax(0.5 * P.tol * sqrt(ff / rr), P.inner_min);
-    total += grp_mgcg<DIM>(P, V, sm, red, sd, t, P.limit - total, g);
+    total += grp_mgcg<DIM>(P, V, sm, red, sd, rr, t, P.limit - total, g);
     for (int c0 = tid; c0 < n; c0 += 4 * nt) {
       double v[4];
 #pragma unroll
@@ -2123,7 +2113,6 @@ cudaError_t cta_pressure(const Mesh& m, const double* kf, const double* f, doubl
   P.dg = w.dg;
   P.f = f;
   P.x = x;
-  P.r = w.r;
   P.kf32 = w.kf32;
   P.dg32 = w.dg32;
   P.x32 = w.x32;
