@@ -446,11 +446,13 @@ struct LvIx {
     fo1 = (int)m.fofs[1];
     fo2 = DIM == 3 ? (int)m.fofs[2] : 0;
   }
-  // stride between neighbouring cells along d (= between its two faces)
-  __device__ __forceinline__ int cs(int d) const { return d == 0 ? 1 : (d == 1 ? n[0] : n[0] * n[1]); }
-  __device__ __forceinline__ int fs(int d) const {
+  // stride between neighbouring cells along d
+  __device__ __forceinline__ int cs(int d) const {
     return d == 0 ? 1 : (d == 1 ? n[0] : n[0] * n[1]);
   }
+  // stride between a cell's low and high face along d (fnx[1] = nx,
+  // fnx[2] fny[2] = nx ny: the cell stride)
+  __device__ __forceinline__ int fs(int d) const { return cs(d); }
   __device__ __forceinline__ int face(int d, const int* id) const {
     const int fx = n[0] + (d == 0), fy = n[1] + (d == 1);
     return (d == 0 ? 0 : d == 1 ? fo1 : fo2) + id[0] + fx * (id[1] + fy * id[2]);
@@ -475,58 +477,58 @@ __device__ void blk_half(const Mesh& m, const float* kf, const float* idg, const
   // pass, leaving the issue slots to those that have one; every thread
   // meets the one barrier at the end
   if (g.rank() < n) {
-  const int pn = (int)pin;
-  const int step = g.size();
-  const float rhx = 1.f / (float)hx, rn1 = 1.f / (float)L.n[1];
-  for (int q0 = g.rank(); q0 < n; q0 += U * step) {
-    float val[U];
-    int cc[U];
+    const int pn = (int)pin;
+    const int step = g.size();
+    const float rhx = 1.f / (float)hx, rn1 = 1.f / (float)L.n[1];
+    for (int q0 = g.rank(); q0 < n; q0 += U * step) {
+      float val[U];
+      int cc[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int q = q0 + u * step;
-      cc[u] = -1;
-      val[u] = 0.f;
-      if (q >= n) continue;
-      int id[3], t;
-      const int row = fdivmod(q, hx, rhx, t);
-      if (DIM == 3) {
-        id[2] = fdivmod(row, L.n[1], rn1, id[1]);
-      } else {
-        id[1] = row;
-        id[2] = 0;
-      }
-      id[0] = 2 * t + ((id[1] + id[2] + color) & 1);
-      if (id[0] >= L.n[0]) continue;
-      const int c = id[0] + L.n[0] * row;
-      cc[u] = c;
-      if (c == pn) {
-        val[u] = b[c];
-        continue;
-      }
-      float acc = b[c];
-      if (!zero) {
+      for (int u = 0; u < U; ++u) {
+        const int q = q0 + u * step;
+        cc[u] = -1;
+        val[u] = 0.f;
+        if (q >= n) continue;
+        int id[3], t;
+        const int row = fdivmod(q, hx, rhx, t);
+        if (DIM == 3) {
+          id[2] = fdivmod(row, L.n[1], rn1, id[1]);
+        } else {
+          id[1] = row;
+          id[2] = 0;
+        }
+        id[0] = 2 * t + ((id[1] + id[2] + color) & 1);
+        if (id[0] >= L.n[0]) continue;
+        const int c = id[0] + L.n[0] * row;
+        cc[u] = c;
+        if (c == pn) {
+          val[u] = b[c];
+          continue;
+        }
+        float acc = b[c];
+        if (!zero) {
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          const int s = L.cs(d);
-          const int fl = L.face(d, id);
-          if (PER) {
-            const int cl = nb_lo_p<PER>(m, d, id[d], c, s);
-            const int ch = nb_hi_p<PER>(m, d, id[d], c, s);
-            if (has_lo_p<PER>(m, d, id[d], c, s) && cl != pn) acc = fmaf(kf[fl], x[cl], acc);
-            if (has_hi_p<PER>(m, d, id[d], c, s) && ch != pn)
-              acc = fmaf(kf[fl + L.fs(d)], x[ch], acc);
-          } else {
-            if (id[d] > 0 && c - s != pn) acc = fmaf(kf[fl], x[c - s], acc);
-            if (id[d] < L.n[d] - 1 && c + s != pn) acc = fmaf(kf[fl + L.fs(d)], x[c + s], acc);
+          for (int d = 0; d < DIM; ++d) {
+            const int s = L.cs(d);
+            const int fl = L.face(d, id);
+            if (PER) {
+              const int cl = nb_lo_p<PER>(m, d, id[d], c, s);
+              const int ch = nb_hi_p<PER>(m, d, id[d], c, s);
+              if (has_lo_p<PER>(m, d, id[d], c, s) && cl != pn) acc = fmaf(kf[fl], x[cl], acc);
+              if (has_hi_p<PER>(m, d, id[d], c, s) && ch != pn)
+                acc = fmaf(kf[fl + L.fs(d)], x[ch], acc);
+            } else {
+              if (id[d] > 0 && c - s != pn) acc = fmaf(kf[fl], x[c - s], acc);
+              if (id[d] < L.n[d] - 1 && c + s != pn) acc = fmaf(kf[fl + L.fs(d)], x[c + s], acc);
+            }
           }
         }
+        val[u] = acc * idg[c];
       }
-      val[u] = acc * idg[c];
-    }
 #pragma unroll
-    for (int u = 0; u < U; ++u)
-      if (cc[u] >= 0) x[cc[u]] = val[u];
-  }
+      for (int u = 0; u < U; ++u)
+        if (cc[u] >= 0) x[cc[u]] = val[u];
+    }
   }
   g.sync();
 }
@@ -538,60 +540,60 @@ __device__ void blk_restrict(const Mesh& fm, const Mesh& cm, const float* kf, co
   constexpr int U = DIM == 3 ? 2 : 4;  // coarse cells per thread per pass, loads first
   const int n = (int)cm.nc;
   if (g.rank() < n) {  // (threads without a coarse cell skip to the barrier)
-  const LvIx<DIM> L(fm);
-  const int cn0 = cm.n[0], cn1 = cm.n[1];
-  const float rc0 = 1.f / (float)cn0, rc1 = 1.f / (float)cn1;
-  const int pn = (int)pin;
-  const int step = g.size();
-  for (int C0 = g.rank(); C0 < n; C0 += U * step) {
-    float sums[U];
+    const LvIx<DIM> L(fm);
+    const int cn0 = cm.n[0], cn1 = cm.n[1];
+    const float rc0 = 1.f / (float)cn0, rc1 = 1.f / (float)cn1;
+    const int pn = (int)pin;
+    const int step = g.size();
+    for (int C0 = g.rank(); C0 < n; C0 += U * step) {
+      float sums[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int C = C0 + u * step;
-      sums[u] = 0.f;
-      if (C >= n) continue;
-      int I[3];
-      blk_ijk<DIM>(cn0, cn1, rc0, rc1, C, I);
-      float sum = 0.f;
+      for (int u = 0; u < U; ++u) {
+        const int C = C0 + u * step;
+        sums[u] = 0.f;
+        if (C >= n) continue;
+        int I[3];
+        blk_ijk<DIM>(cn0, cn1, rc0, rc1, C, I);
+        float sum = 0.f;
 #pragma unroll
-      for (int ck = 0; ck < (DIM == 3 ? 2 : 1); ++ck)
+        for (int ck = 0; ck < (DIM == 3 ? 2 : 1); ++ck)
 #pragma unroll
-        for (int cj = 0; cj < 2; ++cj)
+          for (int cj = 0; cj < 2; ++cj)
 #pragma unroll
-          for (int ci = 0; ci < 2; ++ci) {
-            int id[3] = {2 * I[0] + ci, 2 * I[1] + cj, DIM == 3 ? 2 * I[2] + ck : 0};
-            const int c = id[0] + L.n[0] * (id[1] + L.n[1] * id[2]);
-            float r;
-            if (c == pn) {
-              r = b[c] - x[c];
-            } else {
-              float dg = 0.f, off = 0.f;
+            for (int ci = 0; ci < 2; ++ci) {
+              int id[3] = {2 * I[0] + ci, 2 * I[1] + cj, DIM == 3 ? 2 * I[2] + ck : 0};
+              const int c = id[0] + L.n[0] * (id[1] + L.n[1] * id[2]);
+              float r;
+              if (c == pn) {
+                r = b[c] - x[c];
+              } else {
+                float dg = 0.f, off = 0.f;
 #pragma unroll
-              for (int d = 0; d < DIM; ++d) {
-                const int s = L.cs(d);
-                const int fl = L.face(d, id);
-                float klo = kf[fl], khi = kf[fl + L.fs(d)];
-                dg += klo + khi;
-                if (PER) {
-                  const int cl = nb_lo_p<PER>(fm, d, id[d], c, s);
-                  const int ch = nb_hi_p<PER>(fm, d, id[d], c, s);
-                  if (has_lo_p<PER>(fm, d, id[d], c, s) && cl != pn) off = fmaf(klo, x[cl], off);
-                  if (has_hi_p<PER>(fm, d, id[d], c, s) && ch != pn) off = fmaf(khi, x[ch], off);
-                } else {
-                  if (id[d] > 0 && c - s != pn) off = fmaf(klo, x[c - s], off);
-                  if (id[d] < L.n[d] - 1 && c + s != pn) off = fmaf(khi, x[c + s], off);
+                for (int d = 0; d < DIM; ++d) {
+                  const int s = L.cs(d);
+                  const int fl = L.face(d, id);
+                  float klo = kf[fl], khi = kf[fl + L.fs(d)];
+                  dg += klo + khi;
+                  if (PER) {
+                    const int cl = nb_lo_p<PER>(fm, d, id[d], c, s);
+                    const int ch = nb_hi_p<PER>(fm, d, id[d], c, s);
+                    if (has_lo_p<PER>(fm, d, id[d], c, s) && cl != pn) off = fmaf(klo, x[cl], off);
+                    if (has_hi_p<PER>(fm, d, id[d], c, s) && ch != pn) off = fmaf(khi, x[ch], off);
+                  } else {
+                    if (id[d] > 0 && c - s != pn) off = fmaf(klo, x[c - s], off);
+                    if (id[d] < L.n[d] - 1 && c + s != pn) off = fmaf(khi, x[c + s], off);
+                  }
                 }
+                r = b[c] - (dg * x[c] - off);
               }
-              r = b[c] - (dg * x[c] - off);
+              sum += r;
             }
-            sum += r;
-          }
-      sums[u] = sum;
-    }
+        sums[u] = sum;
+      }
 #pragma unroll
-    for (int u = 0; u < U; ++u)
-      if (C0 + u * step < n) cb[C0 + u * step] = sums[u];
-  }
+      for (int u = 0; u < U; ++u)
+        if (C0 + u * step < n) cb[C0 + u * step] = sums[u];
+    }
   }
   g.sync();
 }
